@@ -1,0 +1,180 @@
+/*
+ * kmhodlr.h -- C ABI of the GB300 HODLR engine for the KernelMatrices.jl hot path.
+ *
+ * Every entry point is a plain C function (extern "C"), takes plain pointers and sizes, and
+ * returns an int status (KM_OK == 0).  Arrays are column-major FP64, as Julia stores them.
+ * Points are `const double*` holding 2*n values in (x, y) pairs -- the memory layout of a Julia
+ * `Vector{SVector{2,Float64}}`, so a Julia caller passes `pointer(pts)` without a copy.
+ * Host-pointer entry points copy their inputs to the device and their outputs back; the `_dev`
+ * variants take device pointers that stay resident in HBM.
+ *
+ * Each declaration names the reference interface it replaces (file:line inside the
+ * KernelMatrices.jl project).  The reference raises Julia exceptions; here a non-zero status is
+ * returned and km_last_error() gives the message.  KM_ERR_NOT_SPD stands for PosDefException.
+ *
+ * Threading: one CUDA stream per handle; different handles may be used from different threads.
+ * A single handle must not be used from two threads at once.
+ */
+#ifndef KMHODLR_H
+#define KMHODLR_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------- */
+enum km_status {
+  KM_OK = 0,
+  KM_ERR_BAD_ARG = 1,      /* invalid argument (sizes, ids, null pointers)                   */
+  KM_ERR_NOT_SPD = 2,      /* a Cholesky pivot was <= 0 (Julia PosDefException)              */
+  KM_ERR_OOM = 3,          /* device allocation failed or the HBM budget would be exceeded   */
+  KM_ERR_CUDA = 4,         /* a CUDA runtime call failed                                      */
+  KM_ERR_STATE = 5,        /* call out of order, e.g. solve before factorize                  */
+  KM_ERR_TIMEOUT = 6,      /* a bounded device-side wait ran out                               */
+  KM_ERR_UNSUPPORTED = 7,  /* valid request this build does not implement                     */
+  KM_ERR_ACA = 8           /* ACA failure (reference: "Incompatible maxrank or matrix dims")  */
+};
+
+/* ---- enumerations ------------------------------------------------------------------------- */
+enum km_kernel_id {
+  /* p1^2 / (1 + (r/p2)^2)^2 + p3 * [x == y]          (README.md:42-48 kernelfunction)       */
+  KM_KERNEL_RATQUAD = 0,
+  /* p1 * (1 + sqrt3 r/p2) exp(-sqrt3 r/p2) + p3*[x==y] (mtn_kernfun at nu = 3/2,
+   * src/covariancefunctions.jl:258-266, with mtn_cor's |x| <= 1e-8 -> 1 rule, :209-212)      */
+  KM_KERNEL_MATERN32 = 1
+};
+enum km_level_kind { KM_LEVEL_FIXED = 0, KM_LEVEL_LOG = 1 };  /* FixedLevel / LogLevel         */
+enum km_method { KM_METHOD_ACA = 0, KM_METHOD_NYSTROM = 1 };
+enum km_precision {
+  KM_PREC_FP64 = 0,   /* every step in FP64                                                   */
+  KM_PREC_MIXED = 1   /* FP32 bulk factorisation + FP64 refinement of solves                  */
+};
+
+typedef struct km_config {
+  int device;                  /* CUDA device ordinal                                          */
+  int precision;               /* enum km_precision                                             */
+  double hbm_budget_fraction;  /* fraction of device memory a handle may hold (0 => 0.8)       */
+  int refine_max_iter;         /* mixed precision: max refinement iterations (0 => 30)         */
+  double refine_tol;           /* mixed precision: relative residual target (0 => 1e-10)       */
+} km_config;
+
+typedef struct km_stats {
+  double assemble_ms, factorize_ms, solve_ms, matvec_ms, logdet_ms, grad_ms;  /* last call     */
+  int64_t device_bytes;        /* bytes of device memory held by the handle                    */
+  int64_t kernel_launches;     /* kernels launched by the handle since creation                 */
+  int refine_iterations;       /* iterations used by the last mixed-precision solve             */
+  double refine_residual;      /* final relative residual of that solve                         */
+} km_stats;
+
+typedef struct km_handle km_handle;
+
+/* ---- tree partition (pure host, bit-exact with the reference) ------------------------------- */
+
+/* Sizes of the HODLR partition of n points: number of levels, leaves and non-leaf blocks.
+ * Replaces _leafsizes (src/HODLR/src/indices.jl:5-24).  n must satisfy 1 <= n < 2^48. */
+int km_partition_sizes(int64_t n, int level_kind, int64_t level, int64_t* out_levels,
+                       int64_t* out_nleaf, int64_t* out_nnonleaf);
+
+/* 1-based inclusive index ranges of every leaf ([s,e,s,e], 4 per leaf) and non-leaf block
+ * ([a,b,c,d], 4 per block, level 1 first; rows a:b = second child, cols c:d = first child).
+ * Replaces HODLRindices (src/HODLR/src/indices.jl:55-65) with _leafindices (:29-37) and
+ * _nextlevel (:40-51).  Buffers sized from km_partition_sizes; either may be NULL. */
+int km_partition(int64_t n, int level_kind, int64_t level, int64_t* out_levels,
+                 int64_t* leaf, int64_t* nonleaf);
+
+/* Nystrom landmark indices (1-based): Int64.(round.(LinRange(1, n, rank)))
+ * (src/HODLR/src/constructor.jl:31). */
+int km_nystrom_landmarks(int64_t n, int64_t rank, int64_t* out);
+
+/* ---- handle lifecycle -------------------------------------------------------------------- */
+int km_create(const km_config* cfg, km_handle** out);
+int km_destroy(km_handle* h);
+const char* km_last_error(const km_handle* h);
+int km_get_stats(const km_handle* h, km_stats* out);
+
+/* ---- assembly ---------------------------------------------------------------------------- */
+
+/* Assemble the HODLR matrix of the kernel matrix K[i,j] = k(pts[i], pts[j], params) with
+ * nparams == 3 parameters (scale, range, nugget).
+ * Replaces KernelMatrix(pts, pts, parms, kernel) (src/structstypes.jl:17) followed by
+ * KernelHODLR(K, ep, maxrank, lvl; nystrom) (src/HODLR/src/constructor.jl:6-58):
+ *   method KM_METHOD_NYSTROM: nystrom_uvt blocks (src/factorizations.jl:86-94), rank = maxrank;
+ *   method KM_METHOD_ACA:     ACA blocks (src/factorizations.jl:9-84) with tolerance tol and
+ *                             rank cap maxrank (0 = none). */
+int km_assemble(km_handle* h, const double* pts, int64_t n, int kernel_id, const double* params,
+                int nparams, int method, double tol, int64_t maxrank, int level_kind,
+                int64_t level);
+
+/* Rank of every off-diagonal block, level 1 first (nnonleaf entries). */
+int km_block_ranks(km_handle* h, int64_t* out);
+
+/* ACA pivots (0-based within the block) of block `block` (global index, level 1 first):
+ * rows and cols receive up to `cap` entries each; *out_rank gets the block rank. */
+int km_aca_pivots(km_handle* h, int64_t block, int64_t cap, int64_t* rows, int64_t* cols,
+                  int64_t* out_rank);
+
+/* Off-diagonal factors U (rows a:b) and V (rows c:d) of block `block`, column-major with the
+ * block rank as column count, as KernelHODLR.U[l][k] / .V[l][k] hold them before
+ * factorisation (src/HODLR/src/structstypes.jl:52-63).  Buffers sized (b-a+1)*rank, (d-c+1)*rank. */
+int km_block_factors(km_handle* h, int64_t block, double* U, double* V);
+
+/* ---- products, factorisation, solves ------------------------------------------------------ */
+
+/* y = K x for k columns (n x k, column-major).
+ * Replaces mul!(target, K::KernelHODLR, src) (src/HODLR/src/baseoverloads.jl:152-179): before
+ * factorisation the leaf + U V' form, after it W (W' x). */
+int km_matvec(km_handle* h, const double* x, double* y, int64_t k);
+
+/* Symmetric factorisation K = W W'.  Replaces symmetricfactorize!
+ * (src/HODLR/src/symfact.jl:6-49). */
+int km_factorize(km_handle* h);
+
+/* x = K^{-1} b for k columns.  Replaces ldiv!(target, K::KernelHODLR, src) and \
+ * (src/HODLR/src/baseoverloads.jl:181-192, :252-263). */
+int km_solve(km_handle* h, const double* b, double* x, int64_t k);
+
+/* x = W^{-1} b (transpose = 0) or W'^{-1} b (transpose = 1).  Replaces ldiv!(t, K.W, v) and
+ * ldiv!(t, K.W', v) (src/HODLR/src/baseoverloads.jl:126-150). */
+int km_factor_solve(km_handle* h, int transpose, const double* b, double* x, int64_t k);
+
+/* x = W b (transpose = 0) or W' b (transpose = 1).  Replaces mul!(t, K.W, v) and
+ * mul!(t, K.W', v) (src/HODLR/src/baseoverloads.jl:95-124). */
+int km_factor_mul(km_handle* h, int transpose, const double* b, double* x, int64_t k);
+
+/* log det K.  Replaces logdet(K::KernelHODLR) (src/HODLR/src/baseoverloads.jl:194-209). */
+int km_logdet(km_handle* h, double* out);
+
+/* Device-resident variants: pointers are device memory of the handle's device; the work is
+ * ordered on the handle's stream and the call returns once it is complete. */
+int km_matvec_dev(km_handle* h, const double* d_x, double* d_y, int64_t k);
+int km_solve_dev(km_handle* h, const double* d_b, double* d_x, int64_t k);
+int km_factor_solve_dev(km_handle* h, int transpose, const double* d_b, double* d_x, int64_t k);
+int km_factor_mul_dev(km_handle* h, int transpose, const double* d_b, double* d_x, int64_t k);
+
+/* ---- Gaussian-process likelihood ---------------------------------------------------------- */
+
+/* y' = dK_j x for the exact derivative of the Nystrom HODLR in parameter j (0 scale,
+ * 1 range, 2 nugget).  Replaces DerivativeHODLR (src/HODLR/src/constructor.jl:66-95) with
+ * mul!(target, DK::DerivativeHODLR, src) (src/HODLR/src/baseoverloads.jl:216-234). */
+int km_derivative_matvec(km_handle* h, int param, const double* x, double* y, int64_t k);
+
+/* Negative log-likelihood 0.5 logdet K + 0.5 y'K^{-1}y and its stochastic gradient over the
+ * nprobe probe vectors (n x nprobe, column-major) for the 3 kernel parameters.
+ * Replaces negloglik (src/HODLR/src/maxlikfunctions.jl:2-9) and stoch_gradient
+ * (src/HODLR/src/stochasticgradient.jl:30-44, shuffle = false).  grad may be NULL (NLL only).
+ * Requires a factorised Nystrom HODLR. */
+int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t nprobe,
+                double* nll, double* grad);
+
+/* ---- diagnostics ------------------------------------------------------------------------- */
+
+/* Device FP64 FMA throughput in TFLOP/s measured by a short timed loop (roofline denominator
+ * for FP64-ALU-bound kernels). */
+int km_probe_fp64_tflops(int device, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KMHODLR_H */

@@ -1,0 +1,127 @@
+// Kernel-entry evaluation: dense leaves, the Nystrom landmark columns Phi = K(X, P) and the
+// landmark matrix S = K(P, P).  Replaces the comprehension in getindex/full
+// (src/baseoverloads.jl:10-29) that KernelHODLR calls for every leaf (src/HODLR/src/
+// constructor.jl:39) and nystrom_uvt calls for every block (src/factorizations.jl:86-94).
+//
+// Layouts (device):
+//   points   : 2n doubles, (x, y) pairs (AoS, the SVector{2,Float64} layout)
+//   leaves   : packed m_j x m_j column-major blocks at d_leaf_koff(j)
+//   panels   : per-leaf m_j x r column-major blocks at leaf_start(j) * r
+#include "km_kernels.h"
+
+namespace km {
+
+// One 32x32 tile of one leaf per CTA; only lower-triangle tiles are evaluated and each is
+// written twice (the kernel is symmetric bit for bit: |x-y| and x == y are symmetric).
+// grid = (ntile, ntile, nleaf), block = (32, 8).
+__global__ void k_eval_leaves(const double* __restrict__ pts, DTree t, KParams kp, int deriv,
+                              double* __restrict__ K) {
+  const int ti = blockIdx.x, tj = blockIdx.y;
+  if (ti < tj) return;
+  const int64_t leaf = blockIdx.z;
+  const int m = d_leaf_size(t, leaf);
+  if (ti * 32 >= m) return;
+  const int64_t s = d_leaf_start(t, leaf);
+  double* A = K + d_leaf_koff(t, leaf);
+  __shared__ double px[2][32], py[2][32];
+  __shared__ double tile[32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tid = ty * 32 + tx;
+  if (tid < 64) {
+    const int which = tid >> 5, q = tid & 31;
+    const int idx = (which == 0 ? ti : tj) * 32 + q;
+    if (idx < m) {
+      px[which][q] = pts[2 * (s + idx)];
+      py[which][q] = pts[2 * (s + idx) + 1];
+    }
+  }
+  __syncthreads();
+  const int i = ti * 32 + tx;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int jl = ty + 8 * q;
+    const int j = tj * 32 + jl;
+    if (i < m && j < m) {
+      const double v = deriv < 0 ? kernel_value(kp, px[0][tx], py[0][tx], px[1][jl], py[1][jl])
+                                 : dkernel_value(kp, deriv, px[0][tx], py[0][tx], px[1][jl], py[1][jl]);
+      A[(int64_t)j * m + i] = v;
+      tile[tx][jl] = v;
+    }
+  }
+  if (ti == tj) return;
+  __syncthreads();
+  // mirrored write: element (row = tj*32+tx, col = ti*32+ty+8q) = tile[ty+8q][tx]
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int il = ty + 8 * q;
+    const int row = tj * 32 + tx, col = ti * 32 + il;
+    if (row < m && col < m) A[(int64_t)col * m + row] = tile[il][tx];
+  }
+}
+
+// Phi[i, c] = k(x_i, p_c) for every point i and landmark c, stored per leaf column-major.
+// grid = (ceil(maxleaf*r / 256), nleaf), block = 256.
+__global__ void k_eval_phi(const double* __restrict__ pts, const double* __restrict__ lnd, int r,
+                           DTree t, KParams kp, int deriv, double* __restrict__ Phi) {
+  extern __shared__ double sl[];  // 2r
+  for (int q = threadIdx.x; q < 2 * r; q += blockDim.x) sl[q] = lnd[q];
+  __syncthreads();
+  const int64_t leaf = blockIdx.y;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf);
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)m * r) return;
+  const int c = (int)(e / m), i = (int)(e % m);
+  const double x = pts[2 * (s + i)], y = pts[2 * (s + i) + 1];
+  const double v = deriv < 0 ? kernel_value(kp, x, y, sl[2 * c], sl[2 * c + 1])
+                             : dkernel_value(kp, deriv, x, y, sl[2 * c], sl[2 * c + 1]);
+  Phi[s * r + (int64_t)c * m + i] = v;
+}
+
+// Dense block out[i + j*ld] = k(a_i, b_j) (or its derivative) for small matrices such as S.
+__global__ void k_eval_dense(const double* __restrict__ a, int na, const double* __restrict__ b,
+                             int nb, KParams kp, int deriv, double* __restrict__ out, int ld) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= na * nb) return;
+  const int i = e % na, j = e / na;
+  const double v = deriv < 0 ? kernel_value(kp, a[2 * i], a[2 * i + 1], b[2 * j], b[2 * j + 1])
+                             : dkernel_value(kp, deriv, a[2 * i], a[2 * i + 1], b[2 * j], b[2 * j + 1]);
+  out[i + (int64_t)j * ld] = v;
+}
+
+// Gathers the landmark points lnd[c] = pts[idx[c]].
+__global__ void k_gather_points(const double* __restrict__ pts, const int64_t* __restrict__ idx,
+                                int r, double* __restrict__ lnd) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < r) {
+    lnd[2 * c] = pts[2 * idx[c]];
+    lnd[2 * c + 1] = pts[2 * idx[c] + 1];
+  }
+}
+
+void launch_eval_leaves(const double* pts, const Tree& t, KParams kp, int deriv, double* K,
+                        cudaStream_t st) {
+  const int nt = (int)((t.max_leaf + 31) / 32);
+  dim3 grid(nt, nt, (unsigned)t.nleaf), block(32, 8);
+  k_eval_leaves<<<grid, block, 0, st>>>(pts, dtree(t), kp, deriv, K);
+}
+
+void launch_eval_phi(const double* pts, const double* lnd, int r, const Tree& t, KParams kp,
+                     int deriv, double* Phi, cudaStream_t st) {
+  const int64_t per = t.max_leaf * r;
+  dim3 grid((unsigned)((per + 255) / 256), (unsigned)t.nleaf);
+  k_eval_phi<<<grid, 256, 2 * r * sizeof(double), st>>>(pts, lnd, r, dtree(t), kp, deriv, Phi);
+}
+
+void launch_eval_dense(const double* a, int na, const double* b, int nb, KParams kp, int deriv,
+                       double* out, int ld, cudaStream_t st) {
+  const int tot = na * nb;
+  k_eval_dense<<<(tot + 255) / 256, 256, 0, st>>>(a, na, b, nb, kp, deriv, out, ld);
+}
+
+void launch_gather_points(const double* pts, const int64_t* idx, int r, double* lnd,
+                          cudaStream_t st) {
+  k_gather_points<<<(r + 127) / 128, 128, 0, st>>>(pts, idx, r, lnd);
+}
+
+}  // namespace km

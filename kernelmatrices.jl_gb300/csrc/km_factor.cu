@@ -1,0 +1,580 @@
+// FP64 factorisation kernels of the nested Nystrom HODLR factorisation.
+//
+// The reference (src/HODLR/src/symfact.jl:6-49) factors K = W W' with
+//   W = L_leaf * W_1 * ... * W_L,  W_N = I + M X M'  (src/HODLR/src/utils.jl:29-35),
+// where every W_N is built from the Householder QR of the node's transformed off-diagonal
+// panels.  With Nystrom blocks every panel is a row block of the single n x r matrix
+// Phi = K(X, P) (or of Phi S^{-1}, S = K(P, P)), and left-multiplication by the earlier factors
+// commutes with the right factor S^{-1}.  So after the leaf stage (A = L^{-1} Phi, A_leaf =
+// Q_leaf R_leaf) every transformed panel of a node N lies in the span of its children's bases:
+//   A[N] = blockdiag(Q_c1, Q_c2) G_N,   G_N = [R_c1 ; L22^{-1}(R_c2 - Ct' R_c1)]   (2r x r)
+// with Ct = R_c1 S^{-1} R_c2' and L22 = chol(I - Ct' Ct), and the reference's
+// X = chol([I C; C' I]) - I equals [[0,0],[C', L22 - I]] in those bases.  QR(G_N) = E_N R_N
+// gives the node basis Q_N = blockdiag(Q_c1, Q_c2) E_N.  Only r x r work is left above the
+// leaves; the factor is the reference's up to the rounding freedom of the QR of rank-deficient
+// panels.  Orthogonal factors are kept in Householder (LAPACK dgeqrf-style) form.
+#include "km_kernels.h"
+
+namespace km {
+
+// ---------------------------------------------------------------------------------------------
+// Small dense Cholesky (r x r, lower, in place, column-major) for S = K(P, P).  One CTA.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_chol_small(double* __restrict__ A, int n, int* __restrict__ info) {
+  extern __shared__ double s[];  // n x (n+1)
+  const int ld = n + 1;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) s[(e % n) + (e / n) * ld] = A[e];
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    const double d = s[j + j * ld];
+    if (!(d > 0.0)) {
+      if (threadIdx.x == 0 && info[0] == 0) info[0] = j + 1;
+      __syncthreads();
+      break;
+    }
+    const double sd = sqrt(d);
+    __syncthreads();
+    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) s[i + j * ld] /= sd;
+    if (threadIdx.x == 0) s[j + j * ld] = sd;
+    __syncthreads();
+    // trailing lower triangle update
+    const int w = n - j - 1;
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+      const int i = j + 1 + e % w, c = j + 1 + e / w;
+      if (i >= c) s[i + c * ld] -= s[i + j * ld] * s[c + j * ld];
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int i = e % n, c = e / n;
+    A[e] = (i >= c) ? s[i + c * ld] : 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Batched leaf Cholesky: Lf_j = chol(K_j) (lower), blocked right-looking, one CTA per leaf.
+// The current column panel (rows below the diagonal block) lives in shared memory.
+// info[j] = first failing column (1-based) of leaf j, 0 if positive definite.
+// ---------------------------------------------------------------------------------------------
+template <int NB>
+__global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K, double* __restrict__ Lf,
+                                                   DTree t, int* __restrict__ info) {
+  extern __shared__ double sm[];
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t off = d_leaf_koff(t, leaf);
+  const double* A0 = K + off;
+  double* A = Lf + off;
+  constexpr int LDP = NB + 1;
+  double* P = sm;                    // (m) x LDP, row-major panel rows
+  double* D = sm + (size_t)m * LDP;  // NB x LDP
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
+  for (int64_t e = tid; e < (int64_t)m * m; e += nth) A[e] = A0[e];
+  __syncthreads();
+  int bad = 0;
+  for (int k0 = 0; k0 < m; k0 += NB) {
+    const int kb = min(NB, m - k0);
+    // (1) diagonal block -> shared, unblocked Cholesky
+    for (int e = tid; e < kb * kb; e += nth) {
+      const int i = e % kb, c = e / kb;
+      D[i * LDP + c] = A[(int64_t)(k0 + c) * m + k0 + i];
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; ++j) {
+      const double d = D[j * LDP + j];
+      const bool ok = d > 0.0;
+      if (!ok && bad == 0) bad = k0 + j + 1;
+      const double sd = ok ? sqrt(d) : 1.0;
+      __syncthreads();
+      for (int i = j + 1 + tid; i < kb; i += nth) D[i * LDP + j] /= sd;
+      if (tid == 0) D[j * LDP + j] = sd;
+      __syncthreads();
+      const int w = kb - j - 1;
+      for (int e = tid; e < w * w; e += nth) {
+        const int i = j + 1 + e % w, c = j + 1 + e / w;
+        if (i >= c) D[i * LDP + c] -= D[i * LDP + j] * D[c * LDP + j];
+      }
+      __syncthreads();
+    }
+    for (int e = tid; e < kb * kb; e += nth) {
+      const int i = e % kb, c = e / kb;
+      if (i >= c) A[(int64_t)(k0 + c) * m + k0 + i] = D[i * LDP + c];
+    }
+    // (2) panel rows i >= k0+kb: x D' = a  (forward substitution per row)
+    const int r0 = k0 + kb, mr = m - r0;
+    for (int ii = tid; ii < mr; ii += nth) {
+      const int i = r0 + ii;
+      double x[NB];
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c < kb) {
+          double v = A[(int64_t)(k0 + c) * m + i];
+          for (int l = 0; l < c; ++l) v -= x[l] * D[c * LDP + l];
+          x[c] = v / D[c * LDP + c];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c < kb) {
+          P[ii * LDP + c] = x[c];
+          A[(int64_t)(k0 + c) * m + i] = x[c];
+        }
+      }
+    }
+    __syncthreads();
+    // (3) trailing update of the lower triangle: A[i, c] -= sum_l P[i,l] P[c,l]
+    for (int cc = warp; cc < mr; cc += nwarp) {
+      double pc[NB];
+#pragma unroll
+      for (int l = 0; l < NB; ++l) pc[l] = (l < kb) ? P[cc * LDP + l] : 0.0;
+      double* col = A + (int64_t)(r0 + cc) * m + r0;
+      for (int ii = cc + lane; ii < mr; ii += 32) {
+        double acc = 0.0;
+#pragma unroll
+        for (int l = 0; l < NB; ++l) acc += P[ii * LDP + l] * pc[l];
+        col[ii] -= acc;
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) info[leaf] = bad;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Batched leaf triangular solve / multiply with the leaf factors (lower, column-major).
+//   op 0: X = L^{-1} B      op 1: X = L^{-T} B      op 2: X = L B      op 3: X = L^T B
+// Operand addressing for leaf j: base + start(j)*bmul, leading dimension (ld_is_m ? m_j : ld).
+// grid = (nleaf, ceil(ncols / 8)), block = 256 (8 warps, one column each).
+// The 8-column chunk of the right-hand side is staged in shared memory (m x 8).
+// ---------------------------------------------------------------------------------------------
+struct LeafOperand {
+  double* ptr;
+  int64_t bmul;     // base offset multiplier of the leaf start
+  int64_t ld;       // leading dimension when !ld_is_m
+  int ld_is_m;
+};
+
+__global__ void __launch_bounds__(256) k_leaf_tri(const double* __restrict__ Lf, DTree t, int op,
+                                                  LeafOperand B, LeafOperand X, int ncols) {
+  extern __shared__ double xs[];  // m x 8, column c at xs[c*m]
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf);
+  const double* L = Lf + d_leaf_koff(t, leaf);
+  const int c0 = blockIdx.y * 8;
+  const int nc = min(8, ncols - c0);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t ldb = B.ld_is_m ? m : B.ld, ldx = X.ld_is_m ? m : X.ld;
+  const double* Bp = B.ptr + s * B.bmul;
+  double* Xp = X.ptr + s * X.bmul;
+  for (int e = threadIdx.x; e < nc * m; e += blockDim.x) {
+    const int c = e / m, i = e % m;
+    xs[c * m + i] = Bp[(int64_t)(c0 + c) * ldb + i];
+  }
+  __syncthreads();
+  if (w < nc) {
+    double* x = xs + w * m;
+    if (op == 0) {  // forward substitution, column oriented
+      for (int l = 0; l < m; ++l) {
+        const double xl = x[l] / L[(int64_t)l * m + l];
+        __syncwarp();
+        if (lane == 0) x[l] = xl;
+        const double* Lc = L + (int64_t)l * m;
+        for (int i = l + 1 + lane; i < m; i += 32) x[i] -= Lc[i] * xl;
+        __syncwarp();
+      }
+    } else if (op == 1) {  // backward substitution with L^T: row oriented dot products
+      for (int i = m - 1; i >= 0; --i) {
+        const double* Lc = L + (int64_t)i * m;  // column i of L = row i of L^T
+        double acc = 0.0;
+        for (int l = i + 1 + lane; l < m; l += 32) acc += Lc[l] * x[l];
+        acc = warp_sum(acc);
+        if (lane == 0) x[i] = (x[i] - acc) / Lc[i];
+        __syncwarp();
+      }
+    } else if (op == 2) {  // y = L x, from the bottom row up so x can be overwritten
+      for (int i = m - 1; i >= 0; --i) {
+        double acc = 0.0;
+        for (int l = lane; l <= i; l += 32) acc += L[(int64_t)l * m + i] * x[l];
+        acc = warp_sum(acc);
+        __syncwarp();
+        if (lane == 0) x[i] = acc;
+        __syncwarp();
+      }
+    } else {  // y = L^T x, from the top row down
+      for (int i = 0; i < m; ++i) {
+        const double* Lc = L + (int64_t)i * m;
+        double acc = 0.0;
+        for (int l = i + lane; l < m; l += 32) acc += Lc[l] * x[l];
+        acc = warp_sum(acc);
+        __syncwarp();
+        if (lane == 0) x[i] = acc;
+        __syncwarp();
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nc * m; e += blockDim.x) {
+    const int c = e / m, i = e % m;
+    Xp[(int64_t)(c0 + c) * ldx + i] = xs[c * m + i];
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Batched Householder QR of the leaf panels A_j (m_j x r, column-major at start(j)*r), in place:
+// reflector vectors below the diagonal (unit leading entry implicit), tau[j*r + c], and
+// R_j (r x r column-major, zeros below the diagonal) written to Rout[j*r*r].
+// Follows LAPACK dgeqr2/dlarfg: beta = -sign(alpha) ||(alpha, x)||, tau = (beta-alpha)/beta,
+// v = x/(alpha-beta); a zero column x gives tau = 0 (H = I).  One CTA per leaf; the panel is
+// copied to shared memory when it fits.
+// ---------------------------------------------------------------------------------------------
+template <bool SMEM>
+__global__ void __launch_bounds__(256) k_leaf_qr(double* __restrict__ Pan, int r, DTree t,
+                                                 double* __restrict__ tau, double* __restrict__ Rout) {
+  extern __shared__ double sm[];
+  __shared__ double red[8];
+  __shared__ double sh_tau;
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf);
+  double* G = Pan + s * r;
+  double* A = SMEM ? sm : G;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (SMEM) {
+    for (int64_t e = tid; e < (int64_t)m * r; e += blockDim.x) sm[e] = G[e];
+    __syncthreads();
+  }
+  const int kmax = min(m, r);
+  for (int j = 0; j < kmax; ++j) {
+    double* aj = A + (int64_t)j * m;
+    double part = 0.0;
+    for (int i = j + 1 + tid; i < m; i += blockDim.x) part += aj[i] * aj[i];
+    part = warp_sum(part);
+    if (lane == 0) red[w] = part;
+    __syncthreads();
+    if (tid == 0) {
+      double sig = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sig += red[q];
+      const double alpha = aj[j];
+      double tj = 0.0, beta = alpha, scal = 0.0;
+      if (sig != 0.0) {
+        const double nrm = sqrt(alpha * alpha + sig);
+        beta = alpha >= 0.0 ? -nrm : nrm;
+        tj = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+      }
+      aj[j] = beta;
+      red[0] = scal;
+      sh_tau = tj;
+    }
+    __syncthreads();
+    const double scal = red[0], tj = sh_tau;
+    for (int i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= scal;
+    if (tid == 0) tau[leaf * r + j] = tj;
+    __syncthreads();
+    if (tj != 0.0) {
+      // apply H_j = I - tau v v' to columns c > j (one warp per column)
+      for (int c = j + 1 + w; c < r; c += (int)(blockDim.x >> 5)) {
+        double* ac = A + (int64_t)c * m;
+        double acc = (lane == 0) ? ac[j] : 0.0;
+        for (int i = j + 1 + lane; i < m; i += 32) acc += aj[i] * ac[i];
+        acc = warp_sum(acc) * tj;
+        if (lane == 0) ac[j] -= acc;
+        for (int i = j + 1 + lane; i < m; i += 32) ac[i] -= acc * aj[i];
+      }
+    }
+    __syncthreads();
+  }
+  for (int j = kmax + tid; j < r; j += blockDim.x) tau[leaf * r + j] = 0.0;
+  for (int e = tid; e < r * r; e += blockDim.x) {
+    const int i = e % r, c = e / r;
+    Rout[leaf * (int64_t)r * r + e] = (i <= c && i < m) ? A[(int64_t)c * m + i] : 0.0;
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int64_t e = tid; e < (int64_t)m * r; e += blockDim.x) G[e] = sm[e];
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Node factorisation, one CTA per node of level l.  Given the children's R factors
+// (slots c1, c2) and Sc = chol(S) (lower):
+//   T1 = R1 Sc^{-T}, T2 = R2 Sc^{-T}   (upper triangular)
+//   Ct = T1 T2'                        (= R1 S^{-1} R2')
+//   L22 = chol(I - Ct' Ct)
+//   if l < L:  G = [R1 ; L22^{-1}(R2 - Ct' R1)],  Householder QR  G = E R_N  (structured:
+//              reflector j is e_j on top plus a dense bottom part, kept in Eref[:, j])
+// Outputs per node: Ct, L22 (lower), Eref (r x r), Etau (r), R_N into slot N.
+// Shared memory: four r x (r+1) matrices.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, const double* __restrict__ Sc,
+                                                     int r, int level, int L, int64_t nleaf,
+                                                     int64_t cbase, int64_t nbase, double* __restrict__ Ct_out,
+                                                     double* __restrict__ L22_out, double* __restrict__ Eref,
+                                                     double* __restrict__ Etau, int* __restrict__ info) {
+  extern __shared__ double sm[];
+  __shared__ double red[8];
+  __shared__ double sh[2];
+  const int ld = r + 1;
+  double* X0 = sm;
+  double* X1 = X0 + r * ld;
+  double* X2 = X1 + r * ld;
+  double* X3 = X2 + r * ld;
+  const int64_t k = blockIdx.x;
+  const int64_t node = nbase + k;  // node index within all nodes (level-major)
+  const double* R1 = R + (cbase + 2 * k) * (int64_t)r * r;
+  const double* R2 = R + (cbase + 2 * k + 1) * (int64_t)r * r;
+  const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
+  // load: X0 = Sc, X1 = R1, X2 = R2   (element (i,c) at i + c*ld)
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    X0[i + c * ld] = Sc[e];
+    X1[i + c * ld] = R1[e];
+    X2[i + c * ld] = R2[e];
+  }
+  __syncthreads();
+  // T = R Sc^{-T}: row i of T solves Sc t' = R[i,:]'. Rows of R1 (i < r) and R2 (r <= i < 2r)
+  // are independent; row i only has entries l >= i (upper triangular inputs).
+  for (int q = tid; q < 2 * r; q += nth) {
+    double* M = q < r ? X1 : X2;
+    const int i = q < r ? q : q - r;
+    for (int l = i; l < r; ++l) {
+      double v = M[i + l * ld];
+      for (int p = i; p < l; ++p) v -= X0[l + p * ld] * M[i + p * ld];
+      M[i + l * ld] = v / X0[l + l * ld];
+    }
+  }
+  __syncthreads();
+  // Ct = T1 T2' -> X3 ; Ct[i][c] = sum_{l >= max(i,c)} T1[i][l] T2[c][l]
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    double acc = 0.0;
+    for (int l = max(i, c); l < r; ++l) acc += X1[i + l * ld] * X2[c + l * ld];
+    X3[i + c * ld] = acc;
+  }
+  __syncthreads();
+  // H = I - Ct' Ct -> X0 (lower triangle)
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    if (i >= c) {
+      double acc = 0.0;
+      for (int l = 0; l < r; ++l) acc += X3[l + i * ld] * X3[l + c * ld];
+      X0[i + c * ld] = (i == c ? 1.0 : 0.0) - acc;
+    }
+  }
+  __syncthreads();
+  // L22 = chol(H) in place (lower)
+  int bad = 0;
+  for (int j = 0; j < r; ++j) {
+    const double d = X0[j + j * ld];
+    const bool ok = d > 0.0;
+    if (!ok && bad == 0) bad = j + 1;
+    const double sd = ok ? sqrt(d) : 1.0;
+    __syncthreads();
+    for (int i = j + 1 + tid; i < r; i += nth) X0[i + j * ld] /= sd;
+    if (tid == 0) X0[j + j * ld] = sd;
+    __syncthreads();
+    const int wdt = r - j - 1;
+    for (int e = tid; e < wdt * wdt; e += nth) {
+      const int i = j + 1 + e % wdt, c = j + 1 + e / wdt;
+      if (i >= c) X0[i + c * ld] -= X0[i + j * ld] * X0[c + j * ld];
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && bad) info[node] = bad;
+  // store Ct and L22
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    Ct_out[node * (int64_t)r * r + e] = X3[i + c * ld];
+    L22_out[node * (int64_t)r * r + e] = (i >= c) ? X0[i + c * ld] : 0.0;
+  }
+  if (level >= L) return;
+  // reload R1 -> X1, R2 -> X2
+  __syncthreads();
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    X1[i + c * ld] = R1[e];
+    X2[i + c * ld] = R2[e];
+  }
+  __syncthreads();
+  // B = R2 - Ct' R1 -> X2 (column c of R1 has entries l <= c)
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    double acc = 0.0;
+    for (int l = 0; l <= c; ++l) acc += X3[l + i * ld] * X1[l + c * ld];
+    X2[i + c * ld] -= acc;
+  }
+  __syncthreads();
+  // B <- L22^{-1} B, columns independent (one thread per column)
+  for (int c = tid; c < r; c += nth) {
+    for (int i = 0; i < r; ++i) {
+      double v = X2[i + c * ld];
+      for (int p = 0; p < i; ++p) v -= X0[i + p * ld] * X2[p + c * ld];
+      X2[i + c * ld] = v / X0[i + i * ld];
+    }
+  }
+  __syncthreads();
+  // structured Householder QR of [X1 (upper r x r) ; X2 (r x r)]:
+  // reflector j acts on row j of the top and all r rows of the bottom.
+  for (int j = 0; j < r; ++j) {
+    double part = 0.0;
+    for (int i = tid; i < r; i += nth) part += X2[i + j * ld] * X2[i + j * ld];
+    part = warp_sum(part);
+    if (lane == 0) red[w] = part;
+    __syncthreads();
+    if (tid == 0) {
+      double sig = 0.0;
+      for (int q = 0; q < nw; ++q) sig += red[q];
+      const double alpha = X1[j + j * ld];
+      double tj = 0.0, beta = alpha, scal = 0.0;
+      if (sig != 0.0) {
+        const double nrm = sqrt(alpha * alpha + sig);
+        beta = alpha >= 0.0 ? -nrm : nrm;
+        tj = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+      }
+      X1[j + j * ld] = beta;
+      sh[0] = scal;
+      sh[1] = tj;
+    }
+    __syncthreads();
+    const double scal = sh[0], tj = sh[1];
+    for (int i = tid; i < r; i += nth) X2[i + j * ld] *= scal;
+    if (tid == 0) Etau[node * (int64_t)r + j] = tj;
+    __syncthreads();
+    if (tj != 0.0) {
+      for (int c = j + 1 + w; c < r; c += nw) {
+        double acc = (lane == 0) ? X1[j + c * ld] : 0.0;
+        for (int i = lane; i < r; i += 32) acc += X2[i + j * ld] * X2[i + c * ld];
+        acc = warp_sum(acc) * tj;
+        if (lane == 0) X1[j + c * ld] -= acc;
+        for (int i = lane; i < r; i += 32) X2[i + c * ld] -= acc * X2[i + j * ld];
+      }
+    }
+    __syncthreads();
+  }
+  double* Rn = R + (nleaf + node) * (int64_t)r * r;
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    Rn[e] = (i <= c) ? X1[i + c * ld] : 0.0;
+    Eref[node * (int64_t)r * r + e] = X2[i + c * ld];
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// log det: 2 sum log diag(L_leaf) + 2 sum log |diag(L22)|, deterministic two-pass reduction.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_logdet_partial(const double* __restrict__ Lf, DTree t, const double* __restrict__ L22,
+                                 int r, int64_t nnode, double* __restrict__ partial) {
+  __shared__ double red[8];
+  const int64_t nleafdiag = t.n;
+  const int64_t tot = nleafdiag + nnode * r;
+  double acc = 0.0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double d;
+    if (e < nleafdiag) {
+      // leaf containing row e
+      const int64_t big = t.rem * (t.m0 + 1);
+      const int64_t j = e < big ? e / (t.m0 + 1) : t.rem + (e - big) / t.m0;
+      const int64_t i = e - d_leaf_start(t, j);
+      const int m = d_leaf_size(t, j);
+      d = Lf[d_leaf_koff(t, j) + i * m + i];
+    } else {
+      const int64_t q = e - nleafdiag;
+      const int64_t node = q / r, i = q % r;
+      d = L22[node * (int64_t)r * r + i * r + i];
+    }
+    acc += 2.0 * log(fabs(d));
+  }
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+    partial[blockIdx.x] = s;
+  }
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partial, int np, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < np; ++q) s += partial[q];
+    out[0] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------------------------
+bool launch_chol_small(double* A, int n, int* info, cudaStream_t st) {
+  const size_t sm = (size_t)n * (n + 1) * sizeof(double);
+  if (sm > 200 * 1024) return false;
+  cudaFuncSetAttribute(k_chol_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_chol_small<<<1, 256, sm, st>>>(A, n, info);
+  return true;
+}
+
+bool launch_leaf_chol(const double* K, double* Lf, const Tree& t, int* info, cudaStream_t st) {
+  const int64_t m = t.max_leaf;
+  auto fits = [&](int nb) { return (size_t)(m + nb) * (nb + 1) * sizeof(double) <= 200 * 1024; };
+  if (fits(32)) {
+    const size_t sm = (size_t)(m + 32) * 33 * sizeof(double);
+    cudaFuncSetAttribute(k_leaf_chol<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_leaf_chol<32><<<(unsigned)t.nleaf, 256, sm, st>>>(K, Lf, dtree(t), info);
+  } else if (fits(16)) {
+    const size_t sm = (size_t)(m + 16) * 17 * sizeof(double);
+    cudaFuncSetAttribute(k_leaf_chol<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_leaf_chol<16><<<(unsigned)t.nleaf, 256, sm, st>>>(K, Lf, dtree(t), info);
+  } else if (fits(8)) {
+    const size_t sm = (size_t)(m + 8) * 9 * sizeof(double);
+    cudaFuncSetAttribute(k_leaf_chol<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_leaf_chol<8><<<(unsigned)t.nleaf, 256, sm, st>>>(K, Lf, dtree(t), info);
+  } else {
+    return false;
+  }
+  return true;
+}
+
+bool launch_leaf_tri(const double* Lf, const Tree& t, int op, double* Bptr, int64_t bmul,
+                     int64_t bld, int bld_is_m, double* Xptr, int64_t xmul, int64_t xld,
+                     int xld_is_m, int ncols, cudaStream_t st) {
+  const size_t sm = (size_t)t.max_leaf * 8 * sizeof(double);
+  if (sm > 200 * 1024) return false;
+  cudaFuncSetAttribute(k_leaf_tri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  LeafOperand B{Bptr, bmul, bld, bld_is_m}, X{Xptr, xmul, xld, xld_is_m};
+  dim3 grid((unsigned)t.nleaf, (unsigned)((ncols + 7) / 8));
+  k_leaf_tri<<<grid, 256, sm, st>>>(Lf, dtree(t), op, B, X, ncols);
+  return true;
+}
+
+void launch_leaf_qr(double* Pan, int r, const Tree& t, double* tau, double* Rout, cudaStream_t st) {
+  const size_t sm = (size_t)t.max_leaf * r * sizeof(double);
+  if (sm <= 200 * 1024) {
+    cudaFuncSetAttribute(k_leaf_qr<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_leaf_qr<true><<<(unsigned)t.nleaf, 256, sm, st>>>(Pan, r, dtree(t), tau, Rout);
+  } else {
+    k_leaf_qr<false><<<(unsigned)t.nleaf, 256, 0, st>>>(Pan, r, dtree(t), tau, Rout);
+  }
+}
+
+void launch_node_factor(double* R, const double* Sc, int r, int level, const Tree& t,
+                        double* Ct, double* L22, double* Eref, double* Etau, int* info,
+                        cudaStream_t st) {
+  const size_t sm = (size_t)4 * r * (r + 1) * sizeof(double);
+  cudaFuncSetAttribute(k_node_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const int64_t cbase = (level == 1) ? 0 : t.nleaf + t.node_off[level - 1];
+  const int64_t nbase = t.node_off[level];
+  k_node_factor<<<(unsigned)t.nodes_at(level), 256, sm, st>>>(R, Sc, r, level, t.L, t.nleaf, cbase,
+                                                              nbase, Ct, L22, Eref, Etau, info);
+}
+
+void launch_logdet(const double* Lf, const Tree& t, const double* L22, int r, double* partial,
+                   int np, double* out, cudaStream_t st) {
+  k_logdet_partial<<<np, 256, 0, st>>>(Lf, dtree(t), L22, r, t.nnode, partial);
+  k_sum_partials<<<1, 32, 0, st>>>(partial, np, out);
+}
+
+}  // namespace km

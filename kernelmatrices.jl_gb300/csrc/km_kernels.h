@@ -1,0 +1,56 @@
+// Launch wrappers of the device kernels (defined in km_assemble.cu, km_factor.cu, km_apply.cu,
+// km_aca.cu, km_grad.cu).  Host orchestration lives in km_api.cu.
+#pragma once
+#include "km_internal.h"
+
+namespace km {
+
+struct NodeMatsH {
+  const double* Ct;
+  const double* L22;
+  const double* Eref;
+  const double* Etau;
+  int r;
+};
+
+// assembly
+void launch_eval_leaves(const double* pts, const Tree& t, KParams kp, int deriv, double* K,
+                        cudaStream_t st);
+void launch_eval_phi(const double* pts, const double* lnd, int r, const Tree& t, KParams kp,
+                     int deriv, double* Phi, cudaStream_t st);
+void launch_eval_dense(const double* a, int na, const double* b, int nb, KParams kp, int deriv,
+                       double* out, int ld, cudaStream_t st);
+void launch_gather_points(const double* pts, const int64_t* idx, int r, double* lnd,
+                          cudaStream_t st);
+
+// factorisation
+bool launch_chol_small(double* A, int n, int* info, cudaStream_t st);
+bool launch_leaf_chol(const double* K, double* Lf, const Tree& t, int* info, cudaStream_t st);
+bool launch_leaf_tri(const double* Lf, const Tree& t, int op, double* Bptr, int64_t bmul,
+                     int64_t bld, int bld_is_m, double* Xptr, int64_t xmul, int64_t xld,
+                     int xld_is_m, int ncols, cudaStream_t st);
+void launch_leaf_qr(double* Pan, int r, const Tree& t, double* tau, double* Rout, cudaStream_t st);
+void launch_node_factor(double* R, const double* Sc, int r, int level, const Tree& t, double* Ct,
+                        double* L22, double* Eref, double* Etau, int* info, cudaStream_t st);
+void launch_logdet(const double* Lf, const Tree& t, const double* L22, int r, double* partial,
+                   int np, double* out, cudaStream_t st);
+
+// products and solves
+enum { UP_PROJ_ = 0, UP_FWD_ = 1, UP_MULT_ = 2, UP_SUM_ = 3 };
+enum { DN_FWD_ = 0, DN_BWD_ = 1, DN_MUL_ = 2, DN_MULT_ = 3, DN_NYS_ = 4 };
+void launch_up(const Tree& t, const NodeMatsH& h, int level, double* VP, double* VD, int k,
+               int mode, cudaStream_t st);
+void launch_down(const Tree& t, const NodeMatsH& h, int level, const double* VP, double* VG,
+                 const double* VD, int k, int mode, cudaStream_t st);
+void launch_leaf_proj(const double* Qref, const double* tau, int r, const Tree& t, const double* Y,
+                      int64_t ldy, double* VP, int k, cudaStream_t st);
+void launch_leaf_expand(const double* Qref, const double* tau, int r, const Tree& t,
+                        const double* VG, double* Y, int64_t ldy, int k, double sign,
+                        cudaStream_t st);
+void launch_leaf_phiT(const double* Phi, int r, const Tree& t, const double* X, int64_t ldx,
+                      double* VP, int k, cudaStream_t st);
+void launch_leaf_nys_apply(const double* Kl, const double* Phi, const double* Sc, int r,
+                           const Tree& t, const double* X, int64_t ldx, const double* VG,
+                           double* Y, int64_t ldy, int k, cudaStream_t st);
+
+}  // namespace km

@@ -1,0 +1,44 @@
+// Device FP64 FMA throughput probe (the roofline denominator of FP64-ALU-bound kernels: the
+// measured peaks file of the GPU pool carries only HBM copy and bf16 tensor rates).
+#include "km_kernels.h"
+
+namespace km {
+
+__global__ void k_dfma_loop(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1.0, x2 = x0 + 2.0, x3 = x0 + 3.0;
+  double x4 = x0 + 4.0, x5 = x0 + 5.0, x6 = x0 + 6.0, x7 = x0 + 7.0;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+}  // namespace km
+
+extern "C" int km_probe_fp64_tflops(int device, double* out) {
+  if (!out) return KM_ERR_BAD_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return KM_ERR_CUDA;
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, device) != cudaSuccess) return KM_ERR_CUDA;
+  const int blocks = p.multiProcessorCount * 4, threads = 256, iters = 4000;
+  double* d = nullptr;
+  if (cudaMalloc(&d, sizeof(double) * blocks * threads) != cudaSuccess) return KM_ERR_OOM;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  km::k_dfma_loop<<<blocks, threads>>>(d, 100, 0.999, 0.001);
+  cudaEventRecord(e0);
+  km::k_dfma_loop<<<blocks, threads>>>(d, iters, 0.999, 0.001);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  const cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess || ms <= 0.f) return KM_ERR_CUDA;
+  *out = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+  return KM_OK;
+}

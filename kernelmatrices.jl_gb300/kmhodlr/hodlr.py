@@ -1,0 +1,260 @@
+"""Python mirror of the KernelMatrices.jl HODLR interface, running on the GB300 engine.
+
+Names, argument meanings and errors follow the reference:
+  KernelMatrix(pts, pts, parms, kernel)              src/structstypes.jl:17
+  FixedLevel(k), LogLevel(k)                         src/HODLR/src/structstypes.jl:30-37
+  KernelHODLR(K, ep, maxrank, lvl; nystrom, ...)     src/HODLR/src/constructor.jl:6-58
+  symmetricfactorize(HK)   (Julia: symmetricfactorize!)  src/HODLR/src/symfact.jl:6-49
+  HK @ x (mul!/*), HK.ldiv(b) / HK \\ b (ldiv!/\\), logdet(HK)   baseoverloads.jl:152-209
+  HK.W.ldiv(v), HK.W.T.ldiv(v), HK.W @ v, HK.W.T @ v            baseoverloads.jl:95-150
+Errors: PosDefException for non-positive-definite factors, KMError (Julia's ErrorException)
+for the rest.  Every operation runs in libkmhodlr.so; nothing falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+
+class KMError(RuntimeError):
+    """A failed engine call (Julia ``error(...)``)."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class PosDefException(KMError):
+    """Mirror of Julia's ``LinearAlgebra.PosDefException``."""
+
+
+def _check(h, rc: int):
+    if rc == L.KM_OK:
+        return
+    lib = L.load()
+    msg = lib.km_last_error(h).decode() if h else "error"
+    if rc == L.KM_ERR_NOT_SPD:
+        raise PosDefException(rc, msg)
+    raise KMError(rc, msg)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+@dataclass(frozen=True)
+class FixedLevel:
+    lv: int
+
+
+@dataclass(frozen=True)
+class LogLevel:
+    lv: int
+
+
+def _level(lvl):
+    if isinstance(lvl, FixedLevel):
+        return L.KM_LEVEL_FIXED, lvl.lv
+    if isinstance(lvl, LogLevel):
+        return L.KM_LEVEL_LOG, lvl.lv
+    raise TypeError("level must be FixedLevel or LogLevel")
+
+
+# ---- kernels ----------------------------------------------------------------------------------
+
+@dataclass(frozen=True)
+class RatQuad:
+    """k(x, y, p) = p1^2 / (1 + (|x-y|/p2)^2)^2 + p3 [x == y]   (README.md:42-48)."""
+    kid: int = L.KM_KERNEL_RATQUAD
+
+
+@dataclass(frozen=True)
+class Matern32:
+    """k(x, y, p) = p1 (1 + sqrt3 r/p2) exp(-sqrt3 r/p2) + p3 [x == y]
+    (mtn_kernfun at nu = 3/2, src/covariancefunctions.jl:258-266)."""
+    kid: int = L.KM_KERNEL_MATERN32
+
+
+@dataclass
+class KernelMatrix:
+    """Lazy kernel matrix (src/structstypes.jl:2-23).  pts is an (n, 2) float64 array."""
+    x1: np.ndarray
+    x2: np.ndarray
+    parms: np.ndarray
+    kernel: object
+
+    def __init__(self, x1, x2, parms, kernel):
+        self.x1 = np.ascontiguousarray(x1, dtype=np.float64)
+        self.x2 = np.ascontiguousarray(x2, dtype=np.float64)
+        self.parms = np.ascontiguousarray(parms, dtype=np.float64)
+        self.kernel = kernel
+        if self.x1.ndim != 2 or self.x1.shape[1] != 2:
+            raise KMError(L.KM_ERR_BAD_ARG, "points must be an (n, 2) array")
+        if self.x1.shape != self.x2.shape:
+            raise KMError(L.KM_ERR_BAD_ARG, "Eltype of pts and pts2 must agree.")
+
+    @property
+    def shape(self):
+        return (len(self.x1), len(self.x2))
+
+
+# ---- partition --------------------------------------------------------------------------------
+
+def HODLRindices(n: int, lvl):
+    """``HODLRindices`` (src/HODLR/src/indices.jl:55-65) through the C ABI: (levels, leaf
+    ranges, non-leaf ranges per level), 1-based inclusive like the reference."""
+    lib = L.load()
+    kind, lv = _level(lvl)
+    levels, nleaf, nnon = C.c_int64(), C.c_int64(), C.c_int64()
+    _check(None, lib.km_partition_sizes(n, kind, lv, C.byref(levels), C.byref(nleaf), C.byref(nnon)))
+    leaf = np.zeros(4 * nleaf.value, dtype=np.int64)
+    non = np.zeros(max(4 * nnon.value, 1), dtype=np.int64)
+    _check(None, lib.km_partition(n, kind, lv, C.byref(levels), _ip(leaf), _ip(non)))
+    leaves = [tuple(int(v) for v in leaf[4 * j:4 * j + 4]) for j in range(nleaf.value)]
+    nonleaf, q = [], 0
+    for l in range(1, levels.value + 1):
+        cnt = nleaf.value >> l
+        nonleaf.append([tuple(int(v) for v in non[4 * (q + k):4 * (q + k) + 4]) for k in range(cnt)])
+        q += cnt
+    if not nonleaf:
+        nonleaf = [[]]
+    return levels.value, leaves, nonleaf
+
+
+def nystrom_landmarks(n: int, rank: int) -> np.ndarray:
+    """1-based landmark indices ``Int64.(round.(LinRange(1, n, rank)))`` (constructor.jl:31)."""
+    lib = L.load()
+    out = np.zeros(rank, dtype=np.int64)
+    _check(None, lib.km_nystrom_landmarks(n, rank, _ip(out)))
+    return out
+
+
+# ---- HODLR ------------------------------------------------------------------------------------
+
+class _FactorView:
+    """``K.W`` / ``K.W'``: products and solves with the symmetric factor."""
+
+    def __init__(self, hk: "KernelHODLR", transpose: bool):
+        self._hk = hk
+        self._t = transpose
+
+    @property
+    def T(self) -> "_FactorView":
+        return _FactorView(self._hk, not self._t)
+
+    def ldiv(self, v: np.ndarray) -> np.ndarray:
+        """``ldiv!(t, K.W, v)`` / ``ldiv!(t, K.W', v)`` (baseoverloads.jl:126-150)."""
+        return self._hk._apply("km_factor_solve", v, self._t)
+
+    def __matmul__(self, v: np.ndarray) -> np.ndarray:
+        """``mul!(t, K.W, v)`` / ``mul!(t, K.W', v)`` (baseoverloads.jl:95-124)."""
+        return self._hk._apply("km_factor_mul", v, self._t)
+
+
+class KernelHODLR:
+    """``HODLR.KernelHODLR`` held on the GPU (src/HODLR/src/constructor.jl:6-58)."""
+
+    def __init__(self, K: KernelMatrix, ep: float, maxrank: int, lvl, nystrom: bool = False,
+                 plel: bool = False, sorted: bool = False, device: int = 0,
+                 precision: int = L.KM_PREC_FP64):
+        lib = L.load()
+        if not np.array_equal(K.x1, K.x2):
+            raise KMError(L.KM_ERR_BAD_ARG, "This function builds symmetric matrices.")
+        kid = getattr(K.kernel, "kid", K.kernel)
+        cfg = L.KmConfig(device=device, precision=precision, hbm_budget_fraction=0.8,
+                         refine_max_iter=0, refine_tol=0.0)
+        h = C.c_void_p()
+        rc = lib.km_create(C.byref(cfg), C.byref(h))
+        if rc != L.KM_OK:
+            raise KMError(rc, "km_create failed (no CUDA device?)")
+        self._h = h
+        self.n = K.shape[0]
+        self.nys = bool(nystrom)
+        self.mrnk = int(maxrank)
+        self.ep = float(ep)
+        kind, lv = _level(lvl)
+        method = L.KM_METHOD_NYSTROM if nystrom else L.KM_METHOD_ACA
+        _check(h, lib.km_assemble(h, _dp(K.x1), self.n, int(kid), _dp(K.parms), len(K.parms),
+                                  method, float(ep), int(maxrank), kind, int(lv)))
+        self.lvl, self.leafindices, self.nonleafindices = HODLRindices(self.n, lvl)
+        self.factorized = False
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            L.load().km_destroy(h)
+            self._h = None
+
+    # -- helpers --
+    def _apply(self, name: str, v: np.ndarray, transpose: Optional[bool] = None) -> np.ndarray:
+        lib = L.load()
+        vec = np.asarray(v, dtype=np.float64)
+        if vec.shape[0] != self.n:
+            raise KMError(L.KM_ERR_BAD_ARG, "Matrix and Vector sizes do not agree.")
+        b = np.asfortranarray(vec.reshape(self.n, -1))
+        out = np.empty_like(b, order="F")
+        k = b.shape[1]
+        fn = getattr(lib, name)
+        if transpose is None:
+            rc = fn(self._h, _dp(b), _dp(out), k)
+        else:
+            rc = fn(self._h, int(transpose), _dp(b), _dp(out), k)
+        _check(self._h, rc)
+        return out.reshape(vec.shape)
+
+    @property
+    def W(self) -> _FactorView:
+        return _FactorView(self, False)
+
+    def stats(self) -> L.KmStats:
+        st = L.KmStats()
+        _check(self._h, L.load().km_get_stats(self._h, C.byref(st)))
+        return st
+
+    def block_ranks(self) -> np.ndarray:
+        cnt = sum(len(x) for x in self.nonleafindices)
+        out = np.zeros(max(cnt, 1), dtype=np.int64)
+        _check(self._h, L.load().km_block_ranks(self._h, _ip(out)))
+        return out[:cnt]
+
+    # -- reference operations --
+    def __matmul__(self, x: np.ndarray) -> np.ndarray:
+        """``mul!(target, K::KernelHODLR, src)`` (baseoverloads.jl:152-179)."""
+        return self._apply("km_matvec", x)
+
+    def ldiv(self, b: np.ndarray) -> np.ndarray:
+        """``K \\ b`` (baseoverloads.jl:181-192, 252-263)."""
+        return self._apply("km_solve", b)
+
+    def logdet(self) -> float:
+        """``logdet(K)`` (baseoverloads.jl:194-209)."""
+        out = C.c_double()
+        _check(self._h, L.load().km_logdet(self._h, C.byref(out)))
+        return out.value
+
+
+def symmetricfactorize(K: KernelHODLR) -> None:
+    """``symmetricfactorize!`` (src/HODLR/src/symfact.jl:6-49)."""
+    _check(K._h, L.load().km_factorize(K._h))
+    K.factorized = True
+
+
+def logdet(K: KernelHODLR) -> float:
+    return K.logdet()
+
+
+def probe_fp64_tflops(device: int = 0) -> float:
+    out = C.c_double()
+    rc = L.load().km_probe_fp64_tflops(device, C.byref(out))
+    if rc != L.KM_OK:
+        raise KMError(rc, "FP64 probe failed")
+    return out.value
