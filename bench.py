@@ -1,0 +1,367 @@
+"""Benchmark of the HODLR hot path: factor + solve + logdet throughput at n = 2^16.
+
+Workload (one step): n = 65536 points uniform on [0,1]^2 (seeded, k-d ordered), Matern nu=3/2
+(variance 1, range 0.1) plus a 1e-3 nugget, Nystrom blocks of global rank 72, FixedLevel(8)
+(256 leaves of 256 points): assemble, one matvec, symmetricfactorize!, a solve with 16 N(0,1)
+right-hand sides and logdet.  The metric is steps per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl ours (default): the GB300 engine (libkmhodlr.so).  `value` is measured with inputs
+resident in HBM through the device entry points; `e2e` through the host-pointer C ABI (pinned
+host buffers, copies inside the timed region).  N > 1 runs N independent replicas (the path does
+not shard; weak scaling).
+--impl reference: the reference's CPU algorithm (the NumPy restatement in oracle/, all host
+threads) on a bounded sample of the same workload, scaled to the workload by the reference
+algorithm's flop count.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "kernelmatrices.jl_gb300"))
+
+N_POINTS = 65536
+RANK = 72
+LEVEL = 8            # FixedLevel(8)
+NRHS = 16
+PARAMS = (1.0, 0.1, 1e-3)
+SEED = 20260101
+WORKLOAD = "matern32_nystrom_n65536_r72_fixedlevel8_16rhs"
+
+
+# ----------------------------------------------------------------------------------------------
+# algorithmic work models
+# ----------------------------------------------------------------------------------------------
+
+def reference_flops(n: int, L: int, m0: int = 256, r: int = RANK, nrhs: int = NRHS) -> float:
+    """Flops of the reference algorithm for one step: leaf Cholesky, leaf solves on the panels of
+    every level, per-level QR, the level-pair Woodbury updates with the dense block-diagonal M
+    (src/HODLR/src/symfact.jl:17-38), the solve (baseoverloads.jl:126-150) and logdet, which
+    re-factors the leaves (:200)."""
+    fact = n * m0 * m0 / 3 + L * n * m0 * r + 4 * L * n * r * r + 4 * L * (L - 1) * n * r * r
+    solve = nrhs * 2 * (n * m0 + 4 * L * n * r)
+    return fact + solve + n * m0 * m0 / 3
+
+
+def engine_flops(n: int, L: int, m0: int = 256, r: int = RANK) -> dict:
+    """Algorithmic FP64 flops per launch class of the engine, for one step."""
+    nleaf = 2 ** L
+    nnode = nleaf - 1
+    return {
+        "leaf_chol": nleaf * m0 ** 3 / 3.0,
+        "leaf_qr": nleaf * (2.0 * m0 * r * r - 2.0 * r ** 3 / 3.0),
+        "node": (nnode - 1) * 7.0 * r ** 3 + 8.0 / 3.0 * r ** 3,
+        # Phi panel solve (r columns) + forward and backward solve of NRHS columns
+        "leaf_tri": nleaf * m0 * m0 * (r + 2 * NRHS),
+    }
+
+
+# ----------------------------------------------------------------------------------------------
+# clocks
+# ----------------------------------------------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------------------------
+# CPU legs (the oracle restatement of the reference)
+# ----------------------------------------------------------------------------------------------
+
+def cpu_sample(n_sample: int, L_sample: int, steps: int = 1) -> dict:
+    """Times the reference's CPU algorithm (oracle/) on a sample problem with the workload's
+    leaf size, rank, kernel and right-hand sides, and scales it to the workload by flop count."""
+    from oracle import hodlr_oracle as O
+    from kmhodlr.data import uniform_points
+    pts = uniform_points(n_sample, SEED)
+    rhs = np.random.default_rng(SEED + 1).standard_normal((n_sample, NRHS))
+    x = np.random.default_rng(SEED + 2).standard_normal((n_sample, 1))
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        K = O.KernelMatrix(pts, pts, np.array(PARAMS), O.KERNEL_MATERN32)
+        HK = O.build_hodlr(K, 0.0, RANK, O.FixedLevel(L_sample), nystrom=True)
+        O.hodlr_mul(HK, x)
+        O.symmetricfactorize(HK)
+        O.hodlr_ldiv(HK, rhs)
+        O.hodlr_logdet(HK)
+        times.append(time.perf_counter() - t0)
+    scale = reference_flops(N_POINTS, LEVEL) / reference_flops(n_sample, L_sample)
+    return {"times": times, "scale": scale}
+
+
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, rank: int):
+    if rank != 0:
+        return
+    tot = args.steps + args.warmup
+    # sample sized so that the whole run stays within a few minutes
+    n_s, L_s = (16384, 6) if tot <= 8 else ((8192, 5) if tot <= 20 else (4096, 4))
+    cpu_sample(n_s, L_s, steps=args.warmup)
+    res = cpu_sample(n_s, L_s, steps=args.steps)
+    per_step = statistics.mean(res["times"]) * res["scale"]
+    value = 1.0 / per_step
+    sample = (f"n={n_s} FixedLevel({L_s}) (256-point leaves, rank 72, same kernel, 16 RHS) per step, "
+              f"scaled x{res['scale']:.2f} to n=65536 FixedLevel(8) by the reference algorithm's flop count")
+    out = {"metric": "HODLR factor+solve+logdet/s", "value": value, "unit": "steps/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "n": N_POINTS, "rank": RANK, "level": "FixedLevel(8)", "nrhs": NRHS,
+                      "kernel": "matern32", "params": list(PARAMS)},
+           "impl": "reference",
+           "cpu_baseline": {"value": value, "unit": "steps/s", "cores": host_threads(), "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ----------------------------------------------------------------------------------------------
+# GPU leg
+# ----------------------------------------------------------------------------------------------
+
+def run_ours(args, rank: int, world: int, local_rank: int):
+    import torch
+    import kmhodlr
+    from kmhodlr import _lib as L
+    from kmhodlr.data import uniform_points
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU (no CPU fallback)")
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    lib = L.load()
+    n = N_POINTS
+    pts = uniform_points(n, SEED + rank)
+    rng = np.random.default_rng(SEED + 100 + rank)
+    rhs = rng.standard_normal((n, NRHS))
+    xv = rng.standard_normal((n, 1))
+
+    # pinned host buffers (column-major = contiguous columns)
+    h_pts = torch.from_numpy(pts.reshape(-1)).pin_memory()
+    h_rhs = torch.from_numpy(np.ascontiguousarray(rhs.T).reshape(-1)).pin_memory()
+    h_x = torch.from_numpy(xv.reshape(-1).copy()).pin_memory()
+    h_sol = torch.empty(n * NRHS, dtype=torch.float64).pin_memory()
+    h_y = torch.empty(n, dtype=torch.float64).pin_memory()
+    d_pts = h_pts.cuda()
+    d_rhs = h_rhs.cuda()
+    d_x = h_x.cuda()
+    d_sol = torch.empty(n * NRHS, dtype=torch.float64, device="cuda")
+    d_y = torch.empty(n, dtype=torch.float64, device="cuda")
+    params = np.array(PARAMS, dtype=np.float64)
+    pp = params.ctypes.data_as(C.POINTER(C.c_double))
+
+    cfg = L.KmConfig(device=dev, precision=L.KM_PREC_FP64, hbm_budget_fraction=0.8, refine_max_iter=0,
+                     refine_tol=0.0)
+    h = C.c_void_p()
+    rc = lib.km_create(C.byref(cfg), C.byref(h))
+    if rc != 0:
+        raise SystemExit(f"km_create failed ({rc})")
+    stream = torch.cuda.current_stream()
+    lib.km_set_stream(h, C.c_void_p(stream.cuda_stream))
+    logdet = C.c_double()
+
+    def check(rc):
+        if rc != 0:
+            raise RuntimeError(lib.km_last_error(h).decode())
+
+    def step_dev():
+        check(lib.km_assemble_dev(h, C.c_void_p(d_pts.data_ptr()), n, L.KM_KERNEL_MATERN32, pp, 3,
+                                  L.KM_METHOD_NYSTROM, 0.0, RANK, L.KM_LEVEL_FIXED, LEVEL))
+        check(lib.km_matvec_dev(h, C.c_void_p(d_x.data_ptr()), C.c_void_p(d_y.data_ptr()), 1))
+        check(lib.km_factorize(h))
+        check(lib.km_solve_dev(h, C.c_void_p(d_rhs.data_ptr()), C.c_void_p(d_sol.data_ptr()), NRHS))
+        check(lib.km_logdet(h, C.byref(logdet)))
+
+    dp = lambda t: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+
+    def step_e2e():
+        check(lib.km_assemble(h, dp(h_pts), n, L.KM_KERNEL_MATERN32, pp, 3, L.KM_METHOD_NYSTROM, 0.0, RANK,
+                              L.KM_LEVEL_FIXED, LEVEL))
+        check(lib.km_matvec(h, dp(h_x), dp(h_y), 1))
+        check(lib.km_factorize(h))
+        check(lib.km_solve(h, dp(h_rhs), dp(h_sol), NRHS))
+        check(lib.km_logdet(h, C.byref(logdet)))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, steps):
+        barrier()
+        st0 = L.KmStats()
+        lib.km_get_stats(h, C.byref(st0))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        st1 = L.KmStats()
+        lib.km_get_stats(h, C.byref(st1))
+        ms = e0.elapsed_time(e1)
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, st1.kernel_launches - st0.kernel_launches
+
+    for _ in range(args.warmup):
+        step_dev()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    ms, launches = timed(step_dev, args.steps)
+    clk = clocks.stop()
+    ms_e2e, _ = timed(step_e2e, args.steps)
+
+    # per-kernel-class device time (a second timed pass with per-launch events)
+    lib.km_profile_enable(h, 1)
+    timed(step_dev, args.steps)
+    prof = {}
+    for ci, name in enumerate(L.PROF_CLASSES):
+        tot, cnt = C.c_double(), C.c_int64()
+        lib.km_profile_get(h, ci, C.byref(tot), C.byref(cnt))
+        if cnt.value:
+            prof[name] = {"ms": tot.value / args.steps, "launches": cnt.value // args.steps}
+    lib.km_profile_enable(h, 0)
+    fp64_peak = kmhodlr.probe_fp64_tflops(dev)
+
+    step_ms = ms / args.steps
+    value = world * args.steps / (ms / 1e3)
+    e2e_value = world * args.steps / (ms_e2e / 1e3)
+    flops = engine_flops(n, LEVEL)
+    dom = max((k for k in prof if k in flops), key=lambda k: prof[k]["ms"], default=None)
+    roof = None
+    if dom:
+        per_launch_ms = prof[dom]["ms"] / max(prof[dom]["launches"], 1)
+        achieved = flops[dom] / (prof[dom]["ms"] * 1e-3) / 1e12
+        traffic = None
+        tf = ROOT / "profiles" / "ncu_traffic.json"
+        if tf.exists():
+            traffic = json.loads(tf.read_text()).get(dom)
+        roof = {"kernel": dom, "bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak, "traffic": traffic, "per_launch_ms": per_launch_ms,
+                "peak_source": "FP64 FMA rate measured live by km_probe_fp64_tflops (the measured-peaks file "
+                               "holds only HBM copy and bf16 tensor rates)"}
+
+    out = {"metric": "HODLR factor+solve+logdet/s", "value": value, "unit": "steps/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "n": n, "rank": RANK, "level": "FixedLevel(8)", "nrhs": NRHS,
+                      "kernel": "matern32", "params": list(PARAMS), "precision": "fp64",
+                      "l2": "inputs larger than L2 (leaf factors alone 268 MB)",
+                      "parallelism": f"replicas{world}"},
+           "e2e": {"value": e2e_value, "unit": "steps/s",
+                   "h2d_bytes_per_step": int((2 * n + n + NRHS * n) * 8),
+                   "d2h_bytes_per_step": int((n + NRHS * n + 1) * 8)},
+           "gpu_launches": int(launches),
+           "clocks": clk,
+           "roofline": roof,
+           "kernel_ms_per_step": prof,
+           "logdet": logdet.value}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        res = cpu_sample(16384, 6, steps=1)
+        v = 1.0 / (res["times"][0] * res["scale"])
+        out["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": host_threads(), "kind": "port",
+                               "sample": f"one n=16384 FixedLevel(6) step of the reference algorithm "
+                                         f"(oracle/, {res['times'][0]:.1f} s) scaled x{res['scale']:.2f} "
+                                         f"to the workload by flop count"}
+    lib.km_destroy(h)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -107,6 +107,11 @@ int km_assemble(km_handle* h, const double* pts, int64_t n, int kernel_id, const
                 int nparams, int method, double tol, int64_t maxrank, int level_kind,
                 int64_t level);
 
+/* As km_assemble with `d_pts` in device memory of the handle's device (inputs resident in HBM). */
+int km_assemble_dev(km_handle* h, const double* d_pts, int64_t n, int kernel_id,
+                    const double* params, int nparams, int method, double tol, int64_t maxrank,
+                    int level_kind, int64_t level);
+
 /* Rank of every off-diagonal block, level 1 first (nnonleaf entries). */
 int km_block_ranks(km_handle* h, int64_t* out);
 
@@ -167,6 +172,33 @@ int km_derivative_matvec(km_handle* h, int param, const double* x, double* y, in
  * Requires a factorised Nystrom HODLR. */
 int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t nprobe,
                 double* nll, double* grad);
+
+/* ---- streams and profiling ---------------------------------------------------------------- */
+
+/* Runs the handle's work on `stream` (a cudaStream_t of the handle's device; NULL restores the
+ * handle's own stream).  The caller keeps ownership of the stream. */
+int km_set_stream(km_handle* h, void* stream);
+
+/* Kernel classes timed by the profiler. */
+enum km_prof_class {
+  KM_PROF_EVAL = 0,        /* kernel-entry evaluation (leaves, landmark columns, S)           */
+  KM_PROF_LEAF_CHOL = 1,   /* batched leaf Cholesky                                           */
+  KM_PROF_LEAF_TRI = 2,    /* leaf triangular solves / products                               */
+  KM_PROF_LEAF_QR = 3,     /* leaf Householder QR                                             */
+  KM_PROF_NODE = 4,        /* per-level node factorisation                                    */
+  KM_PROF_SWEEP = 5,       /* up/down tree sweeps of products and solves                      */
+  KM_PROF_LEAF_REFL = 6,   /* leaf reflector projections / expansions                         */
+  KM_PROF_LEAF_APPLY = 7,  /* leaf products of the HODLR matvec                               */
+  KM_PROF_OTHER = 8,       /* small kernels (logdet reduction, landmark Cholesky, ...)        */
+  KM_PROF_ACA = 9,         /* adaptive cross approximation                                    */
+  KM_PROF_COUNT = 10
+};
+
+/* Enables (1) or disables (0) per-launch CUDA-event timing; enabling clears the counters. */
+int km_profile_enable(km_handle* h, int on);
+
+/* Accumulated device time (ms) and launch count of kernel class `cls` since enabling. */
+int km_profile_get(km_handle* h, int cls, double* total_ms, int64_t* launches);
 
 /* ---- diagnostics ------------------------------------------------------------------------- */
 

@@ -86,6 +86,7 @@ struct km_handle {
   double* d_R = nullptr;
   double* d_S = nullptr;
   double* d_Sc = nullptr;
+  double* d_SinvT = nullptr;
   double* d_Ct = nullptr;
   double* d_L22 = nullptr;
   double* d_Eref = nullptr;
@@ -102,6 +103,17 @@ struct km_handle {
   double* d_Y = nullptr;
   int64_t xcap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaStream_t own_stream = nullptr;  // the handle's own stream (h->stream may be external)
+  // profiler
+  bool prof = false;
+  struct Rec {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  std::vector<Rec> pending;
+  std::vector<cudaEvent_t> pool;
+  double prof_ms[KM_PROF_COUNT] = {};
+  int64_t prof_n[KM_PROF_COUNT] = {};
 };
 
 namespace {
@@ -165,7 +177,7 @@ void free_problem(km_handle* h) {
   h->allocs.clear();
   h->bytes = 0;
   h->d_pts = h->d_lnd = h->d_K = h->d_Lf = h->d_Phi = h->d_Q = h->d_tauleaf = h->d_R = nullptr;
-  h->d_S = h->d_Sc = h->d_Ct = h->d_L22 = h->d_Eref = h->d_Etau = nullptr;
+  h->d_S = h->d_Sc = h->d_SinvT = h->d_Ct = h->d_L22 = h->d_Eref = h->d_Etau = nullptr;
   h->d_lndidx = nullptr;
   h->d_info = nullptr;
   h->d_partial = h->d_scalar = nullptr;
@@ -182,9 +194,51 @@ int check_launch(km_handle* h, const char* where) {
   return KM_OK;
 }
 
+cudaEvent_t pool_event(km_handle* h) {
+  if (!h->pool.empty()) {
+    cudaEvent_t e = h->pool.back();
+    h->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Resolves the pending profiler records (their events have completed after a sync).
+void prof_resolve(km_handle* h) {
+  for (auto& r : h->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      h->prof_ms[r.cls] += ms;
+      h->prof_n[r.cls] += 1;
+    }
+    h->pool.push_back(r.a);
+    h->pool.push_back(r.b);
+  }
+  h->pending.clear();
+  cudaGetLastError();
+}
+
+// Runs one kernel launch `f`, counting it and, when profiling, bracketing it with events.
+template <typename F>
+bool run_launch(km_handle* h, int cls, F&& f) {
+  h->stats.kernel_launches += 1;
+  if (!h->prof) return f();
+  cudaEvent_t a = pool_event(h), b = pool_event(h);
+  cudaEventRecord(a, h->stream);
+  const bool ok = f();
+  cudaEventRecord(b, h->stream);
+  h->pending.push_back({cls, a, b});
+  return ok;
+}
+#define KL(h, cls, expr) run_launch(h, cls, [&]() -> bool { return (expr); })
+#define KLV(h, cls, expr) run_launch(h, cls, [&]() -> bool { expr; return true; })
+
 int sync(km_handle* h, const char* where) {
   cudaError_t e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return cuda_fail(h, e, where);
+  if (h->prof) prof_resolve(h);
   return KM_OK;
 }
 
@@ -232,15 +286,14 @@ NodeMatsH node_mats(km_handle* h) { return NodeMatsH{h->d_Ct, h->d_L22, h->d_Ere
 int nested_fwd(km_handle* h, double* X, int k) {  // X <- W^{-1} X
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
-  if (!launch_leaf_tri(h->d_Lf, t, 0, X, 1, t.n, 0, X, 1, t.n, 0, k, st))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 0, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
   if (t.L == 0) return check_launch(h, "fwd");
   NodeMatsH nm = node_mats(h);
-  launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st);
-  for (int l = 1; l <= t.L; ++l) launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_FWD_, st);
-  for (int l = t.L; l >= 1; --l) launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_FWD_, st);
-  launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, -1.0, st);
-  h->stats.kernel_launches += 3 + 2 * t.L;
+  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st));
+  for (int l = 1; l <= t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_FWD_, st));
+  for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_FWD_, st));
+  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, -1.0, st));
   return check_launch(h, "fwd");
 }
 
@@ -249,15 +302,13 @@ int nested_bwd(km_handle* h, double* X, int k) {  // X <- W'^{-1} X
   cudaStream_t st = h->stream;
   if (t.L > 0) {
     NodeMatsH nm = node_mats(h);
-    launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st);
-    for (int l = 1; l < t.L; ++l) launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_PROJ_, st);
-    for (int l = t.L; l >= 1; --l) launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_BWD_, st);
-    launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, -1.0, st);
-    h->stats.kernel_launches += 2 + 2 * t.L - 1;
+    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st));
+    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_PROJ_, st));
+    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_BWD_, st));
+    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, -1.0, st));
   }
-  if (!launch_leaf_tri(h->d_Lf, t, 1, X, 1, t.n, 0, X, 1, t.n, 0, k, st))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 1, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
-  h->stats.kernel_launches += 1;
   return check_launch(h, "bwd");
 }
 
@@ -266,31 +317,27 @@ int nested_mul(km_handle* h, double* X, int k) {  // X <- W X
   cudaStream_t st = h->stream;
   if (t.L > 0) {
     NodeMatsH nm = node_mats(h);
-    launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st);
-    for (int l = 1; l < t.L; ++l) launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_PROJ_, st);
-    for (int l = t.L; l >= 1; --l) launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_MUL_, st);
-    launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, 1.0, st);
-    h->stats.kernel_launches += 2 + 2 * t.L - 1;
+    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st));
+    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_PROJ_, st));
+    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_MUL_, st));
+    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, 1.0, st));
   }
-  if (!launch_leaf_tri(h->d_Lf, t, 2, X, 1, t.n, 0, X, 1, t.n, 0, k, st))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 2, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular kernel");
-  h->stats.kernel_launches += 1;
   return check_launch(h, "mul");
 }
 
 int nested_mul_t(km_handle* h, double* X, int k) {  // X <- W' X
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
-  if (!launch_leaf_tri(h->d_Lf, t, 3, X, 1, t.n, 0, X, 1, t.n, 0, k, st))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 3, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular kernel");
-  h->stats.kernel_launches += 1;
   if (t.L == 0) return check_launch(h, "mul_t");
   NodeMatsH nm = node_mats(h);
-  launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st);
-  for (int l = 1; l <= t.L; ++l) launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_MULT_, st);
-  for (int l = t.L; l >= 1; --l) launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_MULT_, st);
-  launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, 1.0, st);
-  h->stats.kernel_launches += 2 + 2 * t.L;
+  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st));
+  for (int l = 1; l <= t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_MULT_, st));
+  for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_MULT_, st));
+  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, 1.0, st));
   return check_launch(h, "mul_t");
 }
 
@@ -300,15 +347,13 @@ int nystrom_matvec(km_handle* h, const double* X, double* Y, int k) {
   cudaStream_t st = h->stream;
   NodeMatsH nm = node_mats(h);
   if (t.L > 0) {
-    launch_leaf_phiT(h->d_Phi, h->r, t, X, t.n, h->d_VP, k, st);
-    for (int l = 1; l < t.L; ++l) launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_SUM_, st);
-    for (int l = t.L; l >= 1; --l) launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_NYS_, st);
-    h->stats.kernel_launches += 1 + 2 * t.L - 1;
+    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_phiT(h->d_Phi, h->r, t, X, t.n, h->d_VP, k, st));
+    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_SUM_, st));
+    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_NYS_, st));
   } else {
     cudaMemsetAsync(h->d_VG, 0, sizeof(double) * h->r * k, st);
   }
-  launch_leaf_nys_apply(h->d_K, h->d_Phi, h->d_Sc, h->r, t, X, t.n, h->d_VG, Y, t.n, k, st);
-  h->stats.kernel_launches += 1;
+  KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_nys_apply(h->d_K, h->d_Phi, h->d_Sc, h->r, t, X, t.n, h->d_VG, Y, t.n, k, st));
   return check_launch(h, "matvec");
 }
 
@@ -416,7 +461,37 @@ int km_create(const km_config* cfg, km_handle** out) {
     delete h;
     return KM_ERR_CUDA;
   }
+  h->own_stream = h->stream;
   *out = h;
+  return KM_OK;
+}
+
+int km_set_stream(km_handle* h, void* stream) {
+  if (!h) return KM_ERR_BAD_ARG;
+  cudaSetDevice(h->cfg.device);
+  cudaStreamSynchronize(h->stream);
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return KM_OK;
+}
+
+int km_profile_enable(km_handle* h, int on) {
+  if (!h) return KM_ERR_BAD_ARG;
+  cudaStreamSynchronize(h->stream);
+  prof_resolve(h);
+  h->prof = on != 0;
+  for (int c = 0; c < KM_PROF_COUNT; ++c) {
+    h->prof_ms[c] = 0.0;
+    h->prof_n[c] = 0;
+  }
+  return KM_OK;
+}
+
+int km_profile_get(km_handle* h, int cls, double* total_ms, int64_t* launches) {
+  if (!h || cls < 0 || cls >= KM_PROF_COUNT) return KM_ERR_BAD_ARG;
+  cudaStreamSynchronize(h->stream);
+  prof_resolve(h);
+  if (total_ms) *total_ms = h->prof_ms[cls];
+  if (launches) *launches = h->prof_n[cls];
   return KM_OK;
 }
 
@@ -424,9 +499,11 @@ int km_destroy(km_handle* h) {
   if (!h) return KM_OK;
   cudaSetDevice(h->cfg.device);
   free_problem(h);
+  prof_resolve(h);
+  for (auto e : h->pool) cudaEventDestroy(e);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return KM_OK;
 }
@@ -440,9 +517,9 @@ int km_get_stats(const km_handle* h, km_stats* out) {
   return KM_OK;
 }
 
-int km_assemble(km_handle* h, const double* pts, int64_t n, int kernel_id, const double* params,
-                int nparams, int method, double tol, int64_t maxrank, int level_kind,
-                int64_t level) {
+static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, int kernel_id,
+                         const double* params, int nparams, int method, double tol, int64_t maxrank,
+                         int level_kind, int64_t level) {
   if (!h) return KM_ERR_BAD_ARG;
   cudaSetDevice(h->cfg.device);
   if (!pts || !params) return fail(h, KM_ERR_BAD_ARG, "null pointer");
@@ -463,47 +540,54 @@ int km_assemble(km_handle* h, const double* pts, int64_t n, int kernel_id, const
   if (maxrank >= minleaf - 1)
     return fail(h, KM_ERR_BAD_ARG, "Your nystrom rank is too big. Reduce the HODLR level or nystrom rank.");
   if (maxrank > kMaxNysRank) return fail(h, KM_ERR_UNSUPPORTED, "Nystrom rank above 80 is not supported");
-  free_problem(h);
+  // Buffers are kept when the problem shape (n, levels, rank) is unchanged, so that repeated
+  // assemblies (likelihood evaluations at new parameters) allocate nothing.
+  const bool reuse = h->d_pts && h->tree.n == t.n && h->tree.L == t.L && h->r == (int)maxrank;
+  if (!reuse) free_problem(h);
   h->tree = t;
   h->kp = KParams{kernel_id, params[0], params[1], params[2]};
   h->method = method;
   h->tol = tol;
   h->maxrank = maxrank;
   h->r = (int)maxrank;
+  h->assembled = h->factorized = false;
   const int r = h->r;
   int64_t kbytes = 0;
   for (int64_t j = 0; j < t.nleaf; ++j) kbytes += t.leaf_size(j) * t.leaf_size(j);
   int rc;
-  if ((rc = dalloc(h, &h->d_pts, 2 * n)) || (rc = dalloc(h, &h->d_lnd, 2 * r)) ||
-      (rc = dalloc(h, &h->d_lndidx, r)) || (rc = dalloc(h, &h->d_K, kbytes)) ||
-      (rc = dalloc(h, &h->d_Lf, kbytes)) || (rc = dalloc(h, &h->d_Phi, n * r)) ||
-      (rc = dalloc(h, &h->d_Q, n * r)) || (rc = dalloc(h, &h->d_tauleaf, t.nleaf * r)) ||
-      (rc = dalloc(h, &h->d_R, (t.nleaf + t.nnode) * r * r)) || (rc = dalloc(h, &h->d_S, r * r)) ||
-      (rc = dalloc(h, &h->d_Sc, r * r)) || (rc = dalloc(h, &h->d_Ct, std::max<int64_t>(t.nnode, 1) * r * r)) ||
-      (rc = dalloc(h, &h->d_L22, std::max<int64_t>(t.nnode, 1) * r * r)) ||
-      (rc = dalloc(h, &h->d_Eref, std::max<int64_t>(t.nnode, 1) * r * r)) ||
-      (rc = dalloc(h, &h->d_Etau, std::max<int64_t>(t.nnode, 1) * r)) ||
-      (rc = dalloc(h, &h->d_info, t.nleaf + t.nnode + 1)) ||
-      (rc = dalloc(h, &h->d_partial, kLogdetBlocks)) || (rc = dalloc(h, &h->d_scalar, 4))) {
+  if (!reuse &&
+      ((rc = dalloc(h, &h->d_pts, 2 * n)) || (rc = dalloc(h, &h->d_lnd, 2 * r)) ||
+       (rc = dalloc(h, &h->d_lndidx, r)) || (rc = dalloc(h, &h->d_K, kbytes)) ||
+       (rc = dalloc(h, &h->d_Lf, kbytes)) || (rc = dalloc(h, &h->d_Phi, n * r)) ||
+       (rc = dalloc(h, &h->d_Q, n * r)) || (rc = dalloc(h, &h->d_tauleaf, t.nleaf * r)) ||
+       (rc = dalloc(h, &h->d_R, (t.nleaf + t.nnode) * r * r)) || (rc = dalloc(h, &h->d_S, r * r)) ||
+       (rc = dalloc(h, &h->d_Sc, r * r)) || (rc = dalloc(h, &h->d_SinvT, r * r)) ||
+       (rc = dalloc(h, &h->d_Ct, std::max<int64_t>(t.nnode, 1) * r * r)) ||
+       (rc = dalloc(h, &h->d_L22, std::max<int64_t>(t.nnode, 1) * r * r)) ||
+       (rc = dalloc(h, &h->d_Eref, std::max<int64_t>(t.nnode, 1) * r * r)) ||
+       (rc = dalloc(h, &h->d_Etau, std::max<int64_t>(t.nnode, 1) * r)) ||
+       (rc = dalloc(h, &h->d_info, t.nleaf + t.nnode + 1)) ||
+       (rc = dalloc(h, &h->d_partial, kLogdetBlocks)) || (rc = dalloc(h, &h->d_scalar, 4)))) {
     free_problem(h);
     return rc;
   }
   timer_start(h);
   cudaStream_t st = h->stream;
-  KM_CUDA(h, cudaMemcpyAsync(h->d_pts, pts, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, st));
+  KM_CUDA(h, cudaMemcpyAsync(h->d_pts, pts, sizeof(double) * 2 * n,
+                             dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
   std::vector<int64_t> idx(r);
   km_nystrom_landmarks(n, r, idx.data());
   for (auto& v : idx) v -= 1;
   KM_CUDA(h, cudaMemcpyAsync(h->d_lndidx, idx.data(), sizeof(int64_t) * r, cudaMemcpyHostToDevice, st));
   KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + t.nnode + 1), st));
-  launch_gather_points(h->d_pts, h->d_lndidx, r, h->d_lnd, st);
-  launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st);
-  launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, -1, h->d_Phi, st);
-  launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, -1, h->d_S, r, st);
+  KLV(h, KM_PROF_EVAL, launch_gather_points(h->d_pts, h->d_lndidx, r, h->d_lnd, st));
+  KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st));
+  KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, -1, h->d_Phi, st));
+  KLV(h, KM_PROF_EVAL, launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, -1, h->d_S, r, st));
   KM_CUDA(h, cudaMemcpyAsync(h->d_Sc, h->d_S, sizeof(double) * r * r, cudaMemcpyDeviceToDevice, st));
-  if (!launch_chol_small(h->d_Sc, r, h->d_info + t.nleaf + t.nnode, st))
+  if (!KL(h, KM_PROF_OTHER, launch_chol_small(h->d_Sc, r, h->d_info + t.nleaf + t.nnode, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "rank too large for the landmark Cholesky");
-  h->stats.kernel_launches += 5;
+  KLV(h, KM_PROF_OTHER, launch_tri_inv_t(h->d_Sc, r, h->d_SinvT, st));
   if ((rc = check_launch(h, "assemble")) != KM_OK) return rc;
   h->stats.assemble_ms = timer_stop(h);
   if ((rc = sync(h, "assemble")) != KM_OK) return rc;
@@ -513,6 +597,20 @@ int km_assemble(km_handle* h, const double* pts, int64_t n, int kernel_id, const
   h->assembled = true;
   h->factorized = false;
   return KM_OK;
+}
+
+int km_assemble(km_handle* h, const double* pts, int64_t n, int kernel_id, const double* params,
+                int nparams, int method, double tol, int64_t maxrank, int level_kind,
+                int64_t level) {
+  return assemble_impl(h, pts, false, n, kernel_id, params, nparams, method, tol, maxrank,
+                       level_kind, level);
+}
+
+int km_assemble_dev(km_handle* h, const double* d_pts, int64_t n, int kernel_id,
+                    const double* params, int nparams, int method, double tol, int64_t maxrank,
+                    int level_kind, int64_t level) {
+  return assemble_impl(h, d_pts, true, n, kernel_id, params, nparams, method, tol, maxrank,
+                       level_kind, level);
 }
 
 int km_factorize(km_handle* h) {
@@ -525,19 +623,17 @@ int km_factorize(km_handle* h) {
   int rc;
   timer_start(h);
   KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + t.nnode), st));
-  if (!launch_leaf_chol(h->d_K, h->d_Lf, t, h->d_info, st))
+  if (!KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol(h->d_K, h->d_Lf, t, h->d_info, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the leaf Cholesky kernel");
   // A = L^{-1} Phi on every leaf, then Householder QR of each leaf panel
   KM_CUDA(h, cudaMemcpyAsync(h->d_Q, h->d_Phi, sizeof(double) * t.n * r, cudaMemcpyDeviceToDevice, st));
-  if (!launch_leaf_tri(h->d_Lf, t, 0, h->d_Q, r, 0, 1, h->d_Q, r, 0, 1, r, st))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 0, h->d_Q, r, 0, 1, h->d_Q, r, 0, 1, r, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
-  h->stats.kernel_launches += 2;
   if (t.L > 0) {
-    launch_leaf_qr(h->d_Q, r, t, h->d_tauleaf, h->d_R, st);
+    KLV(h, KM_PROF_LEAF_QR, launch_leaf_qr(h->d_Q, r, t, h->d_tauleaf, h->d_R, st));
     for (int l = 1; l <= t.L; ++l)
-      launch_node_factor(h->d_R, h->d_Sc, r, l, t, h->d_Ct, h->d_L22, h->d_Eref, h->d_Etau,
-                         h->d_info + t.nleaf, st);
-    h->stats.kernel_launches += 1 + t.L;
+      KLV(h, KM_PROF_NODE, launch_node_factor(h->d_R, h->d_SinvT, r, l, t, h->d_Ct, h->d_L22, h->d_Eref,
+                                              h->d_Etau, h->d_info + t.nleaf, st));
   }
   if ((rc = check_launch(h, "factorize")) != KM_OK) return rc;
   h->stats.factorize_ms = timer_stop(h);
@@ -649,8 +745,8 @@ int km_logdet(km_handle* h, double* out) {
   cudaSetDevice(h->cfg.device);
   if (!h->factorized) return fail(h, KM_ERR_STATE, "No logdet without factorization.");
   timer_start(h);
-  launch_logdet(h->d_Lf, h->tree, h->d_L22, h->r, h->d_partial, kLogdetBlocks, h->d_scalar, h->stream);
-  h->stats.kernel_launches += 2;
+  KLV(h, KM_PROF_OTHER, launch_logdet(h->d_Lf, h->tree, h->d_L22, h->r, h->d_partial, kLogdetBlocks, h->d_scalar, h->stream));
+  h->stats.kernel_launches += 1;  // the logdet runs a partial and a final reduction kernel
   int rc;
   if ((rc = check_launch(h, "logdet")) != KM_OK) return rc;
   KM_CUDA(h, cudaMemcpyAsync(out, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, h->stream));

@@ -27,17 +27,16 @@ struct NodeMats {
   int r;
 };
 
-// x (2r, warp-shared) <- H_0 ... H_{r-1} applied in order j = 0..r-1 (E' side) when fwd,
-// or j = r-1..0 (E side) when !fwd.  Reflector j = [e_j ; Eref[:, j]] with tau_j.
-__device__ __forceinline__ void apply_node_reflectors(const double* __restrict__ Eref,
-                                                      const double* __restrict__ tau, int r,
+// x (2r, warp-shared) <- reflectors applied in order j = 0..r-1 (E' x, fwd) or j = r-1..0
+// (E x).  Reflector j = [e_j ; Es[:, j]] with tau ts[j]; Es is r x r with leading dim ld.
+__device__ __forceinline__ void apply_node_reflectors(const double* Es, const double* ts, int r, int ld,
                                                       double* x, bool fwd) {
   const int lane = threadIdx.x & 31;
   for (int q = 0; q < r; ++q) {
     const int j = fwd ? q : r - 1 - q;
-    const double tj = tau[j];
+    const double tj = ts[j];
     if (tj == 0.0) continue;
-    const double* v = Eref + (int64_t)j * r;
+    const double* v = Es + j * ld;
     double acc = 0.0;
     for (int i = lane; i < r; i += 32) acc += v[i] * x[r + i];
     acc = warp_sum(acc);
@@ -54,19 +53,41 @@ enum { UP_PROJ = 0, UP_FWD = 1, UP_MULT = 2, UP_SUM = 3 };
 // down-sweep modes
 enum { DN_FWD = 0, DN_BWD = 1, DN_MUL = 2, DN_MULT = 3, DN_NYS = 4 };
 
-// grid = (nodes at level, ceil(k/8)), block 256: one warp per (node, column).
+// Stages the node's Ct, L22, Eref (leading dimension r+1) and tau in shared memory.
+__device__ __forceinline__ void stage_node(const NodeMats& nm, int64_t node, double* Cs, double* Ls,
+                                           double* Es, double* ts) {
+  const int r = nm.r, ld = r + 1;
+  const int64_t off = node * (int64_t)r * r;
+  for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
+    const int i = e % r, c = e / r;
+    Cs[i + c * ld] = nm.Ct[off + e];
+    Ls[i + c * ld] = nm.L22[off + e];
+    Es[i + c * ld] = nm.Eref[off + e];
+  }
+  for (int e = threadIdx.x; e < r; e += blockDim.x) ts[e] = nm.Etau[node * r + e];
+  __syncthreads();
+}
+
+// grid = (nodes at level, ceil(k/8)), block 256: one warp per (node, column); the node's
+// matrices are shared by the CTA's 8 columns.
 __global__ void __launch_bounds__(256) k_up(NodeMats nm, int level, int L, int64_t cslot0, int64_t nslot0,
                                             int64_t node0, double* __restrict__ VP, double* __restrict__ VD,
                                             int k, int mode) {
   extern __shared__ double sm[];
-  const int r = nm.r;
+  const int r = nm.r, ld = r + 1;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int col = blockIdx.y * 8 + w;
-  if (col >= k) return;
   const int64_t kk = blockIdx.x;
   const int64_t node = node0 + kk;
-  double* x = sm + (size_t)w * 3 * r;  // [0,2r): x   [2r,3r): t
+  double* Cs = sm;
+  double* Ls = Cs + r * ld;
+  double* Es = Ls + r * ld;
+  double* ts = Es + r * ld;
+  const bool mats = (mode != UP_SUM);
+  double* x = (mats ? ts + r : sm) + (size_t)w * 3 * r;  // [0,2r): x   [2r,3r): t
   double* t = x + 2 * r;
+  if (mats) stage_node(nm, node, Cs, Ls, Es, ts);
+  if (col >= k) return;
   const double* z1 = VP + ((cslot0 + 2 * kk) * k + col) * r;
   const double* z2 = VP + ((cslot0 + 2 * kk + 1) * k + col) * r;
   for (int i = lane; i < r; i += 32) {
@@ -74,8 +95,6 @@ __global__ void __launch_bounds__(256) k_up(NodeMats nm, int level, int L, int64
     x[r + i] = z2[i];
   }
   __syncwarp();
-  const double* Ct = nm.Ct + node * (int64_t)r * r;
-  const double* L22 = nm.L22 + node * (int64_t)r * r;
   if (mode == UP_SUM) {
     if (level < L) {
       double* out = VP + ((nslot0 + kk) * k + col) * r;
@@ -86,18 +105,19 @@ __global__ void __launch_bounds__(256) k_up(NodeMats nm, int level, int L, int64
   if (mode == UP_FWD) {
     // t = z2 - Ct' z1
     for (int i = lane; i < r; i += 32) {
-      const double* ci = Ct + (int64_t)i * r;
+      const double* ci = Cs + i * ld;
       double acc = 0.0;
+#pragma unroll 8
       for (int l = 0; l < r; ++l) acc += ci[l] * x[l];
       t[i] = x[r + i] - acc;
     }
     __syncwarp();
     // w = L22^{-1} t (in t)
     for (int l = 0; l < r; ++l) {
-      const double wl = t[l] / L22[(int64_t)l * r + l];
+      const double wl = t[l] / Ls[l * ld + l];
       __syncwarp();
       if (lane == 0) t[l] = wl;
-      for (int i = l + 1 + lane; i < r; i += 32) t[i] -= L22[(int64_t)l * r + i] * wl;
+      for (int i = l + 1 + lane; i < r; i += 32) t[i] -= Ls[l * ld + i] * wl;
       __syncwarp();
     }
     double* d = VD + (node * k + col) * 2 * r;
@@ -111,8 +131,9 @@ __global__ void __launch_bounds__(256) k_up(NodeMats nm, int level, int L, int64
     double* d = VD + (node * k + col) * 2 * r;
     for (int i = lane; i < r; i += 32) {
       double a1 = 0.0, a2 = 0.0;
-      for (int l = 0; l < r; ++l) a1 += Ct[i + (int64_t)l * r] * x[r + l];
-      for (int l = i; l < r; ++l) a2 += L22[l + (int64_t)i * r] * x[r + l];
+#pragma unroll 8
+      for (int l = 0; l < r; ++l) a1 += Cs[i + l * ld] * x[r + l];
+      for (int l = i; l < r; ++l) a2 += Ls[l + i * ld] * x[r + l];
       a2 -= x[r + i];
       d[i] = a1;
       d[r + i] = a2;
@@ -124,7 +145,7 @@ __global__ void __launch_bounds__(256) k_up(NodeMats nm, int level, int L, int64
     __syncwarp();
   }
   if (level < L) {
-    apply_node_reflectors(nm.Eref + node * (int64_t)r * r, nm.Etau + node * r, r, x, true);
+    apply_node_reflectors(Es, ts, r, ld, x, true);
     double* out = VP + ((nslot0 + kk) * k + col) * r;
     for (int i = lane; i < r; i += 32) out[i] = x[i];
   }
@@ -135,27 +156,33 @@ __global__ void __launch_bounds__(256) k_down(NodeMats nm, int level, int L, int
                                               double* __restrict__ VG, const double* __restrict__ VD,
                                               int k, int mode) {
   extern __shared__ double sm[];
-  const int r = nm.r;
+  const int r = nm.r, ld = r + 1;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int col = blockIdx.y * 8 + w;
-  if (col >= k) return;
   const int64_t kk = blockIdx.x;
   const int64_t node = node0 + kk;
-  double* x = sm + (size_t)w * 4 * r;  // [0,2r): base   [2r,4r): scratch
-  double* t = x + 2 * r;
-  const double* g = VG + ((nslot0 + kk) * k + col) * r;
   const bool top = (level >= L);
+  double* Cs = sm;
+  double* Ls = Cs + r * ld;
+  double* Es = Ls + r * ld;
+  double* ts = Es + r * ld;
+  const bool mats = (mode != DN_NYS);
+  double* x = (mats ? ts + r : sm) + (size_t)w * 4 * r;  // [0,2r): base   [2r,4r): scratch
+  double* t = x + 2 * r;
+  if (mats) stage_node(nm, node, Cs, Ls, Es, ts);
+  if (col >= k) return;
+  const double* g = VG + ((nslot0 + kk) * k + col) * r;
   for (int i = lane; i < r; i += 32) {
     x[i] = top ? 0.0 : g[i];
     x[r + i] = 0.0;
   }
   __syncwarp();
+  double* g1 = VG + ((cslot0 + 2 * kk) * k + col) * r;
+  double* g2 = VG + ((cslot0 + 2 * kk + 1) * k + col) * r;
+  const double* p1 = VP + ((cslot0 + 2 * kk) * k + col) * r;
+  const double* p2 = VP + ((cslot0 + 2 * kk + 1) * k + col) * r;
   if (mode == DN_NYS) {
     // coefficient sums: child c1 gets parent + phi(c2), child c2 gets parent + phi(c1)
-    const double* p1 = VP + ((cslot0 + 2 * kk) * k + col) * r;
-    const double* p2 = VP + ((cslot0 + 2 * kk + 1) * k + col) * r;
-    double* g1 = VG + ((cslot0 + 2 * kk) * k + col) * r;
-    double* g2 = VG + ((cslot0 + 2 * kk + 1) * k + col) * r;
     for (int i = lane; i < r; i += 32) {
       const double b = x[i];
       g1[i] = b + p2[i];
@@ -163,11 +190,7 @@ __global__ void __launch_bounds__(256) k_down(NodeMats nm, int level, int L, int
     }
     return;
   }
-  if (!top) apply_node_reflectors(nm.Eref + node * (int64_t)r * r, nm.Etau + node * r, r, x, false);
-  const double* Ct = nm.Ct + node * (int64_t)r * r;
-  const double* L22 = nm.L22 + node * (int64_t)r * r;
-  double* g1 = VG + ((cslot0 + 2 * kk) * k + col) * r;
-  double* g2 = VG + ((cslot0 + 2 * kk + 1) * k + col) * r;
+  if (!top) apply_node_reflectors(Es, ts, r, ld, x, false);
   if (mode == DN_FWD) {
     const double* d = VD + (node * k + col) * 2 * r;
     for (int i = lane; i < r; i += 32) {
@@ -181,8 +204,6 @@ __global__ void __launch_bounds__(256) k_down(NodeMats nm, int level, int L, int
       g2[i] = x[r + i] + d[r + i];
     }
   } else if (mode == DN_BWD) {
-    const double* p1 = VP + ((cslot0 + 2 * kk) * k + col) * r;
-    const double* p2 = VP + ((cslot0 + 2 * kk + 1) * k + col) * r;
     // z2 = p2 - base_bot (kept in t[r..2r)), then t[0..r) = L22^{-T} z2
     for (int i = lane; i < r; i += 32) {
       const double z2 = p2[i] - x[r + i];
@@ -191,22 +212,20 @@ __global__ void __launch_bounds__(256) k_down(NodeMats nm, int level, int L, int
     }
     __syncwarp();
     for (int i = r - 1; i >= 0; --i) {
-      const double xi = t[i] / L22[(int64_t)i * r + i];
+      const double xi = t[i] / Ls[i * ld + i];
       __syncwarp();
       if (lane == 0) t[i] = xi;
-      for (int l = lane; l < i; l += 32) t[l] -= L22[i + (int64_t)l * r] * xi;
+      for (int l = lane; l < i; l += 32) t[l] -= Ls[i + l * ld] * xi;
       __syncwarp();
     }
-    (void)p1;
     for (int i = lane; i < r; i += 32) {
       double acc = 0.0;
-      for (int l = 0; l < r; ++l) acc += Ct[i + (int64_t)l * r] * t[l];
+#pragma unroll 8
+      for (int l = 0; l < r; ++l) acc += Cs[i + l * ld] * t[l];
       g1[i] = x[i] + acc;
       g2[i] = x[r + i] + t[r + i] - t[i];
     }
   } else {  // DN_MUL
-    const double* p1 = VP + ((cslot0 + 2 * kk) * k + col) * r;
-    const double* p2 = VP + ((cslot0 + 2 * kk + 1) * k + col) * r;
     for (int i = lane; i < r; i += 32) {
       t[i] = p1[i] + x[i];
       t[r + i] = p2[i] + x[r + i];
@@ -214,83 +233,15 @@ __global__ void __launch_bounds__(256) k_down(NodeMats nm, int level, int L, int
     __syncwarp();
     for (int i = lane; i < r; i += 32) {
       double acc = 0.0;
-      const double* ci = Ct + (int64_t)i * r;
+      const double* ci = Cs + i * ld;
+#pragma unroll 8
       for (int l = 0; l < r; ++l) acc += ci[l] * t[l];
-      for (int l = 0; l <= i; ++l) acc += L22[i + (int64_t)l * r] * t[r + l];
+      for (int l = 0; l <= i; ++l) acc += Ls[i + l * ld] * t[r + l];
       acc -= t[r + i];
       g1[i] = x[i];
       g2[i] = x[r + i] + acc;
     }
   }
-}
-
-// VP[leaf][col] = (H_{r-1} ... H_0 y_leaf)[0:r]  = Q_leaf' y_leaf.
-// grid = (nleaf, ceil(k/8)), block 256, warp per column; y column staged in shared memory.
-__global__ void __launch_bounds__(256) k_leaf_proj(const double* __restrict__ Qref, const double* __restrict__ tau,
-                                                   int r, DTree t, const double* __restrict__ Y, int64_t ldy,
-                                                   double* __restrict__ VP, int k) {
-  extern __shared__ double sm[];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int col = blockIdx.y * 8 + w;
-  if (col >= k) return;
-  const int64_t leaf = blockIdx.x;
-  const int m = d_leaf_size(t, leaf);
-  const int64_t s = d_leaf_start(t, leaf);
-  double* y = sm + (size_t)w * m;
-  const double* src = Y + (int64_t)col * ldy + s;
-  for (int i = lane; i < m; i += 32) y[i] = src[i];
-  __syncwarp();
-  const double* Q = Qref + s * r;
-  const double* tl = tau + leaf * r;
-  for (int j = 0; j < r; ++j) {
-    const double tj = tl[j];
-    if (tj == 0.0) continue;
-    const double* v = Q + (int64_t)j * m;
-    double acc = 0.0;
-    for (int i = j + 1 + lane; i < m; i += 32) acc += v[i] * y[i];
-    acc = warp_sum(acc);
-    acc = (acc + y[j]) * tj;
-    __syncwarp();
-    if (lane == 0) y[j] -= acc;
-    for (int i = j + 1 + lane; i < m; i += 32) y[i] -= acc * v[i];
-    __syncwarp();
-  }
-  double* out = VP + (leaf * k + col) * r;
-  for (int i = lane; i < r; i += 32) out[i] = y[i];
-}
-
-// y_leaf += sign * Q_leaf g_leaf,  Q g = H_0 ... H_{r-1} [g; 0].
-__global__ void __launch_bounds__(256) k_leaf_expand(const double* __restrict__ Qref, const double* __restrict__ tau,
-                                                     int r, DTree t, const double* __restrict__ VG,
-                                                     double* __restrict__ Y, int64_t ldy, int k, double sign) {
-  extern __shared__ double sm[];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int col = blockIdx.y * 8 + w;
-  if (col >= k) return;
-  const int64_t leaf = blockIdx.x;
-  const int m = d_leaf_size(t, leaf);
-  const int64_t s = d_leaf_start(t, leaf);
-  double* x = sm + (size_t)w * m;
-  const double* g = VG + (leaf * k + col) * r;
-  for (int i = lane; i < m; i += 32) x[i] = (i < r) ? g[i] : 0.0;
-  __syncwarp();
-  const double* Q = Qref + s * r;
-  const double* tl = tau + leaf * r;
-  for (int j = r - 1; j >= 0; --j) {
-    const double tj = tl[j];
-    if (tj == 0.0) continue;
-    const double* v = Q + (int64_t)j * m;
-    double acc = 0.0;
-    for (int i = j + 1 + lane; i < m; i += 32) acc += v[i] * x[i];
-    acc = warp_sum(acc);
-    acc = (acc + x[j]) * tj;
-    __syncwarp();
-    if (lane == 0) x[j] -= acc;
-    for (int i = j + 1 + lane; i < m; i += 32) x[i] -= acc * v[i];
-    __syncwarp();
-  }
-  double* dst = Y + (int64_t)col * ldy + s;
-  for (int i = lane; i < m; i += 32) dst[i] += sign * x[i];
 }
 
 // VP[leaf][col] = Phi_leaf' x_leaf  (r values), Phi per leaf column-major m x r.
@@ -389,7 +340,9 @@ void launch_up(const Tree& t, const NodeMatsH& h, int level, double* VP, double*
                cudaStream_t st) {
   NodeMats nm{h.Ct, h.L22, h.Eref, h.Etau, h.r};
   dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + 7) / 8));
-  k_up<<<grid, 256, (size_t)8 * 3 * h.r * sizeof(double), st>>>(
+  const size_t sm = ((mode != UP_SUM_) ? (size_t)3 * h.r * (h.r + 1) + h.r : 0) * sizeof(double) + (size_t)8 * 3 * h.r * sizeof(double);
+  cudaFuncSetAttribute(k_up, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_up<<<grid, 256, sm, st>>>(
       nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level], t.node_off[level], VP, VD, k, mode);
 }
 
@@ -397,24 +350,10 @@ void launch_down(const Tree& t, const NodeMatsH& h, int level, const double* VP,
                  const double* VD, int k, int mode, cudaStream_t st) {
   NodeMats nm{h.Ct, h.L22, h.Eref, h.Etau, h.r};
   dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + 7) / 8));
-  k_down<<<grid, 256, (size_t)8 * 4 * h.r * sizeof(double), st>>>(
+  const size_t sm = ((mode != DN_NYS_) ? (size_t)3 * h.r * (h.r + 1) + h.r : 0) * sizeof(double) + (size_t)8 * 4 * h.r * sizeof(double);
+  cudaFuncSetAttribute(k_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_down<<<grid, 256, sm, st>>>(
       nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level], t.node_off[level], VP, VG, VD, k, mode);
-}
-
-void launch_leaf_proj(const double* Qref, const double* tau, int r, const Tree& t, const double* Y,
-                      int64_t ldy, double* VP, int k, cudaStream_t st) {
-  dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
-  const size_t sm = (size_t)8 * t.max_leaf * sizeof(double);
-  cudaFuncSetAttribute(k_leaf_proj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_leaf_proj<<<grid, 256, sm, st>>>(Qref, tau, r, dtree(t), Y, ldy, VP, k);
-}
-
-void launch_leaf_expand(const double* Qref, const double* tau, int r, const Tree& t, const double* VG,
-                        double* Y, int64_t ldy, int k, double sign, cudaStream_t st) {
-  dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
-  const size_t sm = (size_t)8 * t.max_leaf * sizeof(double);
-  cudaFuncSetAttribute(k_leaf_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_leaf_expand<<<grid, 256, sm, st>>>(Qref, tau, r, dtree(t), VG, Y, ldy, k, sign);
 }
 
 void launch_leaf_phiT(const double* Phi, int r, const Tree& t, const double* X, int64_t ldx, double* VP,

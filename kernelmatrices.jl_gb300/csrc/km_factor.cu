@@ -142,86 +142,6 @@ __global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K,
 }
 
 // ---------------------------------------------------------------------------------------------
-// Batched leaf triangular solve / multiply with the leaf factors (lower, column-major).
-//   op 0: X = L^{-1} B      op 1: X = L^{-T} B      op 2: X = L B      op 3: X = L^T B
-// Operand addressing for leaf j: base + start(j)*bmul, leading dimension (ld_is_m ? m_j : ld).
-// grid = (nleaf, ceil(ncols / 8)), block = 256 (8 warps, one column each).
-// The 8-column chunk of the right-hand side is staged in shared memory (m x 8).
-// ---------------------------------------------------------------------------------------------
-struct LeafOperand {
-  double* ptr;
-  int64_t bmul;     // base offset multiplier of the leaf start
-  int64_t ld;       // leading dimension when !ld_is_m
-  int ld_is_m;
-};
-
-__global__ void __launch_bounds__(256) k_leaf_tri(const double* __restrict__ Lf, DTree t, int op,
-                                                  LeafOperand B, LeafOperand X, int ncols) {
-  extern __shared__ double xs[];  // m x 8, column c at xs[c*m]
-  const int64_t leaf = blockIdx.x;
-  const int m = d_leaf_size(t, leaf);
-  const int64_t s = d_leaf_start(t, leaf);
-  const double* L = Lf + d_leaf_koff(t, leaf);
-  const int c0 = blockIdx.y * 8;
-  const int nc = min(8, ncols - c0);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t ldb = B.ld_is_m ? m : B.ld, ldx = X.ld_is_m ? m : X.ld;
-  const double* Bp = B.ptr + s * B.bmul;
-  double* Xp = X.ptr + s * X.bmul;
-  for (int e = threadIdx.x; e < nc * m; e += blockDim.x) {
-    const int c = e / m, i = e % m;
-    xs[c * m + i] = Bp[(int64_t)(c0 + c) * ldb + i];
-  }
-  __syncthreads();
-  if (w < nc) {
-    double* x = xs + w * m;
-    if (op == 0) {  // forward substitution, column oriented
-      for (int l = 0; l < m; ++l) {
-        const double xl = x[l] / L[(int64_t)l * m + l];
-        __syncwarp();
-        if (lane == 0) x[l] = xl;
-        const double* Lc = L + (int64_t)l * m;
-        for (int i = l + 1 + lane; i < m; i += 32) x[i] -= Lc[i] * xl;
-        __syncwarp();
-      }
-    } else if (op == 1) {  // backward substitution with L^T: row oriented dot products
-      for (int i = m - 1; i >= 0; --i) {
-        const double* Lc = L + (int64_t)i * m;  // column i of L = row i of L^T
-        double acc = 0.0;
-        for (int l = i + 1 + lane; l < m; l += 32) acc += Lc[l] * x[l];
-        acc = warp_sum(acc);
-        if (lane == 0) x[i] = (x[i] - acc) / Lc[i];
-        __syncwarp();
-      }
-    } else if (op == 2) {  // y = L x, from the bottom row up so x can be overwritten
-      for (int i = m - 1; i >= 0; --i) {
-        double acc = 0.0;
-        for (int l = lane; l <= i; l += 32) acc += L[(int64_t)l * m + i] * x[l];
-        acc = warp_sum(acc);
-        __syncwarp();
-        if (lane == 0) x[i] = acc;
-        __syncwarp();
-      }
-    } else {  // y = L^T x, from the top row down
-      for (int i = 0; i < m; ++i) {
-        const double* Lc = L + (int64_t)i * m;
-        double acc = 0.0;
-        for (int l = i + lane; l < m; l += 32) acc += Lc[l] * x[l];
-        acc = warp_sum(acc);
-        __syncwarp();
-        if (lane == 0) x[i] = acc;
-        __syncwarp();
-      }
-    }
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < nc * m; e += blockDim.x) {
-    const int c = e / m, i = e % m;
-    Xp[(int64_t)(c0 + c) * ldx + i] = xs[c * m + i];
-  }
-}
-
-// ---------------------------------------------------------------------------------------------
 // Batched Householder QR of the leaf panels A_j (m_j x r, column-major at start(j)*r), in place:
 // reflector vectors below the diagonal (unit leading entry implicit), tau[j*r + c], and
 // R_j (r x r column-major, zeros below the diagonal) written to Rout[j*r*r].
@@ -308,7 +228,7 @@ __global__ void __launch_bounds__(256) k_leaf_qr(double* __restrict__ Pan, int r
 // Outputs per node: Ct, L22 (lower), Eref (r x r), Etau (r), R_N into slot N.
 // Shared memory: four r x (r+1) matrices.
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, const double* __restrict__ Sc,
+__global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, const double* __restrict__ SinvT,
                                                      int r, int level, int L, int64_t nleaf,
                                                      int64_t cbase, int64_t nbase, double* __restrict__ Ct_out,
                                                      double* __restrict__ L22_out, double* __restrict__ Eref,
@@ -326,59 +246,71 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
   const double* R1 = R + (cbase + 2 * k) * (int64_t)r * r;
   const double* R2 = R + (cbase + 2 * k + 1) * (int64_t)r * r;
   const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
-  // load: X0 = Sc, X1 = R1, X2 = R2   (element (i,c) at i + c*ld)
+  // load: X0 = Sc^{-T} (upper), X1 = R1, X2 = R2   (element (i,c) at i + c*ld)
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
-    X0[i + c * ld] = Sc[e];
+    X0[i + c * ld] = SinvT[e];
     X1[i + c * ld] = R1[e];
     X2[i + c * ld] = R2[e];
   }
   __syncthreads();
-  // T = R Sc^{-T}: row i of T solves Sc t' = R[i,:]'. Rows of R1 (i < r) and R2 (r <= i < 2r)
-  // are independent; row i only has entries l >= i (upper triangular inputs).
-  for (int q = tid; q < 2 * r; q += nth) {
-    double* M = q < r ? X1 : X2;
-    const int i = q < r ? q : q - r;
-    for (int l = i; l < r; ++l) {
-      double v = M[i + l * ld];
-      for (int p = i; p < l; ++p) v -= X0[l + p * ld] * M[i + p * ld];
-      M[i + l * ld] = v / X0[l + l * ld];
-    }
-  }
-  __syncthreads();
-  // Ct = T1 T2' -> X3 ; Ct[i][c] = sum_{l >= max(i,c)} T1[i][l] T2[c][l]
+  // T1 = R1 Sc^{-T} -> X3 (upper x upper: entries l in [i, c])
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
     double acc = 0.0;
-    for (int l = max(i, c); l < r; ++l) acc += X1[i + l * ld] * X2[c + l * ld];
+    if (i <= c) {
+#pragma unroll 4
+      for (int l = i; l <= c; ++l) acc += X1[i + l * ld] * X0[l + c * ld];
+    }
     X3[i + c * ld] = acc;
   }
   __syncthreads();
-  // H = I - Ct' Ct -> X0 (lower triangle)
+  // T2 = R2 Sc^{-T} -> X1
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    double acc = 0.0;
+    if (i <= c) {
+#pragma unroll 4
+      for (int l = i; l <= c; ++l) acc += X2[i + l * ld] * X0[l + c * ld];
+    }
+    X1[i + c * ld] = acc;
+  }
+  __syncthreads();
+  // Ct = T1 T2' -> X0 ; Ct[i][c] = sum_{l >= max(i,c)} T1[i][l] T2[c][l]
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    double acc = 0.0;
+#pragma unroll 4
+    for (int l = max(i, c); l < r; ++l) acc += X3[i + l * ld] * X1[c + l * ld];
+    X0[i + c * ld] = acc;
+  }
+  __syncthreads();
+  // H = I - Ct' Ct -> X3 (lower triangle)
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
     if (i >= c) {
       double acc = 0.0;
-      for (int l = 0; l < r; ++l) acc += X3[l + i * ld] * X3[l + c * ld];
-      X0[i + c * ld] = (i == c ? 1.0 : 0.0) - acc;
+#pragma unroll 4
+      for (int l = 0; l < r; ++l) acc += X0[l + i * ld] * X0[l + c * ld];
+      X3[i + c * ld] = (i == c ? 1.0 : 0.0) - acc;
     }
   }
   __syncthreads();
   // L22 = chol(H) in place (lower)
   int bad = 0;
   for (int j = 0; j < r; ++j) {
-    const double d = X0[j + j * ld];
+    const double d = X3[j + j * ld];
     const bool ok = d > 0.0;
     if (!ok && bad == 0) bad = j + 1;
     const double sd = ok ? sqrt(d) : 1.0;
     __syncthreads();
-    for (int i = j + 1 + tid; i < r; i += nth) X0[i + j * ld] /= sd;
-    if (tid == 0) X0[j + j * ld] = sd;
+    for (int i = j + 1 + tid; i < r; i += nth) X3[i + j * ld] /= sd;
+    if (tid == 0) X3[j + j * ld] = sd;
     __syncthreads();
     const int wdt = r - j - 1;
     for (int e = tid; e < wdt * wdt; e += nth) {
       const int i = j + 1 + e % wdt, c = j + 1 + e / wdt;
-      if (i >= c) X0[i + c * ld] -= X0[i + j * ld] * X0[c + j * ld];
+      if (i >= c) X3[i + c * ld] -= X3[i + j * ld] * X3[c + j * ld];
     }
     __syncthreads();
   }
@@ -386,35 +318,37 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
   // store Ct and L22
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
-    Ct_out[node * (int64_t)r * r + e] = X3[i + c * ld];
-    L22_out[node * (int64_t)r * r + e] = (i >= c) ? X0[i + c * ld] : 0.0;
+    Ct_out[node * (int64_t)r * r + e] = X0[i + c * ld];
+    L22_out[node * (int64_t)r * r + e] = (i >= c) ? X3[i + c * ld] : 0.0;
   }
   if (level >= L) return;
-  // reload R1 -> X1, R2 -> X2
-  __syncthreads();
+  // reload R1 -> X1 (X2 still holds R2)
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
     X1[i + c * ld] = R1[e];
-    X2[i + c * ld] = R2[e];
   }
   __syncthreads();
   // B = R2 - Ct' R1 -> X2 (column c of R1 has entries l <= c)
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
     double acc = 0.0;
-    for (int l = 0; l <= c; ++l) acc += X3[l + i * ld] * X1[l + c * ld];
+#pragma unroll 4
+    for (int l = 0; l <= c; ++l) acc += X0[l + i * ld] * X1[l + c * ld];
     X2[i + c * ld] -= acc;
   }
   __syncthreads();
-  // B <- L22^{-1} B, columns independent (one thread per column)
-  for (int c = tid; c < r; c += nth) {
-    for (int i = 0; i < r; ++i) {
-      double v = X2[i + c * ld];
-      for (int p = 0; p < i; ++p) v -= X0[i + p * ld] * X2[p + c * ld];
-      X2[i + c * ld] = v / X0[i + i * ld];
+  // B <- L22^{-1} B, row by row with the whole CTA
+  for (int i = 0; i < r; ++i) {
+    const double inv = 1.0 / X3[i + i * ld];
+    for (int c = tid; c < r; c += nth) X2[i + c * ld] *= inv;
+    __syncthreads();
+    const int rows = r - i - 1;
+    for (int e = tid; e < rows * r; e += nth) {
+      const int ii = i + 1 + e % rows, c = e / rows;
+      X2[ii + c * ld] -= X3[ii + i * ld] * X2[i + c * ld];
     }
+    __syncthreads();
   }
-  __syncthreads();
   // structured Householder QR of [X1 (upper r x r) ; X2 (r x r)]:
   // reflector j acts on row j of the top and all r rows of the bottom.
   for (int j = 0; j < r; ++j) {
@@ -437,21 +371,24 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
       X1[j + j * ld] = beta;
       sh[0] = scal;
       sh[1] = tj;
+      Etau[node * (int64_t)r + j] = tj;
     }
     __syncthreads();
     const double scal = sh[0], tj = sh[1];
-    for (int i = tid; i < r; i += nth) X2[i + j * ld] *= scal;
-    if (tid == 0) Etau[node * (int64_t)r + j] = tj;
-    __syncthreads();
     if (tj != 0.0) {
+      // scaled reflector column v = X2[:, j] * scal is formed on the fly; each warp updates
+      // whole columns c > j
       for (int c = j + 1 + w; c < r; c += nw) {
-        double acc = (lane == 0) ? X1[j + c * ld] : 0.0;
+        double acc = 0.0;
         for (int i = lane; i < r; i += 32) acc += X2[i + j * ld] * X2[i + c * ld];
-        acc = warp_sum(acc) * tj;
+        acc = (warp_sum(acc) * scal + X1[j + c * ld]) * tj;
         if (lane == 0) X1[j + c * ld] -= acc;
-        for (int i = lane; i < r; i += 32) X2[i + c * ld] -= acc * X2[i + j * ld];
+        const double f = acc * scal;
+        for (int i = lane; i < r; i += 32) X2[i + c * ld] -= f * X2[i + j * ld];
       }
     }
+    __syncthreads();
+    for (int i = tid; i < r; i += nth) X2[i + j * ld] *= scal;
     __syncthreads();
   }
   double* Rn = R + (nleaf + node) * (int64_t)r * r;
@@ -459,6 +396,24 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
     const int i = e % r, c = e / r;
     Rn[e] = (i <= c) ? X1[i + c * ld] : 0.0;
     Eref[node * (int64_t)r * r + e] = X2[i + c * ld];
+  }
+}
+
+// Sc^{-T} (upper triangular) from the landmark Cholesky factor Sc (lower): one thread per
+// column of Sc^{-1} (forward substitution), one CTA.
+__global__ void k_tri_inv_t(const double* __restrict__ Sc, int r, double* __restrict__ SinvT) {
+  extern __shared__ double s[];
+  const int ld = r + 1;
+  for (int e = threadIdx.x; e < r * r; e += blockDim.x) s[(e % r) + (e / r) * ld] = Sc[e];
+  __syncthreads();
+  for (int j = threadIdx.x; j < r; j += blockDim.x) {
+    // x = Sc^{-1} e_j, rows i >= j
+    for (int i = 0; i < r; ++i) SinvT[j + i * r] = 0.0;
+    for (int i = j; i < r; ++i) {
+      double v = (i == j) ? 1.0 : 0.0;
+      for (int l = j; l < i; ++l) v -= s[i + l * ld] * SinvT[j + l * r];
+      SinvT[j + i * r] = v / s[i + i * ld];
+    }
   }
 }
 
@@ -538,18 +493,6 @@ bool launch_leaf_chol(const double* K, double* Lf, const Tree& t, int* info, cud
   return true;
 }
 
-bool launch_leaf_tri(const double* Lf, const Tree& t, int op, double* Bptr, int64_t bmul,
-                     int64_t bld, int bld_is_m, double* Xptr, int64_t xmul, int64_t xld,
-                     int xld_is_m, int ncols, cudaStream_t st) {
-  const size_t sm = (size_t)t.max_leaf * 8 * sizeof(double);
-  if (sm > 200 * 1024) return false;
-  cudaFuncSetAttribute(k_leaf_tri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  LeafOperand B{Bptr, bmul, bld, bld_is_m}, X{Xptr, xmul, xld, xld_is_m};
-  dim3 grid((unsigned)t.nleaf, (unsigned)((ncols + 7) / 8));
-  k_leaf_tri<<<grid, 256, sm, st>>>(Lf, dtree(t), op, B, X, ncols);
-  return true;
-}
-
 void launch_leaf_qr(double* Pan, int r, const Tree& t, double* tau, double* Rout, cudaStream_t st) {
   const size_t sm = (size_t)t.max_leaf * r * sizeof(double);
   if (sm <= 200 * 1024) {
@@ -560,14 +503,20 @@ void launch_leaf_qr(double* Pan, int r, const Tree& t, double* tau, double* Rout
   }
 }
 
-void launch_node_factor(double* R, const double* Sc, int r, int level, const Tree& t,
+void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st) {
+  const size_t sm = (size_t)r * (r + 1) * sizeof(double);
+  cudaFuncSetAttribute(k_tri_inv_t, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_tri_inv_t<<<1, 128, sm, st>>>(Sc, r, SinvT);
+}
+
+void launch_node_factor(double* R, const double* SinvT, int r, int level, const Tree& t,
                         double* Ct, double* L22, double* Eref, double* Etau, int* info,
                         cudaStream_t st) {
   const size_t sm = (size_t)4 * r * (r + 1) * sizeof(double);
   cudaFuncSetAttribute(k_node_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   const int64_t cbase = (level == 1) ? 0 : t.nleaf + t.node_off[level - 1];
   const int64_t nbase = t.node_off[level];
-  k_node_factor<<<(unsigned)t.nodes_at(level), 256, sm, st>>>(R, Sc, r, level, t.L, t.nleaf, cbase,
+  k_node_factor<<<(unsigned)t.nodes_at(level), 256, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase,
                                                               nbase, Ct, L22, Eref, Etau, info);
 }
 

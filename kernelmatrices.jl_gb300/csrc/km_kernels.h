@@ -5,6 +5,15 @@
 
 namespace km {
 
+// Operand of the leaf triangular kernels: leaf j's block starts at ptr + start(j) * bmul with
+// leading dimension m_j (ld_is_m) or ld.
+struct LeafOperand {
+  double* ptr;
+  int64_t bmul;
+  int64_t ld;
+  int ld_is_m;
+};
+
 struct NodeMatsH {
   const double* Ct;
   const double* L22;
@@ -30,7 +39,8 @@ bool launch_leaf_tri(const double* Lf, const Tree& t, int op, double* Bptr, int6
                      int64_t bld, int bld_is_m, double* Xptr, int64_t xmul, int64_t xld,
                      int xld_is_m, int ncols, cudaStream_t st);
 void launch_leaf_qr(double* Pan, int r, const Tree& t, double* tau, double* Rout, cudaStream_t st);
-void launch_node_factor(double* R, const double* Sc, int r, int level, const Tree& t, double* Ct,
+void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st);
+void launch_node_factor(double* R, const double* SinvT, int r, int level, const Tree& t, double* Ct,
                         double* L22, double* Eref, double* Etau, int* info, cudaStream_t st);
 void launch_logdet(const double* Lf, const Tree& t, const double* L22, int r, double* partial,
                    int np, double* out, cudaStream_t st);

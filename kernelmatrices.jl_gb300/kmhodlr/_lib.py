@@ -28,6 +28,9 @@ KM_METHOD_NYSTROM = 1
 KM_PREC_FP64 = 0
 KM_PREC_MIXED = 1
 
+PROF_CLASSES = ["eval", "leaf_chol", "leaf_tri", "leaf_qr", "node", "sweep", "leaf_refl", "leaf_apply",
+                "other", "aca"]
+
 
 class KmConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("precision", C.c_int), ("hbm_budget_fraction", C.c_double),
@@ -73,6 +76,11 @@ SIGNATURES = {
     "km_derivative_matvec": (C.c_int, [_H, C.c_int, _DP, _DP, C.c_int64]),
     "km_nll_grad": (C.c_int, [_H, _DP, _DP, C.c_int64, _DP, _DP]),
     "km_probe_fp64_tflops": (C.c_int, [C.c_int, _DP]),
+    "km_assemble_dev": (C.c_int, [_H, _P, C.c_int64, C.c_int, _DP, C.c_int, C.c_int, C.c_double, C.c_int64,
+                                  C.c_int, C.c_int64]),
+    "km_set_stream": (C.c_int, [_H, _P]),
+    "km_profile_enable": (C.c_int, [_H, C.c_int]),
+    "km_profile_get": (C.c_int, [_H, C.c_int, _DP, _IP]),
 }
 
 _lib = None
