@@ -1,0 +1,160 @@
+# KMHodlrGPU: the Julia side of the drop-in.  It binds libkmhodlr.so through `ccall` and adds
+# methods for the KernelMatrices.jl HODLR API on a GPU-resident HODLR type.
+#
+# Covered calls (reference file:line):
+#   HODLR.KernelHODLR(K, ep, maxrank, lvl; nystrom)   src/HODLR/src/constructor.jl:6-58
+#   HODLR.symmetricfactorize!(K)                      src/HODLR/src/symfact.jl:6-49
+#   mul!, *, ldiv!, \, logdet                          src/HODLR/src/baseoverloads.jl:152-263
+#   ldiv!(t, K.W, v), ldiv!(t, K.W', v), mul!(t, K.W, v) baseoverloads.jl:95-150
+#   HODLR.stoch_gradient, HODLR.negloglik             stochasticgradient.jl:30-44, maxlikfunctions.jl:2-9
+#
+# Kernels are callable structs, so the same object runs in the reference's CPU path
+# (k(x, y, p) like any kernel function) and is recognised by type here.
+module KMHodlrGPU
+
+using LinearAlgebra, StaticArrays
+import LinearAlgebra: mul!, ldiv!, logdet, adjoint
+import KernelMatrices: KernelMatrix
+import KernelMatrices.HODLR: HierLevel, FixedLevel, LogLevel, symmetricfactorize!
+
+const libkm = joinpath(@__DIR__, "..", "kmhodlr", "libkmhodlr.so")
+
+# ---- kernels ---------------------------------------------------------------------------------
+struct RatQuad end    # p1^2/(1+(r/p2)^2)^2 + p3*(x == y)          (README.md:42-48)
+struct Matern32 end   # p1*(1+sqrt3 r/p2)exp(-sqrt3 r/p2) + p3*(x == y)  (mtn_kernfun, nu = 3/2)
+
+function (::RatQuad)(x, y, p)
+  out = abs2(p[1]) / abs2(1.0 + abs2(norm(x - y) / p[2]))
+  return x == y ? out + p[3] : out
+end
+
+function (::Matern32)(x, y, p)
+  r = norm(x - y)
+  out = p[1]
+  if r > 0.0
+    z = sqrt(3.0) * r / p[2]
+    out = abs(r / p[2]) > 1.0e-8 ? p[1] * (1.0 + z) * exp(-z) : p[1]
+  end
+  return x == y ? out + p[3] : out
+end
+
+kernel_id(::RatQuad) = Cint(0)
+kernel_id(::Matern32) = Cint(1)
+
+# ---- library ---------------------------------------------------------------------------------
+struct KmConfig
+  device::Cint
+  precision::Cint
+  hbm_budget_fraction::Cdouble
+  refine_max_iter::Cint
+  refine_tol::Cdouble
+end
+
+struct PosDefGPU <: Exception
+  msg::String
+end
+
+function check(h::Ptr{Cvoid}, rc::Cint)
+  rc == 0 && return nothing
+  msg = h == C_NULL ? "libkmhodlr error $rc" : unsafe_string(ccall((:km_last_error, libkm), Cstring, (Ptr{Cvoid},), h))
+  rc == 2 && throw(PosDefException(-1))   # KM_ERR_NOT_SPD
+  error(msg)
+end
+
+mutable struct GPUKernelHODLR
+  h::Ptr{Cvoid}
+  n::Int64
+  nys::Bool
+  factorized::Bool
+end
+
+level_args(l::FixedLevel) = (Cint(0), Int64(l.lv))
+level_args(l::LogLevel) = (Cint(1), Int64(l.lv))
+
+function GPUKernelHODLR(K::KernelMatrix, ep::Float64, maxrank::Int64, lvl::HierLevel;
+                        nystrom::Bool=false, device::Int=0, precision::Int=0)
+  K.x1 == K.x2 || error("This function builds symmetric matrices.")
+  pts = Vector{SVector{2,Float64}}(K.x1)          # (x, y) pairs, contiguous
+  prm = Vector{Float64}(K.parms)
+  cfg = Ref(KmConfig(device, precision, 0.8, 0, 0.0))
+  hr = Ref{Ptr{Cvoid}}(C_NULL)
+  check(C_NULL, ccall((:km_create, libkm), Cint, (Ptr{KmConfig}, Ptr{Ptr{Cvoid}}), cfg, hr))
+  out = GPUKernelHODLR(hr[], length(pts), nystrom, false)
+  finalizer(x -> ccall((:km_destroy, libkm), Cint, (Ptr{Cvoid},), x.h), out)
+  kind, lv = level_args(lvl)
+  check(out.h, ccall((:km_assemble, libkm), Cint,
+                     (Ptr{Cvoid}, Ptr{SVector{2,Float64}}, Int64, Cint, Ptr{Float64}, Cint, Cint, Cdouble,
+                      Int64, Cint, Int64),
+                     out.h, pts, length(pts), kernel_id(K.kernel), prm, length(prm), nystrom ? 1 : 0, ep,
+                     maxrank, kind, lv))
+  return out
+end
+
+function symmetricfactorize!(K::GPUKernelHODLR; plel::Bool=false, verbose::Bool=false)
+  check(K.h, ccall((:km_factorize, libkm), Cint, (Ptr{Cvoid},), K.h))
+  K.factorized = true
+  return nothing
+end
+
+function mul!(target::StridedVecOrMat{Float64}, K::GPUKernelHODLR, src::StridedVecOrMat{Float64})
+  check(K.h, ccall((:km_matvec, libkm), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64),
+                   K.h, src, target, size(src, 2)))
+  return target
+end
+
+function ldiv!(target::StridedVecOrMat{Float64}, K::GPUKernelHODLR, src::StridedVecOrMat{Float64})
+  check(K.h, ccall((:km_solve, libkm), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64),
+                   K.h, src, target, size(src, 2)))
+  return target
+end
+
+Base.:*(K::GPUKernelHODLR, x::VecOrMat{Float64}) = mul!(similar(x), K, x)
+Base.:\(K::GPUKernelHODLR, x::VecOrMat{Float64}) = ldiv!(similar(x), K, x)
+
+function logdet(K::GPUKernelHODLR)
+  out = Ref{Cdouble}(0.0)
+  check(K.h, ccall((:km_logdet, libkm), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), K.h, out))
+  return out[]
+end
+
+# K.W and K.W' (FactorHODLR products and solves, baseoverloads.jl:95-150)
+struct GPUFactor
+  K::GPUKernelHODLR
+  t::Bool
+end
+Base.getproperty(K::GPUKernelHODLR, s::Symbol) = s === :W ? GPUFactor(K, false) : getfield(K, s)
+adjoint(W::GPUFactor) = GPUFactor(W.K, !W.t)
+
+function ldiv!(target::StridedVecOrMat{Float64}, W::GPUFactor, src::StridedVecOrMat{Float64})
+  check(W.K.h, ccall((:km_factor_solve, libkm), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Int64),
+                     W.K.h, W.t, src, target, size(src, 2)))
+  return target
+end
+
+function mul!(target::StridedVecOrMat{Float64}, W::GPUFactor, src::StridedVecOrMat{Float64})
+  check(W.K.h, ccall((:km_factor_mul, libkm), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Int64),
+                     W.K.h, W.t, src, target, size(src, 2)))
+  return target
+end
+
+# negloglik (maxlikfunctions.jl:2-9) and stoch_gradient (stochasticgradient.jl:30-44): the
+# derivative functions are the kernel's own parameter derivatives, so `dfuns` is not needed.
+function negloglik(K::GPUKernelHODLR, dat::Vector{Float64})
+  nll = Ref{Cdouble}(0.0)
+  check(K.h, ccall((:km_nll_grad, libkm), Cint,
+                   (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Cdouble}, Ptr{Cdouble}),
+                   K.h, dat, C_NULL, 0, nll, C_NULL))
+  return nll[]
+end
+
+function stoch_gradient(K::GPUKernelHODLR, dat::Vector{Float64}, vecs::Vector{Vector{Float64}})
+  probes = reduce(hcat, vecs)
+  nll = Ref{Cdouble}(0.0)
+  grad = zeros(3)
+  check(K.h, ccall((:km_nll_grad, libkm), Cint,
+                   (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Cdouble}, Ptr{Cdouble}),
+                   K.h, dat, probes, size(probes, 2), nll, grad))
+  return grad
+end
+
+end # module
