@@ -1,6 +1,7 @@
 // C ABI of libkmhodlr: handle lifecycle, partition, and the orchestration of the device kernels.
 // Each entry point mirrors one reference call (cited in include/kmhodlr.h).
 #include <algorithm>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -778,3 +779,67 @@ int km_nll_grad(km_handle* h, const double*, const double*, int64_t, double*, do
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free solve (declared in include/kmhodlr.h).  The workspace is a fixed file-scope
+// device array; host code obtains its device address once per device with cudaGetSymbolAddress
+// (the host-side symbol itself is not a device address and must never be passed to a kernel).
+// ---------------------------------------------------------------------------------------------
+static constexpr size_t kNoAllocDoubles = KM_NOALLOC_SCRATCH_BYTES / sizeof(double);
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_dev[kMaxDevices] = {};
+}  // namespace
+
+extern "C" int km_solve_noalloc(km_handle* h, const double* d_b, double* d_x, int64_t k) {
+  if (!h || !d_b || !d_x || k < 1) return fail(h, KM_ERR_BAD_ARG, "bad solve arguments");
+  const int dev = h->cfg.device;
+  if (dev < 0 || dev >= kMaxDevices) return fail(h, KM_ERR_BAD_ARG, "device ordinal out of range");
+  KM_CUDA(h, cudaSetDevice(dev));
+  if (!h->factorized) return fail(h, KM_ERR_STATE, "No solves without factorization.");
+  const Tree& t = h->tree;
+  const int64_t slots = t.nleaf + t.nnode;
+  const int64_t vp = slots * h->r * k;
+  const int64_t need = 2 * vp + std::max<int64_t>(t.nnode, 1) * 2 * h->r * k;
+  if (need > (int64_t)kNoAllocDoubles) {
+    char buf[256];
+    snprintf(buf, sizeof buf,
+             "km_solve_noalloc: %lld columns need %lld bytes of workspace but the fixed array holds "
+             "%u bytes; pass fewer columns per call",
+             (long long)k, (long long)(need * sizeof(double)), (unsigned)KM_NOALLOC_SCRATCH_BYTES);
+    return fail(h, KM_ERR_BAD_ARG, buf);
+  }
+  double* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_dev[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) return cuda_fail(h, e == cudaSuccess ? cudaErrorUnknown : e, "cudaGetSymbolAddress");
+      g_noalloc_dev[dev] = (double*)p;
+    }
+    base = g_noalloc_dev[dev];
+  }
+  // run the ordinary solve sweeps on the fixed workspace; the handle's own workspace is untouched
+  double* const sv[3] = {h->d_VP, h->d_VG, h->d_VD};
+  const bool prof = h->prof;
+  h->prof = false;  // the profiler creates events on demand
+  h->d_VP = base;
+  h->d_VG = base + vp;
+  h->d_VD = base + 2 * vp;
+  int rc = KM_OK;
+  if (d_x != d_b) {
+    cudaError_t e = cudaMemcpyAsync(d_x, d_b, sizeof(double) * t.n * k, cudaMemcpyDeviceToDevice, h->stream);
+    if (e != cudaSuccess) rc = cuda_fail(h, e, "cudaMemcpyAsync");
+  }
+  if (rc == KM_OK) rc = nested_fwd(h, d_x, (int)k);
+  if (rc == KM_OK) rc = nested_bwd(h, d_x, (int)k);
+  h->d_VP = sv[0];
+  h->d_VG = sv[1];
+  h->d_VD = sv[2];
+  h->prof = prof;
+  if (rc != KM_OK) return rc;
+  return sync(h, "solve_noalloc");
+}

@@ -81,6 +81,7 @@ SIGNATURES = {
     "km_set_stream": (C.c_int, [_H, _P]),
     "km_profile_enable": (C.c_int, [_H, C.c_int]),
     "km_profile_get": (C.c_int, [_H, C.c_int, _DP, _IP]),
+    "km_solve_noalloc": (C.c_int, [_H, _P, _P, C.c_int64]),
 }
 
 _lib = None
