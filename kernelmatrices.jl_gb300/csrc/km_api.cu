@@ -103,6 +103,18 @@ struct km_handle {
   double* d_X = nullptr;
   double* d_Y = nullptr;
   int64_t xcap = 0;
+  // derivative HODLR (evaluated for one parameter at a time) and gradient workspaces
+  int dk_param = -1;
+  double* d_dK = nullptr;
+  double* d_dPhi = nullptr;
+  double* d_Sj = nullptr;
+  double* d_GP = nullptr;
+  double* d_GG = nullptr;
+  int64_t gcap = 0;
+  double* d_T = nullptr;
+  double* d_U = nullptr;
+  double* d_dots = nullptr;
+  int64_t tcap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaStream_t own_stream = nullptr;  // the handle's own stream (h->stream may be external)
   // profiler
@@ -186,6 +198,9 @@ void free_problem(km_handle* h) {
   h->vcap = 0;
   h->d_X = h->d_Y = nullptr;
   h->xcap = 0;
+  h->dk_param = -1;
+  h->d_dK = h->d_dPhi = h->d_Sj = h->d_GP = h->d_GG = h->d_T = h->d_U = h->d_dots = nullptr;
+  h->gcap = h->tcap = 0;
   h->assembled = h->factorized = false;
 }
 
@@ -372,6 +387,48 @@ int check_info(km_handle* h, int64_t count, const char* what) {
   return KM_OK;
 }
 
+// Y = dK_j X for the exact derivative of the Nystrom HODLR in parameter j (device pointers).
+int derivative_apply(km_handle* h, int j, const double* X, double* Y, int k) {
+  const Tree& t = h->tree;
+  const int r = h->r;
+  cudaStream_t st = h->stream;
+  int rc;
+  if (!h->d_dK) {
+    int64_t kbytes = 0;
+    for (int64_t q = 0; q < t.nleaf; ++q) kbytes += t.leaf_size(q) * t.leaf_size(q);
+    if ((rc = dalloc(h, &h->d_dK, kbytes)) || (rc = dalloc(h, &h->d_dPhi, t.n * r)) ||
+        (rc = dalloc(h, &h->d_Sj, r * r)))
+      return rc;
+  }
+  if (k > h->gcap) {
+    dfree(h, h->d_GP);
+    dfree(h, h->d_GG);
+    h->d_GP = h->d_GG = nullptr;
+    h->gcap = 0;
+    const int64_t slots = t.nleaf + t.nnode;
+    if ((rc = dalloc(h, &h->d_GP, slots * 2 * r * k)) || (rc = dalloc(h, &h->d_GG, slots * 2 * r * k))) return rc;
+    h->gcap = k;
+  }
+  if (h->dk_param != j) {
+    // DerivativeHODLR (constructor.jl:66-95): dK leaves, dK(X, P) and Sj = dK(P, P)
+    KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, j, h->d_dK, st));
+    KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, j, h->d_dPhi, st));
+    KLV(h, KM_PROF_EVAL, launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, j, h->d_Sj, r, st));
+    h->dk_param = j;
+  }
+  NodeMatsH nm2{nullptr, nullptr, nullptr, nullptr, 2 * r};
+  if (t.L > 0) {
+    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dphiT(h->d_Phi, h->d_dPhi, r, t, X, t.n, h->d_GP, k, st));
+    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm2, l, h->d_GP, nullptr, k, UP_SUM_, st));
+    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm2, l, h->d_GP, h->d_GG, nullptr, k, DN_NYS_, st));
+  } else {
+    KM_CUDA(h, cudaMemsetAsync(h->d_GG, 0, sizeof(double) * 2 * r * k, st));
+  }
+  KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dnys_apply(h->d_dK, h->d_Phi, h->d_dPhi, h->d_Sc, h->d_Sj, r, t, X, t.n,
+                                                    h->d_GG, Y, t.n, k, st));
+  return check_launch(h, "derivative");
+}
+
 bool finite3(const double* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
 
 }  // namespace
@@ -552,6 +609,7 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   h->maxrank = maxrank;
   h->r = (int)maxrank;
   h->assembled = h->factorized = false;
+  h->dk_param = -1;
   const int r = h->r;
   int64_t kbytes = 0;
   for (int64_t j = 0; j < t.nleaf; ++j) kbytes += t.leaf_size(j) * t.leaf_size(j);
@@ -770,12 +828,80 @@ int km_block_factors(km_handle* h, int64_t, double*, double*) {
   return fail(h, KM_ERR_UNSUPPORTED, "block factor export is not built yet");
 }
 
-int km_derivative_matvec(km_handle* h, int, const double*, double*, int64_t) {
-  return fail(h, KM_ERR_UNSUPPORTED, "derivative products are not built yet");
+int km_derivative_matvec(km_handle* h, int param, const double* x, double* y, int64_t k) {
+  if (!h || !x || !y || k < 1 || param < 0 || param > 2) return fail(h, KM_ERR_BAD_ARG, "bad derivative arguments");
+  cudaSetDevice(h->cfg.device);
+  if (!h->assembled) return fail(h, KM_ERR_STATE, "assemble first");
+  if (h->method != KM_METHOD_NYSTROM) return fail(h, KM_ERR_STATE, "This is only valid for Nystrom-block matrices.");
+  int rc;
+  if ((rc = ensure_xy(h, k)) != KM_OK) return rc;
+  const size_t bytes = sizeof(double) * h->tree.n * k;
+  KM_CUDA(h, cudaMemcpyAsync(h->d_X, x, bytes, cudaMemcpyHostToDevice, h->stream));
+  if ((rc = derivative_apply(h, param, h->d_X, h->d_Y, (int)k)) != KM_OK) return rc;
+  KM_CUDA(h, cudaMemcpyAsync(y, h->d_Y, bytes, cudaMemcpyDeviceToHost, h->stream));
+  return sync(h, "derivative_matvec");
 }
 
-int km_nll_grad(km_handle* h, const double*, const double*, int64_t, double*, double*) {
-  return fail(h, KM_ERR_UNSUPPORTED, "likelihood gradient is not built yet");
+// negloglik (maxlikfunctions.jl:2-9) and stoch_gradient (stochasticgradient.jl:30-44):
+//   alpha = K^{-1} y,  nll = 0.5 logdet K + 0.5 y' alpha,
+//   T = W'^{-1} V (one factor solve for all probes, shared by the three parameters),
+//   g_j = 0.5 (mean_v t_v' dK_j t_v - alpha' dK_j alpha).
+// The data term y' K^{-1} dK_j K^{-1} y of HODLR_grad_term (stochasticgradient.jl:22-25) is
+// evaluated as alpha' dK_j alpha, which is the same quantity since K^{-1} is symmetric.
+int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t nprobe, double* nll,
+                double* grad) {
+  if (!h || !y || !nll || nprobe < 0 || (grad && (nprobe < 1 || !probes)))
+    return fail(h, KM_ERR_BAD_ARG, "bad likelihood arguments");
+  cudaSetDevice(h->cfg.device);
+  if (!h->factorized) return fail(h, KM_ERR_STATE, "The HODLR matrix needs to be factorized for this.");
+  if (grad && h->method != KM_METHOD_NYSTROM) return fail(h, KM_ERR_STATE, "This is only valid for Nystrom-block matrices.");
+  const Tree& t = h->tree;
+  const int64_t n = t.n;
+  const int64_t p = grad ? nprobe : 0;
+  const int64_t kk = p + 1;
+  int rc;
+  timer_start(h);
+  if (kk > h->tcap) {
+    dfree(h, h->d_T);
+    dfree(h, h->d_U);
+    dfree(h, h->d_dots);
+    h->d_T = h->d_U = h->d_dots = nullptr;
+    h->tcap = 0;
+    if ((rc = dalloc(h, &h->d_T, n * kk)) || (rc = dalloc(h, &h->d_U, n * kk)) || (rc = dalloc(h, &h->d_dots, kk)))
+      return rc;
+    h->tcap = kk;
+  }
+  if ((rc = ensure_vec(h, kk)) != KM_OK) return rc;
+  cudaStream_t st = h->stream;
+  double* alpha = h->d_T + n * p;  // last column
+  KM_CUDA(h, cudaMemcpyAsync(alpha, y, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+  if ((rc = nested_fwd(h, alpha, 1)) != KM_OK) return rc;
+  if ((rc = nested_bwd(h, alpha, 1)) != KM_OK) return rc;
+  double ld = 0.0;
+  KLV(h, KM_PROF_OTHER, launch_logdet(h->d_Lf, t, h->d_L22, h->r, h->d_partial, kLogdetBlocks, h->d_scalar, st));
+  KM_CUDA(h, cudaMemcpyAsync(&ld, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st));
+  std::vector<double> a(n);
+  KM_CUDA(h, cudaMemcpyAsync(a.data(), alpha, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  if ((rc = sync(h, "nll")) != KM_OK) return rc;
+  double ya = 0.0;
+  for (int64_t i = 0; i < n; ++i) ya += y[i] * a[i];
+  *nll = 0.5 * ld + 0.5 * ya;
+  if (grad) {
+    KM_CUDA(h, cudaMemcpyAsync(h->d_T, probes, sizeof(double) * n * p, cudaMemcpyHostToDevice, st));
+    if ((rc = nested_bwd(h, h->d_T, (int)p)) != KM_OK) return rc;  // T = W'^{-1} V
+    std::vector<double> dots(kk);
+    for (int j = 0; j < 3; ++j) {
+      if ((rc = derivative_apply(h, j, h->d_T, h->d_U, (int)kk)) != KM_OK) return rc;
+      KLV(h, KM_PROF_OTHER, launch_col_dots(h->d_T, n, h->d_U, n, n, (int)kk, h->d_dots, st));
+      KM_CUDA(h, cudaMemcpyAsync(dots.data(), h->d_dots, sizeof(double) * kk, cudaMemcpyDeviceToHost, st));
+      if ((rc = sync(h, "grad")) != KM_OK) return rc;
+      double tr = 0.0;
+      for (int64_t c = 0; c < p; ++c) tr += dots[c];
+      grad[j] = 0.5 * (tr / (double)p - dots[p]);
+    }
+  }
+  h->stats.grad_ms = timer_stop(h);
+  return sync(h, "nll_grad");
 }
 
 }  // extern "C"

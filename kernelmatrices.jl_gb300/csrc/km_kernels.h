@@ -63,4 +63,13 @@ void launch_leaf_nys_apply(const double* Kl, const double* Phi, const double* Sc
                            const Tree& t, const double* X, int64_t ldx, const double* VG,
                            double* Y, int64_t ldy, int k, cudaStream_t st);
 
+// derivative HODLR and gradient pieces
+void launch_leaf_dphiT(const double* Phi, const double* dPhi, int r, const Tree& t, const double* X,
+                       int64_t ldx, double* VP, int k, cudaStream_t st);
+void launch_leaf_dnys_apply(const double* dKl, const double* Phi, const double* dPhi, const double* Sc,
+                            const double* Sj, int r, const Tree& t, const double* X, int64_t ldx,
+                            const double* VG, double* Y, int64_t ldy, int k, cudaStream_t st);
+void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n, int k,
+                     double* out, cudaStream_t st);
+
 }  // namespace km

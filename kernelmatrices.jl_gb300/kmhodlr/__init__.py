@@ -7,4 +7,5 @@ from ._lib import load, LIB_PATH  # noqa: F401
 from .hodlr import (  # noqa: F401
     FixedLevel, LogLevel, KernelMatrix, KernelHODLR, RatQuad, Matern32, HODLRindices,
     KMError, PosDefException, symmetricfactorize, logdet, nystrom_landmarks, probe_fp64_tflops,
+    negloglik, stoch_gradient, nll_objective,
 )

@@ -241,6 +241,31 @@ class KernelHODLR:
         _check(self._h, L.load().km_logdet(self._h, C.byref(out)))
         return out.value
 
+    def derivative_matvec(self, param: int, x: np.ndarray) -> np.ndarray:
+        """``DerivativeHODLR(K, dfun, HK) * x`` for the derivative in parameter ``param``
+        (0 scale, 1 range, 2 nugget) (constructor.jl:66-95, baseoverloads.jl:216-234)."""
+        lib = L.load()
+        vec = np.asarray(x, dtype=np.float64)
+        b = np.asfortranarray(vec.reshape(self.n, -1))
+        out = np.empty_like(b, order="F")
+        _check(self._h, lib.km_derivative_matvec(self._h, int(param), _dp(b), _dp(out), b.shape[1]))
+        return out.reshape(vec.shape)
+
+    def nll_grad(self, dat: np.ndarray, vecs=None):
+        """(NLL, stochastic gradient or None): ``negloglik`` (maxlikfunctions.jl:2-9) and
+        ``stoch_gradient`` with shuffle = false (stochasticgradient.jl:30-44)."""
+        lib = L.load()
+        y = np.ascontiguousarray(dat, dtype=np.float64).reshape(-1)
+        nll = C.c_double()
+        if vecs is None:
+            _check(self._h, lib.km_nll_grad(self._h, _dp(y), None, 0, C.byref(nll), None))
+            return nll.value, None
+        V = np.asfortranarray(np.column_stack(vecs) if isinstance(vecs, (list, tuple)) else vecs,
+                              dtype=np.float64)
+        g = np.zeros(3)
+        _check(self._h, lib.km_nll_grad(self._h, _dp(y), _dp(V), V.shape[1], C.byref(nll), _dp(g)))
+        return nll.value, g
+
 
 def symmetricfactorize(K: KernelHODLR) -> None:
     """``symmetricfactorize!`` (src/HODLR/src/symfact.jl:6-49)."""
@@ -250,6 +275,36 @@ def symmetricfactorize(K: KernelHODLR) -> None:
 
 def logdet(K: KernelHODLR) -> float:
     return K.logdet()
+
+
+def negloglik(HK: KernelHODLR, dat: np.ndarray) -> float:
+    """``negloglik(HK, dat)`` (src/HODLR/src/maxlikfunctions.jl:2-9)."""
+    if not HK.factorized:
+        raise KMError(L.KM_ERR_STATE, "The HODLR matrix needs to be factorized for this.")
+    return HK.nll_grad(dat)[0]
+
+
+def stoch_gradient(HK: KernelHODLR, dat: np.ndarray, vecs) -> np.ndarray:
+    """``stoch_gradient(K, HK, dat, dfuns, vecs)`` (stochasticgradient.jl:30-44) for the three
+    kernel parameters; the derivative functions are the kernel's own."""
+    if not HK.factorized:
+        raise KMError(L.KM_ERR_STATE, "The matrix needs to be factorized for this to work.")
+    return HK.nll_grad(dat, vecs)[1]
+
+
+def nll_objective(prms, grad, pts: np.ndarray, dat: np.ndarray, kernel, rank: int, lvl, saav,
+                  device: int = 0) -> float:
+    """``nll_objective(prms, grad, data, opts)`` (maxlikfunctions.jl:29-50): Nystrom assembly with
+    ep = 0, factorisation, NLL, and the stochastic gradient written into ``grad`` when it has
+    entries."""
+    K = KernelMatrix(pts, pts, prms, kernel)
+    HK = KernelHODLR(K, 0.0, rank, lvl, nystrom=True, sorted=True, device=device)
+    symmetricfactorize(HK)
+    if grad is not None and len(grad) > 0:
+        nll, g = HK.nll_grad(dat, saav)
+        grad[:] = g
+        return nll
+    return HK.nll_grad(dat)[0]
 
 
 def probe_fp64_tflops(device: int = 0) -> float:

@@ -1,0 +1,133 @@
+"""The CPU oracle against what pins it: the reference's own test identities
+(test/runtests.jl:28-45), the dense formulas of src/HODLR/src/exactmaxlik.jl, the Bessel form of
+the Matern covariance, and the committed golden fixtures.  CPU only."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+import scipy.linalg as sla
+
+from oracle import hodlr_oracle as O
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def kd(pts):
+    from kmhodlr.data import kd_order
+    return pts[kd_order(pts)]
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def basic():
+    """example/basicexample.jl-like fixture: points on [0,10]^2, k-d ordered, RQ kernel with a
+    1e-12 nugget, Nystrom rank 72, LogLevel(8), tol eps (test/runtests.jl:15-22)."""
+    rng = np.random.default_rng(2)
+    pts = kd(rng.uniform(size=(1024, 2)) * 10.0)
+    K = O.KernelMatrix(pts, pts, np.array([3.0, 0.5, 1e-12]), O.KERNEL_RQ)
+    HK = O.build_hodlr(K, np.finfo(float).eps, 72, O.LogLevel(8), nystrom=True)
+    HKf = O.hodlr_full(HK)
+    O.symmetricfactorize(HK)
+    return K, HK, HKf
+
+
+def test_runtests_identities(basic):
+    K, HK, HKf = basic
+    W = O.factor_full(HK.W)
+    tvec = np.random.default_rng(3).standard_normal(HKf.shape[0])
+    assert np.allclose(W @ W.T, HKf, rtol=1.5e-8, atol=1e-12 * np.abs(HKf).max())     # :28
+    assert np.isclose(np.linalg.slogdet(HKf)[1], O.hodlr_logdet(HK), rtol=1e-5)     # :31
+    assert np.allclose(HKf @ tvec, O.hodlr_mul(HK, tvec), rtol=1.5e-8)               # :34
+    assert rel(O.hodlr_ldiv(HK, tvec), np.linalg.solve(HKf, tvec)) < 1e-8             # :37
+    t1 = O.factor_ldiv(HK.W, tvec)
+    assert rel(t1, np.linalg.solve(W, tvec)) < 1e-8                                   # :40-41
+    t2 = O.factor_ldiv_t(HK.W, t1)
+    assert rel(t2, np.linalg.solve(W.T, t1)) < 1e-8                                   # :44-45
+
+
+def test_aca_runtests_identities_and_dense():
+    """C1-like ACA case: N(0,1) points, README RQ kernel p=[1,1] + 1.0 diagonal, tol 1e-12."""
+    rng = np.random.default_rng(4)
+    pts = rng.standard_normal((512, 2))
+    K = O.KernelMatrix(pts, pts, np.array([1.0, 1.0, 1.0]), O.KERNEL_RQ)
+    HK = O.build_hodlr(K, 1e-12, 0, O.LogLevel(7), nystrom=False)
+    HKf = O.hodlr_full(HK)
+    Kd = K.full()
+    assert np.abs(HKf - Kd).max() < 1e-9 * np.abs(Kd).max()      # ACA at 1e-12 reproduces K
+    O.symmetricfactorize(HK)
+    b = rng.standard_normal(512)
+    assert abs(O.hodlr_logdet(HK) - np.linalg.slogdet(Kd)[1]) < 1e-8
+    assert rel(O.hodlr_ldiv(HK, b), np.linalg.solve(Kd, b)) < 1e-8
+
+
+def test_aca_pivot_rules():
+    # restrictedmaxabs: first strict maximum of |x| outside the excluded set (src/utils.jl:2-15)
+    x = np.array([1.0, -3.0, 3.0, 2.0])
+    assert O.restrictedmaxabs(x, set()) == (-3.0, 1)
+    assert O.restrictedmaxabs(x, {1}) == (3.0, 2)
+    assert O.restrictedmaxabs(np.zeros(3), {0}) == (0.0, 1)
+    # a rank-1 matrix is recovered exactly with one pivot
+    rng = np.random.default_rng(5)
+    pts = rng.standard_normal((40, 2))
+    K = O.KernelMatrix(pts[:20], pts[20:], np.array([1.0, 1e6, 0.0]), O.KERNEL_RQ)
+    U, V, rows, cols = O.ACA(K, 1e-12, 0)
+    assert np.allclose(U @ V.T, K.full(), rtol=1e-10)
+
+
+def test_matern_closed_form_matches_bessel():
+    x = np.concatenate([np.linspace(1e-7, 5, 400), [1e-9, 0.0, 20.0]])
+    assert np.allclose(O.mtn_cor(1.5, x), O.mtn_cor_general(1.5, x), rtol=1e-13, atol=1e-300)
+
+
+def test_matern_derivatives_by_finite_differences():
+    rng = np.random.default_rng(6)
+    a, b = rng.uniform(size=(5, 2)), rng.uniform(size=(7, 2))
+    p = np.array([1.3, 0.2, 1e-3])
+    for kid in (O.KERNEL_MATERN32, O.KERNEL_RQ):
+        for j in range(2):
+            h = 1e-6 * p[j]
+            pp, pm = p.copy(), p.copy()
+            pp[j] += h
+            pm[j] -= h
+            fd = (O.kernel_block(kid, a, b, pp) - O.kernel_block(kid, a, b, pm)) / (2 * h)
+            assert np.allclose(O.dkernel_block(kid, j, a, b, p), fd, rtol=1e-6, atol=1e-9)
+
+
+def test_nll_and_gradient_against_dense():
+    rng = np.random.default_rng(7)
+    n = 1024
+    pts = kd(rng.uniform(size=(n, 2)))
+    p = np.array([1.0, 0.1, 1e-3])
+    K = O.KernelMatrix(pts, pts, p, O.KERNEL_MATERN32)
+    y = rng.standard_normal(n)
+    HK = O.build_hodlr(K, 0.0, 64, O.FixedLevel(2), nystrom=True)
+    HKf = O.hodlr_full(HK)
+    O.symmetricfactorize(HK)
+    nll = O.negloglik(HK, y)
+    F = sla.cho_factor(HKf)
+    nll_dense_hodlr = np.sum(np.log(np.diag(F[0]))) + 0.5 * y @ sla.cho_solve(F, y)
+    assert abs(nll - nll_dense_hodlr) < 1e-7 * abs(nll)
+    # stochastic gradient with many probes approaches the exact gradient of the HODLR NLL
+    g_exact = O.hodlr_exact_gradient(K, 64, O.FixedLevel(2), y, 3)
+    vecs = O.givesaa(200, n, 11)
+    g = O.stoch_gradient(K, HK, y, 3, vecs)
+    assert np.all(np.abs(g - g_exact) < 0.05 * np.abs(g_exact) + 5.0)
+    # the derivative matvec equals the dense derivative of the Nystrom HODLR
+    for j in range(3):
+        DK = O.derivative_hodlr(K, j, HK)
+        assert np.allclose(O.derivative_mul(DK, y), O.derivative_full(DK) @ y, rtol=1e-10, atol=1e-10)
+
+
+@pytest.mark.parametrize("case", ["nys_matern_2048", "nys_rq_1500"])
+def test_golden_fixtures_reproduce(case):
+    d = np.load(GOLD / f"{case}.npz")
+    lvl = O.FixedLevel(int(d["level"])) if int(d["level_kind"]) == 0 else O.LogLevel(int(d["level"]))
+    K = O.KernelMatrix(d["pts"], d["pts"], d["params"], int(d["kid"]))
+    HK = O.build_hodlr(K, 0.0, int(d["rank"]), lvl, nystrom=True)
+    assert rel(O.hodlr_mul(HK, d["rhs"]), d["matvec"]) < 1e-14
+    O.symmetricfactorize(HK)
+    assert abs(O.hodlr_logdet(HK) - float(d["logdet"])) < 1e-9
+    assert rel(O.hodlr_ldiv(HK, d["rhs"]), d["solve"]) < 1e-12
