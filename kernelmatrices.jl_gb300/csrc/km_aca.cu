@@ -1,0 +1,599 @@
+// ACA assembly and the general (per-block basis) HODLR factorisation used for ACA blocks.
+//
+// ACA: one CTA per off-diagonal block runs the partially pivoted adaptive cross approximation of
+// the reference (src/factorizations.jl:9-84) step for step: the start-row search, the pivot
+// rule of restrictedmaxabs (src/utils.jl:2-15: first strict maximum of |x| outside the used set,
+// the first unused index when nothing is non-zero), residual updates as a multiply followed by a
+// subtract (Julia's `tmprow .-= U[j][mi]*V[j]` is not fused), the Frobenius-norm estimate update
+// and the stopping rule norm(row)*norm(col) > rtol*sqrt(znorm2).  Kernel rows and columns are
+// evaluated on the fly; U and V are written into per-block panels (column-major).
+//
+// General factorisation (src/HODLR/src/symfact.jl:6-49 without the Nystrom nesting): leaf
+// Cholesky, leaf triangular solves of every panel, then per level the Householder QR of the
+// node's V (rows c1) and U (rows c2) panels with explicit Q, C = R1 R2', L22 = chol(I - C'C),
+// and the application of W_N^{-1} to the coarser panels.  In the QR bases W_N^{-1} only changes
+// the c2 rows:  y_c2 -= Q2 (z2 - L22^{-1}(z2 - C' z1)),  z1 = Q1' y_c1, z2 = Q2' y_c2.
+#include <climits>
+
+#include "km_kernels.h"
+
+namespace km {
+
+// ---------------------------------------------------------------------------------------------
+// CTA-wide reductions (deterministic order)
+// ---------------------------------------------------------------------------------------------
+__device__ double cta_sum(double v, double* sred) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) sred[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double t = (lane < nw) ? sred[lane] : 0.0;
+    t = warp_sum(t);
+    if (lane == 0) sred[32] = t;
+  }
+  __syncthreads();
+  const double t = sred[32];
+  __syncthreads();
+  return t;
+}
+
+// restrictedmaxabs over x[0..n) with excluded flags: returns (value, index).
+__device__ void cta_restricted_argmax(const double* x, const uint8_t* excl, int64_t n, double* sval,
+                                     long long* sidx, double* out_val, int64_t* out_idx) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double best = 0.0;
+  long long bi = LLONG_MAX, first = LLONG_MAX;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    if (excl[i]) continue;
+    if (first == LLONG_MAX) first = i;
+    const double a = fabs(x[i]);
+    if (a > best) {
+      best = a;
+      bi = i;
+    }
+  }
+  // reduce: larger |x| wins, ties go to the smaller index; first = min over threads
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const long long oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    const long long of = __shfl_xor_sync(0xffffffffu, first, o);
+    if (ob > best || (ob == best && oi < bi)) {
+      best = ob;
+      bi = oi;
+    }
+    first = min(first, of);
+  }
+  if (lane == 0) {
+    sval[w] = best;
+    sidx[w] = bi;
+    sidx[32 + w] = first;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    long long ib = LLONG_MAX, f = LLONG_MAX;
+    for (int q = 0; q < nw; ++q) {
+      if (sval[q] > b || (sval[q] == b && sidx[q] < ib)) {
+        b = sval[q];
+        ib = sidx[q];
+      }
+      f = min(f, sidx[32 + q]);
+    }
+    if (b > 0.0) {
+      sval[32] = x[ib];
+      sidx[64] = ib;
+    } else {
+      sval[32] = 0.0;
+      sidx[64] = (f == LLONG_MAX) ? n - 1 : f;
+    }
+  }
+  __syncthreads();
+  *out_val = sval[32];
+  *out_idx = sidx[64];
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------------------------
+// ACA, one CTA (1024 threads) per block.  status: 0 ok, 1 "Incompatible maxrank or matrix
+// dimensions." (factorizations.jl:30), 2 rank capacity of the panel reached before convergence.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_aca(const double* __restrict__ pts, KParams kp,
+                                              const AcaBlock* __restrict__ blocks, double* __restrict__ P,
+                                              uint8_t* __restrict__ F, int* __restrict__ piv, double rtol,
+                                              int* __restrict__ rank_out, int* __restrict__ status) {
+  extern __shared__ double dsm[];  // 2 * cap: dots with previous columns
+  __shared__ double sred[40];
+  __shared__ double sval[40];
+  __shared__ long long sidx[72];
+  const AcaBlock B = blocks[blockIdx.x];
+  const int64_t nro = B.nro, ncl = B.ncl;
+  double* U = P + B.offU;
+  double* V = P + B.offV;
+  uint8_t* urow = F + B.offFlag;
+  uint8_t* ucol = urow + nro;
+  int* prow = piv + 2 * B.offPiv;
+  int* pcol = prow + B.cap;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+  const double* xr = pts + 2 * B.row0;
+  const double* xc = pts + 2 * B.col0;
+  for (int64_t i = tid; i < nro; i += blockDim.x) urow[i] = 0;
+  for (int64_t i = tid; i < ncl; i += blockDim.x) ucol[i] = 0;
+  const int maxsz = B.maxsz;
+  auto eval_row = [&](int64_t i, double* out) {
+    const double px = xr[2 * i], py = xr[2 * i + 1];
+    for (int64_t c = tid; c < ncl; c += blockDim.x) out[c] = kernel_value(kp, px, py, xc[2 * c], xc[2 * c + 1]);
+  };
+  auto eval_col = [&](int64_t j, double* out) {
+    const double px = xc[2 * j], py = xc[2 * j + 1];
+    for (int64_t i = tid; i < nro; i += blockDim.x) out[i] = kernel_value(kp, xr[2 * i], xr[2 * i + 1], px, py);
+  };
+  auto sumsq = [&](const double* x, int64_t n) {
+    double a = 0.0;
+    for (int64_t i = tid; i < n; i += blockDim.x) a += x[i] * x[i];
+    return cta_sum(a, sred);
+  };
+  // first row (factorizations.jl:24-30)
+  int64_t strt = 0;
+  eval_row(strt, V);
+  __syncthreads();
+  {
+    double mx = 0.0;
+    for (int64_t c = tid; c < ncl; c += blockDim.x) mx = fmax(mx, fabs(V[c]));
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) sred[w] = mx;
+    __syncthreads();
+    if (tid == 0) {
+      double m = 0.0;
+      for (int q = 0; q < nw; ++q) m = fmax(m, sred[q]);
+      sred[34] = m;
+    }
+    __syncthreads();
+    mx = sred[34];
+    __syncthreads();
+    while (mx == 0.0 && strt + 1 < maxsz) {
+      ++strt;
+      eval_row(strt, V);
+      __syncthreads();
+      double m2 = 0.0;
+      for (int64_t c = tid; c < ncl; c += blockDim.x) m2 = fmax(m2, fabs(V[c]));
+      for (int o = 16; o > 0; o >>= 1) m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+      if (lane == 0) sred[w] = m2;
+      __syncthreads();
+      if (tid == 0) {
+        double m = 0.0;
+        for (int q = 0; q < nw; ++q) m = fmax(m, sred[q]);
+        sred[34] = m;
+      }
+      __syncthreads();
+      mx = sred[34];
+      __syncthreads();
+    }
+  }
+  if (strt + 1 == maxsz) {
+    if (tid == 0) {
+      status[blockIdx.x] = 1;
+      rank_out[blockIdx.x] = 0;
+    }
+    return;
+  }
+  if (tid == 0) {
+    urow[strt] = 1;
+    prow[0] = (int)strt;
+  }
+  __syncthreads();
+  double mv;
+  int64_t mi;
+  cta_restricted_argmax(V, ucol, ncl, sval, sidx, &mv, &mi);
+  for (int64_t c = tid; c < ncl; c += blockDim.x) V[c] = __ddiv_rn(V[c], mv);
+  eval_col(mi, U);
+  __syncthreads();
+  double sr = sumsq(V, ncl), sc = sumsq(U, nro);
+  double znorm2 = __dmul_rn(sr, sc);
+  if (tid == 0) {
+    ucol[mi] = 1;
+    pcol[0] = (int)mi;
+  }
+  __syncthreads();
+  int frnk = 1;
+  int st = 0;
+  while (__dmul_rn(sqrt(sr), sqrt(sc)) > __dmul_rn(rtol, sqrt(znorm2)) && frnk < maxsz) {
+    const double* lastcol = U + (int64_t)(frnk - 1) * nro;
+    int64_t ri;
+    double rv;
+    cta_restricted_argmax(lastcol, urow, nro, sval, sidx, &rv, &ri);
+    if (tid == 0) urow[ri] = 1;
+    if (frnk >= B.cap) {
+      st = 2;
+      break;
+    }
+    double* row = V + (int64_t)frnk * ncl;
+    {
+      const double px = xr[2 * ri], py = xr[2 * ri + 1];
+      for (int64_t c = tid; c < ncl; c += blockDim.x) {
+        double v = kernel_value(kp, px, py, xc[2 * c], xc[2 * c + 1]);
+        for (int j = 0; j < frnk; ++j) v = __dsub_rn(v, __dmul_rn(U[ri + (int64_t)j * nro], V[c + (int64_t)j * ncl]));
+        row[c] = v;
+      }
+    }
+    __syncthreads();
+    double cv;
+    int64_t cj;
+    cta_restricted_argmax(row, ucol, ncl, sval, sidx, &cv, &cj);
+    if (cv == 0.0) break;
+    if (tid == 0) ucol[cj] = 1;
+    for (int64_t c = tid; c < ncl; c += blockDim.x) row[c] = __ddiv_rn(row[c], cv);
+    double* col = U + (int64_t)frnk * nro;
+    {
+      const double px = xc[2 * cj], py = xc[2 * cj + 1];
+      for (int64_t i = tid; i < nro; i += blockDim.x) {
+        double v = kernel_value(kp, xr[2 * i], xr[2 * i + 1], px, py);
+        for (int j = 0; j < frnk; ++j) v = __dsub_rn(v, __dmul_rn(V[cj + (int64_t)j * ncl], U[i + (int64_t)j * nro]));
+        col[i] = v;
+      }
+    }
+    __syncthreads();
+    // dots with the previous columns, one warp per j
+    for (int j = w; j < frnk; j += nw) {
+      const double* uj = U + (int64_t)j * nro;
+      const double* vj = V + (int64_t)j * ncl;
+      double a = 0.0, b = 0.0;
+      for (int64_t i = lane; i < nro; i += 32) a += uj[i] * col[i];
+      for (int64_t c = lane; c < ncl; c += 32) b += vj[c] * row[c];
+      a = warp_sum(a);
+      b = warp_sum(b);
+      if (lane == 0) {
+        dsm[j] = a;
+        dsm[B.cap + j] = b;
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double z = znorm2;
+      for (int j = 0; j < frnk; ++j) z = __dadd_rn(z, __dmul_rn(__dmul_rn(2.0, fabs(dsm[j])), fabs(dsm[B.cap + j])));
+      sred[36] = z;
+      prow[frnk] = (int)ri;
+      pcol[frnk] = (int)cj;
+    }
+    __syncthreads();
+    znorm2 = sred[36];
+    __syncthreads();
+    sr = sumsq(row, ncl);
+    sc = sumsq(col, nro);
+    znorm2 = __dadd_rn(znorm2, __dmul_rn(sr, sc));
+    ++frnk;
+  }
+  if (tid == 0) {
+    rank_out[blockIdx.x] = frnk;
+    status[blockIdx.x] = st;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Householder QR with explicit Q (LAPACK dgeqr2 + dorg2r), one CTA per panel, in place.
+// The panel becomes Q (m x k); R (k x k, zeros below the diagonal) goes to Rout.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) k_panel_qr(const PanelDesc* __restrict__ descs) {
+  extern __shared__ double tau[];  // k
+  __shared__ double red[20];
+  __shared__ double sh[2];
+  const PanelDesc D = descs[blockIdx.x];
+  double* A = D.A;
+  const int64_t m = D.m, lda = D.lda;
+  const int k = D.k;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+  for (int j = 0; j < k; ++j) {
+    double* aj = A + (int64_t)j * lda;
+    double part = 0.0;
+    for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) part += aj[i] * aj[i];
+    part = warp_sum(part);
+    if (lane == 0) red[w] = part;
+    __syncthreads();
+    if (tid == 0) {
+      double sig = 0.0;
+      for (int q = 0; q < nw; ++q) sig += red[q];
+      const double alpha = aj[j];
+      double tj = 0.0, beta = alpha, scal = 0.0;
+      if (sig != 0.0) {
+        const double nrm = sqrt(alpha * alpha + sig);
+        beta = alpha >= 0.0 ? -nrm : nrm;
+        tj = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+      }
+      aj[j] = beta;
+      sh[0] = scal;
+      sh[1] = tj;
+      tau[j] = tj;
+    }
+    __syncthreads();
+    const double scal = sh[0], tj = sh[1];
+    for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= scal;
+    __syncthreads();
+    if (tj != 0.0) {
+      for (int c = j + 1 + w; c < k; c += nw) {
+        double* ac = A + (int64_t)c * lda;
+        double acc = (lane == 0) ? ac[j] : 0.0;
+        for (int64_t i = j + 1 + lane; i < m; i += 32) acc += aj[i] * ac[i];
+        acc = warp_sum(acc) * tj;
+        if (lane == 0) ac[j] -= acc;
+        for (int64_t i = j + 1 + lane; i < m; i += 32) ac[i] -= acc * aj[i];
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < k * k; e += blockDim.x) {
+    const int i = e % k, c = e / k;
+    D.R[e] = (i <= c) ? A[(int64_t)c * lda + i] : 0.0;
+  }
+  __syncthreads();
+  // explicit Q (dorg2r)
+  for (int j = k - 1; j >= 0; --j) {
+    double* aj = A + (int64_t)j * lda;
+    const double tj = tau[j];
+    if (j < k - 1) {
+      if (tid == 0) aj[j] = 1.0;
+      __syncthreads();
+      for (int c = j + 1 + w; c < k; c += nw) {
+        double* ac = A + (int64_t)c * lda;
+        double acc = 0.0;
+        for (int64_t i = j + lane; i < m; i += 32) acc += aj[i] * ac[i];
+        acc = warp_sum(acc) * tj;
+        for (int64_t i = j + lane; i < m; i += 32) ac[i] -= acc * aj[i];
+      }
+      __syncthreads();
+    }
+    for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= -tj;
+    for (int64_t i = tid; i < j; i += blockDim.x) aj[i] = 0.0;
+    if (tid == 0) aj[j] = 1.0 - tj;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Node capacitance of the general factorisation: C = R1 R2', L22 = chol(I - C'C) (lower), one
+// CTA per node, operands in global memory.  info[node] = failing column (1-based) or 0.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) k_gnode(const GNodeDesc* __restrict__ nodes, int* __restrict__ info) {
+  const GNodeDesc N = nodes[blockIdx.x];
+  const int r = N.r;
+  const double* R1 = N.R1;
+  const double* R2 = N.R2;
+  double* C = N.C;
+  double* Lm = N.L22;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < r * r; e += blockDim.x) {
+    const int i = e % r, c = e / r;
+    double acc = 0.0;
+    for (int l = max(i, c); l < r; ++l) acc += R1[i + (int64_t)l * r] * R2[c + (int64_t)l * r];
+    C[e] = acc;
+  }
+  __syncthreads();
+  for (int e = tid; e < r * r; e += blockDim.x) {
+    const int i = e % r, c = e / r;
+    if (i >= c) {
+      double acc = 0.0;
+      for (int l = 0; l < r; ++l) acc += C[l + (int64_t)i * r] * C[l + (int64_t)c * r];
+      Lm[e] = (i == c ? 1.0 : 0.0) - acc;
+    } else {
+      Lm[e] = 0.0;
+    }
+  }
+  __syncthreads();
+  __shared__ int bad;
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int j = 0; j < r; ++j) {
+    const double d = Lm[j + (int64_t)j * r];
+    const bool ok = d > 0.0;
+    const double sd = ok ? sqrt(d) : 1.0;
+    __syncthreads();
+    if (tid == 0 && !ok && bad == 0) bad = j + 1;
+    for (int i = j + 1 + tid; i < r; i += blockDim.x) Lm[i + (int64_t)j * r] /= sd;
+    if (tid == 0) Lm[j + (int64_t)j * r] = sd;
+    __syncthreads();
+    const int wdt = r - j - 1;
+    for (int e = tid; e < wdt * wdt; e += blockDim.x) {
+      const int i = j + 1 + e % wdt, c = j + 1 + e / wdt;
+      if (i >= c) Lm[i + (int64_t)c * r] -= Lm[i + (int64_t)j * r] * Lm[c + (int64_t)j * r];
+    }
+    __syncthreads();
+  }
+  if (tid == 0) info[blockIdx.x] = bad;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Application of node factors to column blocks, one warp per (item, column):
+//   mode 0 (W^{-1}):  y2 -= Q2 (z2 - L22^{-1}(z2 - C' z1))
+//   mode 1 (W^{-T}):  t = L22^{-T} z2;  y1 -= Q1 C t;  y2 -= Q2 (z2 - t)
+//   mode 2 (W):       y2 += Q2 (C' z1 + L22 z2 - z2)
+//   mode 3 (W'):      y1 += Q1 C z2;  y2 += Q2 (L22' z2 - z2)
+//   mode 4 (pre-factor product): y1 += V (U' y2_in), y2 += U (V' y1_in) with Q1 = V, Q2 = U
+//          reading x (in) and accumulating into y (out)
+// with z1 = Q1' y1, z2 = Q2' y2.  grid = (items, ceil(ncols/8)), block 256.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_gapply(const GApplyItem* __restrict__ items,
+                                                const GNodeDesc* __restrict__ nodes, int mode, double* X,
+                                                const double* Xin, int64_t ldX, int kX) {
+  extern __shared__ double sm[];
+  const GApplyItem I = items[blockIdx.x];
+  const GNodeDesc N = nodes[I.node];
+  const int r = N.r;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int col = blockIdx.y * 8 + w;
+  double* base = I.base ? I.base : X;
+  const int64_t ld = I.base ? I.ld : ldX;
+  const int ncols = I.base ? I.ncols : kX;
+  if (col >= ncols) return;
+  double* z1 = sm + (size_t)w * 3 * r;
+  double* z2 = z1 + r;
+  double* t = z2 + r;
+  double* y1 = base + I.off1 + (int64_t)col * ld;
+  double* y2 = base + I.off2 + (int64_t)col * ld;
+  const double* x1 = (mode == 4) ? Xin + I.off1 + (int64_t)col * ldX : y1;
+  const double* x2 = (mode == 4) ? Xin + I.off2 + (int64_t)col * ldX : y2;
+  const double* Q1 = N.Q1;
+  const double* Q2 = N.Q2;
+  const int64_t s1 = N.s1, s2 = N.s2;
+  // projections z1 = Q1' x1, z2 = Q2' x2 (mode 4: z1 = U' x2, z2 = V' x1)
+  for (int q = 0; q < r; ++q) {
+    const double* q1 = (mode == 4 ? Q2 : Q1) + (int64_t)q * (mode == 4 ? s2 : s1);
+    const double* q2 = (mode == 4 ? Q1 : Q2) + (int64_t)q * (mode == 4 ? s1 : s2);
+    const double* xa = (mode == 4) ? x2 : x1;
+    const double* xb = (mode == 4) ? x1 : x2;
+    const int64_t na = (mode == 4) ? s2 : s1, nb = (mode == 4) ? s1 : s2;
+    double a = 0.0, b = 0.0;
+    if (mode == 0 || mode == 2 || mode == 4)
+      for (int64_t i = lane; i < na; i += 32) a += q1[i] * xa[i];
+    for (int64_t i = lane; i < nb; i += 32) b += q2[i] * xb[i];
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if (lane == 0) {
+      z1[q] = a;
+      z2[q] = b;
+    }
+  }
+  __syncwarp();
+  const double* C = N.C;
+  const double* Lm = N.L22;
+  if (mode == 4) {
+    // y1 (rows c1) += V z1 ; y2 (rows c2) += U z2   (V = Q1 rows c1, U = Q2 rows c2)
+    for (int64_t i = lane; i < s1; i += 32) {
+      double acc = 0.0;
+      for (int q = 0; q < r; ++q) acc += Q1[i + (int64_t)q * s1] * z1[q];
+      y1[i] += acc;
+    }
+    for (int64_t i = lane; i < s2; i += 32) {
+      double acc = 0.0;
+      for (int q = 0; q < r; ++q) acc += Q2[i + (int64_t)q * s2] * z2[q];
+      y2[i] += acc;
+    }
+    return;
+  }
+  if (mode == 0) {
+    for (int i = lane; i < r; i += 32) {
+      double acc = 0.0;
+      for (int l = 0; l < r; ++l) acc += C[l + (int64_t)i * r] * z1[l];
+      t[i] = z2[i] - acc;
+    }
+    __syncwarp();
+    for (int l = 0; l < r; ++l) {
+      const double v = t[l] / Lm[l + (int64_t)l * r];
+      __syncwarp();
+      if (lane == 0) t[l] = v;
+      for (int i = l + 1 + lane; i < r; i += 32) t[i] -= Lm[i + (int64_t)l * r] * v;
+      __syncwarp();
+    }
+    for (int i = lane; i < r; i += 32) t[i] = z2[i] - t[i];
+    __syncwarp();
+    for (int64_t i = lane; i < s2; i += 32) {
+      double acc = 0.0;
+      for (int q = 0; q < r; ++q) acc += Q2[i + (int64_t)q * s2] * t[q];
+      y2[i] -= acc;
+    }
+  } else if (mode == 1) {
+    for (int i = lane; i < r; i += 32) t[i] = z2[i];
+    __syncwarp();
+    for (int i = r - 1; i >= 0; --i) {
+      const double v = t[i] / Lm[i + (int64_t)i * r];
+      __syncwarp();
+      if (lane == 0) t[i] = v;
+      for (int l = lane; l < i; l += 32) t[l] -= Lm[i + (int64_t)l * r] * v;
+      __syncwarp();
+    }
+    // z1 <- C t (reuse z1), z2 <- z2 - t
+    for (int i = lane; i < r; i += 32) {
+      double acc = 0.0;
+      for (int l = 0; l < r; ++l) acc += C[i + (int64_t)l * r] * t[l];
+      z1[i] = acc;
+    }
+    __syncwarp();
+    for (int i = lane; i < r; i += 32) z2[i] -= t[i];
+    __syncwarp();
+    for (int64_t i = lane; i < s1; i += 32) {
+      double acc = 0.0;
+      for (int q = 0; q < r; ++q) acc += Q1[i + (int64_t)q * s1] * z1[q];
+      y1[i] -= acc;
+    }
+    for (int64_t i = lane; i < s2; i += 32) {
+      double acc = 0.0;
+      for (int q = 0; q < r; ++q) acc += Q2[i + (int64_t)q * s2] * z2[q];
+      y2[i] -= acc;
+    }
+  } else if (mode == 2) {
+    for (int i = lane; i < r; i += 32) {
+      double acc = 0.0;
+      for (int l = 0; l < r; ++l) acc += C[l + (int64_t)i * r] * z1[l];
+      for (int l = 0; l <= i; ++l) acc += Lm[i + (int64_t)l * r] * z2[l];
+      t[i] = acc - z2[i];
+    }
+    __syncwarp();
+    for (int64_t i = lane; i < s2; i += 32) {
+      double acc = 0.0;
+      for (int q = 0; q < r; ++q) acc += Q2[i + (int64_t)q * s2] * t[q];
+      y2[i] += acc;
+    }
+  } else {
+    for (int i = lane; i < r; i += 32) {
+      double a1 = 0.0, a2 = 0.0;
+      for (int l = 0; l < r; ++l) a1 += C[i + (int64_t)l * r] * z2[l];
+      for (int l = i; l < r; ++l) a2 += Lm[l + (int64_t)i * r] * z2[l];
+      z1[i] = a1;
+      t[i] = a2 - z2[i];
+    }
+    __syncwarp();
+    for (int64_t i = lane; i < s1; i += 32) {
+      double acc = 0.0;
+      for (int q = 0; q < r; ++q) acc += Q1[i + (int64_t)q * s1] * z1[q];
+      y1[i] += acc;
+    }
+    for (int64_t i = lane; i < s2; i += 32) {
+      double acc = 0.0;
+      for (int q = 0; q < r; ++q) acc += Q2[i + (int64_t)q * s2] * t[q];
+      y2[i] += acc;
+    }
+  }
+}
+
+// 2 sum log |diag(L22)| over the general nodes: one partial per node (deterministic).
+__global__ void k_glogdet(const GNodeDesc* __restrict__ nodes, int nn, double* __restrict__ partial) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nn) return;
+  const GNodeDesc N = nodes[q];
+  double s = 0.0;
+  for (int i = 0; i < N.r; ++i) s += 2.0 * log(fabs(N.L22[i + (int64_t)i * N.r]));
+  partial[q] = s;
+}
+
+// ---------------------------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------------------------
+void launch_aca(const double* pts, KParams kp, const AcaBlock* blocks, int nblocks, int maxcap, double* P,
+                uint8_t* F, int* piv, double rtol, int* rank, int* status, cudaStream_t st) {
+  const size_t sm = (size_t)2 * std::max(maxcap, 1) * sizeof(double);
+  cudaFuncSetAttribute(k_aca, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_aca<<<nblocks, 1024, sm, st>>>(pts, kp, blocks, P, F, piv, rtol, rank, status);
+}
+
+void launch_panel_qr(const PanelDesc* descs, int n, int maxk, cudaStream_t st) {
+  const size_t sm = (size_t)std::max(maxk, 1) * sizeof(double);
+  k_panel_qr<<<n, 512, sm, st>>>(descs);
+}
+
+void launch_gnode(const GNodeDesc* nodes, int n, int* info, cudaStream_t st) {
+  k_gnode<<<n, 512, 0, st>>>(nodes, info);
+}
+
+void launch_gapply(const GApplyItem* items, int n, const GNodeDesc* nodes, int maxr, int maxcols, int mode,
+                   double* X, const double* Xin, int64_t ldX, int kX, cudaStream_t st) {
+  if (n <= 0) return;
+  dim3 grid((unsigned)n, (unsigned)((maxcols + 7) / 8));
+  const size_t sm = (size_t)8 * 3 * std::max(maxr, 1) * sizeof(double);
+  cudaFuncSetAttribute(k_gapply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_gapply<<<grid, 256, sm, st>>>(items, nodes, mode, X, Xin, ldX, kX);
+}
+
+void launch_glogdet(const GNodeDesc* nodes, int nn, double* partial, cudaStream_t st) {
+  k_glogdet<<<(nn + 127) / 128, 128, 0, st>>>(nodes, nn, partial);
+}
+
+}  // namespace km

@@ -103,6 +103,27 @@ struct km_handle {
   double* d_X = nullptr;
   double* d_Y = nullptr;
   int64_t xcap = 0;
+  // general (ACA) path
+  std::vector<AcaBlock> blk;          // off-diagonal blocks, level 1 first
+  std::vector<int> brank;             // ACA rank per block
+  std::vector<int64_t> lvoff;         // first block of each level (size L+2, lvoff[l] for l=1..L+1)
+  AcaBlock* d_blk = nullptr;
+  double* d_panels = nullptr;
+  uint8_t* d_flags = nullptr;
+  int* d_piv = nullptr;
+  int* d_brank = nullptr;
+  int* d_bstatus = nullptr;
+  double* d_R12 = nullptr;
+  double* d_CL = nullptr;
+  GNodeDesc* d_gnodes = nullptr;
+  GApplyItem* d_gsolve = nullptr;     // one item per block, rows relative to the right-hand side
+  GApplyItem* d_gfact = nullptr;      // factorisation updates, grouped by level
+  std::vector<int64_t> gfoff;
+  PanelDesc* d_pdesc = nullptr;
+  LeafDesc* d_ldesc = nullptr;
+  int64_t nldesc = 0;
+  int gmaxr = 0;
+  double* d_gpartial = nullptr;
   // derivative HODLR (evaluated for one parameter at a time) and gradient workspaces
   int dk_param = -1;
   double* d_dK = nullptr;
@@ -198,6 +219,22 @@ void free_problem(km_handle* h) {
   h->vcap = 0;
   h->d_X = h->d_Y = nullptr;
   h->xcap = 0;
+  h->blk.clear();
+  h->brank.clear();
+  h->lvoff.clear();
+  h->gfoff.clear();
+  h->d_blk = nullptr;
+  h->d_panels = nullptr;
+  h->d_flags = nullptr;
+  h->d_piv = h->d_brank = h->d_bstatus = nullptr;
+  h->d_R12 = h->d_CL = nullptr;
+  h->d_gnodes = nullptr;
+  h->d_gsolve = h->d_gfact = nullptr;
+  h->d_pdesc = nullptr;
+  h->d_ldesc = nullptr;
+  h->nldesc = 0;
+  h->gmaxr = 0;
+  h->d_gpartial = nullptr;
   h->dk_param = -1;
   h->d_dK = h->d_dPhi = h->d_Sj = h->d_GP = h->d_GG = h->d_T = h->d_U = h->d_dots = nullptr;
   h->gcap = h->tcap = 0;
@@ -299,7 +336,71 @@ int ensure_xy(km_handle* h, int64_t k) {
 NodeMatsH node_mats(km_handle* h) { return NodeMatsH{h->d_Ct, h->d_L22, h->d_Eref, h->d_Etau, h->r}; }
 
 // ---- factor sweeps on a device block X (n x k, ld = n), in place ---------------------------
+
+// ---- general (ACA) path -------------------------------------------------------------------
+int general_fwd(km_handle* h, double* X, int k) {  // X <- W^{-1} X
+  const Tree& t = h->tree;
+  cudaStream_t st = h->stream;
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 0, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+    return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
+  for (int l = 1; l <= t.L; ++l) {
+    const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
+    KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 0, X, X, t.n, k, st));
+  }
+  return check_launch(h, "general fwd");
+}
+
+int general_bwd(km_handle* h, double* X, int k) {  // X <- W'^{-1} X
+  const Tree& t = h->tree;
+  cudaStream_t st = h->stream;
+  for (int l = t.L; l >= 1; --l) {
+    const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
+    KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 1, X, X, t.n, k, st));
+  }
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 1, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+    return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
+  return check_launch(h, "general bwd");
+}
+
+int general_mul(km_handle* h, double* X, int k) {  // X <- W X
+  const Tree& t = h->tree;
+  cudaStream_t st = h->stream;
+  for (int l = t.L; l >= 1; --l) {
+    const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
+    KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 2, X, X, t.n, k, st));
+  }
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 2, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+    return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular kernel");
+  return check_launch(h, "general mul");
+}
+
+int general_mul_t(km_handle* h, double* X, int k) {  // X <- W' X
+  const Tree& t = h->tree;
+  cudaStream_t st = h->stream;
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 3, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+    return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular kernel");
+  for (int l = 1; l <= t.L; ++l) {
+    const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
+    KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 3, X, X, t.n, k, st));
+  }
+  return check_launch(h, "general mul_t");
+}
+
+// Y = K X before factorisation: leaf products, then V (U' x) and U (V' x) block by block
+// (src/HODLR/src/baseoverloads.jl:152-169), level by level because levels share rows.
+int general_matvec(km_handle* h, const double* X, double* Y, int k) {
+  const Tree& t = h->tree;
+  cudaStream_t st = h->stream;
+  KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_nys_apply(h->d_K, nullptr, nullptr, 0, t, X, t.n, nullptr, Y, t.n, k, st));
+  for (int l = 1; l <= t.L; ++l) {
+    const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
+    KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 4, Y, X, t.n, k, st));
+  }
+  return check_launch(h, "general matvec");
+}
+
 int nested_fwd(km_handle* h, double* X, int k) {  // X <- W^{-1} X
+  if (h->method == KM_METHOD_ACA) return general_fwd(h, X, k);
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
   if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 0, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
@@ -314,6 +415,7 @@ int nested_fwd(km_handle* h, double* X, int k) {  // X <- W^{-1} X
 }
 
 int nested_bwd(km_handle* h, double* X, int k) {  // X <- W'^{-1} X
+  if (h->method == KM_METHOD_ACA) return general_bwd(h, X, k);
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
   if (t.L > 0) {
@@ -329,6 +431,7 @@ int nested_bwd(km_handle* h, double* X, int k) {  // X <- W'^{-1} X
 }
 
 int nested_mul(km_handle* h, double* X, int k) {  // X <- W X
+  if (h->method == KM_METHOD_ACA) return general_mul(h, X, k);
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
   if (t.L > 0) {
@@ -344,6 +447,7 @@ int nested_mul(km_handle* h, double* X, int k) {  // X <- W X
 }
 
 int nested_mul_t(km_handle* h, double* X, int k) {  // X <- W' X
+  if (h->method == KM_METHOD_ACA) return general_mul_t(h, X, k);
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
   if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 3, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
@@ -359,6 +463,7 @@ int nested_mul_t(km_handle* h, double* X, int k) {  // X <- W' X
 
 // Y = K X before factorisation (Nystrom blocks)
 int nystrom_matvec(km_handle* h, const double* X, double* Y, int k) {
+  if (h->method == KM_METHOD_ACA) return general_matvec(h, X, Y, k);
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
   NodeMatsH nm = node_mats(h);
@@ -575,6 +680,221 @@ int km_get_stats(const km_handle* h, km_stats* out) {
   return KM_OK;
 }
 
+
+// ---- ACA assembly (src/HODLR/src/constructor.jl:44-53 with ACA, src/factorizations.jl:9-84) ----
+static int aca_assemble(km_handle* h, const double* pts, bool dev, const Tree& t, const double* params,
+                        int kernel_id, double tol, int64_t maxrank) {
+  free_problem(h);
+  h->tree = t;
+  h->kp = KParams{kernel_id, params[0], params[1], params[2]};
+  h->method = KM_METHOD_ACA;
+  h->tol = tol;
+  h->maxrank = maxrank;
+  h->r = 0;
+  cudaStream_t st = h->stream;
+  // blocks, level 1 first (the reference's order of U[l][k], V[l][k])
+  h->lvoff.assign(t.L + 2, 0);
+  int64_t full = 0;
+  for (int l = 1; l <= t.L; ++l) {
+    h->lvoff[l] = (int64_t)h->blk.size();
+    for (int64_t k = 0; k < t.nodes_at(l); ++k) {
+      AcaBlock b{};
+      b.col0 = t.node_start(l - 1, 2 * k);
+      b.ncl = t.node_size(l - 1, 2 * k);
+      b.row0 = t.node_start(l - 1, 2 * k + 1);
+      b.nro = t.node_size(l - 1, 2 * k + 1);
+      const int64_t minsz = std::min(b.nro, b.ncl);
+      b.maxsz = (int)(maxrank == 0 ? minsz : std::min<int64_t>(maxrank, minsz));
+      full += (b.nro + b.ncl) * (int64_t)b.maxsz;
+      h->blk.push_back(b);
+    }
+  }
+  h->lvoff[t.L + 1] = (int64_t)h->blk.size();
+  const int nb = (int)h->blk.size();
+  // panel capacity: the full rank bound when it fits in 40% of the budget, else 256 columns
+  const bool fits = (double)full * 8.0 <= 0.4 * (double)device_budget(h);
+  int64_t offP = 0, offF = 0, offV = 0;
+  int maxcap = 0;
+  for (auto& b : h->blk) {
+    b.cap = fits ? b.maxsz : std::min(b.maxsz, 256);
+    b.offU = offP;
+    offP += b.nro * b.cap;
+    b.offV = offP;
+    offP += b.ncl * b.cap;
+    b.offFlag = offF;
+    offF += b.nro + b.ncl;
+    b.offPiv = offV;
+    offV += b.cap;
+    maxcap = std::max(maxcap, b.cap);
+  }
+  int64_t kbytes = 0;
+  for (int64_t j = 0; j < t.nleaf; ++j) kbytes += t.leaf_size(j) * t.leaf_size(j);
+  int rc;
+  if ((rc = dalloc(h, &h->d_pts, 2 * t.n)) || (rc = dalloc(h, &h->d_K, kbytes)) || (rc = dalloc(h, &h->d_Lf, kbytes)) ||
+      (rc = dalloc(h, &h->d_panels, offP)) || (rc = dalloc(h, &h->d_flags, offF)) ||
+      (rc = dalloc(h, &h->d_piv, 2 * offV)) || (rc = dalloc(h, &h->d_brank, nb)) ||
+      (rc = dalloc(h, &h->d_bstatus, nb)) || (rc = dalloc(h, &h->d_blk, nb)) ||
+      (rc = dalloc(h, &h->d_info, t.nleaf + nb + 1)) || (rc = dalloc(h, &h->d_partial, kLogdetBlocks)) ||
+      (rc = dalloc(h, &h->d_scalar, 4)) || (rc = dalloc(h, &h->d_gpartial, nb)) ||
+      (rc = dalloc(h, &h->d_gsolve, nb)) || (rc = dalloc(h, &h->d_gnodes, nb))) {
+    free_problem(h);
+    return rc;
+  }
+  timer_start(h);
+  KM_CUDA(h, cudaMemcpyAsync(h->d_pts, pts, sizeof(double) * 2 * t.n,
+                             dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+  if (nb > 0) {
+    KM_CUDA(h, cudaMemcpyAsync(h->d_blk, h->blk.data(), sizeof(AcaBlock) * nb, cudaMemcpyHostToDevice, st));
+    KM_CUDA(h, cudaMemsetAsync(h->d_bstatus, 0, sizeof(int) * nb, st));
+  }
+  KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st));
+  if (nb > 0)
+    KLV(h, KM_PROF_ACA, launch_aca(h->d_pts, h->kp, h->d_blk, nb, maxcap, h->d_panels, h->d_flags, h->d_piv, tol,
+                                   h->d_brank, h->d_bstatus, st));
+  if ((rc = check_launch(h, "aca")) != KM_OK) return rc;
+  h->stats.assemble_ms = timer_stop(h);
+  if ((rc = sync(h, "aca")) != KM_OK) return rc;
+  h->brank.assign(nb, 0);
+  std::vector<int> stat(nb, 0);
+  if (nb > 0) {
+    KM_CUDA(h, cudaMemcpy(h->brank.data(), h->d_brank, sizeof(int) * nb, cudaMemcpyDeviceToHost));
+    KM_CUDA(h, cudaMemcpy(stat.data(), h->d_bstatus, sizeof(int) * nb, cudaMemcpyDeviceToHost));
+  }
+  for (int q = 0; q < nb; ++q) {
+    if (stat[q] == 1) return fail(h, KM_ERR_ACA, "Incompatible maxrank or matrix dimensions.");
+    if (stat[q] == 2)
+      return fail(h, KM_ERR_UNSUPPORTED, "ACA rank reached the panel capacity of 256 columns before the "
+                                         "tolerance; pass a maxrank");
+  }
+  // node descriptors (factor storage sized by the ranks) and the per-block solve items
+  int64_t r2 = 0;
+  h->gmaxr = 1;
+  for (int q = 0; q < nb; ++q) {
+    r2 += (int64_t)h->brank[q] * h->brank[q];
+    h->gmaxr = std::max(h->gmaxr, h->brank[q]);
+  }
+  if ((rc = dalloc(h, &h->d_R12, 2 * r2)) || (rc = dalloc(h, &h->d_CL, 2 * r2))) return rc;
+  std::vector<GNodeDesc> nodes(nb);
+  std::vector<GApplyItem> items(nb);
+  int64_t o = 0;
+  for (int q = 0; q < nb; ++q) {
+    const AcaBlock& b = h->blk[q];
+    const int rq = h->brank[q];
+    GNodeDesc& N = nodes[q];
+    N.Q1 = h->d_panels + b.offV;
+    N.Q2 = h->d_panels + b.offU;
+    N.R1 = h->d_R12 + 2 * o;
+    N.R2 = h->d_R12 + 2 * o + (int64_t)rq * rq;
+    N.C = h->d_CL + 2 * o;
+    N.L22 = h->d_CL + 2 * o + (int64_t)rq * rq;
+    N.s1 = b.ncl;
+    N.s2 = b.nro;
+    N.r = rq;
+    o += (int64_t)rq * rq;
+    items[q] = GApplyItem{q, 0, b.col0, b.row0, 0, nullptr};
+  }
+  if (nb > 0) {
+    KM_CUDA(h, cudaMemcpy(h->d_gnodes, nodes.data(), sizeof(GNodeDesc) * nb, cudaMemcpyHostToDevice));
+    KM_CUDA(h, cudaMemcpy(h->d_gsolve, items.data(), sizeof(GApplyItem) * nb, cudaMemcpyHostToDevice));
+  }
+  h->assembled = true;
+  h->factorized = false;
+  return KM_OK;
+}
+
+// ---- general factorisation (src/HODLR/src/symfact.jl:6-49) ----------------------------------
+static int general_factorize(km_handle* h) {
+  const Tree& t = h->tree;
+  cudaStream_t st = h->stream;
+  const int nb = (int)h->blk.size();
+  int rc;
+  timer_start(h);
+  KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + nb), st));
+  if (!KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol(h->d_K, h->d_Lf, t, h->d_info, st)))
+    return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the leaf Cholesky kernel");
+  if (nb > 0) {
+    // leaf triangular solves of every panel (invapply!, src/HODLR/src/utils.jl:54-65)
+    std::vector<LeafDesc> ld;
+    for (int l = 1; l <= t.L; ++l) {
+      for (int64_t k = 0; k < t.nodes_at(l); ++k) {
+        const int q = (int)(h->lvoff[l] + k);
+        const AcaBlock& b = h->blk[q];
+        const int64_t j0 = k << l, jm = j0 + (int64_t(1) << (l - 1)), j1 = (k + 1) << l;
+        for (int64_t j = j0; j < jm; ++j)
+          ld.push_back(LeafDesc{j, h->d_panels + b.offV + (t.leaf_start(j) - b.col0), b.ncl, h->brank[q]});
+        for (int64_t j = jm; j < j1; ++j)
+          ld.push_back(LeafDesc{j, h->d_panels + b.offU + (t.leaf_start(j) - b.row0), b.nro, h->brank[q]});
+      }
+    }
+    // per-level panel QR descriptors and W_l^{-1} updates of the coarser panels
+    std::vector<PanelDesc> pd;
+    std::vector<GApplyItem> fi;
+    h->gfoff.assign(t.L + 2, 0);
+    std::vector<int64_t> pdoff(t.L + 2, 0);
+    int maxcols = 1;
+    for (int l = 1; l <= t.L; ++l) {
+      pdoff[l] = (int64_t)pd.size();
+      h->gfoff[l] = (int64_t)fi.size();
+      for (int64_t k = 0; k < t.nodes_at(l); ++k) {
+        const int q = (int)(h->lvoff[l] + k);
+        const AcaBlock& b = h->blk[q];
+        int64_t o = 0;
+        for (int p = 0; p < q; ++p) o += (int64_t)h->brank[p] * h->brank[p];
+        const int rq = h->brank[q];
+        pd.push_back(PanelDesc{h->d_panels + b.offV, b.ncl, b.ncl, rq, h->d_R12 + 2 * o});
+        pd.push_back(PanelDesc{h->d_panels + b.offU, b.nro, b.nro, rq, h->d_R12 + 2 * o + (int64_t)rq * rq});
+        for (int lev = l + 1; lev <= t.L; ++lev) {
+          const int64_t kp = k >> (lev - l);
+          const int qp = (int)(h->lvoff[lev] + kp);
+          const AcaBlock& bp = h->blk[qp];
+          const bool first = ((k >> (lev - l - 1)) & 1) == 0;  // node inside the ancestor's c1 side
+          double* panel = h->d_panels + (first ? bp.offV : bp.offU);
+          const int64_t side0 = first ? bp.col0 : bp.row0;
+          const int64_t ldp = first ? bp.ncl : bp.nro;
+          fi.push_back(GApplyItem{q, h->brank[qp], b.col0 - side0, b.row0 - side0, ldp, panel});
+          maxcols = std::max(maxcols, h->brank[qp]);
+        }
+      }
+    }
+    pdoff[t.L + 1] = (int64_t)pd.size();
+    h->gfoff[t.L + 1] = (int64_t)fi.size();
+    dfree(h, h->d_ldesc);
+    dfree(h, h->d_pdesc);
+    dfree(h, h->d_gfact);
+    h->d_ldesc = nullptr;
+    h->d_pdesc = nullptr;
+    h->d_gfact = nullptr;
+    if ((rc = dalloc(h, &h->d_ldesc, (int64_t)ld.size())) || (rc = dalloc(h, &h->d_pdesc, (int64_t)pd.size())) ||
+        (rc = dalloc(h, &h->d_gfact, std::max<int64_t>((int64_t)fi.size(), 1))))
+      return rc;
+    KM_CUDA(h, cudaMemcpy(h->d_ldesc, ld.data(), sizeof(LeafDesc) * ld.size(), cudaMemcpyHostToDevice));
+    KM_CUDA(h, cudaMemcpy(h->d_pdesc, pd.data(), sizeof(PanelDesc) * pd.size(), cudaMemcpyHostToDevice));
+    if (!fi.empty())
+      KM_CUDA(h, cudaMemcpy(h->d_gfact, fi.data(), sizeof(GApplyItem) * fi.size(), cudaMemcpyHostToDevice));
+    if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri_desc(h->d_Lf, t, 0, h->d_ldesc, (int)ld.size(), h->gmaxr, st)))
+      return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
+    for (int l = 1; l <= t.L; ++l) {
+      KLV(h, KM_PROF_LEAF_QR, launch_panel_qr(h->d_pdesc + pdoff[l], (int)(pdoff[l + 1] - pdoff[l]), h->gmaxr, st));
+      KLV(h, KM_PROF_NODE, launch_gnode(h->d_gnodes + h->lvoff[l], (int)(h->lvoff[l + 1] - h->lvoff[l]),
+                                        h->d_info + t.nleaf + h->lvoff[l], st));
+      const int64_t a = h->gfoff[l], b = h->gfoff[l + 1];
+      if (b > a)
+        KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gfact + a, (int)(b - a), h->d_gnodes, h->gmaxr, maxcols, 0,
+                                            nullptr, nullptr, 0, 0, st));
+    }
+  }
+  if ((rc = check_launch(h, "general factorize")) != KM_OK) return rc;
+  h->stats.factorize_ms = timer_stop(h);
+  if ((rc = sync(h, "general factorize")) != KM_OK) return rc;
+  if ((rc = check_info(h, t.nleaf, "leaf")) != KM_OK) return rc;
+  std::vector<int> info(nb);
+  if (nb > 0) KM_CUDA(h, cudaMemcpy(info.data(), h->d_info + t.nleaf, sizeof(int) * nb, cudaMemcpyDeviceToHost));
+  for (int q = 0; q < nb; ++q)
+    if (info[q]) return fail(h, KM_ERR_NOT_SPD, "PosDefException: a low-rank capacitance block is not positive definite");
+  h->factorized = true;
+  return KM_OK;
+}
+
 static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, int kernel_id,
                          const double* params, int nparams, int method, double tol, int64_t maxrank,
                          int level_kind, int64_t level) {
@@ -591,7 +911,10 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   std::string msg;
   if (!build_tree(n, level_kind, level, &t, &msg)) return fail(h, KM_ERR_BAD_ARG, msg);
   if (t.nleaf > 65535) return fail(h, KM_ERR_UNSUPPORTED, "more than 65535 leaves");
-  if (method == KM_METHOD_ACA) return fail(h, KM_ERR_UNSUPPORTED, "ACA assembly is not built yet");
+  if (method == KM_METHOD_ACA) {
+    if (!(tol >= 0.0) || maxrank < 0) return fail(h, KM_ERR_BAD_ARG, "ACA needs tol >= 0 and maxrank >= 0");
+    return aca_assemble(h, pts, dev, t, params, kernel_id, tol, maxrank);
+  }
   // Nystrom checks (src/HODLR/src/constructor.jl:26-28)
   if (maxrank < 2) return fail(h, KM_ERR_BAD_ARG, "Please supply a fixed off-diagonal rank that is >=2.");
   const int64_t minleaf = t.m0;  // smallest leaf size
@@ -676,6 +999,11 @@ int km_factorize(km_handle* h) {
   if (!h) return KM_ERR_BAD_ARG;
   cudaSetDevice(h->cfg.device);
   if (!h->assembled) return fail(h, KM_ERR_STATE, "assemble first");
+  if (h->method == KM_METHOD_ACA) {
+    if (h->factorized)
+      return fail(h, KM_ERR_STATE, "already factorised (U and V were overwritten); assemble again");
+    return general_factorize(h);
+  }
   const Tree& t = h->tree;
   const int r = h->r;
   cudaStream_t st = h->stream;
@@ -804,9 +1132,29 @@ int km_logdet(km_handle* h, double* out) {
   cudaSetDevice(h->cfg.device);
   if (!h->factorized) return fail(h, KM_ERR_STATE, "No logdet without factorization.");
   timer_start(h);
+  int rc;
+  if (h->method == KM_METHOD_ACA) {
+    // 2 sum log diag(L_leaf) + 2 sum log|diag(L22)| (baseoverloads.jl:194-209), summed on the host
+    // in a fixed order
+    Tree t0 = h->tree;
+    t0.nnode = 0;
+    const int nb = (int)h->blk.size();
+    KLV(h, KM_PROF_OTHER, launch_logdet(h->d_Lf, t0, nullptr, 1, h->d_partial, kLogdetBlocks, h->d_scalar, h->stream));
+    if (nb > 0) KLV(h, KM_PROF_OTHER, launch_glogdet(h->d_gnodes, nb, h->d_gpartial, h->stream));
+    if ((rc = check_launch(h, "logdet")) != KM_OK) return rc;
+    double leaf = 0.0;
+    std::vector<double> part(nb);
+    KM_CUDA(h, cudaMemcpyAsync(&leaf, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (nb > 0) KM_CUDA(h, cudaMemcpyAsync(part.data(), h->d_gpartial, sizeof(double) * nb, cudaMemcpyDeviceToHost, h->stream));
+    if ((rc = sync(h, "logdet")) != KM_OK) return rc;
+    double s = leaf;
+    for (int q = 0; q < nb; ++q) s += part[q];
+    *out = s;
+    h->stats.logdet_ms = timer_stop(h);
+    return KM_OK;
+  }
   KLV(h, KM_PROF_OTHER, launch_logdet(h->d_Lf, h->tree, h->d_L22, h->r, h->d_partial, kLogdetBlocks, h->d_scalar, h->stream));
   h->stats.kernel_launches += 1;  // the logdet runs a partial and a final reduction kernel
-  int rc;
   if ((rc = check_launch(h, "logdet")) != KM_OK) return rc;
   KM_CUDA(h, cudaMemcpyAsync(out, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   h->stats.logdet_ms = timer_stop(h);
@@ -816,16 +1164,37 @@ int km_logdet(km_handle* h, double* out) {
 int km_block_ranks(km_handle* h, int64_t* out) {
   if (!h || !out) return fail(h, KM_ERR_BAD_ARG, "null");
   if (!h->assembled) return fail(h, KM_ERR_STATE, "assemble first");
-  for (int64_t q = 0; q < h->tree.nnode; ++q) out[q] = h->r;
+  for (int64_t q = 0; q < h->tree.nnode; ++q)
+    out[q] = (h->method == KM_METHOD_ACA) ? h->brank[q] : h->r;
   return KM_OK;
 }
 
-int km_aca_pivots(km_handle* h, int64_t, int64_t, int64_t*, int64_t*, int64_t*) {
-  return fail(h, KM_ERR_UNSUPPORTED, "ACA assembly is not built yet");
+int km_aca_pivots(km_handle* h, int64_t block, int64_t cap, int64_t* rows, int64_t* cols, int64_t* out_rank) {
+  if (!h || !rows || !cols || !out_rank) return fail(h, KM_ERR_BAD_ARG, "null");
+  if (!h->assembled || h->method != KM_METHOD_ACA) return fail(h, KM_ERR_STATE, "no ACA assembly");
+  if (block < 0 || block >= (int64_t)h->blk.size()) return fail(h, KM_ERR_BAD_ARG, "block out of range");
+  const AcaBlock& b = h->blk[block];
+  const int rq = h->brank[block];
+  std::vector<int> p(2 * (size_t)b.cap);
+  KM_CUDA(h, cudaMemcpy(p.data(), h->d_piv + 2 * b.offPiv, sizeof(int) * 2 * b.cap, cudaMemcpyDeviceToHost));
+  for (int64_t i = 0; i < std::min<int64_t>(cap, rq); ++i) {
+    rows[i] = p[i];
+    cols[i] = p[b.cap + i];
+  }
+  *out_rank = rq;
+  return KM_OK;
 }
 
-int km_block_factors(km_handle* h, int64_t, double*, double*) {
-  return fail(h, KM_ERR_UNSUPPORTED, "block factor export is not built yet");
+int km_block_factors(km_handle* h, int64_t block, double* U, double* V) {
+  if (!h || !U || !V) return fail(h, KM_ERR_BAD_ARG, "null");
+  if (!h->assembled || h->method != KM_METHOD_ACA) return fail(h, KM_ERR_STATE, "no ACA assembly");
+  if (h->factorized) return fail(h, KM_ERR_STATE, "U and V abandoned after overwriting");
+  if (block < 0 || block >= (int64_t)h->blk.size()) return fail(h, KM_ERR_BAD_ARG, "block out of range");
+  const AcaBlock& b = h->blk[block];
+  const int rq = h->brank[block];
+  KM_CUDA(h, cudaMemcpy(U, h->d_panels + b.offU, sizeof(double) * b.nro * rq, cudaMemcpyDeviceToHost));
+  KM_CUDA(h, cudaMemcpy(V, h->d_panels + b.offV, sizeof(double) * b.ncl * rq, cudaMemcpyDeviceToHost));
+  return KM_OK;
 }
 
 int km_derivative_matvec(km_handle* h, int param, const double* x, double* y, int64_t k) {

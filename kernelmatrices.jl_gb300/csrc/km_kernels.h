@@ -14,6 +14,42 @@ struct LeafOperand {
   int ld_is_m;
 };
 
+// ---- general (ACA) path descriptors ----
+struct AcaBlock {             // rows = second child (a:b), cols = first child (c:d), 0-based
+  int64_t row0, nro, col0, ncl;
+  int64_t offU, offV;         // column-major U (nro x cap), V (ncl x cap) in the panel arena
+  int64_t offFlag, offPiv;    // used-row/col flags (nro + ncl bytes); pivots (2 * cap ints at 2*offPiv)
+  int cap, maxsz;
+};
+struct PanelDesc {            // Householder QR with explicit Q of A (m x k, leading dim lda)
+  double* A;
+  int64_t m, lda;
+  int k;
+  double* R;                  // k x k output
+};
+struct GNodeDesc {            // one node of the general factorisation
+  double* Q1;                 // V panel (rows c1), Q after the QR
+  double* Q2;                 // U panel (rows c2)
+  double* C;
+  double* L22;
+  const double* R1;
+  const double* R2;
+  int64_t s1, s2;
+  int r;
+};
+struct GApplyItem {           // node factor applied to rows off1.. (c1) and off2.. (c2) of a block
+  int node;
+  int ncols;
+  int64_t off1, off2, ld;
+  double* base;               // nullptr: the right-hand-side block passed to the kernel
+};
+struct LeafDesc {             // leaf triangular operation on an arbitrary column block
+  int64_t leaf;
+  double* ptr;                // first row of the leaf's rows in the block
+  int64_t ld;
+  int ncols;
+};
+
 struct NodeMatsH {
   const double* Ct;
   const double* L22;
@@ -71,5 +107,16 @@ void launch_leaf_dnys_apply(const double* dKl, const double* Phi, const double* 
                             const double* VG, double* Y, int64_t ldy, int k, cudaStream_t st);
 void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n, int k,
                      double* out, cudaStream_t st);
+
+// ACA and the general factorisation
+void launch_aca(const double* pts, KParams kp, const AcaBlock* blocks, int nblocks, int maxcap, double* P,
+                uint8_t* F, int* piv, double rtol, int* rank, int* status, cudaStream_t st);
+void launch_panel_qr(const PanelDesc* descs, int n, int maxk, cudaStream_t st);
+void launch_gnode(const GNodeDesc* nodes, int n, int* info, cudaStream_t st);
+void launch_gapply(const GApplyItem* items, int n, const GNodeDesc* nodes, int maxr, int maxcols, int mode,
+                   double* X, const double* Xin, int64_t ldX, int kX, cudaStream_t st);
+void launch_glogdet(const GNodeDesc* nodes, int nn, double* partial, cudaStream_t st);
+bool launch_leaf_tri_desc(const double* Lf, const Tree& t, int op, const LeafDesc* descs, int n, int maxcols,
+                          cudaStream_t st);
 
 }  // namespace km

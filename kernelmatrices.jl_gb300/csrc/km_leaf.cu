@@ -17,25 +17,15 @@ namespace km {
 // grid = (nleaf, ceil(ncols / NC)), block = 256.
 // ---------------------------------------------------------------------------------------------
 template <int NC>
-__global__ void __launch_bounds__(256) k_leaf_tri(const double* __restrict__ Lf, DTree t, int op,
-                                                  LeafOperand B, LeafOperand X, int ncols) {
-  extern __shared__ double sm[];
-  const int64_t leaf = blockIdx.x;
-  const int m = d_leaf_size(t, leaf);
-  const int64_t s = d_leaf_start(t, leaf);
-  const double* __restrict__ L = Lf + d_leaf_koff(t, leaf);
-  const int c0 = blockIdx.y * NC;
-  const int nc = min(NC, ncols - c0);
+__device__ void leaf_tri_body(const double* __restrict__ L, int m, int op, const double* Bp, int64_t ldb,
+                              double* Xp, int64_t ldx, int nc, double* sm) {
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  const int64_t ldb = B.ld_is_m ? m : B.ld, ldx = X.ld_is_m ? m : X.ld;
-  const double* Bp = B.ptr + s * B.bmul;
-  double* Xp = X.ptr + s * X.bmul;
   double* xs = sm;                   // NC x m  (column c at xs[c*m])
   double* ys = xs + NC * m;          // NC x m  (products only)
   double* D = ys + ((op >= 2) ? NC * m : 0);  // 32 x 33
   for (int e = tid; e < NC * m; e += blockDim.x) {
     const int c = e / m, i = e % m;
-    xs[e] = (c < nc) ? Bp[(int64_t)(c0 + c) * ldb + i] : 0.0;
+    xs[e] = (c < nc) ? Bp[(int64_t)c * ldb + i] : 0.0;
   }
   __syncthreads();
   if (op == 0 || op == 1) {
@@ -100,7 +90,7 @@ __global__ void __launch_bounds__(256) k_leaf_tri(const double* __restrict__ Lf,
     }
     for (int e = tid; e < nc * m; e += blockDim.x) {
       const int c = e / m, i = e % m;
-      Xp[(int64_t)(c0 + c) * ldx + i] = xs[e];
+      Xp[(int64_t)c * ldx + i] = xs[e];
     }
   } else {
     for (int i = tid; i < m; i += blockDim.x) {
@@ -127,10 +117,39 @@ __global__ void __launch_bounds__(256) k_leaf_tri(const double* __restrict__ Lf,
     __syncthreads();
     for (int e = tid; e < nc * m; e += blockDim.x) {
       const int c = e / m, i = e % m;
-      Xp[(int64_t)(c0 + c) * ldx + i] = ys[e];
+      Xp[(int64_t)c * ldx + i] = ys[e];
     }
   }
 }
+
+template <int NC>
+__global__ void __launch_bounds__(256) k_leaf_tri(const double* __restrict__ Lf, DTree t, int op,
+                                                  LeafOperand B, LeafOperand X, int ncols) {
+  extern __shared__ double sm[];
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf);
+  const int c0 = blockIdx.y * NC;
+  const int nc = min(NC, ncols - c0);
+  const int64_t ldb = B.ld_is_m ? m : B.ld, ldx = X.ld_is_m ? m : X.ld;
+  leaf_tri_body<NC>(Lf + d_leaf_koff(t, leaf), m, op, B.ptr + s * B.bmul + (int64_t)c0 * ldb, ldb,
+                    X.ptr + s * X.bmul + (int64_t)c0 * ldx, ldx, nc, sm);
+}
+
+// Same operation on arbitrary column blocks: descriptor d covers leaf d.leaf's rows of a block.
+template <int NC>
+__global__ void __launch_bounds__(256) k_leaf_tri_desc(const double* __restrict__ Lf, DTree t, int op,
+                                                       const LeafDesc* __restrict__ descs) {
+  extern __shared__ double sm[];
+  const LeafDesc d = descs[blockIdx.x];
+  const int c0 = blockIdx.y * NC;
+  if (c0 >= d.ncols) return;
+  const int nc = min(NC, d.ncols - c0);
+  const int m = d_leaf_size(t, d.leaf);
+  double* p = d.ptr + (int64_t)c0 * d.ld;
+  leaf_tri_body<NC>(Lf + d_leaf_koff(t, d.leaf), m, op, p, d.ld, p, d.ld, nc, sm);
+}
+
 
 // ---------------------------------------------------------------------------------------------
 // Q_leaf' y  (proj) and y += sign * Q_leaf g (expand) through the leaf reflectors.
@@ -236,6 +255,26 @@ bool launch_leaf_tri(const double* Lf, const Tree& t, int op, double* Bptr, int6
   if (tri_launch<8>(Lf, t, op, B, X, ncols, st)) return true;
   if (tri_launch<4>(Lf, t, op, B, X, ncols, st)) return true;
   return tri_launch<1>(Lf, t, op, B, X, ncols, st);
+}
+
+template <int NC>
+static bool tri_desc_launch(const double* Lf, const Tree& t, int op, const LeafDesc* descs, int n, int maxcols,
+                            cudaStream_t st) {
+  const size_t sm = ((size_t)(op >= 2 ? 2 : 1) * NC * t.max_leaf + 32 * 33) * sizeof(double);
+  if (sm > 200 * 1024) return false;
+  cudaFuncSetAttribute(k_leaf_tri_desc<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  dim3 grid((unsigned)n, (unsigned)((maxcols + NC - 1) / NC));
+  k_leaf_tri_desc<NC><<<grid, 256, sm, st>>>(Lf, dtree(t), op, descs);
+  return true;
+}
+
+bool launch_leaf_tri_desc(const double* Lf, const Tree& t, int op, const LeafDesc* descs, int n, int maxcols,
+                          cudaStream_t st) {
+  if (n <= 0) return true;
+  if (tri_desc_launch<16>(Lf, t, op, descs, n, maxcols, st)) return true;
+  if (tri_desc_launch<8>(Lf, t, op, descs, n, maxcols, st)) return true;
+  if (tri_desc_launch<4>(Lf, t, op, descs, n, maxcols, st)) return true;
+  return tri_desc_launch<1>(Lf, t, op, descs, n, maxcols, st);
 }
 
 template <bool EXPAND>

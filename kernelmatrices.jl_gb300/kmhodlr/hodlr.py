@@ -226,6 +226,28 @@ class KernelHODLR:
         _check(self._h, L.load().km_block_ranks(self._h, _ip(out)))
         return out[:cnt]
 
+    def aca_pivots(self, block: int):
+        """Row and column pivots (0-based within the block) of ACA block ``block`` (level 1 first)."""
+        lib = L.load()
+        cap = max(int(self.block_ranks()[block]), 1)
+        rows = np.zeros(cap, dtype=np.int64)
+        cols = np.zeros(cap, dtype=np.int64)
+        rk = C.c_int64()
+        _check(self._h, lib.km_aca_pivots(self._h, int(block), cap, _ip(rows), _ip(cols), C.byref(rk)))
+        return rows[:rk.value], cols[:rk.value]
+
+    def block_factors(self, block: int):
+        """(U, V) of block ``block`` as ``KernelHODLR.U[l][k]``, ``.V[l][k]`` hold them before
+        factorisation (structstypes.jl:52-63)."""
+        lib = L.load()
+        flat = [x for lv in self.nonleafindices for x in lv]
+        a, b, c, d = flat[block]
+        rk = int(self.block_ranks()[block])
+        U = np.zeros((b - a + 1, rk), order="F")
+        V = np.zeros((d - c + 1, rk), order="F")
+        _check(self._h, lib.km_block_factors(self._h, int(block), _dp(U), _dp(V)))
+        return U, V
+
     # -- reference operations --
     def __matmul__(self, x: np.ndarray) -> np.ndarray:
         """``mul!(target, K::KernelHODLR, src)`` (baseoverloads.jl:152-179)."""
