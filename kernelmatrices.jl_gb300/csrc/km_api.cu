@@ -72,6 +72,7 @@ struct km_handle {
   Tree tree;
   KParams kp{};
   int method = KM_METHOD_NYSTROM;
+  bool mixed = false;  // float-pair factor (KM_PREC_MIXED)
   double tol = 0.0;
   int64_t maxrank = 0;
   int r = 0;
@@ -88,10 +89,13 @@ struct km_handle {
   double* d_S = nullptr;
   double* d_Sc = nullptr;
   double* d_SinvT = nullptr;
+  double* d_SinvTf = nullptr;  // float-pair copy for the mixed form
   double* d_Ct = nullptr;
   double* d_L22 = nullptr;
   double* d_Eref = nullptr;
   double* d_Etau = nullptr;
+  double* d_L22i = nullptr;  // L22^{-1} per node
+  double* d_E = nullptr;     // explicit 2r x r transfer per node
   int* d_info = nullptr;
   double* d_partial = nullptr;
   double* d_scalar = nullptr;
@@ -136,8 +140,13 @@ struct km_handle {
   double* d_U = nullptr;
   double* d_dots = nullptr;
   int64_t tcap = 0;
+  double* d_res = nullptr;   // refinement residual (n x rcap)
+  double* d_rdots = nullptr;
+  int64_t rcap = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaStream_t own_stream = nullptr;  // the handle's own stream (h->stream may be external)
+  cudaStream_t side = nullptr;        // forms the solve operators while the node levels run
+  cudaEvent_t sev[kMaxLevels + 3] = {};
   // profiler
   bool prof = false;
   struct Rec {
@@ -211,7 +220,8 @@ void free_problem(km_handle* h) {
   h->allocs.clear();
   h->bytes = 0;
   h->d_pts = h->d_lnd = h->d_K = h->d_Lf = h->d_Phi = h->d_Q = h->d_tauleaf = h->d_R = nullptr;
-  h->d_S = h->d_Sc = h->d_SinvT = h->d_Ct = h->d_L22 = h->d_Eref = h->d_Etau = nullptr;
+  h->d_S = h->d_Sc = h->d_SinvT = h->d_SinvTf = h->d_Ct = h->d_L22 = h->d_Eref = h->d_Etau = nullptr;
+  h->d_L22i = h->d_E = nullptr;
   h->d_lndidx = nullptr;
   h->d_info = nullptr;
   h->d_partial = h->d_scalar = nullptr;
@@ -238,6 +248,8 @@ void free_problem(km_handle* h) {
   h->dk_param = -1;
   h->d_dK = h->d_dPhi = h->d_Sj = h->d_GP = h->d_GG = h->d_T = h->d_U = h->d_dots = nullptr;
   h->gcap = h->tcap = 0;
+  h->d_res = h->d_rdots = nullptr;
+  h->rcap = 0;
   h->assembled = h->factorized = false;
 }
 
@@ -333,7 +345,7 @@ int ensure_xy(km_handle* h, int64_t k) {
   return KM_OK;
 }
 
-NodeMatsH node_mats(km_handle* h) { return NodeMatsH{h->d_Ct, h->d_L22, h->d_Eref, h->d_Etau, h->r}; }
+NodeMatsH node_mats(km_handle* h) { return NodeMatsH{h->d_Ct, h->d_L22, h->d_L22i, h->d_E, h->r}; }
 
 // ---- factor sweeps on a device block X (n x k, ld = n), in place ---------------------------
 
@@ -341,7 +353,7 @@ NodeMatsH node_mats(km_handle* h) { return NodeMatsH{h->d_Ct, h->d_L22, h->d_Ere
 int general_fwd(km_handle* h, double* X, int k) {  // X <- W^{-1} X
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
-  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 0, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<double>(h->d_Lf, t, 0, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
   for (int l = 1; l <= t.L; ++l) {
     const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
@@ -357,7 +369,7 @@ int general_bwd(km_handle* h, double* X, int k) {  // X <- W'^{-1} X
     const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
     KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 1, X, X, t.n, k, st));
   }
-  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 1, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<double>(h->d_Lf, t, 1, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
   return check_launch(h, "general bwd");
 }
@@ -369,7 +381,7 @@ int general_mul(km_handle* h, double* X, int k) {  // X <- W X
     const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
     KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 2, X, X, t.n, k, st));
   }
-  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 2, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<double>(h->d_Lf, t, 2, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular kernel");
   return check_launch(h, "general mul");
 }
@@ -377,7 +389,7 @@ int general_mul(km_handle* h, double* X, int k) {  // X <- W X
 int general_mul_t(km_handle* h, double* X, int k) {  // X <- W' X
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
-  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 3, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<double>(h->d_Lf, t, 3, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular kernel");
   for (int l = 1; l <= t.L; ++l) {
     const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
@@ -399,66 +411,131 @@ int general_matvec(km_handle* h, const double* X, double* Y, int k) {
   return check_launch(h, "general matvec");
 }
 
-int nested_fwd(km_handle* h, double* X, int k) {  // X <- W^{-1} X
-  if (h->method == KM_METHOD_ACA) return general_fwd(h, X, k);
+template <typename T>
+T* P(double* p) {
+  return reinterpret_cast<T*>(p);
+}
+
+template <typename T>
+int nested_fwd_t(km_handle* h, T* X, int k) {  // X <- W^{-1} X
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
-  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 0, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<T>(P<T>(h->d_Lf), t, 0, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
   if (t.L == 0) return check_launch(h, "fwd");
   NodeMatsH nm = node_mats(h);
-  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st));
-  for (int l = 1; l <= t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_FWD_, st));
-  for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_FWD_, st));
-  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, -1.0, st));
+  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, X, t.n, P<T>(h->d_VP), k, st));
+  for (int l = 1; l <= t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VD), k, UP_FWD_, st));
+  for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VG), P<T>(h->d_VD), k, DN_FWD_, st));
+  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, P<T>(h->d_VG), X, t.n, k, -1.0, st));
   return check_launch(h, "fwd");
 }
 
-int nested_bwd(km_handle* h, double* X, int k) {  // X <- W'^{-1} X
-  if (h->method == KM_METHOD_ACA) return general_bwd(h, X, k);
+template <typename T>
+int nested_bwd_t(km_handle* h, T* X, int k) {  // X <- W'^{-1} X
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
   if (t.L > 0) {
     NodeMatsH nm = node_mats(h);
-    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st));
-    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_PROJ_, st));
-    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_BWD_, st));
-    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, -1.0, st));
+    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, X, t.n, P<T>(h->d_VP), k, st));
+    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VD), k, UP_PROJ_, st));
+    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VG), P<T>(h->d_VD), k, DN_BWD_, st));
+    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, P<T>(h->d_VG), X, t.n, k, -1.0, st));
   }
-  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 1, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<T>(P<T>(h->d_Lf), t, 1, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
   return check_launch(h, "bwd");
 }
 
-int nested_mul(km_handle* h, double* X, int k) {  // X <- W X
-  if (h->method == KM_METHOD_ACA) return general_mul(h, X, k);
+template <typename T>
+int nested_mul_t_(km_handle* h, T* X, int k) {  // X <- W X
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
   if (t.L > 0) {
     NodeMatsH nm = node_mats(h);
-    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st));
-    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_PROJ_, st));
-    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_MUL_, st));
-    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, 1.0, st));
+    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, X, t.n, P<T>(h->d_VP), k, st));
+    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VD), k, UP_PROJ_, st));
+    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VG), P<T>(h->d_VD), k, DN_MUL_, st));
+    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, P<T>(h->d_VG), X, t.n, k, 1.0, st));
   }
-  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 2, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<T>(P<T>(h->d_Lf), t, 2, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular kernel");
   return check_launch(h, "mul");
 }
 
-int nested_mul_t(km_handle* h, double* X, int k) {  // X <- W' X
-  if (h->method == KM_METHOD_ACA) return general_mul_t(h, X, k);
+template <typename T>
+int nested_mult_t(km_handle* h, T* X, int k) {  // X <- W' X
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
-  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 3, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<T>(P<T>(h->d_Lf), t, 3, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular kernel");
   if (t.L == 0) return check_launch(h, "mul_t");
   NodeMatsH nm = node_mats(h);
-  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj(h->d_Q, h->d_tauleaf, h->r, t, X, t.n, h->d_VP, k, st));
-  for (int l = 1; l <= t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_MULT_, st));
-  for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_MULT_, st));
-  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand(h->d_Q, h->d_tauleaf, h->r, t, h->d_VG, X, t.n, k, 1.0, st));
+  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, X, t.n, P<T>(h->d_VP), k, st));
+  for (int l = 1; l <= t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VD), k, UP_MULT_, st));
+  for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VG), P<T>(h->d_VD), k, DN_MULT_, st));
+  KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, P<T>(h->d_VG), X, t.n, k, 1.0, st));
   return check_launch(h, "mul_t");
+}
+
+// Dispatch on the method and the precision.  In the mixed form the factor holds float pairs and
+// the block X (n x k, ld n) is converted in place around the float-pair kernels.
+int nested_fwd(km_handle* h, double* X, int k) {
+  if (h->method == KM_METHOD_ACA) return general_fwd(h, X, k);
+  if (!h->mixed) return nested_fwd_t<double>(h, X, k);
+  ff* Xf = reinterpret_cast<ff*>(X);
+  KLV(h, KM_PROF_OTHER, launch_to_ff(X, Xf, h->tree.n * k, h->stream));
+  const int rc = nested_fwd_t<ff>(h, Xf, k);
+  KLV(h, KM_PROF_OTHER, launch_from_ff(Xf, X, h->tree.n * k, h->stream));
+  return rc;
+}
+
+int nested_bwd(km_handle* h, double* X, int k) {
+  if (h->method == KM_METHOD_ACA) return general_bwd(h, X, k);
+  if (!h->mixed) return nested_bwd_t<double>(h, X, k);
+  ff* Xf = reinterpret_cast<ff*>(X);
+  KLV(h, KM_PROF_OTHER, launch_to_ff(X, Xf, h->tree.n * k, h->stream));
+  const int rc = nested_bwd_t<ff>(h, Xf, k);
+  KLV(h, KM_PROF_OTHER, launch_from_ff(Xf, X, h->tree.n * k, h->stream));
+  return rc;
+}
+
+// K^{-1} X = W'^{-1} W^{-1} X with one conversion pair in the mixed form
+int nested_solve(km_handle* h, double* X, int k) {
+  if (h->method == KM_METHOD_ACA) {
+    const int rc = general_fwd(h, X, k);
+    return rc != KM_OK ? rc : general_bwd(h, X, k);
+  }
+  if (!h->mixed) {
+    const int rc = nested_fwd_t<double>(h, X, k);
+    return rc != KM_OK ? rc : nested_bwd_t<double>(h, X, k);
+  }
+  ff* Xf = reinterpret_cast<ff*>(X);
+  KLV(h, KM_PROF_OTHER, launch_to_ff(X, Xf, h->tree.n * k, h->stream));
+  int rc = nested_fwd_t<ff>(h, Xf, k);
+  if (rc == KM_OK) rc = nested_bwd_t<ff>(h, Xf, k);
+  KLV(h, KM_PROF_OTHER, launch_from_ff(Xf, X, h->tree.n * k, h->stream));
+  return rc;
+}
+
+int nested_mul(km_handle* h, double* X, int k) {
+  if (h->method == KM_METHOD_ACA) return general_mul(h, X, k);
+  if (!h->mixed) return nested_mul_t_<double>(h, X, k);
+  ff* Xf = reinterpret_cast<ff*>(X);
+  KLV(h, KM_PROF_OTHER, launch_to_ff(X, Xf, h->tree.n * k, h->stream));
+  const int rc = nested_mul_t_<ff>(h, Xf, k);
+  KLV(h, KM_PROF_OTHER, launch_from_ff(Xf, X, h->tree.n * k, h->stream));
+  return rc;
+}
+
+int nested_mul_t(km_handle* h, double* X, int k) {
+  if (h->method == KM_METHOD_ACA) return general_mul_t(h, X, k);
+  if (!h->mixed) return nested_mult_t<double>(h, X, k);
+  ff* Xf = reinterpret_cast<ff*>(X);
+  KLV(h, KM_PROF_OTHER, launch_to_ff(X, Xf, h->tree.n * k, h->stream));
+  const int rc = nested_mult_t<ff>(h, Xf, k);
+  KLV(h, KM_PROF_OTHER, launch_from_ff(Xf, X, h->tree.n * k, h->stream));
+  return rc;
 }
 
 // Y = K X before factorisation (Nystrom blocks)
@@ -469,13 +546,72 @@ int nystrom_matvec(km_handle* h, const double* X, double* Y, int k) {
   NodeMatsH nm = node_mats(h);
   if (t.L > 0) {
     KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_phiT(h->d_Phi, h->r, t, X, t.n, h->d_VP, k, st));
-    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm, l, h->d_VP, h->d_VD, k, UP_SUM_, st));
-    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_NYS_, st));
+    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up<double>(t, nm, l, h->d_VP, h->d_VD, k, UP_SUM_, st));
+    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down<double>(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_NYS_, st));
   } else {
     cudaMemsetAsync(h->d_VG, 0, sizeof(double) * h->r * k, st);
   }
   KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_nys_apply(h->d_K, h->d_Phi, h->d_Sc, h->r, t, X, t.n, h->d_VG, Y, t.n, k, st));
   return check_launch(h, "matvec");
+}
+
+
+// Mixed form: FP64 iterative refinement x += K~^{-1} (b - K x), with the FP64 Nystrom HODLR
+// product as the residual operator (it keeps the FP64 leaves and landmark columns) and the
+// float-pair factor K~ as the preconditioner; stops at ||b - Kx||_F <= refine_tol ||b||_F.
+int refine(km_handle* h, const double* d_b, double* d_x, int k) {
+  const Tree& t = h->tree;
+  cudaStream_t st = h->stream;
+  int rc;
+  if (k > h->rcap) {
+    dfree(h, h->d_res);
+    dfree(h, h->d_rdots);
+    h->d_res = h->d_rdots = nullptr;
+    h->rcap = 0;
+    if ((rc = dalloc(h, &h->d_res, t.n * k)) || (rc = dalloc(h, &h->d_rdots, 2 * k))) return rc;
+    h->rcap = k;
+  }
+  std::vector<double> dots(2 * k);
+  KLV(h, KM_PROF_OTHER, launch_col_dots(d_b, t.n, d_b, t.n, t.n, k, h->d_rdots + k, st));
+  int it = 0;
+  double relres = 0.0;
+  for (;;) {
+    if ((rc = nystrom_matvec(h, d_x, h->d_res, k)) != KM_OK) return rc;
+    KLV(h, KM_PROF_OTHER, launch_axpby(h->d_res, d_b, 1.0, -1.0, t.n * k, st));  // res = b - K x
+    KLV(h, KM_PROF_OTHER, launch_col_dots(h->d_res, t.n, h->d_res, t.n, t.n, k, h->d_rdots, st));
+    KM_CUDA(h, cudaMemcpyAsync(dots.data(), h->d_rdots, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, st));
+    if ((rc = sync(h, "refine")) != KM_OK) return rc;
+    double rr = 0.0, bb = 0.0;
+    for (int c = 0; c < k; ++c) {
+      rr += dots[c];
+      bb += dots[k + c];
+    }
+    relres = bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
+    if (relres <= h->cfg.refine_tol || it >= h->cfg.refine_max_iter) break;
+    if ((rc = nested_solve(h, h->d_res, k)) != KM_OK) return rc;
+    KLV(h, KM_PROF_OTHER, launch_axpby(d_x, h->d_res, 1.0, 1.0, t.n * k, st));  // x += d
+    ++it;
+  }
+  h->stats.refine_iterations = it;
+  h->stats.refine_residual = relres;
+  return KM_OK;
+}
+
+// Side stream: forms explicit leaf bases and node solve operators concurrently with the node
+// levels on the main stream (they are needed only by solves and products).
+void side_begin(km_handle* h) {
+  cudaEventRecord(h->sev[0], h->stream);
+  cudaStreamWaitEvent(h->side, h->sev[0], 0);
+  h->stats.kernel_launches += 1;
+}
+void side_level(km_handle* h, int l) {
+  cudaEventRecord(h->sev[l], h->stream);
+  cudaStreamWaitEvent(h->side, h->sev[l], 0);
+  h->stats.kernel_launches += 1;
+}
+void side_end(km_handle* h) {
+  cudaEventRecord(h->sev[kMaxLevels + 2], h->side);
+  cudaStreamWaitEvent(h->stream, h->sev[kMaxLevels + 2], 0);
 }
 
 int check_info(km_handle* h, int64_t count, const char* what) {
@@ -524,8 +660,8 @@ int derivative_apply(km_handle* h, int j, const double* X, double* Y, int k) {
   NodeMatsH nm2{nullptr, nullptr, nullptr, nullptr, 2 * r};
   if (t.L > 0) {
     KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dphiT(h->d_Phi, h->d_dPhi, r, t, X, t.n, h->d_GP, k, st));
-    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up(t, nm2, l, h->d_GP, nullptr, k, UP_SUM_, st));
-    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down(t, nm2, l, h->d_GP, h->d_GG, nullptr, k, DN_NYS_, st));
+    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up<double>(t, nm2, l, h->d_GP, nullptr, k, UP_SUM_, st));
+    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down<double>(t, nm2, l, h->d_GP, h->d_GG, nullptr, k, DN_NYS_, st));
   } else {
     KM_CUDA(h, cudaMemsetAsync(h->d_GG, 0, sizeof(double) * 2 * r * k, st));
   }
@@ -605,7 +741,12 @@ int km_create(const km_config* cfg, km_handle** out) {
   *out = nullptr;
   km_handle* h = new km_handle();
   if (cfg) h->cfg = *cfg;
-  if (h->cfg.refine_max_iter <= 0) h->cfg.refine_max_iter = 30;
+  if (h->cfg.precision != KM_PREC_FP64 && h->cfg.precision != KM_PREC_MIXED) {
+    delete h;
+    return KM_ERR_BAD_ARG;
+  }
+  h->mixed = (h->cfg.precision == KM_PREC_MIXED);
+  if (h->cfg.refine_max_iter < 0) h->cfg.refine_max_iter = 0;
   if (h->cfg.refine_tol <= 0) h->cfg.refine_tol = 1e-10;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -625,6 +766,12 @@ int km_create(const km_config* cfg, km_handle** out) {
     return KM_ERR_CUDA;
   }
   h->own_stream = h->stream;
+  if (cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    return KM_ERR_CUDA;
+  }
+  for (auto& e : h->sev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   *out = h;
   return KM_OK;
 }
@@ -666,6 +813,10 @@ int km_destroy(km_handle* h) {
   for (auto e : h->pool) cudaEventDestroy(e);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->side) cudaStreamSynchronize(h->side);
+  for (auto e : h->sev)
+    if (e) cudaEventDestroy(e);
+  if (h->side) cudaStreamDestroy(h->side);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return KM_OK;
@@ -810,7 +961,7 @@ static int general_factorize(km_handle* h) {
   int rc;
   timer_start(h);
   KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + nb), st));
-  if (!KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol(h->d_K, h->d_Lf, t, h->d_info, st)))
+  if (!KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<double>(h->d_K, h->d_Lf, t, h->d_info, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the leaf Cholesky kernel");
   if (nb > 0) {
     // leaf triangular solves of every panel (invapply!, src/HODLR/src/utils.jl:54-65)
@@ -943,11 +1094,13 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
        (rc = dalloc(h, &h->d_Lf, kbytes)) || (rc = dalloc(h, &h->d_Phi, n * r)) ||
        (rc = dalloc(h, &h->d_Q, n * r)) || (rc = dalloc(h, &h->d_tauleaf, t.nleaf * r)) ||
        (rc = dalloc(h, &h->d_R, (t.nleaf + t.nnode) * r * r)) || (rc = dalloc(h, &h->d_S, r * r)) ||
-       (rc = dalloc(h, &h->d_Sc, r * r)) || (rc = dalloc(h, &h->d_SinvT, r * r)) ||
+       (rc = dalloc(h, &h->d_Sc, r * r)) || (rc = dalloc(h, &h->d_SinvT, r * r)) || (rc = dalloc(h, &h->d_SinvTf, r * r)) ||
        (rc = dalloc(h, &h->d_Ct, std::max<int64_t>(t.nnode, 1) * r * r)) ||
        (rc = dalloc(h, &h->d_L22, std::max<int64_t>(t.nnode, 1) * r * r)) ||
        (rc = dalloc(h, &h->d_Eref, std::max<int64_t>(t.nnode, 1) * r * r)) ||
        (rc = dalloc(h, &h->d_Etau, std::max<int64_t>(t.nnode, 1) * r)) ||
+       (rc = dalloc(h, &h->d_L22i, std::max<int64_t>(t.nnode, 1) * r * r)) ||
+       (rc = dalloc(h, &h->d_E, std::max<int64_t>(t.nnode, 1) * 2 * r * r)) ||
        (rc = dalloc(h, &h->d_info, t.nleaf + t.nnode + 1)) ||
        (rc = dalloc(h, &h->d_partial, kLogdetBlocks)) || (rc = dalloc(h, &h->d_scalar, 4)))) {
     free_problem(h);
@@ -970,6 +1123,7 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   if (!KL(h, KM_PROF_OTHER, launch_chol_small(h->d_Sc, r, h->d_info + t.nleaf + t.nnode, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "rank too large for the landmark Cholesky");
   KLV(h, KM_PROF_OTHER, launch_tri_inv_t(h->d_Sc, r, h->d_SinvT, st));
+  KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_SinvT, P<ff>(h->d_SinvTf), (int64_t)r * r, st));
   if ((rc = check_launch(h, "assemble")) != KM_OK) return rc;
   h->stats.assemble_ms = timer_stop(h);
   if ((rc = sync(h, "assemble")) != KM_OK) return rc;
@@ -1010,17 +1164,46 @@ int km_factorize(km_handle* h) {
   int rc;
   timer_start(h);
   KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + t.nnode), st));
-  if (!KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol(h->d_K, h->d_Lf, t, h->d_info, st)))
+  if (!(h->mixed ? KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<ff>(h->d_K, P<ff>(h->d_Lf), t, h->d_info, st))
+                 : KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<double>(h->d_K, h->d_Lf, t, h->d_info, st))))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the leaf Cholesky kernel");
   // A = L^{-1} Phi on every leaf, then Householder QR of each leaf panel
-  KM_CUDA(h, cudaMemcpyAsync(h->d_Q, h->d_Phi, sizeof(double) * t.n * r, cudaMemcpyDeviceToDevice, st));
-  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri(h->d_Lf, t, 0, h->d_Q, r, 0, 1, h->d_Q, r, 0, 1, r, st)))
-    return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
-  if (t.L > 0) {
-    KLV(h, KM_PROF_LEAF_QR, launch_leaf_qr(h->d_Q, r, t, h->d_tauleaf, h->d_R, st));
-    for (int l = 1; l <= t.L; ++l)
-      KLV(h, KM_PROF_NODE, launch_node_factor(h->d_R, h->d_SinvT, r, l, t, h->d_Ct, h->d_L22, h->d_Eref,
-                                              h->d_Etau, h->d_info + t.nleaf, st));
+  if (h->mixed) {
+    // float-pair factor: every FP64-pipe-bound step runs on the FP32 pipe in float-float
+    KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Q), t.n * r, st));
+    if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<ff>(P<ff>(h->d_Lf), t, 0, P<ff>(h->d_Q), r, 0, 1, P<ff>(h->d_Q), r,
+                                                     0, 1, r, st)))
+      return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
+    if (t.L > 0) {
+      KLV(h, KM_PROF_LEAF_QR, launch_leaf_qr<ff>(P<ff>(h->d_Q), r, t, P<ff>(h->d_tauleaf), P<ff>(h->d_R), st));
+      side_begin(h);
+      launch_leaf_formq<ff>(P<ff>(h->d_Q), P<ff>(h->d_tauleaf), r, t, h->side);
+      for (int l = 1; l <= t.L; ++l) {
+        KLV(h, KM_PROF_NODE, launch_node_factor<ff>(P<ff>(h->d_R), P<ff>(h->d_SinvTf), r, l, t, P<ff>(h->d_Ct),
+                                                    P<ff>(h->d_L22), P<ff>(h->d_Eref), P<ff>(h->d_Etau),
+                                                    h->d_info + t.nleaf, st));
+        side_level(h, l);
+        launch_node_finalize<ff>(P<ff>(h->d_L22), P<ff>(h->d_Eref), P<ff>(h->d_Etau), r, l, t, P<ff>(h->d_L22i),
+                                 P<ff>(h->d_E), h->side);
+      }
+      side_end(h);
+    }
+  } else {
+    KM_CUDA(h, cudaMemcpyAsync(h->d_Q, h->d_Phi, sizeof(double) * t.n * r, cudaMemcpyDeviceToDevice, st));
+    if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<double>(h->d_Lf, t, 0, h->d_Q, r, 0, 1, h->d_Q, r, 0, 1, r, st)))
+      return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
+    if (t.L > 0) {
+      KLV(h, KM_PROF_LEAF_QR, launch_leaf_qr<double>(h->d_Q, r, t, h->d_tauleaf, h->d_R, st));
+      side_begin(h);
+      launch_leaf_formq<double>(h->d_Q, h->d_tauleaf, r, t, h->side);
+      for (int l = 1; l <= t.L; ++l) {
+        KLV(h, KM_PROF_NODE, launch_node_factor<double>(h->d_R, h->d_SinvT, r, l, t, h->d_Ct, h->d_L22, h->d_Eref,
+                                                        h->d_Etau, h->d_info + t.nleaf, st));
+        side_level(h, l);
+        launch_node_finalize<double>(h->d_L22, h->d_Eref, h->d_Etau, r, l, t, h->d_L22i, h->d_E, h->side);
+      }
+      side_end(h);
+    }
   }
   if ((rc = check_launch(h, "factorize")) != KM_OK) return rc;
   h->stats.factorize_ms = timer_stop(h);
@@ -1065,8 +1248,10 @@ int km_solve_dev(km_handle* h, const double* d_b, double* d_x, int64_t k) {
   timer_start(h);
   if (d_x != d_b)
     KM_CUDA(h, cudaMemcpyAsync(d_x, d_b, sizeof(double) * h->tree.n * k, cudaMemcpyDeviceToDevice, h->stream));
-  if ((rc = nested_fwd(h, d_x, (int)k)) != KM_OK) return rc;
-  if ((rc = nested_bwd(h, d_x, (int)k)) != KM_OK) return rc;
+  if ((rc = nested_solve(h, d_x, (int)k)) != KM_OK) return rc;
+  if (h->mixed && h->method == KM_METHOD_NYSTROM && h->cfg.refine_max_iter > 0 &&
+      (rc = refine(h, d_b, d_x, (int)k)) != KM_OK)
+    return rc;
   h->stats.solve_ms = timer_stop(h);
   return sync(h, "solve");
 }
@@ -1139,7 +1324,8 @@ int km_logdet(km_handle* h, double* out) {
     Tree t0 = h->tree;
     t0.nnode = 0;
     const int nb = (int)h->blk.size();
-    KLV(h, KM_PROF_OTHER, launch_logdet(h->d_Lf, t0, nullptr, 1, h->d_partial, kLogdetBlocks, h->d_scalar, h->stream));
+    KLV(h, KM_PROF_OTHER, launch_logdet<double>(h->d_Lf, t0, nullptr, 1, h->d_partial, kLogdetBlocks, h->d_scalar,
+                                                h->stream));
     if (nb > 0) KLV(h, KM_PROF_OTHER, launch_glogdet(h->d_gnodes, nb, h->d_gpartial, h->stream));
     if ((rc = check_launch(h, "logdet")) != KM_OK) return rc;
     double leaf = 0.0;
@@ -1153,7 +1339,12 @@ int km_logdet(km_handle* h, double* out) {
     h->stats.logdet_ms = timer_stop(h);
     return KM_OK;
   }
-  KLV(h, KM_PROF_OTHER, launch_logdet(h->d_Lf, h->tree, h->d_L22, h->r, h->d_partial, kLogdetBlocks, h->d_scalar, h->stream));
+  if (h->mixed)
+    KLV(h, KM_PROF_OTHER, launch_logdet<ff>(P<ff>(h->d_Lf), h->tree, P<ff>(h->d_L22), h->r, h->d_partial,
+                                            kLogdetBlocks, h->d_scalar, h->stream));
+  else
+    KLV(h, KM_PROF_OTHER, launch_logdet<double>(h->d_Lf, h->tree, h->d_L22, h->r, h->d_partial, kLogdetBlocks,
+                                                h->d_scalar, h->stream));
   h->stats.kernel_launches += 1;  // the logdet runs a partial and a final reduction kernel
   if ((rc = check_launch(h, "logdet")) != KM_OK) return rc;
   KM_CUDA(h, cudaMemcpyAsync(out, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1244,10 +1435,14 @@ int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t npr
   cudaStream_t st = h->stream;
   double* alpha = h->d_T + n * p;  // last column
   KM_CUDA(h, cudaMemcpyAsync(alpha, y, sizeof(double) * n, cudaMemcpyHostToDevice, st));
-  if ((rc = nested_fwd(h, alpha, 1)) != KM_OK) return rc;
-  if ((rc = nested_bwd(h, alpha, 1)) != KM_OK) return rc;
+  if ((rc = nested_solve(h, alpha, 1)) != KM_OK) return rc;
   double ld = 0.0;
-  KLV(h, KM_PROF_OTHER, launch_logdet(h->d_Lf, t, h->d_L22, h->r, h->d_partial, kLogdetBlocks, h->d_scalar, st));
+  if (h->mixed)
+    KLV(h, KM_PROF_OTHER, launch_logdet<ff>(P<ff>(h->d_Lf), t, P<ff>(h->d_L22), h->r, h->d_partial, kLogdetBlocks,
+                                            h->d_scalar, st));
+  else
+    KLV(h, KM_PROF_OTHER, launch_logdet<double>(h->d_Lf, t, h->d_L22, h->r, h->d_partial, kLogdetBlocks,
+                                                h->d_scalar, st));
   KM_CUDA(h, cudaMemcpyAsync(&ld, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st));
   std::vector<double> a(n);
   KM_CUDA(h, cudaMemcpyAsync(a.data(), alpha, sizeof(double) * n, cudaMemcpyDeviceToHost, st));

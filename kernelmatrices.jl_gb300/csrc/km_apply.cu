@@ -19,227 +19,200 @@
 
 namespace km {
 
+template <typename T>
 struct NodeMats {
-  const double* Ct;
-  const double* L22;
-  const double* Eref;
-  const double* Etau;
+  const T* Ct;    // r x r
+  const T* L22;   // r x r lower
+  const T* L22i;  // r x r lower, inverse of L22
+  const T* E;     // 2r x r explicit transfer
   int r;
 };
-
-// x (2r, warp-shared) <- reflectors applied in order j = 0..r-1 (E' x, fwd) or j = r-1..0
-// (E x).  Reflector j = [e_j ; Es[:, j]] with tau ts[j]; Es is r x r with leading dim ld.
-__device__ __forceinline__ void apply_node_reflectors(const double* Es, const double* ts, int r, int ld,
-                                                      double* x, bool fwd) {
-  const int lane = threadIdx.x & 31;
-  for (int q = 0; q < r; ++q) {
-    const int j = fwd ? q : r - 1 - q;
-    const double tj = ts[j];
-    if (tj == 0.0) continue;
-    const double* v = Es + j * ld;
-    double acc = 0.0;
-    for (int i = lane; i < r; i += 32) acc += v[i] * x[r + i];
-    acc = warp_sum(acc);
-    acc = (acc + x[j]) * tj;
-    __syncwarp();
-    if (lane == 0) x[j] -= acc;
-    for (int i = lane; i < r; i += 32) x[r + i] -= acc * v[i];
-    __syncwarp();
-  }
-}
 
 // up-sweep modes
 enum { UP_PROJ = 0, UP_FWD = 1, UP_MULT = 2, UP_SUM = 3 };
 // down-sweep modes
 enum { DN_FWD = 0, DN_BWD = 1, DN_MUL = 2, DN_MULT = 3, DN_NYS = 4 };
 
-// Stages the node's Ct, L22, Eref (leading dimension r+1) and tau in shared memory.
-__device__ __forceinline__ void stage_node(const NodeMats& nm, int64_t node, double* Cs, double* Ls,
-                                           double* Es, double* ts) {
-  const int r = nm.r, ld = r + 1;
-  const int64_t off = node * (int64_t)r * r;
-  for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
-    const int i = e % r, c = e / r;
-    Cs[i + c * ld] = nm.Ct[off + e];
-    Ls[i + c * ld] = nm.L22[off + e];
-    Es[i + c * ld] = nm.Eref[off + e];
+// sum_l a[l*sa] b[l], l < n, with four independent partial sums (ILP for float pairs)
+template <typename T>
+__device__ __forceinline__ T dot4(const T* __restrict__ a, int sa, const T* __restrict__ b, int n) {
+  T s0 = T(0.0), s1 = T(0.0), s2 = T(0.0), s3 = T(0.0);
+  int l = 0;
+  for (; l + 3 < n; l += 4) {
+    s0 += a[(int64_t)l * sa] * b[l];
+    s1 += a[(int64_t)(l + 1) * sa] * b[l + 1];
+    s2 += a[(int64_t)(l + 2) * sa] * b[l + 2];
+    s3 += a[(int64_t)(l + 3) * sa] * b[l + 3];
   }
-  for (int e = threadIdx.x; e < r; e += blockDim.x) ts[e] = nm.Etau[node * r + e];
-  __syncthreads();
+  for (; l < n; ++l) s0 += a[(int64_t)l * sa] * b[l];
+  return (s0 + s1) + (s2 + s3);
 }
 
-// grid = (nodes at level, ceil(k/8)), block 256: one warp per (node, column); the node's
-// matrices are shared by the CTA's 8 columns.
-__global__ void __launch_bounds__(256) k_up(NodeMats nm, int level, int L, int64_t cslot0, int64_t nslot0,
-                                            int64_t node0, double* __restrict__ VP, double* __restrict__ VD,
-                                            int k, int mode) {
-  extern __shared__ double sm[];
-  const int r = nm.r, ld = r + 1;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int col = blockIdx.y * 8 + w;
+constexpr int KC = 16;  // right-hand-side columns per CTA
+
+// grid = (nodes at level, ceil(k / KC)), block 256.  Every phase is a set of independent dot
+// products (one thread per output entry) separated by barriers; node matrices are read through
+// the L1 cache.
+template <typename T>
+__global__ void __launch_bounds__(512) k_up(NodeMats<T> nm, int level, int L, int64_t cslot0, int64_t nslot0,
+                                            int64_t node0, T* __restrict__ VP, T* __restrict__ VD, int k, int mode) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* z = reinterpret_cast<T*>(smraw);   // KC x 2r : [z1 ; z2] per column
+  const int r = nm.r, r2 = 2 * r;
+  T* tb = z + KC * r2;                    // KC x r
+  T* ub = tb + KC * r;                    // KC x r
   const int64_t kk = blockIdx.x;
   const int64_t node = node0 + kk;
-  double* Cs = sm;
-  double* Ls = Cs + r * ld;
-  double* Es = Ls + r * ld;
-  double* ts = Es + r * ld;
-  const bool mats = (mode != UP_SUM);
-  double* x = (mats ? ts + r : sm) + (size_t)w * 3 * r;  // [0,2r): x   [2r,3r): t
-  double* t = x + 2 * r;
-  if (mats) stage_node(nm, node, Cs, Ls, Es, ts);
-  if (col >= k) return;
-  const double* z1 = VP + ((cslot0 + 2 * kk) * k + col) * r;
-  const double* z2 = VP + ((cslot0 + 2 * kk + 1) * k + col) * r;
-  for (int i = lane; i < r; i += 32) {
-    x[i] = z1[i];
-    x[r + i] = z2[i];
+  const int c0 = blockIdx.y * KC;
+  const int kc = min(KC, k - c0);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int e = tid; e < kc * r2; e += nth) {
+    const int c = e / r2, i = e % r2;
+    const int64_t slot = cslot0 + 2 * kk + (i >= r ? 1 : 0);
+    z[c * r2 + i] = VP[(slot * k + c0 + c) * r + (i >= r ? i - r : i)];
   }
-  __syncwarp();
+  __syncthreads();
+  const T* Ct = nm.Ct + node * (int64_t)r * r;
+  const T* L22 = nm.L22 + node * (int64_t)r * r;
+  const T* L22i = nm.L22i + node * (int64_t)r * r;
   if (mode == UP_SUM) {
-    if (level < L) {
-      double* out = VP + ((nslot0 + kk) * k + col) * r;
-      for (int i = lane; i < r; i += 32) out[i] = x[i] + x[r + i];
-    }
+    if (level < L)
+      for (int e = tid; e < kc * r; e += nth) {
+        const int c = e / r, i = e % r;
+        VP[((nslot0 + kk) * k + c0 + c) * r + i] = z[c * r2 + i] + z[c * r2 + r + i];
+      }
     return;
   }
   if (mode == UP_FWD) {
     // t = z2 - Ct' z1
-    for (int i = lane; i < r; i += 32) {
-      const double* ci = Cs + i * ld;
-      double acc = 0.0;
-#pragma unroll 8
-      for (int l = 0; l < r; ++l) acc += ci[l] * x[l];
-      t[i] = x[r + i] - acc;
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, i = e % r;
+      const T* z1 = z + c * r2;
+      tb[c * r + i] = z1[r + i] - dot4(Ct + (int64_t)i * r, 1, z1, r);
     }
-    __syncwarp();
-    // w = L22^{-1} t (in t)
-    for (int l = 0; l < r; ++l) {
-      const double wl = t[l] / Ls[l * ld + l];
-      __syncwarp();
-      if (lane == 0) t[l] = wl;
-      for (int i = l + 1 + lane; i < r; i += 32) t[i] -= Ls[l * ld + i] * wl;
-      __syncwarp();
+    __syncthreads();
+    // w = L22^{-1} t
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, i = e % r;
+      ub[c * r + i] = dot4(L22i + i, r, tb + c * r, i + 1);
     }
-    double* d = VD + (node * k + col) * 2 * r;
-    for (int i = lane; i < r; i += 32) {
-      d[i] = x[r + i] - t[i];
-      x[r + i] = t[i];
+    __syncthreads();
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, i = e % r;
+      const T w = ub[c * r + i];
+      VD[(node * k + c0 + c) * 2 * r + i] = z[c * r2 + r + i] - w;
+      z[c * r2 + r + i] = w;
     }
-    __syncwarp();
+    __syncthreads();
   } else if (mode == UP_MULT) {
     // D1 = Ct z2 ; D2 = L22' z2 - z2
-    double* d = VD + (node * k + col) * 2 * r;
-    for (int i = lane; i < r; i += 32) {
-      double a1 = 0.0, a2 = 0.0;
-#pragma unroll 8
-      for (int l = 0; l < r; ++l) a1 += Cs[i + l * ld] * x[r + l];
-      for (int l = i; l < r; ++l) a2 += Ls[l + i * ld] * x[r + l];
-      a2 -= x[r + i];
-      d[i] = a1;
-      d[r + i] = a2;
-      t[i] = a2;
-      x[i] += a1;
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, i = e % r;
+      const T* z2 = z + c * r2 + r;
+      const T a1 = dot4(Ct + i, r, z2, r);
+      const T a2 = dot4(L22 + (int64_t)i * r + i, 1, z2 + i, r - i) - z2[i];
+      tb[c * r + i] = a1;
+      ub[c * r + i] = a2;
+      VD[(node * k + c0 + c) * 2 * r + i] = a1;
+      VD[(node * k + c0 + c) * 2 * r + r + i] = a2;
     }
-    __syncwarp();
-    for (int i = lane; i < r; i += 32) x[r + i] += t[i];
-    __syncwarp();
+    __syncthreads();
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, i = e % r;
+      z[c * r2 + i] += tb[c * r + i];
+      z[c * r2 + r + i] += ub[c * r + i];
+    }
+    __syncthreads();
   }
   if (level < L) {
-    apply_node_reflectors(Es, ts, r, ld, x, true);
-    double* out = VP + ((nslot0 + kk) * k + col) * r;
-    for (int i = lane; i < r; i += 32) out[i] = x[i];
+    const T* E = nm.E + node * (int64_t)r2 * r;
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, q = e % r;
+      VP[((nslot0 + kk) * k + c0 + c) * r + q] = dot4(E + (int64_t)q * r2, 1, z + c * r2, r2);
+    }
   }
 }
 
-__global__ void __launch_bounds__(256) k_down(NodeMats nm, int level, int L, int64_t cslot0, int64_t nslot0,
-                                              int64_t node0, const double* __restrict__ VP,
-                                              double* __restrict__ VG, const double* __restrict__ VD,
-                                              int k, int mode) {
-  extern __shared__ double sm[];
-  const int r = nm.r, ld = r + 1;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int col = blockIdx.y * 8 + w;
+template <typename T>
+__global__ void __launch_bounds__(512) k_down(NodeMats<T> nm, int level, int L, int64_t cslot0, int64_t nslot0,
+                                              int64_t node0, const T* __restrict__ VP, T* __restrict__ VG,
+                                              const T* __restrict__ VD, int k, int mode) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* g = reinterpret_cast<T*>(smraw);   // KC x r  (parent coefficient)
+  const int r = nm.r, r2 = 2 * r;
+  T* base = g + KC * r;                   // KC x 2r (E g)
+  T* tb = base + KC * r2;                 // KC x 2r scratch
   const int64_t kk = blockIdx.x;
   const int64_t node = node0 + kk;
+  const int c0 = blockIdx.y * KC;
+  const int kc = min(KC, k - c0);
+  const int tid = threadIdx.x, nth = blockDim.x;
   const bool top = (level >= L);
-  double* Cs = sm;
-  double* Ls = Cs + r * ld;
-  double* Es = Ls + r * ld;
-  double* ts = Es + r * ld;
-  const bool mats = (mode != DN_NYS);
-  double* x = (mats ? ts + r : sm) + (size_t)w * 4 * r;  // [0,2r): base   [2r,4r): scratch
-  double* t = x + 2 * r;
-  if (mats) stage_node(nm, node, Cs, Ls, Es, ts);
-  if (col >= k) return;
-  const double* g = VG + ((nslot0 + kk) * k + col) * r;
-  for (int i = lane; i < r; i += 32) {
-    x[i] = top ? 0.0 : g[i];
-    x[r + i] = 0.0;
+  for (int e = tid; e < kc * r; e += nth) {
+    const int c = e / r, i = e % r;
+    g[c * r + i] = top ? T(0.0) : VG[((nslot0 + kk) * k + c0 + c) * r + i];
   }
-  __syncwarp();
-  double* g1 = VG + ((cslot0 + 2 * kk) * k + col) * r;
-  double* g2 = VG + ((cslot0 + 2 * kk + 1) * k + col) * r;
-  const double* p1 = VP + ((cslot0 + 2 * kk) * k + col) * r;
-  const double* p2 = VP + ((cslot0 + 2 * kk + 1) * k + col) * r;
+  __syncthreads();
+  auto child = [&](int side, int c, int i) -> int64_t { return ((cslot0 + 2 * kk + side) * k + c0 + c) * r + i; };
   if (mode == DN_NYS) {
     // coefficient sums: child c1 gets parent + phi(c2), child c2 gets parent + phi(c1)
-    for (int i = lane; i < r; i += 32) {
-      const double b = x[i];
-      g1[i] = b + p2[i];
-      g2[i] = b + p1[i];
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, i = e % r;
+      const T b = g[c * r + i];
+      const T p1 = VP[child(0, c, i)], p2 = VP[child(1, c, i)];
+      VG[child(0, c, i)] = b + p2;
+      VG[child(1, c, i)] = b + p1;
     }
     return;
   }
-  if (!top) apply_node_reflectors(Es, ts, r, ld, x, false);
-  if (mode == DN_FWD) {
-    const double* d = VD + (node * k + col) * 2 * r;
-    for (int i = lane; i < r; i += 32) {
-      g1[i] = x[i];
-      g2[i] = x[r + i] + d[i];
-    }
-  } else if (mode == DN_MULT) {
-    const double* d = VD + (node * k + col) * 2 * r;
-    for (int i = lane; i < r; i += 32) {
-      g1[i] = x[i] + d[i];
-      g2[i] = x[r + i] + d[r + i];
+  const T* E = nm.E + node * (int64_t)r2 * r;
+  for (int e = tid; e < kc * r2; e += nth) {
+    const int c = e / r2, i = e % r2;
+    base[c * r2 + i] = top ? T(0.0) : dot4(E + i, r2, g + c * r, r);
+  }
+  __syncthreads();
+  const T* Ct = nm.Ct + node * (int64_t)r * r;
+  const T* L22 = nm.L22 + node * (int64_t)r * r;
+  const T* L22i = nm.L22i + node * (int64_t)r * r;
+  if (mode == DN_FWD || mode == DN_MULT) {
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, i = e % r;
+      const T* d = VD + (node * k + c0 + c) * 2 * r;
+      VG[child(0, c, i)] = (mode == DN_MULT) ? base[c * r2 + i] + d[i] : base[c * r2 + i];
+      VG[child(1, c, i)] = base[c * r2 + r + i] + d[(mode == DN_MULT ? r : 0) + i];
     }
   } else if (mode == DN_BWD) {
-    // z2 = p2 - base_bot (kept in t[r..2r)), then t[0..r) = L22^{-T} z2
-    for (int i = lane; i < r; i += 32) {
-      const double z2 = p2[i] - x[r + i];
-      t[r + i] = z2;
-      t[i] = z2;
+    // z2 = p2 - base_bot ; t = L22^{-T} z2 ; g1 = base_top + Ct t ; g2 = base_bot + z2 - t
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, i = e % r;
+      tb[c * r2 + r + i] = VP[child(1, c, i)] - base[c * r2 + r + i];
     }
-    __syncwarp();
-    for (int i = r - 1; i >= 0; --i) {
-      const double xi = t[i] / Ls[i * ld + i];
-      __syncwarp();
-      if (lane == 0) t[i] = xi;
-      for (int l = lane; l < i; l += 32) t[l] -= Ls[i + l * ld] * xi;
-      __syncwarp();
+    __syncthreads();
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, i = e % r;
+      const T* z2 = tb + c * r2 + r;
+      tb[c * r2 + i] = dot4(L22i + (int64_t)i * r + i, 1, z2 + i, r - i);
     }
-    for (int i = lane; i < r; i += 32) {
-      double acc = 0.0;
-#pragma unroll 8
-      for (int l = 0; l < r; ++l) acc += Cs[i + l * ld] * t[l];
-      g1[i] = x[i] + acc;
-      g2[i] = x[r + i] + t[r + i] - t[i];
+    __syncthreads();
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, i = e % r;
+      const T* tc = tb + c * r2;
+      const T acc = dot4(Ct + i, r, tc, r);
+      VG[child(0, c, i)] = base[c * r2 + i] + acc;
+      VG[child(1, c, i)] = base[c * r2 + r + i] + tc[r + i] - tc[i];
     }
-  } else {  // DN_MUL
-    for (int i = lane; i < r; i += 32) {
-      t[i] = p1[i] + x[i];
-      t[r + i] = p2[i] + x[r + i];
+  } else {  // DN_MUL: z = p + base ; D2 = Ct' z1 + L22 z2 - z2
+    for (int e = tid; e < kc * r2; e += nth) {
+      const int c = e / r2, i = e % r2;
+      tb[c * r2 + i] = VP[child(i >= r ? 1 : 0, c, i % r)] + base[c * r2 + i];
     }
-    __syncwarp();
-    for (int i = lane; i < r; i += 32) {
-      double acc = 0.0;
-      const double* ci = Cs + i * ld;
-#pragma unroll 8
-      for (int l = 0; l < r; ++l) acc += ci[l] * t[l];
-      for (int l = 0; l <= i; ++l) acc += Ls[i + l * ld] * t[r + l];
-      acc -= t[r + i];
-      g1[i] = x[i];
-      g2[i] = x[r + i] + acc;
+    __syncthreads();
+    for (int e = tid; e < kc * r; e += nth) {
+      const int c = e / r, i = e % r;
+      const T* zc = tb + c * r2;
+      const T acc = dot4(Ct + (int64_t)i * r, 1, zc, r) + dot4(L22 + i, r, zc + r, i + 1) - zc[r + i];
+      VG[child(0, c, i)] = base[c * r2 + i];
+      VG[child(1, c, i)] = base[c * r2 + r + i] + acc;
     }
   }
 }
@@ -336,24 +309,27 @@ static inline int64_t child_slot0(const Tree& t, int level) {
   return level == 1 ? 0 : t.nleaf + t.node_off[level - 1];
 }
 
-void launch_up(const Tree& t, const NodeMatsH& h, int level, double* VP, double* VD, int k, int mode,
-               cudaStream_t st) {
-  NodeMats nm{h.Ct, h.L22, h.Eref, h.Etau, h.r};
-  dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + 7) / 8));
-  const size_t sm = ((mode != UP_SUM_) ? (size_t)3 * h.r * (h.r + 1) + h.r : 0) * sizeof(double) + (size_t)8 * 3 * h.r * sizeof(double);
-  cudaFuncSetAttribute(k_up, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_up<<<grid, 256, sm, st>>>(
-      nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level], t.node_off[level], VP, VD, k, mode);
+template <typename T>
+void launch_up(const Tree& t, const NodeMatsH& h, int level, T* VP, T* VD, int k, int mode, cudaStream_t st) {
+  NodeMats<T> nm{reinterpret_cast<const T*>(h.Ct), reinterpret_cast<const T*>(h.L22),
+                 reinterpret_cast<const T*>(h.L22i), reinterpret_cast<const T*>(h.E), h.r};
+  dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + KC - 1) / KC));
+  const size_t sm = (size_t)KC * 4 * h.r * sizeof(T);
+  cudaFuncSetAttribute(k_up<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_up<T><<<grid, 512, sm, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
+                                 t.node_off[level], VP, VD, k, mode);
 }
 
-void launch_down(const Tree& t, const NodeMatsH& h, int level, const double* VP, double* VG,
-                 const double* VD, int k, int mode, cudaStream_t st) {
-  NodeMats nm{h.Ct, h.L22, h.Eref, h.Etau, h.r};
-  dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + 7) / 8));
-  const size_t sm = ((mode != DN_NYS_) ? (size_t)3 * h.r * (h.r + 1) + h.r : 0) * sizeof(double) + (size_t)8 * 4 * h.r * sizeof(double);
-  cudaFuncSetAttribute(k_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_down<<<grid, 256, sm, st>>>(
-      nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level], t.node_off[level], VP, VG, VD, k, mode);
+template <typename T>
+void launch_down(const Tree& t, const NodeMatsH& h, int level, const T* VP, T* VG, const T* VD, int k, int mode,
+                 cudaStream_t st) {
+  NodeMats<T> nm{reinterpret_cast<const T*>(h.Ct), reinterpret_cast<const T*>(h.L22),
+                 reinterpret_cast<const T*>(h.L22i), reinterpret_cast<const T*>(h.E), h.r};
+  dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + KC - 1) / KC));
+  const size_t sm = (size_t)KC * 5 * h.r * sizeof(T);
+  cudaFuncSetAttribute(k_down<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_down<T><<<grid, 512, sm, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
+                                   t.node_off[level], VP, VG, VD, k, mode);
 }
 
 void launch_leaf_phiT(const double* Phi, int r, const Tree& t, const double* X, int64_t ldx, double* VP,
@@ -363,7 +339,6 @@ void launch_leaf_phiT(const double* Phi, int r, const Tree& t, const double* X, 
   cudaFuncSetAttribute(k_leaf_phiT, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k_leaf_phiT<<<grid, 256, sm, st>>>(Phi, r, dtree(t), X, ldx, VP, k);
 }
-
 void launch_leaf_nys_apply(const double* Kl, const double* Phi, const double* Sc, int r, const Tree& t,
                            const double* X, int64_t ldx, const double* VG, double* Y, int64_t ldy, int k,
                            cudaStream_t st) {
@@ -372,5 +347,11 @@ void launch_leaf_nys_apply(const double* Kl, const double* Phi, const double* Sc
   cudaFuncSetAttribute(k_leaf_nys_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k_leaf_nys_apply<<<grid, 256, sm, st>>>(Kl, Phi, Sc, r, dtree(t), X, ldx, VG, Y, ldy, k);
 }
+
+template void launch_up<double>(const Tree&, const NodeMatsH&, int, double*, double*, int, int, cudaStream_t);
+template void launch_up<ff>(const Tree&, const NodeMatsH&, int, ff*, ff*, int, int, cudaStream_t);
+template void launch_down<double>(const Tree&, const NodeMatsH&, int, const double*, double*, const double*, int, int,
+                                  cudaStream_t);
+template void launch_down<ff>(const Tree&, const NodeMatsH&, int, const ff*, ff*, const ff*, int, int, cudaStream_t);
 
 }  // namespace km

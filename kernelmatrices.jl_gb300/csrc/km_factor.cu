@@ -13,6 +13,8 @@
 // gives the node basis Q_N = blockdiag(Q_c1, Q_c2) E_N.  Only r x r work is left above the
 // leaves; the factor is the reference's up to the rounding freedom of the QR of rank-deficient
 // panels.  Orthogonal factors are kept in Householder (LAPACK dgeqrf-style) form.
+#include <type_traits>
+
 #include "km_kernels.h"
 
 namespace km {
@@ -56,21 +58,22 @@ __global__ void k_chol_small(double* __restrict__ A, int n, int* __restrict__ in
 // The current column panel (rows below the diagonal block) lives in shared memory.
 // info[j] = first failing column (1-based) of leaf j, 0 if positive definite.
 // ---------------------------------------------------------------------------------------------
-template <int NB>
-__global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K, double* __restrict__ Lf,
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K, T* __restrict__ Lf,
                                                    DTree t, int* __restrict__ info) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
   const int64_t leaf = blockIdx.x;
   const int m = d_leaf_size(t, leaf);
   const int64_t off = d_leaf_koff(t, leaf);
   const double* A0 = K + off;
-  double* A = Lf + off;
+  T* A = Lf + off;
   constexpr int LDP = NB + 1;
-  double* P = sm;                    // (m) x LDP, row-major panel rows
-  double* D = sm + (size_t)m * LDP;  // NB x LDP
+  T* P = sm;                    // (m) x LDP, row-major panel rows
+  T* D = sm + (size_t)m * LDP;  // NB x LDP
   const int tid = threadIdx.x, nth = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
-  for (int64_t e = tid; e < (int64_t)m * m; e += nth) A[e] = A0[e];
+  for (int64_t e = tid; e < (int64_t)m * m; e += nth) A[e] = from_double<T>(A0[e]);
   __syncthreads();
   int bad = 0;
   for (int k0 = 0; k0 < m; k0 += NB) {
@@ -82,10 +85,10 @@ __global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K,
     }
     __syncthreads();
     for (int j = 0; j < kb; ++j) {
-      const double d = D[j * LDP + j];
+      const T d = D[j * LDP + j];
       const bool ok = d > 0.0;
       if (!ok && bad == 0) bad = k0 + j + 1;
-      const double sd = ok ? sqrt(d) : 1.0;
+      const T sd = ok ? sqrt(d) : T(1.0);
       __syncthreads();
       for (int i = j + 1 + tid; i < kb; i += nth) D[i * LDP + j] /= sd;
       if (tid == 0) D[j * LDP + j] = sd;
@@ -105,11 +108,11 @@ __global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K,
     const int r0 = k0 + kb, mr = m - r0;
     for (int ii = tid; ii < mr; ii += nth) {
       const int i = r0 + ii;
-      double x[NB];
+      T x[NB];
 #pragma unroll
       for (int c = 0; c < NB; ++c) {
         if (c < kb) {
-          double v = A[(int64_t)(k0 + c) * m + i];
+          T v = A[(int64_t)(k0 + c) * m + i];
           for (int l = 0; l < c; ++l) v -= x[l] * D[c * LDP + l];
           x[c] = v / D[c * LDP + c];
         }
@@ -125,12 +128,12 @@ __global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K,
     __syncthreads();
     // (3) trailing update of the lower triangle: A[i, c] -= sum_l P[i,l] P[c,l]
     for (int cc = warp; cc < mr; cc += nwarp) {
-      double pc[NB];
+      T pc[NB];
 #pragma unroll
-      for (int l = 0; l < NB; ++l) pc[l] = (l < kb) ? P[cc * LDP + l] : 0.0;
-      double* col = A + (int64_t)(r0 + cc) * m + r0;
+      for (int l = 0; l < NB; ++l) pc[l] = (l < kb) ? P[cc * LDP + l] : T(0.0);
+      T* col = A + (int64_t)(r0 + cc) * m + r0;
       for (int ii = cc + lane; ii < mr; ii += 32) {
-        double acc = 0.0;
+        T acc = T(0.0);
 #pragma unroll
         for (int l = 0; l < NB; ++l) acc += P[ii * LDP + l] * pc[l];
         col[ii] -= acc;
@@ -149,17 +152,18 @@ __global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K,
 // v = x/(alpha-beta); a zero column x gives tau = 0 (H = I).  One CTA per leaf; the panel is
 // copied to shared memory when it fits.
 // ---------------------------------------------------------------------------------------------
-template <bool SMEM>
-__global__ void __launch_bounds__(256) k_leaf_qr(double* __restrict__ Pan, int r, DTree t,
-                                                 double* __restrict__ tau, double* __restrict__ Rout) {
-  extern __shared__ double sm[];
-  __shared__ double red[8];
-  __shared__ double sh_tau;
+template <typename T, bool SMEM>
+__global__ void __launch_bounds__(256) k_leaf_qr(T* __restrict__ Pan, int r, DTree t,
+                                                 T* __restrict__ tau, T* __restrict__ Rout) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
+  __shared__ T red[8];
+  __shared__ T sh_tau;
   const int64_t leaf = blockIdx.x;
   const int m = d_leaf_size(t, leaf);
   const int64_t s = d_leaf_start(t, leaf);
-  double* G = Pan + s * r;
-  double* A = SMEM ? sm : G;
+  T* G = Pan + s * r;
+  T* A = SMEM ? sm : G;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   if (SMEM) {
     for (int64_t e = tid; e < (int64_t)m * r; e += blockDim.x) sm[e] = G[e];
@@ -167,49 +171,94 @@ __global__ void __launch_bounds__(256) k_leaf_qr(double* __restrict__ Pan, int r
   }
   const int kmax = min(m, r);
   for (int j = 0; j < kmax; ++j) {
-    double* aj = A + (int64_t)j * m;
-    double part = 0.0;
+    T* aj = A + (int64_t)j * m;
+    T part = T(0.0);
     for (int i = j + 1 + tid; i < m; i += blockDim.x) part += aj[i] * aj[i];
-    part = warp_sum(part);
+    part = warp_sum_t(part);
     if (lane == 0) red[w] = part;
     __syncthreads();
     if (tid == 0) {
-      double sig = 0.0;
+      T sig = T(0.0);
       for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sig += red[q];
-      const double alpha = aj[j];
-      double tj = 0.0, beta = alpha, scal = 0.0;
+      const T alpha = aj[j];
+      T tj = T(0.0), beta = alpha, scal = T(0.0);
       if (sig != 0.0) {
-        const double nrm = sqrt(alpha * alpha + sig);
+        const T nrm = sqrt(alpha * alpha + sig);
         beta = alpha >= 0.0 ? -nrm : nrm;
         tj = (beta - alpha) / beta;
-        scal = 1.0 / (alpha - beta);
+        scal = T(1.0) / (alpha - beta);
       }
       aj[j] = beta;
       red[0] = scal;
       sh_tau = tj;
     }
     __syncthreads();
-    const double scal = red[0], tj = sh_tau;
+    const T scal = red[0], tj = sh_tau;
     for (int i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= scal;
     if (tid == 0) tau[leaf * r + j] = tj;
     __syncthreads();
     if (tj != 0.0) {
       // apply H_j = I - tau v v' to columns c > j (one warp per column)
       for (int c = j + 1 + w; c < r; c += (int)(blockDim.x >> 5)) {
-        double* ac = A + (int64_t)c * m;
-        double acc = (lane == 0) ? ac[j] : 0.0;
+        T* ac = A + (int64_t)c * m;
+        T acc = (lane == 0) ? ac[j] : T(0.0);
         for (int i = j + 1 + lane; i < m; i += 32) acc += aj[i] * ac[i];
-        acc = warp_sum(acc) * tj;
+        acc = warp_sum_t(acc) * tj;
         if (lane == 0) ac[j] -= acc;
         for (int i = j + 1 + lane; i < m; i += 32) ac[i] -= acc * aj[i];
       }
     }
     __syncthreads();
   }
-  for (int j = kmax + tid; j < r; j += blockDim.x) tau[leaf * r + j] = 0.0;
+  for (int j = kmax + tid; j < r; j += blockDim.x) tau[leaf * r + j] = T(0.0);
   for (int e = tid; e < r * r; e += blockDim.x) {
     const int i = e % r, c = e / r;
-    Rout[leaf * (int64_t)r * r + e] = (i <= c && i < m) ? A[(int64_t)c * m + i] : 0.0;
+    Rout[leaf * (int64_t)r * r + e] = (i <= c && i < m) ? A[(int64_t)c * m + i] : T(0.0);
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int64_t e = tid; e < (int64_t)m * r; e += blockDim.x) G[e] = sm[e];
+  }
+}
+
+
+// Explicit leaf basis Q = H_0 ... H_{r-1} [I; 0] in place of the reflectors (LAPACK dorg2r).
+// Runs on the side stream, overlapped with the node levels (only the solves need Q).
+template <typename T, bool SMEM>
+__global__ void __launch_bounds__(256) k_leaf_formq(T* __restrict__ Pan, const T* __restrict__ tau, int r, DTree t) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf);
+  T* G = Pan + s * r;
+  T* A = SMEM ? sm : G;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (SMEM) {
+    for (int64_t e = tid; e < (int64_t)m * r; e += blockDim.x) sm[e] = G[e];
+  }
+  const int kmax = min(m, r);
+  __syncthreads();
+  // explicit Q = H_0 ... H_{r-1} [I; 0] in place (LAPACK dorg2r)
+  for (int j = kmax - 1; j >= 0; --j) {
+    T* aj = A + (int64_t)j * m;
+    const T tj = tau[leaf * r + j];
+    if (j < r - 1) {
+      if (tid == 0) aj[j] = T(1.0);
+      __syncthreads();
+      for (int c = j + 1 + w; c < r; c += (int)(blockDim.x >> 5)) {
+        T* ac = A + (int64_t)c * m;
+        T acc = T(0.0);
+        for (int i = j + lane; i < m; i += 32) acc += aj[i] * ac[i];
+        acc = warp_sum_t(acc) * tj;
+        for (int i = j + lane; i < m; i += 32) ac[i] -= acc * aj[i];
+      }
+      __syncthreads();
+    }
+    for (int i = j + 1 + tid; i < m; i += blockDim.x) aj[i] = -(tj * aj[i]);
+    for (int i = tid; i < j; i += blockDim.x) aj[i] = T(0.0);
+    if (tid == 0) aj[j] = T(1.0) - tj;
+    __syncthreads();
   }
   if (SMEM) {
     __syncthreads();
@@ -228,23 +277,25 @@ __global__ void __launch_bounds__(256) k_leaf_qr(double* __restrict__ Pan, int r
 // Outputs per node: Ct, L22 (lower), Eref (r x r), Etau (r), R_N into slot N.
 // Shared memory: four r x (r+1) matrices.
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, const double* __restrict__ SinvT,
+template <typename T>
+__global__ void __launch_bounds__(256) k_node_factor(T* __restrict__ R, const T* __restrict__ SinvT,
                                                      int r, int level, int L, int64_t nleaf,
-                                                     int64_t cbase, int64_t nbase, double* __restrict__ Ct_out,
-                                                     double* __restrict__ L22_out, double* __restrict__ Eref,
-                                                     double* __restrict__ Etau, int* __restrict__ info) {
-  extern __shared__ double sm[];
-  __shared__ double red[8];
-  __shared__ double sh[2];
+                                                     int64_t cbase, int64_t nbase, T* __restrict__ Ct_out,
+                                                     T* __restrict__ L22_out, T* __restrict__ Eref,
+                                                     T* __restrict__ Etau, int* __restrict__ info) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
+  __shared__ T red[32];
+  __shared__ T sh[2];
   const int ld = r + 1;
-  double* X0 = sm;
-  double* X1 = X0 + r * ld;
-  double* X2 = X1 + r * ld;
-  double* X3 = X2 + r * ld;
+  T* X0 = sm;
+  T* X1 = X0 + r * ld;
+  T* X2 = X1 + r * ld;
+  T* X3 = X2 + r * ld;
   const int64_t k = blockIdx.x;
   const int64_t node = nbase + k;  // node index within all nodes (level-major)
-  const double* R1 = R + (cbase + 2 * k) * (int64_t)r * r;
-  const double* R2 = R + (cbase + 2 * k + 1) * (int64_t)r * r;
+  const T* R1 = R + (cbase + 2 * k) * (int64_t)r * r;
+  const T* R2 = R + (cbase + 2 * k + 1) * (int64_t)r * r;
   const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
   // load: X0 = Sc^{-T} (upper), X1 = R1, X2 = R2   (element (i,c) at i + c*ld)
   for (int e = tid; e < r * r; e += nth) {
@@ -257,7 +308,7 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
   // T1 = R1 Sc^{-T} -> X3 (upper x upper: entries l in [i, c])
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
-    double acc = 0.0;
+    T acc = T(0.0);
     if (i <= c) {
 #pragma unroll 4
       for (int l = i; l <= c; ++l) acc += X1[i + l * ld] * X0[l + c * ld];
@@ -268,7 +319,7 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
   // T2 = R2 Sc^{-T} -> X1
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
-    double acc = 0.0;
+    T acc = T(0.0);
     if (i <= c) {
 #pragma unroll 4
       for (int l = i; l <= c; ++l) acc += X2[i + l * ld] * X0[l + c * ld];
@@ -279,7 +330,7 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
   // Ct = T1 T2' -> X0 ; Ct[i][c] = sum_{l >= max(i,c)} T1[i][l] T2[c][l]
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
-    double acc = 0.0;
+    T acc = T(0.0);
 #pragma unroll 4
     for (int l = max(i, c); l < r; ++l) acc += X3[i + l * ld] * X1[c + l * ld];
     X0[i + c * ld] = acc;
@@ -289,20 +340,20 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
     if (i >= c) {
-      double acc = 0.0;
+      T acc = T(0.0);
 #pragma unroll 4
       for (int l = 0; l < r; ++l) acc += X0[l + i * ld] * X0[l + c * ld];
-      X3[i + c * ld] = (i == c ? 1.0 : 0.0) - acc;
+      X3[i + c * ld] = T(i == c ? 1.0 : 0.0) - acc;
     }
   }
   __syncthreads();
   // L22 = chol(H) in place (lower)
   int bad = 0;
   for (int j = 0; j < r; ++j) {
-    const double d = X3[j + j * ld];
+    const T d = X3[j + j * ld];
     const bool ok = d > 0.0;
     if (!ok && bad == 0) bad = j + 1;
-    const double sd = ok ? sqrt(d) : 1.0;
+    const T sd = ok ? sqrt(d) : T(1.0);
     __syncthreads();
     for (int i = j + 1 + tid; i < r; i += nth) X3[i + j * ld] /= sd;
     if (tid == 0) X3[j + j * ld] = sd;
@@ -319,9 +370,10 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
     Ct_out[node * (int64_t)r * r + e] = X0[i + c * ld];
-    L22_out[node * (int64_t)r * r + e] = (i >= c) ? X3[i + c * ld] : 0.0;
+    L22_out[node * (int64_t)r * r + e] = (i >= c) ? X3[i + c * ld] : T(0.0);
   }
   if (level >= L) return;
+  __syncthreads();
   // reload R1 -> X1 (X2 still holds R2)
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
@@ -331,7 +383,7 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
   // B = R2 - Ct' R1 -> X2 (column c of R1 has entries l <= c)
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
-    double acc = 0.0;
+    T acc = T(0.0);
 #pragma unroll 4
     for (int l = 0; l <= c; ++l) acc += X0[l + i * ld] * X1[l + c * ld];
     X2[i + c * ld] -= acc;
@@ -339,7 +391,7 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
   __syncthreads();
   // B <- L22^{-1} B, row by row with the whole CTA
   for (int i = 0; i < r; ++i) {
-    const double inv = 1.0 / X3[i + i * ld];
+    const T inv = T(1.0) / X3[i + i * ld];
     for (int c = tid; c < r; c += nth) X2[i + c * ld] *= inv;
     __syncthreads();
     const int rows = r - i - 1;
@@ -352,21 +404,21 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
   // structured Householder QR of [X1 (upper r x r) ; X2 (r x r)]:
   // reflector j acts on row j of the top and all r rows of the bottom.
   for (int j = 0; j < r; ++j) {
-    double part = 0.0;
+    T part = T(0.0);
     for (int i = tid; i < r; i += nth) part += X2[i + j * ld] * X2[i + j * ld];
-    part = warp_sum(part);
+    part = warp_sum_t(part);
     if (lane == 0) red[w] = part;
     __syncthreads();
     if (tid == 0) {
-      double sig = 0.0;
+      T sig = T(0.0);
       for (int q = 0; q < nw; ++q) sig += red[q];
-      const double alpha = X1[j + j * ld];
-      double tj = 0.0, beta = alpha, scal = 0.0;
+      const T alpha = X1[j + j * ld];
+      T tj = T(0.0), beta = alpha, scal = T(0.0);
       if (sig != 0.0) {
-        const double nrm = sqrt(alpha * alpha + sig);
+        const T nrm = sqrt(alpha * alpha + sig);
         beta = alpha >= 0.0 ? -nrm : nrm;
         tj = (beta - alpha) / beta;
-        scal = 1.0 / (alpha - beta);
+        scal = T(1.0) / (alpha - beta);
       }
       X1[j + j * ld] = beta;
       sh[0] = scal;
@@ -374,16 +426,16 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
       Etau[node * (int64_t)r + j] = tj;
     }
     __syncthreads();
-    const double scal = sh[0], tj = sh[1];
+    const T scal = sh[0], tj = sh[1];
     if (tj != 0.0) {
       // scaled reflector column v = X2[:, j] * scal is formed on the fly; each warp updates
       // whole columns c > j
       for (int c = j + 1 + w; c < r; c += nw) {
-        double acc = 0.0;
+        T acc = T(0.0);
         for (int i = lane; i < r; i += 32) acc += X2[i + j * ld] * X2[i + c * ld];
-        acc = (warp_sum(acc) * scal + X1[j + c * ld]) * tj;
+        acc = (warp_sum_t(acc) * scal + X1[j + c * ld]) * tj;
         if (lane == 0) X1[j + c * ld] -= acc;
-        const double f = acc * scal;
+        const T f = acc * scal;
         for (int i = lane; i < r; i += 32) X2[i + c * ld] -= f * X2[i + j * ld];
       }
     }
@@ -391,10 +443,10 @@ __global__ void __launch_bounds__(256) k_node_factor(double* __restrict__ R, con
     for (int i = tid; i < r; i += nth) X2[i + j * ld] *= scal;
     __syncthreads();
   }
-  double* Rn = R + (nleaf + node) * (int64_t)r * r;
+  T* Rn = R + (nleaf + node) * (int64_t)r * r;
   for (int e = tid; e < r * r; e += nth) {
     const int i = e % r, c = e / r;
-    Rn[e] = (i <= c) ? X1[i + c * ld] : 0.0;
+    Rn[e] = (i <= c) ? X1[i + c * ld] : T(0.0);
     Eref[node * (int64_t)r * r + e] = X2[i + c * ld];
   }
 }
@@ -420,7 +472,8 @@ __global__ void k_tri_inv_t(const double* __restrict__ Sc, int r, double* __rest
 // ---------------------------------------------------------------------------------------------
 // log det: 2 sum log diag(L_leaf) + 2 sum log |diag(L22)|, deterministic two-pass reduction.
 // ---------------------------------------------------------------------------------------------
-__global__ void k_logdet_partial(const double* __restrict__ Lf, DTree t, const double* __restrict__ L22,
+template <typename T>
+__global__ void k_logdet_partial(const T* __restrict__ Lf, DTree t, const T* __restrict__ L22,
                                  int r, int64_t nnode, double* __restrict__ partial) {
   __shared__ double red[8];
   const int64_t nleafdiag = t.n;
@@ -428,7 +481,7 @@ __global__ void k_logdet_partial(const double* __restrict__ Lf, DTree t, const d
   double acc = 0.0;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
        e += (int64_t)gridDim.x * blockDim.x) {
-    double d;
+    T d;
     if (e < nleafdiag) {
       // leaf containing row e
       const int64_t big = t.rem * (t.m0 + 1);
@@ -441,7 +494,7 @@ __global__ void k_logdet_partial(const double* __restrict__ Lf, DTree t, const d
       const int64_t node = q / r, i = q % r;
       d = L22[node * (int64_t)r * r + i * r + i];
     }
-    acc += 2.0 * log(fabs(d));
+    acc += 2.0 * log(fabs(to_double(d)));
   }
   acc = warp_sum(acc);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
@@ -472,34 +525,38 @@ bool launch_chol_small(double* A, int n, int* info, cudaStream_t st) {
   return true;
 }
 
-bool launch_leaf_chol(const double* K, double* Lf, const Tree& t, int* info, cudaStream_t st) {
+template <typename T, int NB>
+static void leaf_chol_launch(const double* K, T* Lf, const Tree& t, int* info, cudaStream_t st) {
+  const size_t sm = (size_t)(t.max_leaf + NB) * (NB + 1) * sizeof(T);
+  cudaFuncSetAttribute(k_leaf_chol<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_leaf_chol<T, NB><<<(unsigned)t.nleaf, 256, sm, st>>>(K, Lf, dtree(t), info);
+}
+
+template <typename T>
+bool launch_leaf_chol(const double* K, T* Lf, const Tree& t, int* info, cudaStream_t st) {
   const int64_t m = t.max_leaf;
-  auto fits = [&](int nb) { return (size_t)(m + nb) * (nb + 1) * sizeof(double) <= 200 * 1024; };
-  if (fits(32)) {
-    const size_t sm = (size_t)(m + 32) * 33 * sizeof(double);
-    cudaFuncSetAttribute(k_leaf_chol<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_leaf_chol<32><<<(unsigned)t.nleaf, 256, sm, st>>>(K, Lf, dtree(t), info);
+  auto fits = [&](int nb) { return (size_t)(m + nb) * (nb + 1) * sizeof(T) <= 200 * 1024; };
+  // float pairs need twice the registers per value: use the 16-wide panel for them
+  if (sizeof(T) == sizeof(double) && std::is_same<T, double>::value && fits(32)) {
+    leaf_chol_launch<T, 32>(K, Lf, t, info, st);
   } else if (fits(16)) {
-    const size_t sm = (size_t)(m + 16) * 17 * sizeof(double);
-    cudaFuncSetAttribute(k_leaf_chol<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_leaf_chol<16><<<(unsigned)t.nleaf, 256, sm, st>>>(K, Lf, dtree(t), info);
+    leaf_chol_launch<T, 16>(K, Lf, t, info, st);
   } else if (fits(8)) {
-    const size_t sm = (size_t)(m + 8) * 9 * sizeof(double);
-    cudaFuncSetAttribute(k_leaf_chol<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_leaf_chol<8><<<(unsigned)t.nleaf, 256, sm, st>>>(K, Lf, dtree(t), info);
+    leaf_chol_launch<T, 8>(K, Lf, t, info, st);
   } else {
     return false;
   }
   return true;
 }
 
-void launch_leaf_qr(double* Pan, int r, const Tree& t, double* tau, double* Rout, cudaStream_t st) {
-  const size_t sm = (size_t)t.max_leaf * r * sizeof(double);
+template <typename T>
+void launch_leaf_qr(T* Pan, int r, const Tree& t, T* tau, T* Rout, cudaStream_t st) {
+  const size_t sm = (size_t)t.max_leaf * r * sizeof(T);
   if (sm <= 200 * 1024) {
-    cudaFuncSetAttribute(k_leaf_qr<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_leaf_qr<true><<<(unsigned)t.nleaf, 256, sm, st>>>(Pan, r, dtree(t), tau, Rout);
+    cudaFuncSetAttribute(k_leaf_qr<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_leaf_qr<T, true><<<(unsigned)t.nleaf, 256, sm, st>>>(Pan, r, dtree(t), tau, Rout);
   } else {
-    k_leaf_qr<false><<<(unsigned)t.nleaf, 256, 0, st>>>(Pan, r, dtree(t), tau, Rout);
+    k_leaf_qr<T, false><<<(unsigned)t.nleaf, 256, 0, st>>>(Pan, r, dtree(t), tau, Rout);
   }
 }
 
@@ -509,21 +566,132 @@ void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st) {
   k_tri_inv_t<<<1, 128, sm, st>>>(Sc, r, SinvT);
 }
 
-void launch_node_factor(double* R, const double* SinvT, int r, int level, const Tree& t,
-                        double* Ct, double* L22, double* Eref, double* Etau, int* info,
-                        cudaStream_t st) {
-  const size_t sm = (size_t)4 * r * (r + 1) * sizeof(double);
-  cudaFuncSetAttribute(k_node_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+template <typename T>
+void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T* Ct, T* L22, T* Eref,
+                        T* Etau, int* info, cudaStream_t st) {
+  const size_t sm = (size_t)4 * r * (r + 1) * sizeof(T);
+  cudaFuncSetAttribute(k_node_factor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   const int64_t cbase = (level == 1) ? 0 : t.nleaf + t.node_off[level - 1];
   const int64_t nbase = t.node_off[level];
-  k_node_factor<<<(unsigned)t.nodes_at(level), 256, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase,
-                                                              nbase, Ct, L22, Eref, Etau, info);
+  k_node_factor<T><<<(unsigned)t.nodes_at(level), 256, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase,
+                                                                 nbase, Ct, L22, Eref, Etau, info);
 }
 
-void launch_logdet(const double* Lf, const Tree& t, const double* L22, int r, double* partial,
-                   int np, double* out, cudaStream_t st) {
-  k_logdet_partial<<<np, 256, 0, st>>>(Lf, dtree(t), L22, r, t.nnode, partial);
+template <typename T>
+void launch_logdet(const T* Lf, const Tree& t, const T* L22, int r, double* partial, int np, double* out,
+                   cudaStream_t st) {
+  k_logdet_partial<T><<<np, 256, 0, st>>>(Lf, dtree(t), L22, r, t.nnode, partial);
   k_sum_partials<<<1, 32, 0, st>>>(partial, np, out);
 }
+
+// double -> float pair conversion of n values (in place allowed: same 8-byte slots)
+__global__ void k_to_ff(const double* __restrict__ in, ff* __restrict__ out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = ff(in[i]);
+}
+__global__ void k_from_ff(const ff* __restrict__ in, double* __restrict__ out, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (double)in[i];
+}
+void launch_to_ff(const double* in, ff* out, int64_t n, cudaStream_t st) {
+  k_to_ff<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(in, out, n);
+}
+void launch_from_ff(const ff* in, double* out, int64_t n, cudaStream_t st) {
+  k_from_ff<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(in, out, n);
+}
+
+
+// Solve operators of the nodes of one level, formed off the critical path (side stream):
+// L22^{-1} (lower) and the explicit transfer E = H_0 ... H_{r-1} [I; 0] (2r x r) from the
+// reflectors of QR(G_N).  One CTA per node; columns are independent.
+template <typename T>
+__global__ void __launch_bounds__(256) k_node_finalize(const T* __restrict__ L22, const T* __restrict__ Eref,
+                                                       const T* __restrict__ Etau, int r, int64_t nbase, int with_e,
+                                                       T* __restrict__ L22i, T* __restrict__ Eexp) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* sm = reinterpret_cast<T*>(smraw);
+  const int ld = r + 1;
+  T* Ls = sm;               // L22
+  T* Vs = Ls + r * ld;      // reflector bottoms
+  T* ts = Vs + r * ld;      // tau
+  const int64_t node = nbase + blockIdx.x;
+  const int64_t off = node * (int64_t)r * r;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < r * r; e += blockDim.x) {
+    const int i = e % r, c = e / r;
+    Ls[i + c * ld] = L22[off + e];
+    if (with_e) Vs[i + c * ld] = Eref[off + e];
+  }
+  if (with_e)
+    for (int e = tid; e < r; e += blockDim.x) ts[e] = Etau[node * (int64_t)r + e];
+  __syncthreads();
+  // L22^{-1}: thread per column, forward substitution
+  for (int c = tid; c < r; c += blockDim.x) {
+    T* out = L22i + off + (int64_t)c * r;
+    for (int i = 0; i < c; ++i) out[i] = T(0.0);
+    for (int i = c; i < r; ++i) {
+      T v = T(i == c ? 1.0 : 0.0);
+      for (int p = c; p < i; ++p) v -= Ls[i + p * ld] * out[p];
+      out[i] = v / Ls[i + i * ld];
+    }
+  }
+  if (!with_e) return;
+  // E columns: thread per column c applies H_{r-1}, ..., H_0 to [e_c; 0] (only H_j, j <= c, act)
+  T* Eo = Eexp + node * (int64_t)2 * r * r;
+  for (int c = tid; c < r; c += blockDim.x) {
+    T* top = Eo + (int64_t)c * 2 * r;
+    T* bot = top + r;
+    for (int i = 0; i < r; ++i) {
+      top[i] = T(i == c ? 1.0 : 0.0);
+      bot[i] = T(0.0);
+    }
+    for (int j = c; j >= 0; --j) {
+      const T tj = ts[j];
+      if (tj == 0.0) continue;
+      T acc = top[j];
+      for (int i = 0; i < r; ++i) acc += Vs[i + j * ld] * bot[i];
+      acc = acc * tj;
+      top[j] -= acc;
+      for (int i = 0; i < r; ++i) bot[i] -= acc * Vs[i + j * ld];
+    }
+  }
+}
+
+template <typename T>
+void launch_leaf_formq(T* Pan, const T* tau, int r, const Tree& t, cudaStream_t st) {
+  const size_t sm = (size_t)t.max_leaf * r * sizeof(T);
+  if (sm <= 200 * 1024) {
+    cudaFuncSetAttribute(k_leaf_formq<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_leaf_formq<T, true><<<(unsigned)t.nleaf, 256, sm, st>>>(Pan, tau, r, dtree(t));
+  } else {
+    k_leaf_formq<T, false><<<(unsigned)t.nleaf, 256, 0, st>>>(Pan, tau, r, dtree(t));
+  }
+}
+
+template <typename T>
+void launch_node_finalize(const T* L22, const T* Eref, const T* Etau, int r, int level, const Tree& t, T* L22i,
+                          T* Eexp, cudaStream_t st) {
+  const size_t sm = ((size_t)2 * r * (r + 1) + r) * sizeof(T);
+  cudaFuncSetAttribute(k_node_finalize<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_node_finalize<T><<<(unsigned)t.nodes_at(level), 128, sm, st>>>(L22, Eref, Etau, r, t.node_off[level],
+                                                                   level < t.L ? 1 : 0, L22i, Eexp);
+}
+
+template void launch_leaf_formq<double>(double*, const double*, int, const Tree&, cudaStream_t);
+template void launch_leaf_formq<ff>(ff*, const ff*, int, const Tree&, cudaStream_t);
+template void launch_node_finalize<double>(const double*, const double*, const double*, int, int, const Tree&,
+                                           double*, double*, cudaStream_t);
+template void launch_node_finalize<ff>(const ff*, const ff*, const ff*, int, int, const Tree&, ff*, ff*,
+                                       cudaStream_t);
+
+template bool launch_leaf_chol<double>(const double*, double*, const Tree&, int*, cudaStream_t);
+template bool launch_leaf_chol<ff>(const double*, ff*, const Tree&, int*, cudaStream_t);
+template void launch_leaf_qr<double>(double*, int, const Tree&, double*, double*, cudaStream_t);
+template void launch_leaf_qr<ff>(ff*, int, const Tree&, ff*, ff*, cudaStream_t);
+template void launch_node_factor<double>(double*, const double*, int, int, const Tree&, double*, double*, double*,
+                                         double*, int*, cudaStream_t);
+template void launch_node_factor<ff>(ff*, const ff*, int, int, const Tree&, ff*, ff*, ff*, ff*, int*, cudaStream_t);
+template void launch_logdet<double>(const double*, const Tree&, const double*, int, double*, int, double*, cudaStream_t);
+template void launch_logdet<ff>(const ff*, const Tree&, const ff*, int, double*, int, double*, cudaStream_t);
 
 }  // namespace km

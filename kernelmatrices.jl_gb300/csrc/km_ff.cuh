@@ -1,0 +1,122 @@
+// Float-float ("double-single") arithmetic for the mixed-precision form.
+//
+// GB300 issues FP32 FMAs 64x faster than FP64 ones (128 vs 2 per clock per SM).  A value is kept
+// as an unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2), which carries about 48
+// significant bits.  The operations below are the classical error-free transformations
+// (Knuth's TwoSum, Dekker's FastTwoSum, TwoProd via a fused multiply-add) combined as in the
+// double-double algorithms of Dekker (1971) and Hida, Li and Bailey (2001), specialised to
+// float pairs.  They need IEEE round-to-nearest float operations without reassociation
+// (nvcc does not reassociate float arithmetic).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace km {
+
+// keep the standard overloads visible next to the float-pair ones declared below
+using ::exp;
+using ::fabs;
+using ::fmax;
+using ::fmin;
+using ::log;
+using ::sqrt;
+
+struct ff {
+  float hi, lo;
+  __host__ __device__ ff() : hi(0.f), lo(0.f) {}
+  __device__ ff(float h, float l) : hi(h), lo(l) {}
+  // rounding a double to the nearest float pair
+  __device__ ff(double x) {
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(x - (double)hi);
+  }
+  __device__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+
+__device__ __forceinline__ void ff_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void ff_fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+__device__ __forceinline__ ff operator+(ff a, ff b) {
+  float s, e;
+  ff_two_sum(a.hi, b.hi, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  ff r;
+  ff_fast_two_sum(s, e, r.hi, r.lo);
+  return r;
+}
+
+__device__ __forceinline__ ff operator-(ff a) { return ff(-a.hi, -a.lo); }
+__device__ __forceinline__ ff operator-(ff a, ff b) { return a + (-b); }
+
+__device__ __forceinline__ ff operator*(ff a, ff b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  ff r;
+  ff_fast_two_sum(p, e, r.hi, r.lo);
+  return r;
+}
+
+__device__ __forceinline__ ff operator/(ff a, ff b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const ff r = a - b * ff(q1, 0.f);
+  const float q2 = __fdiv_rn(r.hi, b.hi);
+  ff out;
+  ff_fast_two_sum(q1, q2, out.hi, out.lo);
+  return out;
+}
+
+__device__ __forceinline__ ff& operator+=(ff& a, ff b) { return a = a + b; }
+__device__ __forceinline__ ff& operator-=(ff& a, ff b) { return a = a - b; }
+__device__ __forceinline__ ff& operator*=(ff& a, ff b) { return a = a * b; }
+__device__ __forceinline__ ff& operator/=(ff& a, ff b) { return a = a / b; }
+
+__device__ __forceinline__ bool operator>(ff a, double b) { return (double)a > b; }
+__device__ __forceinline__ bool operator>=(ff a, double b) { return (double)a >= b; }
+__device__ __forceinline__ bool operator==(ff a, double b) { return a.hi == (float)b && a.lo == 0.f && (double)a.hi == b; }
+__device__ __forceinline__ bool operator!=(ff a, double b) { return !(a == b); }
+
+__device__ __forceinline__ ff sqrt(ff a) {
+  if (!(a.hi > 0.f)) return ff(0.f, 0.f);
+  const float s = sqrtf(a.hi);
+  const ff r = a - ff(s, 0.f) * ff(s, 0.f);
+  const float c = __fdiv_rn(r.hi, __fmul_rn(2.f, s));
+  ff out;
+  ff_fast_two_sum(s, c, out.hi, out.lo);
+  return out;
+}
+
+__device__ __forceinline__ ff fabs(ff a) { return a.hi < 0.f ? -a : a; }
+
+__device__ __forceinline__ ff shfl_xor(ff v, int o) {
+  return ff(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
+}
+__device__ __forceinline__ ff shfl_idx(ff v, int src) {
+  return ff(__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src));
+}
+__device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double shfl_idx(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+template <typename T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = v + shfl_xor(v, o);
+  return v;
+}
+
+// conversions used at buffer boundaries
+template <typename T> __device__ __forceinline__ T from_double(double x);
+template <> __device__ __forceinline__ double from_double<double>(double x) { return x; }
+template <> __device__ __forceinline__ ff from_double<ff>(double x) { return ff(x); }
+__device__ __forceinline__ double to_double(double x) { return x; }
+__device__ __forceinline__ double to_double(ff x) { return (double)x; }
+
+}  // namespace km

@@ -9,6 +9,8 @@
 //   y_leaf = dK_leaf x_leaf + dPhi_leaf S^{-1} a + Phi_leaf S^{-1} (b - Sj S^{-1} a)
 // where a and b are the sums of phi and dphi of the siblings along the leaf's path to the root.
 // The sums travel through the tree sweeps with 2r-long vectors [phi ; dphi].
+#include <algorithm>
+
 #include "km_kernels.h"
 
 namespace km {
@@ -129,6 +131,16 @@ __global__ void k_col_dots(const double* __restrict__ A, int64_t lda, const doub
     for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
     out[c] = s;
   }
+}
+
+// y = a x + b y over n values
+__global__ void k_axpby(double* __restrict__ y, const double* __restrict__ x, double a, double b, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i] + b * y[i];
+}
+
+void launch_axpby(double* y, const double* x, double a, double b, int64_t n, cudaStream_t st) {
+  k_axpby<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(y, x, a, b, n);
 }
 
 void launch_leaf_dphiT(const double* Phi, const double* dPhi, int r, const Tree& t, const double* X,

@@ -2,6 +2,7 @@
 // km_aca.cu, km_grad.cu).  Host orchestration lives in km_api.cu.
 #pragma once
 #include "km_internal.h"
+#include "km_ff.cuh"
 
 namespace km {
 
@@ -50,11 +51,11 @@ struct LeafDesc {             // leaf triangular operation on an arbitrary colum
   int ncols;
 };
 
-struct NodeMatsH {
-  const double* Ct;
-  const double* L22;
-  const double* Eref;
-  const double* Etau;
+struct NodeMatsH {          // node factors (double or float pairs, by the caller's precision)
+  const void* Ct;
+  const void* L22;
+  const void* L22i;
+  const void* E;           // explicit 2r x r transfer
   int r;
 };
 
@@ -70,29 +71,42 @@ void launch_gather_points(const double* pts, const int64_t* idx, int r, double* 
 
 // factorisation
 bool launch_chol_small(double* A, int n, int* info, cudaStream_t st);
-bool launch_leaf_chol(const double* K, double* Lf, const Tree& t, int* info, cudaStream_t st);
-bool launch_leaf_tri(const double* Lf, const Tree& t, int op, double* Bptr, int64_t bmul,
-                     int64_t bld, int bld_is_m, double* Xptr, int64_t xmul, int64_t xld,
-                     int xld_is_m, int ncols, cudaStream_t st);
-void launch_leaf_qr(double* Pan, int r, const Tree& t, double* tau, double* Rout, cudaStream_t st);
+template <typename T>
+bool launch_leaf_chol(const double* K, T* Lf, const Tree& t, int* info, cudaStream_t st);
+template <typename T>
+bool launch_leaf_tri(const T* Lf, const Tree& t, int op, T* Bptr, int64_t bmul, int64_t bld, int bld_is_m, T* Xptr,
+                     int64_t xmul, int64_t xld, int xld_is_m, int ncols, cudaStream_t st);
+template <typename T>
+void launch_leaf_qr(T* Pan, int r, const Tree& t, T* tau, T* Rout, cudaStream_t st);
 void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st);
-void launch_node_factor(double* R, const double* SinvT, int r, int level, const Tree& t, double* Ct,
-                        double* L22, double* Eref, double* Etau, int* info, cudaStream_t st);
-void launch_logdet(const double* Lf, const Tree& t, const double* L22, int r, double* partial,
-                   int np, double* out, cudaStream_t st);
+template <typename T>
+void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T* Ct, T* L22, T* Eref, T* Etau,
+                        int* info, cudaStream_t st);
+template <typename T>
+void launch_leaf_formq(T* Pan, const T* tau, int r, const Tree& t, cudaStream_t st);
+template <typename T>
+void launch_node_finalize(const T* L22, const T* Eref, const T* Etau, int r, int level, const Tree& t, T* L22i,
+                          T* Eexp, cudaStream_t st);
+template <typename T>
+void launch_logdet(const T* Lf, const Tree& t, const T* L22, int r, double* partial, int np, double* out,
+                   cudaStream_t st);
+void launch_to_ff(const double* in, ff* out, int64_t n, cudaStream_t st);
+void launch_from_ff(const ff* in, double* out, int64_t n, cudaStream_t st);
 
 // products and solves
 enum { UP_PROJ_ = 0, UP_FWD_ = 1, UP_MULT_ = 2, UP_SUM_ = 3 };
 enum { DN_FWD_ = 0, DN_BWD_ = 1, DN_MUL_ = 2, DN_MULT_ = 3, DN_NYS_ = 4 };
-void launch_up(const Tree& t, const NodeMatsH& h, int level, double* VP, double* VD, int k,
-               int mode, cudaStream_t st);
-void launch_down(const Tree& t, const NodeMatsH& h, int level, const double* VP, double* VG,
-                 const double* VD, int k, int mode, cudaStream_t st);
-void launch_leaf_proj(const double* Qref, const double* tau, int r, const Tree& t, const double* Y,
-                      int64_t ldy, double* VP, int k, cudaStream_t st);
-void launch_leaf_expand(const double* Qref, const double* tau, int r, const Tree& t,
-                        const double* VG, double* Y, int64_t ldy, int k, double sign,
-                        cudaStream_t st);
+template <typename T>
+void launch_up(const Tree& t, const NodeMatsH& h, int level, T* VP, T* VD, int k, int mode, cudaStream_t st);
+template <typename T>
+void launch_down(const Tree& t, const NodeMatsH& h, int level, const T* VP, T* VG, const T* VD, int k, int mode,
+                 cudaStream_t st);
+template <typename T>
+void launch_leaf_proj(const T* Qref, const T* tau, int r, const Tree& t, const T* Y, int64_t ldy, T* VP, int k,
+                      cudaStream_t st);
+template <typename T>
+void launch_leaf_expand(const T* Qref, const T* tau, int r, const Tree& t, const T* VG, T* Y, int64_t ldy, int k,
+                        double sign, cudaStream_t st);
 void launch_leaf_phiT(const double* Phi, int r, const Tree& t, const double* X, int64_t ldx,
                       double* VP, int k, cudaStream_t st);
 void launch_leaf_nys_apply(const double* Kl, const double* Phi, const double* Sc, int r,
@@ -105,6 +119,7 @@ void launch_leaf_dphiT(const double* Phi, const double* dPhi, int r, const Tree&
 void launch_leaf_dnys_apply(const double* dKl, const double* Phi, const double* dPhi, const double* Sc,
                             const double* Sj, int r, const Tree& t, const double* X, int64_t ldx,
                             const double* VG, double* Y, int64_t ldy, int k, cudaStream_t st);
+void launch_axpby(double* y, const double* x, double a, double b, int64_t n, cudaStream_t st);
 void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n, int k,
                      double* out, cudaStream_t st);
 

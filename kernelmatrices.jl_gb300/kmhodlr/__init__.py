@@ -3,7 +3,7 @@
 The compute runs in libkmhodlr.so (hand-written sm_103a CUDA kernels behind a C ABI,
 include/kmhodlr.h).  Importing this package does not require a GPU; creating a KernelHODLR does.
 """
-from ._lib import load, LIB_PATH  # noqa: F401
+from ._lib import load, LIB_PATH, KM_PREC_FP64, KM_PREC_MIXED  # noqa: F401
 from .hodlr import (  # noqa: F401
     FixedLevel, LogLevel, KernelMatrix, KernelHODLR, RatQuad, Matern32, HODLRindices,
     KMError, PosDefException, symmetricfactorize, logdet, nystrom_landmarks, probe_fp64_tflops,

@@ -165,13 +165,13 @@ class KernelHODLR:
 
     def __init__(self, K: KernelMatrix, ep: float, maxrank: int, lvl, nystrom: bool = False,
                  plel: bool = False, sorted: bool = False, device: int = 0,
-                 precision: int = L.KM_PREC_FP64):
+                 precision: int = L.KM_PREC_FP64, refine_max_iter: int = 0, refine_tol: float = 1e-10):
         lib = L.load()
         if not np.array_equal(K.x1, K.x2):
             raise KMError(L.KM_ERR_BAD_ARG, "This function builds symmetric matrices.")
         kid = getattr(K.kernel, "kid", K.kernel)
         cfg = L.KmConfig(device=device, precision=precision, hbm_budget_fraction=0.8,
-                         refine_max_iter=0, refine_tol=0.0)
+                         refine_max_iter=refine_max_iter, refine_tol=refine_tol)
         h = C.c_void_p()
         rc = lib.km_create(C.byref(cfg), C.byref(h))
         if rc != L.KM_OK:

@@ -1,0 +1,82 @@
+"""Mixed-precision form (float-float factor on the FP32 pipe) against the FP64 form.
+
+Targets: logdet within 1e-6 absolute and solves within 1e-8 relative of the FP64 engine (which
+matches the oracle to 1e-10 / 1e-9, see test_gpu_nystrom.py); with FP64 refinement enabled the
+reported relative residual ||b - K x|| / ||b|| must reach 1e-10."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import hodlr_oracle as O
+
+GOLD = Path(__file__).resolve().parent / "golden"
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def pair(pts, params, rank, lvl, kern, **kw):
+    import kmhodlr as K
+    km = K.KernelMatrix(pts, pts, params, kern)
+    h64 = K.KernelHODLR(km, 0.0, rank, lvl, nystrom=True)
+    hmx = K.KernelHODLR(km, 0.0, rank, lvl, nystrom=True, precision=K.KM_PREC_MIXED, **kw)
+    K.symmetricfactorize(h64)
+    K.symmetricfactorize(hmx)
+    return h64, hmx
+
+
+@pytest.mark.parametrize("case", ["nys_matern_2048", "nys_rq_1500", "nys_matern_4096_r72"])
+def test_mixed_golden(case, lib):
+    import kmhodlr as K
+    d = np.load(GOLD / f"{case}.npz")
+    lvl = K.FixedLevel(int(d["level"])) if int(d["level_kind"]) == 0 else K.LogLevel(int(d["level"]))
+    kern = K.Matern32() if int(d["kid"]) == 1 else K.RatQuad()
+    _, hmx = pair(d["pts"], d["params"], int(d["rank"]), lvl, kern)
+    assert abs(hmx.logdet() - float(d["logdet"])) < 1e-6
+    assert rel(hmx.ldiv(d["rhs"]), d["solve"]) < 1e-8
+
+
+def test_mixed_c2_shape(lib):
+    """The benchmark's kernel, rank and leaf size at n = 2^14 (FixedLevel(6))."""
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    n = 16384
+    pts = uniform_points(n, 31)
+    rhs = np.random.default_rng(5).standard_normal((n, 16))
+    h64, hmx = pair(pts, [1.0, 0.1, 1e-3], 72, K.FixedLevel(6), K.Matern32())
+    assert abs(hmx.logdet() - h64.logdet()) < 1e-6
+    assert rel(hmx.ldiv(rhs), h64.ldiv(rhs)) < 1e-8
+    y = hmx.W.ldiv(rhs)
+    assert rel(hmx.W @ y, rhs) < 1e-9
+    x = np.random.default_rng(6).standard_normal((n, 2))
+    assert rel(hmx @ x, h64 @ x) < 1e-9
+
+
+def test_mixed_refinement_reaches_tolerance(lib):
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    n = 8192
+    pts = uniform_points(n, 32)
+    rhs = np.random.default_rng(7).standard_normal((n, 4))
+    h64, hmx = pair(pts, [1.0, 0.1, 1e-4], 72, K.FixedLevel(5), K.Matern32(), refine_max_iter=5, refine_tol=1e-10)
+    x = hmx.ldiv(rhs)
+    st = hmx.stats()
+    assert st.refine_residual <= 1e-10
+    assert rel(x, h64.ldiv(rhs)) < 1e-9
+
+
+def test_mixed_gradient(lib):
+    import kmhodlr as K
+    from kmhodlr.data import rademacher, uniform_points
+    n = 2048
+    pts = uniform_points(n, 33)
+    y = np.random.default_rng(8).standard_normal(n)
+    V = rademacher(n, 16, 9)
+    h64, hmx = pair(pts, [1.0, 0.1, 1e-3], 32, K.FixedLevel(3), K.Matern32())
+    n64, g64 = h64.nll_grad(y, V)
+    nmx, gmx = hmx.nll_grad(y, V)
+    assert abs(nmx - n64) < 1e-6
+    assert np.all(np.abs(gmx - g64) <= 1e-6 * np.abs(g64) + 1e-6)
