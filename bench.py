@@ -5,7 +5,12 @@ Workload (one step): n = 65536 points uniform on [0,1]^2 (seeded, k-d ordered), 
 (256 leaves of 256 points): assemble, one matvec, symmetricfactorize!, a solve with 16 N(0,1)
 right-hand sides and logdet.  The metric is steps per second.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Both arithmetic forms of the engine run on the same inputs: the mixed form (float-pair
+factorisation on the FP32 pipe, FP64 assembly and matvec; `--precision mixed`, the default) and
+the FP64 form.  The one selected is reported as `value`/`e2e`, the other beside it, with the
+logdet and solve differences between them measured outside the timed regions.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--precision mixed|fp64]
 
 --impl ours (default): the GB300 engine (libkmhodlr.so).  `value` is measured with inputs
 resident in HBM through the device entry points; `e2e` through the host-pointer C ABI (pinned
@@ -219,117 +224,150 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     params = np.array(PARAMS, dtype=np.float64)
     pp = params.ctypes.data_as(C.POINTER(C.c_double))
 
-    cfg = L.KmConfig(device=dev, precision=L.KM_PREC_FP64, hbm_budget_fraction=0.8, refine_max_iter=0,
-                     refine_tol=0.0)
-    h = C.c_void_p()
-    rc = lib.km_create(C.byref(cfg), C.byref(h))
-    if rc != 0:
-        raise SystemExit(f"km_create failed ({rc})")
-    stream = torch.cuda.current_stream()
-    lib.km_set_stream(h, C.c_void_p(stream.cuda_stream))
-    logdet = C.c_double()
-
-    def check(rc):
+    def check(h, rc):
         if rc != 0:
             raise RuntimeError(lib.km_last_error(h).decode())
 
-    def step_dev():
-        check(lib.km_assemble_dev(h, C.c_void_p(d_pts.data_ptr()), n, L.KM_KERNEL_MATERN32, pp, 3,
-                                  L.KM_METHOD_NYSTROM, 0.0, RANK, L.KM_LEVEL_FIXED, LEVEL))
-        check(lib.km_matvec_dev(h, C.c_void_p(d_x.data_ptr()), C.c_void_p(d_y.data_ptr()), 1))
-        check(lib.km_factorize(h))
-        check(lib.km_solve_dev(h, C.c_void_p(d_rhs.data_ptr()), C.c_void_p(d_sol.data_ptr()), NRHS))
-        check(lib.km_logdet(h, C.byref(logdet)))
-
     dp = lambda t: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
-
-    def step_e2e():
-        check(lib.km_assemble(h, dp(h_pts), n, L.KM_KERNEL_MATERN32, pp, 3, L.KM_METHOD_NYSTROM, 0.0, RANK,
-                              L.KM_LEVEL_FIXED, LEVEL))
-        check(lib.km_matvec(h, dp(h_x), dp(h_y), 1))
-        check(lib.km_factorize(h))
-        check(lib.km_solve(h, dp(h_rhs), dp(h_sol), NRHS))
-        check(lib.km_logdet(h, C.byref(logdet)))
+    stream = torch.cuda.current_stream()
 
     def barrier():
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
 
-    def timed(fn, steps):
-        barrier()
-        st0 = L.KmStats()
-        lib.km_get_stats(h, C.byref(st0))
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(steps):
-            fn()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-        st1 = L.KmStats()
-        lib.km_get_stats(h, C.byref(st1))
-        ms = e0.elapsed_time(e1)
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms, st1.kernel_launches - st0.kernel_launches
+    def run_form(prec: int, sample_clocks: bool) -> dict:
+        cfg = L.KmConfig(device=dev, precision=prec, hbm_budget_fraction=0.8, refine_max_iter=0, refine_tol=0.0)
+        h = C.c_void_p()
+        rc = lib.km_create(C.byref(cfg), C.byref(h))
+        if rc != 0:
+            raise SystemExit(f"km_create failed ({rc})")
+        lib.km_set_stream(h, C.c_void_p(stream.cuda_stream))
+        logdet = C.c_double()
 
-    for _ in range(args.warmup):
-        step_dev()
-    clocks = ClockSampler(dev)
-    clocks.start()
-    ms, launches = timed(step_dev, args.steps)
-    clk = clocks.stop()
-    ms_e2e, _ = timed(step_e2e, args.steps)
+        def step_dev():
+            check(h, lib.km_assemble_dev(h, C.c_void_p(d_pts.data_ptr()), n, L.KM_KERNEL_MATERN32, pp, 3,
+                                         L.KM_METHOD_NYSTROM, 0.0, RANK, L.KM_LEVEL_FIXED, LEVEL))
+            check(h, lib.km_matvec_dev(h, C.c_void_p(d_x.data_ptr()), C.c_void_p(d_y.data_ptr()), 1))
+            check(h, lib.km_factorize(h))
+            check(h, lib.km_solve_dev(h, C.c_void_p(d_rhs.data_ptr()), C.c_void_p(d_sol.data_ptr()), NRHS))
+            check(h, lib.km_logdet(h, C.byref(logdet)))
 
-    # per-kernel-class device time (a second timed pass with per-launch events)
-    lib.km_profile_enable(h, 1)
-    timed(step_dev, args.steps)
-    prof = {}
-    for ci, name in enumerate(L.PROF_CLASSES):
-        tot, cnt = C.c_double(), C.c_int64()
-        lib.km_profile_get(h, ci, C.byref(tot), C.byref(cnt))
-        if cnt.value:
-            prof[name] = {"ms": tot.value / args.steps, "launches": cnt.value // args.steps}
-    lib.km_profile_enable(h, 0)
+        def step_e2e():
+            check(h, lib.km_assemble(h, dp(h_pts), n, L.KM_KERNEL_MATERN32, pp, 3, L.KM_METHOD_NYSTROM, 0.0, RANK,
+                                     L.KM_LEVEL_FIXED, LEVEL))
+            check(h, lib.km_matvec(h, dp(h_x), dp(h_y), 1))
+            check(h, lib.km_factorize(h))
+            check(h, lib.km_solve(h, dp(h_rhs), dp(h_sol), NRHS))
+            check(h, lib.km_logdet(h, C.byref(logdet)))
+
+        def timed(fn, steps):
+            barrier()
+            st0 = L.KmStats()
+            lib.km_get_stats(h, C.byref(st0))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            barrier()
+            st1 = L.KmStats()
+            lib.km_get_stats(h, C.byref(st1))
+            t = e0.elapsed_time(e1)
+            if dist is not None:
+                tt = torch.tensor([t], device="cuda")
+                dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+                t = float(tt.item())
+            return t, st1.kernel_launches - st0.kernel_launches
+
+        for _ in range(args.warmup):
+            step_dev()
+        clocks = ClockSampler(dev) if sample_clocks else None
+        if clocks:
+            clocks.start()
+        ms, launches = timed(step_dev, args.steps)
+        clk = clocks.stop() if clocks else None
+        sol = d_sol.cpu().numpy().copy()
+        ld = logdet.value
+        ms_e2e, _ = timed(step_e2e, args.steps)
+        lib.km_profile_enable(h, 1)
+        timed(step_dev, args.steps)
+        prof = {}
+        for ci, name in enumerate(L.PROF_CLASSES):
+            tot, cnt = C.c_double(), C.c_int64()
+            lib.km_profile_get(h, ci, C.byref(tot), C.byref(cnt))
+            if cnt.value:
+                prof[name] = {"ms": tot.value / args.steps, "launches": cnt.value // args.steps}
+        lib.km_profile_enable(h, 0)
+        lib.km_destroy(h)
+        return {"ms": ms, "launches": launches, "clk": clk, "ms_e2e": ms_e2e, "prof": prof, "sol": sol, "logdet": ld}
+
+    head_prec = L.KM_PREC_MIXED if args.precision == "mixed" else L.KM_PREC_FP64
+    other_prec = L.KM_PREC_FP64 if head_prec == L.KM_PREC_MIXED else L.KM_PREC_MIXED
+    head = run_form(head_prec, True)
+    other = run_form(other_prec, False)
+    f64 = other if head_prec == L.KM_PREC_MIXED else head
+    mix = head if head_prec == L.KM_PREC_MIXED else other
     fp64_peak = kmhodlr.probe_fp64_tflops(dev)
+    fp32_peak = kmhodlr.probe_fp32_tflops(dev)
 
-    step_ms = ms / args.steps
-    value = world * args.steps / (ms / 1e3)
-    e2e_value = world * args.steps / (ms_e2e / 1e3)
+    def form_summary(fm):
+        return {"value": world * args.steps / (fm["ms"] / 1e3), "ms_per_step": fm["ms"] / args.steps,
+                "e2e_value": world * args.steps / (fm["ms_e2e"] / 1e3), "kernel_ms_per_step": fm["prof"]}
+
+    step_ms = head["ms"] / args.steps
+    value = world * args.steps / (head["ms"] / 1e3)
+    e2e_value = world * args.steps / (head["ms_e2e"] / 1e3)
     flops = engine_flops(n, LEVEL)
+    prof = head["prof"]
     dom = max((k for k in prof if k in flops), key=lambda k: prof[k]["ms"], default=None)
     roof = None
     if dom:
-        per_launch_ms = prof[dom]["ms"] / max(prof[dom]["launches"], 1)
         achieved = flops[dom] / (prof[dom]["ms"] * 1e-3) / 1e12
         traffic = None
         tf = ROOT / "profiles" / "ncu_traffic.json"
         if tf.exists():
-            traffic = json.loads(tf.read_text()).get(dom)
-        roof = {"kernel": dom, "bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak, "traffic": traffic, "per_launch_ms": per_launch_ms,
-                "peak_source": "FP64 FMA rate measured live by km_probe_fp64_tflops (the measured-peaks file "
-                               "holds only HBM copy and bf16 tensor rates)"}
-
+            traffic = json.loads(tf.read_text()).get(f"{args.precision}:{dom}")
+        if head_prec == L.KM_PREC_MIXED:
+            # one float-pair multiply-add (2 algorithmic flops) costs 18 FP32 instructions, i.e. 9 FP32
+            # FMA slots (18 FP32 flops) per algorithmic flop pair: peak = FP32 flop rate / 18
+            peak = fp32_peak / 18.0
+            src = ("FP32 FMA rate measured live by km_probe_fp32_tflops / 18 (a float-pair multiply-add is 18 "
+                   "FP32 instructions for 2 algorithmic flops)")
+            bound = "fp32"
+        else:
+            peak = fp64_peak
+            src = "FP64 FMA rate measured live by km_probe_fp64_tflops"
+            bound = "fp64"
+        roof = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "per_launch_ms": prof[dom]["ms"] / max(prof[dom]["launches"], 1), "peak_source": src,
+                "fp64_peak_tflops": fp64_peak, "fp32_peak_tflops": fp32_peak}
+    accuracy = {"logdet_abs_err_mixed_vs_fp64": abs(mix["logdet"] - f64["logdet"]),
+                "solve_rel_err_mixed_vs_fp64": float(np.linalg.norm(mix["sol"] - f64["sol"]) /
+                                                     np.linalg.norm(f64["sol"])),
+                "targets": {"logdet_abs": 1e-6, "solve_rel": 1e-8}}
     out = {"metric": "HODLR factor+solve+logdet/s", "value": value, "unit": "steps/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head_prec == L.KM_PREC_FP64 else "f32x2+f64",
+           "data": "synthetic",
            "config": {"workload": WORKLOAD, "n": n, "rank": RANK, "level": "FixedLevel(8)", "nrhs": NRHS,
-                      "kernel": "matern32", "params": list(PARAMS), "precision": "fp64",
+                      "kernel": "matern32", "params": list(PARAMS), "precision": args.precision,
                       "l2": "inputs larger than L2 (leaf factors alone 268 MB)",
                       "parallelism": f"replicas{world}"},
            "e2e": {"value": e2e_value, "unit": "steps/s",
                    "h2d_bytes_per_step": int((2 * n + n + NRHS * n) * 8),
                    "d2h_bytes_per_step": int((n + NRHS * n + 1) * 8)},
-           "gpu_launches": int(launches),
-           "clocks": clk,
+           "gpu_launches": int(head["launches"]),
+           "clocks": head["clk"],
            "roofline": roof,
-           "kernel_ms_per_step": prof,
-           "logdet": logdet.value}
+           "fp64_form": form_summary(f64),
+           "mixed_form": form_summary(mix),
+           "mixed_speedup_vs_fp64": f64["ms"] / mix["ms"],
+           "accuracy": accuracy,
+           "logdet": head["logdet"]}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         res = cpu_sample(16384, 6, steps=1)
         v = 1.0 / (res["times"][0] * res["scale"])
@@ -337,7 +375,6 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                                "sample": f"one n=16384 FixedLevel(6) step of the reference algorithm "
                                          f"(oracle/, {res['times'][0]:.1f} s) scaled x{res['scale']:.2f} "
                                          f"to the workload by flop count"}
-    lib.km_destroy(h)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist is not None:
@@ -351,6 +388,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed",
+                    help="form reported as `value` (the other form is reported beside it)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

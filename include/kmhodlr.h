@@ -223,6 +223,10 @@ int km_profile_get(km_handle* h, int cls, double* total_ms, int64_t* launches);
  * for FP64-ALU-bound kernels). */
 int km_probe_fp64_tflops(int device, double* out);
 
+/* Device FP32 FMA throughput in TFLOP/s (denominator for the float-pair kernels of the mixed
+ * form, which run on the FP32 pipe). */
+int km_probe_fp32_tflops(int device, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,7 +14,44 @@ __global__ void k_dfma_loop(double* out, int iters, double a, double b) {
   out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+__global__ void k_ffma_loop(float* out, int iters, float a, float b) {
+  float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1.f, x2 = x0 + 2.f, x3 = x0 + 3.f;
+  float x4 = x0 + 4.f, x5 = x0 + 5.f, x6 = x0 + 6.f, x7 = x0 + 7.f;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
 }  // namespace km
+
+extern "C" int km_probe_fp32_tflops(int device, double* out) {
+  if (!out) return KM_ERR_BAD_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return KM_ERR_CUDA;
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, device) != cudaSuccess) return KM_ERR_CUDA;
+  const int blocks = p.multiProcessorCount * 8, threads = 256, iters = 100000;
+  float* d = nullptr;
+  if (cudaMalloc(&d, sizeof(float) * blocks * threads) != cudaSuccess) return KM_ERR_OOM;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  km::k_ffma_loop<<<blocks, threads>>>(d, 100, 0.999f, 0.001f);
+  cudaEventRecord(e0);
+  km::k_ffma_loop<<<blocks, threads>>>(d, iters, 0.999f, 0.001f);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  const cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess || ms <= 0.f) return KM_ERR_CUDA;
+  *out = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+  return KM_OK;
+}
 
 extern "C" int km_probe_fp64_tflops(int device, double* out) {
   if (!out) return KM_ERR_BAD_ARG;

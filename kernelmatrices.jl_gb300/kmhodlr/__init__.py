@@ -7,5 +7,6 @@ from ._lib import load, LIB_PATH, KM_PREC_FP64, KM_PREC_MIXED  # noqa: F401
 from .hodlr import (  # noqa: F401
     FixedLevel, LogLevel, KernelMatrix, KernelHODLR, RatQuad, Matern32, HODLRindices,
     KMError, PosDefException, symmetricfactorize, logdet, nystrom_landmarks, probe_fp64_tflops,
+    probe_fp32_tflops,
     negloglik, stoch_gradient, nll_objective,
 )

@@ -329,6 +329,14 @@ def nll_objective(prms, grad, pts: np.ndarray, dat: np.ndarray, kernel, rank: in
     return HK.nll_grad(dat)[0]
 
 
+def probe_fp32_tflops(device: int = 0) -> float:
+    out = C.c_double()
+    rc = L.load().km_probe_fp32_tflops(device, C.byref(out))
+    if rc != L.KM_OK:
+        raise KMError(rc, "FP32 probe failed")
+    return out.value
+
+
 def probe_fp64_tflops(device: int = 0) -> float:
     out = C.c_double()
     rc = L.load().km_probe_fp64_tflops(device, C.byref(out))
