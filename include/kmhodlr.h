@@ -190,6 +190,130 @@ int km_derivative_matvec(km_handle* h, int param, const double* x, double* y, in
 int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t nprobe,
                 double* nll, double* grad);
 
+/* km_nll_grad with the probes drawn on the device instead of copied from the host: entry (i, j)
+ * of the n x nprobe block is +1 when the top bit of SplitMix64(SplitMix64(seed) + j*n + i) is
+ * set, else -1.  Replaces givesaa(n, m; seed) (src/utils.jl:22-27) + stoch_gradient
+ * (src/HODLR/src/stochasticgradient.jl:30-44); Julia's own generator is not reproduced, so
+ * the probe values differ from the reference's for the same seed (the estimator is the same). */
+int km_nll_grad_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed, double* nll,
+                       double* grad);
+
+/* Frees the device buffers of the handle's current problem (the handle stays usable; the next
+ * km_assemble allocates again).  No reference counterpart: Julia's GC frees the arrays. */
+int km_trim(km_handle* h);
+
+/* Device bytes one handle holds for a Nystrom problem of n points at this rank and level with
+ * `ncols` right-hand-side columns (probes + 1 for a likelihood gradient), `with_grad` adding
+ * the derivative workspaces.  Pure host arithmetic; -1 for invalid arguments. */
+int64_t km_estimate_bytes(int64_t n, int64_t rank, int level_kind, int64_t level, int64_t ncols,
+                          int with_grad);
+
+/* ---- batched form: many independent likelihood problems ------------------------------------ */
+
+/* One problem of a batch or serving request.  Host pointers; the caller keeps them valid until
+ * the call (batch) or the request (serving) completes. */
+typedef struct km_problem {
+  int64_t n;             /* number of points                                                  */
+  const double* pts;     /* 2*n values, (x, y) pairs, already in the caller's (k-d) order     */
+  const double* y;       /* n observations                                                    */
+  double params[3];      /* kernel parameters (scale, range, nugget)                          */
+} km_problem;
+
+typedef struct km_batch_opts {
+  int kernel_id;         /* enum km_kernel_id                                                 */
+  int64_t rank;          /* Nystrom rank (the gradient needs Nystrom blocks, constructor.jl:69) */
+  int level_kind;        /* enum km_level_kind                                                */
+  int64_t level;
+  int64_t nprobe;        /* Rademacher probes per problem; 0 => NLL only                      */
+  uint64_t probe_seed;   /* problem b draws its probes with seed probe_seed + b               */
+} km_batch_opts;
+
+typedef struct km_batch km_batch;
+
+/* A pool of `nworkers` handles (0 => 8), each with its own stream and host thread, that keeps
+ * its device buffers between calls (grown to the largest problem seen). */
+int km_batch_create(const km_config* cfg, int nworkers, km_batch** out);
+int km_batch_destroy(km_batch* b);
+
+/* For every problem b: assemble (Nystrom), symmetricfactorize!, negloglik and, when nprobe > 0,
+ * the stochastic gradient.  nll[b], grad[3*b .. 3*b+2] and status[b] (enum km_status) are
+ * written per problem; one failing problem does not stop the others.  Problems are dispatched
+ * largest first to the workers, which run concurrently on the GPU.  Replaces the loop a caller
+ * writes around nll_objective (src/HODLR/src/maxlikfunctions.jl:29-50) for independent
+ * datasets; the reference has no batched entry point.  Returns KM_OK when every problem
+ * succeeded, else the first failing status (message in km_batch_last_error). */
+int km_batch_nll_grad(km_batch* b, const km_batch_opts* o, int64_t nprob, const km_problem* probs,
+                      double* nll, double* grad, int* status);
+const char* km_batch_last_error(const km_batch* b);
+
+/* ---- serving form: continuous batching with HBM-budget admission --------------------------- */
+
+enum km_req_kind {
+  KM_REQ_NLL_GRAD = 0,   /* negloglik (+ stochastic gradient when nprobe > 0) of `prob`        */
+  KM_REQ_FACTOR = 1,     /* assemble + factorise `prob` and keep the factor resident          */
+  KM_REQ_SOLVE = 2,      /* x = K^{-1} b with the resident factor `factor_id` (nrhs columns)  */
+  KM_REQ_RELEASE = 3     /* drop the resident factor `factor_id`                               */
+};
+
+typedef struct km_request {
+  int kind;              /* enum km_req_kind                                                  */
+  km_problem prob;       /* NLL_GRAD, FACTOR                                                  */
+  int64_t nprobe;        /* NLL_GRAD                                                          */
+  uint64_t probe_seed;   /* NLL_GRAD                                                          */
+  int64_t factor_id;     /* SOLVE, RELEASE                                                    */
+  const double* b;       /* SOLVE: n x nrhs right-hand sides (host, column-major)              */
+  double* x;             /* SOLVE: n x nrhs solutions (host, column-major)                     */
+  int64_t nrhs;          /* SOLVE                                                             */
+} km_request;
+
+typedef struct km_result {
+  int status;            /* enum km_status of the request                                     */
+  double nll;            /* NLL_GRAD                                                          */
+  double grad[3];        /* NLL_GRAD with nprobe > 0                                          */
+  double logdet;         /* FACTOR                                                            */
+  int64_t factor_id;     /* FACTOR: id for later SOLVE / RELEASE requests                     */
+  double queue_ms;       /* submit -> start                                                   */
+  double run_ms;         /* start -> end                                                      */
+} km_result;
+
+typedef struct km_serve_opts {
+  int kernel_id;
+  int64_t rank;
+  int level_kind;
+  int64_t level;
+  int nworkers;          /* concurrent executors (0 => 8)                                     */
+} km_serve_opts;
+
+typedef struct km_serve_stats {
+  int64_t submitted, completed, failed, rejected;
+  int64_t resident_factors;
+  int64_t bytes_in_use;  /* device bytes held by executors and resident factors               */
+  int64_t peak_bytes;
+  int64_t budget_bytes;  /* hbm_budget_fraction of the device's memory                        */
+  double p50_ms, p99_ms, mean_ms;  /* submit -> completion latency of completed requests      */
+} km_serve_stats;
+
+typedef struct km_server km_server;
+
+/* Starts the scheduler thread and `nworkers` executors.  A request is admitted when its
+ * estimated device bytes fit in the budget next to everything in flight and resident;
+ * admission is first-come first-served with later requests allowed to pass one that does
+ * not fit yet.  A request that cannot fit even on an idle server fails with KM_ERR_OOM.
+ * No reference counterpart (the reference is a library called in-process). */
+int km_serve_create(const km_config* cfg, const km_serve_opts* o, km_server** out);
+
+/* Queues a request; *ticket identifies it for km_serve_wait. */
+int km_serve_submit(km_server* s, const km_request* r, uint64_t* ticket);
+
+/* Waits up to timeout_ms (< 0: forever) for the request; KM_ERR_TIMEOUT if still running.
+ * A result is returned once; its ticket is then forgotten. */
+int km_serve_wait(km_server* s, uint64_t ticket, int64_t timeout_ms, km_result* out);
+
+int km_serve_stats_get(km_server* s, km_serve_stats* out);
+
+/* Drains every queued and running request, releases resident factors and stops the threads. */
+int km_serve_destroy(km_server* s);
+
 /* ---- streams and profiling ---------------------------------------------------------------- */
 
 /* Runs the handle's work on `stream` (a cudaStream_t of the handle's device; NULL restores the

@@ -214,6 +214,23 @@ void dfree(km_handle* h, void* p) {
   }
 }
 
+// Capacity-based allocation: keeps *p when its allocation already holds `count` elements, so a
+// handle that serves problems of varying size reallocates only when a larger one arrives.
+template <typename T>
+int grow(km_handle* h, T** p, int64_t count) {
+  const size_t bytes = (size_t)std::max<int64_t>(count, 1) * sizeof(T);
+  if (*p) {
+    for (auto& a : h->allocs)
+      if (a.first == (void*)*p) {
+        if (a.second >= bytes) return KM_OK;
+        break;
+      }
+    dfree(h, *p);
+    *p = nullptr;
+  }
+  return dalloc(h, p, count);
+}
+
 void free_problem(km_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (auto& a : h->allocs) cudaFree(a.first);
@@ -318,29 +335,22 @@ double timer_stop(km_handle* h) {
 
 int ensure_vec(km_handle* h, int64_t k) {
   if (k <= h->vcap) return KM_OK;
-  dfree(h, h->d_VP);
-  dfree(h, h->d_VG);
-  dfree(h, h->d_VD);
-  h->d_VP = h->d_VG = h->d_VD = nullptr;
   h->vcap = 0;
   const int64_t slots = h->tree.nleaf + h->tree.nnode;
   int rc;
-  if ((rc = dalloc(h, &h->d_VP, slots * h->r * k)) != KM_OK) return rc;
-  if ((rc = dalloc(h, &h->d_VG, slots * h->r * k)) != KM_OK) return rc;
-  if ((rc = dalloc(h, &h->d_VD, std::max<int64_t>(h->tree.nnode, 1) * 2 * h->r * k)) != KM_OK) return rc;
+  if ((rc = grow(h, &h->d_VP, slots * h->r * k)) != KM_OK) return rc;
+  if ((rc = grow(h, &h->d_VG, slots * h->r * k)) != KM_OK) return rc;
+  if ((rc = grow(h, &h->d_VD, std::max<int64_t>(h->tree.nnode, 1) * 2 * h->r * k)) != KM_OK) return rc;
   h->vcap = k;
   return KM_OK;
 }
 
 int ensure_xy(km_handle* h, int64_t k) {
   if (k <= h->xcap) return KM_OK;
-  dfree(h, h->d_X);
-  dfree(h, h->d_Y);
-  h->d_X = h->d_Y = nullptr;
   h->xcap = 0;
   int rc;
-  if ((rc = dalloc(h, &h->d_X, h->tree.n * k)) != KM_OK) return rc;
-  if ((rc = dalloc(h, &h->d_Y, h->tree.n * k)) != KM_OK) return rc;
+  if ((rc = grow(h, &h->d_X, h->tree.n * k)) != KM_OK) return rc;
+  if ((rc = grow(h, &h->d_Y, h->tree.n * k)) != KM_OK) return rc;
   h->xcap = k;
   return KM_OK;
 }
@@ -564,11 +574,8 @@ int refine(km_handle* h, const double* d_b, double* d_x, int k) {
   cudaStream_t st = h->stream;
   int rc;
   if (k > h->rcap) {
-    dfree(h, h->d_res);
-    dfree(h, h->d_rdots);
-    h->d_res = h->d_rdots = nullptr;
     h->rcap = 0;
-    if ((rc = dalloc(h, &h->d_res, t.n * k)) || (rc = dalloc(h, &h->d_rdots, 2 * k))) return rc;
+    if ((rc = grow(h, &h->d_res, t.n * k)) || (rc = grow(h, &h->d_rdots, 2 * k))) return rc;
     h->rcap = k;
   }
   std::vector<double> dots(2 * k);
@@ -634,20 +641,16 @@ int derivative_apply(km_handle* h, int j, const double* X, double* Y, int k) {
   const int r = h->r;
   cudaStream_t st = h->stream;
   int rc;
-  if (!h->d_dK) {
+  if (h->dk_param < 0) {
     int64_t kbytes = 0;
     for (int64_t q = 0; q < t.nleaf; ++q) kbytes += t.leaf_size(q) * t.leaf_size(q);
-    if ((rc = dalloc(h, &h->d_dK, kbytes)) || (rc = dalloc(h, &h->d_dPhi, t.n * r)) ||
-        (rc = dalloc(h, &h->d_Sj, r * r)))
+    if ((rc = grow(h, &h->d_dK, kbytes)) || (rc = grow(h, &h->d_dPhi, t.n * r)) || (rc = grow(h, &h->d_Sj, r * r)))
       return rc;
   }
   if (k > h->gcap) {
-    dfree(h, h->d_GP);
-    dfree(h, h->d_GG);
-    h->d_GP = h->d_GG = nullptr;
     h->gcap = 0;
     const int64_t slots = t.nleaf + t.nnode;
-    if ((rc = dalloc(h, &h->d_GP, slots * 2 * r * k)) || (rc = dalloc(h, &h->d_GG, slots * 2 * r * k))) return rc;
+    if ((rc = grow(h, &h->d_GP, slots * 2 * r * k)) || (rc = grow(h, &h->d_GG, slots * 2 * r * k))) return rc;
     h->gcap = k;
   }
   if (h->dk_param != j) {
@@ -1074,8 +1077,14 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   if (maxrank > kMaxNysRank) return fail(h, KM_ERR_UNSUPPORTED, "Nystrom rank above 80 is not supported");
   // Buffers are kept when the problem shape (n, levels, rank) is unchanged, so that repeated
   // assemblies (likelihood evaluations at new parameters) allocate nothing.
+  // A new shape keeps every allocation that is large enough (grow); only a handle that last
+  // held an ACA problem starts from scratch.
+  if (h->d_blk) free_problem(h);
   const bool reuse = h->d_pts && h->tree.n == t.n && h->tree.L == t.L && h->r == (int)maxrank;
-  if (!reuse) free_problem(h);
+  if (!reuse) {
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->vcap = h->xcap = h->gcap = h->tcap = h->rcap = 0;
+  }
   h->tree = t;
   h->kp = KParams{kernel_id, params[0], params[1], params[2]};
   h->method = method;
@@ -1089,20 +1098,20 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   for (int64_t j = 0; j < t.nleaf; ++j) kbytes += t.leaf_size(j) * t.leaf_size(j);
   int rc;
   if (!reuse &&
-      ((rc = dalloc(h, &h->d_pts, 2 * n)) || (rc = dalloc(h, &h->d_lnd, 2 * r)) ||
-       (rc = dalloc(h, &h->d_lndidx, r)) || (rc = dalloc(h, &h->d_K, kbytes)) ||
-       (rc = dalloc(h, &h->d_Lf, kbytes)) || (rc = dalloc(h, &h->d_Phi, n * r)) ||
-       (rc = dalloc(h, &h->d_Q, n * r)) || (rc = dalloc(h, &h->d_tauleaf, t.nleaf * r)) ||
-       (rc = dalloc(h, &h->d_R, (t.nleaf + t.nnode) * r * r)) || (rc = dalloc(h, &h->d_S, r * r)) ||
-       (rc = dalloc(h, &h->d_Sc, r * r)) || (rc = dalloc(h, &h->d_SinvT, r * r)) || (rc = dalloc(h, &h->d_SinvTf, r * r)) ||
-       (rc = dalloc(h, &h->d_Ct, std::max<int64_t>(t.nnode, 1) * r * r)) ||
-       (rc = dalloc(h, &h->d_L22, std::max<int64_t>(t.nnode, 1) * r * r)) ||
-       (rc = dalloc(h, &h->d_Eref, std::max<int64_t>(t.nnode, 1) * r * r)) ||
-       (rc = dalloc(h, &h->d_Etau, std::max<int64_t>(t.nnode, 1) * r)) ||
-       (rc = dalloc(h, &h->d_L22i, std::max<int64_t>(t.nnode, 1) * r * r)) ||
-       (rc = dalloc(h, &h->d_E, std::max<int64_t>(t.nnode, 1) * 2 * r * r)) ||
-       (rc = dalloc(h, &h->d_info, t.nleaf + t.nnode + 1)) ||
-       (rc = dalloc(h, &h->d_partial, kLogdetBlocks)) || (rc = dalloc(h, &h->d_scalar, 4)))) {
+      ((rc = grow(h, &h->d_pts, 2 * n)) || (rc = grow(h, &h->d_lnd, 2 * r)) ||
+       (rc = grow(h, &h->d_lndidx, r)) || (rc = grow(h, &h->d_K, kbytes)) ||
+       (rc = grow(h, &h->d_Lf, kbytes)) || (rc = grow(h, &h->d_Phi, n * r)) ||
+       (rc = grow(h, &h->d_Q, n * r)) || (rc = grow(h, &h->d_tauleaf, t.nleaf * r)) ||
+       (rc = grow(h, &h->d_R, (t.nleaf + t.nnode) * r * r)) || (rc = grow(h, &h->d_S, r * r)) ||
+       (rc = grow(h, &h->d_Sc, r * r)) || (rc = grow(h, &h->d_SinvT, r * r)) || (rc = grow(h, &h->d_SinvTf, r * r)) ||
+       (rc = grow(h, &h->d_Ct, std::max<int64_t>(t.nnode, 1) * r * r)) ||
+       (rc = grow(h, &h->d_L22, std::max<int64_t>(t.nnode, 1) * r * r)) ||
+       (rc = grow(h, &h->d_Eref, std::max<int64_t>(t.nnode, 1) * r * r)) ||
+       (rc = grow(h, &h->d_Etau, std::max<int64_t>(t.nnode, 1) * r)) ||
+       (rc = grow(h, &h->d_L22i, std::max<int64_t>(t.nnode, 1) * r * r)) ||
+       (rc = grow(h, &h->d_E, std::max<int64_t>(t.nnode, 1) * 2 * r * r)) ||
+       (rc = grow(h, &h->d_info, t.nleaf + t.nnode + 1)) ||
+       (rc = grow(h, &h->d_partial, kLogdetBlocks)) || (rc = grow(h, &h->d_scalar, 4)))) {
     free_problem(h);
     return rc;
   }
@@ -1408,9 +1417,9 @@ int km_derivative_matvec(km_handle* h, int param, const double* x, double* y, in
 //   g_j = 0.5 (mean_v t_v' dK_j t_v - alpha' dK_j alpha).
 // The data term y' K^{-1} dK_j K^{-1} y of HODLR_grad_term (stochasticgradient.jl:22-25) is
 // evaluated as alpha' dK_j alpha, which is the same quantity since K^{-1} is symmetric.
-int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t nprobe, double* nll,
-                double* grad) {
-  if (!h || !y || !nll || nprobe < 0 || (grad && (nprobe < 1 || !probes)))
+static int nll_grad_impl(km_handle* h, const double* y, const double* probes, bool seeded, uint64_t seed,
+                         int64_t nprobe, double* nll, double* grad) {
+  if (!h || !y || !nll || nprobe < 0 || (grad && (nprobe < 1 || (!probes && !seeded))))
     return fail(h, KM_ERR_BAD_ARG, "bad likelihood arguments");
   cudaSetDevice(h->cfg.device);
   if (!h->factorized) return fail(h, KM_ERR_STATE, "The HODLR matrix needs to be factorized for this.");
@@ -1422,12 +1431,8 @@ int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t npr
   int rc;
   timer_start(h);
   if (kk > h->tcap) {
-    dfree(h, h->d_T);
-    dfree(h, h->d_U);
-    dfree(h, h->d_dots);
-    h->d_T = h->d_U = h->d_dots = nullptr;
     h->tcap = 0;
-    if ((rc = dalloc(h, &h->d_T, n * kk)) || (rc = dalloc(h, &h->d_U, n * kk)) || (rc = dalloc(h, &h->d_dots, kk)))
+    if ((rc = grow(h, &h->d_T, n * kk)) || (rc = grow(h, &h->d_U, n * kk)) || (rc = grow(h, &h->d_dots, kk)))
       return rc;
     h->tcap = kk;
   }
@@ -1451,7 +1456,10 @@ int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t npr
   for (int64_t i = 0; i < n; ++i) ya += y[i] * a[i];
   *nll = 0.5 * ld + 0.5 * ya;
   if (grad) {
-    KM_CUDA(h, cudaMemcpyAsync(h->d_T, probes, sizeof(double) * n * p, cudaMemcpyHostToDevice, st));
+    if (seeded)
+      KLV(h, KM_PROF_OTHER, launch_rademacher(h->d_T, n, p, seed, st));
+    else
+      KM_CUDA(h, cudaMemcpyAsync(h->d_T, probes, sizeof(double) * n * p, cudaMemcpyHostToDevice, st));
     if ((rc = nested_bwd(h, h->d_T, (int)p)) != KM_OK) return rc;  // T = W'^{-1} V
     std::vector<double> dots(kk);
     for (int j = 0; j < 3; ++j) {
@@ -1466,6 +1474,16 @@ int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t npr
   }
   h->stats.grad_ms = timer_stop(h);
   return sync(h, "nll_grad");
+}
+
+int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t nprobe, double* nll,
+                double* grad) {
+  return nll_grad_impl(h, y, probes, false, 0, nprobe, nll, grad);
+}
+
+int km_nll_grad_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed, double* nll,
+                       double* grad) {
+  return nll_grad_impl(h, y, nullptr, true, seed, nprobe, nll, grad);
 }
 
 }  // extern "C"
@@ -1532,4 +1550,34 @@ extern "C" int km_solve_noalloc(km_handle* h, const double* d_b, double* d_x, in
   h->prof = prof;
   if (rc != KM_OK) return rc;
   return sync(h, "solve_noalloc");
+}
+
+// ---- memory management helpers for the batched and serving forms ----------------------------
+
+extern "C" int km_trim(km_handle* h) {
+  if (!h) return KM_ERR_BAD_ARG;
+  cudaSetDevice(h->cfg.device);
+  free_problem(h);
+  return KM_OK;
+}
+
+// Mirrors the allocations of assemble_impl (Nystrom), ensure_vec, ensure_xy, derivative_apply
+// and nll_grad_impl for one problem shape.
+extern "C" int64_t km_estimate_bytes(int64_t n, int64_t rank, int level_kind, int64_t level, int64_t ncols,
+                          int with_grad) {
+  Tree t;
+  std::string msg;
+  if (rank < 1 || ncols < 0 || !build_tree(n, level_kind, level, &t, &msg)) return -1;
+  const int64_t r = rank, k = std::max<int64_t>(ncols, 1);
+  const int64_t nn = std::max<int64_t>(t.nnode, 1), slots = t.nleaf + t.nnode;
+  int64_t kb = 0;
+  for (int64_t j = 0; j < t.nleaf; ++j) kb += t.leaf_size(j) * t.leaf_size(j);
+  auto d = [](int64_t c) { return 8 * std::max<int64_t>(c, 1); };
+  int64_t b = d(2 * n) + d(2 * r) + d(r) + 2 * d(kb) + 2 * d(n * r) + d(t.nleaf * r) + d(slots * r * r) +
+              4 * d(r * r) + 3 * d(nn * r * r) + d(nn * r) + d(nn * r * r) + d(nn * 2 * r * r) +
+              4 * std::max<int64_t>(t.nleaf + t.nnode + 1, 1) + d(kLogdetBlocks) + d(4);
+  b += 2 * d(slots * r * k) + d(nn * 2 * r * k);  // ensure_vec
+  b += 2 * d(n * k);                              // ensure_xy
+  if (with_grad) b += d(kb) + d(n * r) + d(r * r) + 2 * d(slots * 2 * r * k) + 2 * d(n * k) + d(k);
+  return b;
 }

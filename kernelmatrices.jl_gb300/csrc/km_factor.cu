@@ -604,8 +604,17 @@ void launch_from_ff(const ff* in, double* out, int64_t n, cudaStream_t st) {
 // Solve operators of the nodes of one level, formed off the critical path (side stream):
 // L22^{-1} (lower) and the explicit transfer E = H_0 ... H_{r-1} [I; 0] (2r x r) from the
 // reflectors of QR(G_N).  One CTA per node; columns are independent.
+// Per node of one level: L22^{-1} (lower) and, below the root, the explicit 2r x r factor E
+// of G = E R_N from the structured reflectors.  One warp per column; the column lives in
+// registers (row i in lane i % 32, slot i / 32, r <= 96), so the dependent chains need no
+// block barriers.  Runs on the side stream, overlapped with the next level's node kernel.
 template <typename T>
-__global__ void __launch_bounds__(256) k_node_finalize(const T* __restrict__ L22, const T* __restrict__ Eref,
+__device__ __forceinline__ T slot_get(const T (&x)[3], int s) {
+  return s == 0 ? x[0] : (s == 1 ? x[1] : x[2]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) k_node_finalize(const T* __restrict__ L22, const T* __restrict__ Eref,
                                                        const T* __restrict__ Etau, int r, int64_t nbase, int with_e,
                                                        T* __restrict__ L22i, T* __restrict__ Eexp) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -616,7 +625,7 @@ __global__ void __launch_bounds__(256) k_node_finalize(const T* __restrict__ L22
   T* ts = Vs + r * ld;      // tau
   const int64_t node = nbase + blockIdx.x;
   const int64_t off = node * (int64_t)r * r;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
   for (int e = tid; e < r * r; e += blockDim.x) {
     const int i = e % r, c = e / r;
     Ls[i + c * ld] = L22[off + e];
@@ -625,34 +634,62 @@ __global__ void __launch_bounds__(256) k_node_finalize(const T* __restrict__ L22
   if (with_e)
     for (int e = tid; e < r; e += blockDim.x) ts[e] = Etau[node * (int64_t)r + e];
   __syncthreads();
-  // L22^{-1}: thread per column, forward substitution
-  for (int c = tid; c < r; c += blockDim.x) {
+  // L22^{-1} e_c by forward substitution in column (axpy) order: row i accumulates
+  // -L[i,p] x_p for p = c .. i-1 and is then divided by L[i,i]
+  for (int c = w; c < r; c += nw) {
+    T x[3];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) x[s] = T((lane + 32 * s) == c ? 1.0 : 0.0);
+    for (int p = c; p < r; ++p) {
+      const T xp = shfl_idx(slot_get(x, p >> 5), p & 31) / Ls[p + p * ld];
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        const int i = lane + 32 * s;
+        if (i == p) x[s] = xp;
+        else if (i > p && i < r) x[s] -= Ls[i + p * ld] * xp;
+      }
+    }
     T* out = L22i + off + (int64_t)c * r;
-    for (int i = 0; i < c; ++i) out[i] = T(0.0);
-    for (int i = c; i < r; ++i) {
-      T v = T(i == c ? 1.0 : 0.0);
-      for (int p = c; p < i; ++p) v -= Ls[i + p * ld] * out[p];
-      out[i] = v / Ls[i + i * ld];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int i = lane + 32 * s;
+      if (i < r) out[i] = x[s];
     }
   }
   if (!with_e) return;
-  // E columns: thread per column c applies H_{r-1}, ..., H_0 to [e_c; 0] (only H_j, j <= c, act)
+  // column c of E: H_c ... H_0 applied in turn (j = c down to 0) to [e_c ; 0]; H_j acts on
+  // top row j and the whole bottom, so top row j is final once H_j has acted
   T* Eo = Eexp + node * (int64_t)2 * r * r;
-  for (int c = tid; c < r; c += blockDim.x) {
+  for (int c = w; c < r; c += nw) {
     T* top = Eo + (int64_t)c * 2 * r;
     T* bot = top + r;
-    for (int i = 0; i < r; ++i) {
-      top[i] = T(i == c ? 1.0 : 0.0);
-      bot[i] = T(0.0);
-    }
+    T b[3] = {T(0.0), T(0.0), T(0.0)};
+    for (int i = c + 1 + lane; i < r; i += 32) top[i] = T(0.0);
     for (int j = c; j >= 0; --j) {
       const T tj = ts[j];
-      if (tj == 0.0) continue;
-      T acc = top[j];
-      for (int i = 0; i < r; ++i) acc += Vs[i + j * ld] * bot[i];
-      acc = acc * tj;
-      top[j] -= acc;
-      for (int i = 0; i < r; ++i) bot[i] -= acc * Vs[i + j * ld];
+      const T tjtop = T(j == c ? 1.0 : 0.0);
+      if (tj == 0.0) {
+        if (lane == 0) top[j] = tjtop;
+        continue;
+      }
+      T part = T(0.0);
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        const int i = lane + 32 * s;
+        if (i < r) part += Vs[i + j * ld] * b[s];
+      }
+      const T acc = (tjtop + warp_sum_t(part)) * tj;
+      if (lane == 0) top[j] = tjtop - acc;
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        const int i = lane + 32 * s;
+        if (i < r) b[s] -= acc * Vs[i + j * ld];
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int i = lane + 32 * s;
+      if (i < r) bot[i] = b[s];
     }
   }
 }
@@ -673,7 +710,7 @@ void launch_node_finalize(const T* L22, const T* Eref, const T* Etau, int r, int
                           T* Eexp, cudaStream_t st) {
   const size_t sm = ((size_t)2 * r * (r + 1) + r) * sizeof(T);
   cudaFuncSetAttribute(k_node_finalize<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_node_finalize<T><<<(unsigned)t.nodes_at(level), 128, sm, st>>>(L22, Eref, Etau, r, t.node_off[level],
+  k_node_finalize<T><<<(unsigned)t.nodes_at(level), 512, sm, st>>>(L22, Eref, Etau, r, t.node_off[level],
                                                                    level < t.L ? 1 : 0, L22i, Eexp);
 }
 

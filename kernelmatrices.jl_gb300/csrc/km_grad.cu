@@ -139,6 +139,27 @@ __global__ void k_axpby(double* __restrict__ y, const double* __restrict__ x, do
     y[i] = a * x[i] + b * y[i];
 }
 
+// SplitMix64 finaliser (Steele, Lea and Flood, "Fast splittable pseudorandom number
+// generators", OOPSLA 2014).  Probe entry (i, j) of an n x p block is +1 when the top bit of
+// mix(mix(seed) + j*n + i) is set and -1 otherwise.
+__device__ __forceinline__ uint64_t splitmix64_mix(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+__global__ void k_rademacher(double* __restrict__ out, int64_t total, uint64_t seed) {
+  const uint64_t base = splitmix64_mix(seed);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = (splitmix64_mix(base + (uint64_t)e) >> 63) ? 1.0 : -1.0;
+}
+
+void launch_rademacher(double* out, int64_t n, int64_t p, uint64_t seed, cudaStream_t st) {
+  const int64_t total = n * p;
+  k_rademacher<<<(unsigned)std::min<int64_t>((total + 255) / 256, 4096), 256, 0, st>>>(out, total, seed);
+}
+
 void launch_axpby(double* y, const double* x, double a, double b, int64_t n, cudaStream_t st) {
   k_axpby<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(y, x, a, b, n);
 }

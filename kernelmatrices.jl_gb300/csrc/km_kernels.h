@@ -120,6 +120,8 @@ void launch_leaf_dnys_apply(const double* dKl, const double* Phi, const double* 
                             const double* Sj, int r, const Tree& t, const double* X, int64_t ldx,
                             const double* VG, double* Y, int64_t ldy, int k, cudaStream_t st);
 void launch_axpby(double* y, const double* x, double a, double b, int64_t n, cudaStream_t st);
+// n x p Rademacher probes (+-1), entry (i, j) from a SplitMix64 hash of (seed, j*n + i)
+void launch_rademacher(double* out, int64_t n, int64_t p, uint64_t seed, cudaStream_t st);
 void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n, int k,
                      double* out, cudaStream_t st);
 

@@ -10,3 +10,4 @@ from .hodlr import (  # noqa: F401
     probe_fp32_tflops,
     negloglik, stoch_gradient, nll_objective,
 )
+from .serving import BatchEngine, Server, Problem, Result, estimate_bytes  # noqa: F401

@@ -44,6 +44,45 @@ class KmStats(C.Structure):
                 ("refine_iterations", C.c_int), ("refine_residual", C.c_double)]
 
 
+KM_REQ_NLL_GRAD = 0
+KM_REQ_FACTOR = 1
+KM_REQ_SOLVE = 2
+KM_REQ_RELEASE = 3
+
+
+class KmProblem(C.Structure):
+    _fields_ = [("n", C.c_int64), ("pts", C.POINTER(C.c_double)), ("y", C.POINTER(C.c_double)),
+                ("params", C.c_double * 3)]
+
+
+class KmBatchOpts(C.Structure):
+    _fields_ = [("kernel_id", C.c_int), ("rank", C.c_int64), ("level_kind", C.c_int), ("level", C.c_int64),
+                ("nprobe", C.c_int64), ("probe_seed", C.c_uint64)]
+
+
+class KmRequest(C.Structure):
+    _fields_ = [("kind", C.c_int), ("prob", KmProblem), ("nprobe", C.c_int64), ("probe_seed", C.c_uint64),
+                ("factor_id", C.c_int64), ("b", C.POINTER(C.c_double)), ("x", C.POINTER(C.c_double)),
+                ("nrhs", C.c_int64)]
+
+
+class KmResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("nll", C.c_double), ("grad", C.c_double * 3), ("logdet", C.c_double),
+                ("factor_id", C.c_int64), ("queue_ms", C.c_double), ("run_ms", C.c_double)]
+
+
+class KmServeOpts(C.Structure):
+    _fields_ = [("kernel_id", C.c_int), ("rank", C.c_int64), ("level_kind", C.c_int), ("level", C.c_int64),
+                ("nworkers", C.c_int)]
+
+
+class KmServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("rejected", C.c_int64), ("resident_factors", C.c_int64), ("bytes_in_use", C.c_int64),
+                ("peak_bytes", C.c_int64), ("budget_bytes", C.c_int64), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("mean_ms", C.c_double)]
+
+
 _P = C.c_void_p
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int64)
@@ -83,6 +122,19 @@ SIGNATURES = {
     "km_profile_enable": (C.c_int, [_H, C.c_int]),
     "km_profile_get": (C.c_int, [_H, C.c_int, _DP, _IP]),
     "km_solve_noalloc": (C.c_int, [_H, _P, _P, C.c_int64]),
+    "km_nll_grad_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP]),
+    "km_trim": (C.c_int, [_H]),
+    "km_estimate_bytes": (C.c_int64, [C.c_int64, C.c_int64, C.c_int, C.c_int64, C.c_int64, C.c_int]),
+    "km_batch_create": (C.c_int, [C.POINTER(KmConfig), C.c_int, C.POINTER(_P)]),
+    "km_batch_destroy": (C.c_int, [_P]),
+    "km_batch_nll_grad": (C.c_int, [_P, C.POINTER(KmBatchOpts), C.c_int64, C.POINTER(KmProblem), _DP, _DP,
+                                    C.POINTER(C.c_int)]),
+    "km_batch_last_error": (C.c_char_p, [_P]),
+    "km_serve_create": (C.c_int, [C.POINTER(KmConfig), C.POINTER(KmServeOpts), C.POINTER(_P)]),
+    "km_serve_submit": (C.c_int, [_P, C.POINTER(KmRequest), C.POINTER(C.c_uint64)]),
+    "km_serve_wait": (C.c_int, [_P, C.c_uint64, C.c_int64, C.POINTER(KmResult)]),
+    "km_serve_stats_get": (C.c_int, [_P, C.POINTER(KmServeStats)]),
+    "km_serve_destroy": (C.c_int, [_P]),
 }
 
 _lib = None

@@ -289,6 +289,19 @@ class KernelHODLR:
         return nll.value, g
 
 
+    def nll_grad_seeded(self, dat: np.ndarray, nprobe: int, seed: int):
+        """``nll_grad`` with ``nprobe`` Rademacher probes drawn on the device: entry (i, j) is +1
+        when the top bit of SplitMix64(SplitMix64(seed) + j*n + i) is set, else -1 (stands in
+        for ``givesaa(n, m; seed)``, src/utils.jl:22-27)."""
+        lib = L.load()
+        y = np.ascontiguousarray(dat, dtype=np.float64).reshape(-1)
+        nll = C.c_double()
+        g = np.zeros(3)
+        _check(self._h, lib.km_nll_grad_seeded(self._h, _dp(y), int(nprobe), int(seed), C.byref(nll),
+                                               _dp(g) if nprobe > 0 else None))
+        return nll.value, (g if nprobe > 0 else None)
+
+
 def symmetricfactorize(K: KernelHODLR) -> None:
     """``symmetricfactorize!`` (src/HODLR/src/symfact.jl:6-49)."""
     _check(K._h, L.load().km_factorize(K._h))

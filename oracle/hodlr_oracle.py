@@ -794,6 +794,26 @@ def hodlr_exact_gradient(K: KernelMatrix, rank: int, lvl, dat: np.ndarray, npara
     return out
 
 
+def _splitmix64_mix(x: np.ndarray) -> np.ndarray:
+    """SplitMix64 finaliser (Steele, Lea and Flood, OOPSLA 2014) on uint64 arrays (wrapping)."""
+    with np.errstate(over="ignore"):
+        x = x + np.uint64(0x9E3779B97F4A7C15)
+        x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return x ^ (x >> np.uint64(31))
+
+
+def rademacher_probes(n: int, p: int, seed: int) -> np.ndarray:
+    """The engine's seeded probe block (n x p): entry (i, j) = +1 when the top bit of
+    SplitMix64(SplitMix64(seed) + j*n + i) is set, else -1.  It stands in for ``givesaa``
+    (src/HODLR/src/utils.jl:22-27), whose Julia generator is not reproduced."""
+    base = _splitmix64_mix(np.array([seed], dtype=np.uint64))[0]
+    with np.errstate(over="ignore"):
+        e = base + np.arange(n * p, dtype=np.uint64)
+    bits = _splitmix64_mix(e) >> np.uint64(63)
+    return np.where(bits == 1, 1.0, -1.0).reshape(p, n).T.copy()
+
+
 def givesaa(length: int, sz: int, seed: int) -> List[np.ndarray]:
     """Rademacher probe vectors as ``givesaa`` (src/HODLR/src/utils.jl:22-27) makes them; the
     generator is NumPy's PCG64 from ``seed`` (Julia's Xoshiro stream is not reproduced)."""

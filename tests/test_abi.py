@@ -7,7 +7,7 @@ ROOT = Path(__file__).resolve().parent.parent
 
 def header_symbols():
     text = (ROOT / "include" / "kmhodlr.h").read_text()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(km_\w+)\s*\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(km_\w+)\s*\(", text, flags=re.M)))
 
 
 def test_header_declares_entry_points():
