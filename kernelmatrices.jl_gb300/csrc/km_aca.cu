@@ -570,7 +570,7 @@ __global__ void k_glogdet(const GNodeDesc* __restrict__ nodes, int nn, double* _
 void launch_aca(const double* pts, KParams kp, const AcaBlock* blocks, int nblocks, int maxcap, double* P,
                 uint8_t* F, int* piv, double rtol, int* rank, int* status, cudaStream_t st) {
   const size_t sm = (size_t)2 * std::max(maxcap, 1) * sizeof(double);
-  cudaFuncSetAttribute(k_aca, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_aca, sm);
   k_aca<<<nblocks, 1024, sm, st>>>(pts, kp, blocks, P, F, piv, rtol, rank, status);
 }
 
@@ -588,7 +588,7 @@ void launch_gapply(const GApplyItem* items, int n, const GNodeDesc* nodes, int m
   if (n <= 0) return;
   dim3 grid((unsigned)n, (unsigned)((maxcols + 7) / 8));
   const size_t sm = (size_t)8 * 3 * std::max(maxr, 1) * sizeof(double);
-  cudaFuncSetAttribute(k_gapply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_gapply, sm);
   k_gapply<<<grid, 256, sm, st>>>(items, nodes, mode, X, Xin, ldX, kX);
 }
 

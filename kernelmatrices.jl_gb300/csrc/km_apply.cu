@@ -48,23 +48,32 @@ __device__ __forceinline__ T dot4(const T* __restrict__ a, int sa, const T* __re
   return (s0 + s1) + (s2 + s3);
 }
 
-constexpr int KC = 16;  // right-hand-side columns per CTA
+constexpr int KC = 16;  // most right-hand-side columns per CTA
 
-// grid = (nodes at level, ceil(k / KC)), block 256.  Every phase is a set of independent dot
-// products (one thread per output entry) separated by barriers; node matrices are read through
-// the L1 cache.
+// Columns per CTA and block size for one level: a level with few nodes spreads its columns over
+// more CTAs so that the sweep of the upper levels still covers the SMs (each CTA's dot products
+// are one node's r x r products on its kcb columns).
+static inline void sweep_shape(int64_t nodes, int k, int* kcb, int* threads) {
+  int c = KC;
+  while (c > 1 && nodes * ((k + c - 1) / c) < 2 * 152) c >>= 1;
+  *kcb = c;
+  *threads = c >= 8 ? 512 : (c >= 4 ? 256 : 128);
+}
+
+// grid = (nodes at level, ceil(k / kcb)).  Every phase is a set of independent dot products (one
+// thread per output entry) separated by barriers; node matrices are read through the L1 cache.
 template <typename T>
 __global__ void __launch_bounds__(512) k_up(NodeMats<T> nm, int level, int L, int64_t cslot0, int64_t nslot0,
-                                            int64_t node0, T* __restrict__ VP, T* __restrict__ VD, int k, int mode) {
+                                            int64_t node0, T* __restrict__ VP, T* __restrict__ VD, int k, int mode, int kcb) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* z = reinterpret_cast<T*>(smraw);   // KC x 2r : [z1 ; z2] per column
+  T* z = reinterpret_cast<T*>(smraw);   // kcb x 2r : [z1 ; z2] per column
   const int r = nm.r, r2 = 2 * r;
-  T* tb = z + KC * r2;                    // KC x r
-  T* ub = tb + KC * r;                    // KC x r
+  T* tb = z + kcb * r2;                    // kcb x r
+  T* ub = tb + kcb * r;                    // kcb x r
   const int64_t kk = blockIdx.x;
   const int64_t node = node0 + kk;
-  const int c0 = blockIdx.y * KC;
-  const int kc = min(KC, k - c0);
+  const int c0 = blockIdx.y * kcb;
+  const int kc = min(kcb, k - c0);
   const int tid = threadIdx.x, nth = blockDim.x;
   for (int e = tid; e < kc * r2; e += nth) {
     const int c = e / r2, i = e % r2;
@@ -136,16 +145,16 @@ __global__ void __launch_bounds__(512) k_up(NodeMats<T> nm, int level, int L, in
 template <typename T>
 __global__ void __launch_bounds__(512) k_down(NodeMats<T> nm, int level, int L, int64_t cslot0, int64_t nslot0,
                                               int64_t node0, const T* __restrict__ VP, T* __restrict__ VG,
-                                              const T* __restrict__ VD, int k, int mode) {
+                                              const T* __restrict__ VD, int k, int mode, int kcb) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* g = reinterpret_cast<T*>(smraw);   // KC x r  (parent coefficient)
+  T* g = reinterpret_cast<T*>(smraw);   // kcb x r  (parent coefficient)
   const int r = nm.r, r2 = 2 * r;
-  T* base = g + KC * r;                   // KC x 2r (E g)
-  T* tb = base + KC * r2;                 // KC x 2r scratch
+  T* base = g + kcb * r;                   // kcb x 2r (E g)
+  T* tb = base + kcb * r2;                 // kcb x 2r scratch
   const int64_t kk = blockIdx.x;
   const int64_t node = node0 + kk;
-  const int c0 = blockIdx.y * KC;
-  const int kc = min(KC, k - c0);
+  const int c0 = blockIdx.y * kcb;
+  const int kc = min(kcb, k - c0);
   const int tid = threadIdx.x, nth = blockDim.x;
   const bool top = (level >= L);
   for (int e = tid; e < kc * r; e += nth) {
@@ -313,11 +322,13 @@ template <typename T>
 void launch_up(const Tree& t, const NodeMatsH& h, int level, T* VP, T* VD, int k, int mode, cudaStream_t st) {
   NodeMats<T> nm{reinterpret_cast<const T*>(h.Ct), reinterpret_cast<const T*>(h.L22),
                  reinterpret_cast<const T*>(h.L22i), reinterpret_cast<const T*>(h.E), h.r};
-  dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + KC - 1) / KC));
-  const size_t sm = (size_t)KC * 4 * h.r * sizeof(T);
-  cudaFuncSetAttribute(k_up<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_up<T><<<grid, 512, sm, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
-                                 t.node_off[level], VP, VD, k, mode);
+  int kcb, nth;
+  sweep_shape(t.nodes_at(level), k, &kcb, &nth);
+  dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + kcb - 1) / kcb));
+  const size_t sm = (size_t)kcb * 4 * h.r * sizeof(T);
+  smem_limit((const void*)k_up<T>, sm);
+  k_up<T><<<grid, nth, sm, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
+                                 t.node_off[level], VP, VD, k, mode, kcb);
 }
 
 template <typename T>
@@ -325,18 +336,20 @@ void launch_down(const Tree& t, const NodeMatsH& h, int level, const T* VP, T* V
                  cudaStream_t st) {
   NodeMats<T> nm{reinterpret_cast<const T*>(h.Ct), reinterpret_cast<const T*>(h.L22),
                  reinterpret_cast<const T*>(h.L22i), reinterpret_cast<const T*>(h.E), h.r};
-  dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + KC - 1) / KC));
-  const size_t sm = (size_t)KC * 5 * h.r * sizeof(T);
-  cudaFuncSetAttribute(k_down<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_down<T><<<grid, 512, sm, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
-                                   t.node_off[level], VP, VG, VD, k, mode);
+  int kcb, nth;
+  sweep_shape(t.nodes_at(level), k, &kcb, &nth);
+  dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + kcb - 1) / kcb));
+  const size_t sm = (size_t)kcb * 5 * h.r * sizeof(T);
+  smem_limit((const void*)k_down<T>, sm);
+  k_down<T><<<grid, nth, sm, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
+                                   t.node_off[level], VP, VG, VD, k, mode, kcb);
 }
 
 void launch_leaf_phiT(const double* Phi, int r, const Tree& t, const double* X, int64_t ldx, double* VP,
                       int k, cudaStream_t st) {
   dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
   const size_t sm = (size_t)8 * t.max_leaf * sizeof(double);
-  cudaFuncSetAttribute(k_leaf_phiT, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_leaf_phiT, sm);
   k_leaf_phiT<<<grid, 256, sm, st>>>(Phi, r, dtree(t), X, ldx, VP, k);
 }
 void launch_leaf_nys_apply(const double* Kl, const double* Phi, const double* Sc, int r, const Tree& t,
@@ -344,7 +357,7 @@ void launch_leaf_nys_apply(const double* Kl, const double* Phi, const double* Sc
                            cudaStream_t st) {
   dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
   const size_t sm = (size_t)8 * (t.max_leaf + r) * sizeof(double);
-  cudaFuncSetAttribute(k_leaf_nys_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_leaf_nys_apply, sm);
   k_leaf_nys_apply<<<grid, 256, sm, st>>>(Kl, Phi, Sc, r, dtree(t), X, ldx, VG, Y, ldy, k);
 }
 

@@ -275,180 +275,233 @@ __global__ void __launch_bounds__(256) k_leaf_formq(T* __restrict__ Pan, const T
 //   if l < L:  G = [R1 ; L22^{-1}(R2 - Ct' R1)],  Householder QR  G = E R_N  (structured:
 //              reflector j is e_j on top plus a dense bottom part, kept in Eref[:, j])
 // Outputs per node: Ct, L22 (lower), Eref (r x r), Etau (r), R_N into slot N.
-// Shared memory: four r x (r+1) matrices.
+//
+// Work mapping: the products are split into (column c, 32-row chunk s) items, one warp per
+// item, lane = row, so that no index needs a division by r and the warps stay converged.  The
+// Cholesky factorises without scaling inside the loop (a_ik -= a_ij a_kj / d_j, one barrier per
+// column; the columns are scaled by sqrt(d_j) at the end), the triangular solve keeps each
+// right-hand-side column in the registers of one warp (no barriers), and every warp forms the
+// norm of the next reflector itself, so the QR needs one barrier per reflector.
+// Shared memory: four r x (r+1) matrices and two r-vectors.
 // ---------------------------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(256) k_node_factor(T* __restrict__ R, const T* __restrict__ SinvT,
+__device__ __forceinline__ T sel(bool p, T a) {
+  return p ? a : T(0.0);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) k_node_factor(T* __restrict__ R, const T* __restrict__ SinvT,
                                                      int r, int level, int L, int64_t nleaf,
                                                      int64_t cbase, int64_t nbase, T* __restrict__ Ct_out,
                                                      T* __restrict__ L22_out, T* __restrict__ Eref,
                                                      T* __restrict__ Etau, int* __restrict__ info) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
-  __shared__ T red[32];
-  __shared__ T sh[2];
   const int ld = r + 1;
   T* X0 = sm;
   T* X1 = X0 + r * ld;
   T* X2 = X1 + r * ld;
   T* X3 = X2 + r * ld;
+  T* va = X3 + r * ld;  // r values: sqrt(d_j), then the reflector betas
+  T* vb = va + r;       // r values: 1 / L22[j][j], then the reflector scales
   const int64_t k = blockIdx.x;
   const int64_t node = nbase + k;  // node index within all nodes (level-major)
   const T* R1 = R + (cbase + 2 * k) * (int64_t)r * r;
   const T* R2 = R + (cbase + 2 * k + 1) * (int64_t)r * r;
   const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
+  const int nch = (r + 31) >> 5;   // 32-row chunks per column (r <= 96)
+  const int nitems = r * nch;
   // load: X0 = Sc^{-T} (upper), X1 = R1, X2 = R2   (element (i,c) at i + c*ld)
-  for (int e = tid; e < r * r; e += nth) {
-    const int i = e % r, c = e / r;
-    X0[i + c * ld] = SinvT[e];
-    X1[i + c * ld] = R1[e];
-    X2[i + c * ld] = R2[e];
-  }
-  __syncthreads();
-  // T1 = R1 Sc^{-T} -> X3 (upper x upper: entries l in [i, c])
-  for (int e = tid; e < r * r; e += nth) {
-    const int i = e % r, c = e / r;
-    T acc = T(0.0);
-    if (i <= c) {
-#pragma unroll 4
-      for (int l = i; l <= c; ++l) acc += X1[i + l * ld] * X0[l + c * ld];
+  for (int c = w; c < r; c += nw)
+    for (int i = lane; i < r; i += 32) {
+      const int e = i + c * r;
+      X0[i + c * ld] = SinvT[e];
+      X1[i + c * ld] = R1[e];
+      X2[i + c * ld] = R2[e];
     }
-    X3[i + c * ld] = acc;
+  __syncthreads();
+  // T1 = R1 Sc^{-T} -> X3: T1[i][c] = sum_{l = i..c} R1[i][l] Sinv[l][c]
+  for (int q = w; q < nitems; q += nw) {
+    const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
+    T a0 = T(0.0), a1 = T(0.0);
+    int l = 32 * s;
+    for (; l + 1 <= c; l += 2) {
+      a0 += sel(l >= i, X1[ii + l * ld]) * X0[l + c * ld];
+      a1 += sel(l + 1 >= i, X1[ii + (l + 1) * ld]) * X0[l + 1 + c * ld];
+    }
+    if (l <= c) a0 += sel(l >= i, X1[ii + l * ld]) * X0[l + c * ld];
+    if (i < r) X3[i + c * ld] = a0 + a1;
   }
   __syncthreads();
   // T2 = R2 Sc^{-T} -> X1
-  for (int e = tid; e < r * r; e += nth) {
-    const int i = e % r, c = e / r;
-    T acc = T(0.0);
-    if (i <= c) {
-#pragma unroll 4
-      for (int l = i; l <= c; ++l) acc += X2[i + l * ld] * X0[l + c * ld];
+  for (int q = w; q < nitems; q += nw) {
+    const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
+    T a0 = T(0.0), a1 = T(0.0);
+    int l = 32 * s;
+    for (; l + 1 <= c; l += 2) {
+      a0 += sel(l >= i, X2[ii + l * ld]) * X0[l + c * ld];
+      a1 += sel(l + 1 >= i, X2[ii + (l + 1) * ld]) * X0[l + 1 + c * ld];
     }
-    X1[i + c * ld] = acc;
+    if (l <= c) a0 += sel(l >= i, X2[ii + l * ld]) * X0[l + c * ld];
+    if (i < r) X1[i + c * ld] = a0 + a1;
   }
   __syncthreads();
-  // Ct = T1 T2' -> X0 ; Ct[i][c] = sum_{l >= max(i,c)} T1[i][l] T2[c][l]
-  for (int e = tid; e < r * r; e += nth) {
-    const int i = e % r, c = e / r;
-    T acc = T(0.0);
-#pragma unroll 4
-    for (int l = max(i, c); l < r; ++l) acc += X3[i + l * ld] * X1[c + l * ld];
-    X0[i + c * ld] = acc;
-  }
-  __syncthreads();
-  // H = I - Ct' Ct -> X3 (lower triangle)
-  for (int e = tid; e < r * r; e += nth) {
-    const int i = e % r, c = e / r;
-    if (i >= c) {
-      T acc = T(0.0);
-#pragma unroll 4
-      for (int l = 0; l < r; ++l) acc += X0[l + i * ld] * X0[l + c * ld];
-      X3[i + c * ld] = T(i == c ? 1.0 : 0.0) - acc;
+  // Ct = T1 T2' -> X0: Ct[i][c] = sum_{l >= max(i, c)} T1[i][l] T2[c][l]
+  for (int q = w; q < nitems; q += nw) {
+    const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
+    T a0 = T(0.0), a1 = T(0.0);
+    int l = max(32 * s, c);
+    for (; l + 1 < r; l += 2) {
+      a0 += sel(l >= i, X3[ii + l * ld]) * X1[c + l * ld];
+      a1 += sel(l + 1 >= i, X3[ii + (l + 1) * ld]) * X1[c + (l + 1) * ld];
     }
+    if (l < r) a0 += sel(l >= i, X3[ii + l * ld]) * X1[c + l * ld];
+    if (i < r) X0[i + c * ld] = a0 + a1;
   }
   __syncthreads();
-  // L22 = chol(H) in place (lower)
+  // H = I - Ct' Ct -> X3 (lower triangle); R1 is reloaded into X1 for the QR meanwhile
+  if (level < L)
+    for (int c = w; c < r; c += nw)
+      for (int i = lane; i < r; i += 32) X1[i + c * ld] = R1[i + c * r];
+  for (int q = w; q < nitems; q += nw) {
+    const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
+    if (32 * s + 31 < c) continue;
+    T a0 = T(0.0), a1 = T(0.0);
+    int l = 0;
+    for (; l + 1 < r; l += 2) {
+      a0 += X0[l + ii * ld] * X0[l + c * ld];
+      a1 += X0[l + 1 + ii * ld] * X0[l + 1 + c * ld];
+    }
+    if (l < r) a0 += X0[l + ii * ld] * X0[l + c * ld];
+    if (i < r && i >= c) X3[i + c * ld] = T(i == c ? 1.0 : 0.0) - (a0 + a1);
+  }
+  __syncthreads();
+  // L22 = chol(H): unscaled right-looking elimination, a_ik -= a_ij a_kj / d_j
   int bad = 0;
   for (int j = 0; j < r; ++j) {
     const T d = X3[j + j * ld];
     const bool ok = d > 0.0;
     if (!ok && bad == 0) bad = j + 1;
-    const T sd = ok ? sqrt(d) : T(1.0);
-    __syncthreads();
-    for (int i = j + 1 + tid; i < r; i += nth) X3[i + j * ld] /= sd;
-    if (tid == 0) X3[j + j * ld] = sd;
-    __syncthreads();
-    const int wdt = r - j - 1;
-    for (int e = tid; e < wdt * wdt; e += nth) {
-      const int i = j + 1 + e % wdt, c = j + 1 + e / wdt;
-      if (i >= c) X3[i + c * ld] -= X3[i + j * ld] * X3[c + j * ld];
+    const T inv = ok ? T(1.0) / d : T(0.0);
+    const int ncol = r - 1 - j;
+    for (int q = w; q < ncol * nch; q += nw) {
+      const int c = j + 1 + q / nch, s = q - (q / nch) * nch, i = 32 * s + lane;
+      if (32 * s + 31 < c) continue;
+      const T f = X3[c + j * ld] * inv;
+      if (i < r && i >= c) X3[i + c * ld] -= X3[i + j * ld] * f;
     }
     __syncthreads();
   }
   if (tid == 0 && bad) info[node] = bad;
+  for (int j = tid; j < r; j += nth) {
+    const T d = X3[j + j * ld];
+    const T sd = d > 0.0 ? sqrt(d) : T(1.0);
+    va[j] = sd;
+    vb[j] = T(1.0) / sd;
+  }
+  __syncthreads();
+  for (int c = w; c < r; c += nw)
+    for (int i = c + lane; i < r; i += 32) X3[i + c * ld] = (i == c) ? va[c] : X3[i + c * ld] * vb[c];
+  __syncthreads();
   // store Ct and L22
-  for (int e = tid; e < r * r; e += nth) {
-    const int i = e % r, c = e / r;
-    Ct_out[node * (int64_t)r * r + e] = X0[i + c * ld];
-    L22_out[node * (int64_t)r * r + e] = (i >= c) ? X3[i + c * ld] : T(0.0);
-  }
-  if (level >= L) return;
-  __syncthreads();
-  // reload R1 -> X1 (X2 still holds R2)
-  for (int e = tid; e < r * r; e += nth) {
-    const int i = e % r, c = e / r;
-    X1[i + c * ld] = R1[e];
-  }
-  __syncthreads();
-  // B = R2 - Ct' R1 -> X2 (column c of R1 has entries l <= c)
-  for (int e = tid; e < r * r; e += nth) {
-    const int i = e % r, c = e / r;
-    T acc = T(0.0);
-#pragma unroll 4
-    for (int l = 0; l <= c; ++l) acc += X0[l + i * ld] * X1[l + c * ld];
-    X2[i + c * ld] -= acc;
-  }
-  __syncthreads();
-  // B <- L22^{-1} B, row by row with the whole CTA
-  for (int i = 0; i < r; ++i) {
-    const T inv = T(1.0) / X3[i + i * ld];
-    for (int c = tid; c < r; c += nth) X2[i + c * ld] *= inv;
-    __syncthreads();
-    const int rows = r - i - 1;
-    for (int e = tid; e < rows * r; e += nth) {
-      const int ii = i + 1 + e % rows, c = e / rows;
-      X2[ii + c * ld] -= X3[ii + i * ld] * X2[i + c * ld];
+  for (int c = w; c < r; c += nw)
+    for (int i = lane; i < r; i += 32) {
+      const int64_t e = node * (int64_t)r * r + i + (int64_t)c * r;
+      Ct_out[e] = X0[i + c * ld];
+      L22_out[e] = (i >= c) ? X3[i + c * ld] : T(0.0);
     }
-    __syncthreads();
+  if (level >= L) return;
+  // B = R2 - Ct' R1 -> X2 (column c of R1 has entries l <= c)
+  for (int q = w; q < nitems; q += nw) {
+    const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
+    T a0 = T(0.0), a1 = T(0.0);
+    int l = 0;
+    for (; l + 1 <= c; l += 2) {
+      a0 += X0[l + ii * ld] * X1[l + c * ld];
+      a1 += X0[l + 1 + ii * ld] * X1[l + 1 + c * ld];
+    }
+    if (l <= c) a0 += X0[l + ii * ld] * X1[l + c * ld];
+    if (i < r) X2[i + c * ld] -= a0 + a1;
   }
-  // structured Householder QR of [X1 (upper r x r) ; X2 (r x r)]:
-  // reflector j acts on row j of the top and all r rows of the bottom.
-  for (int j = 0; j < r; ++j) {
-    T part = T(0.0);
-    for (int i = tid; i < r; i += nth) part += X2[i + j * ld] * X2[i + j * ld];
-    part = warp_sum_t(part);
-    if (lane == 0) red[w] = part;
-    __syncthreads();
-    if (tid == 0) {
-      T sig = T(0.0);
-      for (int q = 0; q < nw; ++q) sig += red[q];
-      const T alpha = X1[j + j * ld];
-      T tj = T(0.0), beta = alpha, scal = T(0.0);
-      if (sig != 0.0) {
-        const T nrm = sqrt(alpha * alpha + sig);
-        beta = alpha >= 0.0 ? -nrm : nrm;
-        tj = (beta - alpha) / beta;
-        scal = T(1.0) / (alpha - beta);
+  __syncthreads();
+  // B <- L22^{-1} B: one warp per column, rows in registers (row i: lane i % 32, slot i / 32)
+  for (int c = w; c < r; c += nw) {
+    T x[3];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int i = lane + 32 * s;
+      x[s] = i < r ? X2[i + c * ld] : T(0.0);
+    }
+    for (int p = 0; p < r; ++p) {
+      const int ps = p >> 5;
+      const T xp = shfl_idx(ps == 0 ? x[0] : (ps == 1 ? x[1] : x[2]), p & 31) * vb[p];
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        const int i = lane + 32 * s;
+        if (i == p) x[s] = xp;
+        else if (i > p && i < r) x[s] -= X3[i + p * ld] * xp;
       }
-      X1[j + j * ld] = beta;
-      sh[0] = scal;
-      sh[1] = tj;
+    }
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int i = lane + 32 * s;
+      if (i < r) X2[i + c * ld] = x[s];
+    }
+  }
+  __syncthreads();
+  // structured Householder QR of [X1 (upper r x r) ; X2 (r x r)]: reflector j acts on row j of
+  // the top and all r rows of the bottom.  Every warp forms the reflector itself; the betas and
+  // the scaling of the reflector columns are applied after the loop.
+  for (int j = 0; j < r; ++j) {
+    T v[3];
+    T part = T(0.0);
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int i = lane + 32 * s;
+      v[s] = i < r ? X2[i + j * ld] : T(0.0);
+      part += v[s] * v[s];
+    }
+    const T sig = warp_sum_t(part);
+    const T alpha = X1[j + j * ld];
+    T tj = T(0.0), beta = alpha, scal = T(0.0);
+    if (sig != 0.0) {
+      const T nrm = sqrt(alpha * alpha + sig);
+      beta = alpha >= 0.0 ? -nrm : nrm;
+      tj = (beta - alpha) / beta;
+      scal = T(1.0) / (alpha - beta);
+    }
+    if (tid == 0) {
+      va[j] = beta;
+      vb[j] = scal;
       Etau[node * (int64_t)r + j] = tj;
     }
-    __syncthreads();
-    const T scal = sh[0], tj = sh[1];
     if (tj != 0.0) {
-      // scaled reflector column v = X2[:, j] * scal is formed on the fly; each warp updates
-      // whole columns c > j
       for (int c = j + 1 + w; c < r; c += nw) {
         T acc = T(0.0);
-        for (int i = lane; i < r; i += 32) acc += X2[i + j * ld] * X2[i + c * ld];
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+          const int i = lane + 32 * s;
+          if (i < r) acc += v[s] * X2[i + c * ld];
+        }
         acc = (warp_sum_t(acc) * scal + X1[j + c * ld]) * tj;
         if (lane == 0) X1[j + c * ld] -= acc;
         const T f = acc * scal;
-        for (int i = lane; i < r; i += 32) X2[i + c * ld] -= f * X2[i + j * ld];
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+          const int i = lane + 32 * s;
+          if (i < r) X2[i + c * ld] -= f * v[s];
+        }
       }
     }
     __syncthreads();
-    for (int i = tid; i < r; i += nth) X2[i + j * ld] *= scal;
-    __syncthreads();
   }
   T* Rn = R + (nleaf + node) * (int64_t)r * r;
-  for (int e = tid; e < r * r; e += nth) {
-    const int i = e % r, c = e / r;
-    Rn[e] = (i <= c) ? X1[i + c * ld] : T(0.0);
-    Eref[node * (int64_t)r * r + e] = X2[i + c * ld];
-  }
+  for (int c = w; c < r; c += nw)
+    for (int i = lane; i < r; i += 32) {
+      const int64_t e = i + (int64_t)c * r;
+      Rn[e] = (i < c) ? X1[i + c * ld] : (i == c ? va[c] : T(0.0));
+      Eref[node * (int64_t)r * r + e] = X2[i + c * ld] * vb[c];
+    }
 }
 
 // Sc^{-T} (upper triangular) from the landmark Cholesky factor Sc (lower): one thread per
@@ -520,7 +573,7 @@ __global__ void k_sum_partials(const double* __restrict__ partial, int np, doubl
 bool launch_chol_small(double* A, int n, int* info, cudaStream_t st) {
   const size_t sm = (size_t)n * (n + 1) * sizeof(double);
   if (sm > 200 * 1024) return false;
-  cudaFuncSetAttribute(k_chol_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_chol_small, sm);
   k_chol_small<<<1, 256, sm, st>>>(A, n, info);
   return true;
 }
@@ -528,7 +581,7 @@ bool launch_chol_small(double* A, int n, int* info, cudaStream_t st) {
 template <typename T, int NB>
 static void leaf_chol_launch(const double* K, T* Lf, const Tree& t, int* info, cudaStream_t st) {
   const size_t sm = (size_t)(t.max_leaf + NB) * (NB + 1) * sizeof(T);
-  cudaFuncSetAttribute(k_leaf_chol<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_leaf_chol<T, NB>, sm);
   k_leaf_chol<T, NB><<<(unsigned)t.nleaf, 256, sm, st>>>(K, Lf, dtree(t), info);
 }
 
@@ -553,7 +606,7 @@ template <typename T>
 void launch_leaf_qr(T* Pan, int r, const Tree& t, T* tau, T* Rout, cudaStream_t st) {
   const size_t sm = (size_t)t.max_leaf * r * sizeof(T);
   if (sm <= 200 * 1024) {
-    cudaFuncSetAttribute(k_leaf_qr<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    smem_limit((const void*)k_leaf_qr<T, true>, sm);
     k_leaf_qr<T, true><<<(unsigned)t.nleaf, 256, sm, st>>>(Pan, r, dtree(t), tau, Rout);
   } else {
     k_leaf_qr<T, false><<<(unsigned)t.nleaf, 256, 0, st>>>(Pan, r, dtree(t), tau, Rout);
@@ -562,18 +615,18 @@ void launch_leaf_qr(T* Pan, int r, const Tree& t, T* tau, T* Rout, cudaStream_t 
 
 void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st) {
   const size_t sm = (size_t)r * (r + 1) * sizeof(double);
-  cudaFuncSetAttribute(k_tri_inv_t, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_tri_inv_t, sm);
   k_tri_inv_t<<<1, 128, sm, st>>>(Sc, r, SinvT);
 }
 
 template <typename T>
 void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T* Ct, T* L22, T* Eref,
                         T* Etau, int* info, cudaStream_t st) {
-  const size_t sm = (size_t)4 * r * (r + 1) * sizeof(T);
-  cudaFuncSetAttribute(k_node_factor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const size_t sm = ((size_t)4 * r * (r + 1) + 2 * r) * sizeof(T);
+  smem_limit((const void*)k_node_factor<T>, sm);
   const int64_t cbase = (level == 1) ? 0 : t.nleaf + t.node_off[level - 1];
   const int64_t nbase = t.node_off[level];
-  k_node_factor<T><<<(unsigned)t.nodes_at(level), 256, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase,
+  k_node_factor<T><<<(unsigned)t.nodes_at(level), 512, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase,
                                                                  nbase, Ct, L22, Eref, Etau, info);
 }
 
@@ -698,7 +751,7 @@ template <typename T>
 void launch_leaf_formq(T* Pan, const T* tau, int r, const Tree& t, cudaStream_t st) {
   const size_t sm = (size_t)t.max_leaf * r * sizeof(T);
   if (sm <= 200 * 1024) {
-    cudaFuncSetAttribute(k_leaf_formq<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    smem_limit((const void*)k_leaf_formq<T, true>, sm);
     k_leaf_formq<T, true><<<(unsigned)t.nleaf, 256, sm, st>>>(Pan, tau, r, dtree(t));
   } else {
     k_leaf_formq<T, false><<<(unsigned)t.nleaf, 256, 0, st>>>(Pan, tau, r, dtree(t));
@@ -709,7 +762,7 @@ template <typename T>
 void launch_node_finalize(const T* L22, const T* Eref, const T* Etau, int r, int level, const Tree& t, T* L22i,
                           T* Eexp, cudaStream_t st) {
   const size_t sm = ((size_t)2 * r * (r + 1) + r) * sizeof(T);
-  cudaFuncSetAttribute(k_node_finalize<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_node_finalize<T>, sm);
   k_node_finalize<T><<<(unsigned)t.nodes_at(level), 512, sm, st>>>(L22, Eref, Etau, r, t.node_off[level],
                                                                    level < t.L ? 1 : 0, L22i, Eexp);
 }

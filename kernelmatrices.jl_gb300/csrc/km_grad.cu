@@ -168,7 +168,7 @@ void launch_leaf_dphiT(const double* Phi, const double* dPhi, int r, const Tree&
                        int64_t ldx, double* VP, int k, cudaStream_t st) {
   dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
   const size_t sm = (size_t)8 * t.max_leaf * sizeof(double);
-  cudaFuncSetAttribute(k_leaf_dphiT, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_leaf_dphiT, sm);
   k_leaf_dphiT<<<grid, 256, sm, st>>>(Phi, dPhi, r, dtree(t), X, ldx, VP, k);
 }
 
@@ -177,7 +177,7 @@ void launch_leaf_dnys_apply(const double* dKl, const double* Phi, const double* 
                             const double* VG, double* Y, int64_t ldy, int k, cudaStream_t st) {
   dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
   const size_t sm = (size_t)8 * (t.max_leaf + 3 * r) * sizeof(double);
-  cudaFuncSetAttribute(k_leaf_dnys_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_leaf_dnys_apply, sm);
   k_leaf_dnys_apply<<<grid, 256, sm, st>>>(dKl, Phi, dPhi, Sc, Sj, r, dtree(t), X, ldx, VG, Y, ldy, k);
 }
 

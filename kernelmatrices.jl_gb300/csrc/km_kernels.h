@@ -6,6 +6,13 @@
 
 namespace km {
 
+// Raises the dynamic shared-memory limit of kernel `func` on the current device so that a launch
+// may request `bytes`.  The limit is set once per kernel and device to the device's opt-in
+// maximum and never lowered, so host threads that launch the same kernel with different sizes
+// (the batched and serving forms) cannot shrink it under one another's launches.
+void smem_limit(const void* func, size_t bytes);
+
+
 // Operand of the leaf triangular kernels: leaf j's block starts at ptr + start(j) * bmul with
 // leading dimension m_j (ld_is_m) or ld.
 struct LeafOperand {

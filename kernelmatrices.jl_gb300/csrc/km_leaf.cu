@@ -226,7 +226,7 @@ static bool tri_launch(const T* Lf, const Tree& t, int op, LeafOperand B, LeafOp
                        cudaStream_t st) {
   const size_t sm = ((size_t)(op >= 2 ? 2 : 1) * NC * t.max_leaf + 32 * 33) * sizeof(T);
   if (sm > 200 * 1024) return false;
-  cudaFuncSetAttribute(k_leaf_tri<T, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_leaf_tri<T, NC>, sm);
   dim3 grid((unsigned)t.nleaf, (unsigned)((ncols + NC - 1) / NC));
   k_leaf_tri<T, NC><<<grid, 256, sm, st>>>(Lf, dtree(t), op, B, X, ncols);
   return true;
@@ -248,7 +248,7 @@ static bool tri_desc_launch(const double* Lf, const Tree& t, int op, const LeafD
                             cudaStream_t st) {
   const size_t sm = ((size_t)(op >= 2 ? 2 : 1) * NC * t.max_leaf + 32 * 33) * sizeof(double);
   if (sm > 200 * 1024) return false;
-  cudaFuncSetAttribute(k_leaf_tri_desc<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_leaf_tri_desc<NC>, sm);
   dim3 grid((unsigned)n, (unsigned)((maxcols + NC - 1) / NC));
   k_leaf_tri_desc<NC><<<grid, 256, sm, st>>>(Lf, dtree(t), op, descs);
   return true;
@@ -268,7 +268,7 @@ void launch_leaf_proj(const T* Q, const T*, int r, const Tree& t, const T* Y, in
                       cudaStream_t st) {
   dim3 grid((unsigned)t.nleaf, (unsigned)((k + 15) / 16));
   const size_t sm = (size_t)16 * t.max_leaf * sizeof(T);
-  cudaFuncSetAttribute(k_leaf_qproj<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  smem_limit((const void*)k_leaf_qproj<T>, sm);
   k_leaf_qproj<T><<<grid, 256, sm, st>>>(Q, r, dtree(t), Y, ldy, VP, k);
 }
 

@@ -1,5 +1,9 @@
 // Device FP64 FMA throughput probe (the roofline denominator of FP64-ALU-bound kernels: the
 // measured peaks file of the GPU pool carries only HBM copy and bf16 tensor rates).
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "km_kernels.h"
 
 namespace km {
@@ -79,3 +83,29 @@ extern "C" int km_probe_fp64_tflops(int device, double* out) {
   *out = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
   return KM_OK;
 }
+
+// ---- dynamic shared-memory limits (declared in km_kernels.h) ---------------------------------
+
+namespace km {
+
+void smem_limit(const void* func, size_t bytes) {
+  if (bytes <= 48 * 1024) return;  // within the default limit
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, bool> raised;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  bool& done = raised[{func, dev}];
+  if (done) return;
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa{};
+  cudaFuncGetAttributes(&fa, func);
+  const int cap = optin - (int)fa.sharedSizeBytes;
+  if (cap > 0 && cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, cap) == cudaSuccess)
+    done = true;
+  else
+    cudaGetLastError();  // the launch then reports the size error itself
+}
+
+}  // namespace km

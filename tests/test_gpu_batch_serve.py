@@ -76,7 +76,8 @@ def test_batch_equals_single_and_oracle(lib):
 
 def test_batch_reports_failing_problem_and_continues(lib):
     import kmhodlr as K
-    probs = problems([2048, 100, 1024], seed=9)  # n = 100 is too small for rank 72
+    probs = problems([2048, 1500, 1024], seed=9)
+    probs[1].params = (1.0, -0.1, 1e-3)  # a negative range is rejected by the assembly
     eng = K.BatchEngine(nworkers=2)
     nll, grad, status = eng.nll_grad(probs, K.Matern32(), RANK, K.LogLevel(8), nprobe=4, seed=1,
                                      raise_on_error=False)
