@@ -381,6 +381,168 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         dist.destroy_process_group()
 
 
+# ----------------------------------------------------------------------------------------------
+# further workloads (not the headline line): batched likelihoods, serving, ACA at 2^18
+# ----------------------------------------------------------------------------------------------
+
+def _loguniform(rng, lo, hi, size):
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), size=size))
+
+
+def batch_problems(count: int, lo: int, hi: int, seed: int):
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    rng = np.random.default_rng(seed)
+    ns = np.round(_loguniform(rng, lo, hi, count)).astype(np.int64)
+    rhos = _loguniform(rng, 0.02, 0.3, count)
+    return [K.Problem(uniform_points(int(n), seed + 1 + b), rng.standard_normal(int(n)), (1.0, float(rho), 1e-3))
+            for b, (n, rho) in enumerate(zip(ns, rhos))]
+
+
+def run_batch(args):
+    """256 independent Nystrom likelihood problems (n log-uniform in [2^10, 2^15], range
+    log-uniform in [0.02, 0.3], nugget 1e-3, rank 72, LogLevel(8), 72 Rademacher probes): NLL and
+    the 3-parameter stochastic gradient of every problem per step."""
+    import torch
+    import kmhodlr as K
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU (no CPU fallback)")
+    probs = batch_problems(256, 2 ** 10, 2 ** 15, SEED)
+    prec = L_prec(args.precision)
+    out_forms = {}
+    for label, nw in (("pool", args.workers), ("one_stream", 1)):
+        eng = K.BatchEngine(nworkers=nw, precision=prec)
+        for _ in range(args.warmup if label == "pool" else 1):
+            eng.nll_grad(probs, K.Matern32(), RANK, K.LogLevel(8), nprobe=72, seed=SEED)
+        steps = args.steps if label == "pool" else 1
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            nll, grad, status = eng.nll_grad(probs, K.Matern32(), RANK, K.LogLevel(8), nprobe=72, seed=SEED)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / steps
+        out_forms[label] = {"workers": nw, "s_per_batch": dt, "problems_per_s": len(probs) / dt}
+        eng.close()
+    v = out_forms["pool"]["problems_per_s"]
+    ns = [len(p.y) for p in probs]
+    out = {"metric": "batched NLL+gradient problems/s", "value": v, "unit": "problems/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * out_forms["pool"]["s_per_batch"],
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64" if prec == 0 else "f32x2+f64", "data": "synthetic",
+           "config": {"workload": "batch256_matern32_nystrom_r72_loglevel8_72probes", "problems": len(probs),
+                      "n_min": int(min(ns)), "n_max": int(max(ns)), "n_total": int(sum(ns)),
+                      "precision": args.precision},
+           "e2e": {"value": v, "unit": "problems/s", "h2d_bytes_per_step": int(sum(24 * n for n in ns)),
+                   "d2h_bytes_per_step": int(len(probs) * 32),
+                   "note": "the batch call takes host inputs; value and e2e are the same host-to-host timing"},
+           "forms": out_forms, "speedup_pool_vs_one_stream": v / out_forms["one_stream"]["problems_per_s"]}
+    print(json.dumps(out), flush=True)
+
+
+def L_prec(name: str) -> int:
+    return 1 if name == "mixed" else 0
+
+
+def run_serve(args):
+    """Serving: Poisson arrivals at 200 requests/s; a request is an NLL + gradient of a new
+    dataset (n log-uniform in [2^12, 2^18], 72 probes) with probability 0.2, else 1-32 solves
+    on one of 8 resident factors (built before the timed region).  80 % HBM budget."""
+    import threading
+    import torch
+    import kmhodlr as K
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU (no CPU fallback)")
+    rng = np.random.default_rng(SEED + 7)
+    nreq = args.requests
+    srv = K.Server(K.Matern32(), RANK, K.LogLevel(8), nworkers=args.workers, precision=L_prec(args.precision),
+                   hbm_budget_fraction=0.8)
+    facs = batch_problems(8, 2 ** 12, 2 ** 18, SEED + 11)
+    fids = []
+    for p in facs:
+        r = srv.wait(srv.submit_factor(p))
+        if r.status != 0:
+            raise SystemExit(f"factor build failed: {r.status}")
+        fids.append((r.factor_id, len(p.y)))
+    pool = batch_problems(64, 2 ** 12, 2 ** 18, SEED + 13)   # datasets of the likelihood requests
+    kinds = rng.uniform(size=nreq) < 0.2
+    gaps = rng.exponential(1.0 / args.rate, size=nreq)
+    rhs_cache = {}
+    tickets = []
+    t_start = time.perf_counter()
+    next_t = t_start
+    for q in range(nreq):
+        next_t += gaps[q]
+        d = next_t - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        if kinds[q]:
+            tickets.append(srv.submit_nll_grad(pool[q % len(pool)], nprobe=72, seed=q))
+        else:
+            fid, n = fids[int(rng.integers(len(fids)))]
+            k = int(rng.integers(1, 33))
+            key = (n, k)
+            if key not in rhs_cache:
+                rhs_cache[key] = np.asfortranarray(np.random.default_rng(k).standard_normal((n, k)))
+            tickets.append(srv.submit_solve(fid, rhs_cache[key]))
+    statuses = [srv.wait(t).status for t in tickets]
+    t_end = time.perf_counter()
+    st = srv.stats()
+    srv.close()
+    ok = sum(1 for x in statuses if x == 0)
+    thr = ok / (t_end - t_start)
+    out = {"metric": "served requests/s", "value": thr, "unit": "requests/s", "n_gpus": 1,
+           "steps": nreq, "warmup": 0, "ms_per_step": 1e3 * (t_end - t_start) / nreq,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64" if L_prec(args.precision) == 0 else "f32x2+f64", "data": "synthetic",
+           "config": {"workload": "serve_poisson_matern32_nystrom_r72_loglevel8", "rate_per_s": args.rate,
+                      "requests": nreq, "nll_fraction": 0.2, "resident_factors": len(fids), "workers": args.workers,
+                      "hbm_budget_fraction": 0.8, "precision": args.precision},
+           "latency_ms": {"p50": st.p50_ms, "p99": st.p99_ms, "mean": st.mean_ms},
+           "completed": int(st.completed), "failed": int(st.failed), "rejected": int(st.rejected),
+           "peak_bytes": int(st.peak_bytes), "budget_bytes": int(st.budget_bytes),
+           "offered_rate_per_s": args.rate}
+    print(json.dumps(out), flush=True)
+
+
+def run_aca(args):
+    """ACA assembly and general factorisation at n = 2^18 (range 0.05, nugget 1e-4, tol 1e-8,
+    LogLevel(8) => 10 levels), 8 right-hand sides, logdet."""
+    import torch
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU (no CPU fallback)")
+    n = args.aca_n
+    pts = uniform_points(n, SEED + 3)
+    rhs = np.asfortranarray(np.random.default_rng(SEED + 4).standard_normal((n, 8)))
+    km = K.KernelMatrix(pts, pts, (1.0, 0.05, 1e-4), K.Matern32())
+    times = []
+    for it in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hk = K.KernelHODLR(km, 1e-8, 0, K.LogLevel(8), nystrom=False)
+        t1 = time.perf_counter()
+        K.symmetricfactorize(hk)
+        t2 = time.perf_counter()
+        x = hk.ldiv(rhs)
+        ld = hk.logdet()
+        t3 = time.perf_counter()
+        if it >= args.warmup:
+            times.append((t1 - t0, t2 - t1, t3 - t2))
+        ranks = hk.block_ranks()
+        del hk
+    a, f, s = (float(np.mean([t[i] for t in times])) for i in range(3))
+    tot = a + f + s
+    out = {"metric": "ACA HODLR assemble+factor+solve/s", "value": 1.0 / tot, "unit": "steps/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"aca_matern32_n{n}_tol1e-8_loglevel8_8rhs", "n": n, "levels": int(np.log2(n)) - 8},
+           "phase_s": {"assemble": a, "factorize": f, "solve_logdet": s},
+           "ranks": {"max": int(ranks.max()), "mean": float(ranks.mean()), "blocks": int(ranks.size)},
+           "logdet": ld}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -390,6 +552,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed",
                     help="form reported as `value` (the other form is reported beside it)")
+    ap.add_argument("--workload", choices=["c2", "batch", "serve", "aca"], default="c2",
+                    help="c2: the headline factor+solve+logdet step; batch / serve / aca: the other forms")
+    ap.add_argument("--workers", type=int, default=8, help="batch / serve: concurrent handles")
+    ap.add_argument("--requests", type=int, default=2000, help="serve: number of requests")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: Poisson arrival rate (1/s)")
+    ap.add_argument("--aca-n", type=int, default=2 ** 18, help="aca: number of points")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -398,6 +566,12 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args, rank)
+    elif args.workload == "batch":
+        run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
+    elif args.workload == "aca":
+        run_aca(args)
     else:
         run_ours(args, rank, world, local_rank)
 

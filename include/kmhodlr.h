@@ -66,6 +66,8 @@ typedef struct km_stats {
   int64_t kernel_launches;     /* kernels launched by the handle since creation                 */
   int refine_iterations;       /* iterations used by the last mixed-precision solve             */
   double refine_residual;      /* final relative residual of that solve                         */
+  int64_t precision_fallbacks; /* mixed-precision factorisations redone in FP64 after a
+                                  non-positive pivot in float-pair arithmetic                  */
 } km_stats;
 
 typedef struct km_handle km_handle;

@@ -162,6 +162,7 @@ struct km_handle {
 namespace {
 
 constexpr int kLogdetBlocks = 256;
+constexpr int kAcaMaxCap = 4096;  // ACA panel columns per block (2 x 4096 doubles of shared memory)
 
 int fail(km_handle* h, int code, const std::string& msg) {
   if (h) h->err = msg;
@@ -865,12 +866,22 @@ static int aca_assemble(km_handle* h, const double* pts, bool dev, const Tree& t
   }
   h->lvoff[t.L + 1] = (int64_t)h->blk.size();
   const int nb = (int)h->blk.size();
-  // panel capacity: the full rank bound when it fits in 40% of the budget, else 256 columns
-  const bool fits = (double)full * 8.0 <= 0.4 * (double)device_budget(h);
+  // panel capacity: the largest column count (256 .. kAcaMaxCap, powers of two) whose panels
+  // fit in 40% of the budget; the ACA kernel keeps two capacity-long vectors in shared memory
+  int capmax = 256;
+  for (int c = kAcaMaxCap; c > 256; c >>= 1) {
+    int64_t tot = 0;
+    for (const auto& b : h->blk) tot += (b.nro + b.ncl) * (int64_t)std::min(b.maxsz, c);
+    if ((double)tot * 8.0 <= 0.4 * (double)device_budget(h)) {
+      capmax = c;
+      break;
+    }
+  }
+  (void)full;
   int64_t offP = 0, offF = 0, offV = 0;
   int maxcap = 0;
   for (auto& b : h->blk) {
-    b.cap = fits ? b.maxsz : std::min(b.maxsz, 256);
+    b.cap = std::min(b.maxsz, capmax);
     b.offU = offP;
     offP += b.nro * b.cap;
     b.offV = offP;
@@ -917,8 +928,8 @@ static int aca_assemble(km_handle* h, const double* pts, bool dev, const Tree& t
   for (int q = 0; q < nb; ++q) {
     if (stat[q] == 1) return fail(h, KM_ERR_ACA, "Incompatible maxrank or matrix dimensions.");
     if (stat[q] == 2)
-      return fail(h, KM_ERR_UNSUPPORTED, "ACA rank reached the panel capacity of 256 columns before the "
-                                         "tolerance; pass a maxrank");
+      return fail(h, KM_ERR_UNSUPPORTED, "ACA rank reached the panel capacity (" + std::to_string(capmax) +
+                                             " columns) before the tolerance; pass a maxrank");
   }
   // node descriptors (factor storage sized by the ranks) and the per-block solve items
   int64_t r2 = 0;
@@ -1093,6 +1104,7 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   h->r = (int)maxrank;
   h->assembled = h->factorized = false;
   h->dk_param = -1;
+  h->mixed = (h->cfg.precision == KM_PREC_MIXED);
   const int r = h->r;
   int64_t kbytes = 0;
   for (int64_t j = 0; j < t.nleaf; ++j) kbytes += t.leaf_size(j) * t.leaf_size(j);
@@ -1217,14 +1229,23 @@ int km_factorize(km_handle* h) {
   if ((rc = check_launch(h, "factorize")) != KM_OK) return rc;
   h->stats.factorize_ms = timer_stop(h);
   if ((rc = sync(h, "factorize")) != KM_OK) return rc;
-  if ((rc = check_info(h, t.nleaf, "leaf")) != KM_OK) return rc;
-  {
+  rc = check_info(h, t.nleaf, "leaf");
+  if (rc == KM_OK) {
     std::vector<int> info(t.nnode);
     if (t.nnode > 0)
       KM_CUDA(h, cudaMemcpy(info.data(), h->d_info + t.nleaf, sizeof(int) * t.nnode, cudaMemcpyDeviceToHost));
-    for (int64_t i = 0; i < t.nnode; ++i)
-      if (info[i]) return fail(h, KM_ERR_NOT_SPD, "PosDefException: a low-rank capacitance block is not positive definite");
+    for (int64_t i = 0; i < t.nnode && rc == KM_OK; ++i)
+      if (info[i]) rc = fail(h, KM_ERR_NOT_SPD, "PosDefException: a low-rank capacitance block is not positive definite");
   }
+  if (rc == KM_ERR_NOT_SPD && h->mixed) {
+    // A pivot that is positive in FP64 can round to <= 0 in float pairs when the capacitance
+    // I - Ct'Ct is close to singular (smooth kernels, large range).  Redo this problem in FP64;
+    // the next assembly returns to the configured precision.
+    h->mixed = false;
+    h->stats.precision_fallbacks += 1;
+    return km_factorize(h);
+  }
+  if (rc != KM_OK) return rc;
   h->factorized = true;
   return KM_OK;
 }

@@ -41,7 +41,8 @@ class KmStats(C.Structure):
     _fields_ = [("assemble_ms", C.c_double), ("factorize_ms", C.c_double), ("solve_ms", C.c_double),
                 ("matvec_ms", C.c_double), ("logdet_ms", C.c_double), ("grad_ms", C.c_double),
                 ("device_bytes", C.c_int64), ("kernel_launches", C.c_int64),
-                ("refine_iterations", C.c_int), ("refine_residual", C.c_double)]
+                ("refine_iterations", C.c_int), ("refine_residual", C.c_double),
+                ("precision_fallbacks", C.c_int64)]
 
 
 KM_REQ_NLL_GRAD = 0
