@@ -157,4 +157,43 @@ function stoch_gradient(K::GPUKernelHODLR, dat::Vector{Float64}, vecs::Vector{Ve
   return grad
 end
 
+# ---- batched form: nll_objective over many independent datasets ------------------------------
+struct KmProblem
+  n::Int64
+  pts::Ptr{SVector{2,Float64}}
+  y::Ptr{Float64}
+  params::NTuple{3,Float64}
+end
+
+struct KmBatchOpts
+  kernel_id::Cint
+  rank::Int64
+  level_kind::Cint
+  level::Int64
+  nprobe::Int64
+  probe_seed::UInt64
+end
+
+# One call for many (points, data, parameters) triples; returns (nll, grad (3 x m), status).
+# Probes are drawn on the device (problem b uses seed + b).
+function batch_nll_grad(pts::Vector{Vector{SVector{2,Float64}}}, dat::Vector{Vector{Float64}},
+                        prms::Vector{NTuple{3,Float64}}, kernel, rank::Int64, lvl::HierLevel;
+                        nprobe::Int64=72, seed::UInt64=UInt64(0), nworkers::Int=8, precision::Int=0)
+  m = length(pts)
+  b = Ref{Ptr{Cvoid}}(C_NULL)
+  cfg = Ref(KmConfig(0, Cint(precision), 0.8, 0, 0.0))
+  check(C_NULL, ccall((:km_batch_create, libkm), Cint, (Ptr{KmConfig}, Cint, Ptr{Ptr{Cvoid}}), cfg, nworkers, b))
+  kind, lv = lvl isa HODLR.FixedLevel ? (Cint(0), Int64(lvl.lv)) : (Cint(1), Int64(lvl.lv))
+  opts = Ref(KmBatchOpts(kernel_id(kernel), rank, kind, lv, nprobe, seed))
+  probs = [KmProblem(length(pts[i]), pointer(pts[i]), pointer(dat[i]), prms[i]) for i in 1:m]
+  nll = zeros(m); grad = zeros(3, m); status = zeros(Cint, m)
+  GC.@preserve pts dat begin
+    rc = ccall((:km_batch_nll_grad, libkm), Cint,
+               (Ptr{Cvoid}, Ptr{KmBatchOpts}, Int64, Ptr{KmProblem}, Ptr{Float64}, Ptr{Float64}, Ptr{Cint}),
+               b[], opts, m, probs, nll, grad, status)
+  end
+  ccall((:km_batch_destroy, libkm), Cint, (Ptr{Cvoid},), b[])
+  return nll, grad, status
+end
+
 end # module
