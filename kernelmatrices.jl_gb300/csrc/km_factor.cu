@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(256) k_leaf_formq(T* __restrict__ Pan, const T
 }
 
 // ---------------------------------------------------------------------------------------------
-// Node factorisation, one CTA per node of level l.  Given the children's R factors
+// Node factorisation, one CTA (1024 threads) per node of level l.  Given the children's R factors
 // (slots c1, c2) and Sc = chol(S) (lower):
 //   T1 = R1 Sc^{-T}, T2 = R2 Sc^{-T}   (upper triangular)
 //   Ct = T1 T2'                        (= R1 S^{-1} R2')
@@ -290,7 +290,7 @@ __device__ __forceinline__ T sel(bool p, T a) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(512) k_node_factor(T* __restrict__ R, const T* __restrict__ SinvT,
+__global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T* __restrict__ SinvT,
                                                      int r, int level, int L, int64_t nleaf,
                                                      int64_t cbase, int64_t nbase, T* __restrict__ Ct_out,
                                                      T* __restrict__ L22_out, T* __restrict__ Eref,
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(512) k_node_factor(T* __restrict__ R, const T*
       a1 += X0[l + 1 + ii * ld] * X0[l + 1 + c * ld];
     }
     if (l < r) a0 += X0[l + ii * ld] * X0[l + c * ld];
-    if (i < r && i >= c) X3[i + c * ld] = T(i == c ? 1.0 : 0.0) - (a0 + a1);
+    if (i < r && i >= c) X3[i + c * ld] = (i == c ? T(1.0) : T(0.0)) - (a0 + a1);
   }
   __syncthreads();
   // L22 = chol(H): unscaled right-looking elimination, a_ik -= a_ij a_kj / d_j
@@ -504,6 +504,182 @@ __global__ void __launch_bounds__(512) k_node_factor(T* __restrict__ R, const T*
     }
 }
 
+// FP64 variant: thread per output entry, 256 threads.  The FP64 pipe (2 DFMA/clk/SM) bounds
+// this kernel, and with few warps per CTA it keeps that pipe busier than the warp-item mapping
+// of k_node_factor.
+__global__ void __launch_bounds__(256) k_node_factor_f64(double* __restrict__ R, const double* __restrict__ SinvT,
+                                                     int r, int level, int L, int64_t nleaf,
+                                                     int64_t cbase, int64_t nbase, double* __restrict__ Ct_out,
+                                                     double* __restrict__ L22_out, double* __restrict__ Eref,
+                                                     double* __restrict__ Etau, int* __restrict__ info) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  double* sm = reinterpret_cast<double*>(smraw);
+  __shared__ double red[32];
+  __shared__ double sh[2];
+  const int ld = r + 1;
+  double* X0 = sm;
+  double* X1 = X0 + r * ld;
+  double* X2 = X1 + r * ld;
+  double* X3 = X2 + r * ld;
+  const int64_t k = blockIdx.x;
+  const int64_t node = nbase + k;  // node index within all nodes (level-major)
+  const double* R1 = R + (cbase + 2 * k) * (int64_t)r * r;
+  const double* R2 = R + (cbase + 2 * k + 1) * (int64_t)r * r;
+  const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
+  // load: X0 = Sc^{-T} (upper), X1 = R1, X2 = R2   (element (i,c) at i + c*ld)
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    X0[i + c * ld] = SinvT[e];
+    X1[i + c * ld] = R1[e];
+    X2[i + c * ld] = R2[e];
+  }
+  __syncthreads();
+  // T1 = R1 Sc^{-T} -> X3 (upper x upper: entries l in [i, c])
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    double acc = double(0.0);
+    if (i <= c) {
+#pragma unroll 4
+      for (int l = i; l <= c; ++l) acc += X1[i + l * ld] * X0[l + c * ld];
+    }
+    X3[i + c * ld] = acc;
+  }
+  __syncthreads();
+  // T2 = R2 Sc^{-T} -> X1
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    double acc = double(0.0);
+    if (i <= c) {
+#pragma unroll 4
+      for (int l = i; l <= c; ++l) acc += X2[i + l * ld] * X0[l + c * ld];
+    }
+    X1[i + c * ld] = acc;
+  }
+  __syncthreads();
+  // Ct = T1 T2' -> X0 ; Ct[i][c] = sum_{l >= max(i,c)} T1[i][l] T2[c][l]
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    double acc = double(0.0);
+#pragma unroll 4
+    for (int l = max(i, c); l < r; ++l) acc += X3[i + l * ld] * X1[c + l * ld];
+    X0[i + c * ld] = acc;
+  }
+  __syncthreads();
+  // H = I - Ct' Ct -> X3 (lower triangle)
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    if (i >= c) {
+      double acc = double(0.0);
+#pragma unroll 4
+      for (int l = 0; l < r; ++l) acc += X0[l + i * ld] * X0[l + c * ld];
+      X3[i + c * ld] = double(i == c ? 1.0 : 0.0) - acc;
+    }
+  }
+  __syncthreads();
+  // L22 = chol(H) in place (lower)
+  int bad = 0;
+  for (int j = 0; j < r; ++j) {
+    const double d = X3[j + j * ld];
+    const bool ok = d > 0.0;
+    if (!ok && bad == 0) bad = j + 1;
+    const double sd = ok ? sqrt(d) : double(1.0);
+    __syncthreads();
+    for (int i = j + 1 + tid; i < r; i += nth) X3[i + j * ld] /= sd;
+    if (tid == 0) X3[j + j * ld] = sd;
+    __syncthreads();
+    const int wdt = r - j - 1;
+    for (int e = tid; e < wdt * wdt; e += nth) {
+      const int i = j + 1 + e % wdt, c = j + 1 + e / wdt;
+      if (i >= c) X3[i + c * ld] -= X3[i + j * ld] * X3[c + j * ld];
+    }
+    __syncthreads();
+  }
+  if (tid == 0 && bad) info[node] = bad;
+  // store Ct and L22
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    Ct_out[node * (int64_t)r * r + e] = X0[i + c * ld];
+    L22_out[node * (int64_t)r * r + e] = (i >= c) ? X3[i + c * ld] : double(0.0);
+  }
+  if (level >= L) return;
+  __syncthreads();
+  // reload R1 -> X1 (X2 still holds R2)
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    X1[i + c * ld] = R1[e];
+  }
+  __syncthreads();
+  // B = R2 - Ct' R1 -> X2 (column c of R1 has entries l <= c)
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    double acc = double(0.0);
+#pragma unroll 4
+    for (int l = 0; l <= c; ++l) acc += X0[l + i * ld] * X1[l + c * ld];
+    X2[i + c * ld] -= acc;
+  }
+  __syncthreads();
+  // B <- L22^{-1} B, row by row with the whole CTA
+  for (int i = 0; i < r; ++i) {
+    const double inv = double(1.0) / X3[i + i * ld];
+    for (int c = tid; c < r; c += nth) X2[i + c * ld] *= inv;
+    __syncthreads();
+    const int rows = r - i - 1;
+    for (int e = tid; e < rows * r; e += nth) {
+      const int ii = i + 1 + e % rows, c = e / rows;
+      X2[ii + c * ld] -= X3[ii + i * ld] * X2[i + c * ld];
+    }
+    __syncthreads();
+  }
+  // structured Householder QR of [X1 (upper r x r) ; X2 (r x r)]:
+  // reflector j acts on row j of the top and all r rows of the bottom.
+  for (int j = 0; j < r; ++j) {
+    double part = double(0.0);
+    for (int i = tid; i < r; i += nth) part += X2[i + j * ld] * X2[i + j * ld];
+    part = warp_sum_t(part);
+    if (lane == 0) red[w] = part;
+    __syncthreads();
+    if (tid == 0) {
+      double sig = double(0.0);
+      for (int q = 0; q < nw; ++q) sig += red[q];
+      const double alpha = X1[j + j * ld];
+      double tj = double(0.0), beta = alpha, scal = double(0.0);
+      if (sig != 0.0) {
+        const double nrm = sqrt(alpha * alpha + sig);
+        beta = alpha >= 0.0 ? -nrm : nrm;
+        tj = (beta - alpha) / beta;
+        scal = double(1.0) / (alpha - beta);
+      }
+      X1[j + j * ld] = beta;
+      sh[0] = scal;
+      sh[1] = tj;
+      Etau[node * (int64_t)r + j] = tj;
+    }
+    __syncthreads();
+    const double scal = sh[0], tj = sh[1];
+    if (tj != 0.0) {
+      // scaled reflector column v = X2[:, j] * scal is formed on the fly; each warp updates
+      // whole columns c > j
+      for (int c = j + 1 + w; c < r; c += nw) {
+        double acc = double(0.0);
+        for (int i = lane; i < r; i += 32) acc += X2[i + j * ld] * X2[i + c * ld];
+        acc = (warp_sum_t(acc) * scal + X1[j + c * ld]) * tj;
+        if (lane == 0) X1[j + c * ld] -= acc;
+        const double f = acc * scal;
+        for (int i = lane; i < r; i += 32) X2[i + c * ld] -= f * X2[i + j * ld];
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < r; i += nth) X2[i + j * ld] *= scal;
+    __syncthreads();
+  }
+  double* Rn = R + (nleaf + node) * (int64_t)r * r;
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    Rn[e] = (i <= c) ? X1[i + c * ld] : double(0.0);
+    Eref[node * (int64_t)r * r + e] = X2[i + c * ld];
+  }
+}
+
 // Sc^{-T} (upper triangular) from the landmark Cholesky factor Sc (lower): one thread per
 // column of Sc^{-1} (forward substitution), one CTA.
 __global__ void k_tri_inv_t(const double* __restrict__ Sc, int r, double* __restrict__ SinvT) {
@@ -622,12 +798,21 @@ void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st) {
 template <typename T>
 void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T* Ct, T* L22, T* Eref,
                         T* Etau, int* info, cudaStream_t st) {
-  const size_t sm = ((size_t)4 * r * (r + 1) + 2 * r) * sizeof(T);
-  smem_limit((const void*)k_node_factor<T>, sm);
   const int64_t cbase = (level == 1) ? 0 : t.nleaf + t.node_off[level - 1];
   const int64_t nbase = t.node_off[level];
-  k_node_factor<T><<<(unsigned)t.nodes_at(level), 512, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase,
-                                                                 nbase, Ct, L22, Eref, Etau, info);
+  if constexpr (std::is_same<T, double>::value) {
+    const size_t sm = (size_t)4 * r * (r + 1) * sizeof(double);
+    smem_limit((const void*)k_node_factor_f64, sm);
+    k_node_factor_f64<<<(unsigned)t.nodes_at(level), 256, sm, st>>>(
+        reinterpret_cast<double*>(R), reinterpret_cast<const double*>(SinvT), r, level, t.L, t.nleaf, cbase, nbase,
+        reinterpret_cast<double*>(Ct), reinterpret_cast<double*>(L22), reinterpret_cast<double*>(Eref),
+        reinterpret_cast<double*>(Etau), info);
+  } else {
+    const size_t sm = ((size_t)4 * r * (r + 1) + 2 * r) * sizeof(T);
+    smem_limit((const void*)k_node_factor<T>, sm);
+    k_node_factor<T><<<(unsigned)t.nodes_at(level), 1024, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase,
+                                                                   nbase, Ct, L22, Eref, Etau, info);
+  }
 }
 
 template <typename T>
@@ -692,7 +877,7 @@ __global__ void __launch_bounds__(512) k_node_finalize(const T* __restrict__ L22
   for (int c = w; c < r; c += nw) {
     T x[3];
 #pragma unroll
-    for (int s = 0; s < 3; ++s) x[s] = T((lane + 32 * s) == c ? 1.0 : 0.0);
+    for (int s = 0; s < 3; ++s) x[s] = (lane + 32 * s) == c ? T(1.0) : T(0.0);
     for (int p = c; p < r; ++p) {
       const T xp = shfl_idx(slot_get(x, p >> 5), p & 31) / Ls[p + p * ld];
 #pragma unroll
@@ -720,7 +905,7 @@ __global__ void __launch_bounds__(512) k_node_finalize(const T* __restrict__ L22
     for (int i = c + 1 + lane; i < r; i += 32) top[i] = T(0.0);
     for (int j = c; j >= 0; --j) {
       const T tj = ts[j];
-      const T tjtop = T(j == c ? 1.0 : 0.0);
+      const T tjtop = j == c ? T(1.0) : T(0.0);
       if (tj == 0.0) {
         if (lane == 0) top[j] = tjtop;
         continue;

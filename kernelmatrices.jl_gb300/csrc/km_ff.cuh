@@ -22,13 +22,11 @@ using ::sqrt;
 
 struct ff {
   float hi, lo;
-  __host__ __device__ ff() : hi(0.f), lo(0.f) {}
-  __device__ ff(float h, float l) : hi(h), lo(l) {}
-  // rounding a double to the nearest float pair
-  __device__ ff(double x) {
-    hi = __double2float_rn(x);
-    lo = __double2float_rn(x - (double)hi);
-  }
+  __host__ __device__ constexpr ff() : hi(0.f), lo(0.f) {}
+  __host__ __device__ constexpr ff(float h, float l) : hi(h), lo(l) {}
+  // rounding a double to the nearest float pair (plain round-to-nearest casts, so that
+  // constants such as ff(0.0) or ff(1.0) fold at compile time and cost no FP64 instruction)
+  __host__ __device__ constexpr ff(double x) : hi(static_cast<float>(x)), lo(static_cast<float>(x - static_cast<double>(static_cast<float>(x)))) {}
   __device__ explicit operator double() const { return (double)hi + (double)lo; }
 };
 
@@ -79,9 +77,21 @@ __device__ __forceinline__ ff& operator-=(ff& a, ff b) { return a = a - b; }
 __device__ __forceinline__ ff& operator*=(ff& a, ff b) { return a = a * b; }
 __device__ __forceinline__ ff& operator/=(ff& a, ff b) { return a = a / b; }
 
-__device__ __forceinline__ bool operator>(ff a, double b) { return (double)a > b; }
-__device__ __forceinline__ bool operator>=(ff a, double b) { return (double)a >= b; }
-__device__ __forceinline__ bool operator==(ff a, double b) { return a.hi == (float)b && a.lo == 0.f && (double)a.hi == b; }
+// Comparisons with a double constant b, in float arithmetic.  Exact when b is a float pair
+// (b == ff(b)), which holds for the constants the kernels compare with (0, 1).  For a normalised
+// pair the order is decided by hi, and by lo when the hi parts are equal.
+__device__ __forceinline__ bool operator>(ff a, double b) {
+  const ff c(b);
+  return a.hi > c.hi || (a.hi == c.hi && a.lo > c.lo);
+}
+__device__ __forceinline__ bool operator>=(ff a, double b) {
+  const ff c(b);
+  return a.hi > c.hi || (a.hi == c.hi && a.lo >= c.lo);
+}
+__device__ __forceinline__ bool operator==(ff a, double b) {
+  const ff c(b);
+  return a.hi == c.hi && a.lo == c.lo;
+}
 __device__ __forceinline__ bool operator!=(ff a, double b) { return !(a == b); }
 
 __device__ __forceinline__ ff sqrt(ff a) {

@@ -35,7 +35,10 @@ __device__ void leaf_tri_body(const T* __restrict__ L, int m, int op, const T* B
       const int ib = min(32, m - i0);
       for (int e = tid; e < 32 * 32; e += blockDim.x) {
         const int i = e & 31, l = e >> 5;
-        if (i < ib && l <= i) D[i * 33 + l] = L[(int64_t)(i0 + l) * m + i0 + i];
+        if (i < ib && l <= i) {
+          const T v = L[(int64_t)(i0 + l) * m + i0 + i];
+          D[i * 33 + l] = (l == i) ? T(1.0) / v : v;  // diagonal kept as its reciprocal
+        }
       }
       __syncthreads();
       // diagonal block, one warp per column, lanes = rows of the block
@@ -43,13 +46,13 @@ __device__ void leaf_tri_body(const T* __restrict__ L, int m, int op, const T* B
         T x = (lane < ib) ? xs[c * m + i0 + lane] : T(0.0);
         if (op == 0) {
           for (int l = 0; l < ib; ++l) {
-            if (lane == l) x = x / D[l * 33 + l];
+            if (lane == l) x = x * D[l * 33 + l];
             const T xl = shfl_idx(x, l);
             if (lane > l && lane < ib) x -= D[lane * 33 + l] * xl;
           }
         } else {
           for (int l = ib - 1; l >= 0; --l) {
-            if (lane == l) x = x / D[l * 33 + l];
+            if (lane == l) x = x * D[l * 33 + l];
             const T xl = shfl_idx(x, l);
             if (lane < l) x -= D[l * 33 + lane] * xl;
           }
@@ -57,34 +60,26 @@ __device__ void leaf_tri_body(const T* __restrict__ L, int m, int op, const T* B
         if (lane < ib) xs[c * m + i0 + lane] = x;
       }
       __syncthreads();
-      // update of the remaining rows with the solved block (thread per row, NC accumulators)
-      if (op == 0) {
-        for (int i = i0 + ib + tid; i < m; i += blockDim.x) {
-          T acc[NC];
+      // update of the remaining rows with the solved block: items of (row, 4 columns), so that
+      // each loaded L entry feeds 4 multiply-adds and all threads stay busy as the remaining
+      // rows shrink
+      const int R = (op == 0) ? m - (i0 + ib) : i0;
+      const int r0 = (op == 0) ? i0 + ib : 0;
+      const int ng = (nc + 3) >> 2;
+      for (int e = tid; e < R * ng; e += blockDim.x) {
+        const int g = e / R, i = r0 + (e - g * R), cb = 4 * g;
+        const T* xc = xs + cb * m + i0;
+        T acc[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
+        for (int l = 0; l < ib; ++l) {
+          const T a = (op == 0) ? L[(int64_t)(i0 + l) * m + i]   // L[i, i0 + l]
+                                : L[(int64_t)i * m + i0 + l];    // L[i0 + l, i]
 #pragma unroll
-          for (int c = 0; c < NC; ++c) acc[c] = T(0.0);
-          for (int l = 0; l < ib; ++l) {
-            const T a = L[(int64_t)(i0 + l) * m + i];
-#pragma unroll
-            for (int c = 0; c < NC; ++c) acc[c] += a * xs[c * m + i0 + l];
-          }
-#pragma unroll
-          for (int c = 0; c < NC; ++c) xs[c * m + i] -= acc[c];
+          for (int j = 0; j < 4; ++j)
+            if (cb + j < nc) acc[j] += a * xc[j * m + l];
         }
-      } else {
-        for (int i = tid; i < i0; i += blockDim.x) {
-          T acc[NC];
 #pragma unroll
-          for (int c = 0; c < NC; ++c) acc[c] = T(0.0);
-          const T* col = L + (int64_t)i * m + i0;  // L[i0 + l, i]
-          for (int l = 0; l < ib; ++l) {
-            const T a = col[l];
-#pragma unroll
-            for (int c = 0; c < NC; ++c) acc[c] += a * xs[c * m + i0 + l];
-          }
-#pragma unroll
-          for (int c = 0; c < NC; ++c) xs[c * m + i] -= acc[c];
-        }
+        for (int j = 0; j < 4; ++j)
+          if (cb + j < nc) xs[(cb + j) * m + i] -= acc[j];
       }
       __syncthreads();
     }
@@ -156,47 +151,64 @@ __global__ void __launch_bounds__(256) k_leaf_tri_desc(const double* __restrict_
 
 // ---------------------------------------------------------------------------------------------
 // Q_leaf' y (proj) and y += sign * Q_leaf g (expand) with the explicit leaf bases Q (m x r,
-// column-major at start*r).  grid = (nleaf, ceil(k / 16)), block 256; the 16-column chunk of y
-// (proj) or of g (expand) is staged in shared memory and every output is an independent dot
-// product.
+// column-major at start*r).  grid = (nleaf, ceil(k / 16)), block 256.
 // ---------------------------------------------------------------------------------------------
-// sum_l a[l*sa] b[l], l < n, with four independent partial sums
-template <typename T>
-__device__ __forceinline__ T dot4l(const T* __restrict__ a, int64_t sa, const T* __restrict__ b, int n) {
-  T s0 = T(0.0), s1 = T(0.0), s2 = T(0.0), s3 = T(0.0);
-  int l = 0;
-  for (; l + 3 < n; l += 4) {
-    s0 += a[l * sa] * b[l];
-    s1 += a[(l + 1) * sa] * b[l + 1];
-    s2 += a[(l + 2) * sa] * b[l + 2];
-    s3 += a[(l + 3) * sa] * b[l + 3];
-  }
-  for (; l < n; ++l) s0 += a[l * sa] * b[l];
-  return (s0 + s1) + (s2 + s3);
-}
+// VP[leaf][c] = Q_leaf' y_c for a chunk of up to 16 columns.  The leaf is processed in chunks of
+// 64 rows: Q (64 x r, padded rows) and y (16 x 64) are staged in shared memory, then thread t
+// owns basis column q = t % r and the columns of group t / r, with up to 6 accumulators.
+constexpr int kProjRows = 64;
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_leaf_qproj(const T* __restrict__ Q, int r, DTree t, const T* __restrict__ Y,
                                                     int64_t ldy, T* __restrict__ VP, int k) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* ys = reinterpret_cast<T*>(smraw);  // 16 x m
+  const int ldq = r + 1;
+  T* qs = reinterpret_cast<T*>(smraw);   // kProjRows x (r + 1): element (i, q) at i * ldq + q
+  T* ys = qs + kProjRows * ldq;           // 16 x kProjRows
   const int64_t leaf = blockIdx.x;
   const int m = d_leaf_size(t, leaf);
   const int64_t s = d_leaf_start(t, leaf);
   const int c0 = blockIdx.y * 16;
   const int nc = min(16, k - c0);
-  for (int e = threadIdx.x; e < nc * m; e += blockDim.x) {
-    const int c = e / m, i = e % m;
-    ys[c * m + i] = Y[(int64_t)(c0 + c) * ldy + s + i];
-  }
-  __syncthreads();
+  const int tid = threadIdx.x;
+  const int G = blockDim.x / r;                 // column groups (>= 3 for r <= 80)
+  const int q = tid % r, g = tid / r;
+  const int cper = (nc + G - 1) / G;            // <= 6
+  const int cb = g * cper, ce = min(nc, cb + cper);
+  const bool active = g < G;
+  T acc[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) acc[j] = T(0.0);
   const T* Ql = Q + s * r;
-  for (int e = threadIdx.x; e < nc * r; e += blockDim.x) {
-    const int q = e % r, c = e / r;
-    VP[(leaf * k + c0 + c) * r + q] = dot4l(Ql + (int64_t)q * m, 1, ys + c * m, m);
+  for (int i0 = 0; i0 < m; i0 += kProjRows) {
+    const int rows = min(kProjRows, m - i0);
+    __syncthreads();
+    for (int e = tid; e < rows * r; e += blockDim.x) {
+      const int qq = e / rows, i = e - qq * rows;
+      qs[i * ldq + qq] = Ql[(int64_t)qq * m + i0 + i];
+    }
+    for (int e = tid; e < nc * rows; e += blockDim.x) {
+      const int c = e / rows, i = e - c * rows;
+      ys[c * kProjRows + i] = Y[(int64_t)(c0 + c) * ldy + s + i0 + i];
+    }
+    __syncthreads();
+    if (active) {
+      for (int i = 0; i < rows; ++i) {
+        const T a = qs[i * ldq + q];
+#pragma unroll
+        for (int j = 0; j < 6; ++j)
+          if (cb + j < ce) acc[j] += a * ys[(cb + j) * kProjRows + i];
+      }
+    }
   }
+  if (active)
+#pragma unroll
+    for (int j = 0; j < 6; ++j)
+      if (cb + j < ce) VP[(leaf * k + c0 + cb + j) * r + q] = acc[j];
 }
 
+// y_c += sign * Q_leaf g_c for a chunk of up to 16 columns: thread per leaf row, the chunk's
+// coefficients g (16 x r) in shared memory, one accumulator per column; Q is read once.
 template <typename T>
 __global__ void __launch_bounds__(256) k_leaf_qexpand(const T* __restrict__ Q, int r, DTree t, const T* __restrict__ VG,
                                                       T* __restrict__ Y, int64_t ldy, int k, double sign) {
@@ -210,11 +222,23 @@ __global__ void __launch_bounds__(256) k_leaf_qexpand(const T* __restrict__ Q, i
   for (int e = threadIdx.x; e < nc * r; e += blockDim.x) gs[e] = VG[(leaf * k + c0) * r + e];
   __syncthreads();
   const T* Ql = Q + s * r;
-  for (int e = threadIdx.x; e < nc * m; e += blockDim.x) {
-    const int i = e % m, c = e / m;
-    const T acc = dot4l(Ql + i, m, gs + c * r, r);
-    T* y = Y + (int64_t)(c0 + c) * ldy + s + i;
-    *y = (sign > 0.0) ? *y + acc : *y - acc;
+  const bool add = sign > 0.0;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    T acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) acc[c] = T(0.0);
+    for (int q = 0; q < r; ++q) {
+      const T a = Ql[(int64_t)q * m + i];
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        if (c < nc) acc[c] += a * gs[c * r + q];
+    }
+#pragma unroll
+    for (int c = 0; c < 16; ++c)
+      if (c < nc) {
+        T* y = Y + (int64_t)(c0 + c) * ldy + s + i;
+        *y = add ? *y + acc[c] : *y - acc[c];
+      }
   }
 }
 
@@ -237,9 +261,13 @@ bool launch_leaf_tri(const T* Lf, const Tree& t, int op, T* Bptr, int64_t bmul, 
                      int64_t xmul, int64_t xld, int xld_is_m, int ncols, cudaStream_t st) {
   LeafOperand B{reinterpret_cast<double*>(Bptr), bmul, bld, bld_is_m};
   LeafOperand X{reinterpret_cast<double*>(Xptr), xmul, xld, xld_is_m};
-  if (ncols > 8 && tri_launch<T, 16>(Lf, t, op, B, X, ncols, st)) return true;
-  if (tri_launch<T, 8>(Lf, t, op, B, X, ncols, st)) return true;
-  if (tri_launch<T, 4>(Lf, t, op, B, X, ncols, st)) return true;
+  // widest column chunk that still gives about four CTAs per SM (each CTA re-reads its leaf's
+  // factor, which the L2 serves)
+  auto ctas = [&](int nc) { return t.nleaf * (int64_t)((ncols + nc - 1) / nc); };
+  const int64_t want = 4 * 152;
+  if (ncols > 8 && ctas(16) >= want && tri_launch<T, 16>(Lf, t, op, B, X, ncols, st)) return true;
+  if (ncols > 4 && ctas(8) >= want && tri_launch<T, 8>(Lf, t, op, B, X, ncols, st)) return true;
+  if (ncols > 1 && tri_launch<T, 4>(Lf, t, op, B, X, ncols, st)) return true;
   return tri_launch<T, 1>(Lf, t, op, B, X, ncols, st);
 }
 
@@ -267,7 +295,7 @@ template <typename T>
 void launch_leaf_proj(const T* Q, const T*, int r, const Tree& t, const T* Y, int64_t ldy, T* VP, int k,
                       cudaStream_t st) {
   dim3 grid((unsigned)t.nleaf, (unsigned)((k + 15) / 16));
-  const size_t sm = (size_t)16 * t.max_leaf * sizeof(T);
+  const size_t sm = ((size_t)kProjRows * (r + 1) + 16 * kProjRows) * sizeof(T);
   smem_limit((const void*)k_leaf_qproj<T>, sm);
   k_leaf_qproj<T><<<grid, 256, sm, st>>>(Q, r, dtree(t), Y, ldy, VP, k);
 }
