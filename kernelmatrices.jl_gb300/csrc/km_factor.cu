@@ -304,6 +304,7 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
   T* X3 = X2 + r * ld;
   T* va = X3 + r * ld;  // r values: sqrt(d_j), then the reflector betas
   T* vb = va + r;       // r values: 1 / L22[j][j], then the reflector scales
+  T* vc = vb + r;       // r values: 1 / d_j during the Cholesky, then the reflector taus
   const int64_t k = blockIdx.x;
   const int64_t node = nbase + k;  // node index within all nodes (level-major)
   const T* R1 = R + (cbase + 2 * k) * (int64_t)r * r;
@@ -376,19 +377,30 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
     if (i < r && i >= c) X3[i + c * ld] = (i == c ? T(1.0) : T(0.0)) - (a0 + a1);
   }
   __syncthreads();
-  // L22 = chol(H): unscaled right-looking elimination, a_ik -= a_ij a_kj / d_j
+  // L22 = chol(H): unscaled right-looking elimination, a_ik -= a_ij a_kj / d_j.  The thread
+  // that updates the next diagonal entry also forms its reciprocal, so a column step costs one
+  // barrier and no division on the other threads.
+  if (tid == 0) {
+    const T d = X3[0];
+    vc[0] = d > 0.0 ? T(1.0) / d : T(0.0);
+  }
+  __syncthreads();
   int bad = 0;
   for (int j = 0; j < r; ++j) {
-    const T d = X3[j + j * ld];
-    const bool ok = d > 0.0;
-    if (!ok && bad == 0) bad = j + 1;
-    const T inv = ok ? T(1.0) / d : T(0.0);
-    const int ncol = r - 1 - j;
-    for (int q = w; q < ncol * nch; q += nw) {
-      const int c = j + 1 + q / nch, s = q - (q / nch) * nch, i = 32 * s + lane;
-      if (32 * s + 31 < c) continue;
+    if (!(X3[j + j * ld] > 0.0) && bad == 0) bad = j + 1;
+    const T inv = vc[j];
+    // column c of the trailing matrix belongs to warp (c - j - 1) % nw; its rows c..r-1 live in
+    // the lanes of the chunks c/32 .. nch-1
+    for (int c = j + 1 + w; c < r; c += nw) {
       const T f = X3[c + j * ld] * inv;
-      if (i < r && i >= c) X3[i + c * ld] -= X3[i + j * ld] * f;
+      for (int s = c >> 5; s < nch; ++s) {
+        const int i = 32 * s + lane;
+        if (i < r && i >= c) {
+          const T v = X3[i + c * ld] - X3[i + j * ld] * f;
+          X3[i + c * ld] = v;
+          if (i == c && c == j + 1) vc[c] = v > 0.0 ? T(1.0) / v : T(0.0);
+        }
+      }
     }
     __syncthreads();
   }
@@ -424,43 +436,56 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
     if (i < r) X2[i + c * ld] -= a0 + a1;
   }
   __syncthreads();
-  // B <- L22^{-1} B: one warp per column, rows in registers (row i: lane i % 32, slot i / 32)
-  for (int c = w; c < r; c += nw) {
-    T x[3];
+  // B <- L22^{-1} B: one warp per column, rows in registers (row i: lane i % 32, slot i / 32);
+  // a warp solves two columns at once (two independent chains) and skips the row slots that
+  // lie above the current pivot
+  for (int c = w; c < r; c += 2 * nw) {
+    const int c2 = c + nw;
+    const bool two = c2 < r;
+    T x[3], y[3];
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
       const int i = lane + 32 * s;
       x[s] = i < r ? X2[i + c * ld] : T(0.0);
+      y[s] = (two && i < r) ? X2[i + c2 * ld] : T(0.0);
     }
     for (int p = 0; p < r; ++p) {
       const int ps = p >> 5;
       const T xp = shfl_idx(ps == 0 ? x[0] : (ps == 1 ? x[1] : x[2]), p & 31) * vb[p];
+      const T yp = shfl_idx(ps == 0 ? y[0] : (ps == 1 ? y[1] : y[2]), p & 31) * vb[p];
 #pragma unroll
       for (int s = 0; s < 3; ++s) {
+        if (32 * s + 31 < p) continue;
         const int i = lane + 32 * s;
-        if (i == p) x[s] = xp;
-        else if (i > p && i < r) x[s] -= X3[i + p * ld] * xp;
+        if (i == p) {
+          x[s] = xp;
+          y[s] = yp;
+        } else if (i > p && i < r) {
+          const T l = X3[i + p * ld];
+          x[s] -= l * xp;
+          y[s] -= l * yp;
+        }
       }
     }
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
       const int i = lane + 32 * s;
-      if (i < r) X2[i + c * ld] = x[s];
+      if (i < r) {
+        X2[i + c * ld] = x[s];
+        if (two) X2[i + c2 * ld] = y[s];
+      }
     }
   }
   __syncthreads();
   // structured Householder QR of [X1 (upper r x r) ; X2 (r x r)]: reflector j acts on row j of
-  // the top and all r rows of the bottom.  Every warp forms the reflector itself; the betas and
-  // the scaling of the reflector columns are applied after the loop.
-  for (int j = 0; j < r; ++j) {
-    T v[3];
+  // the top and all r rows of the bottom.  Warp 0 owns column j+1 at step j: it applies
+  // reflector j to it and forms reflector j+1 from the result, so the other warps read the
+  // reflector scalars (beta, scale, tau) from shared memory; the betas and the scaling of the
+  // reflector columns are applied after the loop.  One barrier per reflector.
+  auto reflector = [&](int j, const T (&v)[3]) {
     T part = T(0.0);
 #pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      const int i = lane + 32 * s;
-      v[s] = i < r ? X2[i + j * ld] : T(0.0);
-      part += v[s] * v[s];
-    }
+    for (int s = 0; s < 3; ++s) part += v[s] * v[s];
     const T sig = warp_sum_t(part);
     const T alpha = X1[j + j * ld];
     T tj = T(0.0), beta = alpha, scal = T(0.0);
@@ -470,28 +495,56 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       tj = (beta - alpha) / beta;
       scal = T(1.0) / (alpha - beta);
     }
-    if (tid == 0) {
+    if (lane == 0) {
       va[j] = beta;
       vb[j] = scal;
+      vc[j] = tj;
       Etau[node * (int64_t)r + j] = tj;
     }
-    if (tj != 0.0) {
-      for (int c = j + 1 + w; c < r; c += nw) {
+  };
+  if (w == 0) {
+    T v[3];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int i = lane + 32 * s;
+      v[s] = i < r ? X2[i] : T(0.0);
+    }
+    reflector(0, v);
+  }
+  __syncthreads();
+  for (int j = 0; j < r; ++j) {
+    const T tj = vc[j], scal = vb[j];
+    T v[3];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int i = lane + 32 * s;
+      v[s] = i < r ? X2[i + j * ld] : T(0.0);
+    }
+    // warp 0: column j+1 (then reflector j+1); warps 1..: columns j+2, j+3, ...
+    const int cfirst = (w == 0) ? j + 1 : j + 1 + w;
+    const int cstep = (w == 0) ? r : nw - 1;
+    for (int c = cfirst; c < r; c += cstep) {
+      T xc[3];
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        const int i = lane + 32 * s;
+        xc[s] = i < r ? X2[i + c * ld] : T(0.0);
+      }
+      if (tj != 0.0) {
         T acc = T(0.0);
 #pragma unroll
-        for (int s = 0; s < 3; ++s) {
-          const int i = lane + 32 * s;
-          if (i < r) acc += v[s] * X2[i + c * ld];
-        }
+        for (int s = 0; s < 3; ++s) acc += v[s] * xc[s];
         acc = (warp_sum_t(acc) * scal + X1[j + c * ld]) * tj;
         if (lane == 0) X1[j + c * ld] -= acc;
         const T f = acc * scal;
 #pragma unroll
         for (int s = 0; s < 3; ++s) {
           const int i = lane + 32 * s;
-          if (i < r) X2[i + c * ld] -= f * v[s];
+          xc[s] -= f * v[s];
+          if (i < r) X2[i + c * ld] = xc[s];
         }
       }
+      if (w == 0) reflector(c, xc);
     }
     __syncthreads();
   }
@@ -808,7 +861,7 @@ void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T
         reinterpret_cast<double*>(Ct), reinterpret_cast<double*>(L22), reinterpret_cast<double*>(Eref),
         reinterpret_cast<double*>(Etau), info);
   } else {
-    const size_t sm = ((size_t)4 * r * (r + 1) + 2 * r) * sizeof(T);
+    const size_t sm = ((size_t)4 * r * (r + 1) + 3 * r) * sizeof(T);
     smem_limit((const void*)k_node_factor<T>, sm);
     k_node_factor<T><<<(unsigned)t.nodes_at(level), 1024, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase,
                                                                    nbase, Ct, L22, Eref, Etau, info);

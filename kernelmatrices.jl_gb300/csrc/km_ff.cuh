@@ -53,15 +53,44 @@ __device__ __forceinline__ ff operator+(ff a, ff b) {
 __device__ __forceinline__ ff operator-(ff a) { return ff(-a.hi, -a.lo); }
 __device__ __forceinline__ ff operator-(ff a, ff b) { return a + (-b); }
 
-__device__ __forceinline__ ff operator*(ff a, ff b) {
+// A product is returned unnormalised (p + e with e the exact rounding error of a.hi*b.hi plus
+// the cross terms) and normalised only when it is used as a value.  acc + a*b and acc - a*b
+// then add (p, e) to acc directly, which saves the intermediate FastTwoSum: 15 FP32
+// instructions per multiply-add instead of 18.
+struct ffprod {
+  float p, e;
+  __device__ __forceinline__ operator ff() const {
+    ff r;
+    ff_fast_two_sum(p, e, r.hi, r.lo);
+    return r;
+  }
+};
+
+__device__ __forceinline__ ffprod operator*(ff a, ff b) {
   const float p = __fmul_rn(a.hi, b.hi);
   float e = __fmaf_rn(a.hi, b.hi, -p);
   e = __fmaf_rn(a.hi, b.lo, e);
   e = __fmaf_rn(a.lo, b.hi, e);
+  return ffprod{p, e};
+}
+
+__device__ __forceinline__ ff operator+(ff a, ffprod b) {
+  float s, t;
+  ff_two_sum(a.hi, b.p, s, t);
+  t = __fadd_rn(t, __fadd_rn(a.lo, b.e));
   ff r;
-  ff_fast_two_sum(p, e, r.hi, r.lo);
+  ff_fast_two_sum(s, t, r.hi, r.lo);
   return r;
 }
+__device__ __forceinline__ ff operator+(ffprod b, ff a) { return a + b; }
+__device__ __forceinline__ ff operator-(ff a, ffprod b) { return a + ffprod{-b.p, -b.e}; }
+__device__ __forceinline__ ff operator-(ffprod b) { return ff(ffprod{-b.p, -b.e}); }
+__device__ __forceinline__ ff operator+(ffprod a, ffprod b) { return ff(a) + b; }
+__device__ __forceinline__ ff operator-(ffprod a, ffprod b) { return ff(a) - b; }
+__device__ __forceinline__ ff operator-(ffprod a, ff b) { return ff(a) - b; }
+__device__ __forceinline__ ffprod operator*(ffprod a, ff b) { return ff(a) * b; }
+__device__ __forceinline__ ffprod operator*(ff a, ffprod b) { return a * ff(b); }
+__device__ __forceinline__ ffprod operator*(ffprod a, ffprod b) { return ff(a) * ff(b); }
 
 __device__ __forceinline__ ff operator/(ff a, ff b) {
   const float q1 = __fdiv_rn(a.hi, b.hi);
@@ -74,7 +103,9 @@ __device__ __forceinline__ ff operator/(ff a, ff b) {
 
 __device__ __forceinline__ ff& operator+=(ff& a, ff b) { return a = a + b; }
 __device__ __forceinline__ ff& operator-=(ff& a, ff b) { return a = a - b; }
-__device__ __forceinline__ ff& operator*=(ff& a, ff b) { return a = a * b; }
+__device__ __forceinline__ ff& operator+=(ff& a, ffprod b) { return a = a + b; }
+__device__ __forceinline__ ff& operator-=(ff& a, ffprod b) { return a = a - b; }
+__device__ __forceinline__ ff& operator*=(ff& a, ff b) { return a = ff(a * b); }
 __device__ __forceinline__ ff& operator/=(ff& a, ff b) { return a = a / b; }
 
 // Comparisons with a double constant b, in float arithmetic.  Exact when b is a float pair
