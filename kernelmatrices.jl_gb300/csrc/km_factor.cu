@@ -376,10 +376,25 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
     if (l < r) a0 += X0[l + ii * ld] * X0[l + c * ld];
     if (i < r && i >= c) X3[i + c * ld] = (i == c ? T(1.0) : T(0.0)) - (a0 + a1);
   }
+  // B = R2 - Ct' R1 -> X2 (column c of R1 has entries l <= c; R1 read from global memory)
+  if (level < L)
+    for (int q = w; q < nitems; q += nw) {
+      const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
+      const T* r1 = R1 + (int64_t)c * r;
+      T a0 = T(0.0), a1 = T(0.0);
+      int l = 0;
+      for (; l + 1 <= c; l += 2) {
+        a0 += X0[l + ii * ld] * r1[l];
+        a1 += X0[l + 1 + ii * ld] * r1[l + 1];
+      }
+      if (l <= c) a0 += X0[l + ii * ld] * r1[l];
+      if (i < r) X2[i + c * ld] -= a0 + a1;
+    }
   __syncthreads();
-  // L22 = chol(H): unscaled right-looking elimination, a_ik -= a_ij a_kj / d_j.  The thread
-  // that updates the next diagonal entry also forms its reciprocal, so a column step costs one
-  // barrier and no division on the other threads.
+  // L22 = chol(H): unscaled right-looking elimination, a_ik -= a_ij a_kj / d_j, with the forward
+  // substitution L22^{-1} B carried along on the rows of B (b_c -= (a_cj / d_j) b_j; row j is
+  // scaled by 1/sqrt(d_j) afterwards).  The thread that updates the next diagonal entry also
+  // forms its reciprocal, so a step costs one barrier and no division on the other threads.
   if (tid == 0) {
     const T d = X3[0];
     vc[0] = d > 0.0 ? T(1.0) / d : T(0.0);
@@ -401,6 +416,11 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
           if (i == c && c == j + 1) vc[c] = v > 0.0 ? T(1.0) / v : T(0.0);
         }
       }
+      if (level < L)
+        for (int s = 0; s < nch; ++s) {
+          const int kk = 32 * s + lane;
+          if (kk < r) X2[c + kk * ld] -= f * X2[j + kk * ld];
+        }
     }
     __syncthreads();
   }
@@ -412,8 +432,11 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
     vb[j] = T(1.0) / sd;
   }
   __syncthreads();
-  for (int c = w; c < r; c += nw)
+  for (int c = w; c < r; c += nw) {
     for (int i = c + lane; i < r; i += 32) X3[i + c * ld] = (i == c) ? va[c] : X3[i + c * ld] * vb[c];
+    if (level < L)
+      for (int k = lane; k < r; k += 32) X2[c + k * ld] = X2[c + k * ld] * vb[c];  // row c of L22^{-1} B
+  }
   __syncthreads();
   // store Ct and L22
   for (int c = w; c < r; c += nw)
@@ -423,70 +446,25 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       L22_out[e] = (i >= c) ? X3[i + c * ld] : T(0.0);
     }
   if (level >= L) return;
-  // B = R2 - Ct' R1 -> X2 (column c of R1 has entries l <= c)
-  for (int q = w; q < nitems; q += nw) {
-    const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
-    T a0 = T(0.0), a1 = T(0.0);
-    int l = 0;
-    for (; l + 1 <= c; l += 2) {
-      a0 += X0[l + ii * ld] * X1[l + c * ld];
-      a1 += X0[l + 1 + ii * ld] * X1[l + 1 + c * ld];
-    }
-    if (l <= c) a0 += X0[l + ii * ld] * X1[l + c * ld];
-    if (i < r) X2[i + c * ld] -= a0 + a1;
-  }
-  __syncthreads();
-  // B <- L22^{-1} B: one warp per column, rows in registers (row i: lane i % 32, slot i / 32);
-  // a warp solves two columns at once (two independent chains) and skips the row slots that
-  // lie above the current pivot
-  for (int c = w; c < r; c += 2 * nw) {
-    const int c2 = c + nw;
-    const bool two = c2 < r;
-    T x[3], y[3];
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      const int i = lane + 32 * s;
-      x[s] = i < r ? X2[i + c * ld] : T(0.0);
-      y[s] = (two && i < r) ? X2[i + c2 * ld] : T(0.0);
-    }
-    for (int p = 0; p < r; ++p) {
-      const int ps = p >> 5;
-      const T xp = shfl_idx(ps == 0 ? x[0] : (ps == 1 ? x[1] : x[2]), p & 31) * vb[p];
-      const T yp = shfl_idx(ps == 0 ? y[0] : (ps == 1 ? y[1] : y[2]), p & 31) * vb[p];
-#pragma unroll
-      for (int s = 0; s < 3; ++s) {
-        if (32 * s + 31 < p) continue;
-        const int i = lane + 32 * s;
-        if (i == p) {
-          x[s] = xp;
-          y[s] = yp;
-        } else if (i > p && i < r) {
-          const T l = X3[i + p * ld];
-          x[s] -= l * xp;
-          y[s] -= l * yp;
-        }
-      }
-    }
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      const int i = lane + 32 * s;
-      if (i < r) {
-        X2[i + c * ld] = x[s];
-        if (two) X2[i + c2 * ld] = y[s];
-      }
-    }
-  }
-  __syncthreads();
   // structured Householder QR of [X1 (upper r x r) ; X2 (r x r)]: reflector j acts on row j of
-  // the top and all r rows of the bottom.  Warp 0 owns column j+1 at step j: it applies
-  // reflector j to it and forms reflector j+1 from the result, so the other warps read the
-  // reflector scalars (beta, scale, tau) from shared memory; the betas and the scaling of the
-  // reflector columns are applied after the loop.  One barrier per reflector.
-  auto reflector = [&](int j, const T (&v)[3]) {
+  // the top and all r rows of the bottom.  A column is held by 8 lanes (lane q of the group has
+  // rows q, q+8, ..., so a dot product needs a 3-level shuffle reduction) and a warp updates 4
+  // columns at once.  Warp 0 owns column j+1 at step j: it applies reflector j to it and forms
+  // reflector j+1 from the result; the other warps read the reflector scalars (beta, scale, tau)
+  // from shared memory.  The betas and the scaling of the reflector columns are applied after
+  // the loop.  One barrier per reflector.
+  const int gq = lane & 7, grp = lane >> 3;
+  const int rpl = (r + 7) >> 3;  // rows per lane (<= 10 for r <= 80)
+  auto gsum = [&](T x) {
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) x = x + shfl_xor(x, o);
+    return x;
+  };
+  auto reflector = [&](int j, const T (&v)[10]) {
     T part = T(0.0);
 #pragma unroll
-    for (int s = 0; s < 3; ++s) part += v[s] * v[s];
-    const T sig = warp_sum_t(part);
+    for (int t = 0; t < 10; ++t) part += v[t] * v[t];
+    const T sig = gsum(part);
     const T alpha = X1[j + j * ld];
     T tj = T(0.0), beta = alpha, scal = T(0.0);
     if (sig != 0.0) {
@@ -502,46 +480,48 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       Etau[node * (int64_t)r + j] = tj;
     }
   };
-  if (w == 0) {
-    T v[3];
+  auto load_col = [&](int c, T (&x)[10]) {
 #pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      const int i = lane + 32 * s;
-      v[s] = i < r ? X2[i] : T(0.0);
+    for (int t = 0; t < 10; ++t) {
+      const int i = gq + 8 * t;
+      x[t] = (t < rpl && i < r) ? X2[i + c * ld] : T(0.0);
     }
+  };
+  if (w == 0) {  // every group of warp 0 forms the same reflector; lane 0 stores it
+    T v[10];
+    load_col(0, v);
     reflector(0, v);
   }
   __syncthreads();
   for (int j = 0; j < r; ++j) {
     const T tj = vc[j], scal = vb[j];
-    T v[3];
+    // warp 0 (all four groups alike, group 0 stores): column j+1, then reflector j+1;
+    // warps 1..: 4 columns each from j+2 on.  All lanes of a warp run the shuffles.
+    const int c = (w == 0) ? j + 1 : j + 2 + 4 * (w - 1) + grp;
+    const bool valid = c < r;
+    const bool mine = valid && (w != 0 || grp == 0);
+    if (__any_sync(0xffffffffu, valid)) {
+      T v[10], xc[10];
+      load_col(j, v);
+      if (valid) {
+        load_col(c, xc);
+      } else {
 #pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      const int i = lane + 32 * s;
-      v[s] = i < r ? X2[i + j * ld] : T(0.0);
-    }
-    // warp 0: column j+1 (then reflector j+1); warps 1..: columns j+2, j+3, ...
-    const int cfirst = (w == 0) ? j + 1 : j + 1 + w;
-    const int cstep = (w == 0) ? r : nw - 1;
-    for (int c = cfirst; c < r; c += cstep) {
-      T xc[3];
-#pragma unroll
-      for (int s = 0; s < 3; ++s) {
-        const int i = lane + 32 * s;
-        xc[s] = i < r ? X2[i + c * ld] : T(0.0);
+        for (int t = 0; t < 10; ++t) xc[t] = T(0.0);
       }
       if (tj != 0.0) {
         T acc = T(0.0);
 #pragma unroll
-        for (int s = 0; s < 3; ++s) acc += v[s] * xc[s];
-        acc = (warp_sum_t(acc) * scal + X1[j + c * ld]) * tj;
-        if (lane == 0) X1[j + c * ld] -= acc;
+        for (int t = 0; t < 10; ++t) acc += v[t] * xc[t];
+        const T top = valid ? X1[j + c * ld] : T(0.0);
+        acc = (gsum(acc) * scal + top) * tj;
+        if (mine && gq == 0) X1[j + c * ld] = top - acc;
         const T f = acc * scal;
 #pragma unroll
-        for (int s = 0; s < 3; ++s) {
-          const int i = lane + 32 * s;
-          xc[s] -= f * v[s];
-          if (i < r) X2[i + c * ld] = xc[s];
+        for (int t = 0; t < 10; ++t) {
+          const int i = gq + 8 * t;
+          xc[t] -= f * v[t];
+          if (mine && t < rpl && i < r) X2[i + c * ld] = xc[t];
         }
       }
       if (w == 0) reflector(c, xc);
