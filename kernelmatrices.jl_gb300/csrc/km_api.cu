@@ -133,6 +133,9 @@ struct km_handle {
   double* d_dK = nullptr;
   double* d_dPhi = nullptr;
   double* d_Sj = nullptr;
+  double* d_dKf = nullptr;    // float-pair copies (mixed form) of dK leaves, dPhi and Phi
+  double* d_dPhif = nullptr;
+  double* d_Phif = nullptr;
   double* d_GP = nullptr;
   double* d_GG = nullptr;
   int64_t gcap = 0;
@@ -265,6 +268,7 @@ void free_problem(km_handle* h) {
   h->d_gpartial = nullptr;
   h->dk_param = -1;
   h->d_dK = h->d_dPhi = h->d_Sj = h->d_GP = h->d_GG = h->d_T = h->d_U = h->d_dots = nullptr;
+  h->d_dKf = h->d_dPhif = h->d_Phif = nullptr;
   h->gcap = h->tcap = 0;
   h->d_res = h->d_rdots = nullptr;
   h->rcap = 0;
@@ -642,11 +646,18 @@ int derivative_apply(km_handle* h, int j, const double* X, double* Y, int k) {
   const int r = h->r;
   cudaStream_t st = h->stream;
   int rc;
+  int64_t kbytes = 0;
+  for (int64_t q = 0; q < t.nleaf; ++q) kbytes += t.leaf_size(q) * t.leaf_size(q);
   if (h->dk_param < 0) {
-    int64_t kbytes = 0;
-    for (int64_t q = 0; q < t.nleaf; ++q) kbytes += t.leaf_size(q) * t.leaf_size(q);
     if ((rc = grow(h, &h->d_dK, kbytes)) || (rc = grow(h, &h->d_dPhi, t.n * r)) || (rc = grow(h, &h->d_Sj, r * r)))
       return rc;
+    if (h->mixed) {
+      // float-pair copies for the derivative products of the mixed form (FP32 pipe)
+      if ((rc = grow(h, &h->d_dKf, kbytes)) || (rc = grow(h, &h->d_dPhif, t.n * r)) ||
+          (rc = grow(h, &h->d_Phif, t.n * r)))
+        return rc;
+      KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Phif), t.n * r, st));
+    }
   }
   if (k > h->gcap) {
     h->gcap = 0;
@@ -659,18 +670,29 @@ int derivative_apply(km_handle* h, int j, const double* X, double* Y, int k) {
     KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, j, h->d_dK, st));
     KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, j, h->d_dPhi, st));
     KLV(h, KM_PROF_EVAL, launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, j, h->d_Sj, r, st));
+    if (h->mixed) {
+      KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_dK, P<ff>(h->d_dKf), kbytes, st));
+      KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_dPhi, P<ff>(h->d_dPhif), t.n * r, st));
+    }
     h->dk_param = j;
   }
   NodeMatsH nm2{nullptr, nullptr, nullptr, nullptr, 2 * r};
   if (t.L > 0) {
-    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dphiT(h->d_Phi, h->d_dPhi, r, t, X, t.n, h->d_GP, k, st));
+    if (h->mixed)
+      KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dphiT<ff>(P<ff>(h->d_Phif), P<ff>(h->d_dPhif), r, t, X, t.n, h->d_GP, k, st));
+    else
+      KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dphiT<double>(h->d_Phi, h->d_dPhi, r, t, X, t.n, h->d_GP, k, st));
     for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up<double>(t, nm2, l, h->d_GP, nullptr, k, UP_SUM_, st));
     for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down<double>(t, nm2, l, h->d_GP, h->d_GG, nullptr, k, DN_NYS_, st));
   } else {
     KM_CUDA(h, cudaMemsetAsync(h->d_GG, 0, sizeof(double) * 2 * r * k, st));
   }
-  KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dnys_apply(h->d_dK, h->d_Phi, h->d_dPhi, h->d_Sc, h->d_Sj, r, t, X, t.n,
-                                                    h->d_GG, Y, t.n, k, st));
+  if (h->mixed)
+    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dnys_apply<ff>(P<ff>(h->d_dKf), P<ff>(h->d_Phif), P<ff>(h->d_dPhif), h->d_Sc,
+                                                          h->d_Sj, r, t, X, t.n, h->d_GG, Y, t.n, k, st));
+  else
+    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dnys_apply<double>(h->d_dK, h->d_Phi, h->d_dPhi, h->d_Sc, h->d_Sj, r, t, X,
+                                                              t.n, h->d_GG, Y, t.n, k, st));
   return check_launch(h, "derivative");
 }
 
@@ -1599,6 +1621,7 @@ extern "C" int64_t km_estimate_bytes(int64_t n, int64_t rank, int level_kind, in
               4 * std::max<int64_t>(t.nleaf + t.nnode + 1, 1) + d(kLogdetBlocks) + d(4);
   b += 2 * d(slots * r * k) + d(nn * 2 * r * k);  // ensure_vec
   b += 2 * d(n * k);                              // ensure_xy
-  if (with_grad) b += d(kb) + d(n * r) + d(r * r) + 2 * d(slots * 2 * r * k) + 2 * d(n * k) + d(k);
+  if (with_grad)  // derivative workspaces, plus the float-pair copies the mixed form keeps
+    b += d(kb) + d(n * r) + d(r * r) + 2 * d(slots * 2 * r * k) + 2 * d(n * k) + d(k) + d(kb) + 2 * d(n * r);
   return b;
 }

@@ -15,54 +15,83 @@
 
 namespace km {
 
-// VP[leaf][col] = [Phi_leaf' x ; dPhi_leaf' x]  (2r values).  grid (nleaf, ceil(k/8)), block 256.
-__global__ void __launch_bounds__(256) k_leaf_dphiT(const double* __restrict__ Phi, const double* __restrict__ dPhi,
-                                                    int r, DTree t, const double* __restrict__ X, int64_t ldx,
-                                                    double* __restrict__ VP, int k) {
-  extern __shared__ double sm[];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int col = blockIdx.y * 8 + w;
-  if (col >= k) return;
-  const int64_t leaf = blockIdx.x;
-  const int m = d_leaf_size(t, leaf);
-  const int64_t s = d_leaf_start(t, leaf);
-  double* x = sm + (size_t)w * m;
-  const double* src = X + (int64_t)col * ldx + s;
-  for (int i = lane; i < m; i += 32) x[i] = src[i];
-  __syncwarp();
-  double* out = VP + (leaf * k + col) * 2 * r;
-  for (int c = 0; c < 2 * r; ++c) {
-    const double* pc = (c < r ? Phi + s * r + (int64_t)c * m : dPhi + s * r + (int64_t)(c - r) * m);
-    double acc = 0.0;
-    for (int i = lane; i < m; i += 32) acc += pc[i] * x[i];
-    acc = warp_sum(acc);
-    if (lane == 0) out[c] = acc;
-  }
-}
+// VP[leaf][col] = [Phi_leaf' x ; dPhi_leaf' x]  (2r values) for a chunk of 8 columns.  The leaf is
+// processed in chunks of 32 rows: [Phi dPhi] (32 x 2r) and x (8 x 32) are staged in shared
+// memory as T, and thread q < 2r owns output row q with 8 accumulators.  T = double (FP64 form)
+// or ff (mixed form: float-pair copies of Phi and dPhi, x converted on load).
+// grid (nleaf, ceil(k/8)), block 256.
+constexpr int kDRows = 32;
 
-// y_leaf = dK_leaf x + dPhi beta1 + Phi beta2, beta1 = S^{-1} a, beta2 = S^{-1}(b - Sj beta1),
-// [a ; b] = VG[leaf][col].  grid (nleaf, ceil(k/8)), block 256.
-__global__ void __launch_bounds__(256) k_leaf_dnys_apply(const double* __restrict__ dKl, const double* __restrict__ Phi,
-                                                         const double* __restrict__ dPhi, const double* __restrict__ Sc,
-                                                         const double* __restrict__ Sj, int r, DTree t,
-                                                         const double* __restrict__ X, int64_t ldx,
-                                                         const double* __restrict__ VG, double* __restrict__ Y,
-                                                         int64_t ldy, int k) {
-  extern __shared__ double sm[];
+template <typename T>
+__global__ void __launch_bounds__(256) k_leaf_dphiT(const T* __restrict__ Phi, const T* __restrict__ dPhi, int r,
+                                                    DTree t, const double* __restrict__ X, int64_t ldx,
+                                                    double* __restrict__ VP, int k) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int r2 = 2 * r, ldp = r2 + 1;
+  T* ps = reinterpret_cast<T*>(smraw);   // kDRows x (2r + 1)
+  T* xs = ps + kDRows * ldp;              // 8 x kDRows
   const int64_t leaf = blockIdx.x;
   const int m = d_leaf_size(t, leaf);
   const int64_t s = d_leaf_start(t, leaf);
   const int c0 = blockIdx.y * 8;
   const int nc = min(8, k - c0);
-  double* xs = sm;            // 8 x m
-  double* bs = sm + 8 * m;    // 8 x 3r : beta1 | beta2 | tmp
+  const int tid = threadIdx.x;
+  T acc[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) acc[c] = T(0.0);
+  for (int i0 = 0; i0 < m; i0 += kDRows) {
+    const int rows = min(kDRows, m - i0);
+    __syncthreads();
+    for (int e = tid; e < rows * r2; e += blockDim.x) {
+      const int q = e / rows, i = e - q * rows;
+      ps[i * ldp + q] = q < r ? Phi[s * r + (int64_t)q * m + i0 + i] : dPhi[s * r + (int64_t)(q - r) * m + i0 + i];
+    }
+    for (int e = tid; e < 8 * kDRows; e += blockDim.x) {
+      const int c = e / kDRows, i = e - c * kDRows;
+      xs[e] = (c < nc && i < rows) ? from_double<T>(X[(int64_t)(c0 + c) * ldx + s + i0 + i]) : T(0.0);
+    }
+    __syncthreads();
+    if (tid < r2)
+      for (int i = 0; i < rows; ++i) {
+        const T a = ps[i * ldp + tid];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[c] += a * xs[c * kDRows + i];
+      }
+  }
+  if (tid < r2)
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (c < nc) VP[(leaf * k + c0 + c) * r2 + tid] = to_double(acc[c]);
+}
+
+// y_leaf = dK_leaf x + dPhi beta1 + Phi beta2, beta1 = S^{-1} a, beta2 = S^{-1}(b - Sj beta1),
+// [a ; b] = VG[leaf][col], for a chunk of 8 columns.  The betas are solved in FP64 (one warp per
+// column), then x and the betas are staged in shared memory as T and each thread owns leaf rows
+// with 8 accumulators, so every matrix entry read feeds 8 multiply-adds.
+// grid (nleaf, ceil(k/8)), block 256.
+template <typename T>
+__global__ void __launch_bounds__(256) k_leaf_dnys_apply(const T* __restrict__ dKl, const T* __restrict__ Phi,
+                                                         const T* __restrict__ dPhi, const double* __restrict__ Sc,
+                                                         const double* __restrict__ Sj, int r, DTree t,
+                                                         const double* __restrict__ X, int64_t ldx,
+                                                         const double* __restrict__ VG, double* __restrict__ Y,
+                                                         int64_t ldy, int k) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf);
+  const int c0 = blockIdx.y * 8;
+  const int nc = min(8, k - c0);
+  double* bd = reinterpret_cast<double*>(smraw);  // 8 x 3r : beta1 | beta2 | (spare), FP64
+  T* xs = reinterpret_cast<T*>(bd + 8 * 3 * r);   // 8 x m
+  T* bs = xs + 8 * m;                              // 8 x 2r : beta1 | beta2
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int e = threadIdx.x; e < nc * m; e += blockDim.x) {
+  for (int e = threadIdx.x; e < 8 * m; e += blockDim.x) {
     const int c = e / m, i = e % m;
-    xs[c * m + i] = X[(int64_t)(c0 + c) * ldx + s + i];
+    xs[e] = c < nc ? from_double<T>(X[(int64_t)(c0 + c) * ldx + s + i]) : T(0.0);
   }
   if (w < nc) {
-    double* b1 = bs + w * 3 * r;
+    double* b1 = bd + w * 3 * r;
     double* b2 = b1 + r;
     const double* g = VG + (leaf * k + c0 + w) * 2 * r;
     for (int i = lane; i < r; i += 32) {
@@ -70,18 +99,18 @@ __global__ void __launch_bounds__(256) k_leaf_dnys_apply(const double* __restric
       b2[i] = g[r + i];
     }
     __syncwarp();
-    // b1 <- S^{-1} b1 = Sc^{-T} Sc^{-1} b1
     for (int pass = 0; pass < 2; ++pass) {
       double* v = pass == 0 ? b1 : b2;
       if (pass == 1) {
         // b2 <- b2 - Sj b1
         for (int i = lane; i < r; i += 32) {
-          double acc = 0.0;
-          for (int l = 0; l < r; ++l) acc += Sj[i + (int64_t)l * r] * b1[l];
-          b2[i] -= acc;
+          double a = 0.0;
+          for (int l = 0; l < r; ++l) a += Sj[i + (int64_t)l * r] * b1[l];
+          b2[i] -= a;
         }
         __syncwarp();
       }
+      // v <- S^{-1} v = Sc^{-T} Sc^{-1} v
       for (int l = 0; l < r; ++l) {
         const double vl = v[l] / Sc[(int64_t)l * r + l];
         __syncwarp();
@@ -97,20 +126,59 @@ __global__ void __launch_bounds__(256) k_leaf_dnys_apply(const double* __restric
         __syncwarp();
       }
     }
+    for (int i = lane; i < 2 * r; i += 32) bs[w * 2 * r + i] = from_double<T>(b1[i]);
+  } else if (w < 8) {
+    for (int i = lane; i < 2 * r; i += 32) bs[w * 2 * r + i] = T(0.0);
   }
   __syncthreads();
-  const double* K = dKl + d_leaf_koff(t, leaf);
-  const double* P = Phi + s * r;
-  const double* dP = dPhi + s * r;
-  for (int e = threadIdx.x; e < nc * m; e += blockDim.x) {
-    const int c = e / m, i = e % m;
-    const double* xc = xs + c * m;
-    double acc = 0.0;
-    for (int l = 0; l < m; ++l) acc += K[i + (int64_t)l * m] * xc[l];
-    const double* b1 = bs + c * 3 * r;
-    const double* b2 = b1 + r;
-    for (int q = 0; q < r; ++q) acc += dP[i + (int64_t)q * m] * b1[q] + P[i + (int64_t)q * m] * b2[q];
-    Y[(int64_t)(c0 + c) * ldy + s + i] = acc;
+  const T* K = dKl + d_leaf_koff(t, leaf);
+  const T* P = Phi + s * r;
+  const T* dP = dPhi + s * r;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    T acc[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[c] = T(0.0);
+    // four matrix entries are loaded ahead of their multiply-adds so that the loads overlap
+    int l = 0;
+    for (; l + 3 < m; l += 4) {
+      const T a0 = K[i + (int64_t)l * m], a1 = K[i + (int64_t)(l + 1) * m];
+      const T a2 = K[i + (int64_t)(l + 2) * m], a3 = K[i + (int64_t)(l + 3) * m];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        acc[c] += a0 * xs[c * m + l];
+        acc[c] += a1 * xs[c * m + l + 1];
+        acc[c] += a2 * xs[c * m + l + 2];
+        acc[c] += a3 * xs[c * m + l + 3];
+      }
+    }
+    for (; l < m; ++l) {
+      const T a = K[i + (int64_t)l * m];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[c] += a * xs[c * m + l];
+    }
+    int q = 0;
+    for (; q + 1 < r; q += 2) {
+      const T dp0 = dP[i + (int64_t)q * m], p0 = P[i + (int64_t)q * m];
+      const T dp1 = dP[i + (int64_t)(q + 1) * m], p1 = P[i + (int64_t)(q + 1) * m];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        acc[c] += dp0 * bs[c * 2 * r + q];
+        acc[c] += p0 * bs[c * 2 * r + r + q];
+        acc[c] += dp1 * bs[c * 2 * r + q + 1];
+        acc[c] += p1 * bs[c * 2 * r + r + q + 1];
+      }
+    }
+    for (; q < r; ++q) {
+      const T dp = dP[i + (int64_t)q * m], p = P[i + (int64_t)q * m];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        acc[c] += dp * bs[c * 2 * r + q];
+        acc[c] += p * bs[c * 2 * r + r + q];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (c < nc) Y[(int64_t)(c0 + c) * ldy + s + i] = to_double(acc[c]);
   }
 }
 
@@ -164,22 +232,35 @@ void launch_axpby(double* y, const double* x, double a, double b, int64_t n, cud
   k_axpby<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(y, x, a, b, n);
 }
 
-void launch_leaf_dphiT(const double* Phi, const double* dPhi, int r, const Tree& t, const double* X,
-                       int64_t ldx, double* VP, int k, cudaStream_t st) {
+template <typename T>
+void launch_leaf_dphiT(const T* Phi, const T* dPhi, int r, const Tree& t, const double* X, int64_t ldx, double* VP,
+                       int k, cudaStream_t st) {
   dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
-  const size_t sm = (size_t)8 * t.max_leaf * sizeof(double);
-  smem_limit((const void*)k_leaf_dphiT, sm);
-  k_leaf_dphiT<<<grid, 256, sm, st>>>(Phi, dPhi, r, dtree(t), X, ldx, VP, k);
+  const size_t sm = ((size_t)kDRows * (2 * r + 1) + 8 * kDRows) * sizeof(T);
+  smem_limit((const void*)k_leaf_dphiT<T>, sm);
+  k_leaf_dphiT<T><<<grid, 256, sm, st>>>(Phi, dPhi, r, dtree(t), X, ldx, VP, k);
 }
 
-void launch_leaf_dnys_apply(const double* dKl, const double* Phi, const double* dPhi, const double* Sc,
-                            const double* Sj, int r, const Tree& t, const double* X, int64_t ldx,
-                            const double* VG, double* Y, int64_t ldy, int k, cudaStream_t st) {
+template <typename T>
+void launch_leaf_dnys_apply(const T* dKl, const T* Phi, const T* dPhi, const double* Sc, const double* Sj, int r,
+                            const Tree& t, const double* X, int64_t ldx, const double* VG, double* Y, int64_t ldy,
+                            int k, cudaStream_t st) {
   dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
-  const size_t sm = (size_t)8 * (t.max_leaf + 3 * r) * sizeof(double);
-  smem_limit((const void*)k_leaf_dnys_apply, sm);
-  k_leaf_dnys_apply<<<grid, 256, sm, st>>>(dKl, Phi, dPhi, Sc, Sj, r, dtree(t), X, ldx, VG, Y, ldy, k);
+  const size_t sm = (size_t)8 * 3 * r * sizeof(double) + ((size_t)8 * t.max_leaf + 8 * 2 * r) * sizeof(T);
+  smem_limit((const void*)k_leaf_dnys_apply<T>, sm);
+  k_leaf_dnys_apply<T><<<grid, 256, sm, st>>>(dKl, Phi, dPhi, Sc, Sj, r, dtree(t), X, ldx, VG, Y, ldy, k);
 }
+
+template void launch_leaf_dphiT<double>(const double*, const double*, int, const Tree&, const double*, int64_t,
+                                        double*, int, cudaStream_t);
+template void launch_leaf_dphiT<ff>(const ff*, const ff*, int, const Tree&, const double*, int64_t, double*, int,
+                                    cudaStream_t);
+template void launch_leaf_dnys_apply<double>(const double*, const double*, const double*, const double*,
+                                             const double*, int, const Tree&, const double*, int64_t,
+                                             const double*, double*, int64_t, int, cudaStream_t);
+template void launch_leaf_dnys_apply<ff>(const ff*, const ff*, const ff*, const double*, const double*, int,
+                                         const Tree&, const double*, int64_t, const double*, double*, int64_t, int,
+                                         cudaStream_t);
 
 void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n, int k,
                      double* out, cudaStream_t st) {

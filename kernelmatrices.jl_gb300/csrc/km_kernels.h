@@ -121,11 +121,13 @@ void launch_leaf_nys_apply(const double* Kl, const double* Phi, const double* Sc
                            double* Y, int64_t ldy, int k, cudaStream_t st);
 
 // derivative HODLR and gradient pieces
-void launch_leaf_dphiT(const double* Phi, const double* dPhi, int r, const Tree& t, const double* X,
-                       int64_t ldx, double* VP, int k, cudaStream_t st);
-void launch_leaf_dnys_apply(const double* dKl, const double* Phi, const double* dPhi, const double* Sc,
-                            const double* Sj, int r, const Tree& t, const double* X, int64_t ldx,
-                            const double* VG, double* Y, int64_t ldy, int k, cudaStream_t st);
+template <typename T>
+void launch_leaf_dphiT(const T* Phi, const T* dPhi, int r, const Tree& t, const double* X, int64_t ldx, double* VP,
+                       int k, cudaStream_t st);
+template <typename T>
+void launch_leaf_dnys_apply(const T* dKl, const T* Phi, const T* dPhi, const double* Sc, const double* Sj, int r,
+                            const Tree& t, const double* X, int64_t ldx, const double* VG, double* Y, int64_t ldy,
+                            int k, cudaStream_t st);
 void launch_axpby(double* y, const double* x, double a, double b, int64_t n, cudaStream_t st);
 // n x p Rademacher probes (+-1), entry (i, j) from a SplitMix64 hash of (seed, j*n + i)
 void launch_rademacher(double* out, int64_t n, int64_t p, uint64_t seed, cudaStream_t st);

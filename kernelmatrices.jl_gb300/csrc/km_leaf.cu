@@ -70,9 +70,24 @@ __device__ void leaf_tri_body(const T* __restrict__ L, int m, int op, const T* B
         const int g = e / R, i = r0 + (e - g * R), cb = 4 * g;
         const T* xc = xs + cb * m + i0;
         T acc[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
-        for (int l = 0; l < ib; ++l) {
-          const T a = (op == 0) ? L[(int64_t)(i0 + l) * m + i]   // L[i, i0 + l]
-                                : L[(int64_t)i * m + i0 + l];    // L[i0 + l, i]
+        auto ld = [&](int l) {
+          return (op == 0) ? L[(int64_t)(i0 + l) * m + i]   // L[i, i0 + l]
+                           : L[(int64_t)i * m + i0 + l];    // L[i0 + l, i]
+        };
+        int l = 0;
+        for (; l + 3 < ib; l += 4) {  // four entries loaded ahead of their multiply-adds
+          const T a0 = ld(l), a1 = ld(l + 1), a2 = ld(l + 2), a3 = ld(l + 3);
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (cb + j < nc) {
+              acc[j] += a0 * xc[j * m + l];
+              acc[j] += a1 * xc[j * m + l + 1];
+              acc[j] += a2 * xc[j * m + l + 2];
+              acc[j] += a3 * xc[j * m + l + 3];
+            }
+        }
+        for (; l < ib; ++l) {
+          const T a = ld(l);
 #pragma unroll
           for (int j = 0; j < 4; ++j)
             if (cb + j < nc) acc[j] += a * xc[j * m + l];
@@ -227,7 +242,17 @@ __global__ void __launch_bounds__(256) k_leaf_qexpand(const T* __restrict__ Q, i
     T acc[16];
 #pragma unroll
     for (int c = 0; c < 16; ++c) acc[c] = T(0.0);
-    for (int q = 0; q < r; ++q) {
+    int q = 0;
+    for (; q + 1 < r; q += 2) {  // two basis entries loaded ahead of their multiply-adds
+      const T a0 = Ql[(int64_t)q * m + i], a1 = Ql[(int64_t)(q + 1) * m + i];
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        if (c < nc) {
+          acc[c] += a0 * gs[c * r + q];
+          acc[c] += a1 * gs[c * r + q + 1];
+        }
+    }
+    for (; q < r; ++q) {
       const T a = Ql[(int64_t)q * m + i];
 #pragma unroll
       for (int c = 0; c < 16; ++c)
