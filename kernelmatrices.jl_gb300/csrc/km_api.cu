@@ -667,8 +667,8 @@ int derivative_apply(km_handle* h, int j, const double* X, double* Y, int k) {
   }
   if (h->dk_param != j) {
     // DerivativeHODLR (constructor.jl:66-95): dK leaves, dK(X, P) and Sj = dK(P, P)
-    KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, j, h->d_dK, st));
-    KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, j, h->d_dPhi, st));
+    KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, j, h->d_dK, st, h->mixed));
+    KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, j, h->d_dPhi, st, h->mixed));
     KLV(h, KM_PROF_EVAL, launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, j, h->d_Sj, r, st));
     if (h->mixed) {
       KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_dK, P<ff>(h->d_dKf), kbytes, st));
@@ -1159,8 +1159,8 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   KM_CUDA(h, cudaMemcpyAsync(h->d_lndidx, idx.data(), sizeof(int64_t) * r, cudaMemcpyHostToDevice, st));
   KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + t.nnode + 1), st));
   KLV(h, KM_PROF_EVAL, launch_gather_points(h->d_pts, h->d_lndidx, r, h->d_lnd, st));
-  KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st));
-  KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, -1, h->d_Phi, st));
+  KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st, h->mixed));
+  KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, -1, h->d_Phi, st, h->mixed));
   KLV(h, KM_PROF_EVAL, launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, -1, h->d_S, r, st));
   KM_CUDA(h, cudaMemcpyAsync(h->d_Sc, h->d_S, sizeof(double) * r * r, cudaMemcpyDeviceToDevice, st));
   if (!KL(h, KM_PROF_OTHER, launch_chol_small(h->d_Sc, r, h->d_info + t.nleaf + t.nnode, st)))

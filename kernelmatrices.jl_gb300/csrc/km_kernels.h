@@ -67,10 +67,11 @@ struct NodeMatsH {          // node factors (double or float pairs, by the calle
 };
 
 // assembly
+// use_ff: float-pair evaluation on the FP32 pipe (mixed form, ~1e-14 relative), else FP64
 void launch_eval_leaves(const double* pts, const Tree& t, KParams kp, int deriv, double* K,
-                        cudaStream_t st);
+                        cudaStream_t st, bool use_ff = false);
 void launch_eval_phi(const double* pts, const double* lnd, int r, const Tree& t, KParams kp,
-                     int deriv, double* Phi, cudaStream_t st);
+                     int deriv, double* Phi, cudaStream_t st, bool use_ff = false);
 void launch_eval_dense(const double* a, int na, const double* b, int nb, KParams kp, int deriv,
                        double* out, int ld, cudaStream_t st);
 void launch_gather_points(const double* pts, const int64_t* idx, int r, double* lnd,

@@ -80,3 +80,23 @@ def test_mixed_gradient(lib):
     nmx, gmx = hmx.nll_grad(y, V)
     assert abs(nmx - n64) < 1e-6
     assert np.all(np.abs(gmx - g64) <= 1e-6 * np.abs(g64) + 1e-6)
+
+
+@pytest.mark.parametrize("kid,params", [(1, (1.0, 0.1, 1e-3)), (1, (2.0, 0.02, 1e-4)), (0, (1.3, 0.2, 1e-2))])
+def test_mixed_kernel_entries(kid, params, lib):
+    """The mixed form evaluates kernel entries in float pairs (own exp: Cody-Waite reduction +
+    Taylor series).  Its pre-factor matvec (leaf blocks + Nystrom sums, FP64 arithmetic on the
+    float-pair-evaluated entries) and derivative products must match the FP64 form to 1e-13 /
+    1e-12 relative."""
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    n = 4096
+    pts = uniform_points(n, 77)
+    kern = K.Matern32() if kid == 1 else K.RatQuad()
+    km = K.KernelMatrix(pts, pts, params, kern)
+    h64 = K.KernelHODLR(km, 0.0, 64, K.FixedLevel(4), nystrom=True)
+    hmx = K.KernelHODLR(km, 0.0, 64, K.FixedLevel(4), nystrom=True, precision=K.KM_PREC_MIXED)
+    x = np.random.default_rng(5).standard_normal((n, 3))
+    assert rel(hmx @ x, h64 @ x) < 1e-13
+    for j in range(3):
+        assert rel(hmx.derivative_matvec(j, x), h64.derivative_matvec(j, x)) < 1e-12
