@@ -96,6 +96,7 @@ struct km_handle {
   double* d_Etau = nullptr;
   double* d_L22i = nullptr;  // L22^{-1} per node
   double* d_E = nullptr;     // explicit 2r x r transfer per node
+  double* d_NT = nullptr;    // transposes per node: Ct', L22', L22^{-1}', E' (5 r^2 per node)
   int* d_info = nullptr;
   double* d_partial = nullptr;
   double* d_scalar = nullptr;
@@ -242,7 +243,7 @@ void free_problem(km_handle* h) {
   h->bytes = 0;
   h->d_pts = h->d_lnd = h->d_K = h->d_Lf = h->d_Phi = h->d_Q = h->d_tauleaf = h->d_R = nullptr;
   h->d_S = h->d_Sc = h->d_SinvT = h->d_SinvTf = h->d_Ct = h->d_L22 = h->d_Eref = h->d_Etau = nullptr;
-  h->d_L22i = h->d_E = nullptr;
+  h->d_L22i = h->d_E = h->d_NT = nullptr;
   h->d_lndidx = nullptr;
   h->d_info = nullptr;
   h->d_partial = h->d_scalar = nullptr;
@@ -360,7 +361,15 @@ int ensure_xy(km_handle* h, int64_t k) {
   return KM_OK;
 }
 
-NodeMatsH node_mats(km_handle* h) { return NodeMatsH{h->d_Ct, h->d_L22, h->d_L22i, h->d_E, h->r}; }
+NodeMatsH node_mats(km_handle* h) {
+  const int64_t blk = std::max<int64_t>(h->tree.nnode, 1) * h->r * h->r;
+  NodeMatsH nm{h->d_Ct, h->d_L22, h->d_L22i, h->d_E, h->r};
+  nm.CtT = h->d_NT;
+  nm.L22T = h->d_NT + blk;
+  nm.L22iT = h->d_NT + 2 * blk;
+  nm.ET = h->d_NT + 3 * blk;
+  return nm;
+}
 
 // ---- factor sweeps on a device block X (n x k, ld = n), in place ---------------------------
 
@@ -1144,6 +1153,7 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
        (rc = grow(h, &h->d_Etau, std::max<int64_t>(t.nnode, 1) * r)) ||
        (rc = grow(h, &h->d_L22i, std::max<int64_t>(t.nnode, 1) * r * r)) ||
        (rc = grow(h, &h->d_E, std::max<int64_t>(t.nnode, 1) * 2 * r * r)) ||
+       (rc = grow(h, &h->d_NT, std::max<int64_t>(t.nnode, 1) * 5 * r * r)) ||
        (rc = grow(h, &h->d_info, t.nleaf + t.nnode + 1)) ||
        (rc = grow(h, &h->d_partial, kLogdetBlocks)) || (rc = grow(h, &h->d_scalar, 4)))) {
     free_problem(h);
@@ -1226,8 +1236,12 @@ int km_factorize(km_handle* h) {
                                                     P<ff>(h->d_L22), P<ff>(h->d_Eref), P<ff>(h->d_Etau),
                                                     h->d_info + t.nleaf, st));
         side_level(h, l);
-        launch_node_finalize<ff>(P<ff>(h->d_L22), P<ff>(h->d_Eref), P<ff>(h->d_Etau), r, l, t, P<ff>(h->d_L22i),
-                                 P<ff>(h->d_E), h->side);
+        {
+          const NodeMatsH nm = node_mats(h);
+          launch_node_finalize<ff>(P<ff>(h->d_L22), P<ff>(h->d_Ct), P<ff>(h->d_Eref), P<ff>(h->d_Etau), r, l, t,
+                                   P<ff>(h->d_L22i), P<ff>(h->d_E), P<ff>((double*)nm.CtT), P<ff>((double*)nm.L22T),
+                                   P<ff>((double*)nm.L22iT), P<ff>((double*)nm.ET), h->side);
+        }
       }
       side_end(h);
     }
@@ -1243,7 +1257,12 @@ int km_factorize(km_handle* h) {
         KLV(h, KM_PROF_NODE, launch_node_factor<double>(h->d_R, h->d_SinvT, r, l, t, h->d_Ct, h->d_L22, h->d_Eref,
                                                         h->d_Etau, h->d_info + t.nleaf, st));
         side_level(h, l);
-        launch_node_finalize<double>(h->d_L22, h->d_Eref, h->d_Etau, r, l, t, h->d_L22i, h->d_E, h->side);
+        {
+          const NodeMatsH nm = node_mats(h);
+          launch_node_finalize<double>(h->d_L22, h->d_Ct, h->d_Eref, h->d_Etau, r, l, t, h->d_L22i, h->d_E,
+                                       (double*)nm.CtT, (double*)nm.L22T, (double*)nm.L22iT, (double*)nm.ET,
+                                       h->side);
+        }
       }
       side_end(h);
     }
@@ -1617,7 +1636,7 @@ extern "C" int64_t km_estimate_bytes(int64_t n, int64_t rank, int level_kind, in
   for (int64_t j = 0; j < t.nleaf; ++j) kb += t.leaf_size(j) * t.leaf_size(j);
   auto d = [](int64_t c) { return 8 * std::max<int64_t>(c, 1); };
   int64_t b = d(2 * n) + d(2 * r) + d(r) + 2 * d(kb) + 2 * d(n * r) + d(t.nleaf * r) + d(slots * r * r) +
-              4 * d(r * r) + 3 * d(nn * r * r) + d(nn * r) + d(nn * r * r) + d(nn * 2 * r * r) +
+              4 * d(r * r) + 3 * d(nn * r * r) + d(nn * r) + d(nn * r * r) + d(nn * 2 * r * r) + d(nn * 5 * r * r) +
               4 * std::max<int64_t>(t.nleaf + t.nnode + 1, 1) + d(kLogdetBlocks) + d(4);
   b += 2 * d(slots * r * k) + d(nn * 2 * r * k);  // ensure_vec
   b += 2 * d(n * k);                              // ensure_xy

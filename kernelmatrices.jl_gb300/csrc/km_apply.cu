@@ -26,6 +26,10 @@ struct NodeMats {
   const T* L22i;  // r x r lower, inverse of L22
   const T* E;     // 2r x r explicit transfer
   int r;
+  const T* CtT;   // transposes: a thread per output row reads consecutive addresses across a warp
+  const T* L22T;
+  const T* L22iT;
+  const T* ET;    // r x 2r
 };
 
 // up-sweep modes
@@ -82,8 +86,9 @@ __global__ void __launch_bounds__(512) k_up(NodeMats<T> nm, int level, int L, in
   }
   __syncthreads();
   const T* Ct = nm.Ct + node * (int64_t)r * r;
-  const T* L22 = nm.L22 + node * (int64_t)r * r;
   const T* L22i = nm.L22i + node * (int64_t)r * r;
+  const T* CtT = nm.CtT + node * (int64_t)r * r;
+  const T* L22T = nm.L22T + node * (int64_t)r * r;
   if (mode == UP_SUM) {
     if (level < L)
       for (int e = tid; e < kc * r; e += nth) {
@@ -97,7 +102,7 @@ __global__ void __launch_bounds__(512) k_up(NodeMats<T> nm, int level, int L, in
     for (int e = tid; e < kc * r; e += nth) {
       const int c = e / r, i = e % r;
       const T* z1 = z + c * r2;
-      tb[c * r + i] = z1[r + i] - dot4(Ct + (int64_t)i * r, 1, z1, r);
+      tb[c * r + i] = z1[r + i] - dot4(CtT + i, r, z1, r);
     }
     __syncthreads();
     // w = L22^{-1} t
@@ -119,7 +124,7 @@ __global__ void __launch_bounds__(512) k_up(NodeMats<T> nm, int level, int L, in
       const int c = e / r, i = e % r;
       const T* z2 = z + c * r2 + r;
       const T a1 = dot4(Ct + i, r, z2, r);
-      const T a2 = dot4(L22 + (int64_t)i * r + i, 1, z2 + i, r - i) - z2[i];
+      const T a2 = dot4(L22T + i + (int64_t)i * r, r, z2 + i, r - i) - z2[i];
       tb[c * r + i] = a1;
       ub[c * r + i] = a2;
       VD[(node * k + c0 + c) * 2 * r + i] = a1;
@@ -134,10 +139,10 @@ __global__ void __launch_bounds__(512) k_up(NodeMats<T> nm, int level, int L, in
     __syncthreads();
   }
   if (level < L) {
-    const T* E = nm.E + node * (int64_t)r2 * r;
+    const T* ET = nm.ET + node * (int64_t)r2 * r;
     for (int e = tid; e < kc * r; e += nth) {
       const int c = e / r, q = e % r;
-      VP[((nslot0 + kk) * k + c0 + c) * r + q] = dot4(E + (int64_t)q * r2, 1, z + c * r2, r2);
+      VP[((nslot0 + kk) * k + c0 + c) * r + q] = dot4(ET + q, r, z + c * r2, r2);
     }
   }
 }
@@ -182,7 +187,8 @@ __global__ void __launch_bounds__(512) k_down(NodeMats<T> nm, int level, int L, 
   __syncthreads();
   const T* Ct = nm.Ct + node * (int64_t)r * r;
   const T* L22 = nm.L22 + node * (int64_t)r * r;
-  const T* L22i = nm.L22i + node * (int64_t)r * r;
+  const T* CtT = nm.CtT + node * (int64_t)r * r;
+  const T* L22iT = nm.L22iT + node * (int64_t)r * r;
   if (mode == DN_FWD || mode == DN_MULT) {
     for (int e = tid; e < kc * r; e += nth) {
       const int c = e / r, i = e % r;
@@ -200,7 +206,7 @@ __global__ void __launch_bounds__(512) k_down(NodeMats<T> nm, int level, int L, 
     for (int e = tid; e < kc * r; e += nth) {
       const int c = e / r, i = e % r;
       const T* z2 = tb + c * r2 + r;
-      tb[c * r2 + i] = dot4(L22i + (int64_t)i * r + i, 1, z2 + i, r - i);
+      tb[c * r2 + i] = dot4(L22iT + i + (int64_t)i * r, r, z2 + i, r - i);
     }
     __syncthreads();
     for (int e = tid; e < kc * r; e += nth) {
@@ -219,7 +225,7 @@ __global__ void __launch_bounds__(512) k_down(NodeMats<T> nm, int level, int L, 
     for (int e = tid; e < kc * r; e += nth) {
       const int c = e / r, i = e % r;
       const T* zc = tb + c * r2;
-      const T acc = dot4(Ct + (int64_t)i * r, 1, zc, r) + dot4(L22 + i, r, zc + r, i + 1) - zc[r + i];
+      const T acc = dot4(CtT + i, r, zc, r) + dot4(L22 + i, r, zc + r, i + 1) - zc[r + i];
       VG[child(0, c, i)] = base[c * r2 + i];
       VG[child(1, c, i)] = base[c * r2 + r + i] + acc;
     }
@@ -320,8 +326,10 @@ static inline int64_t child_slot0(const Tree& t, int level) {
 
 template <typename T>
 void launch_up(const Tree& t, const NodeMatsH& h, int level, T* VP, T* VD, int k, int mode, cudaStream_t st) {
-  NodeMats<T> nm{reinterpret_cast<const T*>(h.Ct), reinterpret_cast<const T*>(h.L22),
-                 reinterpret_cast<const T*>(h.L22i), reinterpret_cast<const T*>(h.E), h.r};
+  NodeMats<T> nm{reinterpret_cast<const T*>(h.Ct),    reinterpret_cast<const T*>(h.L22),
+                 reinterpret_cast<const T*>(h.L22i),  reinterpret_cast<const T*>(h.E), h.r,
+                 reinterpret_cast<const T*>(h.CtT),   reinterpret_cast<const T*>(h.L22T),
+                 reinterpret_cast<const T*>(h.L22iT), reinterpret_cast<const T*>(h.ET)};
   int kcb, nth;
   sweep_shape(t.nodes_at(level), k, &kcb, &nth);
   dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + kcb - 1) / kcb));
@@ -334,8 +342,10 @@ void launch_up(const Tree& t, const NodeMatsH& h, int level, T* VP, T* VD, int k
 template <typename T>
 void launch_down(const Tree& t, const NodeMatsH& h, int level, const T* VP, T* VG, const T* VD, int k, int mode,
                  cudaStream_t st) {
-  NodeMats<T> nm{reinterpret_cast<const T*>(h.Ct), reinterpret_cast<const T*>(h.L22),
-                 reinterpret_cast<const T*>(h.L22i), reinterpret_cast<const T*>(h.E), h.r};
+  NodeMats<T> nm{reinterpret_cast<const T*>(h.Ct),    reinterpret_cast<const T*>(h.L22),
+                 reinterpret_cast<const T*>(h.L22i),  reinterpret_cast<const T*>(h.E), h.r,
+                 reinterpret_cast<const T*>(h.CtT),   reinterpret_cast<const T*>(h.L22T),
+                 reinterpret_cast<const T*>(h.L22iT), reinterpret_cast<const T*>(h.ET)};
   int kcb, nth;
   sweep_shape(t.nodes_at(level), k, &kcb, &nth);
   dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + kcb - 1) / kcb));

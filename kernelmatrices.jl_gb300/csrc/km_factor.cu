@@ -885,26 +885,37 @@ __device__ __forceinline__ T slot_get(const T (&x)[3], int s) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(512) k_node_finalize(const T* __restrict__ L22, const T* __restrict__ Eref,
-                                                       const T* __restrict__ Etau, int r, int64_t nbase, int with_e,
-                                                       T* __restrict__ L22i, T* __restrict__ Eexp) {
+__global__ void __launch_bounds__(512) k_node_finalize(const T* __restrict__ L22, const T* __restrict__ Ct,
+                                                       const T* __restrict__ Eref, const T* __restrict__ Etau, int r,
+                                                       int64_t nbase, int with_e, T* __restrict__ L22i,
+                                                       T* __restrict__ Eexp, T* __restrict__ CtT,
+                                                       T* __restrict__ L22T, T* __restrict__ L22iT,
+                                                       T* __restrict__ ET) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
   const int ld = r + 1;
   T* Ls = sm;               // L22
   T* Vs = Ls + r * ld;      // reflector bottoms
-  T* ts = Vs + r * ld;      // tau
+  T* Cs = Vs + r * ld;      // Ct
+  T* ts = Cs + r * ld;      // tau
   const int64_t node = nbase + blockIdx.x;
   const int64_t off = node * (int64_t)r * r;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
   for (int e = tid; e < r * r; e += blockDim.x) {
     const int i = e % r, c = e / r;
     Ls[i + c * ld] = L22[off + e];
+    Cs[i + c * ld] = Ct[off + e];
     if (with_e) Vs[i + c * ld] = Eref[off + e];
   }
   if (with_e)
     for (int e = tid; e < r; e += blockDim.x) ts[e] = Etau[node * (int64_t)r + e];
   __syncthreads();
+  // transposes of Ct and L22 for the sweeps
+  for (int e = tid; e < r * r; e += blockDim.x) {
+    const int i = e % r, c = e / r;
+    CtT[off + e] = Cs[c + i * ld];
+    L22T[off + e] = Ls[c + i * ld];
+  }
   // L22^{-1} e_c by forward substitution in column (axpy) order: row i accumulates
   // -L[i,p] x_p for p = c .. i-1 and is then divided by L[i,i]
   for (int c = w; c < r; c += nw) {
@@ -924,23 +935,33 @@ __global__ void __launch_bounds__(512) k_node_finalize(const T* __restrict__ L22
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
       const int i = lane + 32 * s;
-      if (i < r) out[i] = x[s];
+      if (i < r) {
+        out[i] = x[s];
+        L22iT[off + c + (int64_t)i * r] = x[s];
+      }
     }
   }
   if (!with_e) return;
   // column c of E: H_c ... H_0 applied in turn (j = c down to 0) to [e_c ; 0]; H_j acts on
   // top row j and the whole bottom, so top row j is final once H_j has acted
   T* Eo = Eexp + node * (int64_t)2 * r * r;
+  T* Et = ET + node * (int64_t)2 * r * r;  // r x 2r: element (c, l) at c + l*r
   for (int c = w; c < r; c += nw) {
     T* top = Eo + (int64_t)c * 2 * r;
     T* bot = top + r;
     T b[3] = {T(0.0), T(0.0), T(0.0)};
-    for (int i = c + 1 + lane; i < r; i += 32) top[i] = T(0.0);
+    for (int i = c + 1 + lane; i < r; i += 32) {
+      top[i] = T(0.0);
+      Et[c + (int64_t)i * r] = T(0.0);
+    }
     for (int j = c; j >= 0; --j) {
       const T tj = ts[j];
       const T tjtop = j == c ? T(1.0) : T(0.0);
       if (tj == 0.0) {
-        if (lane == 0) top[j] = tjtop;
+        if (lane == 0) {
+          top[j] = tjtop;
+          Et[c + (int64_t)j * r] = tjtop;
+        }
         continue;
       }
       T part = T(0.0);
@@ -950,7 +971,10 @@ __global__ void __launch_bounds__(512) k_node_finalize(const T* __restrict__ L22
         if (i < r) part += Vs[i + j * ld] * b[s];
       }
       const T acc = (tjtop + warp_sum_t(part)) * tj;
-      if (lane == 0) top[j] = tjtop - acc;
+      if (lane == 0) {
+        top[j] = tjtop - acc;
+        Et[c + (int64_t)j * r] = tjtop - acc;
+      }
 #pragma unroll
       for (int s = 0; s < 3; ++s) {
         const int i = lane + 32 * s;
@@ -960,7 +984,10 @@ __global__ void __launch_bounds__(512) k_node_finalize(const T* __restrict__ L22
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
       const int i = lane + 32 * s;
-      if (i < r) bot[i] = b[s];
+      if (i < r) {
+        bot[i] = b[s];
+        Et[c + (int64_t)(r + i) * r] = b[s];
+      }
     }
   }
 }
@@ -977,20 +1004,22 @@ void launch_leaf_formq(T* Pan, const T* tau, int r, const Tree& t, cudaStream_t 
 }
 
 template <typename T>
-void launch_node_finalize(const T* L22, const T* Eref, const T* Etau, int r, int level, const Tree& t, T* L22i,
-                          T* Eexp, cudaStream_t st) {
-  const size_t sm = ((size_t)2 * r * (r + 1) + r) * sizeof(T);
+void launch_node_finalize(const T* L22, const T* Ct, const T* Eref, const T* Etau, int r, int level, const Tree& t,
+                          T* L22i, T* Eexp, T* CtT, T* L22T, T* L22iT, T* ET, cudaStream_t st) {
+  const size_t sm = ((size_t)3 * r * (r + 1) + r) * sizeof(T);
   smem_limit((const void*)k_node_finalize<T>, sm);
-  k_node_finalize<T><<<(unsigned)t.nodes_at(level), 512, sm, st>>>(L22, Eref, Etau, r, t.node_off[level],
-                                                                   level < t.L ? 1 : 0, L22i, Eexp);
+  k_node_finalize<T><<<(unsigned)t.nodes_at(level), 512, sm, st>>>(L22, Ct, Eref, Etau, r, t.node_off[level],
+                                                                   level < t.L ? 1 : 0, L22i, Eexp, CtT, L22T,
+                                                                   L22iT, ET);
 }
 
 template void launch_leaf_formq<double>(double*, const double*, int, const Tree&, cudaStream_t);
 template void launch_leaf_formq<ff>(ff*, const ff*, int, const Tree&, cudaStream_t);
-template void launch_node_finalize<double>(const double*, const double*, const double*, int, int, const Tree&,
-                                           double*, double*, cudaStream_t);
-template void launch_node_finalize<ff>(const ff*, const ff*, const ff*, int, int, const Tree&, ff*, ff*,
-                                       cudaStream_t);
+template void launch_node_finalize<double>(const double*, const double*, const double*, const double*, int, int,
+                                           const Tree&, double*, double*, double*, double*, double*, double*,
+                                           cudaStream_t);
+template void launch_node_finalize<ff>(const ff*, const ff*, const ff*, const ff*, int, int, const Tree&, ff*, ff*,
+                                       ff*, ff*, ff*, ff*, cudaStream_t);
 
 template bool launch_leaf_chol<double>(const double*, double*, const Tree&, int*, cudaStream_t);
 template bool launch_leaf_chol<ff>(const double*, ff*, const Tree&, int*, cudaStream_t);

@@ -64,6 +64,11 @@ struct NodeMatsH {          // node factors (double or float pairs, by the calle
   const void* L22i;
   const void* E;           // explicit 2r x r transfer
   int r;
+  // transposed copies (r x r, r x 2r for E^T), so that every sweep product reads coalesced rows
+  const void* CtT = nullptr;
+  const void* L22T = nullptr;
+  const void* L22iT = nullptr;
+  const void* ET = nullptr;
 };
 
 // assembly
@@ -93,8 +98,8 @@ void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T
 template <typename T>
 void launch_leaf_formq(T* Pan, const T* tau, int r, const Tree& t, cudaStream_t st);
 template <typename T>
-void launch_node_finalize(const T* L22, const T* Eref, const T* Etau, int r, int level, const Tree& t, T* L22i,
-                          T* Eexp, cudaStream_t st);
+void launch_node_finalize(const T* L22, const T* Ct, const T* Eref, const T* Etau, int r, int level, const Tree& t,
+                          T* L22i, T* Eexp, T* CtT, T* L22T, T* L22iT, T* ET, cudaStream_t st);
 template <typename T>
 void launch_logdet(const T* Lf, const Tree& t, const T* L22, int r, double* partial, int np, double* out,
                    cudaStream_t st);
