@@ -397,23 +397,26 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
   // forms its reciprocal, so a step costs one barrier and no division on the other threads.
   if (tid == 0) {
     const T d = X3[0];
-    vc[0] = d > 0.0 ? T(1.0) / d : T(0.0);
+    vc[0] = d > 0.0 ? ff_recip(d) : T(0.0);
   }
   __syncthreads();
   int bad = 0;
   for (int j = 0; j < r; ++j) {
     if (!(X3[j + j * ld] > 0.0) && bad == 0) bad = j + 1;
     const T inv = vc[j];
-    // column c of the trailing matrix belongs to warp (c - j - 1) % nw; its rows c..r-1 live in
-    // the lanes of the chunks c/32 .. nch-1
-    for (int c = j + 1 + w; c < r; c += nw) {
+    // warp 0 owns column j+1 (the next pivot, on the critical path) and nothing else; column
+    // c >= j+2 belongs to warp 1 + (c - j - 2) % (nw - 1).  Rows c..r-1 of a column live in the
+    // lanes of the chunks c/32 .. nch-1.
+    const int cfirst = (w == 0) ? j + 1 : j + 1 + w;
+    const int cstep = (w == 0) ? r : nw - 1;
+    for (int c = cfirst; c < r; c += cstep) {
       const T f = X3[c + j * ld] * inv;
       for (int s = c >> 5; s < nch; ++s) {
         const int i = 32 * s + lane;
         if (i < r && i >= c) {
           const T v = X3[i + c * ld] - X3[i + j * ld] * f;
           X3[i + c * ld] = v;
-          if (i == c && c == j + 1) vc[c] = v > 0.0 ? T(1.0) / v : T(0.0);
+          if (i == c && c == j + 1) vc[c] = v > 0.0 ? ff_recip(v) : T(0.0);
         }
       }
       if (level < L)
@@ -429,7 +432,7 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
     const T d = X3[j + j * ld];
     const T sd = d > 0.0 ? sqrt(d) : T(1.0);
     va[j] = sd;
-    vb[j] = T(1.0) / sd;
+    vb[j] = ff_recip(sd);
   }
   __syncthreads();
   for (int c = w; c < r; c += nw) {
@@ -470,8 +473,8 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
     if (sig != 0.0) {
       const T nrm = sqrt(alpha * alpha + sig);
       beta = alpha >= 0.0 ? -nrm : nrm;
-      tj = (beta - alpha) / beta;
-      scal = T(1.0) / (alpha - beta);
+      tj = (beta - alpha) * ff_recip(beta);
+      scal = ff_recip(alpha - beta);
     }
     if (lane == 0) {
       va[j] = beta;

@@ -129,11 +129,20 @@ __device__ __forceinline__ ff sqrt(ff a) {
   if (!(a.hi > 0.f)) return ff(0.f, 0.f);
   const float s = sqrtf(a.hi);
   const ff r = a - ff(s, 0.f) * ff(s, 0.f);
-  const float c = __fdiv_rn(r.hi, __fmul_rn(2.f, s));
+  const float c = __fmul_rn(r.hi, __fmul_rn(0.5f, __frcp_rn(s)));  // (a - s^2) / (2 s)
   ff out;
   ff_fast_two_sum(s, c, out.hi, out.lo);
   return out;
 }
+
+// 1 / b: the rounded float reciprocal refined by one Newton step in float pairs,
+// y + y (1 - b y).  Shorter dependency chain than a / b, for pivots on a critical path.
+__device__ __forceinline__ ff ff_recip(ff b) {
+  const ff y(__frcp_rn(b.hi), 0.f);
+  const ff e = ff(1.0f, 0.f) - b * y;
+  return y + y * e;
+}
+__device__ __forceinline__ double ff_recip(double b) { return 1.0 / b; }
 
 __device__ __forceinline__ ff fabs(ff a) { return a.hi < 0.f ? -a : a; }
 
