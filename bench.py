@@ -282,11 +282,13 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                 t = float(tt.item())
             return t, st1.kernel_launches - st0.kernel_launches
 
-        for _ in range(args.warmup):
-            step_dev()
+        # clocks are sampled from the start of the warm-up through the end of the timed region
+        # (a 10-step timed region is shorter than two sampling periods)
         clocks = ClockSampler(dev) if sample_clocks else None
         if clocks:
             clocks.start()
+        for _ in range(args.warmup):
+            step_dev()
         ms, launches = timed(step_dev, args.steps)
         clk = clocks.stop() if clocks else None
         sol = d_sol.cpu().numpy().copy()
