@@ -20,7 +20,7 @@ using ::fmin;
 using ::log;
 using ::sqrt;
 
-struct ff {
+struct __align__(8) ff {  // 8-byte aligned: one 64-bit load or store per value
   float hi, lo;
   __host__ __device__ constexpr ff() : hi(0.f), lo(0.f) {}
   __host__ __device__ constexpr ff(float h, float l) : hi(h), lo(l) {}

@@ -64,6 +64,26 @@ __global__ void __launch_bounds__(256) k_leaf_dphiT(const T* __restrict__ Phi, c
       if (c < nc) VP[(leaf * k + c0 + c) * r2 + tid] = to_double(acc[c]);
 }
 
+// Eight consecutive values from 16-byte-aligned shared memory with four 16-byte loads.
+__device__ __forceinline__ void load8(const ff* p, ff (&v)[8]) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float4 f = q[k];
+    v[2 * k] = ff(f.x, f.y);
+    v[2 * k + 1] = ff(f.z, f.w);
+  }
+}
+__device__ __forceinline__ void load8(const double* p, double (&v)[8]) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double2 d = q[k];
+    v[2 * k] = d.x;
+    v[2 * k + 1] = d.y;
+  }
+}
+
 // y_leaf = dK_leaf x + dPhi beta1 + Phi beta2, beta1 = S^{-1} a, beta2 = S^{-1}(b - Sj beta1),
 // [a ; b] = VG[leaf][col], for a chunk of 8 columns.  The betas are solved in FP64 (one warp per
 // column), then x and the betas are staged in shared memory as T and each thread owns leaf rows
@@ -83,12 +103,12 @@ __global__ void __launch_bounds__(256) k_leaf_dnys_apply(const T* __restrict__ d
   const int c0 = blockIdx.y * 8;
   const int nc = min(8, k - c0);
   double* bd = reinterpret_cast<double*>(smraw);  // 8 x 3r : beta1 | beta2 | (spare), FP64
-  T* xs = reinterpret_cast<T*>(bd + 8 * 3 * r);   // 8 x m
-  T* bs = xs + 8 * m;                              // 8 x 2r : beta1 | beta2
+  T* xs = reinterpret_cast<T*>(bd + 8 * 3 * r);   // m x 8 (16-byte aligned)
+  T* bs = xs + 8 * m;                              // 2r x 8 : beta1 rows, then beta2 rows
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int e = threadIdx.x; e < 8 * m; e += blockDim.x) {
+  for (int e = threadIdx.x; e < 8 * m; e += blockDim.x) {  // row l of the chunk at xs[8 l]
     const int c = e / m, i = e % m;
-    xs[e] = c < nc ? from_double<T>(X[(int64_t)(c0 + c) * ldx + s + i]) : T(0.0);
+    xs[8 * i + c] = c < nc ? from_double<T>(X[(int64_t)(c0 + c) * ldx + s + i]) : T(0.0);
   }
   if (w < nc) {
     double* b1 = bd + w * 3 * r;
@@ -126,9 +146,9 @@ __global__ void __launch_bounds__(256) k_leaf_dnys_apply(const T* __restrict__ d
         __syncwarp();
       }
     }
-    for (int i = lane; i < 2 * r; i += 32) bs[w * 2 * r + i] = from_double<T>(b1[i]);
+    for (int i = lane; i < 2 * r; i += 32) bs[8 * i + w] = from_double<T>(b1[i]);  // row i at bs[8 i]
   } else if (w < 8) {
-    for (int i = lane; i < 2 * r; i += 32) bs[w * 2 * r + i] = T(0.0);
+    for (int i = lane; i < 2 * r; i += 32) bs[8 * i + w] = T(0.0);
   }
   __syncthreads();
   const T* K = dKl + d_leaf_koff(t, leaf);
@@ -140,40 +160,33 @@ __global__ void __launch_bounds__(256) k_leaf_dnys_apply(const T* __restrict__ d
     for (int c = 0; c < 8; ++c) acc[c] = T(0.0);
     // four matrix entries are loaded ahead of their multiply-adds so that the loads overlap
     int l = 0;
-    for (; l + 3 < m; l += 4) {
+    for (; l + 1 < m; l += 2) {
       const T a0 = K[i + (int64_t)l * m], a1 = K[i + (int64_t)(l + 1) * m];
-      const T a2 = K[i + (int64_t)(l + 2) * m], a3 = K[i + (int64_t)(l + 3) * m];
+      T x0[8], x1[8];
+      load8(xs + 8 * l, x0);
+      load8(xs + 8 * (l + 1), x1);
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        acc[c] += a0 * xs[c * m + l];
-        acc[c] += a1 * xs[c * m + l + 1];
-        acc[c] += a2 * xs[c * m + l + 2];
-        acc[c] += a3 * xs[c * m + l + 3];
+        acc[c] += a0 * x0[c];
+        acc[c] += a1 * x1[c];
       }
     }
     for (; l < m; ++l) {
       const T a = K[i + (int64_t)l * m];
+      T x0[8];
+      load8(xs + 8 * l, x0);
 #pragma unroll
-      for (int c = 0; c < 8; ++c) acc[c] += a * xs[c * m + l];
+      for (int c = 0; c < 8; ++c) acc[c] += a * x0[c];
     }
-    int q = 0;
-    for (; q + 1 < r; q += 2) {
-      const T dp0 = dP[i + (int64_t)q * m], p0 = P[i + (int64_t)q * m];
-      const T dp1 = dP[i + (int64_t)(q + 1) * m], p1 = P[i + (int64_t)(q + 1) * m];
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        acc[c] += dp0 * bs[c * 2 * r + q];
-        acc[c] += p0 * bs[c * 2 * r + r + q];
-        acc[c] += dp1 * bs[c * 2 * r + q + 1];
-        acc[c] += p1 * bs[c * 2 * r + r + q + 1];
-      }
-    }
-    for (; q < r; ++q) {
+    for (int q = 0; q < r; ++q) {
       const T dp = dP[i + (int64_t)q * m], p = P[i + (int64_t)q * m];
+      T b1v[8], b2v[8];
+      load8(bs + 8 * q, b1v);
+      load8(bs + 8 * (r + q), b2v);
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        acc[c] += dp * bs[c * 2 * r + q];
-        acc[c] += p * bs[c * 2 * r + r + q];
+        acc[c] += dp * b1v[c];
+        acc[c] += p * b2v[c];
       }
     }
 #pragma unroll
