@@ -134,6 +134,12 @@ struct km_handle {
   double* d_dK = nullptr;
   double* d_dPhi = nullptr;
   double* d_Sj = nullptr;
+  double* d_Sinv = nullptr;   // mixed form: explicit S^{-1} and S^{-1} Sj S^{-1} (FP64 + float pairs)
+  double* d_SinvF = nullptr;
+  double* d_M2 = nullptr;
+  double* d_M2F = nullptr;
+  double* d_Mtmp = nullptr;
+  double* d_GB = nullptr;     // mixed form: landmark coefficients of the leaf derivative products
   double* d_dKf = nullptr;    // float-pair copies (mixed form) of dK leaves, dPhi and Phi
   double* d_dPhif = nullptr;
   double* d_Phif = nullptr;
@@ -270,6 +276,7 @@ void free_problem(km_handle* h) {
   h->dk_param = -1;
   h->d_dK = h->d_dPhi = h->d_Sj = h->d_GP = h->d_GG = h->d_T = h->d_U = h->d_dots = nullptr;
   h->d_dKf = h->d_dPhif = h->d_Phif = nullptr;
+  h->d_Sinv = h->d_SinvF = h->d_M2 = h->d_M2F = h->d_Mtmp = h->d_GB = nullptr;
   h->gcap = h->tcap = 0;
   h->d_res = h->d_rdots = nullptr;
   h->rcap = 0;
@@ -661,11 +668,16 @@ int derivative_apply(km_handle* h, int j, const double* X, double* Y, int k) {
     if ((rc = grow(h, &h->d_dK, kbytes)) || (rc = grow(h, &h->d_dPhi, t.n * r)) || (rc = grow(h, &h->d_Sj, r * r)))
       return rc;
     if (h->mixed) {
-      // float-pair copies for the derivative products of the mixed form (FP32 pipe)
+      // float-pair copies for the derivative products of the mixed form (FP32 pipe), and the
+      // explicit S^{-1} = Sc^{-T} Sc^{-1} that replaces the per-column landmark solves
       if ((rc = grow(h, &h->d_dKf, kbytes)) || (rc = grow(h, &h->d_dPhif, t.n * r)) ||
-          (rc = grow(h, &h->d_Phif, t.n * r)))
+          (rc = grow(h, &h->d_Phif, t.n * r)) || (rc = grow(h, &h->d_Sinv, r * r)) ||
+          (rc = grow(h, &h->d_SinvF, r * r)) || (rc = grow(h, &h->d_M2, r * r)) || (rc = grow(h, &h->d_M2F, r * r)) ||
+          (rc = grow(h, &h->d_Mtmp, r * r)))
         return rc;
       KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Phif), t.n * r, st));
+      KLV(h, KM_PROF_OTHER, launch_small_gemm(h->d_SinvT, h->d_SinvT, r, 1, h->d_Sinv, st));
+      KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Sinv, P<ff>(h->d_SinvF), (int64_t)r * r, st));
     }
   }
   if (k > h->gcap) {
@@ -682,6 +694,10 @@ int derivative_apply(km_handle* h, int j, const double* X, double* Y, int k) {
     if (h->mixed) {
       KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_dK, P<ff>(h->d_dKf), kbytes, st));
       KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_dPhi, P<ff>(h->d_dPhif), t.n * r, st));
+      // M2 = S^{-1} Sj S^{-1}
+      KLV(h, KM_PROF_OTHER, launch_small_gemm(h->d_Sj, h->d_Sinv, r, 0, h->d_Mtmp, st));
+      KLV(h, KM_PROF_OTHER, launch_small_gemm(h->d_Sinv, h->d_Mtmp, r, 0, h->d_M2, st));
+      KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_M2, P<ff>(h->d_M2F), (int64_t)r * r, st));
     }
     h->dk_param = j;
   }
@@ -696,9 +712,14 @@ int derivative_apply(km_handle* h, int j, const double* X, double* Y, int k) {
   } else {
     KM_CUDA(h, cudaMemsetAsync(h->d_GG, 0, sizeof(double) * 2 * r * k, st));
   }
-  if (h->mixed)
+  if (h->mixed) {
+    if ((rc = grow(h, &h->d_GB, t.nleaf * 2 * r * k))) return rc;
+    KLV(h, KM_PROF_LEAF_APPLY, launch_dbeta<ff>(P<ff>(h->d_SinvF), P<ff>(h->d_M2F), r, h->d_GG, t.nleaf * (int64_t)k,
+                                                P<ff>(h->d_GB), st));
     KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dnys_apply<ff>(P<ff>(h->d_dKf), P<ff>(h->d_Phif), P<ff>(h->d_dPhif), h->d_Sc,
-                                                          h->d_Sj, r, t, X, t.n, h->d_GG, Y, t.n, k, st));
+                                                          h->d_Sj, r, t, X, t.n, h->d_GG, Y, t.n, k, st,
+                                                          P<ff>(h->d_GB)));
+  }
   else
     KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dnys_apply<double>(h->d_dK, h->d_Phi, h->d_dPhi, h->d_Sc, h->d_Sj, r, t, X,
                                                               t.n, h->d_GG, Y, t.n, k, st));
@@ -1641,6 +1662,7 @@ extern "C" int64_t km_estimate_bytes(int64_t n, int64_t rank, int level_kind, in
   b += 2 * d(slots * r * k) + d(nn * 2 * r * k);  // ensure_vec
   b += 2 * d(n * k);                              // ensure_xy
   if (with_grad)  // derivative workspaces, plus the float-pair copies the mixed form keeps
-    b += d(kb) + d(n * r) + d(r * r) + 2 * d(slots * 2 * r * k) + 2 * d(n * k) + d(k) + d(kb) + 2 * d(n * r);
+    b += d(kb) + d(n * r) + d(r * r) + 2 * d(slots * 2 * r * k) + 2 * d(n * k) + d(k) + d(kb) + 2 * d(n * r) +
+         5 * d(r * r) + d(t.nleaf * 2 * r * k);
   return b;
 }

@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) k_leaf_dnys_apply(const T* __restrict__ d
                                                          const double* __restrict__ Sj, int r, DTree t,
                                                          const double* __restrict__ X, int64_t ldx,
                                                          const double* __restrict__ VG, double* __restrict__ Y,
-                                                         int64_t ldy, int k) {
+                                                         int64_t ldy, int k, const T* __restrict__ betas) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int64_t leaf = blockIdx.x;
   const int m = d_leaf_size(t, leaf);
@@ -110,7 +110,12 @@ __global__ void __launch_bounds__(256) k_leaf_dnys_apply(const T* __restrict__ d
     const int c = e / m, i = e % m;
     xs[8 * i + c] = c < nc ? from_double<T>(X[(int64_t)(c0 + c) * ldx + s + i]) : T(0.0);
   }
-  if (w < nc) {
+  if (betas) {  // coefficients formed by k_dbeta
+    for (int e = threadIdx.x; e < 8 * 2 * r; e += blockDim.x) {
+      const int c = e / (2 * r), i = e % (2 * r);
+      bs[8 * i + c] = c < nc ? betas[(leaf * k + c0 + c) * 2 * r + i] : T(0.0);
+    }
+  } else if (w < nc) {
     double* b1 = bd + w * 3 * r;
     double* b2 = b1 + r;
     const double* g = VG + (leaf * k + c0 + w) * 2 * r;
@@ -195,6 +200,56 @@ __global__ void __launch_bounds__(256) k_leaf_dnys_apply(const T* __restrict__ d
   }
 }
 
+// C = A op(B) for r x r column-major FP64 matrices, op(B) = B or B'.  One CTA per column of C.
+__global__ void k_small_gemm(const double* __restrict__ A, const double* __restrict__ B, int r, int transB,
+                             double* __restrict__ Cm) {
+  const int j = blockIdx.x;
+  for (int i = threadIdx.x; i < r; i += blockDim.x) {
+    double acc = 0.0;
+    for (int l = 0; l < r; ++l) acc += A[i + (int64_t)l * r] * (transB ? B[j + (int64_t)l * r] : B[l + (int64_t)j * r]);
+    Cm[i + (int64_t)j * r] = acc;
+  }
+}
+
+// Landmark coefficients of the derivative products for every (leaf, column) pair p:
+//   beta1 = S^{-1} a,  beta2 = S^{-1} b - M2 a,  M2 = S^{-1} Sj S^{-1},  [a ; b] = VG[p],
+// the same quantities k_leaf_dnys_apply otherwise forms with triangular solves, here as
+// products with the explicit r x r operators (float pairs in the mixed form).  Each CTA takes
+// 8 pairs; thread q < 2r owns output row q.  Output: beta[p][0:r] = beta1, beta[p][r:2r] = beta2.
+template <typename T>
+__global__ void __launch_bounds__(256) k_dbeta(const T* __restrict__ Sinv, const T* __restrict__ M2, int r,
+                                               const double* __restrict__ VG, int64_t npairs, T* __restrict__ beta) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* g = reinterpret_cast<T*>(smraw);  // 8 x 2r
+  const int64_t p0 = (int64_t)blockIdx.x * 8;
+  const int np = (int)(npairs - p0 < 8 ? npairs - p0 : 8);
+  const int r2 = 2 * r;
+  for (int e = threadIdx.x; e < 8 * r2; e += blockDim.x)
+    g[e] = (e / r2) < np ? from_double<T>(VG[p0 * r2 + e]) : T(0.0);
+  __syncthreads();
+  const int q = threadIdx.x;
+  if (q >= r2) return;
+  const int qi = q < r ? q : q - r;
+  T acc[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) acc[c] = T(0.0);
+  const int boff = q < r ? 0 : r;  // S^{-1} applies to a (beta1) or to b (beta2)
+  for (int l = 0; l < r; ++l) {
+    const T sv = Sinv[qi + (int64_t)l * r];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[c] += sv * g[c * r2 + boff + l];
+  }
+  if (q >= r)
+    for (int l = 0; l < r; ++l) {
+      const T mv = M2[qi + (int64_t)l * r];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[c] -= mv * g[c * r2 + l];
+    }
+#pragma unroll
+  for (int c = 0; c < 8; ++c)
+    if (c < np) beta[(p0 + c) * r2 + q] = acc[c];
+}
+
 // out[c] = sum_i A[i + c*lda] * B[i + c*ldb], one CTA per column (deterministic order).
 __global__ void k_col_dots(const double* __restrict__ A, int64_t lda, const double* __restrict__ B, int64_t ldb,
                            int64_t n, double* __restrict__ out) {
@@ -257,11 +312,11 @@ void launch_leaf_dphiT(const T* Phi, const T* dPhi, int r, const Tree& t, const 
 template <typename T>
 void launch_leaf_dnys_apply(const T* dKl, const T* Phi, const T* dPhi, const double* Sc, const double* Sj, int r,
                             const Tree& t, const double* X, int64_t ldx, const double* VG, double* Y, int64_t ldy,
-                            int k, cudaStream_t st) {
+                            int k, cudaStream_t st, const T* betas) {
   dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
   const size_t sm = (size_t)8 * 3 * r * sizeof(double) + ((size_t)8 * t.max_leaf + 8 * 2 * r) * sizeof(T);
   smem_limit((const void*)k_leaf_dnys_apply<T>, sm);
-  k_leaf_dnys_apply<T><<<grid, 256, sm, st>>>(dKl, Phi, dPhi, Sc, Sj, r, dtree(t), X, ldx, VG, Y, ldy, k);
+  k_leaf_dnys_apply<T><<<grid, 256, sm, st>>>(dKl, Phi, dPhi, Sc, Sj, r, dtree(t), X, ldx, VG, Y, ldy, k, betas);
 }
 
 template void launch_leaf_dphiT<double>(const double*, const double*, int, const Tree&, const double*, int64_t,
@@ -270,10 +325,22 @@ template void launch_leaf_dphiT<ff>(const ff*, const ff*, int, const Tree&, cons
                                     cudaStream_t);
 template void launch_leaf_dnys_apply<double>(const double*, const double*, const double*, const double*,
                                              const double*, int, const Tree&, const double*, int64_t,
-                                             const double*, double*, int64_t, int, cudaStream_t);
+                                             const double*, double*, int64_t, int, cudaStream_t, const double*);
 template void launch_leaf_dnys_apply<ff>(const ff*, const ff*, const ff*, const double*, const double*, int,
                                          const Tree&, const double*, int64_t, const double*, double*, int64_t, int,
-                                         cudaStream_t);
+                                         cudaStream_t, const ff*);
+
+void launch_small_gemm(const double* A, const double* B, int r, int transB, double* C, cudaStream_t st) {
+  k_small_gemm<<<r, 128, 0, st>>>(A, B, r, transB, C);
+}
+
+template <typename T>
+void launch_dbeta(const T* Sinv, const T* M2, int r, const double* VG, int64_t npairs, T* beta, cudaStream_t st) {
+  if (npairs <= 0) return;
+  const size_t sm = (size_t)8 * 2 * r * sizeof(T);
+  k_dbeta<T><<<(unsigned)((npairs + 7) / 8), 256, sm, st>>>(Sinv, M2, r, VG, npairs, beta);
+}
+template void launch_dbeta<ff>(const ff*, const ff*, int, const double*, int64_t, ff*, cudaStream_t);
 
 void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n, int k,
                      double* out, cudaStream_t st) {

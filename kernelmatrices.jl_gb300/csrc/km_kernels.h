@@ -133,7 +133,12 @@ void launch_leaf_dphiT(const T* Phi, const T* dPhi, int r, const Tree& t, const 
 template <typename T>
 void launch_leaf_dnys_apply(const T* dKl, const T* Phi, const T* dPhi, const double* Sc, const double* Sj, int r,
                             const Tree& t, const double* X, int64_t ldx, const double* VG, double* Y, int64_t ldy,
-                            int k, cudaStream_t st);
+                            int k, cudaStream_t st, const T* betas = nullptr);
+// C = A op(B), r x r FP64 (op = transpose when transB)
+void launch_small_gemm(const double* A, const double* B, int r, int transB, double* C, cudaStream_t st);
+// landmark coefficients of the derivative products from explicit S^{-1} and S^{-1} Sj S^{-1}
+template <typename T>
+void launch_dbeta(const T* Sinv, const T* M2, int r, const double* VG, int64_t npairs, T* beta, cudaStream_t st);
 void launch_axpby(double* y, const double* x, double a, double b, int64_t n, cudaStream_t st);
 // n x p Rademacher probes (+-1), entry (i, j) from a SplitMix64 hash of (seed, j*n + i)
 void launch_rademacher(double* out, int64_t n, int64_t p, uint64_t seed, cudaStream_t st);

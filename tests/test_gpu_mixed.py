@@ -86,8 +86,9 @@ def test_mixed_gradient(lib):
 def test_mixed_kernel_entries(kid, params, lib):
     """The mixed form evaluates kernel entries in float pairs (own exp: Cody-Waite reduction +
     Taylor series).  Its pre-factor matvec (leaf blocks + Nystrom sums, FP64 arithmetic on the
-    float-pair-evaluated entries) and derivative products must match the FP64 form to 1e-13 /
-    1e-12 relative."""
+    float-pair-evaluated entries) must match the FP64 form to 1e-13 relative; its derivative
+    products (float pairs, landmark solves through the explicit S^{-1} and S^{-1} Sj S^{-1})
+    to 1e-10 relative."""
     import kmhodlr as K
     from kmhodlr.data import uniform_points
     n = 4096
@@ -99,4 +100,4 @@ def test_mixed_kernel_entries(kid, params, lib):
     x = np.random.default_rng(5).standard_normal((n, 3))
     assert rel(hmx @ x, h64 @ x) < 1e-13
     for j in range(3):
-        assert rel(hmx.derivative_matvec(j, x), h64.derivative_matvec(j, x)) < 1e-12
+        assert rel(hmx.derivative_matvec(j, x), h64.derivative_matvec(j, x)) < 1e-10
