@@ -1190,14 +1190,21 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   KM_CUDA(h, cudaMemcpyAsync(h->d_lndidx, idx.data(), sizeof(int64_t) * r, cudaMemcpyHostToDevice, st));
   KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + t.nnode + 1), st));
   KLV(h, KM_PROF_EVAL, launch_gather_points(h->d_pts, h->d_lndidx, r, h->d_lnd, st));
+  // S = K(P, P), its Cholesky factor and Sc^{-T} are single-CTA chains: they run on the side
+  // stream while the leaves and the landmark columns are evaluated on the main stream
+  side_begin(h);
+  launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, -1, h->d_S, r, h->side);
+  KM_CUDA(h, cudaMemcpyAsync(h->d_Sc, h->d_S, sizeof(double) * r * r, cudaMemcpyDeviceToDevice, h->side));
+  if (!launch_chol_small(h->d_Sc, r, h->d_info + t.nleaf + t.nnode, h->side)) {
+    side_end(h);
+    return fail(h, KM_ERR_UNSUPPORTED, "rank too large for the landmark Cholesky");
+  }
+  launch_tri_inv_t(h->d_Sc, r, h->d_SinvT, h->side);
+  launch_to_ff(h->d_SinvT, P<ff>(h->d_SinvTf), (int64_t)r * r, h->side);
+  h->stats.kernel_launches += 4;
   KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st, h->mixed));
   KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, -1, h->d_Phi, st, h->mixed));
-  KLV(h, KM_PROF_EVAL, launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, -1, h->d_S, r, st));
-  KM_CUDA(h, cudaMemcpyAsync(h->d_Sc, h->d_S, sizeof(double) * r * r, cudaMemcpyDeviceToDevice, st));
-  if (!KL(h, KM_PROF_OTHER, launch_chol_small(h->d_Sc, r, h->d_info + t.nleaf + t.nnode, st)))
-    return fail(h, KM_ERR_UNSUPPORTED, "rank too large for the landmark Cholesky");
-  KLV(h, KM_PROF_OTHER, launch_tri_inv_t(h->d_Sc, r, h->d_SinvT, st));
-  KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_SinvT, P<ff>(h->d_SinvTf), (int64_t)r * r, st));
+  side_end(h);
   if ((rc = check_launch(h, "assemble")) != KM_OK) return rc;
   h->stats.assemble_ms = timer_stop(h);
   if ((rc = sync(h, "assemble")) != KM_OK) return rc;
