@@ -1303,8 +1303,10 @@ int km_factorize(km_handle* h) {
     std::vector<int> info(t.nnode);
     if (t.nnode > 0)
       KM_CUDA(h, cudaMemcpy(info.data(), h->d_info + t.nleaf, sizeof(int) * t.nnode, cudaMemcpyDeviceToHost));
-    for (int64_t i = 0; i < t.nnode && rc == KM_OK; ++i)
+    for (int64_t i = 0; i < t.nnode && rc == KM_OK; ++i) {
+      if (info[i] < 0) return fail(h, KM_ERR_TIMEOUT, "a bounded wait inside the node factorisation ran out");
       if (info[i]) rc = fail(h, KM_ERR_NOT_SPD, "PosDefException: a low-rank capacitance block is not positive definite");
+    }
   }
   if (rc == KM_ERR_NOT_SPD && h->mixed) {
     // A pivot that is positive in FP64 can round to <= 0 in float pairs when the capacitance

@@ -284,6 +284,10 @@ __global__ void __launch_bounds__(256) k_leaf_formq(T* __restrict__ Pan, const T
 // norm of the next reflector itself, so the QR needs one barrier per reflector.
 // Shared memory: four r x (r+1) matrices and two r-vectors.
 // ---------------------------------------------------------------------------------------------
+// Iteration bound of a spin wait on a shared-memory flag (with 20 ns sleeps: well above any
+// legitimate wait inside one node, far below a watchdog).
+constexpr int kWaitLimit = 1 << 22;
+
 template <typename T>
 __device__ __forceinline__ T sel(bool p, T a) {
   return p ? a : T(0.0);
@@ -304,7 +308,8 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
   T* X3 = X2 + r * ld;
   T* va = X3 + r * ld;  // r values: sqrt(d_j), then the reflector betas
   T* vb = va + r;       // r values: 1 / L22[j][j], then the reflector scales
-  T* vc = vb + r;       // r values: 1 / d_j during the Cholesky, then the reflector taus
+  T* vc = vb + r;       // r values: the reflector taus
+  int* flags = reinterpret_cast<int*>(vc + r);  // r + 1 ints: column published / first bad pivot
   const int64_t k = blockIdx.x;
   const int64_t node = nbase + k;  // node index within all nodes (level-major)
   const T* R1 = R + (cbase + 2 * k) * (int64_t)r * r;
@@ -312,6 +317,7 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
   const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
   const int nch = (r + 31) >> 5;   // 32-row chunks per column (r <= 96)
   const int nitems = r * nch;
+  for (int e = tid; e <= r; e += nth) flags[e] = (e < r) ? 0 : r + 1;
   // load: X0 = Sc^{-T} (upper), X1 = R1, X2 = R2   (element (i,c) at i + c*ld)
   for (int c = w; c < r; c += nw)
     for (int i = lane; i < r; i += 32) {
@@ -391,56 +397,77 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       if (i < r) X2[i + c * ld] -= a0 + a1;
     }
   __syncthreads();
-  // L22 = chol(H): unscaled right-looking elimination, a_ik -= a_ij a_kj / d_j, with the forward
-  // substitution L22^{-1} B carried along on the rows of B (b_c -= (a_cj / d_j) b_j; row j is
-  // scaled by 1/sqrt(d_j) afterwards).  The thread that updates the next diagonal entry also
-  // forms its reciprocal, so a step costs one barrier and no division on the other threads.
-  if (tid == 0) {
-    const T d = X3[0];
-    vc[0] = d > 0.0 ? ff_recip(d) : T(0.0);
-  }
-  __syncthreads();
+  // L22 = chol(H) by columns in dataflow order, with the forward substitution L22^{-1} B carried
+  // on the rows of B.  Warp w owns columns w, w + nw, ... and finishes them in increasing order:
+  // column c (and row c of B) accumulates the contributions of columns k < c as soon as each is
+  // published (flag[k] set after its values are in shared memory), then takes its pivot and
+  // publishes itself.  No block barrier inside the loop: the critical path is one update plus
+  // one pivot per column.  Waits are bounded; a wait that runs out marks the node with
+  // info = -1 (reported as a timeout) and the kernel carries on.
   int bad = 0;
-  for (int j = 0; j < r; ++j) {
-    if (!(X3[j + j * ld] > 0.0) && bad == 0) bad = j + 1;
-    const T inv = vc[j];
-    // warp 0 owns column j+1 (the next pivot, on the critical path) and nothing else; column
-    // c >= j+2 belongs to warp 1 + (c - j - 2) % (nw - 1).  Rows c..r-1 of a column live in the
-    // lanes of the chunks c/32 .. nch-1.
-    const int cfirst = (w == 0) ? j + 1 : j + 1 + w;
-    const int cstep = (w == 0) ? r : nw - 1;
-    for (int c = cfirst; c < r; c += cstep) {
-      const T f = X3[c + j * ld] * inv;
-      for (int s = c >> 5; s < nch; ++s) {
+  {
+    volatile int* vflag = flags;
+    int known = 0;          // columns 0 .. known-1 are published (as seen by this warp)
+    bool timed_out = false;  // after one expired wait this warp stops waiting
+    for (int c = w; c < r; c += nw) {
+      T v[3], b[3];
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
         const int i = 32 * s + lane;
-        if (i < r && i >= c) {
-          const T v = X3[i + c * ld] - X3[i + j * ld] * f;
-          X3[i + c * ld] = v;
-          if (i == c && c == j + 1) vc[c] = v > 0.0 ? ff_recip(v) : T(0.0);
-        }
+        v[s] = (i >= c && i < r) ? X3[i + c * ld] : T(0.0);
+        b[s] = (level < L && i < r) ? X2[c + i * ld] : T(0.0);
       }
-      if (level < L)
-        for (int s = 0; s < nch; ++s) {
-          const int kk = 32 * s + lane;
-          if (kk < r) X2[c + kk * ld] -= f * X2[j + kk * ld];
+      for (int k = 0; k < c; ++k) {
+        if (k >= known && !timed_out) {
+          int spins = 0;
+          while (vflag[k] == 0) {
+            if (++spins > kWaitLimit) {
+              if (lane == 0) info[node] = -1;
+              timed_out = true;
+              break;
+            }
+            __nanosleep(20);
+          }
+          __threadfence_block();
+          known = k + 1;
+          while (known < c && vflag[known] != 0) ++known;
+          __threadfence_block();
         }
+        const T lck = X3[c + k * ld];
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+          if (32 * s + 31 < c) continue;
+          const int i = 32 * s + lane;
+          if (i >= c && i < r) v[s] -= X3[i + k * ld] * lck;
+        }
+        if (level < L)
+#pragma unroll
+          for (int s = 0; s < 3; ++s) {
+            const int kk = 32 * s + lane;
+            if (kk < r) b[s] -= lck * X2[k + kk * ld];
+          }
+      }
+      const int cs = c >> 5;
+      const T d = shfl_idx(cs == 0 ? v[0] : (cs == 1 ? v[1] : v[2]), c & 31);
+      if (!(d > 0.0) && bad == 0) bad = c + 1;
+      const T sd = d > 0.0 ? sqrt(d) : T(1.0);
+      const T inv = ff_recip(sd);
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        const int i = 32 * s + lane;
+        if (i == c) X3[i + c * ld] = sd;
+        else if (i > c && i < r) X3[i + c * ld] = v[s] * inv;
+        if (level < L && i < r) X2[c + i * ld] = b[s] * inv;  // row c of L22^{-1} B
+      }
+      __threadfence_block();
+      __syncwarp();
+      if (lane == 0) vflag[c] = 1;
     }
-    __syncthreads();
   }
-  if (tid == 0 && bad) info[node] = bad;
-  for (int j = tid; j < r; j += nth) {
-    const T d = X3[j + j * ld];
-    const T sd = d > 0.0 ? sqrt(d) : T(1.0);
-    va[j] = sd;
-    vb[j] = ff_recip(sd);
-  }
+  // a warp's first non-positive pivot; the smallest over the warps is written below
+  if (lane == 0 && bad) atomicMin(flags + r, bad);
   __syncthreads();
-  for (int c = w; c < r; c += nw) {
-    for (int i = c + lane; i < r; i += 32) X3[i + c * ld] = (i == c) ? va[c] : X3[i + c * ld] * vb[c];
-    if (level < L)
-      for (int k = lane; k < r; k += 32) X2[c + k * ld] = X2[c + k * ld] * vb[c];  // row c of L22^{-1} B
-  }
-  __syncthreads();
+  if (tid == 0 && flags[r] < r + 1 && info[node] == 0) info[node] = flags[r];
   // store Ct and L22
   for (int c = w; c < r; c += nw)
     for (int i = lane; i < r; i += 32) {
@@ -844,7 +871,7 @@ void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T
         reinterpret_cast<double*>(Ct), reinterpret_cast<double*>(L22), reinterpret_cast<double*>(Eref),
         reinterpret_cast<double*>(Etau), info);
   } else {
-    const size_t sm = ((size_t)4 * r * (r + 1) + 3 * r) * sizeof(T);
+    const size_t sm = ((size_t)4 * r * (r + 1) + 3 * r) * sizeof(T) + (size_t)(r + 1) * sizeof(int);
     smem_limit((const void*)k_node_factor<T>, sm);
     k_node_factor<T><<<(unsigned)t.nodes_at(level), 1024, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase,
                                                                    nbase, Ct, L22, Eref, Etau, info);
