@@ -284,8 +284,9 @@ __global__ void __launch_bounds__(256) k_leaf_formq(T* __restrict__ Pan, const T
 // norm of the next reflector itself, so the QR needs one barrier per reflector.
 // Shared memory: four r x (r+1) matrices and two r-vectors.
 // ---------------------------------------------------------------------------------------------
-// Iteration bound of a spin wait on a shared-memory flag (with 20 ns sleeps: well above any
-// legitimate wait inside one node, far below a watchdog).
+// Iteration bound of a spin wait on a shared-memory flag (a few tens of cycles per iteration:
+// well above any legitimate wait inside one node, far below a watchdog).  The spin does not
+// sleep: a sleeping waiter wakes too late for the column-to-column handoff.
 constexpr int kWaitLimit = 1 << 22;
 
 template <typename T>
@@ -426,7 +427,6 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
               timed_out = true;
               break;
             }
-            __nanosleep(20);
           }
           __threadfence_block();
           known = k + 1;

@@ -125,20 +125,24 @@ __device__ __forceinline__ bool operator==(ff a, double b) {
 }
 __device__ __forceinline__ bool operator!=(ff a, double b) { return !(a == b); }
 
+// sqrt(a): the fast approximate float square root (s = a.hi rsqrt(a.hi)) corrected by one
+// Newton step in float pairs, s + (a - s^2) / (2 s); relative error about 1e-13.
 __device__ __forceinline__ ff sqrt(ff a) {
   if (!(a.hi > 0.f)) return ff(0.f, 0.f);
-  const float s = sqrtf(a.hi);
+  const float rs = rsqrtf(a.hi);
+  const float s = __fmul_rn(a.hi, rs);
   const ff r = a - ff(s, 0.f) * ff(s, 0.f);
-  const float c = __fmul_rn(r.hi, __fmul_rn(0.5f, __frcp_rn(s)));  // (a - s^2) / (2 s)
+  const float c = __fmul_rn(r.hi, __fmul_rn(0.5f, rs));  // (a - s^2) / (2 s), 1/s ~ rsqrt(a)
   ff out;
   ff_fast_two_sum(s, c, out.hi, out.lo);
   return out;
 }
 
-// 1 / b: the rounded float reciprocal refined by one Newton step in float pairs,
-// y + y (1 - b y).  Shorter dependency chain than a / b, for pivots on a critical path.
+// 1 / b: the fast approximate float reciprocal refined by one Newton step in float pairs,
+// y + y (1 - b y) (relative error about 1e-13).  A much shorter dependency chain than a / b,
+// for pivots on a critical path.
 __device__ __forceinline__ ff ff_recip(ff b) {
-  const ff y(__frcp_rn(b.hi), 0.f);
+  const ff y(__fdividef(1.0f, b.hi), 0.f);
   const ff e = ff(1.0f, 0.f) - b * y;
   return y + y * e;
 }
