@@ -270,82 +270,218 @@ __global__ void __launch_bounds__(1024) k_aca(const double* __restrict__ pts, KP
 }
 
 // ---------------------------------------------------------------------------------------------
-// Householder QR with explicit Q (LAPACK dgeqr2 + dorg2r), one CTA per panel, in place.
-// The panel becomes Q (m x k); R (k x k, zeros below the diagonal) goes to Rout.
+// Householder QR with explicit Q of one panel per CTA, blocked (LAPACK dgeqrf / dorgqr
+// structure: reflectors of kQB columns are formed by the unblocked dgeqr2 / dlarfg rules and
+// applied to the rest of the panel as one compact-WY block reflector I - V T V').  The trailing
+// columns are then read and written once per block instead of once per reflector.  V is staged
+// in shared memory kQC rows at a time; trailing columns are processed kQT at a time.
 // ---------------------------------------------------------------------------------------------
+constexpr int kQB = 16;
+constexpr int kQC = 256;
+constexpr int kQT = 256;
+constexpr int kQV = kQB + 1;  // row stride of the staged V chunk (conflict-free column reads)
+
+// T (kQB x kQB, upper, column-major) of the block reflector of columns j0 .. j0+jb-1:
+//   T[q][q] = tau_q,  T[0:q, q] = -tau_q T[0:q, 0:q] (V[:, 0:q]' v_q)
+// with v_p = e_p + A[p+1:, p] (zero above row p).  G holds the dots v_p . v_q.
+__device__ void panel_block_T(const double* A, int64_t m, int64_t lda, int j0, int jb, const double* tau,
+                              double* G, double* Tm) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int pq = w; pq < jb * jb; pq += nw) {
+    const int p = pq % jb, q = pq / jb;
+    if (p >= q) continue;
+    const double* vp = A + (int64_t)(j0 + p) * lda;
+    const double* vq = A + (int64_t)(j0 + q) * lda;
+    // v_p[j0+q] * 1 + sum_{i > j0+q} v_p[i] v_q[i]
+    double acc = 0.0;
+    for (int64_t i = j0 + q + 1 + lane; i < m; i += 32) acc += vp[i] * vq[i];
+    acc = warp_sum(acc);
+    if (lane == 0) G[p + q * kQB] = acc + vp[j0 + q];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < jb; ++q) {
+      const double tq = tau[j0 + q];
+      for (int p = 0; p < q; ++p) {
+        double z = 0.0;
+        for (int l = p; l < q; ++l) z += Tm[p + l * kQB] * G[l + q * kQB];
+        Tm[p + q * kQB] = -tq * z;
+      }
+      Tm[q + q * kQB] = tq;
+      for (int p = q + 1; p < kQB; ++p) Tm[p + q * kQB] = 0.0;
+    }
+  }
+  __syncthreads();
+}
+
+// C[:, c0:c1] <- (I - V op(T) V') C[:, c0:c1] over rows j0 .. m-1, op(T) = T' (QR, transT = 1)
+// or T (forming Q, transT = 0); V = the block's reflectors (columns j0 .. j0+jb-1 of A).
+__device__ void panel_apply_block(double* A, int64_t m, int64_t lda, int j0, int jb, int c0, int c1,
+                                  const double* Tm, int transT, double* W, double* W2, double* Vc) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
+  for (int t0 = c0; t0 < c1; t0 += kQT) {
+    const int nt = min(kQT, c1 - t0);
+    for (int e = tid; e < kQB * nt; e += blockDim.x) W[e] = 0.0;
+    __syncthreads();
+    // W = V' C  (rows from j0 on, chunked)
+    for (int64_t r0 = j0; r0 < m; r0 += kQC) {
+      const int rows = (int)(m - r0 < kQC ? m - r0 : kQC);
+      for (int e = tid; e < rows * kQB; e += blockDim.x) {
+        const int ii = e % rows, p = e / rows;  // consecutive threads: consecutive rows of a column
+        const int64_t i = r0 + ii, ip = j0 + p;
+        double v = 0.0;
+        if (p < jb) v = (i == ip) ? 1.0 : (i > ip ? A[(int64_t)(j0 + p) * lda + i] : 0.0);
+        Vc[ii * kQV + p] = v;
+      }
+      __syncthreads();
+      for (int c = w; c < nt; c += nw) {
+        const double* col = A + (int64_t)(t0 + c) * lda + r0;
+        double acc[kQB];
+#pragma unroll
+        for (int p = 0; p < kQB; ++p) acc[p] = 0.0;
+        for (int ii = lane; ii < rows; ii += 32) {
+          const double x = col[ii];
+#pragma unroll
+          for (int p = 0; p < kQB; ++p) acc[p] += Vc[ii * kQV + p] * x;
+        }
+#pragma unroll
+        for (int p = 0; p < kQB; ++p) {
+          const double sum = warp_sum(acc[p]);
+          if (lane == 0) W[p + c * kQB] += sum;
+        }
+      }
+      __syncthreads();
+    }
+    // W2 = op(T) W
+    for (int e = tid; e < kQB * nt; e += blockDim.x) {
+      const int q = e % kQB, c = e / kQB;
+      double z = 0.0;
+      if (transT) {
+        for (int p = 0; p <= q; ++p) z += Tm[p + q * kQB] * W[p + c * kQB];
+      } else {
+        for (int p = q; p < kQB; ++p) z += Tm[q + p * kQB] * W[p + c * kQB];
+      }
+      W2[e] = z;
+    }
+    __syncthreads();
+    // C -= V W2
+    for (int64_t r0 = j0; r0 < m; r0 += kQC) {
+      const int rows = (int)(m - r0 < kQC ? m - r0 : kQC);
+      for (int e = tid; e < rows * kQB; e += blockDim.x) {
+        const int ii = e % rows, p = e / rows;  // consecutive threads: consecutive rows of a column
+        const int64_t i = r0 + ii, ip = j0 + p;
+        double v = 0.0;
+        if (p < jb) v = (i == ip) ? 1.0 : (i > ip ? A[(int64_t)(j0 + p) * lda + i] : 0.0);
+        Vc[ii * kQV + p] = v;
+      }
+      __syncthreads();
+      for (int c = w; c < nt; c += nw) {
+        double* col = A + (int64_t)(t0 + c) * lda + r0;
+        const double* wc = W2 + c * kQB;
+        for (int ii = lane; ii < rows; ii += 32) {
+          double z = 0.0;
+#pragma unroll
+          for (int p = 0; p < kQB; ++p) z += Vc[ii * kQV + p] * wc[p];
+          col[ii] -= z;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 __global__ void __launch_bounds__(512) k_panel_qr(const PanelDesc* __restrict__ descs) {
-  extern __shared__ double tau[];  // k
-  __shared__ double red[20];
+  extern __shared__ double sm[];
+  __shared__ double red[40];
   __shared__ double sh[2];
   const PanelDesc D = descs[blockIdx.x];
   double* A = D.A;
   const int64_t m = D.m, lda = D.lda;
   const int k = D.k;
+  double* tau = sm;                 // k
+  double* Tm = tau + k;             // kQB x kQB
+  double* G = Tm + kQB * kQB;       // kQB x kQB
+  double* W = G + kQB * kQB;        // kQB x kQT
+  double* W2 = W + kQB * kQT;       // kQB x kQT
+  double* Vc = W2 + kQB * kQT;      // kQC x kQV
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
-  for (int j = 0; j < k; ++j) {
-    double* aj = A + (int64_t)j * lda;
-    double part = 0.0;
-    for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) part += aj[i] * aj[i];
-    part = warp_sum(part);
-    if (lane == 0) red[w] = part;
-    __syncthreads();
-    if (tid == 0) {
-      double sig = 0.0;
-      for (int q = 0; q < nw; ++q) sig += red[q];
-      const double alpha = aj[j];
-      double tj = 0.0, beta = alpha, scal = 0.0;
-      if (sig != 0.0) {
-        const double nrm = sqrt(alpha * alpha + sig);
-        beta = alpha >= 0.0 ? -nrm : nrm;
-        tj = (beta - alpha) / beta;
-        scal = 1.0 / (alpha - beta);
+  for (int j0 = 0; j0 < k; j0 += kQB) {
+    const int jb = min(kQB, k - j0);
+    // unblocked dgeqr2 on the block's columns (dlarfg: beta = -sign(alpha) ||.||)
+    for (int j = j0; j < j0 + jb; ++j) {
+      double* aj = A + (int64_t)j * lda;
+      double part = 0.0;
+      for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) part += aj[i] * aj[i];
+      const double sig = cta_sum(part, red);
+      if (tid == 0) {
+        const double alpha = aj[j];
+        double tj = 0.0, beta = alpha, scal = 0.0;
+        if (sig != 0.0) {
+          const double nrm = sqrt(alpha * alpha + sig);
+          beta = alpha >= 0.0 ? -nrm : nrm;
+          tj = (beta - alpha) / beta;
+          scal = 1.0 / (alpha - beta);
+        }
+        aj[j] = beta;
+        sh[0] = scal;
+        sh[1] = tj;
+        tau[j] = tj;
       }
-      aj[j] = beta;
-      sh[0] = scal;
-      sh[1] = tj;
-      tau[j] = tj;
-    }
-    __syncthreads();
-    const double scal = sh[0], tj = sh[1];
-    for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= scal;
-    __syncthreads();
-    if (tj != 0.0) {
-      for (int c = j + 1 + w; c < k; c += nw) {
-        double* ac = A + (int64_t)c * lda;
-        double acc = (lane == 0) ? ac[j] : 0.0;
-        for (int64_t i = j + 1 + lane; i < m; i += 32) acc += aj[i] * ac[i];
-        acc = warp_sum(acc) * tj;
-        if (lane == 0) ac[j] -= acc;
-        for (int64_t i = j + 1 + lane; i < m; i += 32) ac[i] -= acc * aj[i];
+      __syncthreads();
+      const double scal = sh[0], tj = sh[1];
+      for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= scal;
+      __syncthreads();
+      if (tj != 0.0) {
+        for (int c = j + 1 + w; c < j0 + jb; c += nw) {
+          double* ac = A + (int64_t)c * lda;
+          double acc = (lane == 0) ? ac[j] : 0.0;
+          for (int64_t i = j + 1 + lane; i < m; i += 32) acc += aj[i] * ac[i];
+          acc = warp_sum(acc) * tj;
+          if (lane == 0) ac[j] -= acc;
+          for (int64_t i = j + 1 + lane; i < m; i += 32) ac[i] -= acc * aj[i];
+        }
       }
+      __syncthreads();
     }
-    __syncthreads();
+    if (j0 + jb < k) {
+      panel_block_T(A, m, lda, j0, jb, tau, G, Tm);
+      panel_apply_block(A, m, lda, j0, jb, j0 + jb, k, Tm, 1, W, W2, Vc);
+    }
   }
   for (int e = tid; e < k * k; e += blockDim.x) {
     const int i = e % k, c = e / k;
     D.R[e] = (i <= c) ? A[(int64_t)c * lda + i] : 0.0;
   }
   __syncthreads();
-  // explicit Q (dorg2r)
-  for (int j = k - 1; j >= 0; --j) {
-    double* aj = A + (int64_t)j * lda;
-    const double tj = tau[j];
-    if (j < k - 1) {
-      if (tid == 0) aj[j] = 1.0;
-      __syncthreads();
-      for (int c = j + 1 + w; c < k; c += nw) {
-        double* ac = A + (int64_t)c * lda;
-        double acc = 0.0;
-        for (int64_t i = j + lane; i < m; i += 32) acc += aj[i] * ac[i];
-        acc = warp_sum(acc) * tj;
-        for (int64_t i = j + lane; i < m; i += 32) ac[i] -= acc * aj[i];
+  // explicit Q (dorgqr): blocks from the last to the first; a block first applies its block
+  // reflector to the columns already formed to its right, then forms its own columns (dorg2r)
+  const int nblk = (k + kQB - 1) / kQB;
+  for (int bq = nblk - 1; bq >= 0; --bq) {
+    const int j0 = bq * kQB, jb = min(kQB, k - j0), j1 = j0 + jb;
+    if (j1 < k) {
+      panel_block_T(A, m, lda, j0, jb, tau, G, Tm);
+      panel_apply_block(A, m, lda, j0, jb, j1, k, Tm, 0, W, W2, Vc);
+    }
+    for (int j = j1 - 1; j >= j0; --j) {
+      double* aj = A + (int64_t)j * lda;
+      const double tj = tau[j];
+      if (j < j1 - 1) {
+        if (tid == 0) aj[j] = 1.0;
+        __syncthreads();
+        for (int c = j + 1 + w; c < j1; c += nw) {
+          double* ac = A + (int64_t)c * lda;
+          double acc = 0.0;
+          for (int64_t i = j + lane; i < m; i += 32) acc += aj[i] * ac[i];
+          acc = warp_sum(acc) * tj;
+          for (int64_t i = j + lane; i < m; i += 32) ac[i] -= acc * aj[i];
+        }
+        __syncthreads();
       }
+      for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= -tj;
+      for (int64_t i = tid; i < j; i += blockDim.x) aj[i] = 0.0;
+      if (tid == 0) aj[j] = 1.0 - tj;
       __syncthreads();
     }
-    for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= -tj;
-    for (int64_t i = tid; i < j; i += blockDim.x) aj[i] = 0.0;
-    if (tid == 0) aj[j] = 1.0 - tj;
-    __syncthreads();
   }
 }
 
@@ -575,7 +711,8 @@ void launch_aca(const double* pts, KParams kp, const AcaBlock* blocks, int nbloc
 }
 
 void launch_panel_qr(const PanelDesc* descs, int n, int maxk, cudaStream_t st) {
-  const size_t sm = (size_t)std::max(maxk, 1) * sizeof(double);
+  const size_t sm = ((size_t)std::max(maxk, 1) + 2 * kQB * kQB + 2 * kQB * kQT + kQC * kQV) * sizeof(double);
+  smem_limit((const void*)k_panel_qr, sm);
   k_panel_qr<<<n, 512, sm, st>>>(descs);
 }
 
