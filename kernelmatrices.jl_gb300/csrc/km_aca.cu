@@ -317,10 +317,10 @@ __device__ void panel_block_T(const double* A, int64_t m, int64_t lda, int j0, i
 // C[:, c0:c1] <- (I - V op(T) V') C[:, c0:c1] over rows j0 .. m-1, op(T) = T' (QR, transT = 1)
 // or T (forming Q, transT = 0); V = the block's reflectors (columns j0 .. j0+jb-1 of A).
 __device__ void panel_apply_block(double* A, int64_t m, int64_t lda, int j0, int jb, int c0, int c1,
-                                  const double* Tm, int transT, double* W, double* W2, double* Vc) {
+                                  const double* Tm, int transT, double* W, double* W2, double* Vc, int wcap) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
-  for (int t0 = c0; t0 < c1; t0 += kQT) {
-    const int nt = min(kQT, c1 - t0);
+  for (int t0 = c0; t0 < c1; t0 += wcap) {
+    const int nt = min(wcap, c1 - t0);
     for (int e = tid; e < kQB * nt; e += blockDim.x) W[e] = 0.0;
     __syncthreads();
     // W = V' C  (rows from j0 on, chunked)
@@ -390,98 +390,132 @@ __device__ void panel_apply_block(double* A, int64_t m, int64_t lda, int j0, int
   }
 }
 
-__global__ void __launch_bounds__(512) k_panel_qr(const PanelDesc* __restrict__ descs) {
-  extern __shared__ double sm[];
+// The panel QR of a level runs as a sequence of launches per reflector block, so that the
+// trailing updates of a tall panel spread over many CTAs (one FP64-bound SM per panel took
+// seconds for the 32768 x 549 panels of an n = 2^16 ACA matrix):
+//   k_pq_factor  (one CTA per panel)        dgeqr2 on the block's kQB columns, its T
+//   k_pq_update  (panels x column tiles)    block reflector applied to kQU trailing columns each
+//   k_pq_rout    (one CTA per panel)        R out
+//   then, blocks from last to first: k_pq_update on the formed columns, k_pq_form (dorg2r on
+//   the block's own columns).  tau and the T factors live in global scratch between launches.
+constexpr int kQU = 32;  // trailing columns per update CTA
+
+__global__ void __launch_bounds__(512) k_pq_factor(const PanelDesc* __restrict__ descs, int j0,
+                                                   double* __restrict__ taus, int ldtau, double* __restrict__ Ts,
+                                                   int nblk) {
   __shared__ double red[40];
   __shared__ double sh[2];
+  __shared__ double G[kQB * kQB], Tm[kQB * kQB];
   const PanelDesc D = descs[blockIdx.x];
+  const int k = D.k;
+  if (j0 >= k) return;
   double* A = D.A;
   const int64_t m = D.m, lda = D.lda;
-  const int k = D.k;
-  double* tau = sm;                 // k
-  double* Tm = tau + k;             // kQB x kQB
-  double* G = Tm + kQB * kQB;       // kQB x kQB
-  double* W = G + kQB * kQB;        // kQB x kQT
-  double* W2 = W + kQB * kQT;       // kQB x kQT
-  double* Vc = W2 + kQB * kQT;      // kQC x kQV
+  double* tau = taus + (int64_t)blockIdx.x * ldtau;
+  const int jb = min(kQB, k - j0);
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
-  for (int j0 = 0; j0 < k; j0 += kQB) {
-    const int jb = min(kQB, k - j0);
-    // unblocked dgeqr2 on the block's columns (dlarfg: beta = -sign(alpha) ||.||)
-    for (int j = j0; j < j0 + jb; ++j) {
-      double* aj = A + (int64_t)j * lda;
-      double part = 0.0;
-      for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) part += aj[i] * aj[i];
-      const double sig = cta_sum(part, red);
-      if (tid == 0) {
-        const double alpha = aj[j];
-        double tj = 0.0, beta = alpha, scal = 0.0;
-        if (sig != 0.0) {
-          const double nrm = sqrt(alpha * alpha + sig);
-          beta = alpha >= 0.0 ? -nrm : nrm;
-          tj = (beta - alpha) / beta;
-          scal = 1.0 / (alpha - beta);
-        }
-        aj[j] = beta;
-        sh[0] = scal;
-        sh[1] = tj;
-        tau[j] = tj;
+  for (int j = j0; j < j0 + jb; ++j) {  // dgeqr2 / dlarfg: beta = -sign(alpha) ||.||
+    double* aj = A + (int64_t)j * lda;
+    double part = 0.0;
+    for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) part += aj[i] * aj[i];
+    const double sig = cta_sum(part, red);
+    if (tid == 0) {
+      const double alpha = aj[j];
+      double tj = 0.0, beta = alpha, scal = 0.0;
+      if (sig != 0.0) {
+        const double nrm = sqrt(alpha * alpha + sig);
+        beta = alpha >= 0.0 ? -nrm : nrm;
+        tj = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
       }
-      __syncthreads();
-      const double scal = sh[0], tj = sh[1];
-      for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= scal;
-      __syncthreads();
-      if (tj != 0.0) {
-        for (int c = j + 1 + w; c < j0 + jb; c += nw) {
-          double* ac = A + (int64_t)c * lda;
-          double acc = (lane == 0) ? ac[j] : 0.0;
-          for (int64_t i = j + 1 + lane; i < m; i += 32) acc += aj[i] * ac[i];
-          acc = warp_sum(acc) * tj;
-          if (lane == 0) ac[j] -= acc;
-          for (int64_t i = j + 1 + lane; i < m; i += 32) ac[i] -= acc * aj[i];
-        }
+      aj[j] = beta;
+      sh[0] = scal;
+      sh[1] = tj;
+      tau[j] = tj;
+    }
+    __syncthreads();
+    const double scal = sh[0], tj = sh[1];
+    for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= scal;
+    __syncthreads();
+    if (tj != 0.0) {
+      for (int c = j + 1 + w; c < j0 + jb; c += nw) {
+        double* ac = A + (int64_t)c * lda;
+        double acc = (lane == 0) ? ac[j] : 0.0;
+        for (int64_t i = j + 1 + lane; i < m; i += 32) acc += aj[i] * ac[i];
+        acc = warp_sum(acc) * tj;
+        if (lane == 0) ac[j] -= acc;
+        for (int64_t i = j + 1 + lane; i < m; i += 32) ac[i] -= acc * aj[i];
       }
-      __syncthreads();
     }
-    if (j0 + jb < k) {
-      panel_block_T(A, m, lda, j0, jb, tau, G, Tm);
-      panel_apply_block(A, m, lda, j0, jb, j0 + jb, k, Tm, 1, W, W2, Vc);
-    }
+    __syncthreads();
   }
-  for (int e = tid; e < k * k; e += blockDim.x) {
-    const int i = e % k, c = e / k;
-    D.R[e] = (i <= c) ? A[(int64_t)c * lda + i] : 0.0;
+  if (j0 + jb < k) {
+    panel_block_T(A, m, lda, j0, jb, tau, G, Tm);
+    double* Tout = Ts + ((int64_t)blockIdx.x * nblk + j0 / kQB) * kQB * kQB;
+    for (int e = tid; e < kQB * kQB; e += blockDim.x) Tout[e] = Tm[e];
   }
+}
+
+// grid (panels, tiles): the reflector block at j0 applied to trailing columns j0+kQB + y*kQU ..
+// (transT = 1: QR, I - V T' V'; transT = 0: forming Q, I - V T V').
+__global__ void __launch_bounds__(256) k_pq_update(const PanelDesc* __restrict__ descs, int j0,
+                                                   const double* __restrict__ Ts, int nblk, int transT) {
+  extern __shared__ double smq[];
+  __shared__ double Tm[kQB * kQB];
+  const PanelDesc D = descs[blockIdx.x];
+  const int k = D.k;
+  if (j0 >= k) return;
+  const int jb = min(kQB, k - j0), j1 = j0 + jb;
+  const int c0 = j1 + blockIdx.y * kQU;
+  if (c0 >= k) return;
+  const double* Tin = Ts + ((int64_t)blockIdx.x * nblk + j0 / kQB) * kQB * kQB;
+  for (int e = threadIdx.x; e < kQB * kQB; e += blockDim.x) Tm[e] = Tin[e];
+  double* W = smq;               // kQB x kQU
+  double* W2 = W + kQB * kQU;    // kQB x kQU
+  double* Vc = W2 + kQB * kQU;   // kQC x kQV
   __syncthreads();
-  // explicit Q (dorgqr): blocks from the last to the first; a block first applies its block
-  // reflector to the columns already formed to its right, then forms its own columns (dorg2r)
-  const int nblk = (k + kQB - 1) / kQB;
-  for (int bq = nblk - 1; bq >= 0; --bq) {
-    const int j0 = bq * kQB, jb = min(kQB, k - j0), j1 = j0 + jb;
-    if (j1 < k) {
-      panel_block_T(A, m, lda, j0, jb, tau, G, Tm);
-      panel_apply_block(A, m, lda, j0, jb, j1, k, Tm, 0, W, W2, Vc);
-    }
-    for (int j = j1 - 1; j >= j0; --j) {
-      double* aj = A + (int64_t)j * lda;
-      const double tj = tau[j];
-      if (j < j1 - 1) {
-        if (tid == 0) aj[j] = 1.0;
-        __syncthreads();
-        for (int c = j + 1 + w; c < j1; c += nw) {
-          double* ac = A + (int64_t)c * lda;
-          double acc = 0.0;
-          for (int64_t i = j + lane; i < m; i += 32) acc += aj[i] * ac[i];
-          acc = warp_sum(acc) * tj;
-          for (int64_t i = j + lane; i < m; i += 32) ac[i] -= acc * aj[i];
-        }
-        __syncthreads();
+  panel_apply_block(D.A, D.m, D.lda, j0, jb, c0, min(c0 + kQU, k), Tm, transT, W, W2, Vc, kQU);
+}
+
+__global__ void k_pq_rout(const PanelDesc* __restrict__ descs) {
+  const PanelDesc D = descs[blockIdx.x];
+  const int k = D.k;
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+    const int i = e % k, c = e / k;
+    D.R[e] = (i <= c) ? D.A[(int64_t)c * D.lda + i] : 0.0;
+  }
+}
+
+// dorg2r on the block's own columns j0 .. j1-1 (the columns to its right are already formed).
+__global__ void __launch_bounds__(512) k_pq_form(const PanelDesc* __restrict__ descs, int j0,
+                                                 const double* __restrict__ taus, int ldtau) {
+  const PanelDesc D = descs[blockIdx.x];
+  const int k = D.k;
+  if (j0 >= k) return;
+  double* A = D.A;
+  const int64_t m = D.m, lda = D.lda;
+  const double* tau = taus + (int64_t)blockIdx.x * ldtau;
+  const int j1 = min(j0 + kQB, k);
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+  for (int j = j1 - 1; j >= j0; --j) {
+    double* aj = A + (int64_t)j * lda;
+    const double tj = tau[j];
+    if (j < j1 - 1) {
+      if (tid == 0) aj[j] = 1.0;
+      __syncthreads();
+      for (int c = j + 1 + w; c < j1; c += nw) {
+        double* ac = A + (int64_t)c * lda;
+        double acc = 0.0;
+        for (int64_t i = j + lane; i < m; i += 32) acc += aj[i] * ac[i];
+        acc = warp_sum(acc) * tj;
+        for (int64_t i = j + lane; i < m; i += 32) ac[i] -= acc * aj[i];
       }
-      for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= -tj;
-      for (int64_t i = tid; i < j; i += blockDim.x) aj[i] = 0.0;
-      if (tid == 0) aj[j] = 1.0 - tj;
       __syncthreads();
     }
+    for (int64_t i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= -tj;
+    for (int64_t i = tid; i < j; i += blockDim.x) aj[i] = 0.0;
+    if (tid == 0) aj[j] = 1.0 - tj;
+    __syncthreads();
   }
 }
 
@@ -710,10 +744,26 @@ void launch_aca(const double* pts, KParams kp, const AcaBlock* blocks, int nbloc
   k_aca<<<nblocks, 1024, sm, st>>>(pts, kp, blocks, P, F, piv, rtol, rank, status);
 }
 
-void launch_panel_qr(const PanelDesc* descs, int n, int maxk, cudaStream_t st) {
-  const size_t sm = ((size_t)std::max(maxk, 1) + 2 * kQB * kQB + 2 * kQB * kQT + kQC * kQV) * sizeof(double);
-  smem_limit((const void*)k_panel_qr, sm);
-  k_panel_qr<<<n, 512, sm, st>>>(descs);
+void launch_panel_qr(const PanelDesc* descs, int n, int kmax, double* taus, double* Ts, cudaStream_t st) {
+  if (n <= 0 || kmax <= 0) return;
+  const int nblk = (kmax + kQB - 1) / kQB;
+  const int ntiles = (kmax + kQU - 1) / kQU;
+  const size_t smu = ((size_t)2 * kQB * kQU + kQC * kQV) * sizeof(double);
+  smem_limit((const void*)k_pq_update, smu);
+  for (int b = 0; b < nblk; ++b) {
+    k_pq_factor<<<n, 512, 0, st>>>(descs, b * kQB, taus, kmax, Ts, nblk);
+    k_pq_update<<<dim3((unsigned)n, (unsigned)ntiles), 256, smu, st>>>(descs, b * kQB, Ts, nblk, 1);
+  }
+  k_pq_rout<<<n, 256, 0, st>>>(descs);
+  for (int b = nblk - 1; b >= 0; --b) {
+    k_pq_update<<<dim3((unsigned)n, (unsigned)ntiles), 256, smu, st>>>(descs, b * kQB, Ts, nblk, 0);
+    k_pq_form<<<n, 512, 0, st>>>(descs, b * kQB, taus, kmax);
+  }
+}
+
+int64_t panel_qr_scratch(int n, int kmax) {
+  const int nblk = (kmax + kQB - 1) / kQB;
+  return (int64_t)n * kmax + (int64_t)n * nblk * kQB * kQB;
 }
 
 void launch_gnode(const GNodeDesc* nodes, int n, int* info, cudaStream_t st) {

@@ -129,6 +129,7 @@ struct km_handle {
   int64_t nldesc = 0;
   int gmaxr = 0;
   double* d_gpartial = nullptr;
+  double* d_pqs = nullptr;            // panel QR scratch (taus, block reflector T factors)
   // derivative HODLR (evaluated for one parameter at a time) and gradient workspaces
   int dk_param = -1;
   double* d_dK = nullptr;
@@ -273,6 +274,7 @@ void free_problem(km_handle* h) {
   h->nldesc = 0;
   h->gmaxr = 0;
   h->d_gpartial = nullptr;
+  h->d_pqs = nullptr;
   h->dk_param = -1;
   h->d_dK = h->d_dPhi = h->d_Sj = h->d_GP = h->d_GG = h->d_T = h->d_U = h->d_dots = nullptr;
   h->d_dKf = h->d_dPhif = h->d_Phif = nullptr;
@@ -1088,10 +1090,20 @@ static int general_factorize(km_handle* h) {
     KM_CUDA(h, cudaMemcpy(h->d_pdesc, pd.data(), sizeof(PanelDesc) * pd.size(), cudaMemcpyHostToDevice));
     if (!fi.empty())
       KM_CUDA(h, cudaMemcpy(h->d_gfact, fi.data(), sizeof(GApplyItem) * fi.size(), cudaMemcpyHostToDevice));
+    // panel QR scratch (taus and block T factors) for the largest level
+    std::vector<int> kmax_l(t.L + 2, 0);
+    int64_t pqs = 1;
+    for (int l = 1; l <= t.L; ++l) {
+      for (int64_t p = pdoff[l]; p < pdoff[l + 1]; ++p) kmax_l[l] = std::max(kmax_l[l], pd[p].k);
+      pqs = std::max(pqs, panel_qr_scratch((int)(pdoff[l + 1] - pdoff[l]), kmax_l[l]));
+    }
+    if ((rc = grow(h, &h->d_pqs, pqs))) return rc;
     if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri_desc(h->d_Lf, t, 0, h->d_ldesc, (int)ld.size(), h->gmaxr, st)))
       return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
     for (int l = 1; l <= t.L; ++l) {
-      KLV(h, KM_PROF_LEAF_QR, launch_panel_qr(h->d_pdesc + pdoff[l], (int)(pdoff[l + 1] - pdoff[l]), h->gmaxr, st));
+      const int np = (int)(pdoff[l + 1] - pdoff[l]);
+      KLV(h, KM_PROF_LEAF_QR, launch_panel_qr(h->d_pdesc + pdoff[l], np, kmax_l[l], h->d_pqs,
+                                              h->d_pqs + (int64_t)np * kmax_l[l], st));
       KLV(h, KM_PROF_NODE, launch_gnode(h->d_gnodes + h->lvoff[l], (int)(h->lvoff[l + 1] - h->lvoff[l]),
                                         h->d_info + t.nleaf + h->lvoff[l], st));
       const int64_t a = h->gfoff[l], b = h->gfoff[l + 1];

@@ -148,7 +148,10 @@ void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb,
 // ACA and the general factorisation
 void launch_aca(const double* pts, KParams kp, const AcaBlock* blocks, int nblocks, int maxcap, double* P,
                 uint8_t* F, int* piv, double rtol, int* rank, int* status, cudaStream_t st);
-void launch_panel_qr(const PanelDesc* descs, int n, int maxk, cudaStream_t st);
+// Householder QR with explicit Q of n panels (largest column count kmax); scratch of
+// panel_qr_scratch(n, kmax) doubles: taus (n x kmax) then the T factors
+void launch_panel_qr(const PanelDesc* descs, int n, int kmax, double* taus, double* Ts, cudaStream_t st);
+int64_t panel_qr_scratch(int n, int kmax);
 void launch_gnode(const GNodeDesc* nodes, int n, int* info, cudaStream_t st);
 void launch_gapply(const GApplyItem* items, int n, const GNodeDesc* nodes, int maxr, int maxcols, int mode,
                    double* X, const double* Xin, int64_t ldX, int kX, cudaStream_t st);
