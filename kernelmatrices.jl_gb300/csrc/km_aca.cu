@@ -101,12 +101,14 @@ __device__ void cta_restricted_argmax(const double* x, const uint8_t* excl, int6
 __global__ void __launch_bounds__(1024) k_aca(const double* __restrict__ pts, KParams kp,
                                               const AcaBlock* __restrict__ blocks, double* __restrict__ P,
                                               uint8_t* __restrict__ F, int* __restrict__ piv, double rtol,
-                                              int* __restrict__ rank_out, int* __restrict__ status) {
+                                              int* __restrict__ rank_out, int* __restrict__ status, int only) {
   extern __shared__ double dsm[];  // 2 * cap: dots with previous columns
   __shared__ double sred[40];
   __shared__ double sval[40];
   __shared__ long long sidx[72];
-  const AcaBlock B = blocks[blockIdx.x];
+  const int bid = only >= 0 ? only : (int)blockIdx.x;
+  const AcaBlock B = blocks[bid];
+  if (only < 0 && B.grid) return;  // compressed by k_aca_grid
   const int64_t nro = B.nro, ncl = B.ncl;
   double* U = P + B.offU;
   double* V = P + B.offV;
@@ -172,8 +174,8 @@ __global__ void __launch_bounds__(1024) k_aca(const double* __restrict__ pts, KP
   }
   if (strt + 1 == maxsz) {
     if (tid == 0) {
-      status[blockIdx.x] = 1;
-      rank_out[blockIdx.x] = 0;
+      status[bid] = 1;
+      rank_out[bid] = 0;
     }
     return;
   }
@@ -264,8 +266,8 @@ __global__ void __launch_bounds__(1024) k_aca(const double* __restrict__ pts, KP
     ++frnk;
   }
   if (tid == 0) {
-    rank_out[blockIdx.x] = frnk;
-    status[blockIdx.x] = st;
+    rank_out[bid] = frnk;
+    status[bid] = st;
   }
 }
 
@@ -398,7 +400,7 @@ __device__ void panel_apply_block(double* A, int64_t m, int64_t lda, int j0, int
 //   k_pq_rout    (one CTA per panel)        R out
 //   then, blocks from last to first: k_pq_update on the formed columns, k_pq_form (dorg2r on
 //   the block's own columns).  tau and the T factors live in global scratch between launches.
-constexpr int kQU = 32;  // trailing columns per update CTA
+constexpr int kQU = 8;  // trailing columns per update CTA (each CTA is FP64-bound: narrow tiles, more SMs)
 
 __global__ void __launch_bounds__(512) k_pq_factor(const PanelDesc* __restrict__ descs, int j0,
                                                    double* __restrict__ taus, int ldtau, double* __restrict__ Ts,
@@ -735,13 +737,404 @@ __global__ void k_glogdet(const GNodeDesc* __restrict__ nodes, int nn, double* _
 }
 
 // ---------------------------------------------------------------------------------------------
+// ACA of one large block by every SM (cooperative launch, one CTA per SM).  The steps are those
+// of k_aca (factorizations.jl:9-84): each CTA owns a slice of the rows and a slice of the
+// columns, evaluates its part of the residual row / column, and the argmax searches and the
+// norms are reduced over the CTAs' partial results in a fixed order, so every CTA takes the
+// same pivots.  Values written by other CTAs (records, pivots' entries, the published norms) are
+// read with ld.global.cg (L2, the coherence point); a CTA sets the used-row/column flags of its
+// own slices only.  Grid barriers spin a bounded number of times; a barrier that runs out sets the
+// block's status to 3 (timeout) and the CTAs leave the loop together at the next check.
+// ---------------------------------------------------------------------------------------------
+constexpr long long kGridSpinLimit = 1ll << 20;  // L2 polls per barrier wait (~0.3 s)
+
+struct GridBar {
+  unsigned* count;
+  volatile unsigned* gen;
+  volatile int* err;
+};
+
+__device__ bool grid_barrier(GridBar gb) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned g = *gb.gen;
+    __threadfence();
+    if (atomicAdd(gb.count, 1u) == gridDim.x - 1) {
+      *gb.count = 0;
+      __threadfence();
+      atomicExch((unsigned*)gb.gen, g + 1);
+    } else {
+      long long spins = 0;
+      while (*gb.gen == g && *gb.err == 0) {
+        if (++spins > kGridSpinLimit) {
+          atomicExch((int*)gb.err, 1);
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *gb.err == 0;
+}
+
+// partial argmax record of one CTA: (|x| best, its index, first unflagged index)
+__device__ void slice_argmax(const double* x, const uint8_t* excl, int64_t lo, int64_t hi, double* sval,
+                             long long* sidx, double* pval, long long* pidx) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double best = 0.0;
+  long long bi = LLONG_MAX, first = LLONG_MAX;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    if (excl[i]) continue;
+    if (first == LLONG_MAX) first = i;
+    const double a = fabs(x[i]);
+    if (a > best) {
+      best = a;
+      bi = i;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const long long oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    const long long of = __shfl_xor_sync(0xffffffffu, first, o);
+    if (ob > best || (ob == best && oi < bi)) {
+      best = ob;
+      bi = oi;
+    }
+    first = min(first, of);
+  }
+  if (lane == 0) {
+    sval[w] = best;
+    sidx[w] = bi;
+    sidx[32 + w] = first;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    long long ib = LLONG_MAX, f = LLONG_MAX;
+    for (int q = 0; q < nw; ++q) {
+      if (sval[q] > b || (sval[q] == b && sidx[q] < ib)) {
+        b = sval[q];
+        ib = sidx[q];
+      }
+      f = min(f, sidx[32 + q]);
+    }
+    *pval = b;
+    pidx[0] = ib;
+    pidx[1] = f;
+  }
+  __syncthreads();
+}
+
+// combine the CTAs' argmax records (same order in every CTA): restrictedmaxabs semantics.
+// CTA g's record: value at pval[g * stride], indices at pidx[2 g] (best) and pidx[2 g + 1] (first).
+__device__ void grid_argmax(const double* x, int64_t n, const double* pval, const long long* pidx, int stride,
+                            double* sh, long long* shi, double* out_val, int64_t* out_idx) {
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    long long ib = LLONG_MAX, f = LLONG_MAX;
+    for (int g = 0; g < (int)gridDim.x; ++g) {
+      const double v = __ldcg(pval + (int64_t)g * stride);
+      const long long i = __ldcg(pidx + 2 * g), fi = __ldcg(pidx + 2 * g + 1);
+      if (v > b || (v == b && i < ib)) {
+        b = v;
+        ib = i;
+      }
+      f = min(f, fi);
+    }
+    if (b > 0.0) {
+      sh[0] = __ldcg(x + ib);
+      shi[0] = ib;
+    } else {
+      sh[0] = 0.0;
+      shi[0] = (f == LLONG_MAX) ? n - 1 : f;
+    }
+  }
+  __syncthreads();
+  *out_val = sh[0];
+  *out_idx = shi[0];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(512) k_aca_grid(const double* __restrict__ pts, KParams kp,
+                                                  const AcaBlock* __restrict__ blocks, int bidx,
+                                                  double* __restrict__ P, uint8_t* __restrict__ F,
+                                                  int* __restrict__ piv, double rtol, int* __restrict__ rank_out,
+                                                  int* __restrict__ status, double* __restrict__ scr,
+                                                  GridBar gb) {
+  extern __shared__ double coef[];  // cap: U[ri, j] or V[cj, j] of the previous columns
+  __shared__ double sred[40];
+  __shared__ double sval[40];
+  __shared__ long long sidx[72];
+  __shared__ double sh[4];
+  __shared__ long long shi[2];
+  const AcaBlock B = blocks[bidx];
+  const int64_t nro = B.nro, ncl = B.ncl;
+  const int cap = B.cap;
+  double* U = P + B.offU;
+  double* V = P + B.offV;
+  uint8_t* urow = F + B.offFlag;
+  uint8_t* ucol = urow + nro;
+  int* prow = piv + 2 * B.offPiv;
+  int* pcol = prow + cap;
+  const int G = gridDim.x, g = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+  const int64_t rs = (nro + G - 1) / G, cs = (ncl + G - 1) / G;
+  auto mn = [](int64_t a, int64_t b) { return a < b ? a : b; };
+  const int64_t r_lo = mn(nro, (int64_t)g * rs), r_hi = mn(nro, r_lo + rs);
+  const int64_t c_lo = mn(ncl, (int64_t)g * cs), c_hi = mn(ncl, c_lo + cs);
+  const double* xr = pts + 2 * B.row0;
+  const double* xc = pts + 2 * B.col0;
+  // scratch: per CTA a record of stride S doubles: [0] argmax value, [1] sum 1, [2] sum 2,
+  // [3 .. 3+cap) dots a_j, [3+cap .. 3+2cap) dots b_j; then 2 long longs per CTA; then scalars
+  const int S = 3 + 2 * cap;
+  double* rec = scr + (int64_t)g * S;
+  long long* irec = reinterpret_cast<long long*>(scr + (int64_t)G * S);
+  double* scal = scr + (int64_t)G * S + 2 * G;  // [0] znorm2, [1] sr, [2] sc
+  for (int64_t i = r_lo + tid; i < r_hi; i += blockDim.x) urow[i] = 0;
+  for (int64_t c = c_lo + tid; c < c_hi; c += blockDim.x) ucol[c] = 0;
+  if (!grid_barrier(gb)) goto done;
+  {
+    const int maxsz = B.maxsz;
+    auto slice_max = [&](const double* x) {
+      double mx = 0.0;
+      for (int64_t c = c_lo + tid; c < c_hi; c += blockDim.x) mx = fmax(mx, fabs(x[c]));
+      for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if (lane == 0) sred[w] = mx;
+      __syncthreads();
+      if (tid == 0) {
+        double m = 0.0;
+        for (int q = 0; q < nw; ++q) m = fmax(m, sred[q]);
+        rec[0] = m;
+      }
+      __syncthreads();
+    };
+    auto all_max = [&]() {
+      if (tid == 0) {
+        double m = 0.0;
+        for (int q = 0; q < G; ++q) m = fmax(m, __ldcg(scr + (int64_t)q * S));
+        sh[2] = m;
+      }
+      __syncthreads();
+      const double m = sh[2];
+      __syncthreads();
+      return m;
+    };
+    auto slice_sum = [&](const double* x, int64_t lo, int64_t hi) {
+      double a = 0.0;
+      for (int64_t i = lo + tid; i < hi; i += blockDim.x) a += x[i] * x[i];
+      return cta_sum(a, sred);
+    };
+    // first row not all zero (factorizations.jl:24-30)
+    int64_t strt = 0;
+    for (;;) {
+      const double px = xr[2 * strt], py = xr[2 * strt + 1];
+      for (int64_t c = c_lo + tid; c < c_hi; c += blockDim.x) V[c] = kernel_value(kp, px, py, xc[2 * c], xc[2 * c + 1]);
+      __syncthreads();
+      slice_max(V);
+      if (!grid_barrier(gb)) goto done;
+      const double m = all_max();
+      if (m != 0.0 || strt + 1 >= maxsz) break;
+      ++strt;
+      if (!grid_barrier(gb)) goto done;  // records are rewritten by the next row
+    }
+    if (strt + 1 == maxsz) {
+      if (g == 0 && tid == 0) {
+        status[bidx] = 1;
+        rank_out[bidx] = 0;
+      }
+      goto done;
+    }
+    if (tid == 0 && strt >= r_lo && strt < r_hi) urow[strt] = 1;  // flags are set by their slice's owner
+    if (g == 0 && tid == 0) prow[0] = (int)strt;
+    double mv;
+    int64_t mi;
+    slice_argmax(V, ucol, c_lo, c_hi, sval, sidx, rec, irec + 2 * g);
+    if (!grid_barrier(gb)) goto done;
+    grid_argmax(V, ncl, scr, irec, S, sh, shi, &mv, &mi);
+    if (!grid_barrier(gb)) goto done;  // V[mi] is read before the division below
+    for (int64_t c = c_lo + tid; c < c_hi; c += blockDim.x) V[c] = __ddiv_rn(V[c], mv);
+    {
+      const double px = xc[2 * mi], py = xc[2 * mi + 1];
+      for (int64_t i = r_lo + tid; i < r_hi; i += blockDim.x) U[i] = kernel_value(kp, xr[2 * i], xr[2 * i + 1], px, py);
+    }
+    __syncthreads();
+    {
+      const double a = slice_sum(V, c_lo, c_hi), b = slice_sum(U, r_lo, r_hi);
+      if (tid == 0) {
+        rec[1] = a;
+        rec[2] = b;
+      }
+    }
+    if (tid == 0 && mi >= c_lo && mi < c_hi) ucol[mi] = 1;
+    if (g == 0 && tid == 0) pcol[0] = (int)mi;
+    if (!grid_barrier(gb)) goto done;
+    double sr = 0.0, sc = 0.0;
+    for (int q = 0; q < G; ++q) {
+      sr += __ldcg(scr + (int64_t)q * S + 1);
+      sc += __ldcg(scr + (int64_t)q * S + 2);
+    }
+    double znorm2 = __dmul_rn(sr, sc);
+    int frnk = 1, st = 0;
+    while (__dmul_rn(sqrt(sr), sqrt(sc)) > __dmul_rn(rtol, sqrt(znorm2)) && frnk < maxsz) {
+      // next row pivot: argmax of the last column over unused rows
+      const double* lastcol = U + (int64_t)(frnk - 1) * nro;
+      double rv;
+      int64_t ri;
+      if (!grid_barrier(gb)) goto done;  // the records of the previous step have been read
+      slice_argmax(lastcol, urow, r_lo, r_hi, sval, sidx, rec, irec + 2 * g);
+      if (!grid_barrier(gb)) goto done;
+      grid_argmax(lastcol, nro, scr, irec, S, sh, shi, &rv, &ri);
+      if (frnk >= cap) {
+        st = 2;
+        break;
+      }
+      for (int j = tid; j < frnk; j += blockDim.x) coef[j] = __ldcg(U + ri + (int64_t)j * nro);
+      __syncthreads();
+      double* row = V + (int64_t)frnk * ncl;
+      {
+        const double px = xr[2 * ri], py = xr[2 * ri + 1];
+        for (int64_t c = c_lo + tid; c < c_hi; c += blockDim.x) {
+          double v = kernel_value(kp, px, py, xc[2 * c], xc[2 * c + 1]);
+          for (int j = 0; j < frnk; ++j) v = __dsub_rn(v, __dmul_rn(coef[j], V[c + (int64_t)j * ncl]));
+          row[c] = v;
+        }
+      }
+      if (!grid_barrier(gb)) goto done;  // urow[ri] is set after every CTA searched
+      if (tid == 0 && ri >= r_lo && ri < r_hi) urow[ri] = 1;
+      double cv;
+      int64_t cj;
+      slice_argmax(row, ucol, c_lo, c_hi, sval, sidx, rec, irec + 2 * g);
+      if (!grid_barrier(gb)) goto done;
+      grid_argmax(row, ncl, scr, irec, S, sh, shi, &cv, &cj);
+      if (cv == 0.0) break;
+      if (!grid_barrier(gb)) goto done;  // row[cj] is read before the division below
+      if (tid == 0 && cj >= c_lo && cj < c_hi) ucol[cj] = 1;
+      for (int64_t c = c_lo + tid; c < c_hi; c += blockDim.x) row[c] = __ddiv_rn(row[c], cv);
+      for (int j = tid; j < frnk; j += blockDim.x) coef[j] = __ldcg(V + cj + (int64_t)j * ncl);
+      __syncthreads();
+      double* col = U + (int64_t)frnk * nro;
+      {
+        const double px = xc[2 * cj], py = xc[2 * cj + 1];
+        for (int64_t i = r_lo + tid; i < r_hi; i += blockDim.x) {
+          double v = kernel_value(kp, xr[2 * i], xr[2 * i + 1], px, py);
+          for (int j = 0; j < frnk; ++j) v = __dsub_rn(v, __dmul_rn(coef[j], U[i + (int64_t)j * nro]));
+          col[i] = v;
+        }
+      }
+      __syncthreads();
+      // partial dots with the previous columns and the new squared norms
+      for (int j = w; j < frnk; j += nw) {
+        const double* uj = U + (int64_t)j * nro;
+        const double* vj = V + (int64_t)j * ncl;
+        double a = 0.0, b = 0.0;
+        for (int64_t i = r_lo + lane; i < r_hi; i += 32) a += uj[i] * col[i];
+        for (int64_t c = c_lo + lane; c < c_hi; c += 32) b += vj[c] * row[c];
+        a = warp_sum(a);
+        b = warp_sum(b);
+        if (lane == 0) {
+          rec[3 + j] = a;
+          rec[3 + cap + j] = b;
+        }
+      }
+      {
+        const double a = slice_sum(row, c_lo, c_hi), b = slice_sum(col, r_lo, r_hi);
+        if (tid == 0) {
+          rec[1] = a;
+          rec[2] = b;
+        }
+      }
+      if (!grid_barrier(gb)) goto done;
+      if (g == 0) {
+        // dots summed over the CTAs in a fixed order, one warp per j
+        for (int j = w; j < frnk; j += nw) {
+          double a = 0.0, b = 0.0;
+          for (int q = lane; q < G; q += 32) {
+            a += __ldcg(scr + (int64_t)q * S + 3 + j);
+            b += __ldcg(scr + (int64_t)q * S + 3 + cap + j);
+          }
+          a = warp_sum(a);
+          b = warp_sum(b);
+          if (lane == 0) coef[j] = __dmul_rn(__dmul_rn(2.0, fabs(a)), fabs(b));
+        }
+        __syncthreads();
+        if (tid == 0) {
+          double z = znorm2;
+          for (int j = 0; j < frnk; ++j) z = __dadd_rn(z, coef[j]);
+          double s1 = 0.0, s2 = 0.0;
+          for (int q = 0; q < G; ++q) {
+            s1 += __ldcg(scr + (int64_t)q * S + 1);
+            s2 += __ldcg(scr + (int64_t)q * S + 2);
+          }
+          scal[0] = __dadd_rn(z, __dmul_rn(s1, s2));
+          scal[1] = s1;
+          scal[2] = s2;
+          prow[frnk] = (int)ri;
+          pcol[frnk] = (int)cj;
+        }
+      }
+      if (!grid_barrier(gb)) goto done;
+      znorm2 = __ldcg(scal);
+      sr = __ldcg(scal + 1);
+      sc = __ldcg(scal + 2);
+      ++frnk;
+    }
+    if (g == 0 && tid == 0) {
+      rank_out[bidx] = frnk;
+      status[bidx] = st;
+    }
+  }
+done:
+  if (g == 0 && tid == 0 && *gb.err) status[bidx] = 3;
+}
+
+int64_t aca_grid_scratch(int cap) {
+  const int G = 152 * 2;  // upper bound of the grid
+  return (int64_t)G * (3 + 2 * cap) + 2 * G + 8 + 4;
+}
+
+bool launch_aca_grid(const double* pts, KParams kp, const AcaBlock* blocks, int b, int cap, double* P, uint8_t* F,
+                     int* piv, double rtol, int* rank, int* status, double* scratch, cudaStream_t st) {
+  int dev = 0, coop = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (!coop) return false;
+  const size_t sm = (size_t)std::max(cap, 1) * sizeof(double);
+  smem_limit((const void*)k_aca_grid, sm);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_aca_grid, 512, sm) != cudaSuccess || per < 1) {
+    cudaGetLastError();
+    return false;
+  }
+  const int G = std::min(nsm, 152 * 2);
+  // barrier words live after the records in the scratch
+  unsigned* words = reinterpret_cast<unsigned*>(scratch + (int64_t)G * (3 + 2 * cap) + 2 * G + 8);
+  if (cudaMemsetAsync(words, 0, 4 * sizeof(unsigned), st) != cudaSuccess) return false;
+  GridBar gb{words, words + 1, reinterpret_cast<volatile int*>(words + 2)};
+  void* args[] = {(void*)&pts, (void*)&kp, (void*)&blocks, (void*)&b, (void*)&P, (void*)&F, (void*)&piv,
+                  (void*)&rtol, (void*)&rank, (void*)&status, (void*)&scratch, (void*)&gb};
+  if (cudaLaunchCooperativeKernel((const void*)k_aca_grid, dim3(G), dim3(512), args, sm, st) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return true;
+}
+
+void launch_aca_one(const double* pts, KParams kp, const AcaBlock* blocks, int b, int maxcap, double* P,
+                    uint8_t* F, int* piv, double rtol, int* rank, int* status, cudaStream_t st) {
+  const size_t sm = (size_t)2 * std::max(maxcap, 1) * sizeof(double);
+  smem_limit((const void*)k_aca, sm);
+  k_aca<<<1, 1024, sm, st>>>(pts, kp, blocks, P, F, piv, rtol, rank, status, b);
+}
+
+// ---------------------------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------------------------
 void launch_aca(const double* pts, KParams kp, const AcaBlock* blocks, int nblocks, int maxcap, double* P,
                 uint8_t* F, int* piv, double rtol, int* rank, int* status, cudaStream_t st) {
   const size_t sm = (size_t)2 * std::max(maxcap, 1) * sizeof(double);
   smem_limit((const void*)k_aca, sm);
-  k_aca<<<nblocks, 1024, sm, st>>>(pts, kp, blocks, P, F, piv, rtol, rank, status);
+  k_aca<<<nblocks, 1024, sm, st>>>(pts, kp, blocks, P, F, piv, rtol, rank, status, -1);
 }
 
 void launch_panel_qr(const PanelDesc* descs, int n, int kmax, double* taus, double* Ts, cudaStream_t st) {

@@ -130,6 +130,7 @@ struct km_handle {
   int gmaxr = 0;
   double* d_gpartial = nullptr;
   double* d_pqs = nullptr;            // panel QR scratch (taus, block reflector T factors)
+  double* d_acascr = nullptr;         // grid-wide ACA scratch (per-CTA records, barrier words)
   // derivative HODLR (evaluated for one parameter at a time) and gradient workspaces
   int dk_param = -1;
   double* d_dK = nullptr;
@@ -173,7 +174,8 @@ struct km_handle {
 namespace {
 
 constexpr int kLogdetBlocks = 256;
-constexpr int kAcaMaxCap = 4096;  // ACA panel columns per block (2 x 4096 doubles of shared memory)
+constexpr int kAcaMaxCap = 4096;       // ACA panel columns per block (2 x 4096 doubles of shared memory)
+constexpr int64_t kAcaGridMin = 8192;  // blocks at least this wide run the grid-wide ACA kernel
 
 int fail(km_handle* h, int code, const std::string& msg) {
   if (h) h->err = msg;
@@ -275,6 +277,7 @@ void free_problem(km_handle* h) {
   h->gmaxr = 0;
   h->d_gpartial = nullptr;
   h->d_pqs = nullptr;
+  h->d_acascr = nullptr;
   h->dk_param = -1;
   h->d_dK = h->d_dPhi = h->d_Sj = h->d_GP = h->d_GG = h->d_T = h->d_U = h->d_dots = nullptr;
   h->d_dKf = h->d_dPhif = h->d_Phif = nullptr;
@@ -914,6 +917,7 @@ static int aca_assemble(km_handle* h, const double* pts, bool dev, const Tree& t
       b.nro = t.node_size(l - 1, 2 * k + 1);
       const int64_t minsz = std::min(b.nro, b.ncl);
       b.maxsz = (int)(maxrank == 0 ? minsz : std::min<int64_t>(maxrank, minsz));
+      b.grid = minsz >= kAcaGridMin ? 1 : 0;
       full += (b.nro + b.ncl) * (int64_t)b.maxsz;
       h->blk.push_back(b);
     }
@@ -970,6 +974,24 @@ static int aca_assemble(km_handle* h, const double* pts, bool dev, const Tree& t
   if (nb > 0)
     KLV(h, KM_PROF_ACA, launch_aca(h->d_pts, h->kp, h->d_blk, nb, maxcap, h->d_panels, h->d_flags, h->d_piv, tol,
                                    h->d_brank, h->d_bstatus, st));
+  // large blocks: one cooperative launch each, all SMs on one block
+  {
+    int gmax = 0;
+    for (const auto& b : h->blk)
+      if (b.grid) gmax = std::max(gmax, b.cap);
+    if (gmax > 0) {
+      if ((rc = grow(h, &h->d_acascr, aca_grid_scratch(gmax)))) return rc;
+      for (int q = 0; q < nb; ++q) {
+        if (!h->blk[q].grid) continue;
+        bool ok = false;
+        KLV(h, KM_PROF_ACA, ok = launch_aca_grid(h->d_pts, h->kp, h->d_blk, q, h->blk[q].cap, h->d_panels, h->d_flags,
+                                                 h->d_piv, tol, h->d_brank, h->d_bstatus, h->d_acascr, st));
+        if (!ok)
+          KLV(h, KM_PROF_ACA, launch_aca_one(h->d_pts, h->kp, h->d_blk, q, maxcap, h->d_panels, h->d_flags, h->d_piv,
+                                             tol, h->d_brank, h->d_bstatus, st));
+      }
+    }
+  }
   if ((rc = check_launch(h, "aca")) != KM_OK) return rc;
   h->stats.assemble_ms = timer_stop(h);
   if ((rc = sync(h, "aca")) != KM_OK) return rc;
@@ -981,6 +1003,7 @@ static int aca_assemble(km_handle* h, const double* pts, bool dev, const Tree& t
   }
   for (int q = 0; q < nb; ++q) {
     if (stat[q] == 1) return fail(h, KM_ERR_ACA, "Incompatible maxrank or matrix dimensions.");
+    if (stat[q] == 3) return fail(h, KM_ERR_TIMEOUT, "a bounded grid barrier of the ACA kernel ran out");
     if (stat[q] == 2)
       return fail(h, KM_ERR_UNSUPPORTED, "ACA rank reached the panel capacity (" + std::to_string(capmax) +
                                              " columns) before the tolerance; pass a maxrank");

@@ -28,6 +28,7 @@ struct AcaBlock {             // rows = second child (a:b), cols = first child (
   int64_t offU, offV;         // column-major U (nro x cap), V (ncl x cap) in the panel arena
   int64_t offFlag, offPiv;    // used-row/col flags (nro + ncl bytes); pivots (2 * cap ints at 2*offPiv)
   int cap, maxsz;
+  int grid;                   // 1: large block, compressed by the grid-wide ACA kernel
 };
 struct PanelDesc {            // Householder QR with explicit Q of A (m x k, leading dim lda)
   double* A;
@@ -148,6 +149,15 @@ void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb,
 // ACA and the general factorisation
 void launch_aca(const double* pts, KParams kp, const AcaBlock* blocks, int nblocks, int maxcap, double* P,
                 uint8_t* F, int* piv, double rtol, int* rank, int* status, cudaStream_t st);
+// ACA of one large block (blocks[b].grid == 1) by all SMs in one cooperative launch, with
+// bounded grid barriers; scratch of aca_grid_scratch(cap) doubles.  Returns false when the
+// cooperative launch is unavailable (the caller then runs the block in the one-CTA kernel).
+bool launch_aca_grid(const double* pts, KParams kp, const AcaBlock* blocks, int b, int cap, double* P, uint8_t* F,
+                     int* piv, double rtol, int* rank, int* status, double* scratch, cudaStream_t st);
+int64_t aca_grid_scratch(int cap);
+// one-CTA ACA of a single block regardless of its grid flag (fallback)
+void launch_aca_one(const double* pts, KParams kp, const AcaBlock* blocks, int b, int maxcap, double* P,
+                    uint8_t* F, int* piv, double rtol, int* rank, int* status, cudaStream_t st);
 // Householder QR with explicit Q of n panels (largest column count kmax); scratch of
 // panel_qr_scratch(n, kmax) doubles: taus (n x kmax) then the T factors
 void launch_panel_qr(const PanelDesc* descs, int n, int kmax, double* taus, double* Ts, cudaStream_t st);
