@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(1024) k_aca(const double* __restrict__ pts, KP
 // columns are then read and written once per block instead of once per reflector.  V is staged
 // in shared memory kQC rows at a time; trailing columns are processed kQT at a time.
 // ---------------------------------------------------------------------------------------------
-constexpr int kQB = 16;
+constexpr int kQB = 8;
 constexpr int kQC = 256;
 constexpr int kQT = 256;
 constexpr int kQV = kQB + 1;  // row stride of the staged V chunk (conflict-free column reads)
