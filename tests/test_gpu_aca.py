@@ -106,3 +106,38 @@ def test_aca_errors(lib):
     K.symmetricfactorize(hk)
     with pytest.raises(K.KMError, match="abandoned"):
         hk.block_factors(0)
+
+
+def test_grid_aca_large_block(lib):
+    """n = 16384 puts an 8192 x 8192 top block on the grid-wide ACA kernel (every SM on one
+    block) and the 4096 x 4096 level-2 blocks on the one-CTA kernel.  On the rational-quadratic
+    kernel the pivots and ranks of both must equal the oracle's exactly; products, logdet and
+    solves follow at the usual tolerances."""
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    n = 16384
+    pts = uniform_points(n, 99)
+    params = (1.0, 0.2, 1e-2)
+    ok = O.KernelMatrix(pts, pts, np.array(params), O.KERNEL_RQ)
+    ohk = O.build_hodlr(ok, 1e-10, 0, O.LogLevel(8), nystrom=False)
+    km = K.KernelMatrix(pts, pts, params, K.RatQuad())
+    hk = K.KernelHODLR(km, 1e-10, 0, K.LogLevel(8), nystrom=False)
+    oranks = [u.shape[1] for lv in ohk.U for u in lv]
+    assert list(hk.block_ranks()) == oranks
+    q = 0
+    for lv in range(len(ohk.U)):
+        for kk in range(len(ohk.U[lv])):
+            rows, cols = hk.aca_pivots(q)
+            orow, ocol = ohk.pivots[lv][kk]
+            assert list(rows) == list(orow) and list(cols) == list(ocol)
+            q += 1
+    U, V = hk.block_factors(q - 1)  # the top block, last in the oracle's order
+    assert U.shape[0] == n // 2
+    assert rel(U @ V.T, ohk.U[-1][0] @ ohk.V[-1][0].T) < 1e-12
+    rhs = np.random.default_rng(7).standard_normal((n, 2))
+    assert rel(hk @ rhs, O.hodlr_mul(ohk, rhs)) < 1e-12
+    O.symmetricfactorize(ohk)
+    K.symmetricfactorize(hk)
+    ld0 = O.hodlr_logdet(ohk)
+    assert abs(hk.logdet() - ld0) < 1e-8 + 1e-12 * abs(ld0)
+    assert rel(hk.ldiv(rhs), O.hodlr_ldiv(ohk, rhs)) < 1e-9
