@@ -200,6 +200,27 @@ int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t npr
 int km_nll_grad_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed, double* nll,
                        double* grad);
 
+/* Profile likelihood: the scale parameter profiled out.  nll = 0.5 (logdet K + n log(y'K^{-1}y)),
+ * grad_j = 0.5 (tr-estimate_j - n y'K^{-1} dK_j K^{-1}y / y'K^{-1}y).  Replaces profile_negloglik
+ * (src/HODLR/src/maxlikfunctions.jl:11-19) and stoch_profile_gradient
+ * (src/HODLR/src/stochasticgradient.jl:48-86, shuffle = false); the arguments are those of
+ * km_nll_grad / km_nll_grad_seeded.  KM_ERR_BAD_ARG when y'K^{-1}y <= 0 (e.g. y = 0), where the
+ * reference's log would return -Inf or NaN. */
+int km_profile_nll_grad(km_handle* h, const double* y, const double* probes, int64_t nprobe,
+                        double* nll, double* grad);
+int km_profile_nll_grad_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed,
+                               double* nll, double* grad);
+
+/* NLL, stochastic gradient and the stochastic Fisher information matrix from one set of probes:
+ * fisher (3 x 3, symmetric, column-major) F_jk = 0.5 mean_v (W^{-1} dK_j W'^{-1} v)'
+ * (W^{-1} dK_k W'^{-1} v).  Replaces grad_and_fisher_matrix (src/HODLR/src/stochastichessian.jl:
+ * 152-181), fisher_matrix (src/HODLR/src/maxlikfunctions.jl:138-146) and stoch_fisher
+ * (stochastichessian.jl:91-115, shuffle = false).  grad and fisher are required, nprobe >= 1. */
+int km_grad_fisher(km_handle* h, const double* y, const double* probes, int64_t nprobe,
+                   double* nll, double* grad, double* fisher);
+int km_grad_fisher_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed,
+                          double* nll, double* grad, double* fisher);
+
 /* Frees the device buffers of the handle's current problem (the handle stays usable; the next
  * km_assemble allocates again).  No reference counterpart: Julia's GC frees the arrays. */
 int km_trim(km_handle* h);
@@ -228,6 +249,8 @@ typedef struct km_batch_opts {
   int64_t level;
   int64_t nprobe;        /* Rademacher probes per problem; 0 => NLL only                      */
   uint64_t probe_seed;   /* problem b draws its probes with seed probe_seed + b               */
+  int profile;           /* nonzero => profile likelihood (nlpl_objective,                     */
+                         /* src/HODLR/src/maxlikfunctions.jl:61-82) instead of nll_objective  */
 } km_batch_opts;
 
 typedef struct km_batch km_batch;
@@ -254,14 +277,15 @@ enum km_req_kind {
   KM_REQ_NLL_GRAD = 0,   /* negloglik (+ stochastic gradient when nprobe > 0) of `prob`        */
   KM_REQ_FACTOR = 1,     /* assemble + factorise `prob` and keep the factor resident          */
   KM_REQ_SOLVE = 2,      /* x = K^{-1} b with the resident factor `factor_id` (nrhs columns)  */
-  KM_REQ_RELEASE = 3     /* drop the resident factor `factor_id`                               */
+  KM_REQ_RELEASE = 3,    /* drop the resident factor `factor_id`                               */
+  KM_REQ_PROFILE_NLL_GRAD = 4 /* profile_negloglik (+ stoch_profile_gradient) of `prob`       */
 };
 
 typedef struct km_request {
   int kind;              /* enum km_req_kind                                                  */
-  km_problem prob;       /* NLL_GRAD, FACTOR                                                  */
-  int64_t nprobe;        /* NLL_GRAD                                                          */
-  uint64_t probe_seed;   /* NLL_GRAD                                                          */
+  km_problem prob;       /* NLL_GRAD, PROFILE_NLL_GRAD, FACTOR                                */
+  int64_t nprobe;        /* NLL_GRAD, PROFILE_NLL_GRAD                                        */
+  uint64_t probe_seed;   /* NLL_GRAD, PROFILE_NLL_GRAD                                        */
   int64_t factor_id;     /* SOLVE, RELEASE                                                    */
   const double* b;       /* SOLVE: n x nrhs right-hand sides (host, column-major)              */
   double* x;             /* SOLVE: n x nrhs solutions (host, column-major)                     */

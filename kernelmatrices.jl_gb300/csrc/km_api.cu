@@ -152,6 +152,7 @@ struct km_handle {
   double* d_U = nullptr;
   double* d_dots = nullptr;
   int64_t tcap = 0;
+  double* d_A = nullptr;     // Fisher: W^{-1} dK_j W'^{-1} V for the three parameters (3 n x p)
   double* d_res = nullptr;   // refinement residual (n x rcap)
   double* d_rdots = nullptr;
   int64_t rcap = 0;
@@ -279,7 +280,7 @@ void free_problem(km_handle* h) {
   h->d_pqs = nullptr;
   h->d_acascr = nullptr;
   h->dk_param = -1;
-  h->d_dK = h->d_dPhi = h->d_Sj = h->d_GP = h->d_GG = h->d_T = h->d_U = h->d_dots = nullptr;
+  h->d_dK = h->d_dPhi = h->d_Sj = h->d_GP = h->d_GG = h->d_T = h->d_U = h->d_dots = h->d_A = nullptr;
   h->d_dKf = h->d_dPhif = h->d_Phif = nullptr;
   h->d_Sinv = h->d_SinvF = h->d_M2 = h->d_M2F = h->d_Mtmp = h->d_GB = nullptr;
   h->gcap = h->tcap = 0;
@@ -1544,9 +1545,17 @@ int km_derivative_matvec(km_handle* h, int param, const double* x, double* y, in
 //   g_j = 0.5 (mean_v t_v' dK_j t_v - alpha' dK_j alpha).
 // The data term y' K^{-1} dK_j K^{-1} y of HODLR_grad_term (stochasticgradient.jl:22-25) is
 // evaluated as alpha' dK_j alpha, which is the same quantity since K^{-1} is symmetric.
+// With `profile` the scale is profiled out (profile_negloglik, maxlikfunctions.jl:11-19;
+// HODLR_p_grad_term, stochasticgradient.jl:48-64): nll = 0.5 (logdet K + n log(y' alpha)) and
+// g_j = 0.5 (mean_v t_v' dK_j t_v - n alpha' dK_j alpha / y' alpha), from the same solves.
+// With `fisher` the stochastic Fisher matrix of stoch_fisher (stochastichessian.jl:91-115) and
+// grad_and_fisher_matrix (:152-181) is formed from the same probes: A_j = W^{-1} dK_j T,
+// F_jk = 0.5 mean_v (A_j v)'(A_k v).  The reference forms the off-diagonal entries by
+// polarisation, 0.5 (0.5 mean |A_j v + A_k v|^2 - F_jj - F_kk), which is the same quantity.
 static int nll_grad_impl(km_handle* h, const double* y, const double* probes, bool seeded, uint64_t seed,
-                         int64_t nprobe, double* nll, double* grad) {
-  if (!h || !y || !nll || nprobe < 0 || (grad && (nprobe < 1 || (!probes && !seeded))))
+                         int64_t nprobe, double* nll, double* grad, bool profile = false,
+                         double* fisher = nullptr) {
+  if (!h || !y || !nll || nprobe < 0 || (grad && (nprobe < 1 || (!probes && !seeded))) || (fisher && !grad))
     return fail(h, KM_ERR_BAD_ARG, "bad likelihood arguments");
   cudaSetDevice(h->cfg.device);
   if (!h->factorized) return fail(h, KM_ERR_STATE, "The HODLR matrix needs to be factorized for this.");
@@ -1581,22 +1590,45 @@ static int nll_grad_impl(km_handle* h, const double* y, const double* probes, bo
   if ((rc = sync(h, "nll")) != KM_OK) return rc;
   double ya = 0.0;
   for (int64_t i = 0; i < n; ++i) ya += y[i] * a[i];
-  *nll = 0.5 * ld + 0.5 * ya;
+  if (profile && !(ya > 0.0)) return fail(h, KM_ERR_BAD_ARG, "y' K^-1 y is not positive (zero data?)");
+  *nll = profile ? 0.5 * (ld + (double)n * std::log(ya)) : 0.5 * ld + 0.5 * ya;
   if (grad) {
     if (seeded)
       KLV(h, KM_PROF_OTHER, launch_rademacher(h->d_T, n, p, seed, st));
     else
       KM_CUDA(h, cudaMemcpyAsync(h->d_T, probes, sizeof(double) * n * p, cudaMemcpyHostToDevice, st));
     if ((rc = nested_bwd(h, h->d_T, (int)p)) != KM_OK) return rc;  // T = W'^{-1} V
+    if (fisher && (rc = grow(h, &h->d_A, 3 * n * p + 6 * p)) != KM_OK) return rc;  // + pairwise dots
     std::vector<double> dots(kk);
     for (int j = 0; j < 3; ++j) {
       if ((rc = derivative_apply(h, j, h->d_T, h->d_U, (int)kk)) != KM_OK) return rc;
       KLV(h, KM_PROF_OTHER, launch_col_dots(h->d_T, n, h->d_U, n, n, (int)kk, h->d_dots, st));
       KM_CUDA(h, cudaMemcpyAsync(dots.data(), h->d_dots, sizeof(double) * kk, cudaMemcpyDeviceToHost, st));
+      if (fisher) {
+        double* Aj = h->d_A + (int64_t)j * n * p;
+        KM_CUDA(h, cudaMemcpyAsync(Aj, h->d_U, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, st));
+        if ((rc = nested_fwd(h, Aj, (int)p)) != KM_OK) return rc;  // A_j = W^{-1} dK_j T
+      }
       if ((rc = sync(h, "grad")) != KM_OK) return rc;
       double tr = 0.0;
       for (int64_t c = 0; c < p; ++c) tr += dots[c];
-      grad[j] = 0.5 * (tr / (double)p - dots[p]);
+      grad[j] = 0.5 * (tr / (double)p - (profile ? (double)n * dots[p] / ya : dots[p]));
+    }
+    if (fisher) {
+      std::vector<double> fd(6 * p);
+      double* d_fd = h->d_A + 3 * n * p;
+      for (int j = 0, q = 0; j < 3; ++j)
+        for (int k = j; k < 3; ++k, ++q)
+          KLV(h, KM_PROF_OTHER, launch_col_dots(h->d_A + (int64_t)j * n * p, n, h->d_A + (int64_t)k * n * p, n, n,
+                                                (int)p, d_fd + q * p, st));
+      KM_CUDA(h, cudaMemcpyAsync(fd.data(), d_fd, sizeof(double) * 6 * p, cudaMemcpyDeviceToHost, st));
+      if ((rc = sync(h, "fisher")) != KM_OK) return rc;
+      for (int j = 0, q = 0; j < 3; ++j)
+        for (int k = j; k < 3; ++k, ++q) {
+          double m = 0.0;
+          for (int64_t c = 0; c < p; ++c) m += fd[q * p + c];
+          fisher[3 * j + k] = fisher[3 * k + j] = 0.5 * m / (double)p;
+        }
     }
   }
   h->stats.grad_ms = timer_stop(h);
@@ -1611,6 +1643,28 @@ int km_nll_grad(km_handle* h, const double* y, const double* probes, int64_t npr
 int km_nll_grad_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed, double* nll,
                        double* grad) {
   return nll_grad_impl(h, y, nullptr, true, seed, nprobe, nll, grad);
+}
+
+int km_grad_fisher(km_handle* h, const double* y, const double* probes, int64_t nprobe, double* nll,
+                   double* grad, double* fisher) {
+  if (!fisher) return fail(h, KM_ERR_BAD_ARG, "bad likelihood arguments");
+  return nll_grad_impl(h, y, probes, false, 0, nprobe, nll, grad, false, fisher);
+}
+
+int km_grad_fisher_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed, double* nll,
+                          double* grad, double* fisher) {
+  if (!fisher) return fail(h, KM_ERR_BAD_ARG, "bad likelihood arguments");
+  return nll_grad_impl(h, y, nullptr, true, seed, nprobe, nll, grad, false, fisher);
+}
+
+int km_profile_nll_grad(km_handle* h, const double* y, const double* probes, int64_t nprobe, double* nll,
+                        double* grad) {
+  return nll_grad_impl(h, y, probes, false, 0, nprobe, nll, grad, true);
+}
+
+int km_profile_nll_grad_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed, double* nll,
+                               double* grad) {
+  return nll_grad_impl(h, y, nullptr, true, seed, nprobe, nll, grad, true);
 }
 
 }  // extern "C"

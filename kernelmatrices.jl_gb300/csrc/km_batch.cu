@@ -56,14 +56,15 @@ extern "C" int km_batch_destroy(km_batch* b) {
 
 extern "C" const char* km_batch_last_error(const km_batch* b) { return b ? b->err.c_str() : "null batch"; }
 
-// one problem on one handle: assemble, factorise, NLL (+ gradient)
+// one problem on one handle: assemble, factorise, NLL (+ gradient), or their profile forms
 static int run_problem(km_handle* h, const km_batch_opts& o, const km_problem& p, uint64_t seed, double* nll,
                        double* grad) {
   int rc = km_assemble(h, p.pts, p.n, o.kernel_id, p.params, 3, KM_METHOD_NYSTROM, 0.0, o.rank, o.level_kind,
                        o.level);
   if (rc != KM_OK) return rc;
   if ((rc = km_factorize(h)) != KM_OK) return rc;
-  return km_nll_grad_seeded(h, p.y, o.nprobe, seed, nll, o.nprobe > 0 ? grad : nullptr);
+  return (o.profile ? km_profile_nll_grad_seeded : km_nll_grad_seeded)(h, p.y, o.nprobe, seed, nll,
+                                                                        o.nprobe > 0 ? grad : nullptr);
 }
 
 extern "C" int km_batch_nll_grad(km_batch* b, const km_batch_opts* o, int64_t nprob, const km_problem* probs,

@@ -111,6 +111,9 @@ void finish(km_server* s, const Job& j, km_result r, bool rejected = false) {
   s->cv_done.notify_all();
 }
 
+// likelihood requests: assemble + factorise + (profile) NLL and gradient on an executor's handle
+inline bool is_lik(int kind) { return kind == KM_REQ_NLL_GRAD || kind == KM_REQ_PROFILE_NLL_GRAD; }
+
 // runs one admitted job outside the lock; returns the result
 km_result execute(km_server* s, Executor* e, Job& j, Factor* f) {
   km_result r{};
@@ -118,12 +121,14 @@ km_result execute(km_server* s, Executor* e, Job& j, Factor* f) {
   const km_request& q = j.req;
   const km_serve_opts& o = s->o;
   switch (q.kind) {
-    case KM_REQ_NLL_GRAD: {
+    case KM_REQ_NLL_GRAD:
+    case KM_REQ_PROFILE_NLL_GRAD: {
       int rc = km_assemble(e->h, q.prob.pts, q.prob.n, o.kernel_id, q.prob.params, 3, KM_METHOD_NYSTROM, 0.0, o.rank,
                            o.level_kind, o.level);
       if (rc == KM_OK) rc = km_factorize(e->h);
       if (rc == KM_OK)
-        rc = km_nll_grad_seeded(e->h, q.prob.y, q.nprobe, q.probe_seed, &r.nll, q.nprobe > 0 ? r.grad : nullptr);
+        rc = (q.kind == KM_REQ_PROFILE_NLL_GRAD ? km_profile_nll_grad_seeded : km_nll_grad_seeded)(
+            e->h, q.prob.y, q.nprobe, q.probe_seed, &r.nll, q.nprobe > 0 ? r.grad : nullptr);
       r.status = rc;
       break;
     }
@@ -182,7 +187,7 @@ void executor_loop(km_server* s, Executor* e) {
     lk.unlock();
     km_result r = execute(s, e, j, f);
     int64_t held = e->held;
-    if (j.req.kind == KM_REQ_NLL_GRAD) {
+    if (is_lik(j.req.kind)) {
       km_stats st{};
       km_get_stats(e->h, &st);
       held = st.device_bytes;
@@ -218,6 +223,7 @@ int64_t estimate(km_server* s, const km_request& q, Factor* f) {
   const km_serve_opts& o = s->o;
   switch (q.kind) {
     case KM_REQ_NLL_GRAD:
+    case KM_REQ_PROFILE_NLL_GRAD:
       return km_estimate_bytes(q.prob.n, o.rank, o.level_kind, o.level, q.nprobe + 1, q.nprobe > 0);
     case KM_REQ_FACTOR:
       return km_estimate_bytes(q.prob.n, o.rank, o.level_kind, o.level, 1, 0);
@@ -276,7 +282,7 @@ void scheduler_loop(km_server* s) {
         continue;
       }
       // the executor's idle buffers are reused by an NLL request
-      const bool uses_exec_mem = q.kind == KM_REQ_NLL_GRAD;
+      const bool uses_exec_mem = is_lik(q.kind);
       auto fits = [&] {
         const int64_t base = in_use(s) - (uses_exec_mem ? e->held : 0);
         return base + (uses_exec_mem ? std::max(need, e->held) : need) <= s->budget;
@@ -370,8 +376,8 @@ extern "C" int km_serve_create(const km_config* cfg, const km_serve_opts* o, km_
 extern "C" int km_serve_submit(km_server* s, const km_request* r, uint64_t* ticket) {
   if (!s || !r || !ticket) return KM_ERR_BAD_ARG;
   const km_request& q = *r;
-  if (q.kind == KM_REQ_NLL_GRAD || q.kind == KM_REQ_FACTOR) {
-    if (!q.prob.pts || q.prob.n < 1 || (q.kind == KM_REQ_NLL_GRAD && (!q.prob.y || q.nprobe < 0)))
+  if (is_lik(q.kind) || q.kind == KM_REQ_FACTOR) {
+    if (!q.prob.pts || q.prob.n < 1 || (is_lik(q.kind) && (!q.prob.y || q.nprobe < 0)))
       return KM_ERR_BAD_ARG;
   } else if (q.kind == KM_REQ_SOLVE) {
     if (!q.b || !q.x || q.nrhs < 1) return KM_ERR_BAD_ARG;

@@ -7,6 +7,8 @@
 #   mul!, *, ldiv!, \, logdet                          src/HODLR/src/baseoverloads.jl:152-263
 #   ldiv!(t, K.W, v), ldiv!(t, K.W', v), mul!(t, K.W, v) baseoverloads.jl:95-150
 #   HODLR.stoch_gradient, HODLR.negloglik             stochasticgradient.jl:30-44, maxlikfunctions.jl:2-9
+#   HODLR.stoch_profile_gradient, profile_negloglik   stochasticgradient.jl:68-86, maxlikfunctions.jl:11-19
+#   grad_and_fisher_matrix, stoch_fisher              stochastichessian.jl:91-115,152-181
 #
 # Kernels are callable structs, so the same object runs in the reference's CPU path
 # (k(x, y, p) like any kernel function) and is recognised by type here.
@@ -157,6 +159,39 @@ function stoch_gradient(K::GPUKernelHODLR, dat::Vector{Float64}, vecs::Vector{Ve
   return grad
 end
 
+# profile_negloglik (maxlikfunctions.jl:11-19) and stoch_profile_gradient
+# (stochasticgradient.jl:68-86): the scale parameter profiled out.
+function profile_negloglik(K::GPUKernelHODLR, dat::Vector{Float64})
+  nll = Ref{Cdouble}(0.0)
+  check(K.h, ccall((:km_profile_nll_grad, libkm), Cint,
+                   (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Cdouble}, Ptr{Cdouble}),
+                   K.h, dat, C_NULL, 0, nll, C_NULL))
+  return nll[]
+end
+
+function stoch_profile_gradient(K::GPUKernelHODLR, dat::Vector{Float64}, vecs::Vector{Vector{Float64}})
+  probes = reduce(hcat, vecs)
+  nll = Ref{Cdouble}(0.0)
+  grad = zeros(3)
+  check(K.h, ccall((:km_profile_nll_grad, libkm), Cint,
+                   (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Cdouble}, Ptr{Cdouble}),
+                   K.h, dat, probes, size(probes, 2), nll, grad))
+  return grad
+end
+
+# grad_and_fisher_matrix (stochastichessian.jl:152-181) / stoch_fisher (:91-115) on a factorised
+# GPU HODLR: (nll, gradient, 3 x 3 Fisher matrix) from one set of probes.
+function grad_and_fisher(K::GPUKernelHODLR, dat::Vector{Float64}, vecs::Vector{Vector{Float64}})
+  probes = reduce(hcat, vecs)
+  nll = Ref{Cdouble}(0.0)
+  grad = zeros(3)
+  fisher = zeros(3, 3)
+  check(K.h, ccall((:km_grad_fisher, libkm), Cint,
+                   (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                   K.h, dat, probes, size(probes, 2), nll, grad, fisher))
+  return nll[], grad, Symmetric(fisher)
+end
+
 # ---- batched form: nll_objective over many independent datasets ------------------------------
 struct KmProblem
   n::Int64
@@ -172,19 +207,21 @@ struct KmBatchOpts
   level::Int64
   nprobe::Int64
   probe_seed::UInt64
+  profile::Cint
 end
 
 # One call for many (points, data, parameters) triples; returns (nll, grad (3 x m), status).
 # Probes are drawn on the device (problem b uses seed + b).
 function batch_nll_grad(pts::Vector{Vector{SVector{2,Float64}}}, dat::Vector{Vector{Float64}},
                         prms::Vector{NTuple{3,Float64}}, kernel, rank::Int64, lvl::HierLevel;
-                        nprobe::Int64=72, seed::UInt64=UInt64(0), nworkers::Int=8, precision::Int=0)
+                        nprobe::Int64=72, seed::UInt64=UInt64(0), nworkers::Int=8, precision::Int=0,
+                        profile::Bool=false)
   m = length(pts)
   b = Ref{Ptr{Cvoid}}(C_NULL)
   cfg = Ref(KmConfig(0, Cint(precision), 0.8, 0, 0.0))
   check(C_NULL, ccall((:km_batch_create, libkm), Cint, (Ptr{KmConfig}, Cint, Ptr{Ptr{Cvoid}}), cfg, nworkers, b))
   kind, lv = lvl isa HODLR.FixedLevel ? (Cint(0), Int64(lvl.lv)) : (Cint(1), Int64(lvl.lv))
-  opts = Ref(KmBatchOpts(kernel_id(kernel), rank, kind, lv, nprobe, seed))
+  opts = Ref(KmBatchOpts(kernel_id(kernel), rank, kind, lv, nprobe, seed, Cint(profile)))
   probs = [KmProblem(length(pts[i]), pointer(pts[i]), pointer(dat[i]), prms[i]) for i in 1:m]
   nll = zeros(m); grad = zeros(3, m); status = zeros(Cint, m)
   GC.@preserve pts dat begin

@@ -8,6 +8,7 @@ from .hodlr import (  # noqa: F401
     FixedLevel, LogLevel, KernelMatrix, KernelHODLR, RatQuad, Matern32, HODLRindices,
     KMError, PosDefException, symmetricfactorize, logdet, nystrom_landmarks, probe_fp64_tflops,
     probe_fp32_tflops,
-    negloglik, stoch_gradient, nll_objective,
+    negloglik, stoch_gradient, nll_objective, profile_negloglik, stoch_profile_gradient, nlpl_objective,
+    scaleparm_mle, gpsimulate, stoch_fisher, grad_and_fisher, grad_and_fisher_matrix,
 )
 from .serving import BatchEngine, Server, Problem, Result, estimate_bytes  # noqa: F401

@@ -49,6 +49,7 @@ KM_REQ_NLL_GRAD = 0
 KM_REQ_FACTOR = 1
 KM_REQ_SOLVE = 2
 KM_REQ_RELEASE = 3
+KM_REQ_PROFILE_NLL_GRAD = 4
 
 
 class KmProblem(C.Structure):
@@ -58,7 +59,7 @@ class KmProblem(C.Structure):
 
 class KmBatchOpts(C.Structure):
     _fields_ = [("kernel_id", C.c_int), ("rank", C.c_int64), ("level_kind", C.c_int), ("level", C.c_int64),
-                ("nprobe", C.c_int64), ("probe_seed", C.c_uint64)]
+                ("nprobe", C.c_int64), ("probe_seed", C.c_uint64), ("profile", C.c_int)]
 
 
 class KmRequest(C.Structure):
@@ -124,6 +125,10 @@ SIGNATURES = {
     "km_profile_get": (C.c_int, [_H, C.c_int, _DP, _IP]),
     "km_solve_noalloc": (C.c_int, [_H, _P, _P, C.c_int64]),
     "km_nll_grad_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP]),
+    "km_profile_nll_grad": (C.c_int, [_H, _DP, _DP, C.c_int64, _DP, _DP]),
+    "km_grad_fisher": (C.c_int, [_H, _DP, _DP, C.c_int64, _DP, _DP, _DP]),
+    "km_grad_fisher_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP, _DP]),
+    "km_profile_nll_grad_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP]),
     "km_trim": (C.c_int, [_H]),
     "km_estimate_bytes": (C.c_int64, [C.c_int64, C.c_int64, C.c_int, C.c_int64, C.c_int64, C.c_int]),
     "km_batch_create": (C.c_int, [C.POINTER(KmConfig), C.c_int, C.POINTER(_P)]),

@@ -273,33 +273,49 @@ class KernelHODLR:
         _check(self._h, lib.km_derivative_matvec(self._h, int(param), _dp(b), _dp(out), b.shape[1]))
         return out.reshape(vec.shape)
 
-    def nll_grad(self, dat: np.ndarray, vecs=None):
+    def nll_grad(self, dat: np.ndarray, vecs=None, profile: bool = False):
         """(NLL, stochastic gradient or None): ``negloglik`` (maxlikfunctions.jl:2-9) and
-        ``stoch_gradient`` with shuffle = false (stochasticgradient.jl:30-44)."""
+        ``stoch_gradient`` with shuffle = false (stochasticgradient.jl:30-44); with ``profile``
+        ``profile_negloglik`` (maxlikfunctions.jl:11-19) and ``stoch_profile_gradient``
+        (stochasticgradient.jl:48-86)."""
         lib = L.load()
+        fn = lib.km_profile_nll_grad if profile else lib.km_nll_grad
         y = np.ascontiguousarray(dat, dtype=np.float64).reshape(-1)
         nll = C.c_double()
         if vecs is None:
-            _check(self._h, lib.km_nll_grad(self._h, _dp(y), None, 0, C.byref(nll), None))
+            _check(self._h, fn(self._h, _dp(y), None, 0, C.byref(nll), None))
             return nll.value, None
         V = np.asfortranarray(np.column_stack(vecs) if isinstance(vecs, (list, tuple)) else vecs,
                               dtype=np.float64)
         g = np.zeros(3)
-        _check(self._h, lib.km_nll_grad(self._h, _dp(y), _dp(V), V.shape[1], C.byref(nll), _dp(g)))
+        _check(self._h, fn(self._h, _dp(y), _dp(V), V.shape[1], C.byref(nll), _dp(g)))
         return nll.value, g
 
-
-    def nll_grad_seeded(self, dat: np.ndarray, nprobe: int, seed: int):
+    def nll_grad_seeded(self, dat: np.ndarray, nprobe: int, seed: int, profile: bool = False):
         """``nll_grad`` with ``nprobe`` Rademacher probes drawn on the device: entry (i, j) is +1
         when the top bit of SplitMix64(SplitMix64(seed) + j*n + i) is set, else -1 (stands in
         for ``givesaa(n, m; seed)``, src/utils.jl:22-27)."""
         lib = L.load()
+        fn = lib.km_profile_nll_grad_seeded if profile else lib.km_nll_grad_seeded
         y = np.ascontiguousarray(dat, dtype=np.float64).reshape(-1)
         nll = C.c_double()
         g = np.zeros(3)
-        _check(self._h, lib.km_nll_grad_seeded(self._h, _dp(y), int(nprobe), int(seed), C.byref(nll),
-                                               _dp(g) if nprobe > 0 else None))
+        _check(self._h, fn(self._h, _dp(y), int(nprobe), int(seed), C.byref(nll), _dp(g) if nprobe > 0 else None))
         return nll.value, (g if nprobe > 0 else None)
+
+
+def _grad_fisher(HK: "KernelHODLR", dat: np.ndarray, vecs=None, nprobe: int = 0, seed: int = 0):
+    lib = L.load()
+    y = np.ascontiguousarray(dat, dtype=np.float64).reshape(-1)
+    nll = C.c_double()
+    g = np.zeros(3)
+    F = np.zeros((3, 3), order="F")
+    if vecs is None:
+        _check(HK._h, lib.km_grad_fisher_seeded(HK._h, _dp(y), int(nprobe), int(seed), C.byref(nll), _dp(g), _dp(F)))
+    else:
+        V = np.asfortranarray(np.column_stack(vecs) if isinstance(vecs, (list, tuple)) else vecs, dtype=np.float64)
+        _check(HK._h, lib.km_grad_fisher(HK._h, _dp(y), _dp(V), V.shape[1], C.byref(nll), _dp(g), _dp(F)))
+    return nll.value, g, F
 
 
 def symmetricfactorize(K: KernelHODLR) -> None:
@@ -340,6 +356,84 @@ def nll_objective(prms, grad, pts: np.ndarray, dat: np.ndarray, kernel, rank: in
         grad[:] = g
         return nll
     return HK.nll_grad(dat)[0]
+
+
+def stoch_fisher(HK: KernelHODLR, vecs) -> np.ndarray:
+    """``stoch_fisher(K, HK, DKs, vecs)`` (src/HODLR/src/stochastichessian.jl:91-115) for the three
+    kernel parameters: F_jk = 0.5 mean_v (W^-1 dK_j W'^-1 v)'(W^-1 dK_k W'^-1 v)."""
+    if not HK.factorized:
+        raise KMError(L.KM_ERR_STATE, "The matrix needs to be factorized.")
+    return _grad_fisher(HK, np.ones(HK.n), vecs)[2]
+
+
+def grad_and_fisher(HK: KernelHODLR, dat: np.ndarray, vecs=None, nprobe: int = 0, seed: int = 0):
+    """(NLL, gradient, Fisher matrix) from one set of probes on a factorised Nystrom HODLR: the
+    per-matrix part of ``grad_and_fisher_matrix`` (stochastichessian.jl:152-181).  Probes are
+    ``vecs`` (host) or ``nprobe`` seeded Rademacher probes drawn on the device."""
+    if not HK.factorized:
+        raise KMError(L.KM_ERR_STATE, "The matrix needs to be factorized.")
+    return _grad_fisher(HK, dat, vecs, nprobe, seed)
+
+
+def grad_and_fisher_matrix(prms, pts: np.ndarray, dat: np.ndarray, kernel, rank: int, lvl, saav,
+                           device: int = 0):
+    """``grad_and_fisher_matrix(prm, data, opts)`` (stochastichessian.jl:152-181): assemble
+    (Nystrom, ep = 0), factorise, and return (gradient, Fisher matrix)."""
+    K = KernelMatrix(pts, pts, prms, kernel)
+    HK = KernelHODLR(K, 0.0, rank, lvl, nystrom=True, sorted=True, device=device)
+    symmetricfactorize(HK)
+    _, g, F = _grad_fisher(HK, dat, saav)
+    return g, F
+
+
+def profile_negloglik(HK: KernelHODLR, dat: np.ndarray) -> float:
+    """``profile_negloglik(HK, dat)`` (src/HODLR/src/maxlikfunctions.jl:11-19):
+    0.5*(logdet HK + n*log(dat' HK^-1 dat))."""
+    if not HK.factorized:
+        raise KMError(L.KM_ERR_STATE, "The HODLR matrix needs to be factorized for this.")
+    return HK.nll_grad(dat, profile=True)[0]
+
+
+def stoch_profile_gradient(HK: KernelHODLR, dat: np.ndarray, vecs) -> np.ndarray:
+    """``stoch_profile_gradient(K, HK, dat, dfuns, vecs)`` (stochasticgradient.jl:68-86)."""
+    if not HK.factorized:
+        raise KMError(L.KM_ERR_STATE, "The matrix needs to be factorized for this to work.")
+    return HK.nll_grad(dat, vecs, profile=True)[1]
+
+
+def nlpl_objective(prms, grad, pts: np.ndarray, dat: np.ndarray, kernel, rank: int, lvl, saav,
+                   device: int = 0) -> float:
+    """``nlpl_objective(prms, grad, data, opts)`` (maxlikfunctions.jl:61-82): ``nll_objective``
+    for the profile likelihood."""
+    K = KernelMatrix(pts, pts, prms, kernel)
+    HK = KernelHODLR(K, 0.0, rank, lvl, nystrom=True, sorted=True, device=device)
+    symmetricfactorize(HK)
+    if grad is not None and len(grad) > 0:
+        nll, g = HK.nll_grad(dat, saav, profile=True)
+        grad[:] = g
+        return nll
+    return HK.nll_grad(dat, profile=True)[0]
+
+
+def scaleparm_mle(prms, pts: np.ndarray, dat: np.ndarray, kernel, rank: int, lvl, device: int = 0) -> float:
+    """``scaleparm_mle`` / ``nlpl_scale`` (maxlikfunctions.jl:21-27,52-58): the profiled scale
+    dat' K^-1 dat / n of a freshly assembled and factorised Nystrom HODLR."""
+    K = KernelMatrix(pts, pts, prms, kernel)
+    HK = KernelHODLR(K, 0.0, rank, lvl, nystrom=True, sorted=True, device=device)
+    symmetricfactorize(HK)
+    y = np.ascontiguousarray(dat, dtype=np.float64).reshape(-1)
+    return float(np.dot(y, HK.ldiv(y))) / y.size
+
+
+def gpsimulate(kernel, pts: np.ndarray, parms, rank: int, lvl, z: np.ndarray, device: int = 0) -> np.ndarray:
+    """``gpsimulate(kernel, locs, parms, opts)`` HODLR branch (maxlikfunctions.jl:148-172):
+    out = W z with W the symmetric factor of the Nystrom HODLR (K ~ W W').  ``z`` is the
+    standard-normal input (the reference draws it with ``randn``); points are used in the
+    order given (k-d sort them first, as ``kdtreesort=true`` does)."""
+    K = KernelMatrix(pts, pts, parms, kernel)
+    HK = KernelHODLR(K, 0.0, rank, lvl, nystrom=True, device=device)
+    symmetricfactorize(HK)
+    return HK.W @ np.asarray(z, dtype=np.float64)
 
 
 def probe_fp32_tflops(device: int = 0) -> float:

@@ -81,12 +81,13 @@ class BatchEngine:
         self.close()
 
     def nll_grad(self, problems: List[Problem], kernel, rank: int, lvl, nprobe: int = 72, seed: int = 0,
-                 raise_on_error: bool = True):
-        """(nll[nprob], grad[nprob, 3] or None, status[nprob]); problem b uses probe seed seed + b."""
+                 raise_on_error: bool = True, profile: bool = False):
+        """(nll[nprob], grad[nprob, 3] or None, status[nprob]); problem b uses probe seed seed + b.
+        ``profile`` evaluates the profile likelihood (``nlpl_objective``) instead."""
         lib = L.load()
         kind, lv = _level(lvl)
         o = L.KmBatchOpts(kernel_id=int(getattr(kernel, "kid", kernel)), rank=int(rank), level_kind=kind,
-                          level=int(lv), nprobe=int(nprobe), probe_seed=int(seed))
+                          level=int(lv), nprobe=int(nprobe), probe_seed=int(seed), profile=int(bool(profile)))
         keep: list = []
         arr = (L.KmProblem * max(len(problems), 1))()
         for i, p in enumerate(problems):
@@ -141,9 +142,10 @@ class Server:
         self._keep[t.value] = keep
         return t.value
 
-    def submit_nll_grad(self, prob: Problem, nprobe: int = 72, seed: int = 0) -> int:
+    def submit_nll_grad(self, prob: Problem, nprobe: int = 72, seed: int = 0, profile: bool = False) -> int:
         keep: list = []
-        req = L.KmRequest(kind=L.KM_REQ_NLL_GRAD, nprobe=int(nprobe), probe_seed=int(seed))
+        req = L.KmRequest(kind=L.KM_REQ_PROFILE_NLL_GRAD if profile else L.KM_REQ_NLL_GRAD, nprobe=int(nprobe),
+                          probe_seed=int(seed))
         req.prob = prob._c(keep)
         return self._submit(req, (keep, None))
 

@@ -758,6 +758,105 @@ def nll_objective(prms, grad: Optional[np.ndarray], pts: np.ndarray, dat: np.nda
     return nll
 
 
+def profile_negloglik(HK: KernelHODLR, dat: np.ndarray) -> float:
+    """``profile_negloglik`` (src/HODLR/src/maxlikfunctions.jl:11-19): the NLL with the scale
+    parameter profiled out, 0.5*(logdet K + n*log(y' K^-1 y))."""
+    if HK.U is not None:
+        raise RuntimeError("The HODLR matrix needs to be factorized for this.")
+    return 0.5 * (hodlr_logdet(HK) + len(dat) * np.log(float(np.dot(dat, hodlr_ldiv(HK, dat)))))
+
+
+def scaleparm_mle(HK: KernelHODLR, dat: np.ndarray) -> float:
+    """``scaleparm_mle`` / ``nlpl_scale`` (maxlikfunctions.jl:21-27,52-58) on a factorised
+    matrix: the profiled scale estimate y' K^-1 y / n."""
+    return float(np.dot(dat, hodlr_ldiv(HK, dat))) / len(dat)
+
+
+def hodlr_p_grad_term(K: KernelMatrix, HK: KernelHODLR, j: int, dat: np.ndarray, vecs) -> float:
+    """``HODLR_p_grad_term`` (stochasticgradient.jl:48-64)."""
+    DK = derivative_hodlr(K, j, HK)
+    prvec = hodlr_ldiv(HK, derivative_mul(DK, hodlr_ldiv(HK, dat)))
+    trtm = sum(hodlr_trace_apply(HK, DK, v) for v in vecs) / len(vecs)
+    return 0.5 * (trtm - len(dat) * float(np.dot(dat, prvec)) / float(np.dot(dat, hodlr_ldiv(HK, dat))))
+
+
+def stoch_profile_gradient(K: KernelMatrix, HK: KernelHODLR, dat: np.ndarray, nparams: int, vecs) -> np.ndarray:
+    """``stoch_profile_gradient`` (stochasticgradient.jl:68-86) with shuffle=false."""
+    if HK.U is not None:
+        raise RuntimeError("The matrix needs to be factorized for this to work.")
+    return np.array([hodlr_p_grad_term(K, HK, j, dat, vecs) for j in range(nparams)])
+
+
+def nlpl_objective(prms, grad: Optional[np.ndarray], pts: np.ndarray, dat: np.ndarray, kid: int,
+                   rank: int, lvl, saav) -> float:
+    """``nlpl_objective`` (maxlikfunctions.jl:61-82): ``nll_objective`` for the profile
+    likelihood."""
+    K = KernelMatrix(pts, pts, np.asarray(prms, dtype=np.float64), kid)
+    HK = build_hodlr(K, 0.0, rank, lvl, nystrom=True)
+    symmetricfactorize(HK)
+    nll = profile_negloglik(HK, dat)
+    if grad is not None and len(grad) > 0:
+        grad[:] = stoch_profile_gradient(K, HK, dat, len(grad), saav)
+    return nll
+
+
+def hess_tr1_sym_diag(HK: KernelHODLR, DKj: DerivativeHODLR, v: np.ndarray) -> float:
+    """``HODLR_hess_tr1_sym_diag`` (src/HODLR/src/stochastichessian.jl:58-66):
+    |W^-1 dK_j W'^-1 v|^2."""
+    tp2 = factor_ldiv(HK.W, derivative_mul(DKj, factor_ldiv_t(HK.W, v)))
+    return float(np.dot(tp2, tp2))
+
+
+def hess_tr1_sym_offdiag(HK: KernelHODLR, DKj: DerivativeHODLR, DKk: DerivativeHODLR, v: np.ndarray) -> float:
+    """``HODLR_hess_tr1_sym_offdiag`` (stochastichessian.jl:68-77): |W^-1 (dK_j + dK_k) W'^-1 v|^2."""
+    tp1 = factor_ldiv_t(HK.W, v)
+    tp2 = factor_ldiv(HK.W, derivative_mul(DKj, tp1) + derivative_mul(DKk, tp1))
+    return float(np.dot(tp2, tp2))
+
+
+def stoch_fisher(K: KernelMatrix, HK: KernelHODLR, DKs, vecs) -> np.ndarray:
+    """``stoch_fisher`` (stochastichessian.jl:91-115) with shuffle=false: diagonal first, then
+    the off-diagonal entries by polarisation."""
+    if HK.U is not None:
+        raise RuntimeError("The matrix needs to be factorized.")
+    m = len(DKs)
+    out = np.zeros((m, m))
+    for j in range(m):
+        out[j, j] = 0.5 * sum(hess_tr1_sym_diag(HK, DKs[j], v) for v in vecs) / len(vecs)
+    for j in range(m):
+        for k in range(j + 1, m):
+            tmp1 = 0.5 * sum(hess_tr1_sym_offdiag(HK, DKs[j], DKs[k], v) for v in vecs) / len(vecs)
+            out[j, k] = 0.5 * (tmp1 - out[j, j] - out[k, k])
+            out[k, j] = out[j, k]
+    return out
+
+
+def grad_and_fisher_matrix(prms, pts: np.ndarray, dat: np.ndarray, kid: int, rank: int, lvl, saav):
+    """``grad_and_fisher_matrix(prm, data, opts)`` (stochastichessian.jl:152-181): the
+    stochastic gradient and Fisher matrix of a freshly assembled Nystrom HODLR."""
+    K = KernelMatrix(pts, pts, np.asarray(prms, dtype=np.float64), kid)
+    HK = build_hodlr(K, 0.0, rank, lvl, nystrom=True)
+    symmetricfactorize(HK)
+    m = len(prms)
+    g = np.zeros(m)
+    F = np.zeros((m, m))
+    for j in range(m):
+        HKj = derivative_hodlr(K, j, HK)
+        trace_j = float(np.mean([hodlr_trace_apply(HK, HKj, v) for v in saav]))
+        g[j] = 0.5 * (trace_j - float(np.dot(dat, hodlr_ldiv(HK, derivative_mul(HKj, hodlr_ldiv(HK, dat))))))
+        for k in range(j, m):
+            HKk = derivative_hodlr(K, k, HK)
+            if k == j:
+                F[j, j] = 0.5 * float(np.mean([hess_tr1_sym_diag(HK, HKj, v) for v in saav]))
+            else:
+                F[j, k] = 0.25 * float(np.mean([hess_tr1_sym_offdiag(HK, HKj, HKk, v) for v in saav]))
+    for j in range(m):
+        for k in range(j + 1, m):
+            F[j, k] -= 0.5 * (F[j, j] + F[k, k])
+            F[k, j] = F[j, k]
+    return g, F
+
+
 # ----------------------------------------------------------------------------------------------
 # Dense oracle: src/HODLR/src/exactmaxlik.jl
 # ----------------------------------------------------------------------------------------------

@@ -74,6 +74,32 @@ def test_batch_equals_single_and_oracle(lib):
     eng.close()
 
 
+def test_profile_batch_and_serve_equal_single(lib):
+    """The profile form (nlpl_objective, maxlikfunctions.jl:61-82) through the batch and the
+    server equals a single handle bit for bit, in a mix with ordinary likelihood requests."""
+    import kmhodlr as K
+    lvl = K.LogLevel(8)
+    probs = problems([2048, 1024, 3000, 1500], seed=31)
+    eng = K.BatchEngine(nworkers=2)
+    nll, grad, status = eng.nll_grad(probs, K.Matern32(), RANK, lvl, nprobe=16, seed=400, profile=True)
+    assert np.all(status == 0)
+    ones = []
+    for b, p in enumerate(probs):
+        hk, _ = single(p, 0, 0, lvl)
+        ones.append(hk.nll_grad_seeded(p.y, 16, 400 + b, profile=True))
+        assert nll[b] == ones[b][0], b
+        assert np.array_equal(grad[b], ones[b][1]), b
+    eng.close()
+    srv = K.Server(K.Matern32(), RANK, lvl, nworkers=3)
+    tp = [srv.submit_nll_grad(p, nprobe=16, seed=400 + b, profile=True) for b, p in enumerate(probs)]
+    tn = [srv.submit_nll_grad(p, nprobe=16, seed=400 + b) for b, p in enumerate(probs)]
+    for b in range(len(probs)):
+        r = srv.wait(tp[b])
+        assert r.status == 0 and r.nll == ones[b][0] and np.array_equal(r.grad, ones[b][1])
+        assert srv.wait(tn[b]).nll != r.nll
+    srv.close()
+
+
 def test_batch_reports_failing_problem_and_continues(lib):
     import kmhodlr as K
     probs = problems([2048, 1500, 1024], seed=9)

@@ -71,3 +71,91 @@ def test_nll_objective_mirror(lib):
                            [V[:, c] for c in range(8)])
     assert abs(nll - nll0) < 1e-10 * abs(nll0)
     assert np.all(np.abs(grad - g0) <= 1e-6 * np.abs(g0) + 1e-8)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_profile_likelihood_and_gradient(lib, mixed):
+    """profile_negloglik / stoch_profile_gradient / nlpl_objective against the oracle with the
+    same probes, in the FP64 form (NLL rel 1e-12, gradient rel 1e-6) and the mixed form (NLL abs
+    1e-6 + rel 1e-9, gradient rel 1e-5)."""
+    import kmhodlr as K
+    from kmhodlr.data import rademacher, uniform_points
+    n, rank, level = 2048, 32, 3
+    pts = uniform_points(n, 12)
+    p = (1.0, 0.1, 1e-3)
+    y = np.random.default_rng(5).standard_normal(n)
+    V = rademacher(n, 16, 6)
+    vecs = [V[:, c] for c in range(V.shape[1])]
+    ok = O.KernelMatrix(pts, pts, np.array(p), O.KERNEL_MATERN32)
+    ohk = O.build_hodlr(ok, 0.0, rank, O.FixedLevel(level), nystrom=True)
+    O.symmetricfactorize(ohk)
+    prec = K.KM_PREC_MIXED if mixed else K.KM_PREC_FP64
+    hk = K.KernelHODLR(K.KernelMatrix(pts, pts, p, K.Matern32()), 0.0, rank, K.FixedLevel(level), nystrom=True,
+                       precision=prec)
+    K.symmetricfactorize(hk)
+    nll0 = O.profile_negloglik(ohk, y)
+    g0 = O.stoch_profile_gradient(ok, ohk, y, 3, vecs)
+    nll = K.profile_negloglik(hk, y)
+    g = K.stoch_profile_gradient(hk, y, V)
+    if mixed:
+        assert abs(nll - nll0) < 1e-6 + 1e-9 * abs(nll0)
+        assert np.all(np.abs(g - g0) <= 1e-5 * np.abs(g0) + 1e-6)
+    else:
+        assert abs(nll - nll0) < 1e-12 * abs(nll0)
+        assert np.all(np.abs(g - g0) <= 1e-6 * np.abs(g0) + 1e-8)
+        grad = np.zeros(3)
+        assert K.nlpl_objective(p, grad, pts, y, K.Matern32(), rank, K.FixedLevel(level), V) == nll
+        assert np.array_equal(grad, g)
+        ya = float(y @ O.hodlr_ldiv(ohk, y))
+        assert abs(K.scaleparm_mle(p, pts, y, K.Matern32(), rank, K.FixedLevel(level)) - ya / n) < 1e-12 * ya / n
+    with pytest.raises(K.KMError, match="not positive"):
+        K.profile_negloglik(hk, np.zeros(n))
+
+
+def test_gpsimulate_is_factor_product(lib):
+    """gpsimulate's HODLR branch (maxlikfunctions.jl:148-172) returns W z; W z has covariance
+    W W' = the HODLR matrix, and equals the oracle's factor product to rel 1e-10."""
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    n, rank, level = 2048, 32, 3
+    pts = uniform_points(n, 31)
+    p = (1.0, 0.1, 1e-3)
+    z = np.random.default_rng(8).standard_normal(n)
+    out = K.gpsimulate(K.Matern32(), pts, p, rank, K.FixedLevel(level), z)
+    ok = O.KernelMatrix(pts, pts, np.array(p), O.KERNEL_MATERN32)
+    ohk = O.build_hodlr(ok, 0.0, rank, O.FixedLevel(level), nystrom=True)
+    O.symmetricfactorize(ohk)
+    assert rel(out, O.factor_mul(ohk.W, z)) < 1e-10
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_grad_and_fisher(lib, mixed):
+    """km_grad_fisher against the oracle's stoch_fisher with the same probes (rel 1e-6 of the
+    largest entry in FP64, 1e-5 mixed); its gradient equals km_nll_grad's bit for bit, and the
+    seeded form equals the host-probe form with the same probes."""
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    n, rank, level = 2048, 32, 3
+    pts = uniform_points(n, 41)
+    p = (1.0, 0.1, 1e-3)
+    y = np.random.default_rng(9).standard_normal(n)
+    V = O.rademacher_probes(n, 12, 17)
+    vecs = [V[:, c] for c in range(V.shape[1])]
+    ok = O.KernelMatrix(pts, pts, np.array(p), O.KERNEL_MATERN32)
+    ohk = O.build_hodlr(ok, 0.0, rank, O.FixedLevel(level), nystrom=True)
+    O.symmetricfactorize(ohk)
+    F0 = O.stoch_fisher(ok, ohk, [O.derivative_hodlr(ok, j, ohk) for j in range(3)], vecs)
+    prec = K.KM_PREC_MIXED if mixed else K.KM_PREC_FP64
+    hk = K.KernelHODLR(K.KernelMatrix(pts, pts, p, K.Matern32()), 0.0, rank, K.FixedLevel(level), nystrom=True,
+                       precision=prec)
+    K.symmetricfactorize(hk)
+    nll, g, F = K.grad_and_fisher(hk, y, V)
+    assert np.array_equal(F, F.T)
+    assert np.max(np.abs(F - F0)) <= (1e-5 if mixed else 1e-6) * np.max(np.abs(F0))
+    nll1, g1 = hk.nll_grad(y, V)
+    assert nll == nll1 and np.array_equal(g, g1)
+    nll2, g2, F2 = K.grad_and_fisher(hk, y, nprobe=12, seed=17)
+    assert nll2 == nll and np.array_equal(g2, g) and np.array_equal(F2, F)
+    if not mixed:
+        g3, F3 = K.grad_and_fisher_matrix(p, pts, y, K.Matern32(), rank, K.FixedLevel(level), V)
+        assert np.array_equal(g3, g) and np.array_equal(F3, F)

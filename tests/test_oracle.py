@@ -131,3 +131,70 @@ def test_golden_fixtures_reproduce(case):
     O.symmetricfactorize(HK)
     assert abs(O.hodlr_logdet(HK) - float(d["logdet"])) < 1e-9
     assert rel(O.hodlr_ldiv(HK, d["rhs"]), d["solve"]) < 1e-12
+
+
+def test_profile_likelihood_identities():
+    """The profile NLL is the NLL minimised over a scale c of K (Nystrom HODLR(cK) = c HODLR(K)):
+    profile = min_c nll(cK) + n/2 (log n - 1), attained at c = y'K^-1y / n (scaleparm_mle).
+    The profile gradient differs from the NLL gradient (same probes) by 0.5 u_j (1 - n/q),
+    u_j = y'K^-1 dK_j K^-1 y, q = y'K^-1 y (stochasticgradient.jl:14-26 vs :48-64)."""
+    rng = np.random.default_rng(21)
+    n = 768
+    pts = kd(rng.uniform(size=(n, 2)))
+    p = np.array([1.0, 0.1, 1e-3])
+    y = rng.standard_normal(n)
+    K = O.KernelMatrix(pts, pts, p, O.KERNEL_MATERN32)
+    HK = O.build_hodlr(K, 0.0, 32, O.FixedLevel(2), nystrom=True)
+    O.symmetricfactorize(HK)
+    c = O.scaleparm_mle(HK, y)
+    Kc = O.KernelMatrix(pts, pts, p * np.array([c, 1.0, c]), O.KERNEL_MATERN32)
+    HKc = O.build_hodlr(Kc, 0.0, 32, O.FixedLevel(2), nystrom=True)
+    O.symmetricfactorize(HKc)
+    prof = O.profile_negloglik(HK, y)
+    assert abs(prof - (O.negloglik(HKc, y) + 0.5 * n * (np.log(n) - 1.0))) < 1e-9 * abs(prof)
+    for cc in (0.5 * c, 2.0 * c):
+        Kx = O.KernelMatrix(pts, pts, p * np.array([cc, 1.0, cc]), O.KERNEL_MATERN32)
+        HKx = O.build_hodlr(Kx, 0.0, 32, O.FixedLevel(2), nystrom=True)
+        O.symmetricfactorize(HKx)
+        assert O.negloglik(HKx, y) > O.negloglik(HKc, y)
+    vecs = O.givesaa(6, n, 3)
+    g = O.stoch_gradient(K, HK, y, 3, vecs)
+    gp = O.stoch_profile_gradient(K, HK, y, 3, vecs)
+    a = O.hodlr_ldiv(HK, y)
+    q = float(y @ a)
+    for j in range(3):
+        u = float(a @ O.derivative_mul(O.derivative_hodlr(K, j, HK), a))
+        assert abs(gp[j] - (g[j] + 0.5 * u * (1.0 - n / q))) < 1e-9 * (abs(gp[j]) + abs(u))
+
+
+def test_stochastic_fisher():
+    """stoch_fisher and grad_and_fisher_matrix agree (stochastichessian.jl:91-115,152-181); the
+    Fisher matrix is symmetric positive semi-definite, its off-diagonal polarisation equals
+    0.5 mean (A_j v)'(A_k v), and with many probes it approaches the exact HODLR Fisher matrix
+    0.5 tr(HK^-1 dHK_j HK^-1 dHK_k)."""
+    rng = np.random.default_rng(23)
+    n, rank, lvl = 512, 32, O.FixedLevel(2)
+    pts = kd(rng.uniform(size=(n, 2)))
+    p = np.array([1.0, 0.1, 1e-3])
+    y = rng.standard_normal(n)
+    K = O.KernelMatrix(pts, pts, p, O.KERNEL_MATERN32)
+    HK = O.build_hodlr(K, 0.0, rank, lvl, nystrom=True)
+    O.symmetricfactorize(HK)
+    DKs = [O.derivative_hodlr(K, j, HK) for j in range(3)]
+    vecs = O.givesaa(8, n, 5)
+    F = O.stoch_fisher(K, HK, DKs, vecs)
+    g2, F2 = O.grad_and_fisher_matrix(p, pts, y, O.KERNEL_MATERN32, rank, lvl, vecs)
+    assert np.allclose(F, F2, rtol=1e-12, atol=0)
+    assert np.allclose(g2, O.stoch_gradient(K, HK, y, 3, vecs), rtol=1e-12, atol=1e-12)
+    assert np.allclose(F, F.T) and np.all(np.linalg.eigvalsh(F) > -1e-9 * np.abs(F).max())
+    A = [np.column_stack([O.factor_ldiv(HK.W, O.derivative_mul(D, O.factor_ldiv_t(HK.W, v))) for v in vecs])
+         for D in DKs]
+    for j in range(3):
+        for k in range(3):
+            assert abs(F[j, k] - 0.5 * np.mean(np.sum(A[j] * A[k], axis=0))) < 1e-10 * abs(F).max()
+    HKf = O.hodlr_full(O.build_hodlr(K, 0.0, rank, lvl, nystrom=True))
+    D = [O.derivative_full(DK) for DK in DKs]
+    Si = np.linalg.inv(HKf)
+    Fex = np.array([[0.5 * np.trace(Si @ D[j] @ Si @ D[k]) for k in range(3)] for j in range(3)])
+    Fmc = O.stoch_fisher(K, HK, DKs, O.givesaa(300, n, 6))
+    assert np.all(np.abs(Fmc - Fex) < 0.15 * np.sqrt(np.outer(np.diag(Fex), np.diag(Fex))))
