@@ -37,7 +37,8 @@ enum { UP_PROJ = 0, UP_FWD = 1, UP_MULT = 2, UP_SUM = 3 };
 // down-sweep modes
 enum { DN_FWD = 0, DN_BWD = 1, DN_MUL = 2, DN_MULT = 3, DN_NYS = 4 };
 
-// sum_l a[l*sa] b[l], l < n, with four independent partial sums (ILP for float pairs)
+// sum_l a[l*sa] b[l], l < n, with four independent partial sums (ILP for float pairs; the
+// loads of the four terms are in flight together, which bounds these latency-bound sweeps)
 template <typename T>
 __device__ __forceinline__ T dot4(const T* __restrict__ a, int sa, const T* __restrict__ b, int n) {
   T s0 = T(0.0), s1 = T(0.0), s2 = T(0.0), s3 = T(0.0);

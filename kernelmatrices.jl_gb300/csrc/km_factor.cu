@@ -58,9 +58,9 @@ __global__ void k_chol_small(double* __restrict__ A, int n, int* __restrict__ in
 // The current column panel (rows below the diagonal block) lives in shared memory.
 // info[j] = first failing column (1-based) of leaf j, 0 if positive definite.
 // ---------------------------------------------------------------------------------------------
-template <typename T, int NB>
-__global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K, T* __restrict__ Lf,
-                                                   DTree t, int* __restrict__ info) {
+template <typename T, int NB, int NT>
+__global__ void __launch_bounds__(NT) k_leaf_chol(const double* __restrict__ K, T* __restrict__ Lf,
+                                                  DTree t, int* __restrict__ info) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
   const int64_t leaf = blockIdx.x;
@@ -112,9 +112,9 @@ __global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K,
 #pragma unroll
       for (int c = 0; c < NB; ++c) {
         if (c < kb) {
-          T v = A[(int64_t)(k0 + c) * m + i];
+          acc_t<T> v = A[(int64_t)(k0 + c) * m + i];
           for (int l = 0; l < c; ++l) v -= x[l] * D[c * LDP + l];
-          x[c] = v / D[c * LDP + c];
+          x[c] = accv(v) / D[c * LDP + c];
         }
       }
 #pragma unroll
@@ -133,10 +133,10 @@ __global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K,
       for (int l = 0; l < NB; ++l) pc[l] = (l < kb) ? P[cc * LDP + l] : T(0.0);
       T* col = A + (int64_t)(r0 + cc) * m + r0;
       for (int ii = cc + lane; ii < mr; ii += 32) {
-        T acc = T(0.0);
+        acc_t<T> acc{};
 #pragma unroll
         for (int l = 0; l < NB; ++l) acc += P[ii * LDP + l] * pc[l];
-        col[ii] -= acc;
+        col[ii] -= accv(acc);
       }
     }
     __syncthreads();
@@ -152,12 +152,19 @@ __global__ void __launch_bounds__(256) k_leaf_chol(const double* __restrict__ K,
 // v = x/(alpha-beta); a zero column x gives tau = 0 (H = I).  One CTA per leaf; the panel is
 // copied to shared memory when it fits.
 // ---------------------------------------------------------------------------------------------
+// One CTA per leaf.  With float pairs it has 1024 threads: the panel (up to 200 KB of shared
+// memory) admits one CTA per SM, so the CTA takes all the warps the SM can hold to hide the
+// latency of the float-pair dot products.  The FP64 kernel is bound by the FP64 pipe and keeps
+// 256 threads (and the registers that go with them).
+template <typename T>
+constexpr int leaf_qr_threads() { return std::is_same<T, double>::value ? 256 : 1024; }
+
 template <typename T, bool SMEM>
-__global__ void __launch_bounds__(256) k_leaf_qr(T* __restrict__ Pan, int r, DTree t,
-                                                 T* __restrict__ tau, T* __restrict__ Rout) {
+__global__ void __launch_bounds__(leaf_qr_threads<T>()) k_leaf_qr(T* __restrict__ Pan, int r, DTree t,
+                                                                 T* __restrict__ tau, T* __restrict__ Rout) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
-  __shared__ T red[8];
+  __shared__ T red[32];
   __shared__ T sh_tau;
   const int64_t leaf = blockIdx.x;
   const int m = d_leaf_size(t, leaf);
@@ -225,7 +232,8 @@ __global__ void __launch_bounds__(256) k_leaf_qr(T* __restrict__ Pan, int r, DTr
 // Explicit leaf basis Q = H_0 ... H_{r-1} [I; 0] in place of the reflectors (LAPACK dorg2r).
 // Runs on the side stream, overlapped with the node levels (only the solves need Q).
 template <typename T, bool SMEM>
-__global__ void __launch_bounds__(256) k_leaf_formq(T* __restrict__ Pan, const T* __restrict__ tau, int r, DTree t) {
+__global__ void __launch_bounds__(leaf_qr_threads<T>()) k_leaf_formq(T* __restrict__ Pan, const T* __restrict__ tau,
+                                                                     int r, DTree t) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
   const int64_t leaf = blockIdx.x;
@@ -277,12 +285,12 @@ __global__ void __launch_bounds__(256) k_leaf_formq(T* __restrict__ Pan, const T
 // Outputs per node: Ct, L22 (lower), Eref (r x r), Etau (r), R_N into slot N.
 //
 // Work mapping: the products are split into (column c, 32-row chunk s) items, one warp per
-// item, lane = row, so that no index needs a division by r and the warps stay converged.  The
-// Cholesky factorises without scaling inside the loop (a_ik -= a_ij a_kj / d_j, one barrier per
-// column; the columns are scaled by sqrt(d_j) at the end), the triangular solve keeps each
-// right-hand-side column in the registers of one warp (no barriers), and every warp forms the
-// norm of the next reflector itself, so the QR needs one barrier per reflector.
-// Shared memory: four r x (r+1) matrices and two r-vectors.
+// item, lane = row, so that no index needs a division by r and the warps stay converged; sums
+// use the Dot2 accumulator (km_ff.cuh).  The Cholesky runs in dataflow order over columns (one
+// warp per column, shared-memory flags instead of block barriers), L22^{-1} B is then solved by
+// blocks of 8 rows with all threads, and the QR is a dataflow pipeline in which each warp owns
+// four columns and forms their reflectors itself.
+// Shared memory: four r x (r+1) matrices, three r-vectors and r + 1 flags.
 // ---------------------------------------------------------------------------------------------
 // Iteration bound of a spin wait on a shared-memory flag (a few tens of cycles per iteration:
 // well above any legitimate wait inside one node, far below a watchdog).  The spin does not
@@ -331,40 +339,40 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
   // T1 = R1 Sc^{-T} -> X3: T1[i][c] = sum_{l = i..c} R1[i][l] Sinv[l][c]
   for (int q = w; q < nitems; q += nw) {
     const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
-    T a0 = T(0.0), a1 = T(0.0);
+    acc_t<T> a0{}, a1{};
     int l = 32 * s;
     for (; l + 1 <= c; l += 2) {
       a0 += sel(l >= i, X1[ii + l * ld]) * X0[l + c * ld];
       a1 += sel(l + 1 >= i, X1[ii + (l + 1) * ld]) * X0[l + 1 + c * ld];
     }
     if (l <= c) a0 += sel(l >= i, X1[ii + l * ld]) * X0[l + c * ld];
-    if (i < r) X3[i + c * ld] = a0 + a1;
+    if (i < r) X3[i + c * ld] = accv(a0) + accv(a1);
   }
   __syncthreads();
   // T2 = R2 Sc^{-T} -> X1
   for (int q = w; q < nitems; q += nw) {
     const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
-    T a0 = T(0.0), a1 = T(0.0);
+    acc_t<T> a0{}, a1{};
     int l = 32 * s;
     for (; l + 1 <= c; l += 2) {
       a0 += sel(l >= i, X2[ii + l * ld]) * X0[l + c * ld];
       a1 += sel(l + 1 >= i, X2[ii + (l + 1) * ld]) * X0[l + 1 + c * ld];
     }
     if (l <= c) a0 += sel(l >= i, X2[ii + l * ld]) * X0[l + c * ld];
-    if (i < r) X1[i + c * ld] = a0 + a1;
+    if (i < r) X1[i + c * ld] = accv(a0) + accv(a1);
   }
   __syncthreads();
   // Ct = T1 T2' -> X0: Ct[i][c] = sum_{l >= max(i, c)} T1[i][l] T2[c][l]
   for (int q = w; q < nitems; q += nw) {
     const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
-    T a0 = T(0.0), a1 = T(0.0);
+    acc_t<T> a0{}, a1{};
     int l = max(32 * s, c);
     for (; l + 1 < r; l += 2) {
       a0 += sel(l >= i, X3[ii + l * ld]) * X1[c + l * ld];
       a1 += sel(l + 1 >= i, X3[ii + (l + 1) * ld]) * X1[c + (l + 1) * ld];
     }
     if (l < r) a0 += sel(l >= i, X3[ii + l * ld]) * X1[c + l * ld];
-    if (i < r) X0[i + c * ld] = a0 + a1;
+    if (i < r) X0[i + c * ld] = accv(a0) + accv(a1);
   }
   __syncthreads();
   // H = I - Ct' Ct -> X3 (lower triangle); R1 is reloaded into X1 for the QR meanwhile
@@ -374,49 +382,47 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
   for (int q = w; q < nitems; q += nw) {
     const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
     if (32 * s + 31 < c) continue;
-    T a0 = T(0.0), a1 = T(0.0);
+    acc_t<T> a0{}, a1{};
     int l = 0;
     for (; l + 1 < r; l += 2) {
       a0 += X0[l + ii * ld] * X0[l + c * ld];
       a1 += X0[l + 1 + ii * ld] * X0[l + 1 + c * ld];
     }
     if (l < r) a0 += X0[l + ii * ld] * X0[l + c * ld];
-    if (i < r && i >= c) X3[i + c * ld] = (i == c ? T(1.0) : T(0.0)) - (a0 + a1);
+    if (i < r && i >= c) X3[i + c * ld] = (i == c ? T(1.0) : T(0.0)) - (accv(a0) + accv(a1));
   }
   // B = R2 - Ct' R1 -> X2 (column c of R1 has entries l <= c; R1 read from global memory)
   if (level < L)
     for (int q = w; q < nitems; q += nw) {
       const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
       const T* r1 = R1 + (int64_t)c * r;
-      T a0 = T(0.0), a1 = T(0.0);
+      acc_t<T> a0{}, a1{};
       int l = 0;
       for (; l + 1 <= c; l += 2) {
         a0 += X0[l + ii * ld] * r1[l];
         a1 += X0[l + 1 + ii * ld] * r1[l + 1];
       }
       if (l <= c) a0 += X0[l + ii * ld] * r1[l];
-      if (i < r) X2[i + c * ld] -= a0 + a1;
+      if (i < r) X2[i + c * ld] -= accv(a0) + accv(a1);
     }
   __syncthreads();
-  // L22 = chol(H) by columns in dataflow order, with the forward substitution L22^{-1} B carried
-  // on the rows of B.  Warp w owns columns w, w + nw, ... and finishes them in increasing order:
-  // column c (and row c of B) accumulates the contributions of columns k < c as soon as each is
-  // published (flag[k] set after its values are in shared memory), then takes its pivot and
-  // publishes itself.  No block barrier inside the loop: the critical path is one update plus
-  // one pivot per column.  Waits are bounded; a wait that runs out marks the node with
-  // info = -1 (reported as a timeout) and the kernel carries on.
+  // L22 = chol(H) by columns in dataflow order.  Warp w owns columns w, w + nw, ... and finishes
+  // them in increasing order: column c accumulates the contributions of columns k < c as soon as
+  // each is published (flag[k] set after its values are in shared memory), then takes its pivot
+  // and publishes itself; vc[c] keeps the reciprocal pivot.  No block barrier inside the loop.
+  // Waits are bounded; a wait that runs out marks the node with info = -1 (reported as a
+  // timeout) and the kernel carries on.
   int bad = 0;
   {
     volatile int* vflag = flags;
-    int known = 0;          // columns 0 .. known-1 are published (as seen by this warp)
+    int known = 0;           // columns 0 .. known-1 are published (as seen by this warp)
     bool timed_out = false;  // after one expired wait this warp stops waiting
     for (int c = w; c < r; c += nw) {
-      T v[3], b[3];
+      acc_t<T> v[3];
 #pragma unroll
       for (int s = 0; s < 3; ++s) {
         const int i = 32 * s + lane;
         v[s] = (i >= c && i < r) ? X3[i + c * ld] : T(0.0);
-        b[s] = (level < L && i < r) ? X2[c + i * ld] : T(0.0);
       }
       for (int k = 0; k < c; ++k) {
         if (k >= known && !timed_out) {
@@ -440,15 +446,9 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
           const int i = 32 * s + lane;
           if (i >= c && i < r) v[s] -= X3[i + k * ld] * lck;
         }
-        if (level < L)
-#pragma unroll
-          for (int s = 0; s < 3; ++s) {
-            const int kk = 32 * s + lane;
-            if (kk < r) b[s] -= lck * X2[k + kk * ld];
-          }
       }
       const int cs = c >> 5;
-      const T d = shfl_idx(cs == 0 ? v[0] : (cs == 1 ? v[1] : v[2]), c & 31);
+      const T d = shfl_idx(accv(cs == 0 ? v[0] : (cs == 1 ? v[1] : v[2])), c & 31);
       if (!(d > 0.0) && bad == 0) bad = c + 1;
       const T sd = d > 0.0 ? sqrt(d) : T(1.0);
       const T inv = ff_recip(sd);
@@ -456,14 +456,45 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       for (int s = 0; s < 3; ++s) {
         const int i = 32 * s + lane;
         if (i == c) X3[i + c * ld] = sd;
-        else if (i > c && i < r) X3[i + c * ld] = v[s] * inv;
-        if (level < L && i < r) X2[c + i * ld] = b[s] * inv;  // row c of L22^{-1} B
+        else if (i > c && i < r) X3[i + c * ld] = accv(v[s]) * inv;
       }
+      if (lane == 0) vc[c] = inv;
       __threadfence_block();
       __syncwarp();
       if (lane == 0) vflag[c] = 1;
     }
   }
+  __syncthreads();
+  // B' = L22^{-1} B (element (i, c) at X2[i + c * ld]) by blocks of 8 rows: the rows of a block
+  // take the contributions of all earlier rows (one output per thread, a dot product over the
+  // solved rows), then a thread per column solves them with the 8 x 8 diagonal block.
+  if (level < L)
+    for (int k0 = 0; k0 < r; k0 += 8) {
+      const int kb = min(8, r - k0);
+      if (k0 > 0) {
+        for (int e = tid; e < kb * r; e += nth) {
+          const int jj = e % kb, c = e / kb;
+          acc_t<T> acc = X2[k0 + jj + c * ld];
+          for (int q = 0; q < k0; ++q) acc -= X3[k0 + jj + q * ld] * X2[q + c * ld];
+          X2[k0 + jj + c * ld] = accv(acc);
+        }
+        __syncthreads();
+      }
+      if (tid < r) {
+        T y[8];
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+          if (jj < kb) {
+            acc_t<T> acc = X2[k0 + jj + tid * ld];
+#pragma unroll
+            for (int q = 0; q < jj; ++q) acc -= X3[k0 + jj + (k0 + q) * ld] * y[q];
+            y[jj] = accv(acc) * vc[k0 + jj];
+            X2[k0 + jj + tid * ld] = y[jj];
+          }
+        }
+      }
+      __syncthreads();
+    }
   // a warp's first non-positive pivot; the smallest over the warps is written below
   if (lane == 0 && bad) atomicMin(flags + r, bad);
   __syncthreads();
@@ -477,12 +508,16 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
     }
   if (level >= L) return;
   // structured Householder QR of [X1 (upper r x r) ; X2 (r x r)]: reflector j acts on row j of
-  // the top and all r rows of the bottom.  A column is held by 8 lanes (lane q of the group has
-  // rows q, q+8, ..., so a dot product needs a 3-level shuffle reduction) and a warp updates 4
-  // columns at once.  Warp 0 owns column j+1 at step j: it applies reflector j to it and forms
-  // reflector j+1 from the result; the other warps read the reflector scalars (beta, scale, tau)
-  // from shared memory.  The betas and the scaling of the reflector columns are applied after
-  // the loop.  One barrier per reflector.
+  // the top and all r rows of the bottom.  Dataflow over columns: column c belongs to the group
+  // of 8 lanes c & 3 of warp c >> 2 (lane q of the group holds bottom rows q, q+8, ..., so a dot
+  // product is a 3-level shuffle reduction) and stays in registers.  A warp applies reflectors
+  // 0, 1, ... to its four columns as they are published; when the next reflector is formed from
+  // one of its own columns it forms it at once and publishes it (the unscaled vector into
+  // X2[:, j], beta, scale and tau into va, vb, vc, then flag[j]).  No block barrier inside the
+  // loop; three of four handoffs stay inside a warp.  The betas and the scaling of the reflector
+  // columns are applied in the output loop.
+  for (int e = tid; e < r; e += nth) flags[e] = 0;  // reused: the Cholesky waits ended at the barrier above
+  __syncthreads();
   const int gq = lane & 7, grp = lane >> 3;
   const int rpl = (r + 7) >> 3;  // rows per lane (<= 10 for r <= 80)
   auto gsum = [&](T x) {
@@ -490,74 +525,88 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
     for (int o = 4; o > 0; o >>= 1) x = x + shfl_xor(x, o);
     return x;
   };
-  auto reflector = [&](int j, const T (&v)[10]) {
-    T part = T(0.0);
-#pragma unroll
-    for (int t = 0; t < 10; ++t) part += v[t] * v[t];
-    const T sig = gsum(part);
-    const T alpha = X1[j + j * ld];
-    T tj = T(0.0), beta = alpha, scal = T(0.0);
-    if (sig != 0.0) {
-      const T nrm = sqrt(alpha * alpha + sig);
-      beta = alpha >= 0.0 ? -nrm : nrm;
-      tj = (beta - alpha) * ff_recip(beta);
-      scal = ff_recip(alpha - beta);
-    }
-    if (lane == 0) {
-      va[j] = beta;
-      vb[j] = scal;
-      vc[j] = tj;
-      Etau[node * (int64_t)r + j] = tj;
-    }
-  };
-  auto load_col = [&](int c, T (&x)[10]) {
+  if (w < ((r + 3) >> 2)) {
+    volatile int* vflag = flags;
+    const int c0 = 4 * w, cmine = c0 + grp;  // this group's column (may be >= r on the last warp)
+    const int clast = min(c0 + 3, r - 1);
+    T x[10];
 #pragma unroll
     for (int t = 0; t < 10; ++t) {
       const int i = gq + 8 * t;
-      x[t] = (t < rpl && i < r) ? X2[i + c * ld] : T(0.0);
+      x[t] = (t < rpl && i < r && cmine < r) ? X2[i + cmine * ld] : T(0.0);
     }
-  };
-  if (w == 0) {  // every group of warp 0 forms the same reflector; lane 0 stores it
-    T v[10];
-    load_col(0, v);
-    reflector(0, v);
-  }
-  __syncthreads();
-  for (int j = 0; j < r; ++j) {
-    const T tj = vc[j], scal = vb[j];
-    // warp 0 (all four groups alike, group 0 stores): column j+1, then reflector j+1;
-    // warps 1..: 4 columns each from j+2 on.  All lanes of a warp run the shuffles.
-    const int c = (w == 0) ? j + 1 : j + 2 + 4 * (w - 1) + grp;
-    const bool valid = c < r;
-    const bool mine = valid && (w != 0 || grp == 0);
-    if (__any_sync(0xffffffffu, valid)) {
-      T v[10], xc[10];
-      load_col(j, v);
-      if (valid) {
-        load_col(c, xc);
-      } else {
+    bool timed_out = false;
+    for (int j = 0; j <= clast; ++j) {
+      if (j >= c0) {
+        // reflector j from this warp's column j (group j - c0); every group computes its own
+        // column's norm alike, the owning group publishes
+        acc_t<T> part{};
 #pragma unroll
-        for (int t = 0; t < 10; ++t) xc[t] = T(0.0);
+        for (int t = 0; t < 10; ++t) part += x[t] * x[t];
+        const T sig = gsum(accv(part));
+        const T alpha = X1[j + j * ld];
+        T tj = T(0.0), beta = alpha, scal = T(0.0);
+        if (sig != 0.0) {
+          const T nrm = sqrt(alpha * alpha + sig);
+          beta = alpha >= 0.0 ? -nrm : nrm;
+          tj = (beta - alpha) * ff_recip(beta);
+          scal = ff_recip(alpha - beta);
+        }
+        if (cmine == j) {
+#pragma unroll
+          for (int t = 0; t < 10; ++t) {
+            const int i = gq + 8 * t;
+            if (t < rpl && i < r) X2[i + j * ld] = x[t];
+          }
+          if (gq == 0) {
+            va[j] = beta;
+            vb[j] = scal;
+            vc[j] = tj;
+            Etau[node * (int64_t)r + j] = tj;
+          }
+        }
+        __threadfence_block();
+        __syncwarp();
+        if (lane == 0) vflag[j] = 1;
+      } else if (!timed_out) {
+        int spins = 0;
+        while (vflag[j] == 0) {
+          if (++spins > kWaitLimit) {
+            if (lane == 0) info[node] = -1;
+            timed_out = true;
+            break;
+          }
+        }
+        __threadfence_block();
       }
-      if (tj != 0.0) {
-        T acc = T(0.0);
+      // apply reflector j to this warp's columns c > j
+      if (j < clast) {
+        const T tj = vc[j];
+        if (tj != 0.0) {
+          const T scal = vb[j];
+          T v[10];
 #pragma unroll
-        for (int t = 0; t < 10; ++t) acc += v[t] * xc[t];
-        const T top = valid ? X1[j + c * ld] : T(0.0);
-        acc = (gsum(acc) * scal + top) * tj;
-        if (mine && gq == 0) X1[j + c * ld] = top - acc;
-        const T f = acc * scal;
+          for (int t = 0; t < 10; ++t) {
+            const int i = gq + 8 * t;
+            v[t] = (t < rpl && i < r) ? X2[i + j * ld] : T(0.0);
+          }
+          acc_t<T> dacc{};
 #pragma unroll
-        for (int t = 0; t < 10; ++t) {
-          const int i = gq + 8 * t;
-          xc[t] -= f * v[t];
-          if (mine && t < rpl && i < r) X2[i + c * ld] = xc[t];
+          for (int t = 0; t < 10; ++t) dacc += v[t] * x[t];
+          const bool live = cmine > j && cmine < r;
+          const T top = live ? X1[j + cmine * ld] : T(0.0);
+          const T acc = (gsum(accv(dacc)) * scal + top) * tj;
+          if (live) {
+            if (gq == 0) X1[j + cmine * ld] = top - acc;
+            const T f = acc * scal;
+#pragma unroll
+            for (int t = 0; t < 10; ++t) x[t] -= f * v[t];
+          }
         }
       }
-      if (w == 0) reflector(c, xc);
     }
-    __syncthreads();
   }
+  __syncthreads();
   T* Rn = R + (nleaf + node) * (int64_t)r * r;
   for (int c = w; c < r; c += nw)
     for (int i = lane; i < r; i += 32) {
@@ -819,9 +868,10 @@ bool launch_chol_small(double* A, int n, int* info, cudaStream_t st) {
 
 template <typename T, int NB>
 static void leaf_chol_launch(const double* K, T* Lf, const Tree& t, int* info, cudaStream_t st) {
+  constexpr int NT = 256;
   const size_t sm = (size_t)(t.max_leaf + NB) * (NB + 1) * sizeof(T);
-  smem_limit((const void*)k_leaf_chol<T, NB>, sm);
-  k_leaf_chol<T, NB><<<(unsigned)t.nleaf, 256, sm, st>>>(K, Lf, dtree(t), info);
+  smem_limit((const void*)k_leaf_chol<T, NB, NT>, sm);
+  k_leaf_chol<T, NB, NT><<<(unsigned)t.nleaf, NT, sm, st>>>(K, Lf, dtree(t), info);
 }
 
 template <typename T>
@@ -846,9 +896,9 @@ void launch_leaf_qr(T* Pan, int r, const Tree& t, T* tau, T* Rout, cudaStream_t 
   const size_t sm = (size_t)t.max_leaf * r * sizeof(T);
   if (sm <= 200 * 1024) {
     smem_limit((const void*)k_leaf_qr<T, true>, sm);
-    k_leaf_qr<T, true><<<(unsigned)t.nleaf, 256, sm, st>>>(Pan, r, dtree(t), tau, Rout);
+    k_leaf_qr<T, true><<<(unsigned)t.nleaf, leaf_qr_threads<T>(), sm, st>>>(Pan, r, dtree(t), tau, Rout);
   } else {
-    k_leaf_qr<T, false><<<(unsigned)t.nleaf, 256, 0, st>>>(Pan, r, dtree(t), tau, Rout);
+    k_leaf_qr<T, false><<<(unsigned)t.nleaf, leaf_qr_threads<T>(), 0, st>>>(Pan, r, dtree(t), tau, Rout);
   }
 }
 
@@ -1027,9 +1077,9 @@ void launch_leaf_formq(T* Pan, const T* tau, int r, const Tree& t, cudaStream_t 
   const size_t sm = (size_t)t.max_leaf * r * sizeof(T);
   if (sm <= 200 * 1024) {
     smem_limit((const void*)k_leaf_formq<T, true>, sm);
-    k_leaf_formq<T, true><<<(unsigned)t.nleaf, 256, sm, st>>>(Pan, tau, r, dtree(t));
+    k_leaf_formq<T, true><<<(unsigned)t.nleaf, leaf_qr_threads<T>(), sm, st>>>(Pan, tau, r, dtree(t));
   } else {
-    k_leaf_formq<T, false><<<(unsigned)t.nleaf, 256, 0, st>>>(Pan, tau, r, dtree(t));
+    k_leaf_formq<T, false><<<(unsigned)t.nleaf, leaf_qr_threads<T>(), 0, st>>>(Pan, tau, r, dtree(t));
   }
 }
 

@@ -108,6 +108,41 @@ __device__ __forceinline__ ff& operator-=(ff& a, ffprod b) { return a = a - b; }
 __device__ __forceinline__ ff& operator*=(ff& a, ff b) { return a = ff(a * b); }
 __device__ __forceinline__ ff& operator/=(ff& a, ff b) { return a = a / b; }
 
+// Dot-product accumulator in the manner of Dot2 (Ogita, Rump and Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26, 2005): the high parts are summed with TwoSum and every
+// rounding error (TwoSum's and the product's) is summed in a plain float, renormalised once when
+// the value is read.  The loop-carried dependency is a single float add per term (the
+// renormalising accumulate carries nine), and a multiply-add costs 12 FP32 instructions; the
+// result is as accurate as if the sum were formed in twice the float precision.
+struct ffacc {
+  float s, c;
+  __device__ __forceinline__ constexpr ffacc() : s(0.f), c(0.f) {}
+  __device__ __forceinline__ constexpr ffacc(ff a) : s(a.hi), c(a.lo) {}
+  __device__ __forceinline__ void add(float x, float ex) {
+    const float t = __fadd_rn(s, x);
+    const float bb = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(x, bb));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(e, ex));
+  }
+  __device__ __forceinline__ ff value() const {
+    ff r;
+    ff_two_sum(s, c, r.hi, r.lo);
+    return r;
+  }
+};
+__device__ __forceinline__ ffacc& operator+=(ffacc& a, ffprod b) { a.add(b.p, b.e); return a; }
+__device__ __forceinline__ ffacc& operator-=(ffacc& a, ffprod b) { a.add(-b.p, -b.e); return a; }
+__device__ __forceinline__ ffacc& operator+=(ffacc& a, ff b) { a.add(b.hi, b.lo); return a; }
+__device__ __forceinline__ ffacc& operator-=(ffacc& a, ff b) { a.add(-b.hi, -b.lo); return a; }
+
+// acc_t<T>: the accumulator of a sum of T terms (T itself for double); accv reads its value.
+template <typename T> struct AccOf { using type = T; };
+template <> struct AccOf<ff> { using type = ffacc; };
+template <typename T> using acc_t = typename AccOf<T>::type;
+__device__ __forceinline__ double accv(double a) { return a; }
+__device__ __forceinline__ ff accv(const ffacc& a) { return a.value(); }
+
 // Comparisons with a double constant b, in float arithmetic.  Exact when b is a float pair
 // (b == ff(b)), which holds for the constants the kernels compare with (0, 1).  For a normalised
 // pair the order is decided by hi, and by lo when the hi parts are equal.

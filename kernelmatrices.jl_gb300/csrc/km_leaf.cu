@@ -43,18 +43,19 @@ __device__ void leaf_tri_body(const T* __restrict__ L, int m, int op, const T* B
       __syncthreads();
       // diagonal block, one warp per column, lanes = rows of the block
       for (int c = w; c < nc; c += 8) {
-        T x = (lane < ib) ? xs[c * m + i0 + lane] : T(0.0);
+        acc_t<T> xa = (lane < ib) ? xs[c * m + i0 + lane] : T(0.0);  // row `lane`, updates pending
+        T x = T(0.0);                                                  // row `lane`, solved
         if (op == 0) {
           for (int l = 0; l < ib; ++l) {
-            if (lane == l) x = x * D[l * 33 + l];
+            if (lane == l) x = accv(xa) * D[l * 33 + l];
             const T xl = shfl_idx(x, l);
-            if (lane > l && lane < ib) x -= D[lane * 33 + l] * xl;
+            if (lane > l && lane < ib) xa -= D[lane * 33 + l] * xl;
           }
         } else {
           for (int l = ib - 1; l >= 0; --l) {
-            if (lane == l) x = x * D[l * 33 + l];
+            if (lane == l) x = accv(xa) * D[l * 33 + l];
             const T xl = shfl_idx(x, l);
-            if (lane < l) x -= D[l * 33 + lane] * xl;
+            if (lane < l) xa -= D[l * 33 + lane] * xl;
           }
         }
         if (lane < ib) xs[c * m + i0 + lane] = x;
@@ -69,7 +70,7 @@ __device__ void leaf_tri_body(const T* __restrict__ L, int m, int op, const T* B
       for (int e = tid; e < R * ng; e += blockDim.x) {
         const int g = e / R, i = r0 + (e - g * R), cb = 4 * g;
         const T* xc = xs + cb * m + i0;
-        T acc[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
+        acc_t<T> acc[4] = {};
         auto ld = [&](int l) {
           return (op == 0) ? L[(int64_t)(i0 + l) * m + i]   // L[i, i0 + l]
                            : L[(int64_t)i * m + i0 + l];    // L[i0 + l, i]
@@ -94,7 +95,7 @@ __device__ void leaf_tri_body(const T* __restrict__ L, int m, int op, const T* B
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-          if (cb + j < nc) xs[(cb + j) * m + i] -= acc[j];
+          if (cb + j < nc) xs[(cb + j) * m + i] -= accv(acc[j]);
       }
       __syncthreads();
     }
@@ -104,9 +105,7 @@ __device__ void leaf_tri_body(const T* __restrict__ L, int m, int op, const T* B
     }
   } else {
     for (int i = tid; i < m; i += blockDim.x) {
-      T acc[NC];
-#pragma unroll
-      for (int c = 0; c < NC; ++c) acc[c] = T(0.0);
+      acc_t<T> acc[NC] = {};
       if (op == 2) {  // row i of L: L[i, l], l <= i
         for (int l = 0; l <= i; ++l) {
           const T a = L[(int64_t)l * m + i];
@@ -122,7 +121,7 @@ __device__ void leaf_tri_body(const T* __restrict__ L, int m, int op, const T* B
         }
       }
 #pragma unroll
-      for (int c = 0; c < NC; ++c) ys[c * m + i] = acc[c];
+      for (int c = 0; c < NC; ++c) ys[c * m + i] = accv(acc[c]);
     }
     __syncthreads();
     for (int e = tid; e < nc * m; e += blockDim.x) {
@@ -191,9 +190,7 @@ __global__ void __launch_bounds__(256) k_leaf_qproj(const T* __restrict__ Q, int
   const int cper = (nc + G - 1) / G;            // <= 6
   const int cb = g * cper, ce = min(nc, cb + cper);
   const bool active = g < G;
-  T acc[6];
-#pragma unroll
-  for (int j = 0; j < 6; ++j) acc[j] = T(0.0);
+  acc_t<T> acc[6] = {};
   const T* Ql = Q + s * r;
   for (int i0 = 0; i0 < m; i0 += kProjRows) {
     const int rows = min(kProjRows, m - i0);
@@ -219,7 +216,7 @@ __global__ void __launch_bounds__(256) k_leaf_qproj(const T* __restrict__ Q, int
   if (active)
 #pragma unroll
     for (int j = 0; j < 6; ++j)
-      if (cb + j < ce) VP[(leaf * k + c0 + cb + j) * r + q] = acc[j];
+      if (cb + j < ce) VP[(leaf * k + c0 + cb + j) * r + q] = accv(acc[j]);
 }
 
 // y_c += sign * Q_leaf g_c for a chunk of up to 16 columns: thread per leaf row, the chunk's
@@ -239,9 +236,7 @@ __global__ void __launch_bounds__(256) k_leaf_qexpand(const T* __restrict__ Q, i
   const T* Ql = Q + s * r;
   const bool add = sign > 0.0;
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
-    T acc[16];
-#pragma unroll
-    for (int c = 0; c < 16; ++c) acc[c] = T(0.0);
+    acc_t<T> acc[16] = {};
     int q = 0;
     for (; q + 1 < r; q += 2) {  // two basis entries loaded ahead of their multiply-adds
       const T a0 = Ql[(int64_t)q * m + i], a1 = Ql[(int64_t)(q + 1) * m + i];
@@ -262,7 +257,7 @@ __global__ void __launch_bounds__(256) k_leaf_qexpand(const T* __restrict__ Q, i
     for (int c = 0; c < 16; ++c)
       if (c < nc) {
         T* y = Y + (int64_t)(c0 + c) * ldy + s + i;
-        *y = add ? *y + acc[c] : *y - acc[c];
+        *y = add ? *y + accv(acc[c]) : *y - accv(acc[c]);
       }
   }
 }
