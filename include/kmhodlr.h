@@ -221,6 +221,23 @@ int km_grad_fisher(km_handle* h, const double* y, const double* probes, int64_t 
 int km_grad_fisher_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed,
                           double* nll, double* grad, double* fisher);
 
+/* k-d ordering of n 2-D points (AoS x, y) on the device, the input step of maxlikdata
+ * (src/HODLR/src/constructor.jl:171-181), which sorts with NearestNeighbors.KDTree(pts).data.
+ * That package's permutation is not reproduced; this library's ordering is: a range of more than
+ * `leaf` points is sorted stably by its coordinate of larger spread (max - min, x on a tie), its
+ * first floor(len/2) points form the left child, the rest the right child, recursively; ranges of
+ * at most `leaf` points keep their order.  perm[i] = original index of sorted position i.
+ * Coordinates must be finite; n < 2^31.  Uses the handle's device and stream, not its problem. */
+int km_kd_order(km_handle* h, const double* pts, int64_t n, int64_t leaf, int64_t* perm);
+
+/* maxlikdata(pts=, data=, sortmethod=:KDTree) with the ordering of km_kd_order: the sorted points
+ * (2 n values) and the data carried with them (data_reorder, src/utils.jl:22-25).  data and
+ * data_sorted may be NULL (points only), perm may be NULL.  The reference looks data up by point
+ * value, so duplicated points all receive the datum of the last duplicate; here every point keeps
+ * its own datum. */
+int km_maxlikdata(km_handle* h, const double* pts, const double* data, int64_t n, int64_t leaf,
+                  double* pts_sorted, double* data_sorted, int64_t* perm);
+
 /* Frees the device buffers of the handle's current problem (the handle stays usable; the next
  * km_assemble allocates again).  No reference counterpart: Julia's GC frees the arrays. */
 int km_trim(km_handle* h);

@@ -1742,6 +1742,75 @@ extern "C" int km_trim(km_handle* h) {
   return KM_OK;
 }
 
+// ---- k-d ordering of the input points (maxlikdata, src/HODLR/src/constructor.jl:171-181) -------
+
+// Orders n points (AoS x, y, host) on the device; writes the permutation (perm[i] = original
+// index of sorted position i) and, when pts_s is given, the sorted points and data.  Temporary
+// device buffers are taken from the handle's budget and returned before the call ends.
+static int kd_impl(km_handle* h, const double* pts, const double* data, int64_t n, int64_t leaf, int64_t* perm,
+                   double* pts_s, double* data_s) {
+  if (!h) return KM_ERR_BAD_ARG;
+  if (!pts || n < 1 || leaf < 1 || n >= (int64_t(1) << 31) || (!perm && !pts_s) || (data && pts_s && !data_s))
+    return fail(h, KM_ERR_BAD_ARG, "bad k-d ordering arguments");
+  for (int64_t i = 0; i < 2 * n; ++i)
+    if (!std::isfinite(pts[i])) return fail(h, KM_ERR_BAD_ARG, "a point coordinate is not finite");
+  cudaSetDevice(h->cfg.device);
+  double* d_pts = nullptr;
+  double* d_data = nullptr;
+  double* d_ps = nullptr;
+  double* d_ds = nullptr;
+  int64_t* d_perm = nullptr;
+  unsigned char* d_scr = nullptr;
+  auto release = [&] {
+    dfree(h, d_pts);
+    dfree(h, d_data);
+    dfree(h, d_ps);
+    dfree(h, d_ds);
+    dfree(h, d_perm);
+    dfree(h, d_scr);
+  };
+  const bool with_data = data && pts_s;
+  int rc = dalloc(h, &d_pts, 2 * n);
+  if (rc == KM_OK) rc = dalloc(h, &d_perm, n);
+  if (rc == KM_OK) rc = dalloc(h, &d_scr, (int64_t)kd_scratch_bytes(n));
+  if (rc == KM_OK && pts_s) rc = dalloc(h, &d_ps, 2 * n);
+  if (rc == KM_OK && with_data) rc = dalloc(h, &d_data, n);
+  if (rc == KM_OK && with_data) rc = dalloc(h, &d_ds, n);
+  if (rc != KM_OK) {
+    release();
+    return rc;
+  }
+  cudaStream_t st = h->stream;
+  std::string err;
+  cudaError_t e = cudaMemcpyAsync(d_pts, pts, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && with_data) e = cudaMemcpyAsync(d_data, data, sizeof(double) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && !kd_order_device(d_pts, n, leaf, d_perm, d_scr, st, &err)) {
+    release();
+    return fail(h, KM_ERR_CUDA, err);
+  }
+  if (e == cudaSuccess && pts_s) {
+    launch_gather_sorted(d_pts, with_data ? d_data : nullptr, d_perm, n, d_ps, d_ds, st);
+    e = cudaMemcpyAsync(pts_s, d_ps, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && with_data) e = cudaMemcpyAsync(data_s, d_ds, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+  }
+  if (e == cudaSuccess && perm) e = cudaMemcpyAsync(perm, d_perm, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  release();
+  if (e != cudaSuccess) return cuda_fail(h, e, "k-d ordering");
+  return KM_OK;
+}
+
+extern "C" int km_kd_order(km_handle* h, const double* pts, int64_t n, int64_t leaf, int64_t* perm) {
+  return kd_impl(h, pts, nullptr, n, leaf, perm, nullptr, nullptr);
+}
+
+extern "C" int km_maxlikdata(km_handle* h, const double* pts, const double* data, int64_t n, int64_t leaf,
+                             double* pts_sorted, double* data_sorted, int64_t* perm) {
+  if (!pts_sorted) return fail(h, KM_ERR_BAD_ARG, "bad k-d ordering arguments");
+  return kd_impl(h, pts, data, n, leaf, perm, pts_sorted, data_sorted);
+}
+
 // Mirrors the allocations of assemble_impl (Nystrom), ensure_vec, ensure_xy, derivative_apply
 // and nll_grad_impl for one problem shape.
 extern "C" int64_t km_estimate_bytes(int64_t n, int64_t rank, int level_kind, int64_t level, int64_t ncols,

@@ -169,4 +169,16 @@ void launch_glogdet(const GNodeDesc* nodes, int nn, double* partial, cudaStream_
 bool launch_leaf_tri_desc(const double* Lf, const Tree& t, int op, const LeafDesc* descs, int n, int maxcols,
                           cudaStream_t st);
 
+// k-d ordering of 2-D points (km_kd.cu): a contiguous range of positions, split or final
+struct KdSeg {
+  int64_t start, len;
+  int split;
+};
+size_t kd_scratch_bytes(int64_t n);
+bool kd_order_device(const double* d_pts, int64_t n, int64_t leaf, int64_t* d_perm, void* d_scratch,
+                     cudaStream_t st, std::string* err);
+// pts_s[i] = pts[perm[i]] (2-D), data_s[i] = data[perm[i]] when data is not null
+void launch_gather_sorted(const double* pts, const double* data, const int64_t* perm, int64_t n, double* pts_s,
+                          double* data_s, cudaStream_t st);
+
 }  // namespace km

@@ -9,6 +9,7 @@
 #   HODLR.stoch_gradient, HODLR.negloglik             stochasticgradient.jl:30-44, maxlikfunctions.jl:2-9
 #   HODLR.stoch_profile_gradient, profile_negloglik   stochasticgradient.jl:68-86, maxlikfunctions.jl:11-19
 #   grad_and_fisher_matrix, stoch_fisher              stochastichessian.jl:91-115,152-181
+#   maxlikdata(...; sortmethod=:KDTree)               constructor.jl:171-181 (own k-d ordering)
 #
 # Kernels are callable structs, so the same object runs in the reference's CPU path
 # (k(x, y, p) like any kernel function) and is recognised by type here.
@@ -190,6 +191,26 @@ function grad_and_fisher(K::GPUKernelHODLR, dat::Vector{Float64}, vecs::Vector{V
                    (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
                    K.h, dat, probes, size(probes, 2), nll, grad, fisher))
   return nll[], grad, Symmetric(fisher)
+end
+
+# maxlikdata(pts=, data=, sortmethod=:KDTree) (constructor.jl:171-181) with the library's own k-d
+# ordering computed on the GPU (NearestNeighbors' permutation is not reproduced).
+function maxlikdata_gpu(pts::Vector{SVector{2,Float64}}, data::Vector{Float64}; leaf::Int64=32, device::Int=0)
+  length(pts) == length(data) || error("points and data disagree in length")
+  h = Ref{Ptr{Cvoid}}(C_NULL)
+  cfg = Ref(KmConfig(device, Cint(0), 0.8, 0, 0.0))
+  check(C_NULL, ccall((:km_create, libkm), Cint, (Ptr{KmConfig}, Ptr{Ptr{Cvoid}}), cfg, h))
+  pts_s = similar(pts)
+  data_s = similar(data)
+  try
+    check(h[], ccall((:km_maxlikdata, libkm), Cint,
+                     (Ptr{Cvoid}, Ptr{SVector{2,Float64}}, Ptr{Float64}, Int64, Int64,
+                      Ptr{SVector{2,Float64}}, Ptr{Float64}, Ptr{Int64}),
+                     h[], pts, data, length(pts), leaf, pts_s, data_s, C_NULL))
+  finally
+    ccall((:km_destroy, libkm), Cint, (Ptr{Cvoid},), h[])
+  end
+  return pts_s, data_s
 end
 
 # ---- batched form: nll_objective over many independent datasets ------------------------------

@@ -127,6 +127,8 @@ SIGNATURES = {
     "km_nll_grad_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP]),
     "km_profile_nll_grad": (C.c_int, [_H, _DP, _DP, C.c_int64, _DP, _DP]),
     "km_grad_fisher": (C.c_int, [_H, _DP, _DP, C.c_int64, _DP, _DP, _DP]),
+    "km_kd_order": (C.c_int, [_H, _DP, C.c_int64, C.c_int64, C.POINTER(C.c_int64)]),
+    "km_maxlikdata": (C.c_int, [_H, _DP, _DP, C.c_int64, C.c_int64, _DP, _DP, C.POINTER(C.c_int64)]),
     "km_grad_fisher_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP, _DP]),
     "km_profile_nll_grad_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP]),
     "km_trim": (C.c_int, [_H]),

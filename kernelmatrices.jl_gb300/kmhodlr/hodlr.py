@@ -436,6 +436,60 @@ def gpsimulate(kernel, pts: np.ndarray, parms, rank: int, lvl, z: np.ndarray, de
     return HK.W @ np.asarray(z, dtype=np.float64)
 
 
+class _Scratch:
+    """A handle without a problem, for calls that only need a device and a stream."""
+
+    def __init__(self, device: int = 0):
+        lib = L.load()
+        cfg = L.KmConfig(device=device, precision=L.KM_PREC_FP64, hbm_budget_fraction=0.8, refine_max_iter=0,
+                         refine_tol=0.0)
+        h = C.c_void_p()
+        rc = lib.km_create(C.byref(cfg), C.byref(h))
+        if rc != L.KM_OK:
+            raise KMError(rc, "km_create failed (no CUDA device?)")
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            L.load().km_destroy(self._h)
+            self._h = None
+
+
+def kd_order(pts: np.ndarray, leaf: int = 32, device: int = 0) -> np.ndarray:
+    """k-d ordering permutation of (n, 2) points computed on the GPU (``km_kd_order``): ranges of
+    more than ``leaf`` points are sorted stably on their coordinate of larger spread and split at
+    floor(len/2), recursively.  Stands in for ``NearestNeighbors.KDTree(pts).data``
+    (src/HODLR/src/constructor.jl:180), whose own permutation is not reproduced."""
+    P = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 2)
+    n = P.shape[0]
+    perm = np.empty(n, dtype=np.int64)
+    s = _Scratch(device)
+    _check(s._h, L.load().km_kd_order(s._h, _dp(P), n, int(leaf), perm.ctypes.data_as(C.POINTER(C.c_int64))))
+    return perm
+
+
+def maxlikdata(pts: np.ndarray, data: np.ndarray, sortmethod: str = "kdtree", leaf: int = 32, device: int = 0):
+    """``maxlikdata(pts=, data=, sortmethod=)`` (src/HODLR/src/constructor.jl:171-202): returns the
+    (points, data) pair sorted by the GPU k-d ordering (``"kdtree"``) or unchanged
+    (``"nothing"``); any other method raises as the reference does.  Each datum travels with its
+    own point (the reference's data_reorder looks data up by point value, src/utils.jl:22-25)."""
+    P = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 2)
+    y = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)
+    if P.shape[0] != y.size:
+        raise KMError(L.KM_ERR_BAD_ARG, "points and data disagree in length")
+    m = str(sortmethod).lower().lstrip(":")
+    if m == "nothing":
+        return P.copy(), y.copy()
+    if m != "kdtree":
+        raise KMError(L.KM_ERR_BAD_ARG, "The options are :Nothing and :KDTree")
+    n = P.shape[0]
+    ps = np.empty_like(P)
+    ys = np.empty_like(y)
+    s = _Scratch(device)
+    _check(s._h, L.load().km_maxlikdata(s._h, _dp(P), _dp(y), n, int(leaf), _dp(ps), _dp(ys), None))
+    return ps, ys
+
+
 def probe_fp32_tflops(device: int = 0) -> float:
     out = C.c_double()
     rc = L.load().km_probe_fp32_tflops(device, C.byref(out))

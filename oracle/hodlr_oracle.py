@@ -857,6 +857,36 @@ def grad_and_fisher_matrix(prms, pts: np.ndarray, dat: np.ndarray, kid: int, ran
     return g, F
 
 
+def kd_order(pts: np.ndarray, leaf: int = 32) -> np.ndarray:
+    """k-d ordering checked against the GPU's ``km_kd_order``.  The reference sorts with
+    NearestNeighbors 0.4.9 ``KDTree(pts).data`` (src/HODLR/src/constructor.jl:180), a third-party
+    permutation that is not reproduced (parity unpinned against it); this is the build's own
+    rule: a range of more than ``leaf`` points is sorted stably on the coordinate of larger spread
+    (max - min, x on a tie), split at floor(len/2), and both halves ordered the same way."""
+    pts = np.asarray(pts, dtype=np.float64).reshape(-1, 2)
+    out = np.arange(len(pts), dtype=np.int64)
+
+    def rec(lo: int, hi: int) -> None:
+        if hi - lo <= leaf:
+            return
+        seg = out[lo:hi]
+        sub = pts[seg]
+        ax = 0 if (sub[:, 0].max() - sub[:, 0].min()) >= (sub[:, 1].max() - sub[:, 1].min()) else 1
+        out[lo:hi] = seg[np.argsort(sub[:, ax], kind="stable")]
+        h = (hi - lo) // 2
+        rec(lo, lo + h)
+        rec(lo + h, hi)
+
+    import sys
+    old = sys.getrecursionlimit()
+    sys.setrecursionlimit(max(old, 10000))
+    try:
+        rec(0, len(pts))
+    finally:
+        sys.setrecursionlimit(old)
+    return out
+
+
 # ----------------------------------------------------------------------------------------------
 # Dense oracle: src/HODLR/src/exactmaxlik.jl
 # ----------------------------------------------------------------------------------------------

@@ -198,3 +198,16 @@ def test_stochastic_fisher():
     Fex = np.array([[0.5 * np.trace(Si @ D[j] @ Si @ D[k]) for k in range(3)] for j in range(3)])
     Fmc = O.stoch_fisher(K, HK, DKs, O.givesaa(300, n, 6))
     assert np.all(np.abs(Fmc - Fex) < 0.15 * np.sqrt(np.outer(np.diag(Fex), np.diag(Fex))))
+
+
+def test_kd_order_oracle_matches_host_helper():
+    """The oracle's recursive k-d ordering equals the host helper that generates the ordered test
+    inputs (stack form of the same rule), also with ties, duplicates and signed zeros."""
+    from kmhodlr.data import kd_order as host_kd
+    rng = np.random.default_rng(5)
+    g = np.stack(np.meshgrid(np.arange(23.0), np.arange(17.0)), -1).reshape(-1, 2)
+    cases = [rng.uniform(size=(1000, 2)), g, np.concatenate([g, g[::3]]),
+             np.array([[0.0, 1.0], [-0.0, 1.0], [0.0, -0.0], [1.0, 0.0]] * 20)]
+    for P in cases:
+        for leaf in (1, 7, 32):
+            assert np.array_equal(O.kd_order(P, leaf), host_kd(P, leaf))
