@@ -238,6 +238,32 @@ int km_kd_order(km_handle* h, const double* pts, int64_t n, int64_t leaf, int64_
 int km_maxlikdata(km_handle* h, const double* pts, const double* data, int64_t n, int64_t leaf,
                   double* pts_sorted, double* data_sorted, int64_t* perm);
 
+/* ---- RKernelHODLR: recursive product-only HODLR of K(x1, x2) ------------------------------- */
+
+/* The recursive HODLR of a not necessarily symmetric or square kernel matrix, replacing
+ * RKernelHODLR(K, tol, maxrank, lvl) (src/HODLR/src/constructor.jl:130-161; struct
+ * src/HODLR/src/structstypes.jl:22-27).  At every level rows split at floor(n1/2), columns at
+ * floor(n2/2); A12 and A21 are compressed by ACA (src/factorizations.jl:9-84), the diagonal
+ * blocks after `level` splits are dense.  LogLevel(lv) resolves to FixedLevel(floor(log2(min(n1,
+ * n2))) - lv).  x1 (n1 points) and x2 (n2 points) are AoS x, y.  Blocks are numbered A12, A21,
+ * then the blocks of A11, then those of A22 (the reference's recursive order).  On failure *out
+ * is NULL and km_rhodlr_create_error() gives the message. */
+typedef struct km_rhodlr km_rhodlr;
+int km_rhodlr_create(const km_config* cfg, const double* x1, int64_t n1, const double* x2, int64_t n2,
+                     int kernel_id, const double* params, int nparams, double tol, int64_t maxrank,
+                     int level_kind, int64_t level, km_rhodlr** out);
+int km_rhodlr_destroy(km_rhodlr* r);
+const char* km_rhodlr_create_error(void);
+const char* km_rhodlr_last_error(const km_rhodlr* r);
+/* number of ACA blocks, dense leaves and levels */
+int km_rhodlr_info(const km_rhodlr* r, int64_t* nblocks, int64_t* nleaves, int64_t* levels);
+int km_rhodlr_block_ranks(const km_rhodlr* r, int64_t* ranks);
+int km_rhodlr_aca_pivots(km_rhodlr* r, int64_t block, int64_t cap, int64_t* rows, int64_t* cols,
+                         int64_t* rank);
+/* y (n1 x k) = R x (x: n2 x k), host column-major; replaces *(R::RKernelHODLR, V)
+ * (src/HODLR/src/baseoverloads.jl:301-305), column by column. */
+int km_rhodlr_matvec(km_rhodlr* r, const double* x, double* y, int64_t k);
+
 /* Frees the device buffers of the handle's current problem (the handle stays usable; the next
  * km_assemble allocates again).  No reference counterpart: Julia's GC frees the arrays. */
 int km_trim(km_handle* h);

@@ -175,8 +175,6 @@ struct km_handle {
 namespace {
 
 constexpr int kLogdetBlocks = 256;
-constexpr int kAcaMaxCap = 4096;       // ACA panel columns per block (2 x 4096 doubles of shared memory)
-constexpr int64_t kAcaGridMin = 8192;  // blocks at least this wide run the grid-wide ACA kernel
 
 int fail(km_handle* h, int code, const std::string& msg) {
   if (h) h->err = msg;

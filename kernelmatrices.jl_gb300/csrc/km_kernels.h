@@ -147,6 +147,8 @@ void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb,
                      double* out, cudaStream_t st);
 
 // ACA and the general factorisation
+constexpr int kAcaMaxCap = 4096;       // ACA panel columns per block (2 x 4096 doubles of shared memory)
+constexpr int64_t kAcaGridMin = 8192;  // blocks at least this wide run the grid-wide ACA kernel
 void launch_aca(const double* pts, KParams kp, const AcaBlock* blocks, int nblocks, int maxcap, double* P,
                 uint8_t* F, int* piv, double rtol, int* rank, int* status, cudaStream_t st);
 // ACA of one large block (blocks[b].grid == 1) by all SMs in one cooperative launch, with

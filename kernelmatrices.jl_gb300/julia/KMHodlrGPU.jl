@@ -10,6 +10,7 @@
 #   HODLR.stoch_profile_gradient, profile_negloglik   stochasticgradient.jl:68-86, maxlikfunctions.jl:11-19
 #   grad_and_fisher_matrix, stoch_fisher              stochastichessian.jl:91-115,152-181
 #   maxlikdata(...; sortmethod=:KDTree)               constructor.jl:171-181 (own k-d ordering)
+#   RKernelHODLR(K, tol, maxrank, lvl), R * v         constructor.jl:130-161, baseoverloads.jl:301-305
 #
 # Kernels are callable structs, so the same object runs in the reference's CPU path
 # (k(x, y, p) like any kernel function) and is recognised by type here.
@@ -211,6 +212,39 @@ function maxlikdata_gpu(pts::Vector{SVector{2,Float64}}, data::Vector{Float64}; 
     ccall((:km_destroy, libkm), Cint, (Ptr{Cvoid},), h[])
   end
   return pts_s, data_s
+end
+
+# RKernelHODLR(K, tol, maxrank, lvl) (constructor.jl:130-161) for K(x1, x2) of any shape, held on
+# the GPU; only products, as in the reference (baseoverloads.jl:301-305).
+mutable struct GPURKernelHODLR
+  r::Ptr{Cvoid}
+  n1::Int64
+  n2::Int64
+end
+
+function GPURKernelHODLR(K::KernelMatrix, tol::Float64, maxrank::Int64=0, lvl::HierLevel=LogLevel(7);
+                         device::Int=0)
+  kind, lv = lvl isa FixedLevel ? (Cint(0), Int64(lvl.lv)) : (Cint(1), Int64(lvl.lv))
+  cfg = Ref(KmConfig(device, Cint(0), 0.8, 0, 0.0))
+  prm = Vector{Float64}(collect(K.parms))
+  r = Ref{Ptr{Cvoid}}(C_NULL)
+  rc = ccall((:km_rhodlr_create, libkm), Cint,
+             (Ptr{KmConfig}, Ptr{SVector{2,Float64}}, Int64, Ptr{SVector{2,Float64}}, Int64, Cint, Ptr{Float64},
+              Cint, Float64, Int64, Cint, Int64, Ptr{Ptr{Cvoid}}),
+             cfg, K.x1, length(K.x1), K.x2, length(K.x2), kernel_id(K.kernel), prm, length(prm), tol, maxrank,
+             kind, lv, r)
+  rc == 0 || error(unsafe_string(ccall((:km_rhodlr_create_error, libkm), Cstring, ())))
+  R = GPURKernelHODLR(r[], length(K.x1), length(K.x2))
+  finalizer(x -> ccall((:km_rhodlr_destroy, libkm), Cint, (Ptr{Cvoid},), x.r), R)
+  return R
+end
+
+function Base.:*(R::GPURKernelHODLR, v::Vector{Float64})
+  length(v) == R.n2 || error("dimension mismatch")
+  out = Vector{Float64}(undef, R.n1)
+  rc = ccall((:km_rhodlr_matvec, libkm), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64), R.r, v, out, 1)
+  rc == 0 || error(unsafe_string(ccall((:km_rhodlr_last_error, libkm), Cstring, (Ptr{Cvoid},), R.r)))
+  return out
 end
 
 # ---- batched form: nll_objective over many independent datasets ------------------------------

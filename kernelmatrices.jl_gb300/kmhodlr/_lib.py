@@ -128,6 +128,16 @@ SIGNATURES = {
     "km_profile_nll_grad": (C.c_int, [_H, _DP, _DP, C.c_int64, _DP, _DP]),
     "km_grad_fisher": (C.c_int, [_H, _DP, _DP, C.c_int64, _DP, _DP, _DP]),
     "km_kd_order": (C.c_int, [_H, _DP, C.c_int64, C.c_int64, C.POINTER(C.c_int64)]),
+    "km_rhodlr_create": (C.c_int, [C.POINTER(KmConfig), _DP, C.c_int64, _DP, C.c_int64, C.c_int, _DP, C.c_int,
+                                   C.c_double, C.c_int64, C.c_int, C.c_int64, C.POINTER(_P)]),
+    "km_rhodlr_destroy": (C.c_int, [_P]),
+    "km_rhodlr_create_error": (C.c_char_p, []),
+    "km_rhodlr_last_error": (C.c_char_p, [_P]),
+    "km_rhodlr_info": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "km_rhodlr_block_ranks": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "km_rhodlr_aca_pivots": (C.c_int, [_P, C.c_int64, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_int64)]),
+    "km_rhodlr_matvec": (C.c_int, [_P, _DP, _DP, C.c_int64]),
     "km_maxlikdata": (C.c_int, [_H, _DP, _DP, C.c_int64, C.c_int64, _DP, _DP, C.POINTER(C.c_int64)]),
     "km_grad_fisher_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP, _DP]),
     "km_profile_nll_grad_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP]),

@@ -97,10 +97,8 @@ class KernelMatrix:
         self.x2 = np.ascontiguousarray(x2, dtype=np.float64)
         self.parms = np.ascontiguousarray(parms, dtype=np.float64)
         self.kernel = kernel
-        if self.x1.ndim != 2 or self.x1.shape[1] != 2:
-            raise KMError(L.KM_ERR_BAD_ARG, "points must be an (n, 2) array")
-        if self.x1.shape != self.x2.shape:
-            raise KMError(L.KM_ERR_BAD_ARG, "Eltype of pts and pts2 must agree.")
+        if self.x1.ndim != 2 or self.x1.shape[1] != 2 or self.x2.ndim != 2 or self.x2.shape[1] != 2:
+            raise KMError(L.KM_ERR_BAD_ARG, "points must be (n, 2) arrays")
 
     @property
     def shape(self):
@@ -167,8 +165,9 @@ class KernelHODLR:
                  plel: bool = False, sorted: bool = False, device: int = 0,
                  precision: int = L.KM_PREC_FP64, refine_max_iter: int = 0, refine_tol: float = 1e-10):
         lib = L.load()
-        if not np.array_equal(K.x1, K.x2):
-            raise KMError(L.KM_ERR_BAD_ARG, "This function builds symmetric matrices.")
+        if K.x1.shape != K.x2.shape or not np.array_equal(K.x1, K.x2):
+            raise KMError(L.KM_ERR_BAD_ARG, "This function builds symmetric matrices. If you want a non-symmetric "
+                          "HODLR matrix, please use the recursive RKernelHODLR, which will only allow matvecs.")
         kid = getattr(K.kernel, "kid", K.kernel)
         cfg = L.KmConfig(device=device, precision=precision, hbm_budget_fraction=0.8,
                          refine_max_iter=refine_max_iter, refine_tol=refine_tol)
@@ -434,6 +433,63 @@ def gpsimulate(kernel, pts: np.ndarray, parms, rank: int, lvl, z: np.ndarray, de
     HK = KernelHODLR(K, 0.0, rank, lvl, nystrom=True, device=device)
     symmetricfactorize(HK)
     return HK.W @ np.asarray(z, dtype=np.float64)
+
+
+class RKernelHODLR:
+    """``RKernelHODLR(K, tol, maxrank, lvl)`` (src/HODLR/src/constructor.jl:130-161) held on the GPU:
+    the recursive product-only HODLR of K(x1, x2) with x1 and x2 of any lengths, ACA off-diagonal
+    blocks and dense diagonal leaves.  ``R @ x`` is the product of baseoverloads.jl:301-305."""
+
+    def __init__(self, K: KernelMatrix, tol: float, maxrank: int = 0, lvl=None, device: int = 0):
+        lib = L.load()
+        lvl = LogLevel(7) if lvl is None else lvl
+        kind, lv = _level(lvl)
+        kid = getattr(K.kernel, "kid", K.kernel)
+        cfg = L.KmConfig(device=device, precision=L.KM_PREC_FP64, hbm_budget_fraction=0.8, refine_max_iter=0,
+                         refine_tol=0.0)
+        r = C.c_void_p()
+        rc = lib.km_rhodlr_create(C.byref(cfg), _dp(K.x1), K.x1.shape[0], _dp(K.x2), K.x2.shape[0], int(kid),
+                                  _dp(K.parms), len(K.parms), float(tol), int(maxrank), kind, int(lv), C.byref(r))
+        if rc != L.KM_OK:
+            raise KMError(rc, lib.km_rhodlr_create_error().decode())
+        self._r = r
+        self.shape = (K.x1.shape[0], K.x2.shape[0])
+        nb, nl, lvs = C.c_int64(), C.c_int64(), C.c_int64()
+        lib.km_rhodlr_info(r, C.byref(nb), C.byref(nl), C.byref(lvs))
+        self.nblocks, self.nleaves, self.levels = nb.value, nl.value, lvs.value
+
+    def __del__(self):
+        r = getattr(self, "_r", None)
+        if r:
+            L.load().km_rhodlr_destroy(r)
+            self._r = None
+
+    def block_ranks(self) -> np.ndarray:
+        out = np.zeros(max(self.nblocks, 1), dtype=np.int64)
+        L.load().km_rhodlr_block_ranks(self._r, out.ctypes.data_as(C.POINTER(C.c_int64)))
+        return out[:self.nblocks]
+
+    def aca_pivots(self, block: int):
+        lib = L.load()
+        cap = 8192
+        rows = np.zeros(cap, dtype=np.int64)
+        cols = np.zeros(cap, dtype=np.int64)
+        rk = C.c_int64()
+        rc = lib.km_rhodlr_aca_pivots(self._r, int(block), cap, rows.ctypes.data_as(C.POINTER(C.c_int64)),
+                                      cols.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(rk))
+        if rc != L.KM_OK:
+            raise KMError(rc, lib.km_rhodlr_last_error(self._r).decode())
+        return rows[:rk.value], cols[:rk.value]
+
+    def __matmul__(self, x: np.ndarray) -> np.ndarray:
+        lib = L.load()
+        v = np.asarray(x, dtype=np.float64)
+        X = np.asfortranarray(v.reshape(self.shape[1], -1))
+        Y = np.empty((self.shape[0], X.shape[1]), order="F")
+        rc = lib.km_rhodlr_matvec(self._r, _dp(X), _dp(Y), X.shape[1])
+        if rc != L.KM_OK:
+            raise KMError(rc, lib.km_rhodlr_last_error(self._r).decode())
+        return Y.reshape(self.shape[0]) if v.ndim == 1 else Y
 
 
 class _Scratch:

@@ -887,6 +887,65 @@ def kd_order(pts: np.ndarray, leaf: int = 32) -> np.ndarray:
     return out
 
 
+@dataclass
+class RKernelHODLR:
+    """``RKernelHODLR`` (src/HODLR/src/structstypes.jl:22-27): A11 and A22 dense or recursive,
+    A12 and A21 as (U, V, row pivots, column pivots) from ACA."""
+    A11: object
+    A22: object
+    A12: tuple
+    A21: tuple
+
+
+def rkernel_hodlr(K: KernelMatrix, tol: float, maxrank: int = 0, lvl=None):
+    """``RKernelHODLR(K, tol, maxrank, lvl)`` (src/HODLR/src/constructor.jl:130-161)."""
+    lvl = LogLevel(7) if lvl is None else lvl
+    if isinstance(lvl, LogLevel):
+        return rkernel_hodlr(K, tol, maxrank, FixedLevel(_floor_log2(min(K.shape)) - lvl.lv))
+    if lvl.lv == 0:
+        return K.full()
+    len1, len2 = K.shape
+    m1, m2 = len1 // 2, len2 // 2
+
+    def sub(a, b, c, d):
+        return KernelMatrix(K.x1[a:b], K.x2[c:d], K.parms, K.kid, K.deriv)
+
+    K11, K22 = sub(0, m1, 0, m2), sub(m1, len1, m2, len2)
+    A12 = ACA(sub(0, m1, m2, len2), tol, maxrank)
+    A21 = ACA(sub(m1, len1, 0, m2), tol, maxrank)
+    if lvl.lv == 1:
+        return RKernelHODLR(K11.full(), K22.full(), A12, A21)
+    return RKernelHODLR(rkernel_hodlr(K11, tol, maxrank, FixedLevel(lvl.lv - 1)),
+                        rkernel_hodlr(K22, tol, maxrank, FixedLevel(lvl.lv - 1)), A12, A21)
+
+
+def rhodlr_shape(R) -> Tuple[int, int]:
+    """``size(R)`` (src/HODLR/src/baseoverloads.jl:297-299)."""
+    if isinstance(R, np.ndarray):
+        return R.shape
+    a, b = rhodlr_shape(R.A11), rhodlr_shape(R.A22)
+    return a[0] + b[0], a[1] + b[1]
+
+
+def rhodlr_mul(R, v: np.ndarray) -> np.ndarray:
+    """``*(R::RKernelHODLR, V)`` (src/HODLR/src/baseoverloads.jl:301-305), UVt products as
+    U (V' v) (:295)."""
+    if isinstance(R, np.ndarray):
+        return R @ v
+    c1 = rhodlr_shape(R.A11)[1]
+    v1, v2 = v[:c1], v[c1:]
+    top = rhodlr_mul(R.A11, v1) + R.A12[0] @ (R.A12[1].T @ v2)
+    bot = R.A21[0] @ (R.A21[1].T @ v1) + rhodlr_mul(R.A22, v2)
+    return np.concatenate([top, bot])
+
+
+def rhodlr_blocks(R) -> list:
+    """Off-diagonal blocks in recursive order: A12, A21, then those of A11, then of A22."""
+    if isinstance(R, np.ndarray):
+        return []
+    return [R.A12, R.A21] + rhodlr_blocks(R.A11) + rhodlr_blocks(R.A22)
+
+
 # ----------------------------------------------------------------------------------------------
 # Dense oracle: src/HODLR/src/exactmaxlik.jl
 # ----------------------------------------------------------------------------------------------
