@@ -508,7 +508,10 @@ def run_serve(args):
 
 def run_aca(args):
     """ACA assembly and general factorisation at n = 2^18 (range 0.05, nugget 1e-4, tol 1e-8,
-    LogLevel(8) => 10 levels), 8 right-hand sides, logdet."""
+    LogLevel(8) => 10 levels), 8 right-hand sides, logdet.  ``--aca-nugget`` changes the nugget:
+    at n = 2^18 the ACA error of the widest blocks is of the order of 1e-4, so the compressed
+    matrix with the config's nugget is not positive definite (the factorisation raises
+    PosDefException, as the reference's would)."""
     import torch
     import kmhodlr as K
     from kmhodlr.data import uniform_points
@@ -517,7 +520,7 @@ def run_aca(args):
     n = args.aca_n
     pts = uniform_points(n, SEED + 3)
     rhs = np.asfortranarray(np.random.default_rng(SEED + 4).standard_normal((n, 8)))
-    km = K.KernelMatrix(pts, pts, (1.0, 0.05, 1e-4), K.Matern32())
+    km = K.KernelMatrix(pts, pts, (1.0, 0.05, args.aca_nugget), K.Matern32())
     times = []
     for it in range(args.warmup + args.steps):
         torch.cuda.synchronize()
@@ -538,7 +541,8 @@ def run_aca(args):
     out = {"metric": "ACA HODLR assemble+factor+solve/s", "value": 1.0 / tot, "unit": "steps/s", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"aca_matern32_n{n}_tol1e-8_loglevel8_8rhs", "n": n, "levels": int(np.log2(n)) - 8},
+           "config": {"workload": f"aca_matern32_n{n}_tol1e-8_loglevel8_8rhs", "n": n, "levels": int(np.log2(n)) - 8,
+                      "params": [1.0, 0.05, args.aca_nugget]},
            "phase_s": {"assemble": a, "factorize": f, "solve_logdet": s},
            "ranks": {"max": int(ranks.max()), "mean": float(ranks.mean()), "blocks": int(ranks.size)},
            "logdet": ld}
@@ -560,6 +564,7 @@ def main():
     ap.add_argument("--requests", type=int, default=2000, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: Poisson arrival rate (1/s)")
     ap.add_argument("--aca-n", type=int, default=2 ** 18, help="aca: number of points")
+    ap.add_argument("--aca-nugget", type=float, default=1e-4, help="aca: nugget of the Matern kernel")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

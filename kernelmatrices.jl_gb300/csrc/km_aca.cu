@@ -588,6 +588,7 @@ __global__ void __launch_bounds__(256) k_gapply(const GApplyItem* __restrict__ i
                                                 const double* Xin, int64_t ldX, int kX) {
   extern __shared__ double sm[];
   const GApplyItem I = items[blockIdx.x];
+  if (I.big) return;  // large nodes go through the library-GEMM path
   const GNodeDesc N = nodes[I.node];
   const int r = N.r;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -722,6 +723,76 @@ __global__ void __launch_bounds__(256) k_gapply(const GApplyItem* __restrict__ i
       double acc = 0.0;
       for (int q = 0; q < r; ++q) acc += Q2[i + (int64_t)q * s2] * t[q];
       y2[i] += acc;
+    }
+  }
+}
+
+// The r x r part of k_gapply (same operations in the same order) for the nodes whose
+// projections and expansions run as library GEMMs: one warp per column.
+__global__ void k_gsmall(const GNodeDesc* __restrict__ node, int mode, const double* __restrict__ Z1,
+                         const double* __restrict__ Z2, double* __restrict__ G1, double* __restrict__ G2) {
+  extern __shared__ double sm[];
+  const GNodeDesc N = *node;
+  const int r = N.r;
+  const int lane = threadIdx.x;
+  const int col = blockIdx.x;
+  double* z1 = sm;
+  double* z2 = z1 + r;
+  double* t = z2 + r;
+  for (int i = lane; i < r; i += 32) {
+    z1[i] = (mode == 0 || mode == 2) ? Z1[(int64_t)col * r + i] : 0.0;
+    z2[i] = Z2[(int64_t)col * r + i];
+  }
+  __syncwarp();
+  const double* C = N.C;
+  const double* Lm = N.L22;
+  double* g1 = G1 + (int64_t)col * r;
+  double* g2 = G2 + (int64_t)col * r;
+  if (mode == 0) {
+    for (int i = lane; i < r; i += 32) {
+      double acc = 0.0;
+      for (int l = 0; l < r; ++l) acc += C[l + (int64_t)i * r] * z1[l];
+      t[i] = z2[i] - acc;
+    }
+    __syncwarp();
+    for (int l = 0; l < r; ++l) {
+      const double v = t[l] / Lm[l + (int64_t)l * r];
+      __syncwarp();
+      if (lane == 0) t[l] = v;
+      for (int i = l + 1 + lane; i < r; i += 32) t[i] -= Lm[i + (int64_t)l * r] * v;
+      __syncwarp();
+    }
+    for (int i = lane; i < r; i += 32) g2[i] = z2[i] - t[i];
+  } else if (mode == 1) {
+    for (int i = lane; i < r; i += 32) t[i] = z2[i];
+    __syncwarp();
+    for (int i = r - 1; i >= 0; --i) {
+      const double v = t[i] / Lm[i + (int64_t)i * r];
+      __syncwarp();
+      if (lane == 0) t[i] = v;
+      for (int l = lane; l < i; l += 32) t[l] -= Lm[i + (int64_t)l * r] * v;
+      __syncwarp();
+    }
+    for (int i = lane; i < r; i += 32) {
+      double acc = 0.0;
+      for (int l = 0; l < r; ++l) acc += C[i + (int64_t)l * r] * t[l];
+      g1[i] = acc;
+      g2[i] = z2[i] - t[i];
+    }
+  } else if (mode == 2) {
+    for (int i = lane; i < r; i += 32) {
+      double acc = 0.0;
+      for (int l = 0; l < r; ++l) acc += C[l + (int64_t)i * r] * z1[l];
+      for (int l = 0; l <= i; ++l) acc += Lm[i + (int64_t)l * r] * z2[l];
+      g2[i] = acc - z2[i];
+    }
+  } else {
+    for (int i = lane; i < r; i += 32) {
+      double a1 = 0.0, a2 = 0.0;
+      for (int l = 0; l < r; ++l) a1 += C[i + (int64_t)l * r] * z2[l];
+      for (int l = i; l < r; ++l) a2 += Lm[l + (int64_t)i * r] * z2[l];
+      g1[i] = a1;
+      g2[i] = a2 - z2[i];
     }
   }
 }
@@ -1170,6 +1241,14 @@ void launch_gapply(const GApplyItem* items, int n, const GNodeDesc* nodes, int m
   const size_t sm = (size_t)8 * 3 * std::max(maxr, 1) * sizeof(double);
   smem_limit((const void*)k_gapply, sm);
   k_gapply<<<grid, 256, sm, st>>>(items, nodes, mode, X, Xin, ldX, kX);
+}
+
+void launch_gsmall(const GNodeDesc* node, int mode, const double* Z1, const double* Z2, double* G1, double* G2,
+                   int r, int ncols, cudaStream_t st) {
+  if (ncols <= 0 || r <= 0) return;
+  const size_t sm = (size_t)3 * r * sizeof(double);
+  smem_limit((const void*)k_gsmall, sm);
+  k_gsmall<<<(unsigned)ncols, 32, sm, st>>>(node, mode, Z1, Z2, G1, G2);
 }
 
 void launch_glogdet(const GNodeDesc* nodes, int nn, double* partial, cudaStream_t st) {

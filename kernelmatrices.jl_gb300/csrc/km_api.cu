@@ -3,6 +3,8 @@
 #include <algorithm>
 #include <mutex>
 #include <cmath>
+
+#include <cublas_v2.h>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -123,6 +125,10 @@ struct km_handle {
   GNodeDesc* d_gnodes = nullptr;
   GApplyItem* d_gsolve = nullptr;     // one item per block, rows relative to the right-hand side
   GApplyItem* d_gfact = nullptr;      // factorisation updates, grouped by level
+  std::vector<GNodeDesc> gnodes_h;    // host copies: the library-GEMM path of large nodes reads them
+  std::vector<GApplyItem> gsolve_h, gfact_h;
+  double* d_gz = nullptr;             // projections and coefficients of one large node (4 x r x ncols)
+  cublasHandle_t cublas = nullptr;
   std::vector<int64_t> gfoff;
   PanelDesc* d_pdesc = nullptr;
   LeafDesc* d_ldesc = nullptr;
@@ -270,6 +276,10 @@ void free_problem(km_handle* h) {
   h->d_R12 = h->d_CL = nullptr;
   h->d_gnodes = nullptr;
   h->d_gsolve = h->d_gfact = nullptr;
+  h->gnodes_h.clear();
+  h->gsolve_h.clear();
+  h->gfact_h.clear();
+  h->d_gz = nullptr;
   h->d_pdesc = nullptr;
   h->d_ldesc = nullptr;
   h->nldesc = 0;
@@ -385,6 +395,84 @@ NodeMatsH node_mats(km_handle* h) {
 // ---- factor sweeps on a device block X (n x k, ld = n), in place ---------------------------
 
 // ---- general (ACA) path -------------------------------------------------------------------
+
+// Nodes at least this large (rows of both children) apply their factor through library GEMMs:
+// k_gapply gives one warp per (node, column), which serialises the O(size x rank) projections
+// of the top levels on a few SMs.
+constexpr int64_t kGapplyBig = 16384;
+
+// Applies the node factors of items [a, b) of a level (host list hl, device list dl): k_gapply for
+// the small nodes, and for every large node Z = Q' x (DGEMM), the r x r part (k_gsmall), then
+// y -= / += Q G (DGEMM).  Modes as in k_gapply: 0 W^{-1}, 1 W'^{-1}, 2 W, 3 W', 4 pre-factor
+// product (Q1 = V rows c1, Q2 = U rows c2; y1 += V U' x2, y2 += U V' x1).
+static int run_gapply(km_handle* h, const std::vector<GApplyItem>& hl, GApplyItem* dl, int64_t a, int64_t b,
+                      int maxcols, int mode, double* X, const double* Xin, int64_t ldX, int kX) {
+  cudaStream_t st = h->stream;
+  if (b <= a) return KM_OK;
+  KLV(h, KM_PROF_SWEEP, launch_gapply(dl + a, (int)(b - a), h->d_gnodes, h->gmaxr, maxcols, mode, X, Xin, ldX, kX, st));
+  int64_t need = 0;
+  for (int64_t q = a; q < b; ++q)
+    if (hl[q].big) {
+      const GNodeDesc& N = h->gnodes_h[hl[q].node];
+      const int nc = hl[q].base ? hl[q].ncols : kX;
+      need = std::max<int64_t>(need, 4 * (int64_t)N.r * nc);
+    }
+  if (need == 0) return KM_OK;
+  int rc;
+  if ((rc = grow(h, &h->d_gz, need)) != KM_OK) return rc;
+  if (!h->cublas) {
+    if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS) return fail(h, KM_ERR_CUDA, "cublasCreate failed");
+  }
+  cublasSetStream(h->cublas, st);
+  const double one = 1.0, zero = 0.0, mone = -1.0;
+  for (int64_t q = a; q < b; ++q) {
+    const GApplyItem& I = hl[q];
+    if (!I.big) continue;
+    const GNodeDesc& N = h->gnodes_h[I.node];
+    const int r = N.r;
+    double* base = I.base ? I.base : X;
+    const int64_t ld = I.base ? I.ld : ldX;
+    const int nc = I.base ? I.ncols : kX;
+    if (r <= 0 || nc <= 0) continue;
+    double* y1 = base + I.off1;
+    double* y2 = base + I.off2;
+    const double* x1 = (mode == 4) ? Xin + I.off1 : y1;
+    const double* x2 = (mode == 4) ? Xin + I.off2 : y2;
+    double* Z1 = h->d_gz;
+    double* Z2 = Z1 + (int64_t)r * nc;
+    double* G1 = Z2 + (int64_t)r * nc;
+    double* G2 = G1 + (int64_t)r * nc;
+    const int s1 = (int)N.s1, s2 = (int)N.s2;
+    const int ldi = (int)ld;
+    cublasStatus_t cs = CUBLAS_STATUS_SUCCESS;
+    auto gemm_t = [&](const double* Q, int s, const double* x, double* Z) {  // Z = Q' x
+      if (cs == CUBLAS_STATUS_SUCCESS)
+        cs = cublasDgemm(h->cublas, CUBLAS_OP_T, CUBLAS_OP_N, r, nc, s, &one, Q, s, x, ldi, &zero, Z, r);
+    };
+    auto gemm_n = [&](const double* Q, int s, const double* G, double* y, const double* alpha) {  // y += a Q G
+      if (cs == CUBLAS_STATUS_SUCCESS)
+        cs = cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, s, nc, r, alpha, Q, s, G, r, &one, y, ldi);
+    };
+    const GNodeDesc* dN = h->d_gnodes + I.node;
+    KLV(h, KM_PROF_SWEEP, {
+      if (mode == 4) {
+        gemm_t(N.Q2, s2, x2, Z1);  // U' x2
+        gemm_t(N.Q1, s1, x1, Z2);  // V' x1
+        gemm_n(N.Q1, s1, Z1, y1, &one);
+        gemm_n(N.Q2, s2, Z2, y2, &one);
+      } else {
+        if (mode == 0 || mode == 2) gemm_t(N.Q1, s1, x1, Z1);
+        gemm_t(N.Q2, s2, x2, Z2);
+        launch_gsmall(dN, mode, Z1, Z2, G1, G2, r, nc, st);
+        if (mode == 1 || mode == 3) gemm_n(N.Q1, s1, G1, y1, mode == 1 ? &mone : &one);
+        gemm_n(N.Q2, s2, G2, y2, (mode == 0 || mode == 1) ? &mone : &one);
+      }
+    });
+    if (cs != CUBLAS_STATUS_SUCCESS) return fail(h, KM_ERR_CUDA, "cublasDgemm failed");
+  }
+  return KM_OK;
+}
+
 int general_fwd(km_handle* h, double* X, int k) {  // X <- W^{-1} X
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
@@ -392,7 +480,8 @@ int general_fwd(km_handle* h, double* X, int k) {  // X <- W^{-1} X
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
   for (int l = 1; l <= t.L; ++l) {
     const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
-    KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 0, X, X, t.n, k, st));
+    int rc;
+    if ((rc = run_gapply(h, h->gsolve_h, h->d_gsolve, a, b, k, 0, X, X, t.n, k)) != KM_OK) return rc;
   }
   return check_launch(h, "general fwd");
 }
@@ -402,7 +491,8 @@ int general_bwd(km_handle* h, double* X, int k) {  // X <- W'^{-1} X
   cudaStream_t st = h->stream;
   for (int l = t.L; l >= 1; --l) {
     const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
-    KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 1, X, X, t.n, k, st));
+    int rc;
+    if ((rc = run_gapply(h, h->gsolve_h, h->d_gsolve, a, b, k, 1, X, X, t.n, k)) != KM_OK) return rc;
   }
   if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<double>(h->d_Lf, t, 1, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
@@ -414,7 +504,8 @@ int general_mul(km_handle* h, double* X, int k) {  // X <- W X
   cudaStream_t st = h->stream;
   for (int l = t.L; l >= 1; --l) {
     const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
-    KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 2, X, X, t.n, k, st));
+    int rc;
+    if ((rc = run_gapply(h, h->gsolve_h, h->d_gsolve, a, b, k, 2, X, X, t.n, k)) != KM_OK) return rc;
   }
   if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<double>(h->d_Lf, t, 2, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular kernel");
@@ -428,7 +519,8 @@ int general_mul_t(km_handle* h, double* X, int k) {  // X <- W' X
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular kernel");
   for (int l = 1; l <= t.L; ++l) {
     const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
-    KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 3, X, X, t.n, k, st));
+    int rc;
+    if ((rc = run_gapply(h, h->gsolve_h, h->d_gsolve, a, b, k, 3, X, X, t.n, k)) != KM_OK) return rc;
   }
   return check_launch(h, "general mul_t");
 }
@@ -441,7 +533,8 @@ int general_matvec(km_handle* h, const double* X, double* Y, int k) {
   KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_nys_apply(h->d_K, nullptr, nullptr, 0, t, X, t.n, nullptr, Y, t.n, k, st));
   for (int l = 1; l <= t.L; ++l) {
     const int64_t a = h->lvoff[l], b = h->lvoff[l + 1];
-    KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gsolve + a, (int)(b - a), h->d_gnodes, h->gmaxr, k, 4, Y, X, t.n, k, st));
+    int rc;
+    if ((rc = run_gapply(h, h->gsolve_h, h->d_gsolve, a, b, k, 4, Y, X, t.n, k)) != KM_OK) return rc;
   }
   return check_launch(h, "general matvec");
 }
@@ -818,15 +911,21 @@ int km_create(const km_config* cfg, km_handle** out) {
     delete h;
     return KM_ERR_BAD_ARG;
   }
+  // The main stream runs at the highest priority and the side stream (solve operators formed
+  // while the node levels run) at the lowest: a node-level CTA needs a whole SM, and when a level
+  // ends the next level and the previous level's side work become ready together; the priorities
+  // let the block scheduler place the critical-path CTAs first.
+  int prio_low = 0, prio_high = 0;
   if (cudaSetDevice(h->cfg.device) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
       cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
     cudaGetLastError();
     delete h;
     return KM_ERR_CUDA;
   }
   h->own_stream = h->stream;
-  if (cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_low) != cudaSuccess) {
     cudaGetLastError();
     delete h;
     return KM_ERR_CUDA;
@@ -869,6 +968,7 @@ int km_destroy(km_handle* h) {
   if (!h) return KM_OK;
   cudaSetDevice(h->cfg.device);
   free_problem(h);
+  if (h->cublas) cublasDestroy(h->cublas);
   prof_resolve(h);
   for (auto e : h->pool) cudaEventDestroy(e);
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -1032,8 +1132,10 @@ static int aca_assemble(km_handle* h, const double* pts, bool dev, const Tree& t
     N.s2 = b.nro;
     N.r = rq;
     o += (int64_t)rq * rq;
-    items[q] = GApplyItem{q, 0, b.col0, b.row0, 0, nullptr};
+    items[q] = GApplyItem{q, 0, b.col0, b.row0, 0, nullptr, (b.nro + b.ncl >= kGapplyBig) ? 1 : 0};
   }
+  h->gnodes_h = nodes;
+  h->gsolve_h = items;
   if (nb > 0) {
     KM_CUDA(h, cudaMemcpy(h->d_gnodes, nodes.data(), sizeof(GNodeDesc) * nb, cudaMemcpyHostToDevice));
     KM_CUDA(h, cudaMemcpy(h->d_gsolve, items.data(), sizeof(GApplyItem) * nb, cudaMemcpyHostToDevice));
@@ -1092,7 +1194,8 @@ static int general_factorize(km_handle* h) {
           double* panel = h->d_panels + (first ? bp.offV : bp.offU);
           const int64_t side0 = first ? bp.col0 : bp.row0;
           const int64_t ldp = first ? bp.ncl : bp.nro;
-          fi.push_back(GApplyItem{q, h->brank[qp], b.col0 - side0, b.row0 - side0, ldp, panel});
+          fi.push_back(GApplyItem{q, h->brank[qp], b.col0 - side0, b.row0 - side0, ldp, panel,
+                                  (b.nro + b.ncl >= kGapplyBig) ? 1 : 0});
           maxcols = std::max(maxcols, h->brank[qp]);
         }
       }
@@ -1112,6 +1215,7 @@ static int general_factorize(km_handle* h) {
     KM_CUDA(h, cudaMemcpy(h->d_pdesc, pd.data(), sizeof(PanelDesc) * pd.size(), cudaMemcpyHostToDevice));
     if (!fi.empty())
       KM_CUDA(h, cudaMemcpy(h->d_gfact, fi.data(), sizeof(GApplyItem) * fi.size(), cudaMemcpyHostToDevice));
+    h->gfact_h = fi;
     // panel QR scratch (taus and block T factors) for the largest level
     std::vector<int> kmax_l(t.L + 2, 0);
     int64_t pqs = 1;
@@ -1129,9 +1233,8 @@ static int general_factorize(km_handle* h) {
       KLV(h, KM_PROF_NODE, launch_gnode(h->d_gnodes + h->lvoff[l], (int)(h->lvoff[l + 1] - h->lvoff[l]),
                                         h->d_info + t.nleaf + h->lvoff[l], st));
       const int64_t a = h->gfoff[l], b = h->gfoff[l + 1];
-      if (b > a)
-        KLV(h, KM_PROF_SWEEP, launch_gapply(h->d_gfact + a, (int)(b - a), h->d_gnodes, h->gmaxr, maxcols, 0,
-                                            nullptr, nullptr, 0, 0, st));
+      if (b > a && (rc = run_gapply(h, h->gfact_h, h->d_gfact, a, b, maxcols, 0, nullptr, nullptr, 0, 0)) != KM_OK)
+        return rc;
     }
   }
   if ((rc = check_launch(h, "general factorize")) != KM_OK) return rc;

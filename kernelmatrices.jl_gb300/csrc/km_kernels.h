@@ -51,6 +51,7 @@ struct GApplyItem {           // node factor applied to rows off1.. (c1) and off
   int ncols;
   int64_t off1, off2, ld;
   double* base;               // nullptr: the right-hand-side block passed to the kernel
+  int big;                    // 1: applied with library GEMMs by the host path (k_gapply skips it)
 };
 struct LeafDesc {             // leaf triangular operation on an arbitrary column block
   int64_t leaf;
@@ -168,6 +169,10 @@ void launch_gnode(const GNodeDesc* nodes, int n, int* info, cudaStream_t st);
 void launch_gapply(const GApplyItem* items, int n, const GNodeDesc* nodes, int maxr, int maxcols, int mode,
                    double* X, const double* Xin, int64_t ldX, int kX, cudaStream_t st);
 void launch_glogdet(const GNodeDesc* nodes, int nn, double* partial, cudaStream_t st);
+// the r x r part of k_gapply for one node and ncols columns: from the projections Z1 = Q1' x1,
+// Z2 = Q2' x2 (r x ncols each; mode 4 is not handled here) to the expansion coefficients G1, G2
+void launch_gsmall(const GNodeDesc* node, int mode, const double* Z1, const double* Z2, double* G1, double* G2,
+                   int r, int ncols, cudaStream_t st);
 bool launch_leaf_tri_desc(const double* Lf, const Tree& t, int op, const LeafDesc* descs, int n, int maxcols,
                           cudaStream_t st);
 
