@@ -15,6 +15,8 @@
 // the c2 rows:  y_c2 -= Q2 (z2 - L22^{-1}(z2 - C' z1)),  z1 = Q1' y_c1, z2 = Q2' y_c2.
 #include <climits>
 
+#include <cublas_v2.h>
+
 #include "km_kernels.h"
 
 namespace km {
@@ -466,7 +468,7 @@ __global__ void __launch_bounds__(256) k_pq_update(const PanelDesc* __restrict__
   __shared__ double Tm[kQB * kQB];
   const PanelDesc D = descs[blockIdx.x];
   const int k = D.k;
-  if (j0 >= k) return;
+  if (j0 >= k || D.big) return;
   const int jb = min(kQB, k - j0), j1 = j0 + jb;
   const int c0 = j1 + blockIdx.y * kQU;
   if (c0 >= k) return;
@@ -1221,6 +1223,74 @@ void launch_panel_qr(const PanelDesc* descs, int n, int kmax, double* taus, doub
   k_pq_rout<<<n, 256, 0, st>>>(descs);
   for (int b = nblk - 1; b >= 0; --b) {
     k_pq_update<<<dim3((unsigned)n, (unsigned)ntiles), 256, smu, st>>>(descs, b * kQB, Ts, nblk, 0);
+    k_pq_form<<<n, 512, 0, st>>>(descs, b * kQB, taus, kmax);
+  }
+}
+
+// explicit reflector block V (rows j0 .. m-1 of columns j0 .. j0+jb-1: unit diagonal, zeros
+// above it, the stored vectors below), column-major with leading dimension m - j0
+__global__ void k_pq_vcopy(const PanelDesc* __restrict__ desc, int j0, double* __restrict__ V) {
+  const PanelDesc D = *desc;
+  const int jb = min(kQB, D.k - j0);
+  const int64_t mr = D.m - j0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < mr * jb; e += (int64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(e / mr);
+    const int64_t i = e - (int64_t)p * mr;
+    V[e] = (i == p) ? 1.0 : (i > p ? D.A[(int64_t)(j0 + p) * D.lda + j0 + i] : 0.0);
+  }
+}
+
+int64_t panel_qr_gemm_scratch(const PanelDesc* hdescs, int n, int kmax) {
+  int64_t mbig = 0;
+  for (int p = 0; p < n; ++p)
+    if (hdescs[p].big) mbig = std::max<int64_t>(mbig, hdescs[p].m);
+  return mbig * kQB + 2 * (int64_t)kQB * std::max(kmax, 1);
+}
+
+// C[:, j1:k] <- (I - V op(T) V') C[:, j1:k] for big panel p, block j0: W = V' C, W2 = op(T) W,
+// C -= V W2 (op(T) = T' while factoring, T while forming Q), then the small panels' blocks by
+// k_pq_update
+static void panel_block_gemm(const PanelDesc* descs, const PanelDesc& D, int p, int j0, int nblk, const double* Ts,
+                             double* scr, int kmax, cublasHandle_t cub, int transT, cudaStream_t st) {
+  const int k = D.k;
+  if (j0 >= k) return;
+  const int jb = std::min(kQB, k - j0), j1 = j0 + jb;
+  const int nt = k - j1;
+  if (nt <= 0) return;
+  const int64_t mr = D.m - j0;
+  double* V = scr;
+  double* W = V + mr * kQB;
+  double* W2 = W + (int64_t)kQB * kmax;
+  const unsigned g = (unsigned)std::min<int64_t>((mr * jb + 255) / 256, 4096);
+  k_pq_vcopy<<<g, 256, 0, st>>>(descs + p, j0, V);
+  const double* Tm = Ts + ((int64_t)p * nblk + j0 / kQB) * kQB * kQB;
+  double* C = D.A + (int64_t)j1 * D.lda + j0;
+  const double one = 1.0, zero = 0.0, mone = -1.0;
+  cublasDgemm(cub, CUBLAS_OP_T, CUBLAS_OP_N, jb, nt, (int)mr, &one, V, (int)mr, C, (int)D.lda, &zero, W, jb);
+  cublasDgemm(cub, transT ? CUBLAS_OP_T : CUBLAS_OP_N, CUBLAS_OP_N, jb, nt, jb, &one, Tm, kQB, W, jb, &zero, W2, jb);
+  cublasDgemm(cub, CUBLAS_OP_N, CUBLAS_OP_N, (int)mr, nt, jb, &mone, V, (int)mr, W2, jb, &one, C, (int)D.lda);
+}
+
+void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n, int kmax, double* taus,
+                          double* Ts, double* gemm_scratch, void* cublas_handle, cudaStream_t st) {
+  if (n <= 0 || kmax <= 0) return;
+  cublasHandle_t cub = static_cast<cublasHandle_t>(cublas_handle);
+  cublasSetStream(cub, st);
+  const int nblk = (kmax + kQB - 1) / kQB;
+  const int ntiles = (kmax + kQU - 1) / kQU;
+  const size_t smu = ((size_t)2 * kQB * kQU + kQC * kQV) * sizeof(double);
+  smem_limit((const void*)k_pq_update, smu);
+  for (int b = 0; b < nblk; ++b) {
+    k_pq_factor<<<n, 512, 0, st>>>(descs, b * kQB, taus, kmax, Ts, nblk);
+    k_pq_update<<<dim3((unsigned)n, (unsigned)ntiles), 256, smu, st>>>(descs, b * kQB, Ts, nblk, 1);
+    for (int p = 0; p < n; ++p)
+      if (hdescs[p].big) panel_block_gemm(descs, hdescs[p], p, b * kQB, nblk, Ts, gemm_scratch, kmax, cub, 1, st);
+  }
+  k_pq_rout<<<n, 256, 0, st>>>(descs);
+  for (int b = nblk - 1; b >= 0; --b) {
+    k_pq_update<<<dim3((unsigned)n, (unsigned)ntiles), 256, smu, st>>>(descs, b * kQB, Ts, nblk, 0);
+    for (int p = 0; p < n; ++p)
+      if (hdescs[p].big) panel_block_gemm(descs, hdescs[p], p, b * kQB, nblk, Ts, gemm_scratch, kmax, cub, 0, st);
     k_pq_form<<<n, 512, 0, st>>>(descs, b * kQB, taus, kmax);
   }
 }

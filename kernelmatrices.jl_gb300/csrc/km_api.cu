@@ -129,6 +129,7 @@ struct km_handle {
   std::vector<GNodeDesc> gnodes_h;    // host copies: the library-GEMM path of large nodes reads them
   std::vector<GApplyItem> gsolve_h, gfact_h;
   double* d_gz = nullptr;             // projections and coefficients of one large node (4 x r x ncols)
+  double* d_pqg = nullptr;            // explicit reflector block and products of the tall-panel QR
   cublasHandle_t cublas = nullptr;
   std::vector<int64_t> gfoff;
   PanelDesc* d_pdesc = nullptr;
@@ -291,6 +292,7 @@ void free_problem(km_handle* h) {
   h->gsolve_h.clear();
   h->gfact_h.clear();
   h->d_gz = nullptr;
+  h->d_pqg = nullptr;
   h->d_pdesc = nullptr;
   h->d_ldesc = nullptr;
   h->nldesc = 0;
@@ -411,6 +413,9 @@ NodeMatsH node_mats(km_handle* h) {
 // k_gapply gives one warp per (node, column), which serialises the O(size x rank) projections
 // of the top levels on a few SMs.
 constexpr int64_t kGapplyBig = 16384;
+// Panels with at least this many rows apply their block reflectors as library GEMMs (one CTA per
+// 8-column tile over all rows leaves most SMs idle on the few tall panels of the top levels).
+constexpr int64_t kPanelBig = 16384;
 
 // Applies the node factors of items [a, b) of a level (host list hl, device list dl): k_gapply for
 // the small nodes, and for every large node Z = Q' x (DGEMM), the r x r part (k_gsmall), then
@@ -1255,8 +1260,9 @@ static int general_factorize(km_handle* h) {
         int64_t o = 0;
         for (int p = 0; p < q; ++p) o += (int64_t)h->brank[p] * h->brank[p];
         const int rq = h->brank[q];
-        pd.push_back(PanelDesc{h->d_panels + b.offV, b.ncl, b.ncl, rq, h->d_R12 + 2 * o});
-        pd.push_back(PanelDesc{h->d_panels + b.offU, b.nro, b.nro, rq, h->d_R12 + 2 * o + (int64_t)rq * rq});
+        pd.push_back(PanelDesc{h->d_panels + b.offV, b.ncl, b.ncl, rq, h->d_R12 + 2 * o, b.ncl >= kPanelBig ? 1 : 0});
+        pd.push_back(PanelDesc{h->d_panels + b.offU, b.nro, b.nro, rq, h->d_R12 + 2 * o + (int64_t)rq * rq,
+                               b.nro >= kPanelBig ? 1 : 0});
         for (int lev = l + 1; lev <= t.L; ++lev) {
           const int64_t kp = k >> (lev - l);
           const int qp = (int)(h->lvoff[lev] + kp);
@@ -1299,8 +1305,19 @@ static int general_factorize(km_handle* h) {
       return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
     for (int l = 1; l <= t.L; ++l) {
       const int np = (int)(pdoff[l + 1] - pdoff[l]);
-      KLV(h, KM_PROF_LEAF_QR, launch_panel_qr(h->d_pdesc + pdoff[l], np, kmax_l[l], h->d_pqs,
-                                              h->d_pqs + (int64_t)np * kmax_l[l], st));
+      bool anybig = false;
+      for (int64_t p = pdoff[l]; p < pdoff[l + 1]; ++p) anybig |= pd[p].big != 0;
+      if (anybig) {
+        if (!h->cublas && cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS)
+          return fail(h, KM_ERR_CUDA, "cublasCreate failed");
+        if ((rc = grow(h, &h->d_pqg, panel_qr_gemm_scratch(pd.data() + pdoff[l], np, kmax_l[l])))) return rc;
+        KLV(h, KM_PROF_LEAF_QR, launch_panel_qr_gemm(h->d_pdesc + pdoff[l], pd.data() + pdoff[l], np, kmax_l[l],
+                                                     h->d_pqs, h->d_pqs + (int64_t)np * kmax_l[l], h->d_pqg,
+                                                     h->cublas, st));
+      } else {
+        KLV(h, KM_PROF_LEAF_QR, launch_panel_qr(h->d_pdesc + pdoff[l], np, kmax_l[l], h->d_pqs,
+                                                h->d_pqs + (int64_t)np * kmax_l[l], st));
+      }
       KLV(h, KM_PROF_NODE, launch_gnode(h->d_gnodes + h->lvoff[l], (int)(h->lvoff[l + 1] - h->lvoff[l]),
                                         h->d_info + t.nleaf + h->lvoff[l], st));
       const int64_t a = h->gfoff[l], b = h->gfoff[l + 1];

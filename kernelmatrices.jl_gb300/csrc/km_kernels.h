@@ -35,6 +35,7 @@ struct PanelDesc {            // Householder QR with explicit Q of A (m x k, lea
   int64_t m, lda;
   int k;
   double* R;                  // k x k output
+  int big;                    // 1: block reflectors applied with library GEMMs (k_pq_update skips it)
 };
 struct GNodeDesc {            // one node of the general factorisation
   double* Q1;                 // V panel (rows c1), Q after the QR
@@ -164,6 +165,11 @@ void launch_aca_one(const double* pts, KParams kp, const AcaBlock* blocks, int b
 // Householder QR with explicit Q of n panels (largest column count kmax); scratch of
 // panel_qr_scratch(n, kmax) doubles: taus (n x kmax) then the T factors
 void launch_panel_qr(const PanelDesc* descs, int n, int kmax, double* taus, double* Ts, cudaStream_t st);
+// the same with the block-reflector applications of the panels marked big run as cuBLAS DGEMMs
+// (hdescs: host copies of descs; gemm_scratch: panel_qr_gemm_scratch(hdescs, n, kmax) doubles)
+void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n, int kmax, double* taus,
+                          double* Ts, double* gemm_scratch, void* cublas_handle, cudaStream_t st);
+int64_t panel_qr_gemm_scratch(const PanelDesc* hdescs, int n, int kmax);
 int64_t panel_qr_scratch(int n, int kmax);
 void launch_gnode(const GNodeDesc* nodes, int n, int* info, cudaStream_t st);
 void launch_gapply(const GApplyItem* items, int n, const GNodeDesc* nodes, int maxr, int maxcols, int mode,

@@ -141,3 +141,27 @@ def test_grid_aca_large_block(lib):
     ld0 = O.hodlr_logdet(ohk)
     assert abs(hk.logdet() - ld0) < 1e-8 + 1e-12 * abs(ld0)
     assert rel(hk.ldiv(rhs), O.hodlr_ldiv(ohk, rhs)) < 1e-9
+
+
+def test_tall_panels_library_gemm_path(lib):
+    """n = 32768: the top blocks have 16384 rows, so their panel QR block reflectors and the
+    application of their node factors run as library GEMMs; ranks and pivots (RQ) equal the
+    oracle's, and logdet and solves agree as on the kernel path."""
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    n = 32768
+    pts = uniform_points(n, 77)
+    params = (1.0, 0.15, 1e-2)
+    ok = O.KernelMatrix(pts, pts, np.array(params), O.KERNEL_RQ)
+    ohk = O.build_hodlr(ok, 1e-9, 0, O.LogLevel(8), nystrom=False)
+    hk = K.KernelHODLR(K.KernelMatrix(pts, pts, params, K.RatQuad()), 1e-9, 0, K.LogLevel(8), nystrom=False)
+    assert list(hk.block_ranks()) == [u.shape[1] for lv in ohk.U for u in lv]
+    rhs = np.random.default_rng(9).standard_normal((n, 2))
+    assert rel(hk @ rhs, O.hodlr_mul(ohk, rhs)) < 1e-12
+    O.symmetricfactorize(ohk)
+    K.symmetricfactorize(hk)
+    ld0 = O.hodlr_logdet(ohk)
+    assert abs(hk.logdet() - ld0) < 1e-8 + 1e-12 * abs(ld0)
+    assert rel(hk.ldiv(rhs), O.hodlr_ldiv(ohk, rhs)) < 1e-9
+    assert rel(hk.W.T @ hk.W.T.ldiv(rhs), rhs) < 1e-10
+    assert rel(hk.W @ hk.W.ldiv(rhs), rhs) < 1e-10
