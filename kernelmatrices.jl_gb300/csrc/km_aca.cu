@@ -406,13 +406,13 @@ constexpr int kQU = 8;  // trailing columns per update CTA (each CTA is FP64-bou
 
 __global__ void __launch_bounds__(512) k_pq_factor(const PanelDesc* __restrict__ descs, int j0,
                                                    double* __restrict__ taus, int ldtau, double* __restrict__ Ts,
-                                                   int nblk) {
+                                                   int nblk, int skip_big = 0) {
   __shared__ double red[40];
   __shared__ double sh[2];
   __shared__ double G[kQB * kQB], Tm[kQB * kQB];
   const PanelDesc D = descs[blockIdx.x];
   const int k = D.k;
-  if (j0 >= k) return;
+  if (j0 >= k || (skip_big && D.big)) return;
   double* A = D.A;
   const int64_t m = D.m, lda = D.lda;
   double* tau = taus + (int64_t)blockIdx.x * ldtau;
@@ -492,10 +492,10 @@ __global__ void k_pq_rout(const PanelDesc* __restrict__ descs) {
 
 // dorg2r on the block's own columns j0 .. j1-1 (the columns to its right are already formed).
 __global__ void __launch_bounds__(512) k_pq_form(const PanelDesc* __restrict__ descs, int j0,
-                                                 const double* __restrict__ taus, int ldtau) {
+                                                 const double* __restrict__ taus, int ldtau, int skip_big = 0) {
   const PanelDesc D = descs[blockIdx.x];
   const int k = D.k;
-  if (j0 >= k) return;
+  if (j0 >= k || (skip_big && D.big)) return;
   double* A = D.A;
   const int64_t m = D.m, lda = D.lda;
   const double* tau = taus + (int64_t)blockIdx.x * ldtau;
@@ -1227,6 +1227,188 @@ void launch_panel_qr(const PanelDesc* descs, int n, int kmax, double* taus, doub
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Factor and form steps of one 8-column block of ONE tall panel by all SMs (cooperative launch):
+// CTA b owns the contiguous row slice [b*rows, (b+1)*rows); every sum over rows is formed as
+// per-CTA partials that all CTAs add in CTA order after a bounded grid barrier (same value in
+// every CTA, same bits on every run); the partial buffers alternate between two halves so that a
+// phase never overwrites partials another CTA may still be reading; every element is updated by
+// the CTA that owns its row.  The operations per element are those of k_pq_factor / k_pq_form
+// (dgeqr2 / dlarfg and dorg2r rules); only the order of the row sums differs.
+// ---------------------------------------------------------------------------------------------
+constexpr int kPqParts = 32;  // partial slots per CTA per phase
+
+__device__ __forceinline__ double sum_parts(const double* part, int G, int slot) {
+  double s = 0.0;
+  for (int q = 0; q < G; ++q) s += __ldcg(part + (int64_t)q * kPqParts + slot);
+  return s;
+}
+
+// CTA partial of up to 28 values in one pass: red holds nw x kPqParts doubles
+__device__ void cta_parts(double (&v)[kPqParts], int nv, double* red, double* out) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int t = 0; t < nv; ++t) {
+    const double x = warp_sum(v[t]);
+    if (lane == 0) red[w * kPqParts + t] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double s = 0.0;
+    for (int q = 0; q < nw; ++q) s += red[q * kPqParts + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_pq_factor_grid(const PanelDesc* __restrict__ desc, int j0,
+                                                        double* __restrict__ tau, double* __restrict__ Tout,
+                                                        double* __restrict__ part, GridBar gb) {
+  __shared__ double red[8 * kPqParts];
+  const PanelDesc D = *desc;
+  double* A = D.A;
+  const int64_t m = D.m, lda = D.lda;
+  const int jb = min(kQB, D.k - j0), j1 = j0 + jb;
+  const int G = gridDim.x, b = blockIdx.x;
+  const int64_t rows = (m + G - 1) / G, r0 = (int64_t)b * rows, r1 = min(m, r0 + rows);
+  int phase = 0;
+  auto slot = [&]() { return part + (int64_t)(phase & 1) * G * kPqParts; };
+  for (int j = j0; j < j1; ++j) {
+    double* aj = A + (int64_t)j * lda;
+    const bool own_j = (j >= r0 && j < r1);
+    // ||x||^2 over rows j+1 .. m-1
+    double v[kPqParts];
+    v[0] = 0.0;
+    // alpha travels in slot 1 from the CTA owning row j (the other CTAs add exact zeros): the
+    // owner overwrites A[j][j] with beta once it is past the barrier
+    v[1] = (own_j && threadIdx.x == 0) ? aj[j] : 0.0;
+    for (int64_t i = max(r0, (int64_t)j + 1) + threadIdx.x; i < r1; i += blockDim.x) v[0] += aj[i] * aj[i];
+    cta_parts(v, 2, red, slot() + (int64_t)b * kPqParts);
+    if (!grid_barrier(gb)) return;
+    const double sig = sum_parts(slot(), G, 0);
+    const double alpha = sum_parts(slot(), G, 1);
+    ++phase;
+    double tj = 0.0, beta = alpha, scal = 0.0;
+    if (sig != 0.0) {
+      const double nrm = sqrt(alpha * alpha + sig);
+      beta = alpha >= 0.0 ? -nrm : nrm;
+      tj = (beta - alpha) / beta;
+      scal = 1.0 / (alpha - beta);
+    }
+    __syncthreads();  // every thread has read alpha before its owner overwrites it
+    if (own_j && threadIdx.x == 0) aj[j] = beta;
+    if (b == 0 && threadIdx.x == 0) tau[j] = tj;
+    for (int64_t i = max(r0, (int64_t)j + 1) + threadIdx.x; i < r1; i += blockDim.x) aj[i] *= scal;
+    __syncthreads();
+    if (tj == 0.0 || j + 1 >= j1) continue;
+    // v . A[:, c] for the block's columns c > j (unit entry of v at row j)
+    const int nc = j1 - j - 1;
+    for (int t = 0; t < nc; ++t) v[t] = 0.0;
+    for (int64_t i = max(r0, (int64_t)j + 1) + threadIdx.x; i < r1; i += blockDim.x) {
+      const double x = aj[i];
+      for (int t = 0; t < nc; ++t) v[t] += x * A[(int64_t)(j + 1 + t) * lda + i];
+    }
+    if (own_j && threadIdx.x == 0)
+      for (int t = 0; t < nc; ++t) v[t] += A[(int64_t)(j + 1 + t) * lda + j];
+    cta_parts(v, nc, red, slot() + (int64_t)b * kPqParts);
+    if (!grid_barrier(gb)) return;
+    double acc[kQB];
+    for (int t = 0; t < nc; ++t) acc[t] = sum_parts(slot(), G, t) * tj;
+    ++phase;
+    for (int64_t i = max(r0, (int64_t)j + 1) + threadIdx.x; i < r1; i += blockDim.x) {
+      const double x = aj[i];
+      for (int t = 0; t < nc; ++t) A[(int64_t)(j + 1 + t) * lda + i] -= acc[t] * x;
+    }
+    if (own_j && threadIdx.x == 0)
+      for (int t = 0; t < nc; ++t) A[(int64_t)(j + 1 + t) * lda + j] -= acc[t];
+    __syncthreads();
+  }
+  if (j1 >= D.k || Tout == nullptr) return;
+  // T of the block (panel_block_T): G[p][q] = v_p[j0+q] + sum_{i > j0+q} v_p[i] v_q[i], p < q
+  double v[kPqParts];
+  int np = 0;
+  for (int q = 1; q < jb; ++q)
+    for (int p2 = 0; p2 < q; ++p2) v[np++] = 0.0;
+  for (int64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+    int t = 0;
+    for (int q = 1; q < jb; ++q)
+      for (int p2 = 0; p2 < q; ++p2, ++t)
+        if (i > j0 + q) v[t] += A[(int64_t)(j0 + p2) * lda + i] * A[(int64_t)(j0 + q) * lda + i];
+  }
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int q = 1; q < jb; ++q)
+      for (int p2 = 0; p2 < q; ++p2, ++t)
+        if (j0 + q >= r0 && j0 + q < r1) v[t] += A[(int64_t)(j0 + p2) * lda + j0 + q];
+  }
+  cta_parts(v, np, red, slot() + (int64_t)b * kPqParts);
+  if (!grid_barrier(gb)) return;
+  if (b != 0 || threadIdx.x != 0) return;
+  double Gm[kQB * kQB], Tm[kQB * kQB];
+  {
+    int t = 0;
+    for (int q = 1; q < jb; ++q)
+      for (int p2 = 0; p2 < q; ++p2, ++t) Gm[p2 + q * kQB] = sum_parts(slot(), G, t);
+  }
+  for (int q = 0; q < jb; ++q) {
+    const double tq = tau[j0 + q];
+    for (int p2 = 0; p2 < q; ++p2) {
+      double z = 0.0;
+      for (int l = p2; l < q; ++l) z += Tm[p2 + l * kQB] * Gm[l + q * kQB];
+      Tm[p2 + q * kQB] = -tq * z;
+    }
+    Tm[q + q * kQB] = tq;
+    for (int p2 = q + 1; p2 < kQB; ++p2) Tm[p2 + q * kQB] = 0.0;
+  }
+  for (int e = 0; e < kQB * kQB; ++e) Tout[e] = (e % kQB < jb && e / kQB < jb) ? Tm[e] : 0.0;
+}
+
+// dorg2r on the block's own columns j0 .. j1-1 of one tall panel by all SMs
+__global__ void __launch_bounds__(256) k_pq_form_grid(const PanelDesc* __restrict__ desc, int j0,
+                                                      const double* __restrict__ tau, double* __restrict__ part,
+                                                      GridBar gb) {
+  __shared__ double red[8 * kPqParts];
+  const PanelDesc D = *desc;
+  double* A = D.A;
+  const int64_t m = D.m, lda = D.lda;
+  const int j1 = min(j0 + kQB, D.k);
+  const int G = gridDim.x, b = blockIdx.x;
+  const int64_t rows = (m + G - 1) / G, r0 = (int64_t)b * rows, r1 = min(m, r0 + rows);
+  int phase = 0;
+  for (int j = j1 - 1; j >= j0; --j) {
+    double* aj = A + (int64_t)j * lda;
+    const double tj = tau[j];
+    const bool own_j = (j >= r0 && j < r1);
+    if (j < j1 - 1) {
+      // v = e_j + A[j+1:, j]; c <- c - tau (v . c) v for the block's columns c > j
+      const int nc = j1 - j - 1;
+      double v[kPqParts];
+      for (int t = 0; t < nc; ++t) v[t] = 0.0;
+      for (int64_t i = max(r0, (int64_t)j + 1) + threadIdx.x; i < r1; i += blockDim.x) {
+        const double x = aj[i];
+        for (int t = 0; t < nc; ++t) v[t] += x * A[(int64_t)(j + 1 + t) * lda + i];
+      }
+      if (own_j && threadIdx.x == 0)
+        for (int t = 0; t < nc; ++t) v[t] += A[(int64_t)(j + 1 + t) * lda + j];
+      double* sl = part + (int64_t)(phase & 1) * G * kPqParts;
+      cta_parts(v, nc, red, sl + (int64_t)b * kPqParts);
+      if (!grid_barrier(gb)) return;
+      double acc[kQB];
+      for (int t = 0; t < nc; ++t) acc[t] = sum_parts(sl, G, t) * tj;
+      ++phase;
+      for (int64_t i = max(r0, (int64_t)j + 1) + threadIdx.x; i < r1; i += blockDim.x) {
+        const double x = aj[i];
+        for (int t = 0; t < nc; ++t) A[(int64_t)(j + 1 + t) * lda + i] -= acc[t] * x;
+      }
+      if (own_j && threadIdx.x == 0)
+        for (int t = 0; t < nc; ++t) A[(int64_t)(j + 1 + t) * lda + j] -= acc[t];
+    }
+    for (int64_t i = max(r0, (int64_t)j + 1) + threadIdx.x; i < r1; i += blockDim.x) aj[i] *= -tj;
+    for (int64_t i = r0 + threadIdx.x; i < min(r1, (int64_t)j); i += blockDim.x) aj[i] = 0.0;
+    if (own_j && threadIdx.x == 0) aj[j] = 1.0 - tj;
+    __syncthreads();
+  }
+}
+
 // explicit reflector block V (rows j0 .. m-1 of columns j0 .. j0+jb-1: unit diagonal, zeros
 // above it, the stored vectors below), column-major with leading dimension m - j0
 __global__ void k_pq_vcopy(const PanelDesc* __restrict__ desc, int j0, double* __restrict__ V) {
@@ -1244,7 +1426,7 @@ int64_t panel_qr_gemm_scratch(const PanelDesc* hdescs, int n, int kmax) {
   int64_t mbig = 0;
   for (int p = 0; p < n; ++p)
     if (hdescs[p].big) mbig = std::max<int64_t>(mbig, hdescs[p].m);
-  return mbig * kQB + 2 * (int64_t)kQB * std::max(kmax, 1);
+  return mbig * kQB + 2 * (int64_t)kQB * std::max(kmax, 1) + 2 * 152 * kPqParts + 8;
 }
 
 // C[:, j1:k] <- (I - V op(T) V') C[:, j1:k] for big panel p, block j0: W = V' C, W2 = op(T) W,
@@ -1271,8 +1453,34 @@ static void panel_block_gemm(const PanelDesc* descs, const PanelDesc& D, int p, 
   cublasDgemm(cub, CUBLAS_OP_N, CUBLAS_OP_N, (int)mr, nt, jb, &mone, V, (int)mr, W2, jb, &one, C, (int)D.lda);
 }
 
+// grid size of the cooperative factor / form steps of a tall panel (0: cooperative launch
+// unavailable); every CTA must be resident at once
+static int pq_grid_size(int64_t m) {
+  static int nsm = -1, per = 0;
+  if (nsm < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int coop = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pq_factor_grid, 256, 0) != cudaSuccess ||
+        per < 1) {
+      cudaGetLastError();
+      per = 0;
+    }
+    int per2 = 0;
+    if (per > 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, k_pq_form_grid, 256, 0) != cudaSuccess ||
+                    per2 < 1)) {
+      cudaGetLastError();
+      per = 0;
+    }
+  }
+  if (per == 0) return 0;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(nsm, m / 512));
+}
+
 void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n, int kmax, double* taus,
-                          double* Ts, double* gemm_scratch, void* cublas_handle, cudaStream_t st) {
+                          double* Ts, double* gemm_scratch, void* cublas_handle, int* grid_err, cudaStream_t st) {
   if (n <= 0 || kmax <= 0) return;
   cublasHandle_t cub = static_cast<cublasHandle_t>(cublas_handle);
   cublasSetStream(cub, st);
@@ -1280,8 +1488,45 @@ void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n
   const int ntiles = (kmax + kQU - 1) / kQU;
   const size_t smu = ((size_t)2 * kQB * kQU + kQC * kQV) * sizeof(double);
   smem_limit((const void*)k_pq_update, smu);
+  // scratch after the GEMM buffers: partials of the cooperative steps and the barrier words
+  int64_t mbig = 0;
+  for (int p = 0; p < n; ++p)
+    if (hdescs[p].big) mbig = std::max<int64_t>(mbig, hdescs[p].m);
+  double* part = gemm_scratch + mbig * kQB + 2 * (int64_t)kQB * std::max(kmax, 1);
+  unsigned* words = reinterpret_cast<unsigned*>(part + 2 * 152 * kPqParts);
+  cudaMemsetAsync(words, 0, 4 * sizeof(unsigned), st);
+  GridBar gb{words, words + 1, grid_err};
+  auto factor_big = [&](int p, int b) {
+    const int G = pq_grid_size(hdescs[p].m);
+    const PanelDesc* dp = descs + p;
+    int j0 = b * kQB;
+    double* tau = taus + (int64_t)p * kmax;
+    double* Tout = Ts + ((int64_t)p * nblk + b) * kQB * kQB;
+    if (G > 0 && G <= 152) {
+      void* args[] = {(void*)&dp, (void*)&j0, (void*)&tau, (void*)&Tout, (void*)&part, (void*)&gb};
+      if (cudaLaunchCooperativeKernel((const void*)k_pq_factor_grid, dim3(G), dim3(256), args, 0, st) == cudaSuccess)
+        return;
+      cudaGetLastError();
+    }
+    k_pq_factor<<<1, 512, 0, st>>>(dp, j0, tau, kmax, Ts + (int64_t)p * nblk * kQB * kQB, nblk, 0);
+  };
+  auto form_big = [&](int p, int b) {
+    const int G = pq_grid_size(hdescs[p].m);
+    const PanelDesc* dp = descs + p;
+    int j0 = b * kQB;
+    const double* tau = taus + (int64_t)p * kmax;
+    if (G > 0 && G <= 152) {
+      void* args[] = {(void*)&dp, (void*)&j0, (void*)&tau, (void*)&part, (void*)&gb};
+      if (cudaLaunchCooperativeKernel((const void*)k_pq_form_grid, dim3(G), dim3(256), args, 0, st) == cudaSuccess)
+        return;
+      cudaGetLastError();
+    }
+    k_pq_form<<<1, 512, 0, st>>>(dp, j0, tau, kmax, 0);
+  };
   for (int b = 0; b < nblk; ++b) {
-    k_pq_factor<<<n, 512, 0, st>>>(descs, b * kQB, taus, kmax, Ts, nblk);
+    k_pq_factor<<<n, 512, 0, st>>>(descs, b * kQB, taus, kmax, Ts, nblk, 1);
+    for (int p = 0; p < n; ++p)
+      if (hdescs[p].big && b * kQB < hdescs[p].k) factor_big(p, b);
     k_pq_update<<<dim3((unsigned)n, (unsigned)ntiles), 256, smu, st>>>(descs, b * kQB, Ts, nblk, 1);
     for (int p = 0; p < n; ++p)
       if (hdescs[p].big) panel_block_gemm(descs, hdescs[p], p, b * kQB, nblk, Ts, gemm_scratch, kmax, cub, 1, st);
@@ -1291,7 +1536,9 @@ void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n
     k_pq_update<<<dim3((unsigned)n, (unsigned)ntiles), 256, smu, st>>>(descs, b * kQB, Ts, nblk, 0);
     for (int p = 0; p < n; ++p)
       if (hdescs[p].big) panel_block_gemm(descs, hdescs[p], p, b * kQB, nblk, Ts, gemm_scratch, kmax, cub, 0, st);
-    k_pq_form<<<n, 512, 0, st>>>(descs, b * kQB, taus, kmax);
+    k_pq_form<<<n, 512, 0, st>>>(descs, b * kQB, taus, kmax, 1);
+    for (int p = 0; p < n; ++p)
+      if (hdescs[p].big && b * kQB < hdescs[p].k) form_big(p, b);
   }
 }
 

@@ -1228,7 +1228,7 @@ static int general_factorize(km_handle* h) {
   const int nb = (int)h->blk.size();
   int rc;
   timer_start(h);
-  KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + nb), st));
+  KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + nb + 1), st));  // + grid-barrier word
   if (!KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<double>(h->d_K, h->d_Lf, t, h->d_info, st)))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the leaf Cholesky kernel");
   if (nb > 0) {
@@ -1313,7 +1313,7 @@ static int general_factorize(km_handle* h) {
         if ((rc = grow(h, &h->d_pqg, panel_qr_gemm_scratch(pd.data() + pdoff[l], np, kmax_l[l])))) return rc;
         KLV(h, KM_PROF_LEAF_QR, launch_panel_qr_gemm(h->d_pdesc + pdoff[l], pd.data() + pdoff[l], np, kmax_l[l],
                                                      h->d_pqs, h->d_pqs + (int64_t)np * kmax_l[l], h->d_pqg,
-                                                     h->cublas, st));
+                                                     h->cublas, h->d_info + t.nleaf + nb, st));
       } else {
         KLV(h, KM_PROF_LEAF_QR, launch_panel_qr(h->d_pdesc + pdoff[l], np, kmax_l[l], h->d_pqs,
                                                 h->d_pqs + (int64_t)np * kmax_l[l], st));
@@ -1329,8 +1329,9 @@ static int general_factorize(km_handle* h) {
   h->stats.factorize_ms = timer_stop(h);
   if ((rc = sync(h, "general factorize")) != KM_OK) return rc;
   if ((rc = check_info(h, t.nleaf, "leaf")) != KM_OK) return rc;
-  std::vector<int> info(nb);
-  if (nb > 0) KM_CUDA(h, cudaMemcpy(info.data(), h->d_info + t.nleaf, sizeof(int) * nb, cudaMemcpyDeviceToHost));
+  std::vector<int> info(nb + 1);
+  KM_CUDA(h, cudaMemcpy(info.data(), h->d_info + t.nleaf, sizeof(int) * (nb + 1), cudaMemcpyDeviceToHost));
+  if (info[nb]) return fail(h, KM_ERR_TIMEOUT, "a bounded grid barrier of the panel QR ran out");
   for (int q = 0; q < nb; ++q)
     if (info[q]) return fail(h, KM_ERR_NOT_SPD, "PosDefException: a low-rank capacitance block is not positive definite");
   h->factorized = true;

@@ -165,10 +165,12 @@ void launch_aca_one(const double* pts, KParams kp, const AcaBlock* blocks, int b
 // Householder QR with explicit Q of n panels (largest column count kmax); scratch of
 // panel_qr_scratch(n, kmax) doubles: taus (n x kmax) then the T factors
 void launch_panel_qr(const PanelDesc* descs, int n, int kmax, double* taus, double* Ts, cudaStream_t st);
-// the same with the block-reflector applications of the panels marked big run as cuBLAS DGEMMs
-// (hdescs: host copies of descs; gemm_scratch: panel_qr_gemm_scratch(hdescs, n, kmax) doubles)
+// the same with the panels marked big handled by all SMs: their 8-column factor and form steps
+// as cooperative launches (bounded grid barriers; a barrier that runs out sets *grid_err) and
+// their block-reflector applications as cuBLAS DGEMMs (hdescs: host copies of descs;
+// gemm_scratch: panel_qr_gemm_scratch(hdescs, n, kmax) doubles)
 void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n, int kmax, double* taus,
-                          double* Ts, double* gemm_scratch, void* cublas_handle, cudaStream_t st);
+                          double* Ts, double* gemm_scratch, void* cublas_handle, int* grid_err, cudaStream_t st);
 int64_t panel_qr_gemm_scratch(const PanelDesc* hdescs, int n, int kmax);
 int64_t panel_qr_scratch(int n, int kmax);
 void launch_gnode(const GNodeDesc* nodes, int n, int* info, cudaStream_t st);
