@@ -76,6 +76,9 @@ struct km_handle {
   KParams kp{};
   int method = KM_METHOD_NYSTROM;
   bool mixed = false;  // float-pair factor (KM_PREC_MIXED)
+  // CTAs per node of the float-pair node kernel at most (thread-block clusters on levels with
+  // few nodes); 1 for handles of the batch and serving pools, whose streams fill the SMs already
+  int node_cluster_max = 8;
   double tol = 0.0;
   int64_t maxrank = 0;
   int r = 0;
@@ -187,6 +190,13 @@ struct km_handle {
   double prof_ms[KM_PROF_COUNT] = {};
   int64_t prof_n[KM_PROF_COUNT] = {};
 };
+
+namespace km {
+// Handles of the batch and serving pools (one stream each, many at once) keep one CTA per node.
+void set_node_cluster_max(km_handle* h, int v) {
+  if (h) h->node_cluster_max = v < 1 ? 1 : v;
+}
+}  // namespace km
 
 namespace {
 
@@ -1480,7 +1490,7 @@ static int factorize_launches(km_handle* h) {
       for (int l = 1; l <= t.L; ++l) {
         KLV(h, KM_PROF_NODE, launch_node_factor<ff>(P<ff>(h->d_R), P<ff>(h->d_SinvTf), r, l, t, P<ff>(h->d_Ct),
                                                     P<ff>(h->d_L22), P<ff>(h->d_Eref), P<ff>(h->d_Etau),
-                                                    h->d_info + t.nleaf, st));
+                                                    h->d_info + t.nleaf, st, h->node_cluster_max));
         side_level(h, l);
         {
           const NodeMatsH nm = node_mats(h);

@@ -15,6 +15,8 @@
 //
 // Vector workspaces (per column, r doubles per slot): VP projections, VG down-going
 // coefficients, VD per-node corrections (2r).  Slot s, column c: (s * k + c) * r.
+#include <type_traits>
+
 #include "km_kernels.h"
 
 namespace km {
@@ -37,12 +39,30 @@ enum { UP_PROJ = 0, UP_FWD = 1, UP_MULT = 2, UP_SUM = 3 };
 // down-sweep modes
 enum { DN_FWD = 0, DN_BWD = 1, DN_MUL = 2, DN_MULT = 3, DN_NYS = 4 };
 
-// sum_l a[l*sa] b[l], l < n, with four independent partial sums (ILP for float pairs; the
-// loads of the four terms are in flight together, which bounds these latency-bound sweeps)
+// sum_l a[l*sa] b[l], l < n, with four independent partial sums (term l into sum l % 4, the
+// tail after the last full group of four into the first).  The node matrices come from L2.  In
+// FP64 a sweep phase is bound by the round trips of these loads, so sixteen are issued before
+// their terms are summed (about n / 16 round trips instead of n / 4, same order of summation:
+// 1.38 -> 1.22 ms of sweeps per C2 step); the float-pair sums are bound by their arithmetic and
+// ran slower that way (1.15 -> 1.54 ms), so they keep groups of four.
 template <typename T>
 __device__ __forceinline__ T dot4(const T* __restrict__ a, int sa, const T* __restrict__ b, int n) {
   T s0 = T(0.0), s1 = T(0.0), s2 = T(0.0), s3 = T(0.0);
   int l = 0;
+  if constexpr (std::is_same<T, double>::value) {
+    for (; l + 15 < n; l += 16) {
+      T av[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) av[u] = a[(int64_t)(l + u) * sa];
+#pragma unroll
+      for (int u = 0; u < 16; u += 4) {
+        s0 += av[u] * b[l + u];
+        s1 += av[u + 1] * b[l + u + 1];
+        s2 += av[u + 2] * b[l + u + 2];
+        s3 += av[u + 3] * b[l + u + 3];
+      }
+    }
+  }
   for (; l + 3 < n; l += 4) {
     s0 += a[(int64_t)l * sa] * b[l];
     s1 += a[(int64_t)(l + 1) * sa] * b[l + 1];

@@ -19,6 +19,10 @@
 
 #include "../../include/kmhodlr.h"
 
+namespace km {
+void set_node_cluster_max(km_handle* h, int v);
+}
+
 struct km_batch {
   km_config cfg{};
   std::vector<km_handle*> workers;
@@ -41,6 +45,7 @@ extern "C" int km_batch_create(const km_config* cfg, int nworkers, km_batch** ou
       delete b;
       return rc;
     }
+    km::set_node_cluster_max(h, 1);
     b->workers.push_back(h);
   }
   *out = b;

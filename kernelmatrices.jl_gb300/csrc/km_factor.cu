@@ -13,11 +13,17 @@
 // gives the node basis Q_N = blockdiag(Q_c1, Q_c2) E_N.  Only r x r work is left above the
 // leaves; the factor is the reference's up to the rounding freedom of the QR of rank-deficient
 // panels.  Orthogonal factors are kept in Householder (LAPACK dgeqrf-style) form.
+#include <cooperative_groups.h>
+
+#include <atomic>
+#include <cstdlib>
 #include <type_traits>
 
 #include "km_kernels.h"
 
 namespace km {
+
+namespace cg = cooperative_groups;
 
 // ---------------------------------------------------------------------------------------------
 // Small dense Cholesky (r x r, lower, in place, column-major) for S = K(P, P).  One CTA.
@@ -291,6 +297,16 @@ __global__ void __launch_bounds__(leaf_qr_threads<T>()) k_leaf_formq(T* __restri
 // blocks of 8 rows with all threads, and the QR is a dataflow pipeline in which each warp owns
 // four columns and forms their reflectors itself.
 // Shared memory: four r x (r+1) matrices, three r-vectors and r + 1 flags.
+//
+// Cluster form (csize = 2, 4 or 8 CTAs per node, 1-D thread-block clusters): on levels with fewer
+// nodes than SMs the product phases (T1, T2, Ct, H, B) are split by columns over the CTAs of the
+// node's cluster, CTA `rank` taking columns rank, rank + csize, ...  Every CTA loads the inputs;
+// T1, T2 and Ct are all-gathered by storing each column into every CTA's shared memory
+// (distributed shared memory), H and B are stored into CTA 0 only, and cluster barriers separate
+// the phases (they also make sure that every CTA has started before the first remote store and
+// that no CTA exits while others still write to it).  CTA 0 then runs the Cholesky, the solve,
+// the QR and the stores alone; the other CTAs return.  With csize = 1 the kernel is the
+// one-CTA form (block barriers, local stores).
 // ---------------------------------------------------------------------------------------------
 // Iteration bound of a spin wait on a shared-memory flag (a few tens of cycles per iteration:
 // well above any legitimate wait inside one node, far below a watchdog).  The spin does not
@@ -302,12 +318,40 @@ __device__ __forceinline__ T sel(bool p, T a) {
   return p ? a : T(0.0);
 }
 
+// v into the same shared-memory location as p in every CTA of the cluster (locally if csize = 1)
+template <typename T>
+__device__ __forceinline__ void put_all(T* p, T v, int csize) {
+  if (csize == 1) {
+    *p = v;
+    return;
+  }
+  cg::cluster_group cl = cg::this_cluster();
+  for (int d = 0; d < csize; ++d) *cl.map_shared_rank(p, (unsigned)d) = v;
+}
+
+// v into the same shared-memory location as p in CTA 0 of the cluster (locally if csize = 1)
+template <typename T>
+__device__ __forceinline__ void put_rank0(T* p, T v, int csize) {
+  if (csize == 1) {
+    *p = v;
+    return;
+  }
+  *cg::this_cluster().map_shared_rank(p, 0u) = v;
+}
+
+// barrier over the cluster (release/acquire for the remote stores), or over the CTA if csize = 1
+__device__ __forceinline__ void node_barrier(int csize) {
+  if (csize == 1) __syncthreads();
+  else cg::this_cluster().sync();
+}
+
 template <typename T>
 __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T* __restrict__ SinvT,
                                                      int r, int level, int L, int64_t nleaf,
                                                      int64_t cbase, int64_t nbase, T* __restrict__ Ct_out,
                                                      T* __restrict__ L22_out, T* __restrict__ Eref,
-                                                     T* __restrict__ Etau, int* __restrict__ info) {
+                                                     T* __restrict__ Etau, int* __restrict__ info,
+                                                     int csize) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
   const int ld = r + 1;
@@ -319,13 +363,15 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
   T* vb = va + r;       // r values: 1 / L22[j][j], then the reflector scales
   T* vc = vb + r;       // r values: the reflector taus
   int* flags = reinterpret_cast<int*>(vc + r);  // r + 1 ints: column published / first bad pivot
-  const int64_t k = blockIdx.x;
+  const int64_t k = blockIdx.x / csize;
+  const int rank = (int)(blockIdx.x % csize);  // rank in the node's cluster (1-D clusters)
   const int64_t node = nbase + k;  // node index within all nodes (level-major)
   const T* R1 = R + (cbase + 2 * k) * (int64_t)r * r;
   const T* R2 = R + (cbase + 2 * k + 1) * (int64_t)r * r;
   const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, w = tid >> 5, nw = nth >> 5;
   const int nch = (r + 31) >> 5;   // 32-row chunks per column (r <= 96)
-  const int nitems = r * nch;
+  // product items of this CTA: (column c = rank + csize * lc, 32-row chunk s)
+  const int nitems = ((r - rank + csize - 1) / csize) * nch;
   for (int e = tid; e <= r; e += nth) flags[e] = (e < r) ? 0 : r + 1;
   // load: X0 = Sc^{-T} (upper), X1 = R1, X2 = R2   (element (i,c) at i + c*ld)
   for (int c = w; c < r; c += nw)
@@ -335,10 +381,10 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       X1[i + c * ld] = R1[e];
       X2[i + c * ld] = R2[e];
     }
-  __syncthreads();
+  node_barrier(csize);
   // T1 = R1 Sc^{-T} -> X3: T1[i][c] = sum_{l = i..c} R1[i][l] Sinv[l][c]
   for (int q = w; q < nitems; q += nw) {
-    const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
+    const int lc = q / nch, s = q - lc * nch, c = rank + csize * lc, i = 32 * s + lane, ii = min(i, r - 1);
     acc_t<T> a0{}, a1{};
     int l = 32 * s;
     for (; l + 1 <= c; l += 2) {
@@ -346,12 +392,12 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       a1 += sel(l + 1 >= i, X1[ii + (l + 1) * ld]) * X0[l + 1 + c * ld];
     }
     if (l <= c) a0 += sel(l >= i, X1[ii + l * ld]) * X0[l + c * ld];
-    if (i < r) X3[i + c * ld] = accv(a0) + accv(a1);
+    if (i < r) put_all(X3 + i + c * ld, accv(a0) + accv(a1), csize);
   }
-  __syncthreads();
+  node_barrier(csize);
   // T2 = R2 Sc^{-T} -> X1
   for (int q = w; q < nitems; q += nw) {
-    const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
+    const int lc = q / nch, s = q - lc * nch, c = rank + csize * lc, i = 32 * s + lane, ii = min(i, r - 1);
     acc_t<T> a0{}, a1{};
     int l = 32 * s;
     for (; l + 1 <= c; l += 2) {
@@ -359,12 +405,12 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       a1 += sel(l + 1 >= i, X2[ii + (l + 1) * ld]) * X0[l + 1 + c * ld];
     }
     if (l <= c) a0 += sel(l >= i, X2[ii + l * ld]) * X0[l + c * ld];
-    if (i < r) X1[i + c * ld] = accv(a0) + accv(a1);
+    if (i < r) put_all(X1 + i + c * ld, accv(a0) + accv(a1), csize);
   }
-  __syncthreads();
+  node_barrier(csize);
   // Ct = T1 T2' -> X0: Ct[i][c] = sum_{l >= max(i, c)} T1[i][l] T2[c][l]
   for (int q = w; q < nitems; q += nw) {
-    const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
+    const int lc = q / nch, s = q - lc * nch, c = rank + csize * lc, i = 32 * s + lane, ii = min(i, r - 1);
     acc_t<T> a0{}, a1{};
     int l = max(32 * s, c);
     for (; l + 1 < r; l += 2) {
@@ -372,15 +418,15 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       a1 += sel(l + 1 >= i, X3[ii + (l + 1) * ld]) * X1[c + (l + 1) * ld];
     }
     if (l < r) a0 += sel(l >= i, X3[ii + l * ld]) * X1[c + l * ld];
-    if (i < r) X0[i + c * ld] = accv(a0) + accv(a1);
+    if (i < r) put_all(X0 + i + c * ld, accv(a0) + accv(a1), csize);
   }
-  __syncthreads();
-  // H = I - Ct' Ct -> X3 (lower triangle); R1 is reloaded into X1 for the QR meanwhile
-  if (level < L)
+  node_barrier(csize);
+  // H = I - Ct' Ct -> X3 of CTA 0 (lower triangle); CTA 0 reloads R1 into X1 for the QR meanwhile
+  if (level < L && rank == 0)
     for (int c = w; c < r; c += nw)
       for (int i = lane; i < r; i += 32) X1[i + c * ld] = R1[i + c * r];
   for (int q = w; q < nitems; q += nw) {
-    const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
+    const int lc = q / nch, s = q - lc * nch, c = rank + csize * lc, i = 32 * s + lane, ii = min(i, r - 1);
     if (32 * s + 31 < c) continue;
     acc_t<T> a0{}, a1{};
     int l = 0;
@@ -389,12 +435,12 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       a1 += X0[l + 1 + ii * ld] * X0[l + 1 + c * ld];
     }
     if (l < r) a0 += X0[l + ii * ld] * X0[l + c * ld];
-    if (i < r && i >= c) X3[i + c * ld] = (i == c ? T(1.0) : T(0.0)) - (accv(a0) + accv(a1));
+    if (i < r && i >= c) put_rank0(X3 + i + c * ld, (i == c ? T(1.0) : T(0.0)) - (accv(a0) + accv(a1)), csize);
   }
-  // B = R2 - Ct' R1 -> X2 (column c of R1 has entries l <= c; R1 read from global memory)
+  // B = R2 - Ct' R1 -> X2 of CTA 0 (column c of R1 has entries l <= c; R1 read from global memory)
   if (level < L)
     for (int q = w; q < nitems; q += nw) {
-      const int c = q / nch, s = q - c * nch, i = 32 * s + lane, ii = min(i, r - 1);
+      const int lc = q / nch, s = q - lc * nch, c = rank + csize * lc, i = 32 * s + lane, ii = min(i, r - 1);
       const T* r1 = R1 + (int64_t)c * r;
       acc_t<T> a0{}, a1{};
       int l = 0;
@@ -403,9 +449,10 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
         a1 += X0[l + 1 + ii * ld] * r1[l + 1];
       }
       if (l <= c) a0 += X0[l + ii * ld] * r1[l];
-      if (i < r) X2[i + c * ld] -= accv(a0) + accv(a1);
+      if (i < r) put_rank0(X2 + i + c * ld, X2[i + c * ld] - (accv(a0) + accv(a1)), csize);
     }
-  __syncthreads();
+  node_barrier(csize);
+  if (rank != 0) return;  // the rest runs in CTA 0; no CTA touches another's memory after the barrier
   // L22 = chol(H) by columns in dataflow order.  Warp w owns columns w, w + nw, ... and finishes
   // them in increasing order: column c accumulates the contributions of columns k < c as soon as
   // each is published (flag[k] set after its values are in shared memory), then takes its pivot
@@ -908,9 +955,67 @@ void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st) {
   k_tri_inv_t<<<1, 128, sm, st>>>(Sc, r, SinvT);
 }
 
+// SM count of the current device (cached per device)
+static int sm_count() {
+  constexpr int kDevMax = 64;
+  static std::atomic<int> nsm_of[kDevMax];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevMax) return 1;
+  int v = nsm_of[dev].load();
+  if (v == 0) {
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    v = nsm > 0 ? nsm : 1;
+    nsm_of[dev].store(v);
+  }
+  return v;
+}
+
+// CTAs per node of the float-pair node kernel: the largest of 8, 4, 2 with nodes x csize <= the
+// SM count and at least one such cluster schedulable (checked once per size and device), else 1.
+// max_cs (the handle's setting) and KM_NODE_CLUSTER=1, 2, 4 or 8 cap it (1 gives the one-CTA
+// form).
+static int node_cluster_size(const void* fn, int64_t nodes, int threads, size_t smem, int max_cs) {
+  static const int cap = [] {
+    const char* e = std::getenv("KM_NODE_CLUSTER");
+    const int v = e ? std::atoi(e) : 8;
+    return v >= 8 ? 8 : v >= 4 ? 4 : v >= 2 ? 2 : 1;
+  }();
+  constexpr int kDevMax = 64;
+  // per device and size 1, 2, 4, 8: 0 unknown, 1 schedulable, -1 not (handles on several host
+  // threads may ask at once; a repeated query gives the same answer)
+  static std::atomic<int> ok[kDevMax][4];
+  const int nsm = sm_count();
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevMax) return 1;
+  const int top = std::min(cap, max_cs);
+  for (int cs = top, lg = top >= 8 ? 3 : top == 4 ? 2 : top == 2 ? 1 : 0; cs > 1; cs >>= 1, --lg) {
+    if (nodes * cs > nsm) continue;
+    if (ok[dev][lg].load() == 0) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)cs);
+      cfg.blockDim = dim3((unsigned)threads);
+      cfg.dynamicSmemBytes = smem;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)cs;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      const cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg);
+      if (e != cudaSuccess) cudaGetLastError();  // clear the query's error; the size is not used
+      ok[dev][lg].store((e == cudaSuccess && nclusters > 0) ? 1 : -1);
+    }
+    if (ok[dev][lg].load() > 0) return cs;
+  }
+  return 1;
+}
+
 template <typename T>
 void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T* Ct, T* L22, T* Eref,
-                        T* Etau, int* info, cudaStream_t st) {
+                        T* Etau, int* info, cudaStream_t st, int max_cluster) {
   const int64_t cbase = (level == 1) ? 0 : t.nleaf + t.node_off[level - 1];
   const int64_t nbase = t.node_off[level];
   if constexpr (std::is_same<T, double>::value) {
@@ -923,8 +1028,33 @@ void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T
   } else {
     const size_t sm = ((size_t)4 * r * (r + 1) + 3 * r) * sizeof(T) + (size_t)(r + 1) * sizeof(int);
     smem_limit((const void*)k_node_factor<T>, sm);
-    k_node_factor<T><<<(unsigned)t.nodes_at(level), 1024, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase,
-                                                                   nbase, Ct, L22, Eref, Etau, info);
+    const int64_t nodes = t.nodes_at(level);
+    const int cs = node_cluster_size((const void*)k_node_factor<T>, nodes, 1024, sm, max_cluster);
+    if (cs > 1) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)(nodes * cs));
+      cfg.blockDim = dim3(1024);
+      cfg.dynamicSmemBytes = sm;
+      cfg.stream = st;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = (unsigned)cs;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      const cudaError_t prior = cudaPeekAtLastError();
+      if (cudaLaunchKernelEx(&cfg, k_node_factor<T>, R, SinvT, r, level, t.L, t.nleaf, cbase, nbase, Ct, L22, Eref,
+                             Etau, info, cs) == cudaSuccess)
+        return;
+      // the cluster launch was refused (nothing ran): one CTA per node instead; an error from
+      // before this launch stays for the caller
+      if (prior == cudaSuccess) cudaGetLastError();
+    }
+    {
+      k_node_factor<T><<<(unsigned)nodes, 1024, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase, nbase, Ct, L22,
+                                                          Eref, Etau, info, 1);
+    }
   }
 }
 
@@ -958,7 +1088,10 @@ void launch_from_ff(const ff* in, double* out, int64_t n, cudaStream_t st) {
 // Per node of one level: L22^{-1} (lower) and, below the root, the explicit 2r x r factor E
 // of G = E R_N from the structured reflectors.  One warp per column; the column lives in
 // registers (row i in lane i % 32, slot i / 32, r <= 96), so the dependent chains need no
-// block barriers.  Runs on the side stream, overlapped with the next level's node kernel.
+// block barriers.  Column c's two chains take r - c and c + 1 steps, r + 1 together, so every
+// column costs the same; gridDim.y CTAs share a node's columns (warp w of CTA y takes columns
+// y * nw + w, stepping gridDim.y * nw), enough on levels with few nodes for one column per warp.
+// Runs on the side stream, overlapped with the next level's node kernel.
 template <typename T>
 __device__ __forceinline__ T slot_get(const T (&x)[3], int s) {
   return s == 0 ? x[0] : (s == 1 ? x[1] : x[2]);
@@ -981,6 +1114,7 @@ __global__ void __launch_bounds__(512) k_node_finalize(const T* __restrict__ L22
   const int64_t node = nbase + blockIdx.x;
   const int64_t off = node * (int64_t)r * r;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+  const int c0 = (int)blockIdx.y * nw + w, cstep = (int)gridDim.y * nw;  // this warp's columns
   for (int e = tid; e < r * r; e += blockDim.x) {
     const int i = e % r, c = e / r;
     Ls[i + c * ld] = L22[off + e];
@@ -990,15 +1124,15 @@ __global__ void __launch_bounds__(512) k_node_finalize(const T* __restrict__ L22
   if (with_e)
     for (int e = tid; e < r; e += blockDim.x) ts[e] = Etau[node * (int64_t)r + e];
   __syncthreads();
-  // transposes of Ct and L22 for the sweeps
-  for (int e = tid; e < r * r; e += blockDim.x) {
+  // transposes of Ct and L22 for the sweeps (entries split over the node's CTAs)
+  for (int e = (int)blockIdx.y * blockDim.x + tid; e < r * r; e += (int)gridDim.y * blockDim.x) {
     const int i = e % r, c = e / r;
     CtT[off + e] = Cs[c + i * ld];
     L22T[off + e] = Ls[c + i * ld];
   }
   // L22^{-1} e_c by forward substitution in column (axpy) order: row i accumulates
   // -L[i,p] x_p for p = c .. i-1 and is then divided by L[i,i]
-  for (int c = w; c < r; c += nw) {
+  for (int c = c0; c < r; c += cstep) {
     T x[3];
 #pragma unroll
     for (int s = 0; s < 3; ++s) x[s] = (lane + 32 * s) == c ? T(1.0) : T(0.0);
@@ -1026,7 +1160,7 @@ __global__ void __launch_bounds__(512) k_node_finalize(const T* __restrict__ L22
   // top row j and the whole bottom, so top row j is final once H_j has acted
   T* Eo = Eexp + node * (int64_t)2 * r * r;
   T* Et = ET + node * (int64_t)2 * r * r;  // r x 2r: element (c, l) at c + l*r
-  for (int c = w; c < r; c += nw) {
+  for (int c = c0; c < r; c += cstep) {
     T* top = Eo + (int64_t)c * 2 * r;
     T* bot = top + r;
     T b[3] = {T(0.0), T(0.0), T(0.0)};
@@ -1088,9 +1222,13 @@ void launch_node_finalize(const T* L22, const T* Ct, const T* Eref, const T* Eta
                           T* L22i, T* Eexp, T* CtT, T* L22T, T* L22iT, T* ET, cudaStream_t st) {
   const size_t sm = ((size_t)3 * r * (r + 1) + r) * sizeof(T);
   smem_limit((const void*)k_node_finalize<T>, sm);
-  k_node_finalize<T><<<(unsigned)t.nodes_at(level), 512, sm, st>>>(L22, Ct, Eref, Etau, r, t.node_off[level],
-                                                                   level < t.L ? 1 : 0, L22i, Eexp, CtT, L22T,
-                                                                   L22iT, ET);
+  // CTAs per node: enough for one column per warp (16 warps per CTA) while nodes x CTAs stays
+  // within the SM count; one per node on the wide levels
+  const int64_t nodes = t.nodes_at(level);
+  const int nsm = sm_count();
+  const int per_node = (int)std::max<int64_t>(1, std::min<int64_t>((r + 15) / 16, nsm / std::max<int64_t>(nodes, 1)));
+  k_node_finalize<T><<<dim3((unsigned)nodes, (unsigned)per_node), 512, sm, st>>>(
+      L22, Ct, Eref, Etau, r, t.node_off[level], level < t.L ? 1 : 0, L22i, Eexp, CtT, L22T, L22iT, ET);
 }
 
 template void launch_leaf_formq<double>(double*, const double*, int, const Tree&, cudaStream_t);
@@ -1106,8 +1244,9 @@ template bool launch_leaf_chol<ff>(const double*, ff*, const Tree&, int*, cudaSt
 template void launch_leaf_qr<double>(double*, int, const Tree&, double*, double*, cudaStream_t);
 template void launch_leaf_qr<ff>(ff*, int, const Tree&, ff*, ff*, cudaStream_t);
 template void launch_node_factor<double>(double*, const double*, int, int, const Tree&, double*, double*, double*,
-                                         double*, int*, cudaStream_t);
-template void launch_node_factor<ff>(ff*, const ff*, int, int, const Tree&, ff*, ff*, ff*, ff*, int*, cudaStream_t);
+                                         double*, int*, cudaStream_t, int);
+template void launch_node_factor<ff>(ff*, const ff*, int, int, const Tree&, ff*, ff*, ff*, ff*, int*, cudaStream_t,
+                                     int);
 template void launch_logdet<double>(const double*, const Tree&, const double*, int, double*, int, double*, cudaStream_t);
 template void launch_logdet<ff>(const ff*, const Tree&, const ff*, int, double*, int, double*, cudaStream_t);
 

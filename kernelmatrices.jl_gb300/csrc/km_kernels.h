@@ -97,7 +97,7 @@ void launch_leaf_qr(T* Pan, int r, const Tree& t, T* tau, T* Rout, cudaStream_t 
 void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st);
 template <typename T>
 void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T* Ct, T* L22, T* Eref, T* Etau,
-                        int* info, cudaStream_t st);
+                        int* info, cudaStream_t st, int max_cluster = 8);
 template <typename T>
 void launch_leaf_formq(T* Pan, const T* tau, int r, const Tree& t, cudaStream_t st);
 template <typename T>

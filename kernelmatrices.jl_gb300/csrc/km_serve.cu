@@ -29,6 +29,10 @@
 
 #include "../../include/kmhodlr.h"
 
+namespace km {
+void set_node_cluster_max(km_handle* h, int v);
+}
+
 namespace {
 
 using Clock = std::chrono::steady_clock;
@@ -135,6 +139,7 @@ km_result execute(km_server* s, Executor* e, Job& j, Factor* f) {
     case KM_REQ_FACTOR: {
       km_handle* h = nullptr;
       int rc = km_create(&s->cfg, &h);
+      if (rc == KM_OK) km::set_node_cluster_max(h, 1);
       if (rc == KM_OK)
         rc = km_assemble(h, q.prob.pts, q.prob.n, o.kernel_id, q.prob.params, 3, KM_METHOD_NYSTROM, 0.0, o.rank,
                          o.level_kind, o.level);
@@ -364,6 +369,7 @@ extern "C" int km_serve_create(const km_config* cfg, const km_serve_opts* o, km_
       for (auto& x : s->ex) km_destroy(x->h);
       return rc;
     }
+    km::set_node_cluster_max(e->h, 1);
     s->ex.push_back(std::move(e));
   }
   km_server* raw = s.get();
