@@ -15,6 +15,7 @@
 //
 // Vector workspaces (per column, r doubles per slot): VP projections, VG down-going
 // coefficients, VD per-node corrections (2r).  Slot s, column c: (s * k + c) * r.
+#include <atomic>
 #include <type_traits>
 
 #include "km_kernels.h"
@@ -43,8 +44,8 @@ enum { DN_FWD = 0, DN_BWD = 1, DN_MUL = 2, DN_MULT = 3, DN_NYS = 4 };
 // tail after the last full group of four into the first).  The node matrices come from L2.  In
 // FP64 a sweep phase is bound by the round trips of these loads, so sixteen are issued before
 // their terms are summed (about n / 16 round trips instead of n / 4, same order of summation:
-// 1.38 -> 1.22 ms of sweeps per C2 step); the float-pair sums are bound by their arithmetic and
-// ran slower that way (1.15 -> 1.54 ms), so they keep groups of four.
+// 1.38 -> 1.22 ms of sweeps per C2 step); the float-pair sums ran slower that way (1.15 -> 1.54
+// ms), so they keep groups of four (staged launches read the matrices from shared memory).
 template <typename T>
 __device__ __forceinline__ T dot4(const T* __restrict__ a, int sa, const T* __restrict__ b, int n) {
   T s0 = T(0.0), s1 = T(0.0), s2 = T(0.0), s3 = T(0.0);
@@ -85,9 +86,26 @@ static inline void sweep_shape(int64_t nodes, int k, int* kcb, int* threads) {
   *threads = c >= 8 ? 512 : (c >= 4 ? 256 : 128);
 }
 
-// grid = (nodes at level, ceil(k / kcb)).  Every phase is a set of independent dot products (one
-// thread per output entry) separated by barriers; node matrices are read through the L1 cache.
+// Staged launches (STAGE): the node matrices a phase reads are copied into shared memory at the
+// start of the kernel with asynchronous 8-byte copies (no registers held, all in flight at
+// once, overlapped with the vector loads), and the dot products read them from there instead of
+// waiting on L2 / DRAM round trips.  Used when the launch's CTAs fit in one wave at one CTA per
+// SM (the staged matrices take 4 r^2 values of shared memory); the sums are the same.
 template <typename T>
+__device__ __forceinline__ void stage_async(T* dst, const T* __restrict__ src, int n, int tid, int nth) {
+  static_assert(sizeof(T) == 8, "8-byte elements");
+  const unsigned base = (unsigned)__cvta_generic_to_shared(dst);
+  for (int e = tid; e < n; e += nth)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(base + 8u * (unsigned)e), "l"(src + e) : "memory");
+}
+__device__ __forceinline__ void stage_wait() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// grid = (nodes at level, ceil(k / kcb)).  Every phase is a set of independent dot products (one
+// thread per output entry) separated by barriers; node matrices are read through the L1 cache,
+// or from shared memory in a staged launch.
+template <typename T, bool STAGE>
 __global__ void __launch_bounds__(512) k_up(NodeMats<T> nm, int level, int L, int64_t cslot0, int64_t nslot0,
                                             int64_t node0, T* __restrict__ VP, T* __restrict__ VD, int k, int mode, int kcb) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -100,16 +118,41 @@ __global__ void __launch_bounds__(512) k_up(NodeMats<T> nm, int level, int L, in
   const int c0 = blockIdx.y * kcb;
   const int kc = min(kcb, k - c0);
   const int tid = threadIdx.x, nth = blockDim.x;
+  const int64_t rr = (int64_t)r * r;
+  const T* Ct = nm.Ct + node * rr;
+  const T* L22i = nm.L22i + node * rr;
+  const T* CtT = nm.CtT + node * rr;
+  const T* L22T = nm.L22T + node * rr;
+  const T* ETn = nm.ET + node * (int64_t)r2 * r;
+  if constexpr (STAGE) {
+    if (mode != UP_SUM) {
+      T* sA = ub + kcb * r;  // r^2: CtT or Ct
+      T* sB = sA + rr;       // r^2: L22i or L22T
+      T* sE = sB + rr;       // 2 r^2: ET
+      if (mode == UP_FWD) {
+        stage_async(sA, CtT, r * r, tid, nth);
+        stage_async(sB, L22i, r * r, tid, nth);
+        CtT = sA;
+        L22i = sB;
+      } else if (mode == UP_MULT) {
+        stage_async(sA, Ct, r * r, tid, nth);
+        stage_async(sB, L22T, r * r, tid, nth);
+        Ct = sA;
+        L22T = sB;
+      }
+      if (level < L) {
+        stage_async(sE, ETn, 2 * r * r, tid, nth);
+        ETn = sE;
+      }
+    }
+  }
   for (int e = tid; e < kc * r2; e += nth) {
     const int c = e / r2, i = e % r2;
     const int64_t slot = cslot0 + 2 * kk + (i >= r ? 1 : 0);
     z[c * r2 + i] = VP[(slot * k + c0 + c) * r + (i >= r ? i - r : i)];
   }
+  if constexpr (STAGE) stage_wait();
   __syncthreads();
-  const T* Ct = nm.Ct + node * (int64_t)r * r;
-  const T* L22i = nm.L22i + node * (int64_t)r * r;
-  const T* CtT = nm.CtT + node * (int64_t)r * r;
-  const T* L22T = nm.L22T + node * (int64_t)r * r;
   if (mode == UP_SUM) {
     if (level < L)
       for (int e = tid; e < kc * r; e += nth) {
@@ -160,15 +203,14 @@ __global__ void __launch_bounds__(512) k_up(NodeMats<T> nm, int level, int L, in
     __syncthreads();
   }
   if (level < L) {
-    const T* ET = nm.ET + node * (int64_t)r2 * r;
     for (int e = tid; e < kc * r; e += nth) {
       const int c = e / r, q = e % r;
-      VP[((nslot0 + kk) * k + c0 + c) * r + q] = dot4(ET + q, r, z + c * r2, r2);
+      VP[((nslot0 + kk) * k + c0 + c) * r + q] = dot4(ETn + q, r, z + c * r2, r2);
     }
   }
 }
 
-template <typename T>
+template <typename T, bool STAGE>
 __global__ void __launch_bounds__(512) k_down(NodeMats<T> nm, int level, int L, int64_t cslot0, int64_t nslot0,
                                               int64_t node0, const T* __restrict__ VP, T* __restrict__ VG,
                                               const T* __restrict__ VD, int k, int mode, int kcb) {
@@ -183,10 +225,39 @@ __global__ void __launch_bounds__(512) k_down(NodeMats<T> nm, int level, int L, 
   const int kc = min(kcb, k - c0);
   const int tid = threadIdx.x, nth = blockDim.x;
   const bool top = (level >= L);
+  const int64_t rr = (int64_t)r * r;
+  const T* E = nm.E + node * (int64_t)r2 * r;
+  const T* Ct = nm.Ct + node * rr;
+  const T* L22 = nm.L22 + node * rr;
+  const T* CtT = nm.CtT + node * rr;
+  const T* L22iT = nm.L22iT + node * rr;
+  if constexpr (STAGE) {
+    if (mode != DN_NYS) {
+      T* sE = tb + kcb * r2;  // 2 r^2: E
+      T* sA = sE + 2 * rr;    // r^2: Ct or CtT
+      T* sB = sA + rr;        // r^2: L22iT or L22
+      if (!top) {
+        stage_async(sE, E, 2 * r * r, tid, nth);
+        E = sE;
+      }
+      if (mode == DN_BWD) {
+        stage_async(sA, Ct, r * r, tid, nth);
+        stage_async(sB, L22iT, r * r, tid, nth);
+        Ct = sA;
+        L22iT = sB;
+      } else if (mode == DN_MUL) {
+        stage_async(sA, CtT, r * r, tid, nth);
+        stage_async(sB, L22, r * r, tid, nth);
+        CtT = sA;
+        L22 = sB;
+      }
+    }
+  }
   for (int e = tid; e < kc * r; e += nth) {
     const int c = e / r, i = e % r;
     g[c * r + i] = top ? T(0.0) : VG[((nslot0 + kk) * k + c0 + c) * r + i];
   }
+  if constexpr (STAGE) stage_wait();
   __syncthreads();
   auto child = [&](int side, int c, int i) -> int64_t { return ((cslot0 + 2 * kk + side) * k + c0 + c) * r + i; };
   if (mode == DN_NYS) {
@@ -200,16 +271,11 @@ __global__ void __launch_bounds__(512) k_down(NodeMats<T> nm, int level, int L, 
     }
     return;
   }
-  const T* E = nm.E + node * (int64_t)r2 * r;
   for (int e = tid; e < kc * r2; e += nth) {
     const int c = e / r2, i = e % r2;
     base[c * r2 + i] = top ? T(0.0) : dot4(E + i, r2, g + c * r, r);
   }
   __syncthreads();
-  const T* Ct = nm.Ct + node * (int64_t)r * r;
-  const T* L22 = nm.L22 + node * (int64_t)r * r;
-  const T* CtT = nm.CtT + node * (int64_t)r * r;
-  const T* L22iT = nm.L22iT + node * (int64_t)r * r;
   if (mode == DN_FWD || mode == DN_MULT) {
     for (int e = tid; e < kc * r; e += nth) {
       const int c = e / r, i = e % r;
@@ -341,6 +407,23 @@ __global__ void __launch_bounds__(256) k_leaf_nys_apply(const double* __restrict
 // ---------------------------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------------------------
+// SM count of the current device (cached per device); a staged sweep launch has at most this
+// many CTAs
+static int sweep_sm_count() {
+  constexpr int kDevMax = 64;
+  static std::atomic<int> nsm_of[kDevMax];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevMax) return 1;
+  int v = nsm_of[dev].load();
+  if (v == 0) {
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    v = nsm > 0 ? nsm : 1;
+    nsm_of[dev].store(v);
+  }
+  return v;
+}
+
 static inline int64_t child_slot0(const Tree& t, int level) {
   return level == 1 ? 0 : t.nleaf + t.node_off[level - 1];
 }
@@ -355,9 +438,16 @@ void launch_up(const Tree& t, const NodeMatsH& h, int level, T* VP, T* VD, int k
   sweep_shape(t.nodes_at(level), k, &kcb, &nth);
   dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + kcb - 1) / kcb));
   const size_t sm = (size_t)kcb * 4 * h.r * sizeof(T);
-  smem_limit((const void*)k_up<T>, sm);
-  k_up<T><<<grid, nth, sm, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
-                                 t.node_off[level], VP, VD, k, mode, kcb);
+  if (mode != UP_SUM && (int64_t)grid.x * grid.y <= sweep_sm_count()) {
+    const size_t sms = sm + (size_t)4 * h.r * h.r * sizeof(T);
+    smem_limit((const void*)k_up<T, true>, sms);
+    k_up<T, true><<<grid, nth, sms, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
+                                          t.node_off[level], VP, VD, k, mode, kcb);
+    return;
+  }
+  smem_limit((const void*)k_up<T, false>, sm);
+  k_up<T, false><<<grid, nth, sm, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
+                                        t.node_off[level], VP, VD, k, mode, kcb);
 }
 
 template <typename T>
@@ -371,9 +461,16 @@ void launch_down(const Tree& t, const NodeMatsH& h, int level, const T* VP, T* V
   sweep_shape(t.nodes_at(level), k, &kcb, &nth);
   dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + kcb - 1) / kcb));
   const size_t sm = (size_t)kcb * 5 * h.r * sizeof(T);
-  smem_limit((const void*)k_down<T>, sm);
-  k_down<T><<<grid, nth, sm, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
-                                   t.node_off[level], VP, VG, VD, k, mode, kcb);
+  if (mode != DN_NYS && (int64_t)grid.x * grid.y <= sweep_sm_count()) {
+    const size_t sms = sm + (size_t)4 * h.r * h.r * sizeof(T);
+    smem_limit((const void*)k_down<T, true>, sms);
+    k_down<T, true><<<grid, nth, sms, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
+                                            t.node_off[level], VP, VG, VD, k, mode, kcb);
+    return;
+  }
+  smem_limit((const void*)k_down<T, false>, sm);
+  k_down<T, false><<<grid, nth, sm, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
+                                          t.node_off[level], VP, VG, VD, k, mode, kcb);
 }
 
 void launch_leaf_phiT(const double* Phi, int r, const Tree& t, const double* X, int64_t ldx, double* VP,
