@@ -407,6 +407,10 @@ __global__ void __launch_bounds__(256) k_leaf_nys_apply(const double* __restrict
 // ---------------------------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------------------------
+// Shared memory a staged sweep launch may take (below the 227 KB opt-in limit per CTA; r <= 80
+// needs at most 203 KB)
+constexpr size_t kStageSmemMax = 220 * 1024;
+
 // SM count of the current device (cached per device); a staged sweep launch has at most this
 // many CTAs
 static int sweep_sm_count() {
@@ -438,8 +442,8 @@ void launch_up(const Tree& t, const NodeMatsH& h, int level, T* VP, T* VD, int k
   sweep_shape(t.nodes_at(level), k, &kcb, &nth);
   dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + kcb - 1) / kcb));
   const size_t sm = (size_t)kcb * 4 * h.r * sizeof(T);
-  if (mode != UP_SUM && (int64_t)grid.x * grid.y <= sweep_sm_count()) {
-    const size_t sms = sm + (size_t)4 * h.r * h.r * sizeof(T);
+  const size_t sms = sm + (size_t)4 * h.r * h.r * sizeof(T);
+  if (mode != UP_SUM && (int64_t)grid.x * grid.y <= sweep_sm_count() && sms <= kStageSmemMax) {
     smem_limit((const void*)k_up<T, true>, sms);
     k_up<T, true><<<grid, nth, sms, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
                                           t.node_off[level], VP, VD, k, mode, kcb);
@@ -461,8 +465,8 @@ void launch_down(const Tree& t, const NodeMatsH& h, int level, const T* VP, T* V
   sweep_shape(t.nodes_at(level), k, &kcb, &nth);
   dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + kcb - 1) / kcb));
   const size_t sm = (size_t)kcb * 5 * h.r * sizeof(T);
-  if (mode != DN_NYS && (int64_t)grid.x * grid.y <= sweep_sm_count()) {
-    const size_t sms = sm + (size_t)4 * h.r * h.r * sizeof(T);
+  const size_t sms = sm + (size_t)4 * h.r * h.r * sizeof(T);
+  if (mode != DN_NYS && (int64_t)grid.x * grid.y <= sweep_sm_count() && sms <= kStageSmemMax) {
     smem_limit((const void*)k_down<T, true>, sms);
     k_down<T, true><<<grid, nth, sms, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
                                             t.node_off[level], VP, VG, VD, k, mode, kcb);
