@@ -91,6 +91,11 @@ int km_partition(int64_t n, int level_kind, int64_t level, int64_t* out_levels,
 int km_nystrom_landmarks(int64_t n, int64_t rank, int64_t* out);
 
 /* ---- handle lifecycle -------------------------------------------------------------------- */
+/* A handle holds one problem's device state: it stands for the KernelHODLR object
+ * (src/HODLR/src/structstypes.jl:52-63) together with the factor W it keeps after
+ * symmetricfactorize! (FactorHODLR, structstypes.jl:46-49).  km_last_error gives the message of
+ * the last failing call (where the reference throws, with the reference's message where one
+ * exists); km_get_stats has no reference counterpart. */
 int km_create(const km_config* cfg, km_handle** out);
 int km_destroy(km_handle* h);
 const char* km_last_error(const km_handle* h);
@@ -114,11 +119,14 @@ int km_assemble_dev(km_handle* h, const double* d_pts, int64_t n, int kernel_id,
                     const double* params, int nparams, int method, double tol, int64_t maxrank,
                     int level_kind, int64_t level);
 
-/* Rank of every off-diagonal block, level 1 first (nnonleaf entries). */
+/* Rank of every off-diagonal block, level 1 first (nnonleaf entries): size(K.U[l][k], 2) of the
+ * reference's KernelHODLR (src/HODLR/src/structstypes.jl:52-63), which has no accessor of its
+ * own.  Exposed, with the pivots and factors below, for parity checks. */
 int km_block_ranks(km_handle* h, int64_t* out);
 
 /* ACA pivots (0-based within the block) of block `block` (global index, level 1 first):
- * rows and cols receive up to `cap` entries each; *out_rank gets the block rank. */
+ * rows and cols receive up to `cap` entries each; *out_rank gets the block rank.  The
+ * reference's ACA (src/factorizations.jl:9-84) keeps its pivots internal. */
 int km_aca_pivots(km_handle* h, int64_t block, int64_t cap, int64_t* rows, int64_t* cols,
                   int64_t* out_rank);
 
@@ -153,8 +161,9 @@ int km_factor_mul(km_handle* h, int transpose, const double* b, double* x, int64
 /* log det K.  Replaces logdet(K::KernelHODLR) (src/HODLR/src/baseoverloads.jl:194-209). */
 int km_logdet(km_handle* h, double* out);
 
-/* Device-resident variants: pointers are device memory of the handle's device; the work is
- * ordered on the handle's stream and the call returns once it is complete. */
+/* Device-resident variants of km_matvec, km_solve, km_factor_solve and km_factor_mul (the same
+ * reference calls): pointers are device memory of the handle's device; the work is ordered on
+ * the handle's stream and the call returns once it is complete. */
 int km_matvec_dev(km_handle* h, const double* d_x, double* d_y, int64_t k);
 int km_solve_dev(km_handle* h, const double* d_b, double* d_x, int64_t k);
 int km_factor_solve_dev(km_handle* h, int transpose, const double* d_b, double* d_x, int64_t k);
@@ -255,7 +264,9 @@ int km_rhodlr_create(const km_config* cfg, const double* x1, int64_t n1, const d
 int km_rhodlr_destroy(km_rhodlr* r);
 const char* km_rhodlr_create_error(void);
 const char* km_rhodlr_last_error(const km_rhodlr* r);
-/* number of ACA blocks, dense leaves and levels */
+/* Number of ACA blocks, dense leaves and levels; the rank of every ACA block (block order
+ * above); the pivots of one block.  The reference's RKernelHODLR keeps these in its fields
+ * (structstypes.jl:22-27) without accessors; exposed for parity checks. */
 int km_rhodlr_info(const km_rhodlr* r, int64_t* nblocks, int64_t* nleaves, int64_t* levels);
 int km_rhodlr_block_ranks(const km_rhodlr* r, int64_t* ranks);
 int km_rhodlr_aca_pivots(km_rhodlr* r, int64_t block, int64_t cap, int64_t* rows, int64_t* cols,
@@ -299,7 +310,8 @@ typedef struct km_batch_opts {
 typedef struct km_batch km_batch;
 
 /* A pool of `nworkers` handles (0 => 8), each with its own stream and host thread, that keeps
- * its device buffers between calls (grown to the largest problem seen). */
+ * its device buffers between calls (grown to the largest problem seen).  No reference
+ * counterpart (see km_batch_nll_grad). */
 int km_batch_create(const km_config* cfg, int nworkers, km_batch** out);
 int km_batch_destroy(km_batch* b);
 
@@ -371,7 +383,8 @@ typedef struct km_server km_server;
  * No reference counterpart (the reference is a library called in-process). */
 int km_serve_create(const km_config* cfg, const km_serve_opts* o, km_server** out);
 
-/* Queues a request; *ticket identifies it for km_serve_wait. */
+/* Queues a request; *ticket identifies it for km_serve_wait.  This and the calls below have no
+ * reference counterpart, like km_serve_create. */
 int km_serve_submit(km_server* s, const km_request* r, uint64_t* ticket);
 
 /* Waits up to timeout_ms (< 0: forever) for the request; KM_ERR_TIMEOUT if still running.
@@ -386,7 +399,8 @@ int km_serve_destroy(km_server* s);
 /* ---- streams and profiling ---------------------------------------------------------------- */
 
 /* Runs the handle's work on `stream` (a cudaStream_t of the handle's device; NULL restores the
- * handle's own stream).  The caller keeps ownership of the stream. */
+ * handle's own stream).  The caller keeps ownership of the stream.  The streams, profiling and
+ * diagnostics calls below have no reference counterpart (the reference runs on the host). */
 int km_set_stream(km_handle* h, void* stream);
 
 /* Kernel classes timed by the profiler. */
