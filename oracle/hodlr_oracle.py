@@ -857,6 +857,178 @@ def grad_and_fisher_matrix(prms, pts: np.ndarray, dat: np.ndarray, kid: int, ran
     return g, F
 
 
+# ----------------------------------------------------------------------------------------------
+# Stochastic Hessian: constructor.jl:100-121 (second-derivative leaves and blocks),
+# utils.jl:100-177 (SBlock, SDBlock_mul, SDBlock_mul_t, Deriv2mul), stochastichessian.jl:3-56,
+# 79-89, 117-147 (the solve and trace terms, stoch_hessian)
+# ----------------------------------------------------------------------------------------------
+
+
+def d2kernel_block(kid: int, j: int, k: int, x1: np.ndarray, x2: np.ndarray, p: Sequence[float]) -> np.ndarray:
+    """Second derivative of ``kernel_block`` in parameters j and k (0: scale, 1: range, 2: nugget).
+
+    The reference takes these as user functions (``d2funs`` of stoch_hessian,
+    stochastichessian.jl:117-121); this is the closed form of the same kernels:
+    Matern-3/2, k = p0 (1 + z) e^-z with z = sqrt(3) r / p1: d00 = 0, d01 = z^2 e^-z / p1,
+    d11 = p0 z^2 (z - 3) e^-z / p1^2 (0 where r / p1 <= 1e-8, as for the first derivative);
+    RQ, k = p0^2 / u^2 with u = 1 + t^2, t = r / p1: d00 = 2 / u^2, d01 = 8 p0 r^2 / (p1^3 u^3),
+    d11 = 12 p0^2 r^2 (t^2 - 1) / (p1^4 u^4).  Every pair with the nugget is 0."""
+    j, k = min(j, k), max(j, k)
+    r, _ = _pairwise(x1, x2)
+    if k == 2:
+        return np.zeros(r.shape)
+    if kid == KERNEL_RQ:
+        t = r / p[1]
+        u = 1.0 + t * t
+        if (j, k) == (0, 0):
+            return 2.0 / (u * u)
+        if (j, k) == (0, 1):
+            return 8.0 * p[0] * r * r / (p[1] ** 3) / (u * u * u)
+        return 12.0 * p[0] * p[0] * r * r * (t * t - 1.0) / (p[1] ** 4) / (u ** 4)
+    if kid == KERNEL_MATERN32:
+        out = np.zeros(r.shape)
+        if (j, k) == (0, 0):
+            return out
+        x = r / p[1]
+        m = np.abs(x) > 1.0e-8
+        z = SQRT3 * x[m]
+        e = np.exp(-z)
+        if (j, k) == (0, 1):
+            out[m] = z * z * e / p[1]
+        else:
+            out[m] = p[0] * z * z * (z - 3.0) * e / (p[1] * p[1])
+        return out
+    raise ValueError("unknown kernel id")
+
+
+def d2_is_zero(kid: int, j: int, k: int) -> bool:
+    """Pairs whose second derivative vanishes identically (``ZeroFunction`` in stoch_hessian)."""
+    j, k = min(j, k), max(j, k)
+    return k == 2 or (kid == KERNEL_MATERN32 and (j, k) == (0, 0))
+
+
+@dataclass
+class SecondDerivativeBlock:
+    """``SecondDerivativeBlock`` (src/HODLR/src/structstypes.jl:77-80)."""
+    K1pjk: np.ndarray
+    Kp2jk: np.ndarray
+
+
+def second_derivative_parts(K: KernelMatrix, HK: KernelHODLR, j: int, k: int):
+    """``SecondDerivativeBlocks`` and ``SecondDerivativeLeaves`` (constructor.jl:100-121) and
+    ``Sjk`` (HODLR_hess_extra, stochastichessian.jl:33-47): the d2 blocks K(x1, P), K(P, x2) of every non-leaf block,
+    the dense d2 leaves, and d2 K(P, P)."""
+    lnd = K.x1[nystrom_landmarks(K.shape[0], HK.mrnk)]
+    blocks = []
+    for lev in range(HK.lvl):
+        Bl = []
+        for x in HK.nonleafindices[lev]:
+            a, b, c, d = x
+            Bl.append(SecondDerivativeBlock(d2kernel_block(K.kid, j, k, K.x1[a - 1:b], lnd, K.parms),
+                                            d2kernel_block(K.kid, j, k, lnd, K.x2[c - 1:d], K.parms)))
+        blocks.append(Bl)
+    leaves = []
+    for x in HK.leafindices:
+        a, b, c, d = x
+        leaves.append(d2kernel_block(K.kid, j, k, K.x1[a - 1:b], K.x2[c - 1:d], K.parms))
+    Sjk = d2kernel_block(K.kid, j, k, lnd, lnd, K.parms)
+    return blocks, leaves, Sjk
+
+
+def sdblock_mul(Bj: DerivativeBlock, Bk: DerivativeBlock, Bjk: SecondDerivativeBlock, src, S, Spj, Spk, Spjk):
+    """``SDBlock_mul`` (src/HODLR/src/utils.jl:110-132), term for term (the reference's own terms,
+    which are not the second derivative of a Nystrom block; see the design notes)."""
+    out = Bjk.K1pjk @ _cs(S, Bj.Kp2 @ src)
+    out = out - Bj.K1pd @ _cs(S, Spk @ _cs(S, Bj.Kp2 @ src))
+    out = out + Bj.K1pd @ _cs(S, Bk.Kp2d @ src)
+    out = out + Bk.K1pd @ _cs(S, Spj @ _cs(S, Bj.Kp2 @ src))
+    out = out - Bk.K1p @ _cs(S, Spk @ _cs(S, Spj @ _cs(S, Bk.Kp2 @ src)))
+    out = out + Bk.K1p @ _cs(S, Spjk @ _cs(S, Bk.Kp2 @ src))
+    out = out - Bk.K1p @ _cs(S, Spj @ _cs(S, Spk @ _cs(S, Bk.Kp2 @ src)))
+    out = out + Bk.K1p @ _cs(S, Spj @ _cs(S, Bj.Kp2d @ src))
+    out = out + Bk.K1pd @ _cs(S, Bk.Kp2 @ src)
+    out = out - Bk.K1p @ _cs(S, Spk @ _cs(S, Bk.Kp2 @ src))
+    out = out + Bk.K1p @ _cs(S, Bjk.Kp2jk @ src)
+    return out
+
+
+def sdblock_mul_t(Bj: DerivativeBlock, Bk: DerivativeBlock, Bjk: SecondDerivativeBlock, src, S, Spj, Spk, Spjk):
+    """``SDBlock_mul_t`` (utils.jl:134-155), term for term (t_mul(A, x) = A' x)."""
+    out = Bj.Kp2.T @ _cs(S, Bjk.K1pjk.T @ src)
+    out = out - Bj.Kp2.T @ _cs(S, Spk @ _cs(S, Bj.K1pd.T @ src))
+    out = out + Bk.Kp2d.T @ _cs(S, Bk.K1pd.T @ src)
+    out = out + Bj.Kp2.T @ _cs(S, Spj @ _cs(S, Bk.K1pd.T @ src))
+    out = out - Bj.Kp2.T @ _cs(S, Spj @ _cs(S, Spk @ _cs(S, Bk.K1p.T @ src)))
+    out = out + Bj.Kp2.T @ _cs(S, Spjk @ _cs(S, Bk.K1p.T @ src))
+    out = out - Bj.Kp2.T @ _cs(S, Spk @ _cs(S, Spj @ _cs(S, Bk.K1p.T @ src)))
+    out = out + Bk.Kp2d.T @ _cs(S, Spj @ _cs(S, Bk.K1p.T @ src))
+    out = out + Bj.Kp2d.T @ _cs(S, Bk.K1pd.T @ src)
+    out = out - Bj.Kp2d.T @ _cs(S, Spk @ _cs(S, Bk.K1p.T @ src))
+    out = out + Bjk.Kp2jk.T @ _cs(S, Bk.K1p.T @ src)
+    return out
+
+
+def deriv2mul(DKj: DerivativeHODLR, DKk: DerivativeHODLR, D2B2, D2BL, Sjk, src: np.ndarray) -> np.ndarray:
+    """``Deriv2mul`` (utils.jl:157-177): the d2 leaves, then per non-leaf block SDBlock_mul_t into
+    the column range and SDBlock_mul into the row range."""
+    tgt = np.zeros_like(src, dtype=np.float64)
+    for q, Lq in enumerate(D2BL):
+        c, d = DKj.leafindices[q][2:4]
+        tgt[c - 1:d] += Lq @ src[c - 1:d]
+    for lev in range(len(DKj.B)):
+        for q in range(len(DKj.B[lev])):
+            a, b, c, d = DKj.nonleafindices[lev][q]
+            Bj, Bk, Bjk = DKj.B[lev][q], DKk.B[lev][q], D2B2[lev][q]
+            tgt[c - 1:d] += sdblock_mul_t(Bj, Bk, Bjk, src[a - 1:b], DKj.S, DKj.Sj, DKk.Sj, Sjk)
+            tgt[a - 1:b] += sdblock_mul(Bj, Bk, Bjk, src[c - 1:d], DKj.S, DKj.Sj, DKk.Sj, Sjk)
+    return tgt
+
+
+def hess_slv(HK: KernelHODLR, DKj, DKk, D2B2, D2BL, Sjk, data, HKsd) -> float:
+    """``HODLR_hess_slv`` (stochastichessian.jl:3-13)."""
+    out = -hodlr_ldiv(HK, derivative_mul(DKk, hodlr_ldiv(HK, derivative_mul(DKj, HKsd))))
+    out = out - hodlr_ldiv(HK, derivative_mul(DKj, hodlr_ldiv(HK, derivative_mul(DKk, HKsd))))
+    out = out + hodlr_ldiv(HK, deriv2mul(DKj, DKk, D2B2, D2BL, Sjk, HKsd))
+    return float(np.dot(data, out))
+
+
+def hess_slv_no2d(HK: KernelHODLR, DKj, DKk, data, HKsd) -> float:
+    """``HODLR_hess_slv_no2d`` (stochastichessian.jl:50-56)."""
+    out = -hodlr_ldiv(HK, derivative_mul(DKk, hodlr_ldiv(HK, derivative_mul(DKj, HKsd))))
+    out = out - hodlr_ldiv(HK, derivative_mul(DKj, hodlr_ldiv(HK, derivative_mul(DKk, HKsd))))
+    return float(np.dot(data, out))
+
+
+def hess_tr2(HK: KernelHODLR, DKj, DKk, D2B2, D2BL, Sjk, v) -> float:
+    """``HODLR_hess_tr2`` (stochastichessian.jl:79-89): tp1 = W'^-1 v, tp1 . Deriv2mul(tp1)."""
+    tp1 = factor_ldiv_t(HK.W, v)
+    return float(np.dot(tp1, deriv2mul(DKj, DKk, D2B2, D2BL, Sjk, tp1)))
+
+
+def stoch_hessian(K: KernelMatrix, HK: KernelHODLR, dat: np.ndarray, vecs) -> np.ndarray:
+    """``stoch_hessian`` (stochastichessian.jl:117-147) with shuffle = false and profile = false:
+    minus the stochastic Fisher matrix, plus for every pair j <= k the solve term (with the
+    second-derivative product where the second derivative is not identically zero, otherwise
+    ``HODLR_hess_slv_no2d``) and the trace term (``HODLR_hess_extra``, :33-47).  Returns the
+    symmetric matrix of the upper triangle."""
+    if HK.U is not None:
+        raise RuntimeError("The matrix needs to be factorized.")
+    m = len(K.parms)
+    DKs = [derivative_hodlr(K, j, HK) for j in range(m)]
+    out = -stoch_fisher(K, HK, DKs, vecs)
+    HKsd = hodlr_ldiv(HK, dat)
+    for j in range(m):
+        for k in range(j, m):
+            if not d2_is_zero(K.kid, j, k):
+                D2B2, D2BL, Sjk = second_derivative_parts(K, HK, j, k)
+                sterm = hess_slv(HK, DKs[j], DKs[k], D2B2, D2BL, Sjk, dat, HKsd)
+                t2 = sum(hess_tr2(HK, DKs[j], DKs[k], D2B2, D2BL, Sjk, v) for v in vecs) / len(vecs)
+                out[j, k] += 0.5 * t2 - 0.5 * sterm
+            else:
+                out[j, k] -= 0.5 * hess_slv_no2d(HK, DKs[j], DKs[k], dat, HKsd)
+    return np.triu(out) + np.triu(out, 1).T
+
+
 def kd_order(pts: np.ndarray, leaf: int = 32) -> np.ndarray:
     """k-d ordering checked against the GPU's ``km_kd_order``.  The reference sorts with
     NearestNeighbors 0.4.9 ``KDTree(pts).data`` (src/HODLR/src/constructor.jl:180), a third-party

@@ -211,3 +211,96 @@ def test_kd_order_oracle_matches_host_helper():
     for P in cases:
         for leaf in (1, 7, 32):
             assert np.array_equal(O.kd_order(P, leaf), host_kd(P, leaf))
+
+
+def test_second_derivatives_match_finite_differences():
+    """d2kernel_block (the closed forms restated for the reference's user-supplied d2funs) is the
+    parameter derivative of dkernel_block: central differences, both kernels, every pair."""
+    rng = np.random.default_rng(11)
+    x1, x2 = rng.uniform(size=(40, 2)), rng.uniform(size=(30, 2))
+    x2[:5] = x1[:5]  # coincident points (the nugget indicator)
+    for kid, p in ((O.KERNEL_MATERN32, [1.3, 0.2, 1e-2]), (O.KERNEL_RQ, [1.1, 0.15, 1e-2])):
+        for j in range(3):
+            for k in range(3):
+                h = 1e-6 * max(abs(p[k]), 1e-3)
+                pp, pm = list(p), list(p)
+                pp[k] += h
+                pm[k] -= h
+                fd = (O.dkernel_block(kid, j, x1, x2, pp) - O.dkernel_block(kid, j, x1, x2, pm)) / (2 * h)
+                d2 = O.d2kernel_block(kid, j, k, x1, x2, p)
+                assert np.allclose(d2, fd, rtol=1e-6, atol=1e-7 * np.abs(fd).max() + 1e-12), (kid, j, k)
+                assert np.array_equal(d2, O.d2kernel_block(kid, k, j, x1, x2, p))
+                if O.d2_is_zero(kid, j, k):
+                    assert not np.any(d2)
+
+
+def sd_transforms(S, Sj, Sk, Sjk):
+    """The reference's SDBlock_mul / SDBlock_mul_t as linear maps of the four projections
+    [Phi' s; Phi_j' s; Phi_k' s; Phi_jk' s] to the four expansion coefficients (the form the GPU
+    down-sweep applies): A = S^-1, B_x = A S_x A, C_jk = B_j S_k A, C_kj = B_k S_j A."""
+    A = np.linalg.inv(S)
+    Bj, Bk, Bjk = A @ Sj @ A, A @ Sk @ A, A @ Sjk @ A
+    Cjk, Ckj = Bj @ Sk @ A, Bk @ Sj @ A
+    Z = np.zeros_like(A)
+    Tmul = np.block([[-Ckj + Bjk - Cjk - Bk, Bj, Z, A],
+                     [-Bk, Z, A, Z],
+                     [Bj + A, Z, Z, Z],
+                     [A, Z, Z, Z]])
+    Tmult = np.block([[-Cjk + Bjk - Ckj, -Bk, Bj, A],
+                      [-Bk, Z, A, Z],
+                      [Bj, Z, A, Z],
+                      [A, Z, Z, Z]])
+    return Tmul, Tmult
+
+
+def test_sdblock_products_equal_their_projection_form():
+    """SDBlock_mul and SDBlock_mul_t, restated term for term, equal the 4-projection transforms
+    (rows: coefficients of Phi, Phi_j, Phi_k, Phi_jk) on random blocks."""
+    rng = np.random.default_rng(12)
+    r, mi, mj = 9, 31, 23
+    G = rng.standard_normal((r, r))
+    S = G @ G.T + r * np.eye(r)
+    sym = lambda: (lambda M: M + M.T)(rng.standard_normal((r, r)))
+    Sj, Sk, Sjk = sym(), sym(), sym()
+    PhI = [rng.standard_normal((mi, r)) for _ in range(4)]   # Phi, Phi_j, Phi_k, Phi_jk on I
+    PhJ = [rng.standard_normal((mj, r)) for _ in range(4)]   # the same on J
+    Bj = O.DerivativeBlock(PhI[0], PhI[1], PhJ[0].T, PhJ[1].T)
+    Bk = O.DerivativeBlock(PhI[0], PhI[2], PhJ[0].T, PhJ[2].T)
+    Bjk = O.SecondDerivativeBlock(PhI[3], PhJ[3].T)
+    Sc = sla.cho_factor(S, lower=False)
+    Tmul, Tmult = sd_transforms(S, Sj, Sk, Sjk)
+    sJ, sI = rng.standard_normal(mj), rng.standard_normal(mi)
+    ref = O.sdblock_mul(Bj, Bk, Bjk, sJ, Sc, Sj, Sk, Sjk)
+    c = Tmul @ np.concatenate([P.T @ sJ for P in PhJ])
+    got = sum(PhI[v] @ c[v * r:(v + 1) * r] for v in range(4))
+    assert np.allclose(got, ref, rtol=1e-10, atol=1e-10 * np.abs(ref).max())
+    ref_t = O.sdblock_mul_t(Bj, Bk, Bjk, sI, Sc, Sj, Sk, Sjk)
+    d = Tmult @ np.concatenate([P.T @ sI for P in PhI])
+    got_t = sum(PhJ[v] @ d[v * r:(v + 1) * r] for v in range(4))
+    assert np.allclose(got_t, ref_t, rtol=1e-10, atol=1e-10 * np.abs(ref_t).max())
+
+
+def test_stoch_hessian_oracle():
+    """stoch_hessian restated: symmetric, its no-second-derivative entries equal minus the Fisher
+    entry minus half the solve term, and Deriv2mul is linear."""
+    n, rank, lvl = 512, 24, O.FixedLevel(3)
+    rng = np.random.default_rng(13)
+    pts = rng.uniform(size=(n, 2))
+    pts = pts[O.kd_order(pts, 16)]
+    for kid, p in ((O.KERNEL_MATERN32, [1.0, 0.1, 1e-2]), (O.KERNEL_RQ, [1.0, 0.15, 1e-2])):
+        K = O.KernelMatrix(pts, pts, np.asarray(p), kid)
+        HK = O.build_hodlr(K, 0.0, rank, lvl, nystrom=True)
+        O.symmetricfactorize(HK)
+        y = rng.standard_normal(n)
+        vecs = O.givesaa(6, n, 7)
+        H = O.stoch_hessian(K, HK, y, vecs)
+        assert np.array_equal(H, H.T) and np.all(np.isfinite(H))
+        DKs = [O.derivative_hodlr(K, j, HK) for j in range(3)]
+        F = O.stoch_fisher(K, HK, DKs, vecs)
+        u = O.hodlr_ldiv(HK, y)
+        assert abs(H[2, 2] - (-F[2, 2] - 0.5 * O.hess_slv_no2d(HK, DKs[2], DKs[2], y, u))) < 1e-10 * abs(H).max()
+        D2B2, D2BL, Sjk = O.second_derivative_parts(K, HK, 0, 1)
+        a, b = rng.standard_normal(n), rng.standard_normal(n)
+        lhs = O.deriv2mul(DKs[0], DKs[1], D2B2, D2BL, Sjk, 2.0 * a - b)
+        rhs = 2.0 * O.deriv2mul(DKs[0], DKs[1], D2B2, D2BL, Sjk, a) - O.deriv2mul(DKs[0], DKs[1], D2B2, D2BL, Sjk, b)
+        assert np.allclose(lhs, rhs, rtol=1e-10, atol=1e-10 * np.abs(rhs).max())
