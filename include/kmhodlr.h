@@ -230,6 +230,23 @@ int km_grad_fisher(km_handle* h, const double* y, const double* probes, int64_t 
 int km_grad_fisher_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed,
                           double* nll, double* grad, double* fisher);
 
+/* Stochastic Hessian of the negative log-likelihood with respect to (scale, range, nugget):
+ * hess (3 x 3, symmetric, column-major) = -F + for every pair j <= k the trace term
+ * 0.5 mean_v t'D2_jk t (t = W'^{-1} v) where the second derivative is not identically zero, and
+ * minus half the solve term -u'dK_k K^{-1} dK_j u - u'dK_j K^{-1} dK_k u + u'D2_jk u
+ * (u = K^{-1} y); F is the stochastic Fisher matrix of km_grad_fisher from the same probes, and
+ * nll and grad are km_grad_fisher's.  D2_jk is the reference's second-derivative product
+ * Deriv2mul with its block terms SDBlock_mul / SDBlock_mul_t as written there (they are not the
+ * exact second derivative of a Nystrom block).  Replaces stoch_hessian
+ * (src/HODLR/src/stochastichessian.jl:117-147, shuffle = false, profile = false) with the
+ * second-derivative functions (its d2funs) of the built-in kernels in closed form; pairs with the
+ * nugget, and scale-scale for the Matern kernel, are the reference's ZeroFunction case.
+ * nprobe >= 1. */
+int km_stoch_hessian(km_handle* h, const double* y, const double* probes, int64_t nprobe, double* nll,
+                     double* grad, double* hess);
+int km_stoch_hessian_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed, double* nll,
+                            double* grad, double* hess);
+
 /* k-d ordering of n 2-D points (AoS x, y) on the device, the input step of maxlikdata
  * (src/HODLR/src/constructor.jl:171-181), which sorts with NearestNeighbors.KDTree(pts).data.
  * That package's permutation is not reproduced; this library's ordering is: a range of more than

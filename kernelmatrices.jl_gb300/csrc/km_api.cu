@@ -164,6 +164,18 @@ struct km_handle {
   double* d_dots = nullptr;
   int64_t tcap = 0;
   double* d_A = nullptr;     // Fisher: W^{-1} dK_j W'^{-1} V for the three parameters (3 n x p)
+  // stochastic Hessian: second-derivative product, evaluated for one parameter pair at a time
+  int d2_pair = -1;           // evaluation code (kD2Base + 3 j + k) of the cached pair, -1 none
+  double* d_hPhi3 = nullptr;  // Phi_j, Phi_k, Phi_jk (3 n r, the per-leaf layout of Phi)
+  double* d_hD2 = nullptr;    // dense second-derivative leaves
+  double* d_hS = nullptr;     // Sj, Sk, Sjk, three products with S^{-1}, then A, Bj, Bk, Bjk, Cjk, Ckj
+  double* d_hT = nullptr;     // Tmul, Tmult ((4r)^2 each)
+  double* d_hP = nullptr;     // per slot and column: four projections (4r) ...
+  double* d_hG = nullptr;     // ... and four expansion coefficients (4r)
+  int64_t hcap = 0;
+  double* d_hA = nullptr;     // a_j = dK_j u and b_j = K^{-1} a_j (6 n)
+  double* d_hY = nullptr;     // second-derivative products of [W'^{-1} V | u]
+  double* d_hdots = nullptr;
   double* d_res = nullptr;   // refinement residual (n x rcap)
   double* d_rdots = nullptr;
   int64_t rcap = 0;
@@ -317,6 +329,9 @@ void free_problem(km_handle* h) {
   h->gcap = h->tcap = 0;
   h->d_res = h->d_rdots = nullptr;
   h->rcap = 0;
+  h->d2_pair = -1;
+  h->d_hPhi3 = h->d_hD2 = h->d_hS = h->d_hT = h->d_hP = h->d_hG = h->d_hA = h->d_hY = h->d_hdots = nullptr;
+  h->hcap = 0;
   h->assembled = h->factorized = false;
 }
 
@@ -848,6 +863,79 @@ int derivative_apply(km_handle* h, int j, const double* X, double* Y, int k) {
                                                               t.n, h->d_GG, Y, t.n, k, st));
   return check_launch(h, "derivative");
 }
+
+// Y = D2_jk X (Deriv2mul, src/HODLR/src/utils.jl:157-177) for parameters j <= k: the dense
+// second-derivative leaves plus the reference's block products SDBlock_mul / SDBlock_mul_t
+// (utils.jl:110-155) of every non-leaf block, in the nested form of km_grad.cu (device pointers,
+// FP64 in both precision forms; k columns).
+int deriv2_apply(km_handle* h, int j, int k, const double* X, double* Y, int kc) {
+  const Tree& t = h->tree;
+  const int r = h->r, R = 4 * r;
+  cudaStream_t st = h->stream;
+  int rc;
+  const int code = kD2Base + 3 * j + k;
+  if (h->d2_pair != code) {
+    int64_t kbytes = 0;
+    for (int64_t q = 0; q < t.nleaf; ++q) kbytes += t.leaf_size(q) * t.leaf_size(q);
+    const int64_t rr = (int64_t)r * r;
+    if ((rc = grow(h, &h->d_hPhi3, 3 * t.n * r)) || (rc = grow(h, &h->d_hD2, kbytes)) ||
+        (rc = grow(h, &h->d_hS, 12 * rr)) || (rc = grow(h, &h->d_hT, 2 * (int64_t)R * R)))
+      return rc;
+    double* Pj = h->d_hPhi3;
+    double* Pk = Pj + t.n * r;
+    double* Pjk = Pk + t.n * r;
+    // SecondDerivativeLeaves / SecondDerivativeBlocks (constructor.jl:100-121) and the first
+    // derivatives of the same blocks (constructor.jl:66-95)
+    KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, j, Pj, st, false));
+    KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, k, Pk, st, false));
+    KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, code, Pjk, st, false));
+    KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, code, h->d_hD2, st, false));
+    double* Sj = h->d_hS;
+    double* Sk = Sj + rr;
+    double* Sjk = Sk + rr;
+    double* tA = Sjk + rr;
+    double* tB = tA + rr;
+    double* tC = tB + rr;
+    double* M = tC + rr;  // A = S^{-1}, Bj, Bk, Bjk, Cjk, Ckj
+    KLV(h, KM_PROF_EVAL, launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, j, Sj, r, st));
+    KLV(h, KM_PROF_EVAL, launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, k, Sk, r, st));
+    KLV(h, KM_PROF_EVAL, launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, code, Sjk, r, st));
+    KLV(h, KM_PROF_OTHER, launch_small_gemm(h->d_SinvT, h->d_SinvT, r, 1, M, st));  // S^{-1} = Sc^{-T} Sc^{-1}
+    KLV(h, KM_PROF_OTHER, launch_small_gemm(Sj, M, r, 0, tA, st));
+    KLV(h, KM_PROF_OTHER, launch_small_gemm(Sk, M, r, 0, tB, st));
+    KLV(h, KM_PROF_OTHER, launch_small_gemm(Sjk, M, r, 0, tC, st));
+    KLV(h, KM_PROF_OTHER, launch_small_gemm(M, tA, r, 0, M + rr, st));          // Bj = A Sj A
+    KLV(h, KM_PROF_OTHER, launch_small_gemm(M, tB, r, 0, M + 2 * rr, st));      // Bk
+    KLV(h, KM_PROF_OTHER, launch_small_gemm(M, tC, r, 0, M + 3 * rr, st));      // Bjk
+    KLV(h, KM_PROF_OTHER, launch_small_gemm(M + rr, tB, r, 0, M + 4 * rr, st));  // Cjk = Bj Sk A
+    KLV(h, KM_PROF_OTHER, launch_small_gemm(M + 2 * rr, tA, r, 0, M + 5 * rr, st));  // Ckj = Bk Sj A
+    KLV(h, KM_PROF_OTHER, launch_d2_assemble(M, r, h->d_hT, h->d_hT + (int64_t)R * R, st));
+    h->d2_pair = code;
+  }
+  if (kc > h->hcap) {
+    h->hcap = 0;
+    const int64_t slots = t.nleaf + t.nnode;
+    if ((rc = grow(h, &h->d_hP, slots * R * kc)) || (rc = grow(h, &h->d_hG, slots * R * kc))) return rc;
+    h->hcap = kc;
+  }
+  if (t.L > 0) {
+    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_phi4T(h->d_Phi, h->d_hPhi3, r, t, X, t.n, h->d_hP, kc, st));
+    NodeMatsH nm4{nullptr, nullptr, nullptr, nullptr, R};
+    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up<double>(t, nm4, l, h->d_hP, nullptr, kc, UP_SUM_, st));
+    for (int l = t.L; l >= 1; --l)
+      KLV(h, KM_PROF_SWEEP, launch_d2_down(h->d_hT, h->d_hT + (int64_t)R * R, r, t, l, h->d_hP, h->d_hG, kc, st));
+    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_d2_apply(h->d_hD2, h->d_Phi, h->d_hPhi3, r, t, X, t.n, h->d_hG, Y, t.n,
+                                                    kc, st));
+  } else {
+    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_d2_apply(h->d_hD2, h->d_Phi, h->d_hPhi3, r, t, X, t.n, nullptr, Y, t.n,
+                                                    kc, st));
+  }
+  return check_launch(h, "second derivative");
+}
+
+// Pairs whose second derivative vanishes identically (ZeroFunction in stoch_hessian): every
+// pair with the nugget, and scale-scale for the Matern kernel (linear in the scale).
+bool d2_zero(int kid, int j, int k) { return k == 2 || j == 2 || (kid == KM_KERNEL_MATERN32 && j == 0 && k == 0); }
 
 bool finite3(const double* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
 
@@ -1392,6 +1480,7 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   h->r = (int)maxrank;
   h->assembled = h->factorized = false;
   h->dk_param = -1;
+  h->d2_pair = -1;
   h->mixed = (h->cfg.precision == KM_PREC_MIXED);
   const int r = h->r;
   int64_t kbytes = 0;
@@ -1874,6 +1963,70 @@ int km_grad_fisher_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_
                           double* grad, double* fisher) {
   if (!fisher) return fail(h, KM_ERR_BAD_ARG, "bad likelihood arguments");
   return nll_grad_impl(h, y, nullptr, true, seed, nprobe, nll, grad, false, fisher);
+}
+
+// Stochastic Hessian of the NLL (stoch_hessian, src/HODLR/src/stochastichessian.jl:117-147, with
+// shuffle = false and profile = false): minus the stochastic Fisher matrix, plus for every pair
+// j <= k the trace term 0.5 mean_v t'D2_jk t (t = W'^{-1} v, HODLR_hess_tr2 :79-89) where the
+// second derivative is not identically zero, and minus half the solve term
+// -u'dK_k K^{-1} dK_j u - u'dK_j K^{-1} dK_k u (+ u'D2_jk u), u = K^{-1} y (HODLR_hess_slv(_no2d)
+// :3-13, :50-56), written with the symmetry of K^{-1} and dK_j.  The probes, W'^{-1} V and u come
+// from the gradient and Fisher call.
+static int hessian_impl(km_handle* h, const double* y, const double* probes, bool seeded, uint64_t seed,
+                        int64_t nprobe, double* nll, double* grad, double* hess) {
+  if (!h || !hess || !grad || nprobe < 1) return fail(h, KM_ERR_BAD_ARG, "bad Hessian arguments");
+  double F[9];
+  int rc = nll_grad_impl(h, y, probes, seeded, seed, nprobe, nll, grad, false, F);
+  if (rc != KM_OK) return rc;
+  const Tree& t = h->tree;
+  const int64_t n = t.n, p = nprobe;
+  cudaStream_t st = h->stream;
+  const double* u = h->d_T + n * p;  // d_T = [W'^{-1} V | K^{-1} y]
+  if ((rc = grow(h, &h->d_hA, 6 * n)) || (rc = grow(h, &h->d_hY, n * (p + 1))) ||
+      (rc = grow(h, &h->d_hdots, p + 1 + 9)))
+    return rc;
+  double* a = h->d_hA;      // a_j = dK_j u
+  double* b = a + 3 * n;    // b_j = K^{-1} a_j
+  for (int j = 0; j < 3; ++j) {
+    if ((rc = derivative_apply(h, j, u, a + j * n, 1)) != KM_OK) return rc;
+    KM_CUDA(h, cudaMemcpyAsync(b + j * n, a + j * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    if ((rc = nested_solve(h, b + j * n, 1)) != KM_OK) return rc;
+  }
+  double* d_ab = h->d_hdots + p + 1;  // d_ab[3 j + k] = a_k . b_j
+  for (int j = 0; j < 3; ++j)
+    for (int k = 0; k < 3; ++k)
+      KLV(h, KM_PROF_OTHER, launch_col_dots(a + k * n, n, b + j * n, n, n, 1, d_ab + 3 * j + k, st));
+  double ab[9];
+  KM_CUDA(h, cudaMemcpyAsync(ab, d_ab, sizeof ab, cudaMemcpyDeviceToHost, st));
+  if ((rc = sync(h, "hessian")) != KM_OK) return rc;
+  std::vector<double> dd(p + 1);
+  for (int j = 0; j < 3; ++j)
+    for (int k = j; k < 3; ++k) {
+      double sterm = -(ab[3 * j + k] + ab[3 * k + j]);
+      double tr = 0.0;
+      if (!d2_zero(h->kp.kid, j, k)) {
+        if ((rc = deriv2_apply(h, j, k, h->d_T, h->d_hY, (int)(p + 1))) != KM_OK) return rc;
+        KLV(h, KM_PROF_OTHER, launch_col_dots(h->d_T, n, h->d_hY, n, n, (int)(p + 1), h->d_hdots, st));
+        KM_CUDA(h, cudaMemcpyAsync(dd.data(), h->d_hdots, sizeof(double) * (p + 1), cudaMemcpyDeviceToHost, st));
+        if ((rc = sync(h, "hessian")) != KM_OK) return rc;
+        for (int64_t c = 0; c < p; ++c) tr += dd[c];
+        tr /= (double)p;
+        sterm += dd[p];  // u' D2_jk u
+      }
+      hess[3 * j + k] = hess[3 * k + j] = -F[3 * j + k] + 0.5 * tr - 0.5 * sterm;
+    }
+  return KM_OK;
+}
+
+int km_stoch_hessian(km_handle* h, const double* y, const double* probes, int64_t nprobe, double* nll,
+                     double* grad, double* hess) {
+  if (!probes) return fail(h, KM_ERR_BAD_ARG, "bad Hessian arguments");
+  return hessian_impl(h, y, probes, false, 0, nprobe, nll, grad, hess);
+}
+
+int km_stoch_hessian_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed, double* nll,
+                            double* grad, double* hess) {
+  return hessian_impl(h, y, nullptr, true, seed, nprobe, nll, grad, hess);
 }
 
 int km_profile_nll_grad(km_handle* h, const double* y, const double* probes, int64_t nprobe, double* nll,

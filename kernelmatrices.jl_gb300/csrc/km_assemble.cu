@@ -101,6 +101,8 @@ __device__ __forceinline__ double dkernel_value_ff(const KParams& kp, int j, dou
 
 __device__ __forceinline__ double eval_entry(bool use_ff, const KParams& kp, int deriv, double x1, double y1,
                                              double x2, double y2) {
+  if (deriv >= kD2Base)  // second derivatives: FP64 only
+    return d2kernel_value(kp, (deriv - kD2Base) / 3, (deriv - kD2Base) % 3, x1, y1, x2, y2);
   if (use_ff)
     return deriv < 0 ? kernel_value_ff(kp, x1, y1, x2, y2) : dkernel_value_ff(kp, deriv, x1, y1, x2, y2);
   return deriv < 0 ? kernel_value(kp, x1, y1, x2, y2) : dkernel_value(kp, deriv, x1, y1, x2, y2);
@@ -176,8 +178,7 @@ __global__ void k_eval_dense(const double* __restrict__ a, int na, const double*
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= na * nb) return;
   const int i = e % na, j = e / na;
-  const double v = deriv < 0 ? kernel_value(kp, a[2 * i], a[2 * i + 1], b[2 * j], b[2 * j + 1])
-                             : dkernel_value(kp, deriv, a[2 * i], a[2 * i + 1], b[2 * j], b[2 * j + 1]);
+  const double v = eval_entry(false, kp, deriv, a[2 * i], a[2 * i + 1], b[2 * j], b[2 * j + 1]);
   out[i + (int64_t)j * ld] = v;
 }
 

@@ -330,6 +330,189 @@ template void launch_leaf_dnys_apply<ff>(const ff*, const ff*, const ff*, const 
                                          const Tree&, const double*, int64_t, const double*, double*, int64_t, int,
                                          cudaStream_t, const ff*);
 
+// ---------------------------------------------------------------------------------------------
+// Second-derivative product of the stochastic Hessian (Deriv2mul, src/HODLR/src/utils.jl:157-177)
+// in the nested Nystrom form.  The landmark matrices are global, so the reference's block
+// products SDBlock_mul / SDBlock_mul_t (utils.jl:110-155) are linear maps of the four projections
+// [Phi' s; Phi_j' s; Phi_k' s; Phi_jk' s] of the source block onto the four expansion coefficients
+// of the target block: Tmul and Tmult (R x R, R = 4r, formed once from S^{-1}, S_j, S_k, S_jk).
+// A node's projections are sums of its leaves' (up-sweep, UP_SUM at width R).  The reference's
+// block (a:b, c:d) of a node has the rows of its second child and the columns of its first
+// (HODLRindices), so Deriv2mul adds SDBlock_mul of the first child's values to the second child
+// and SDBlock_mul_t of the second child's values to the first: the down-sweep gives the second
+// child Tmul (projections of the first) and the first child Tmult (projections of the second)
+// on top of its parent's coefficients; a leaf then adds its dense second-derivative block and
+// its four basis expansions.  Variant order: Phi, Phi_j, Phi_k,
+// Phi_jk; Phi3 holds Phi_j, Phi_k, Phi_jk (n r values each, the per-leaf layout of Phi).
+// ---------------------------------------------------------------------------------------------
+
+// VP[(leaf k + c) R + v r + q] = Phi_v(leaf)' x_c.  grid (nleaf, k), block 256.
+__global__ void __launch_bounds__(256) k_leaf_phi4T(const double* __restrict__ Phi, const double* __restrict__ Phi3,
+                                                    int64_t nr, int r, DTree t, const double* __restrict__ X,
+                                                    int64_t ldx, double* __restrict__ VP, int k) {
+  extern __shared__ double xs[];  // the leaf's rows of column c
+  const int64_t leaf = blockIdx.x;
+  const int c = blockIdx.y;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf);
+  for (int i = threadIdx.x; i < m; i += blockDim.x) xs[i] = X[(int64_t)c * ldx + s + i];
+  __syncthreads();
+  const int R = 4 * r;
+  for (int e = threadIdx.x; e < R; e += blockDim.x) {
+    const int v = e / r, q = e - v * r;
+    const double* P = (v == 0 ? Phi : Phi3 + (int64_t)(v - 1) * nr) + s * r + (int64_t)q * m;
+    double acc = 0.0;
+    for (int i = 0; i < m; ++i) acc += P[i] * xs[i];
+    VP[(leaf * k + c) * R + e] = acc;
+  }
+}
+
+// Down-sweep of one level: VG(child 1) = g + Tmult VP(child 2), VG(child 2) = g + Tmul VP(child 1),
+// g the parent's coefficients (zero at the root).  Tmul, Tmult column-major R x R.
+// grid (nodes at the level, k), block 256.
+__global__ void __launch_bounds__(256) k_d2_down(const double* __restrict__ Tmul, const double* __restrict__ Tmult,
+                                                 int R, int top, int64_t cslot0, int64_t nslot0,
+                                                 const double* __restrict__ VP, double* __restrict__ VG, int k) {
+  extern __shared__ double sd[];  // g, p1, p2 (R each)
+  double* g = sd;
+  double* p1 = g + R;
+  double* p2 = p1 + R;
+  const int64_t kk = blockIdx.x;
+  const int c = blockIdx.y;
+  const int64_t s1 = cslot0 + 2 * kk, s2 = s1 + 1;
+  for (int e = threadIdx.x; e < R; e += blockDim.x) {
+    g[e] = top ? 0.0 : VG[((nslot0 + kk) * k + c) * R + e];
+    p1[e] = VP[(s1 * k + c) * R + e];
+    p2[e] = VP[(s2 * k + c) * R + e];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < R; e += blockDim.x) {
+    double a1 = g[e], a2 = g[e];
+    for (int f = 0; f < R; ++f) {
+      a1 += Tmult[e + (int64_t)f * R] * p2[f];
+      a2 += Tmul[e + (int64_t)f * R] * p1[f];
+    }
+    VG[(s1 * k + c) * R + e] = a1;
+    VG[(s2 * k + c) * R + e] = a2;
+  }
+}
+
+// Y_leaf = D2_leaf x_leaf + sum_v Phi_v(leaf) G_v(leaf); G = 0 when VG is null (one leaf).
+// grid (nleaf, k), block 256; D2 the dense leaf blocks (column-major m x m at the leaf offset).
+__global__ void __launch_bounds__(256) k_leaf_d2_apply(const double* __restrict__ D2, const double* __restrict__ Phi,
+                                                       const double* __restrict__ Phi3, int64_t nr, int r, DTree t,
+                                                       const double* __restrict__ X, int64_t ldx,
+                                                       const double* __restrict__ VG, double* __restrict__ Y,
+                                                       int64_t ldy, int k) {
+  extern __shared__ double sa[];  // x (m), G (4r)
+  const int64_t leaf = blockIdx.x;
+  const int c = blockIdx.y;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf);
+  const int R = 4 * r;
+  double* xs = sa;
+  double* G = sa + m;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) xs[i] = X[(int64_t)c * ldx + s + i];
+  for (int e = threadIdx.x; e < R; e += blockDim.x) G[e] = VG ? VG[(leaf * k + c) * R + e] : 0.0;
+  __syncthreads();
+  const double* A = D2 + d_leaf_koff(t, leaf);
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    double acc = 0.0;
+    for (int j = 0; j < m; ++j) acc += A[(int64_t)j * m + i] * xs[j];
+    for (int v = 0; v < 4; ++v) {
+      const double* P = (v == 0 ? Phi : Phi3 + (int64_t)(v - 1) * nr) + s * r;
+      for (int q = 0; q < r; ++q) acc += P[(int64_t)q * m + i] * G[v * r + q];
+    }
+    Y[(int64_t)c * ldy + s + i] = acc;
+  }
+}
+
+// Tmul and Tmult (column-major R x R) from M = [A, Bj, Bk, Bjk, Cjk, Ckj] (r x r each), with
+// A = S^{-1}, B_x = A S_x A, Cjk = Bj Sk A, Ckj = Bk Sj A; blocks (output variant, input variant):
+//   Tmul  = [[-Ckj + Bjk - Cjk - Bk, Bj, 0, A], [-Bk, 0, A, 0], [Bj + A, 0, 0, 0], [A, 0, 0, 0]]
+//   Tmult = [[-Cjk + Bjk - Ckj, -Bk, Bj, A], [-Bk, 0, A, 0], [Bj, 0, A, 0], [A, 0, 0, 0]]
+// (SDBlock_mul and SDBlock_mul_t read term by term as maps of the four projections).
+__global__ void k_d2_assemble(const double* __restrict__ M, int r, double* __restrict__ Tmul,
+                              double* __restrict__ Tmult) {
+  const int R = 4 * r;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)R * R) return;
+  const int row = (int)(e % R), col = (int)(e / R);
+  const int bi = row / r, bj = col / r;
+  const int64_t rr = (int64_t)r * r;
+  const int64_t o = (row - bi * r) + (int64_t)(col - bj * r) * r;
+  const double A = M[o], Bj = M[rr + o], Bk = M[2 * rr + o], Bjk = M[3 * rr + o], Cjk = M[4 * rr + o],
+               Ckj = M[5 * rr + o];
+  double u = 0.0, w = 0.0;
+  if (bi == 0) {
+    if (bj == 0) {
+      u = -Ckj + Bjk - Cjk - Bk;
+      w = -Cjk + Bjk - Ckj;
+    } else if (bj == 1) {
+      u = Bj;
+      w = -Bk;
+    } else if (bj == 2) {
+      w = Bj;
+    } else {
+      u = A;
+      w = A;
+    }
+  } else if (bi == 1) {
+    if (bj == 0) {
+      u = -Bk;
+      w = -Bk;
+    } else if (bj == 2) {
+      u = A;
+      w = A;
+    }
+  } else if (bi == 2) {
+    if (bj == 0) {
+      u = Bj + A;
+      w = Bj;
+    } else if (bj == 2) {
+      w = A;
+    }
+  } else if (bj == 0) {
+    u = A;
+    w = A;
+  }
+  Tmul[e] = u;
+  Tmult[e] = w;
+}
+
+void launch_leaf_phi4T(const double* Phi, const double* Phi3, int r, const Tree& t, const double* X, int64_t ldx,
+                       double* VP, int k, cudaStream_t st) {
+  const size_t sm = (size_t)t.max_leaf * sizeof(double);
+  smem_limit((const void*)k_leaf_phi4T, sm);
+  k_leaf_phi4T<<<dim3((unsigned)t.nleaf, (unsigned)k), 256, sm, st>>>(Phi, Phi3, t.n * (int64_t)r, r, dtree(t), X,
+                                                                      ldx, VP, k);
+}
+
+void launch_d2_down(const double* Tmul, const double* Tmult, int r, const Tree& t, int level, const double* VP,
+                    double* VG, int k, cudaStream_t st) {
+  const int R = 4 * r;
+  const int64_t cslot0 = level == 1 ? 0 : t.nleaf + t.node_off[level - 1];
+  const int64_t nslot0 = t.nleaf + t.node_off[level];
+  const size_t sm = (size_t)3 * R * sizeof(double);
+  smem_limit((const void*)k_d2_down, sm);
+  k_d2_down<<<dim3((unsigned)t.nodes_at(level), (unsigned)k), 256, sm, st>>>(Tmul, Tmult, R, level >= t.L ? 1 : 0,
+                                                                             cslot0, nslot0, VP, VG, k);
+}
+
+void launch_leaf_d2_apply(const double* D2, const double* Phi, const double* Phi3, int r, const Tree& t,
+                          const double* X, int64_t ldx, const double* VG, double* Y, int64_t ldy, int k,
+                          cudaStream_t st) {
+  const size_t sm = ((size_t)t.max_leaf + 4 * r) * sizeof(double);
+  smem_limit((const void*)k_leaf_d2_apply, sm);
+  k_leaf_d2_apply<<<dim3((unsigned)t.nleaf, (unsigned)k), 256, sm, st>>>(D2, Phi, Phi3, t.n * (int64_t)r, r,
+                                                                         dtree(t), X, ldx, VG, Y, ldy, k);
+}
+
+void launch_d2_assemble(const double* M, int r, double* Tmul, double* Tmult, cudaStream_t st) {
+  const int64_t tot = (int64_t)16 * r * r;
+  k_d2_assemble<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(M, r, Tmul, Tmult);
+}
+
 void launch_small_gemm(const double* A, const double* B, int r, int transB, double* C, cudaStream_t st) {
   k_small_gemm<<<r, 128, 0, st>>>(A, B, r, transB, C);
 }

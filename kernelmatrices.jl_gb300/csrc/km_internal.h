@@ -149,6 +149,46 @@ __device__ __forceinline__ double dkernel_value(const KParams& kp, int j, double
   return __ddiv_rn(__dmul_rn(__dmul_rn(-kp.p0, dc), r), __dmul_rn(kp.p1, kp.p1));
 }
 
+// Second derivative of kernel_value in parameters j and k (0 scale, 1 range, 2 nugget), the
+// closed forms of the second-derivative functions the reference's stoch_hessian takes from its
+// caller (d2funs, src/HODLR/src/stochastichessian.jl:117-121):
+//   MATERN32 (z = sqrt3 r / p1): d00 = 0, d01 = z^2 e^-z / p1, d11 = p0 z^2 (z - 3) e^-z / p1^2,
+//            0 where r / p1 <= 1e-8 as for the first derivative;
+//   RATQUAD  (u = 1 + t^2, t = r / p1): d00 = 2 / u^2, d01 = 8 p0 r^2 / (p1^3 u^3),
+//            d11 = 12 p0^2 r^2 (t^2 - 1) / (p1^4 u^4);
+//   any pair with the nugget: 0.
+// Evaluation kernels select it with deriv = kD2Base + 3 j + k.
+constexpr int kD2Base = 10;
+
+__device__ __forceinline__ double d2kernel_value(const KParams& kp, int j, int k, double x1, double y1,
+                                                 double x2, double y2) {
+  if (j > k) {
+    const int s = j;
+    j = k;
+    k = s;
+  }
+  if (k == 2) return 0.0;
+  const double dx = x1 - x2, dy = y1 - y2;
+  const double r2 = dx * dx + dy * dy;
+  const double r = sqrt(r2);
+  if (kp.kid == KM_KERNEL_RATQUAD) {
+    const double t = r / kp.p1;
+    const double u = 1.0 + t * t;
+    if (j == 0 && k == 0) return 2.0 / (u * u);
+    const double p13 = kp.p1 * kp.p1 * kp.p1;
+    if (j == 0) return 8.0 * kp.p0 * r2 / p13 / (u * u * u);
+    return 12.0 * kp.p0 * kp.p0 * r2 * (t * t - 1.0) / (p13 * kp.p1) / (u * u * u * u);
+  }
+  if (j == 0 && k == 0) return 0.0;
+  if (!(r > 0.0)) return 0.0;
+  const double x = r / kp.p1;
+  if (!(fabs(x) > 1.0e-8)) return 0.0;
+  const double z = kSqrt3 * x;
+  const double e = exp(-z);
+  if (j == 0) return z * z * e / kp.p1;
+  return kp.p0 * z * z * (z - 3.0) * e / (kp.p1 * kp.p1);
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

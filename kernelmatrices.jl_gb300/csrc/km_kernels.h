@@ -138,6 +138,15 @@ void launch_leaf_dnys_apply(const T* dKl, const T* Phi, const T* dPhi, const dou
                             const Tree& t, const double* X, int64_t ldx, const double* VG, double* Y, int64_t ldy,
                             int k, cudaStream_t st, const T* betas = nullptr);
 // C = A op(B), r x r FP64 (op = transpose when transB)
+// second-derivative product of the stochastic Hessian (km_grad.cu)
+void launch_leaf_phi4T(const double* Phi, const double* Phi3, int r, const Tree& t, const double* X, int64_t ldx,
+                       double* VP, int k, cudaStream_t st);
+void launch_d2_down(const double* Tmul, const double* Tmult, int r, const Tree& t, int level, const double* VP,
+                    double* VG, int k, cudaStream_t st);
+void launch_leaf_d2_apply(const double* D2, const double* Phi, const double* Phi3, int r, const Tree& t,
+                          const double* X, int64_t ldx, const double* VG, double* Y, int64_t ldy, int k,
+                          cudaStream_t st);
+void launch_d2_assemble(const double* M, int r, double* Tmul, double* Tmult, cudaStream_t st);
 void launch_small_gemm(const double* A, const double* B, int r, int transB, double* C, cudaStream_t st);
 // landmark coefficients of the derivative products from explicit S^{-1} and S^{-1} Sj S^{-1}
 template <typename T>

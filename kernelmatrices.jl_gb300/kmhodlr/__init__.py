@@ -9,7 +9,8 @@ from .hodlr import (  # noqa: F401
     KMError, PosDefException, symmetricfactorize, logdet, nystrom_landmarks, probe_fp64_tflops,
     probe_fp32_tflops,
     negloglik, stoch_gradient, nll_objective, profile_negloglik, stoch_profile_gradient, nlpl_objective,
-    scaleparm_mle, gpsimulate, stoch_fisher, grad_and_fisher, grad_and_fisher_matrix, kd_order, maxlikdata,
+    scaleparm_mle, gpsimulate, stoch_fisher, grad_and_fisher, grad_and_fisher_matrix, stoch_hessian,
+    grad_fisher_hessian, kd_order, maxlikdata,
     RKernelHODLR,
 )
 from .serving import BatchEngine, Server, Problem, Result, estimate_bytes  # noqa: F401

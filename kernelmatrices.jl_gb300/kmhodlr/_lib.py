@@ -140,6 +140,8 @@ SIGNATURES = {
     "km_rhodlr_matvec": (C.c_int, [_P, _DP, _DP, C.c_int64]),
     "km_maxlikdata": (C.c_int, [_H, _DP, _DP, C.c_int64, C.c_int64, _DP, _DP, C.POINTER(C.c_int64)]),
     "km_grad_fisher_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP, _DP]),
+    "km_stoch_hessian": (C.c_int, [_H, _DP, _DP, C.c_int64, _DP, _DP, _DP]),
+    "km_stoch_hessian_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP, _DP]),
     "km_profile_nll_grad_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP]),
     "km_trim": (C.c_int, [_H]),
     "km_estimate_bytes": (C.c_int64, [C.c_int64, C.c_int64, C.c_int, C.c_int64, C.c_int64, C.c_int]),

@@ -374,6 +374,38 @@ def grad_and_fisher(HK: KernelHODLR, dat: np.ndarray, vecs=None, nprobe: int = 0
     return _grad_fisher(HK, dat, vecs, nprobe, seed)
 
 
+def _hessian(HK: "KernelHODLR", dat: np.ndarray, vecs=None, nprobe: int = 0, seed: int = 0):
+    lib = L.load()
+    y = np.ascontiguousarray(dat, dtype=np.float64).reshape(-1)
+    nll = C.c_double()
+    g = np.zeros(3)
+    H = np.zeros((3, 3), order="F")
+    if vecs is None:
+        _check(HK._h, lib.km_stoch_hessian_seeded(HK._h, _dp(y), int(nprobe), int(seed), C.byref(nll), _dp(g),
+                                                  _dp(H)))
+    else:
+        V = np.asfortranarray(np.column_stack(vecs) if isinstance(vecs, (list, tuple)) else vecs, dtype=np.float64)
+        _check(HK._h, lib.km_stoch_hessian(HK._h, _dp(y), _dp(V), V.shape[1], C.byref(nll), _dp(g), _dp(H)))
+    return nll.value, g, H
+
+
+def stoch_hessian(HK: KernelHODLR, dat: np.ndarray, vecs=None, nprobe: int = 0, seed: int = 0) -> np.ndarray:
+    """``stoch_hessian(K, HK, dat, d1funs, d2funs, vecs)`` (src/HODLR/src/stochastichessian.jl:117-147,
+    shuffle = false, profile = false) for the three kernel parameters, with the closed-form second
+    derivatives of the built-in kernels as d2funs.  Probes are ``vecs`` (host) or ``nprobe``
+    seeded Rademacher probes drawn on the device."""
+    if not HK.factorized:
+        raise KMError(L.KM_ERR_STATE, "The matrix needs to be factorized.")
+    return _hessian(HK, dat, vecs, nprobe, seed)[2]
+
+
+def grad_fisher_hessian(HK: KernelHODLR, dat: np.ndarray, vecs=None, nprobe: int = 0, seed: int = 0):
+    """(NLL, gradient, stochastic Hessian) from one set of probes (see ``stoch_hessian``)."""
+    if not HK.factorized:
+        raise KMError(L.KM_ERR_STATE, "The matrix needs to be factorized.")
+    return _hessian(HK, dat, vecs, nprobe, seed)
+
+
 def grad_and_fisher_matrix(prms, pts: np.ndarray, dat: np.ndarray, kernel, rank: int, lvl, saav,
                            device: int = 0):
     """``grad_and_fisher_matrix(prm, data, opts)`` (stochastichessian.jl:152-181): assemble

@@ -1,0 +1,50 @@
+"""The stochastic Hessian (km_stoch_hessian) against the oracle's restatement of stoch_hessian
+(src/HODLR/src/stochastichessian.jl:117-147) on the same points, data and probes: both kernels,
+FP64 and mixed forms, rel 1e-6 (FP64) / 1e-5 (mixed) of the largest entry, the tolerance of the
+Fisher matrix it contains (the per-probe terms go through W^{-T}), and every entry to 1e-5 / 1e-4
+of sqrt(|H_jj H_kk|).  The second-derivative terms
+alone (Hessian + Fisher) are checked to the same bound, and the seeded form against the
+explicit-probe form with the same probes."""
+import numpy as np
+import pytest
+
+from oracle import hodlr_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("kid,params", [(O.KERNEL_MATERN32, (1.0, 0.1, 1e-2)), (O.KERNEL_RQ, (1.2, 0.15, 1e-2))])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_stoch_hessian_matches_oracle(lib, kid, params, mixed):
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    n, rank, level = 2048, 32, 3
+    pts = uniform_points(n, 43)
+    y = np.random.default_rng(19).standard_normal(n)
+    V = O.rademacher_probes(n, 8, 23)
+    vecs = [V[:, c] for c in range(V.shape[1])]
+    ok = O.KernelMatrix(pts, pts, np.array(params), kid)
+    ohk = O.build_hodlr(ok, 0.0, rank, O.FixedLevel(level), nystrom=True)
+    O.symmetricfactorize(ohk)
+    H0 = O.stoch_hessian(ok, ohk, y, vecs)
+    F0 = O.stoch_fisher(ok, ohk, [O.derivative_hodlr(ok, j, ohk) for j in range(3)], vecs)
+    prec = K.KM_PREC_MIXED if mixed else K.KM_PREC_FP64
+    kern = K.Matern32() if kid == O.KERNEL_MATERN32 else K.RatQuad()
+    hk = K.KernelHODLR(K.KernelMatrix(pts, pts, params, kern), 0.0, rank, K.FixedLevel(level), nystrom=True,
+                       precision=prec)
+    K.symmetricfactorize(hk)
+    nll, g, H = K.grad_fisher_hessian(hk, y, V)
+    tol = (1e-5 if mixed else 1e-6) * np.max(np.abs(H0))
+    # the entries span orders of magnitude: each is also checked against sqrt(|H_jj H_kk|)
+    scale = np.sqrt(np.outer(np.abs(np.diag(H0)), np.abs(np.diag(H0))))
+    etol = (1e-4 if mixed else 1e-5) * scale
+    assert np.array_equal(H, H.T) and np.all(np.isfinite(H))
+    assert np.max(np.abs(H - H0)) <= tol, (H, H0)
+    assert np.all(np.abs(H - H0) <= etol), (H, H0)
+    _, _, F = K.grad_and_fisher(hk, y, V)
+    assert np.max(np.abs((H + F) - (H0 + F0))) <= tol
+    assert np.all(np.abs((H + F) - (H0 + F0)) <= etol)
+    nll2, g2, F2 = K.grad_and_fisher(hk, y, V)
+    assert nll2 == nll and np.array_equal(g2, g)
+    H2 = K.stoch_hessian(hk, y, nprobe=8, seed=23)
+    assert np.array_equal(H2, H)
