@@ -406,6 +406,16 @@ def grad_fisher_hessian(HK: KernelHODLR, dat: np.ndarray, vecs=None, nprobe: int
     return _hessian(HK, dat, vecs, nprobe, seed)
 
 
+def nll_hessian(prms, pts: np.ndarray, dat: np.ndarray, kernel, rank: int, lvl, saav, device: int = 0) -> np.ndarray:
+    """``nll_hessian(prms, data, opts)`` (src/HODLR/src/maxlikfunctions.jl:101-116): assemble
+    (Nystrom, ep = 0), factorise and return the stochastic Hessian over the probes ``saav``
+    (``stoch_hessian`` with the built-in kernels' second derivatives)."""
+    K = KernelMatrix(pts, pts, prms, kernel)
+    HK = KernelHODLR(K, 0.0, rank, lvl, nystrom=True, sorted=True, device=device)
+    symmetricfactorize(HK)
+    return _hessian(HK, dat, saav)[2]
+
+
 def grad_and_fisher_matrix(prms, pts: np.ndarray, dat: np.ndarray, kernel, rank: int, lvl, saav,
                            device: int = 0):
     """``grad_and_fisher_matrix(prm, data, opts)`` (stochastichessian.jl:152-181): assemble

@@ -48,3 +48,5 @@ def test_stoch_hessian_matches_oracle(lib, kid, params, mixed):
     assert nll2 == nll and np.array_equal(g2, g)
     H2 = K.stoch_hessian(hk, y, nprobe=8, seed=23)
     assert np.array_equal(H2, H)
+    if not mixed:  # the assemble + factorise + Hessian driver on a fresh FP64 handle
+        assert np.array_equal(K.nll_hessian(params, pts, y, kern, rank, K.FixedLevel(level), V), H)
