@@ -169,20 +169,26 @@ int km_solve_dev(km_handle* h, const double* d_b, double* d_x, int64_t k);
 int km_factor_solve_dev(km_handle* h, int transpose, const double* d_b, double* d_x, int64_t k);
 int km_factor_mul_dev(km_handle* h, int transpose, const double* d_b, double* d_x, int64_t k);
 
-/* Allocation-free solve: x = K^{-1} b for k columns, device pointers, same arithmetic and result
- * as km_solve_dev.  It has no counterpart in the reference.  It exists for callers that cannot
- * call cudaMalloc at solve time: cudaMalloc and cudaFree synchronise the whole device (a serving
- * loop that keeps other streams busy cannot afford that), and some hosts hand every byte of device
- * memory to their own pool allocator.  Instead of the handle's growable workspace, the call uses
- * one fixed device array compiled into this library, KM_NOALLOC_SCRATCH_BYTES (8 MiB) large, which
- * every GPU that loads the library holds until the process exits.  The handle must already be
- * factorised (its factor was allocated by km_assemble/km_factorize).  A request whose workspace,
- * 8 * k * r * (2 * (nleaves + nnodes) + 2 * nnodes) bytes, exceeds the array is rejected with
- * KM_ERR_BAD_ARG; split the columns over several calls.  The first call on a device looks up the
- * array's device address with that device current, so make it before any stream capture.  All
- * calls share the array and it keeps the last call's contents (the solve writes every workspace
- * entry before reading it, so nothing needs clearing): calls that overlap on the GPU, from any
- * handle or thread, race on it and must be serialised by the caller. */
+/* Allocation-free solve: x = K^{-1} b for k columns, device pointers, for Nystrom handles.  It
+ * has no counterpart in the reference.  It runs the kernels of km_solve_dev in the same order
+ * (one conversion to float pairs and back in the mixed form, and the FP64 iterative refinement
+ * when the handle's config asks for it), so its result equals km_solve_dev's.  It exists for
+ * callers that cannot call cudaMalloc at solve time: cudaMalloc and cudaFree synchronise the
+ * whole device (a serving loop that keeps other streams busy cannot afford that), and some hosts
+ * hand every byte of device memory to their own pool allocator.  Instead of the handle's growable
+ * workspace, the call uses one fixed device array compiled into this library,
+ * KM_NOALLOC_SCRATCH_BYTES (8 MiB) large, which every GPU that loads the library holds until the
+ * process exits.  The handle must already be factorised (its factor was allocated by
+ * km_assemble/km_factorize).  The workspace is 8 * k * r * (2 * (nleaves + nnodes) + 2 * nnodes)
+ * bytes, plus 8 * k * (n + 2) for the refinement of a mixed handle and another 8 * n * k when that
+ * call runs in place (d_x == d_b); a request above the array, or a refined one of more than 256
+ * columns, is rejected with KM_ERR_BAD_ARG: split the columns over several calls.  ACA handles
+ * are rejected with KM_ERR_UNSUPPORTED (their solve workspace depends on the block ranks and is
+ * grown on demand).  The first call on a device looks up the array's device address with that
+ * device current, so make it before any stream capture.  All calls share the array and it keeps
+ * the last call's contents (the solve writes every workspace entry before reading it, so nothing
+ * needs clearing): calls that overlap on the GPU, from any handle or thread, race on it and must
+ * be serialised by the caller. */
 #define KM_NOALLOC_SCRATCH_BYTES (8u << 20)
 int km_solve_noalloc(km_handle* h, const double* d_b, double* d_x, int64_t k);
 

@@ -728,39 +728,48 @@ int nystrom_matvec(km_handle* h, const double* X, double* Y, int k) {
 // Mixed form: FP64 iterative refinement x += K~^{-1} (b - K x), with the FP64 Nystrom HODLR
 // product as the residual operator (it keeps the FP64 leaves and landmark columns) and the
 // float-pair factor K~ as the preconditioner; stops at ||b - Kx||_F <= refine_tol ||b||_F.
-int refine(km_handle* h, const double* d_b, double* d_x, int k) {
+// The caller provides the buffers: res (n x k doubles), rdots (2k doubles, device) and hdots
+// (2k doubles, host).  d_b must not alias d_x.
+int refine_with(km_handle* h, const double* d_b, double* d_x, int k, double* res, double* rdots, double* hdots) {
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
   int rc;
-  if (k > h->rcap) {
-    h->rcap = 0;
-    if ((rc = grow(h, &h->d_res, t.n * k)) || (rc = grow(h, &h->d_rdots, 2 * k))) return rc;
-    h->rcap = k;
-  }
-  std::vector<double> dots(2 * k);
-  KLV(h, KM_PROF_OTHER, launch_col_dots(d_b, t.n, d_b, t.n, t.n, k, h->d_rdots + k, st));
+  KLV(h, KM_PROF_OTHER, launch_col_dots(d_b, t.n, d_b, t.n, t.n, k, rdots + k, st));
   int it = 0;
   double relres = 0.0;
   for (;;) {
-    if ((rc = nystrom_matvec(h, d_x, h->d_res, k)) != KM_OK) return rc;
-    KLV(h, KM_PROF_OTHER, launch_axpby(h->d_res, d_b, 1.0, -1.0, t.n * k, st));  // res = b - K x
-    KLV(h, KM_PROF_OTHER, launch_col_dots(h->d_res, t.n, h->d_res, t.n, t.n, k, h->d_rdots, st));
-    KM_CUDA(h, cudaMemcpyAsync(dots.data(), h->d_rdots, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, st));
+    if ((rc = nystrom_matvec(h, d_x, res, k)) != KM_OK) return rc;
+    KLV(h, KM_PROF_OTHER, launch_axpby(res, d_b, 1.0, -1.0, t.n * k, st));  // res = b - K x
+    KLV(h, KM_PROF_OTHER, launch_col_dots(res, t.n, res, t.n, t.n, k, rdots, st));
+    KM_CUDA(h, cudaMemcpyAsync(hdots, rdots, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, st));
     if ((rc = sync(h, "refine")) != KM_OK) return rc;
     double rr = 0.0, bb = 0.0;
     for (int c = 0; c < k; ++c) {
-      rr += dots[c];
-      bb += dots[k + c];
+      rr += hdots[c];
+      bb += hdots[k + c];
     }
     relres = bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
     if (relres <= h->cfg.refine_tol || it >= h->cfg.refine_max_iter) break;
-    if ((rc = nested_solve(h, h->d_res, k)) != KM_OK) return rc;
-    KLV(h, KM_PROF_OTHER, launch_axpby(d_x, h->d_res, 1.0, 1.0, t.n * k, st));  // x += d
+    if ((rc = nested_solve(h, res, k)) != KM_OK) return rc;
+    KLV(h, KM_PROF_OTHER, launch_axpby(d_x, res, 1.0, 1.0, t.n * k, st));  // x += d
     ++it;
   }
   h->stats.refine_iterations = it;
   h->stats.refine_residual = relres;
   return KM_OK;
+}
+
+// Refinement on the handle's own workspace.  d_b_saved is a copy of the right-hand sides when
+// the solve ran in place (d_b == d_x), else d_b itself.
+int refine(km_handle* h, const double* d_b, double* d_x, int k) {
+  int rc;
+  if (k > h->rcap) {
+    h->rcap = 0;
+    if ((rc = grow(h, &h->d_res, 2 * h->tree.n * k)) || (rc = grow(h, &h->d_rdots, 2 * k))) return rc;
+    h->rcap = k;
+  }
+  std::vector<double> dots(2 * k);
+  return refine_with(h, d_b, d_x, k, h->d_res, h->d_rdots, dots.data());
 }
 
 // Side stream: forms explicit leaf bases and node solve operators concurrently with the node
@@ -1470,7 +1479,7 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   const bool reuse = h->d_pts && h->tree.n == t.n && h->tree.L == t.L && h->r == (int)maxrank;
   if (!reuse) {
     if (h->stream) cudaStreamSynchronize(h->stream);
-    h->vcap = h->xcap = h->gcap = h->tcap = h->rcap = 0;
+    h->vcap = h->xcap = h->gcap = h->tcap = h->rcap = h->hcap = 0;
   }
   h->tree = t;
   h->kp = KParams{kernel_id, params[0], params[1], params[2]};
@@ -1683,9 +1692,22 @@ int km_solve_dev(km_handle* h, const double* d_b, double* d_x, int64_t k) {
   if (!h->factorized) return fail(h, KM_ERR_STATE, "No solves without factorization.");
   int rc;
   if ((rc = ensure_vec(h, k)) != KM_OK) return rc;
+  const bool refining = h->mixed && h->method == KM_METHOD_NYSTROM && h->cfg.refine_max_iter > 0;
+  if (refining && k > h->rcap) {
+    h->rcap = 0;
+    if ((rc = grow(h, &h->d_res, 2 * h->tree.n * k)) || (rc = grow(h, &h->d_rdots, 2 * k))) return rc;
+    h->rcap = k;
+  }
   timer_start(h);
-  if (d_x != d_b)
+  const double* b_keep = d_b;
+  if (d_x != d_b) {
     KM_CUDA(h, cudaMemcpyAsync(d_x, d_b, sizeof(double) * h->tree.n * k, cudaMemcpyDeviceToDevice, h->stream));
+  } else if (refining) {
+    // in place: the refinement residual needs the right-hand sides after x has replaced them
+    double* keep = h->d_res + h->tree.n * k;
+    KM_CUDA(h, cudaMemcpyAsync(keep, d_b, sizeof(double) * h->tree.n * k, cudaMemcpyDeviceToDevice, h->stream));
+    b_keep = keep;
+  }
   if (h->method == KM_METHOD_NYSTROM) {
     const int64_t sk[7] = {(int64_t)h->alloc_epoch, h->tree.n, h->tree.L, h->r, h->mixed ? 1 : 0,
                            (int64_t)(uintptr_t)d_x, k};
@@ -1694,9 +1716,7 @@ int km_solve_dev(km_handle* h, const double* d_b, double* d_x, int64_t k) {
     rc = nested_solve(h, d_x, (int)k);
   }
   if (rc != KM_OK) return rc;
-  if (h->mixed && h->method == KM_METHOD_NYSTROM && h->cfg.refine_max_iter > 0 &&
-      (rc = refine(h, d_b, d_x, (int)k)) != KM_OK)
-    return rc;
+  if (refining && (rc = refine(h, b_keep, d_x, (int)k)) != KM_OK) return rc;
   h->stats.solve_ms = timer_stop(h);
   return sync(h, "solve");
 }
@@ -2054,22 +2074,37 @@ std::mutex g_noalloc_mu;
 double* g_noalloc_dev[kMaxDevices] = {};
 }  // namespace
 
+// Columns the refinement of a mixed-precision handle can take in one allocation-free call: its
+// residual norms come back to a host array of this fixed size on the stack.
+static constexpr int64_t kNoAllocRefineCols = 256;
+
 extern "C" int km_solve_noalloc(km_handle* h, const double* d_b, double* d_x, int64_t k) {
   if (!h || !d_b || !d_x || k < 1) return fail(h, KM_ERR_BAD_ARG, "bad solve arguments");
   const int dev = h->cfg.device;
   if (dev < 0 || dev >= kMaxDevices) return fail(h, KM_ERR_BAD_ARG, "device ordinal out of range");
   KM_CUDA(h, cudaSetDevice(dev));
   if (!h->factorized) return fail(h, KM_ERR_STATE, "No solves without factorization.");
+  if (h->method != KM_METHOD_NYSTROM)
+    return fail(h, KM_ERR_UNSUPPORTED,
+                "km_solve_noalloc: only Nystrom handles; an ACA handle's solve sizes its workspace by the "
+                "block ranks and grows it on the device, use km_solve_dev");
   const Tree& t = h->tree;
   const int64_t slots = t.nleaf + t.nnode;
   const int64_t vp = slots * h->r * k;
-  const int64_t need = 2 * vp + std::max<int64_t>(t.nnode, 1) * 2 * h->r * k;
-  if (need > (int64_t)kNoAllocDoubles) {
-    char buf[256];
+  const int64_t vd = std::max<int64_t>(t.nnode, 1) * 2 * h->r * k;
+  const bool refining = h->mixed && h->cfg.refine_max_iter > 0;
+  const bool in_place = d_x == d_b;
+  // solve sweeps: VP, VG, VD; refinement: residual (n x k), its norms (2k) and, for an in-place
+  // call, a copy of the right-hand sides (n x k)
+  const int64_t need =
+      2 * vp + vd + (refining ? t.n * k + 2 * k + (in_place ? t.n * k : 0) : 0);
+  if (need > (int64_t)kNoAllocDoubles || (refining && k > kNoAllocRefineCols)) {
+    char buf[320];
     snprintf(buf, sizeof buf,
              "km_solve_noalloc: %lld columns need %lld bytes of workspace but the fixed array holds "
-             "%u bytes; pass fewer columns per call",
-             (long long)k, (long long)(need * sizeof(double)), (unsigned)KM_NOALLOC_SCRATCH_BYTES);
+             "%u bytes (refinement takes at most %lld columns); pass fewer columns per call",
+             (long long)k, (long long)(need * sizeof(double)), (unsigned)KM_NOALLOC_SCRATCH_BYTES,
+             (long long)kNoAllocRefineCols);
     return fail(h, KM_ERR_BAD_ARG, buf);
   }
   double* base = nullptr;
@@ -2083,20 +2118,32 @@ extern "C" int km_solve_noalloc(km_handle* h, const double* d_b, double* d_x, in
     }
     base = g_noalloc_dev[dev];
   }
-  // run the ordinary solve sweeps on the fixed workspace; the handle's own workspace is untouched
+  // run the ordinary solve (and refinement) on the fixed workspace; the handle's own workspace is
+  // untouched
   double* const sv[3] = {h->d_VP, h->d_VG, h->d_VD};
   const bool prof = h->prof;
   h->prof = false;  // the profiler creates events on demand
   h->d_VP = base;
   h->d_VG = base + vp;
   h->d_VD = base + 2 * vp;
+  double* res = base + 2 * vp + vd;
+  double* rdots = res + t.n * k;
+  double* bcopy = rdots + 2 * k;
   int rc = KM_OK;
-  if (d_x != d_b) {
-    cudaError_t e = cudaMemcpyAsync(d_x, d_b, sizeof(double) * t.n * k, cudaMemcpyDeviceToDevice, h->stream);
-    if (e != cudaSuccess) rc = cuda_fail(h, e, "cudaMemcpyAsync");
+  const double* b_keep = d_b;
+  cudaError_t e = cudaSuccess;
+  if (!in_place) {
+    e = cudaMemcpyAsync(d_x, d_b, sizeof(double) * t.n * k, cudaMemcpyDeviceToDevice, h->stream);
+  } else if (refining) {
+    e = cudaMemcpyAsync(bcopy, d_b, sizeof(double) * t.n * k, cudaMemcpyDeviceToDevice, h->stream);
+    b_keep = bcopy;
   }
-  if (rc == KM_OK) rc = nested_fwd(h, d_x, (int)k);
-  if (rc == KM_OK) rc = nested_bwd(h, d_x, (int)k);
+  if (e != cudaSuccess) rc = cuda_fail(h, e, "cudaMemcpyAsync");
+  if (rc == KM_OK) rc = nested_solve(h, d_x, (int)k);
+  if (rc == KM_OK && refining) {
+    double hdots[2 * kNoAllocRefineCols];
+    rc = refine_with(h, b_keep, d_x, (int)k, res, rdots, hdots);
+  }
   h->d_VP = sv[0];
   h->d_VG = sv[1];
   h->d_VD = sv[2];

@@ -50,3 +50,36 @@ def test_stoch_hessian_matches_oracle(lib, kid, params, mixed):
     assert np.array_equal(H2, H)
     if not mixed:  # the assemble + factorise + Hessian driver on a fresh FP64 handle
         assert np.array_equal(K.nll_hessian(params, pts, y, kern, rank, K.FixedLevel(level), V), H)
+
+
+def test_hessian_after_reassembly_at_a_larger_shape(lib):
+    """A handle that computed a Hessian at a small shape and is then reassembled at a larger one
+    regrows its second-derivative workspace: the Hessian equals, bit for bit, that of a fresh
+    handle at the larger shape."""
+    import kmhodlr as K
+    from kmhodlr import _lib as L
+    from kmhodlr import hodlr as KH
+    from kmhodlr.data import uniform_points
+    params = np.array([1.0, 0.1, 1e-2])
+    small = uniform_points(1024, 5)
+    big = uniform_points(4096, 6)
+    y_s = np.random.default_rng(1).standard_normal(1024)
+    y_b = np.random.default_rng(2).standard_normal(4096)
+    V_s = O.rademacher_probes(1024, 8, 3)
+    V_b = O.rademacher_probes(4096, 8, 4)
+    hk = K.KernelHODLR(K.KernelMatrix(small, small, params, K.Matern32()), 0.0, 16, K.FixedLevel(2),
+                       nystrom=True)
+    K.symmetricfactorize(hk)
+    K.stoch_hessian(hk, y_s, V_s)
+    kind, lv = KH._level(K.FixedLevel(4))
+    pb = np.ascontiguousarray(big)
+    rc = lib.km_assemble(hk._h, KH._dp(pb), 4096, int(K.Matern32().kid), KH._dp(params), 3,
+                         L.KM_METHOD_NYSTROM, 0.0, 32, kind, lv)
+    assert rc == L.KM_OK, lib.km_last_error(hk._h)
+    hk.n = 4096
+    K.symmetricfactorize(hk)
+    H = K.stoch_hessian(hk, y_b, V_b)
+    fresh = K.KernelHODLR(K.KernelMatrix(big, big, params, K.Matern32()), 0.0, 32, K.FixedLevel(4),
+                          nystrom=True)
+    K.symmetricfactorize(fresh)
+    assert np.array_equal(H, K.stoch_hessian(fresh, y_b, V_b))
