@@ -16,9 +16,12 @@ logdet and solve differences between them measured outside the timed regions.
 resident in HBM through the device entry points; `e2e` through the host-pointer C ABI (pinned
 host buffers, copies inside the timed region).  N > 1 runs N independent replicas (the path does
 not shard; weak scaling).
---impl reference: the reference's CPU algorithm (the NumPy restatement in oracle/, all host
-threads) on a bounded sample of the same workload, scaled to the workload by the reference
-algorithm's flop count.
+--impl reference: the reference's CPU algorithm (the NumPy restatement in oracle/) on the host
+cores, every timed step a full step of the same workload (n = 65536, FixedLevel(8)), with the
+reference's own parallel structure (`plel = true`: its `mapf`/`foreachf` maps over leaves, blocks
+and levels on a thread pool of all host threads, one BLAS thread per worker as the reference's
+`BLAS.set_num_threads(1)`).  It re-executes itself with OPENBLAS_NUM_THREADS=1 when that is not
+set, since the BLAS thread count is fixed when NumPy loads.
 """
 from __future__ import annotations
 
@@ -50,16 +53,6 @@ WORKLOAD = "matern32_nystrom_n65536_r72_fixedlevel8_16rhs"
 # ----------------------------------------------------------------------------------------------
 # algorithmic work models
 # ----------------------------------------------------------------------------------------------
-
-def reference_flops(n: int, L: int, m0: int = 256, r: int = RANK, nrhs: int = NRHS) -> float:
-    """Flops of the reference algorithm for one step: leaf Cholesky, leaf solves on the panels of
-    every level, per-level QR, the level-pair Woodbury updates with the dense block-diagonal M
-    (src/HODLR/src/symfact.jl:17-38), the solve (baseoverloads.jl:126-150) and logdet, which
-    re-factors the leaves (:200)."""
-    fact = n * m0 * m0 / 3 + L * n * m0 * r + 4 * L * n * r * r + 4 * L * (L - 1) * n * r * r
-    solve = nrhs * 2 * (n * m0 + 4 * L * n * r)
-    return fact + solve + n * m0 * m0 / 3
-
 
 def engine_flops(n: int, L: int, m0: int = 256, r: int = RANK) -> dict:
     """Algorithmic FP64 flops per launch class of the engine, for one step."""
@@ -132,26 +125,11 @@ class ClockSampler:
 # CPU legs (the oracle restatement of the reference)
 # ----------------------------------------------------------------------------------------------
 
-def cpu_sample(n_sample: int, L_sample: int, steps: int = 1) -> dict:
-    """Times the reference's CPU algorithm (oracle/) on a sample problem with the workload's
-    leaf size, rank, kernel and right-hand sides, and scales it to the workload by flop count."""
-    from oracle import hodlr_oracle as O
-    from kmhodlr.data import uniform_points
-    pts = uniform_points(n_sample, SEED)
-    rhs = np.random.default_rng(SEED + 1).standard_normal((n_sample, NRHS))
-    x = np.random.default_rng(SEED + 2).standard_normal((n_sample, 1))
-    times = []
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        K = O.KernelMatrix(pts, pts, np.array(PARAMS), O.KERNEL_MATERN32)
-        HK = O.build_hodlr(K, 0.0, RANK, O.FixedLevel(L_sample), nystrom=True)
-        O.hodlr_mul(HK, x)
-        O.symmetricfactorize(HK)
-        O.hodlr_ldiv(HK, rhs)
-        O.hodlr_logdet(HK)
-        times.append(time.perf_counter() - t0)
-    scale = reference_flops(N_POINTS, LEVEL) / reference_flops(n_sample, L_sample)
-    return {"times": times, "scale": scale}
+def line_config(world: int) -> dict:
+    """The workload keys shared by the GPU line and the reference line."""
+    return {"workload": WORKLOAD, "n": N_POINTS, "rank": RANK, "level": "FixedLevel(8)", "nrhs": NRHS,
+            "kernel": "matern32", "params": list(PARAMS),
+            "l2": "inputs larger than L2 (leaf factors alone 268 MB)", "parallelism": f"replicas{world}"}
 
 
 def host_threads() -> int:
@@ -161,28 +139,103 @@ def host_threads() -> int:
         return os.cpu_count() or 1
 
 
-def run_reference(args, rank: int):
+def cpu_full_steps(steps: int, warmup: int, budget_s: float) -> dict:
+    """Times full workload steps of the reference's CPU algorithm (oracle/): assemble, matvec,
+    symmetricfactorize!, a 16-column solve and logdet at n = 65536, FixedLevel(8), with the
+    reference's plel maps on a thread pool of all host threads.  Runs ``warmup`` untimed steps,
+    then up to ``steps`` timed ones, fewer when the next one would end past ``budget_s`` seconds
+    of timed work (at least one)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import hodlr_oracle as O
+    from kmhodlr.data import uniform_points
+    nt = host_threads()
+    pool = ThreadPoolExecutor(nt) if nt > 1 else None
+    pts = uniform_points(N_POINTS, SEED)
+    rng = np.random.default_rng(SEED + 100)
+    rhs = rng.standard_normal((N_POINTS, NRHS))
+    xv = rng.standard_normal((N_POINTS, 1))
+
+    def step():
+        K = O.KernelMatrix(pts, pts, np.array(PARAMS), O.KERNEL_MATERN32)
+        HK = O.build_hodlr(K, 0.0, RANK, O.FixedLevel(LEVEL), nystrom=True, pool=pool)
+        O.hodlr_mul(HK, xv)
+        O.symmetricfactorize(HK, pool=pool)
+        O.hodlr_ldiv(HK, rhs)
+        return O.hodlr_logdet(HK)
+
+    for _ in range(warmup):
+        step()
+    times = []
+    ld = None
+    while len(times) < steps:
+        if times and sum(times) + statistics.mean(times) > budget_s:
+            break
+        t0 = time.perf_counter()
+        ld = step()
+        times.append(time.perf_counter() - t0)
+    if pool is not None:
+        pool.shutdown()
+    return {"times": times, "threads": nt, "logdet": ld, "blas": os.environ.get("OPENBLAS_NUM_THREADS")}
+
+
+def _single_blas_env() -> dict:
+    env = dict(os.environ)
+    for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
+        env[k] = "1"
+    return env
+
+
+REF_SAMPLE = ("every timed step is a full workload step (n=65536 FixedLevel(8), Nystrom rank 72, 16 RHS: "
+              "assemble, matvec, symmetricfactorize!, solve, logdet) of the reference algorithm restated in "
+              "oracle/, with the reference's plel=true maps on a thread pool of all host threads and one BLAS "
+              "thread per worker")
+
+
+def run_reference(args, rank: int, world: int):
     if rank != 0:
         return
-    tot = args.steps + args.warmup
-    # sample sized so that the whole run stays within a few minutes
-    n_s, L_s = (16384, 6) if tot <= 8 else ((8192, 5) if tot <= 20 else (4096, 4))
-    cpu_sample(n_s, L_s, steps=args.warmup)
-    res = cpu_sample(n_s, L_s, steps=args.steps)
-    per_step = statistics.mean(res["times"]) * res["scale"]
+    if os.environ.get("OPENBLAS_NUM_THREADS") != "1":
+        # the BLAS thread count is read when NumPy loads: start over with one BLAS thread
+        os.execve(sys.executable, [sys.executable, str(Path(__file__).resolve()), *sys.argv[1:]],
+                  _single_blas_env())
+    # warm-up: the algorithm has no caches to warm; two steps page the code and data in
+    warm = min(args.warmup, 2)
+    res = cpu_full_steps(args.steps, warm, budget_s=args.ref_budget)
+    per_step = statistics.mean(res["times"])
     value = 1.0 / per_step
-    sample = (f"n={n_s} FixedLevel({L_s}) (256-point leaves, rank 72, same kernel, 16 RHS) per step, "
-              f"scaled x{res['scale']:.2f} to n=65536 FixedLevel(8) by the reference algorithm's flop count")
-    out = {"metric": "HODLR factor+solve+logdet/s", "value": value, "unit": "steps/s", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
+    steps = len(res["times"])
+    sample = REF_SAMPLE
+    if steps < args.steps:
+        sample += f"; {steps} of the {args.steps} requested steps timed (time budget {args.ref_budget:.0f} s)"
+    out = {"metric": "HODLR factor+solve+logdet/s", "value": value, "unit": "steps/s", "n_gpus": world,
+           "steps": steps, "warmup": warm, "ms_per_step": per_step * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "n": N_POINTS, "rank": RANK, "level": "FixedLevel(8)", "nrhs": NRHS,
-                      "kernel": "matern32", "params": list(PARAMS)},
+           "config": line_config(world), "precision": "fp64",
            "impl": "reference",
-           "cpu_baseline": {"value": value, "unit": "steps/s", "cores": host_threads(), "kind": "port",
+           "cpu_baseline": {"value": value, "unit": "steps/s", "cores": res["threads"], "kind": "port",
                             "sample": sample},
-           "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "step_s": res["times"], "logdet": res["logdet"]}
     print(json.dumps(out), flush=True)
+
+
+def cpu_baseline_line(steps: int = 2, warmup: int = 1) -> dict:
+    """The cpu_baseline object of the GPU line: a bounded sample of the reference arm (two full
+    workload steps after one untimed step), run in a child process with one BLAS thread."""
+    cmd = [sys.executable, str(Path(__file__).resolve()), "--impl", "reference", "--steps", str(steps),
+           "--warmup", str(warmup), "--ref-budget", "60"]
+    env = _single_blas_env()
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        env.pop(k, None)
+    r = subprocess.run(cmd, env=env, capture_output=True, text=True)
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    if r.returncode != 0 or not line:
+        return {"value": None, "unit": "steps/s", "cores": host_threads(), "kind": "port",
+                "sample": f"reference leg failed: {r.stderr.strip()[-200:]}"}
+    ref = json.loads(line[-1])
+    cb = dict(ref["cpu_baseline"])
+    cb["sample"] = f"{ref['steps']} timed full steps after {ref['warmup']} untimed; " + cb["sample"]
+    return cb
 
 
 # ----------------------------------------------------------------------------------------------
@@ -355,10 +408,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head_prec == L.KM_PREC_FP64 else "f32x2+f64",
            "data": "synthetic",
-           "config": {"workload": WORKLOAD, "n": n, "rank": RANK, "level": "FixedLevel(8)", "nrhs": NRHS,
-                      "kernel": "matern32", "params": list(PARAMS), "precision": args.precision,
-                      "l2": "inputs larger than L2 (leaf factors alone 268 MB)",
-                      "parallelism": f"replicas{world}"},
+           "config": line_config(world), "precision": args.precision,
            "e2e": {"value": e2e_value, "unit": "steps/s",
                    "h2d_bytes_per_step": int((2 * n + n + NRHS * n) * 8),
                    "d2h_bytes_per_step": int((n + NRHS * n + 1) * 8)},
@@ -371,12 +421,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
            "accuracy": accuracy,
            "logdet": head["logdet"]}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        res = cpu_sample(16384, 6, steps=1)
-        v = 1.0 / (res["times"][0] * res["scale"])
-        out["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": host_threads(), "kind": "port",
-                               "sample": f"one n=16384 FixedLevel(6) step of the reference algorithm "
-                                         f"(oracle/, {res['times'][0]:.1f} s) scaled x{res['scale']:.2f} "
-                                         f"to the workload by flop count"}
+        out["cpu_baseline"] = cpu_baseline_line()
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist is not None:
@@ -556,6 +601,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-budget", type=float, default=900.0,
+                    help="reference arm: seconds of timed CPU work after which no further step starts")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed",
                     help="form reported as `value` (the other form is reported beside it)")
     ap.add_argument("--workload", choices=["c2", "batch", "serve", "aca"], default="c2",
@@ -569,10 +616,10 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.warmup < 3:
+    if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
-        run_reference(args, rank)
+        run_reference(args, rank, world)
     elif args.workload == "batch":
         run_batch(args)
     elif args.workload == "serve":

@@ -421,7 +421,24 @@ class KernelHODLR:
         return sum(x.shape[0] for x in self.L)
 
 
-def build_hodlr(K: KernelMatrix, ep: float, maxrank: int, lvl, nystrom: bool = False) -> KernelHODLR:
+def mapf(f, v, pool=None) -> list:
+    """``mapf(f, v, plel)`` (src/HODLR/src/utils.jl:5-8): a map over independent items, run on the
+    thread pool ``pool`` when given (the reference's ``plel = true`` with ``ThreadedEx``), else in
+    order.  NumPy releases the interpreter lock inside its LAPACK/BLAS calls, so with one BLAS
+    thread per worker (the reference's ``BLAS.set_num_threads(1)``, test/runtests.jl:9) the items
+    run concurrently.  The result of every item is the same either way."""
+    items = list(v)
+    if pool is None:
+        return [f(x) for x in items]
+    return list(pool.map(f, items))
+
+
+def foreachf(f, v, pool=None) -> None:
+    """``foreachf(f, v, plel)`` (src/HODLR/src/utils.jl:10-13)."""
+    mapf(f, v, pool)
+
+
+def build_hodlr(K: KernelMatrix, ep: float, maxrank: int, lvl, nystrom: bool = False, pool=None) -> KernelHODLR:
     """``KernelHODLR(K, ep, maxrank, lvl; nystrom)`` (src/HODLR/src/constructor.jl:6-58)."""
     n = K.shape[0]
     level, leafinds, nonleafinds = HODLRindices(n, lvl)
@@ -434,25 +451,27 @@ def build_hodlr(K: KernelMatrix, ep: float, maxrank: int, lvl, nystrom: bool = F
         lnd = K.x1[nyind]
         Spp = kernel_block(K.kid, lnd, lnd, K.parms)
         F = sla.cho_factor(Spp, lower=False, check_finite=False)
-    leaves = [K.submatrix(x).full() for x in leafinds]
+    # leaves and blocks: mapf over each list (constructor.jl:39, 47-49)
+    leaves = mapf(lambda x: K.submatrix(x).full(), leafinds, pool)
+
+    def one_block(x):
+        sub = K.submatrix(x)
+        if nystrom:
+            # nystrom_uvt (src/factorizations.jl:86-94)
+            u = kernel_block(K.kid, sub.x1, lnd, K.parms)
+            v = sla.cho_solve(F, kernel_block(K.kid, lnd, sub.x2, K.parms), check_finite=False).T
+            pv = None
+        else:
+            u, v, rr, cc = ACA(sub, ep, maxrank)
+            pv = (rr, cc)
+        return np.ascontiguousarray(u), np.ascontiguousarray(v), pv
+
     U, V, piv = [], [], []
     for j in range(level):
-        Uj, Vj, Pj = [], [], []
-        for x in nonleafinds[j]:
-            sub = K.submatrix(x)
-            if nystrom:
-                # nystrom_uvt (src/factorizations.jl:86-94)
-                u = kernel_block(K.kid, sub.x1, lnd, K.parms)
-                v = sla.cho_solve(F, kernel_block(K.kid, lnd, sub.x2, K.parms), check_finite=False).T
-                Pj.append(None)
-            else:
-                u, v, rr, cc = ACA(sub, ep, maxrank)
-                Pj.append((rr, cc))
-            Uj.append(np.ascontiguousarray(u))
-            Vj.append(np.ascontiguousarray(v))
-        U.append(Uj)
-        V.append(Vj)
-        piv.append(Pj)
+        res = mapf(one_block, nonleafinds[j], pool)
+        U.append([x[0] for x in res])
+        V.append([x[1] for x in res])
+        piv.append([x[2] for x in res])
     return KernelHODLR(ep, level, maxrank, leafinds, nonleafinds, U, V, leaves, None, nystrom, piv)
 
 
@@ -482,16 +501,15 @@ def invapply(Wvec, Uvec, Vvec) -> None:
         i0 += 2 * stepsz
 
 
-def symmetricfactorize(K: KernelHODLR) -> None:
-    """``symmetricfactorize!`` (src/HODLR/src/symfact.jl:6-49)."""
-    LW = [np.linalg.cholesky(x) for x in K.L]
-    for lv in range(len(K.U)):
-        invapply(LW, K.U[lv], K.V[lv])
+def symmetricfactorize(K: KernelHODLR, pool=None) -> None:
+    """``symmetricfactorize!`` (src/HODLR/src/symfact.jl:6-49); ``pool`` runs the reference's
+    ``plel = true`` maps (leaf factors, invapply! per level, lrsymfact per block) concurrently."""
+    LW = mapf(np.linalg.cholesky, K.L, pool)
+    foreachf(lambda lv: invapply(LW, K.U[lv], K.V[lv]), range(len(K.U)), pool)
     nonleafW: List[List[LowRankW]] = []
     for lv in range(len(K.U)):
-        nonleafW.append([lrsymfact(v, u) for v, u in zip(K.V[lv], K.U[lv])])
-        for lev in range(lv + 1, len(K.U)):
-            invapply(nonleafW[lv], K.U[lev], K.V[lev])
+        nonleafW.append(mapf(lambda vu: lrsymfact(vu[0], vu[1]), list(zip(K.V[lv], K.U[lv])), pool))
+        foreachf(lambda lev: invapply(nonleafW[lv], K.U[lev], K.V[lev]), range(lv + 1, len(K.U)), pool)
     K.W = FactorHODLR(LW, nonleafW)
     K.U = None
     K.V = None
