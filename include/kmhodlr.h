@@ -438,7 +438,8 @@ enum km_prof_class {
   KM_PROF_LEAF_APPLY = 7,  /* leaf products of the HODLR matvec                               */
   KM_PROF_OTHER = 8,       /* small kernels (logdet reduction, landmark Cholesky, ...)        */
   KM_PROF_ACA = 9,         /* adaptive cross approximation                                    */
-  KM_PROF_COUNT = 10
+  KM_PROF_LEAF_TC = 10,    /* tensor-core trailing updates of the mixed-form leaf Cholesky     */
+  KM_PROF_COUNT = 11
 };
 
 /* Enables (1) or disables (0) per-launch CUDA-event timing; enabling clears the counters. */
@@ -456,6 +457,14 @@ int km_probe_fp64_tflops(int device, double* out);
 /* Device FP32 FMA throughput in TFLOP/s (denominator for the float-pair kernels of the mixed
  * form, which run on the FP32 pipe). */
 int km_probe_fp32_tflops(int device, double* out);
+
+/* The tensor-core split product of the mixed-form leaf stage on one tile (host pointers):
+ * C = A B' for A (128 x 64) and B (64 x 64), row-major doubles, C 128 x 64 row-major.  mode 0:
+ * A and B hold integers of magnitude <= 128, passed to the tensor cores as single bf16 slices,
+ * and C is their fp32 sum (exact); mode 1: A and B are rounded to float pairs, cut into slices
+ * and multiplied as in the leaf updates.  Used to check the tensor-core data layout and the
+ * accuracy of the split product.  No reference counterpart. */
+int km_probe_tc_gemm(int device, const double* A, const double* B, int mode, double* C);
 
 #ifdef __cplusplus
 }

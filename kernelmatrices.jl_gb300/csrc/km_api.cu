@@ -76,6 +76,8 @@ struct km_handle {
   KParams kp{};
   int method = KM_METHOD_NYSTROM;
   bool mixed = false;  // float-pair factor (KM_PREC_MIXED)
+  bool leaf_tc = false;  // mixed form: leaf Cholesky and L^{-1} Phi on the tensor cores
+  double* d_lcscr = nullptr;  // slices and row exponents of the tensor-core leaf stage
   // CTAs per node of the float-pair node kernel at most (thread-block clusters on levels with
   // few nodes); 1 for handles of the batch and serving pools, whose streams fill the SMs already
   int node_cluster_max = 8;
@@ -205,6 +207,16 @@ struct km_handle {
 
 namespace km {
 // Handles of the batch and serving pools (one stream each, many at once) keep one CTA per node.
+// The mixed form runs its leaf stage on the tensor cores unless KM_LEAF_TC=0 (the float-pair
+// CUDA-core kernels, kept for comparison and for leaves above 1024 points).
+bool leaf_tc_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("KM_LEAF_TC");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 void set_node_cluster_max(km_handle* h, int v) {
   if (h) h->node_cluster_max = v < 1 ? 1 : v;
 }
@@ -292,6 +304,7 @@ void free_problem(km_handle* h) {
   h->d_pts = h->d_lnd = h->d_K = h->d_Lf = h->d_Phi = h->d_Q = h->d_tauleaf = h->d_R = nullptr;
   h->d_S = h->d_Sc = h->d_SinvT = h->d_SinvTf = h->d_Ct = h->d_L22 = h->d_Eref = h->d_Etau = nullptr;
   h->d_L22i = h->d_E = h->d_NT = nullptr;
+  h->d_lcscr = nullptr;
   h->d_lndidx = nullptr;
   h->d_info = nullptr;
   h->d_partial = h->d_scalar = nullptr;
@@ -793,6 +806,7 @@ int check_info(km_handle* h, int64_t count, const char* what) {
   std::vector<int> info(count);
   KM_CUDA(h, cudaMemcpy(info.data(), h->d_info, sizeof(int) * count, cudaMemcpyDeviceToHost));
   for (int64_t i = 0; i < count; ++i) {
+    if (info[i] < 0) return fail(h, KM_ERR_TIMEOUT, "a bounded wait of the tensor-core leaf update ran out");
     if (info[i] != 0) {
       char buf[160];
       snprintf(buf, sizeof buf, "PosDefException: %s %lld is not positive definite (pivot %d)",
@@ -1514,6 +1528,11 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
     free_problem(h);
     return rc;
   }
+  h->leaf_tc = h->mixed && leaf_tc_enabled() && leaf_chol_tc_supported(t, r);
+  if (h->leaf_tc && (rc = grow(h, &h->d_lcscr, (leaf_chol_tc_scratch_bytes(t, r) + 7) / 8)) != KM_OK) {
+    free_problem(h);
+    return rc;
+  }
   timer_start(h);
   cudaStream_t st = h->stream;
   KM_CUDA(h, cudaMemcpyAsync(h->d_pts, pts, sizeof(double) * 2 * n,
@@ -1571,16 +1590,30 @@ static int factorize_launches(km_handle* h) {
   const int r = h->r;
   cudaStream_t st = h->stream;
   KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + t.nnode), st));
-  if (!(h->mixed ? KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<ff>(h->d_K, P<ff>(h->d_Lf), t, h->d_info, st))
-                 : KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<double>(h->d_K, h->d_Lf, t, h->d_info, st))))
+  if (h->mixed && h->leaf_tc) {
+    // L_j and A_j = L_j^{-1} Phi_j from one blocked Cholesky of [K_j; Phi_j'] whose trailing
+    // updates run on the tensor cores (km_leaf_tc.cu)
+    KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Q), t.n * r, st));
+    for (int p = 0; p < leaf_chol_tc_steps(t); ++p) {
+      KLV(h, KM_PROF_LEAF_CHOL, launch_leaf_chol_tc_panel(h->d_K, P<ff>(h->d_Lf), P<ff>(h->d_Q), r, t, p, h->d_lcscr,
+                                                          h->d_info, st));
+      if (leaf_chol_tc_has_update(t, p))
+        KLV(h, KM_PROF_LEAF_TC, launch_leaf_chol_tc_update(h->d_K, P<ff>(h->d_Lf), P<ff>(h->d_Q), r, t, p,
+                                                           h->d_lcscr, h->d_info, st));
+    }
+  } else if (!(h->mixed ? KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<ff>(h->d_K, P<ff>(h->d_Lf), t, h->d_info, st))
+                        : KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<double>(h->d_K, h->d_Lf, t, h->d_info, st)))) {
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the leaf Cholesky kernel");
+  }
   // A = L^{-1} Phi on every leaf, then Householder QR of each leaf panel
   if (h->mixed) {
     // float-pair factor: every FP64-pipe-bound step runs on the FP32 pipe in float-float
-    KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Q), t.n * r, st));
-    if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<ff>(P<ff>(h->d_Lf), t, 0, P<ff>(h->d_Q), r, 0, 1, P<ff>(h->d_Q), r,
-                                                     0, 1, r, st)))
-      return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
+    if (!h->leaf_tc) {
+      KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Q), t.n * r, st));
+      if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<ff>(P<ff>(h->d_Lf), t, 0, P<ff>(h->d_Q), r, 0, 1, P<ff>(h->d_Q),
+                                                       r, 0, 1, r, st)))
+        return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
+    }
     if (t.L > 0) {
       KLV(h, KM_PROF_LEAF_QR, launch_leaf_qr<ff>(P<ff>(h->d_Q), r, t, P<ff>(h->d_tauleaf), P<ff>(h->d_R), st));
       side_begin(h);

@@ -94,6 +94,19 @@ bool launch_leaf_tri(const T* Lf, const Tree& t, int op, T* Bptr, int64_t bmul, 
                      int64_t xmul, int64_t xld, int xld_is_m, int ncols, cudaStream_t st);
 template <typename T>
 void launch_leaf_qr(T* Pan, int r, const Tree& t, T* tau, T* Rout, cudaStream_t st);
+// Mixed form on the tensor cores (km_leaf_tc.cu): blocked Cholesky of the augmented leaf matrices
+// [K_j; Phi_j'] giving Lf_j (float pairs) and A_j = L_j^{-1} Phi_j in place of G (= the float-pair
+// Phi, m x r per leaf); step p: the panel launch, then (when has_update) the tensor-core update.
+// scratch: leaf_chol_tc_scratch_bytes(t, r) bytes; info as launch_leaf_chol (-1: a bounded wait
+// of the update ran out).
+bool leaf_chol_tc_supported(const Tree& t, int r);
+int64_t leaf_chol_tc_scratch_bytes(const Tree& t, int r);
+int leaf_chol_tc_steps(const Tree& t);
+bool leaf_chol_tc_has_update(const Tree& t, int p);
+void launch_leaf_chol_tc_panel(const double* K, ff* Lf, ff* G, int r, const Tree& t, int p, void* scratch, int* info,
+                               cudaStream_t st);
+void launch_leaf_chol_tc_update(const double* K, ff* Lf, ff* G, int r, const Tree& t, int p, void* scratch,
+                                int* info, cudaStream_t st);
 void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st);
 template <typename T>
 void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T* Ct, T* L22, T* Eref, T* Etau,

@@ -29,7 +29,7 @@ KM_PREC_FP64 = 0
 KM_PREC_MIXED = 1
 
 PROF_CLASSES = ["eval", "leaf_chol", "leaf_tri", "leaf_qr", "node", "sweep", "leaf_refl", "leaf_apply",
-                "other", "aca"]
+                "other", "aca", "leaf_tc"]
 
 
 class KmConfig(C.Structure):
@@ -118,6 +118,7 @@ SIGNATURES = {
     "km_nll_grad": (C.c_int, [_H, _DP, _DP, C.c_int64, _DP, _DP]),
     "km_probe_fp64_tflops": (C.c_int, [C.c_int, _DP]),
     "km_probe_fp32_tflops": (C.c_int, [C.c_int, _DP]),
+    "km_probe_tc_gemm": (C.c_int, [C.c_int, _DP, _DP, C.c_int, _DP]),
     "km_assemble_dev": (C.c_int, [_H, _P, C.c_int64, C.c_int, _DP, C.c_int, C.c_int, C.c_double, C.c_int64,
                                   C.c_int, C.c_int64]),
     "km_set_stream": (C.c_int, [_H, _P]),
