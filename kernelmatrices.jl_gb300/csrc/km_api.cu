@@ -77,6 +77,7 @@ struct km_handle {
   int method = KM_METHOD_NYSTROM;
   bool mixed = false;  // float-pair factor (KM_PREC_MIXED)
   bool leaf_tc = false;  // mixed form: leaf Cholesky and L^{-1} Phi on the tensor cores
+  bool lf_holds_k = false;  // d_Lf holds the float-pair leaf matrices (written by the assembly)
   double* d_lcscr = nullptr;  // slices and row exponents of the tensor-core leaf stage
   // CTAs per node of the float-pair node kernel at most (thread-block clusters on levels with
   // few nodes); 1 for handles of the batch and serving pools, whose streams fill the SMs already
@@ -1477,6 +1478,7 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   if (t.nleaf > 65535) return fail(h, KM_ERR_UNSUPPORTED, "more than 65535 leaves");
   if (method == KM_METHOD_ACA) {
     if (!(tol >= 0.0) || maxrank < 0) return fail(h, KM_ERR_BAD_ARG, "ACA needs tol >= 0 and maxrank >= 0");
+    h->leaf_tc = h->lf_holds_k = false;
     return aca_assemble(h, pts, dev, t, params, kernel_id, tol, maxrank);
   }
   // Nystrom checks (src/HODLR/src/constructor.jl:26-28)
@@ -1555,7 +1557,9 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   launch_tri_inv_t(h->d_Sc, r, h->d_SinvT, h->side);
   launch_to_ff(h->d_SinvT, P<ff>(h->d_SinvTf), (int64_t)r * r, h->side);
   h->stats.kernel_launches += 4;
-  KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st, h->mixed));
+  KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st, h->mixed,
+                                          h->leaf_tc ? P<ff>(h->d_Lf) : nullptr));
+  h->lf_holds_k = h->leaf_tc;
   KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, -1, h->d_Phi, st, h->mixed));
   side_end(h);
   if ((rc = check_launch(h, "assemble")) != KM_OK) return rc;
@@ -1595,11 +1599,12 @@ static int factorize_launches(km_handle* h) {
     // updates run on the tensor cores (km_leaf_tc.cu)
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Q), t.n * r, st));
     for (int p = 0; p < leaf_chol_tc_steps(t); ++p) {
-      KLV(h, KM_PROF_LEAF_CHOL, launch_leaf_chol_tc_panel(h->d_K, P<ff>(h->d_Lf), P<ff>(h->d_Q), r, t, p, h->d_lcscr,
-                                                          h->d_info, st));
+      KLV(h, KM_PROF_LEAF_CHOL, launch_leaf_chol_tc_diag(P<ff>(h->d_Lf), r, t, p, h->d_lcscr, h->d_info, st));
+      KLV(h, KM_PROF_LEAF_TC, launch_leaf_chol_tc_trsm(P<ff>(h->d_Lf), P<ff>(h->d_Q), r, t, p, h->d_lcscr,
+                                                       h->d_info, st));
       if (leaf_chol_tc_has_update(t, p))
-        KLV(h, KM_PROF_LEAF_TC, launch_leaf_chol_tc_update(h->d_K, P<ff>(h->d_Lf), P<ff>(h->d_Q), r, t, p,
-                                                           h->d_lcscr, h->d_info, st));
+        KLV(h, KM_PROF_LEAF_TC, launch_leaf_chol_tc_update(P<ff>(h->d_Lf), P<ff>(h->d_Q), r, t, p, h->d_lcscr,
+                                                           h->d_info, st));
     }
   } else if (!(h->mixed ? KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<ff>(h->d_K, P<ff>(h->d_Lf), t, h->d_info, st))
                         : KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<double>(h->d_K, h->d_Lf, t, h->d_info, st)))) {
@@ -1671,6 +1676,12 @@ int km_factorize(km_handle* h) {
   cudaStream_t st = h->stream;
   int rc;
   timer_start(h);
+  if (h->mixed && h->leaf_tc && !h->lf_holds_k) {
+    // a second factorisation of the same assembly: the leaf matrices evaluated again (the same
+    // kernel on the same points, so the same float pairs and FP64 values as the assembly's)
+    KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st, true, P<ff>(h->d_Lf)));
+  }
+  h->lf_holds_k = false;
   const int64_t fk[5] = {(int64_t)h->alloc_epoch, t.n, t.L, r, h->mixed ? 1 : 0};
   rc = run_graphed(h, &h->fgraph, h->fkey, fk, [&]() -> int { return factorize_launches(h); });
   if (rc != KM_OK) return rc;
@@ -2280,6 +2291,8 @@ extern "C" int64_t km_estimate_bytes(int64_t n, int64_t rank, int level_kind, in
               4 * std::max<int64_t>(t.nleaf + t.nnode + 1, 1) + d(kLogdetBlocks) + d(4);
   b += 2 * d(slots * r * k) + d(nn * 2 * r * k);  // ensure_vec
   b += 2 * d(n * k);                              // ensure_xy
+  if (leaf_tc_enabled() && leaf_chol_tc_supported(t, (int)r))  // slices of the tensor-core leaf stage
+    b += leaf_chol_tc_scratch_bytes(t, (int)r);
   if (with_grad)  // derivative workspaces, plus the float-pair copies the mixed form keeps
     b += d(kb) + d(n * r) + d(r * r) + 2 * d(slots * 2 * r * k) + 2 * d(n * k) + d(k) + d(kb) + 2 * d(n * r) +
          5 * d(r * r) + d(t.nleaf * 2 * r * k);

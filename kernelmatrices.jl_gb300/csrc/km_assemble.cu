@@ -43,8 +43,9 @@ __device__ __forceinline__ ff ff_exp_neg(ff z) {
   return ff(p.hi * sc, p.lo * sc);
 }
 
-// kernel_value (km_internal.h) in float pairs; the same formulas and special cases.
-__device__ __forceinline__ double kernel_value_ff(const KParams& kp, double x1, double y1, double x2, double y2) {
+// kernel_value (km_internal.h) in float pairs, without the nugget; the same formulas and
+// special cases.
+__device__ __forceinline__ ff kernel_value_ffv(const KParams& kp, double x1, double y1, double x2, double y2) {
   const ff dx(__dsub_rn(x1, x2)), dy(__dsub_rn(y1, y2));
   const ff r = sqrt(ff(dx * dx) + dy * dy);
   ff out;
@@ -62,7 +63,11 @@ __device__ __forceinline__ double kernel_value_ff(const KParams& kp, double x1, 
       }
     }
   }
-  double v = to_double(out);
+  return out;
+}
+
+__device__ __forceinline__ double kernel_value_ff(const KParams& kp, double x1, double y1, double x2, double y2) {
+  double v = to_double(kernel_value_ffv(kp, x1, y1, x2, y2));
   if (x1 == x2 && y1 == y2) v = __dadd_rn(v, kp.p2);
   return v;
 }
@@ -110,9 +115,12 @@ __device__ __forceinline__ double eval_entry(bool use_ff, const KParams& kp, int
 
 // One 32x32 tile of one leaf per CTA; only lower-triangle tiles are evaluated and each is
 // written twice (the kernel is symmetric bit for bit: |x-y| and x == y are symmetric).
+// Kff (the kernel itself in float pairs, may be null): the entries of the evaluated tiles
+// (every lower-triangle entry) also as float pairs, for the tensor-core leaf factorisation;
+// the same kernel on the same points always gives the same pairs.
 // grid = (ntile, ntile, nleaf), block = (32, 8).
 __global__ void k_eval_leaves(const double* __restrict__ pts, DTree t, KParams kp, int deriv, bool use_ff,
-                              double* __restrict__ K) {
+                              double* __restrict__ K, ff* __restrict__ Kff) {
   const int ti = blockIdx.x, tj = blockIdx.y;
   if (ti < tj) return;
   const int64_t leaf = blockIdx.z;
@@ -139,7 +147,19 @@ __global__ void k_eval_leaves(const double* __restrict__ pts, DTree t, KParams k
     const int jl = ty + 8 * q;
     const int j = tj * 32 + jl;
     if (i < m && j < m) {
-      const double v = eval_entry(use_ff, kp, deriv, px[0][tx], py[0][tx], px[1][jl], py[1][jl]);
+      double v;
+      if (Kff) {
+        const double x1 = px[0][tx], y1 = py[0][tx], x2 = px[1][jl], y2 = py[1][jl];
+        ff f = kernel_value_ffv(kp, x1, y1, x2, y2);
+        v = to_double(f);
+        if (x1 == x2 && y1 == y2) {  // the diagonal: the FP64 sum with the nugget, rounded to a pair
+          v = __dadd_rn(v, kp.p2);
+          f = ff(v);
+        }
+        Kff[d_leaf_koff(t, leaf) + (int64_t)j * m + i] = f;
+      } else {
+        v = eval_entry(use_ff, kp, deriv, px[0][tx], py[0][tx], px[1][jl], py[1][jl]);
+      }
       A[(int64_t)j * m + i] = v;
       tile[tx][jl] = v;
     }
@@ -193,10 +213,11 @@ __global__ void k_gather_points(const double* __restrict__ pts, const int64_t* _
 }
 
 void launch_eval_leaves(const double* pts, const Tree& t, KParams kp, int deriv, double* K,
-                        cudaStream_t st, bool use_ff) {
+                        cudaStream_t st, bool use_ff, ff* Kff) {
   const int nt = (int)((t.max_leaf + 31) / 32);
   dim3 grid(nt, nt, (unsigned)t.nleaf), block(32, 8);
-  k_eval_leaves<<<grid, block, 0, st>>>(pts, dtree(t), kp, deriv, use_ff, K);
+  k_eval_leaves<<<grid, block, 0, st>>>(pts, dtree(t), kp, deriv, use_ff, K,
+                                        (use_ff && deriv < 0) ? Kff : nullptr);
 }
 
 void launch_eval_phi(const double* pts, const double* lnd, int r, const Tree& t, KParams kp,

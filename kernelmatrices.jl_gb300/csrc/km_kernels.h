@@ -76,8 +76,9 @@ struct NodeMatsH {          // node factors (double or float pairs, by the calle
 
 // assembly
 // use_ff: float-pair evaluation on the FP32 pipe (mixed form, ~1e-14 relative), else FP64
+// Kff: also the float-pair entries of the kernel itself (mixed form, deriv < 0), lower triangle
 void launch_eval_leaves(const double* pts, const Tree& t, KParams kp, int deriv, double* K,
-                        cudaStream_t st, bool use_ff = false);
+                        cudaStream_t st, bool use_ff = false, ff* Kff = nullptr);
 void launch_eval_phi(const double* pts, const double* lnd, int r, const Tree& t, KParams kp,
                      int deriv, double* Phi, cudaStream_t st, bool use_ff = false);
 void launch_eval_dense(const double* a, int na, const double* b, int nb, KParams kp, int deriv,
@@ -96,17 +97,19 @@ template <typename T>
 void launch_leaf_qr(T* Pan, int r, const Tree& t, T* tau, T* Rout, cudaStream_t st);
 // Mixed form on the tensor cores (km_leaf_tc.cu): blocked Cholesky of the augmented leaf matrices
 // [K_j; Phi_j'] giving Lf_j (float pairs) and A_j = L_j^{-1} Phi_j in place of G (= the float-pair
-// Phi, m x r per leaf); step p: the panel launch, then (when has_update) the tensor-core update.
-// scratch: leaf_chol_tc_scratch_bytes(t, r) bytes; info as launch_leaf_chol (-1: a bounded wait
-// of the update ran out).
+// Phi, m x r per leaf).  Lf holds the float-pair leaf matrices (lower triangles) on entry.  Step
+// p: the diagonal-block launch, the block-column launch, then (when has_update) the trailing
+// update.  scratch: leaf_chol_tc_scratch_bytes(t, r) bytes; info as launch_leaf_chol (-1: a
+// bounded wait of a tensor-core launch ran out).
 bool leaf_chol_tc_supported(const Tree& t, int r);
 int64_t leaf_chol_tc_scratch_bytes(const Tree& t, int r);
 int leaf_chol_tc_steps(const Tree& t);
 bool leaf_chol_tc_has_update(const Tree& t, int p);
-void launch_leaf_chol_tc_panel(const double* K, ff* Lf, ff* G, int r, const Tree& t, int p, void* scratch, int* info,
-                               cudaStream_t st);
-void launch_leaf_chol_tc_update(const double* K, ff* Lf, ff* G, int r, const Tree& t, int p, void* scratch,
-                                int* info, cudaStream_t st);
+void launch_leaf_chol_tc_diag(ff* Lf, int r, const Tree& t, int p, void* scratch, int* info, cudaStream_t st);
+void launch_leaf_chol_tc_trsm(ff* Lf, ff* G, int r, const Tree& t, int p, void* scratch, int* info,
+                              cudaStream_t st);
+void launch_leaf_chol_tc_update(ff* Lf, ff* G, int r, const Tree& t, int p, void* scratch, int* info,
+                                cudaStream_t st);
 void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st);
 template <typename T>
 void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T* Ct, T* L22, T* Eref, T* Etau,

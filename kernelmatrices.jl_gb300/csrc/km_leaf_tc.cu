@@ -10,15 +10,20 @@
 // the panel buffer.
 //
 // Per 64-column block (step) of every leaf:
-//   * k_lc_panel (CUDA cores, one CTA per leaf): Cholesky of the 64 x 64 diagonal block, then
-//     the block column below it by forward substitution x D' = a per row (float pairs, Dot2
-//     sums), written back, and every row of the block column cut into kSlices bf16 slices with
-//     a row exponent (km_tc.cuh) in the tensor cores' shared-memory layout;
+//   * k_lc_diag (CUDA cores, one CTA per leaf): Cholesky D of the 64 x 64 diagonal block and,
+//     in the same column sweep, X = D^{-1} (float pairs, shared memory); the rows of X cut into
+//     bf16 slices for the next kernel;
+//   * k_lc_trsm (tensor cores, one CTA per 128-row tile of the rows below the block: trailing
+//     rows of K_j, then the rows of Phi_j'): the block column P = A X' (the triangular solve
+//     P D' = A with the explicit inverse of the diagonal block) as a split product, written back
+//     and cut into slices (with row exponents) for the update;
 //   * k_lc_update (tensor cores, one CTA per 128 x 64 tile of the trailing rows / columns):
-//     C -= P P' from the slices: the 28 slice products with i + j <= 6 accumulate per diagonal
-//     i + j in tensor memory (exact integer sums in fp32), and the epilogue adds the 7 diagonal
-//     sums in float pairs, scales by 2^(e_row + e_col) and subtracts from C.
-// The first step reads the FP64 leaf matrix K_j directly (conversion to float pairs on load).
+//     C -= P P' from the slices.
+// A float-pair value is cut into kSlices bf16 slices with a row exponent (km_tc.cuh); both
+// products take the 28 slice products with i + j <= 6, accumulated per diagonal i + j in tensor
+// memory (exact integer sums in fp32), and the epilogues add the 7 diagonal sums in float pairs
+// and scale them by 2^(e_row + e_col).  The leaf matrices enter in float pairs (written by the
+// mixed-form leaf evaluation).
 #include "km_kernels.h"
 #include "km_tc.cuh"
 
@@ -26,11 +31,13 @@ namespace km {
 
 using tc::kSlices;
 
-constexpr int kLcNB = 64;            // panel width = K of the update products
-constexpr int kLcTileM = 128;        // rows of an update tile (MMA M)
-constexpr int kLcTileN = 64;         // columns of an update tile (MMA N)
-constexpr int kLcPanelThreads = 128;
-constexpr int kLcUpdThreads = 256;   // 8 warps: warp w reads tensor-memory lanes 32 (w % 4) ..
+constexpr int kLcNB = 64;              // panel width = K of the products
+constexpr int kLcTileM = 128;          // rows of a tile (MMA M)
+constexpr int kLcTileN = 64;           // columns of a tile (MMA N)
+constexpr int kLcTcThreads = 512;      // 16 warps: warp w reads tensor-memory lanes 32 (w % 4) .. + 31,
+                                       // columns 16 (w / 4) .. + 15 of a tile
+constexpr int kLcDiagThreads = 256;
+constexpr int kLcProbeThreads = 256;
 constexpr uint32_t kLcTmemCols = 512;  // kSlices x kLcTileN = 448 accumulator columns
 constexpr uint32_t kATileBytes = kLcTileM * kLcNB * 2;  // one slice of a 128-row tile
 constexpr uint32_t kBTileBytes = kLcTileN * kLcNB * 2;  // one slice of a 64-row tile
@@ -40,9 +47,9 @@ constexpr int kLcMaxRank = 256;
 
 __host__ __device__ inline int64_t lc_rows_padded(int64_t rows) { return (rows + 127) / 128 * 128; }
 
-// bf16 element index of (slice s, row rho, column c) in the slice array of one leaf and step:
-// core matrix (rho / 8, c / 8) of slice s is 64 consecutive elements, core matrices ordered by
-// slice, then row group, then column group; rp = padded rows of the step.
+// bf16 element index of (slice s, row rho, column c) in a slice array of rp rows: core matrix
+// (rho / 8, c / 8) of slice s is 64 consecutive elements, core matrices ordered by slice, then
+// row group, then column group.
 __host__ __device__ inline int64_t lc_slice_index(int s, int64_t rp, int64_t rho, int c) {
   return ((((int64_t)s * (rp / 8) + rho / 8) * 8 + c / 8) * 64) + (rho % 8) * 8 + (c % 8);
 }
@@ -61,112 +68,12 @@ __device__ __forceinline__ void store_slices8(uint16_t* base, int64_t rp, int64_
   }
 #pragma unroll
   for (int s = 0; s < kSlices; ++s)
-    *reinterpret_cast<uint4*>(base + lc_slice_index(s, rp, rho, 8 * kc)) = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+    *reinterpret_cast<uint4*>(base + lc_slice_index(s, rp, rho, 8 * kc)) =
+        make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
 }
 
-// ---------------------------------------------------------------------------------------------
-// Panel step: grid = nleaf, block = kLcPanelThreads.
-// ---------------------------------------------------------------------------------------------
-template <bool FROM_K>
-__global__ void __launch_bounds__(kLcPanelThreads) k_lc_panel(const double* __restrict__ K, ff* __restrict__ Lf,
-                                                              ff* __restrict__ G, int r, DTree t, int c0,
-                                                              uint16_t* __restrict__ slices, int* __restrict__ rexp,
-                                                              int64_t slice_stride, int64_t exp_stride,
-                                                              int* __restrict__ info) {
-  extern __shared__ __align__(16) unsigned char lc_smem_p[];
-  constexpr int LD = kLcNB + 1;
-  ff* D = reinterpret_cast<ff*>(lc_smem_p);  // kLcNB x LD, D[i * LD + c]
-  ff* xs = D + kLcNB * LD;               // kLcNB x NT, xs[c * NT + tid]
-  __shared__ ff dinv[kLcNB];
-  __shared__ int sbad;
-  const int64_t leaf = blockIdx.x;
-  const int m = d_leaf_size(t, leaf);
-  if (c0 >= m) return;
-  const int nb = min(kLcNB, m - c0);
-  const int64_t koff = d_leaf_koff(t, leaf);
-  const int64_t qoff = d_leaf_start(t, leaf) * r;
-  const int T = m - c0 - nb;  // trailing rows of K_j
-  const int R = T + r;        // rows below the block: trailing K rows, then the r rows of Phi'
-  const int64_t RP = lc_rows_padded(R);
-  uint16_t* sl = slices + leaf * slice_stride;
-  int* ex = rexp + leaf * exp_stride;
-  const int tid = threadIdx.x, NT = blockDim.x;
-  auto src = [&](int row, int col) -> ff {  // lower-triangle entry of the matrix being factored
-    const int64_t o = koff + (int64_t)col * m + row;
-    if (FROM_K) return ff(K[o]);
-    return Lf[o];
-  };
-  // (1) diagonal block: unblocked Cholesky in shared memory
-  for (int e = tid; e < nb * nb; e += NT) {
-    const int i = e % nb, c = e / nb;
-    if (i >= c) D[i * LD + c] = src(c0 + i, c0 + c);
-  }
-  if (tid == 0) sbad = 0;
-  __syncthreads();
-  for (int j = 0; j < nb; ++j) {
-    const ff d = D[j * LD + j];
-    const bool ok = d > 0.0;
-    const ff sd = ok ? sqrt(d) : ff(1.0);
-    if (!ok && tid == 0 && sbad == 0) sbad = c0 + j + 1;
-    __syncthreads();
-    for (int i = j + 1 + tid; i < nb; i += NT) D[i * LD + j] /= sd;
-    if (tid == 0) D[j * LD + j] = sd;
-    __syncthreads();
-    const int w = nb - j - 1;
-    for (int e = tid; e < w * w; e += NT) {
-      const int i = j + 1 + e % w, c = j + 1 + e / w;
-      if (i >= c) D[i * LD + c] -= D[i * LD + j] * D[c * LD + j];
-    }
-    __syncthreads();
-  }
-  for (int c = tid; c < nb; c += NT) dinv[c] = ff(1.0) / D[c * LD + c];
-  for (int e = tid; e < nb * nb; e += NT) {
-    const int i = e % nb, c = e / nb;
-    if (i >= c) Lf[koff + (int64_t)(c0 + c) * m + c0 + i] = D[i * LD + c];
-  }
-  if (tid == 0 && sbad != 0 && info[leaf] == 0) info[leaf] = sbad;
-  __syncthreads();
-  // (2) rows below: x D' = a, one row per thread; then the row's slices
-  for (int64_t base = 0; base < RP; base += NT) {
-    const int64_t rho = base + tid;
-    const bool valid = rho < R;
-    float amax = 0.f;
-    if (valid) {
-      for (int c = 0; c < nb; ++c) {
-        const ff a = rho < T ? src(c0 + nb + (int)rho, c0 + c) : G[qoff + (rho - T) * m + c0 + c];
-        acc_t<ff> acc(a);
-        for (int k = 0; k < c; ++k) acc -= xs[k * NT + tid] * D[c * LD + k];
-        const ff x = accv(acc) * dinv[c];
-        xs[c * NT + tid] = x;
-        amax = fmaxf(amax, fabsf(x.hi));
-      }
-      for (int c = 0; c < nb; ++c) {
-        const ff x = xs[c * NT + tid];
-        if (rho < T)
-          Lf[koff + (int64_t)(c0 + c) * m + c0 + nb + rho] = x;
-        else
-          G[qoff + (rho - T) * m + c0 + c] = x;
-      }
-    }
-    const int e = tc::row_exponent(amax);
-    ex[rho] = e;
-#pragma unroll 1
-    for (int kc = 0; kc < kLcNB / 8; ++kc) {
-      ff x[8];
-#pragma unroll
-      for (int cc = 0; cc < 8; ++cc) {
-        const int c = 8 * kc + cc;
-        x[cc] = (valid && c < nb) ? xs[c * NT + tid] : ff(0.0);
-      }
-      store_slices8(sl, RP, rho, kc, x, e);
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------------------------
-// Trailing update step: grid = (nleaf, row tiles, column tiles), block = kLcUpdThreads.
-// Shared memory: kSlices A slices (kATileBytes each), then kSlices B slices (kBTileBytes each).
-// ---------------------------------------------------------------------------------------------
+// Split products of one 128 x 64 tile: A slices (kSlices x kATileBytes) times B slices
+// (kSlices x kBTileBytes) into kSlices accumulators of kLcTileN columns, one per diagonal i + j.
 __device__ __forceinline__ void lc_issue_products(uint32_t tmem, uint32_t smA, uint32_t smB) {
   constexpr uint32_t idesc = tc::idesc_bf16(kLcTileM, kLcTileN);
 #pragma unroll 1
@@ -186,12 +93,287 @@ __device__ __forceinline__ void lc_issue_products(uint32_t tmem, uint32_t smA, u
   }
 }
 
-template <bool FROM_K>
-__global__ void __launch_bounds__(kLcUpdThreads, 1) k_lc_update(const double* __restrict__ K, ff* __restrict__ Lf,
-                                                                ff* __restrict__ G, int r, DTree t, int c0,
-                                                                const uint16_t* __restrict__ slices,
-                                                                const int* __restrict__ rexp, int64_t slice_stride,
-                                                                int64_t exp_stride, int* __restrict__ info) {
+// The 8 float-pair values of accumulator columns j0 .. j0 + 7 of this thread's lane: the 7
+// diagonal sums combined and scaled by 2^(erow + ecol[jj]).
+__device__ __forceinline__ void lc_tile_values(uint32_t tl, int j0, int erow, const int* ecol, ff (&out)[8]) {
+  float s[kSlices][8];
+#pragma unroll
+  for (int d = 0; d < kSlices; ++d) tc::tmem_ld8(tl + d * kLcTileN + j0, s[d]);
+  tc::tmem_wait_ld();
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) {
+    float sd[kSlices];
+#pragma unroll
+    for (int d = 0; d < kSlices; ++d) sd[d] = s[d][jj];
+    out[jj] = tc::ff_ldexp(tc::combine_diagonals(sd), erow + ecol[jj]);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Diagonal block: grid = nleaf, block = kLcDiagThreads, dynamic shared memory 2 x 64 x 65 float
+// pairs.  D = chol(B) and X = D^{-1} for the block B = rows / columns [c0, c0 + nb) of the
+// matrix being factored (row j of X is finalised at step j, then rows i > j subtract L_ij X_j);
+// beyond nb both are the identity.  Writes D to Lf and the slices of the rows of X (64 rows,
+// the canonical layout) with their exponents.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kLcDiagThreads) k_lc_diag(ff* __restrict__ Lf, DTree t, int c0,
+                                                            uint16_t* __restrict__ xsl, int* __restrict__ xexp,
+                                                            int* __restrict__ info) {
+  extern __shared__ __align__(16) unsigned char lc_smem_d[];
+  constexpr int LD = kLcNB + 1;
+  ff* D = reinterpret_cast<ff*>(lc_smem_d);
+  ff* X = D + kLcNB * LD;
+  __shared__ int sbad;
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  if (c0 >= m) return;
+  const int nb = min(kLcNB, m - c0);
+  const int64_t koff = d_leaf_koff(t, leaf);
+  const int tid = threadIdx.x, NT = blockDim.x;
+  for (int e = tid; e < kLcNB * kLcNB; e += NT) {
+    const int i = e % kLcNB, c = e / kLcNB;
+    ff v(0.0);
+    if (i < nb && c < nb) {
+      if (i >= c) v = Lf[koff + (int64_t)(c0 + c) * m + c0 + i];
+    } else if (i == c) {
+      v = ff(1.0);
+    }
+    D[i * LD + c] = v;
+    X[i * LD + c] = ff(i == c ? 1.0 : 0.0);
+  }
+  if (tid == 0) sbad = 0;
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    const ff d = D[j * LD + j];
+    const bool ok = d > 0.0;
+    const ff sd = ok ? sqrt(d) : ff(1.0);
+    const ff rinv = ff(1.0) / sd;
+    if (!ok && tid == 0 && sbad == 0) sbad = c0 + j + 1;
+    __syncthreads();
+    for (int i = j + 1 + tid; i < nb; i += NT) D[i * LD + j] = ff(D[i * LD + j] * rinv);
+    for (int c = tid; c <= j; c += NT) X[j * LD + c] = ff(X[j * LD + c] * rinv);
+    if (tid == 0) D[j * LD + j] = sd;
+    __syncthreads();
+    // trailing lower triangle of D (i >= c > j) and rows i > j of X (columns c <= j)
+    const int wr = nb - j - 1;
+    const int nd = wr * (wr + 1) / 2, nx = wr * (j + 1);
+    for (int e = tid; e < nd + nx; e += NT) {
+      if (e < nd) {
+        int a = (int)((sqrtf(8.f * (float)e + 1.f) - 1.f) * 0.5f);  // e = a (a + 1) / 2 + b, b <= a
+        if ((a + 1) * (a + 2) / 2 <= e) ++a;
+        if (a * (a + 1) / 2 > e) --a;
+        const int i = j + 1 + a, c = j + 1 + (e - a * (a + 1) / 2);
+        D[i * LD + c] -= D[i * LD + j] * D[c * LD + j];
+      } else {
+        const int q = e - nd;
+        const int i = j + 1 + q % wr, c = q / wr;
+        X[i * LD + c] -= D[i * LD + j] * X[j * LD + c];
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < nb * nb; e += NT) {
+    const int i = e % nb, c = e / nb;
+    if (i >= c) Lf[koff + (int64_t)(c0 + c) * m + c0 + i] = D[i * LD + c];
+  }
+  if (tid == 0 && sbad != 0 && info[leaf] == 0) info[leaf] = sbad;
+  // rows of X: four threads per row, 16 columns each
+  uint16_t* dst = xsl + leaf * (int64_t)(kSlices * kLcNB * kLcNB);
+  for (int rr = tid >> 2; rr < kLcNB; rr += NT >> 2) {
+    const int qq = tid & 3;
+    float amax = 0.f;
+    ff xv[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      xv[k] = X[rr * LD + 16 * qq + k];
+      amax = fmaxf(amax, fabsf(xv[k].hi));
+    }
+    amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, 1));
+    amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, 2));
+    const int e = tc::row_exponent(amax);
+    if (qq == 0) xexp[leaf * kLcNB + rr] = e;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      ff xg[8];
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) xg[cc] = xv[8 * g + cc];
+      store_slices8(dst, kLcNB, rr, 2 * qq + g, xg, e);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Block column below the diagonal block: grid = (nleaf, row tiles), block = kLcTcThreads,
+// dynamic shared memory kSlices x (kATileBytes + kBTileBytes).  Rows [128 rt, 128 rt + 128) of
+// the rows below (trailing rows of K_j, then the r rows of Phi_j', then zero padding up to RP).
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kLcTcThreads, 1) k_lc_trsm(ff* __restrict__ Lf, ff* __restrict__ G, int r,
+                                                             DTree t, int c0, const uint16_t* __restrict__ xsl,
+                                                             const int* __restrict__ xexp,
+                                                             uint16_t* __restrict__ slices, int* __restrict__ rexp,
+                                                             int64_t slice_stride, int64_t exp_stride,
+                                                             int* __restrict__ info) {
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  constexpr int LD = kLcNB + 1;
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t tslot;
+  __shared__ int serr;
+  __shared__ int bexp[kLcNB];
+  __shared__ int aexp[kLcTileM];
+  const int64_t leaf = blockIdx.x;
+  const int rt = blockIdx.y;
+  const int m = d_leaf_size(t, leaf);
+  if (c0 >= m) return;
+  const int nb = min(kLcNB, m - c0);
+  const int T = m - c0 - nb;
+  const int R = T + r;
+  const int64_t RP = lc_rows_padded(R);
+  if ((int64_t)kLcTileM * rt >= RP) return;
+  const int64_t koff = d_leaf_koff(t, leaf);
+  const int64_t qoff = d_leaf_start(t, leaf) * r;
+  uint16_t* sl = slices + leaf * slice_stride;
+  int* ex = rexp + leaf * exp_stride;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  uint16_t* sA = reinterpret_cast<uint16_t*>(smraw);
+  uint16_t* sB = sA + kSlices * kATileBytes / 2;
+  ff* Pst = reinterpret_cast<ff*>(smraw);  // after the products: P, kLcTileM x LD
+  const uint32_t smA = tc::smem_u32(sA), smB = tc::smem_u32(sB);
+
+  if (tid == 0) {
+    tc::mbar_init(&bar[0], 1);
+    tc::mbar_init(&bar[1], 1);
+    tc::mbar_fence_init();
+    serr = 0;
+  }
+  if (w == 0) {
+    tc::tmem_alloc(&tslot, kLcTmemCols);
+    tc::tmem_relinquish();
+  }
+  if (tid < kLcNB) bexp[tid] = xexp[leaf * kLcNB + tid];
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = tslot;
+  if (tid == 0) {
+    tc::mbar_arrive_expect_tx(&bar[0], kSlices * kBTileBytes);
+    const uint16_t* xs = xsl + leaf * (int64_t)(kSlices * kLcNB * kLcNB);
+    for (int s = 0; s < kSlices; ++s)
+      tc::bulk_g2s(reinterpret_cast<unsigned char*>(sB) + s * kBTileBytes, xs + (int64_t)s * kLcNB * kLcNB,
+                   kBTileBytes, &bar[0]);
+  }
+  // A slices: four threads per row, 16 columns each
+  const int i4 = tid >> 2, qq = tid & 3;
+  const int64_t rho4 = (int64_t)kLcTileM * rt + i4;
+  const bool valid4 = rho4 < R;
+  {
+    ff a[16];
+    float amax = 0.f;
+#pragma unroll
+    for (int cc = 0; cc < 16; ++cc) {
+      const int c = 16 * qq + cc;
+      ff v(0.0);
+      if (valid4 && c < nb)
+        v = rho4 < T ? Lf[koff + (int64_t)(c0 + c) * m + c0 + nb + rho4] : G[qoff + (rho4 - T) * m + c0 + c];
+      a[cc] = v;
+      amax = fmaxf(amax, fabsf(v.hi));
+    }
+    amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, 1));
+    amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, 2));
+    const int e = tc::row_exponent(amax);
+    if (qq == 0) aexp[i4] = e;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      ff xg[8];
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) xg[cc] = a[8 * g + cc];
+      store_slices8(sA, kLcTileM, i4, 2 * qq + g, xg, e);
+    }
+  }
+  tc::fence_proxy_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  if (tid == 0) {
+    if (tc::mbar_wait(&bar[0], 0, kTcWaitLimit)) {
+      tc::tc_fence_after();
+      lc_issue_products(tmem, smA, smB);
+    } else {
+      serr = 1;
+    }
+    tc::mma_commit(&bar[1]);
+  }
+  __syncwarp();
+  if (!tc::mbar_wait(&bar[1], 0, kTcWaitLimit)) atomicExch(&serr, 1);
+  tc::tc_fence_after();
+  __syncthreads();  // serr is the same in every thread from here on
+  if (serr) {
+    if (tid == 0) {
+      tc::mbar_wait(&bar[0], 0, kTcWaitLimit);  // copies still in flight land before the exit
+      info[leaf] = -1;
+    }
+  } else {
+    // P = A X' into shared memory (over the A slices, which the products have read)
+    const int q = w & 3, h = w >> 2;
+    const int i = 32 * q + lane;
+    const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16);
+#pragma unroll 1
+    for (int cc = 0; cc < 2; ++cc) {
+      const int j0 = 16 * h + 8 * cc;
+      ff pv[8];
+      lc_tile_values(tl, j0, aexp[i], bexp + j0, pv);
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) Pst[i * LD + j0 + jj] = pv[jj];
+    }
+    __syncthreads();
+    // P back to Lf / G, its row exponent and slices for the update step
+    ff pv[16];
+    float amax = 0.f;
+#pragma unroll
+    for (int cc = 0; cc < 16; ++cc) {
+      const int c = 16 * qq + cc;
+      const ff v = (valid4 && c < nb) ? Pst[i4 * LD + c] : ff(0.0);
+      pv[cc] = v;
+      amax = fmaxf(amax, fabsf(v.hi));
+    }
+    if (valid4) {
+#pragma unroll
+      for (int cc = 0; cc < 16; ++cc) {
+        const int c = 16 * qq + cc;
+        if (c < nb) {
+          if (rho4 < T)
+            Lf[koff + (int64_t)(c0 + c) * m + c0 + nb + rho4] = pv[cc];
+          else
+            G[qoff + (rho4 - T) * m + c0 + c] = pv[cc];
+        }
+      }
+    }
+    amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, 1));
+    amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, 2));
+    const int e = tc::row_exponent(amax);
+    if (qq == 0) ex[rho4] = e;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      ff xg[8];
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) xg[cc] = pv[8 * g + cc];
+      store_slices8(sl, RP, rho4, 2 * qq + g, xg, e);
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (w == 0) tc::tmem_dealloc(tmem, kLcTmemCols);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Trailing update step: grid = (nleaf, row tiles, column tiles), block = kLcTcThreads.
+// Shared memory: kSlices A slices (kATileBytes each), then kSlices B slices (kBTileBytes each).
+// A thread updates 16 entries of C (tile row 32 (w % 4) + lane, columns 16 (w / 4) .. + 15),
+// loading the first eight while the products run and the next eight one chunk ahead.
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kLcTcThreads, 1) k_lc_update(ff* __restrict__ Lf, ff* __restrict__ G, int r,
+                                                               DTree t, int c0, const uint16_t* __restrict__ slices,
+                                                               const int* __restrict__ rexp, int64_t slice_stride,
+                                                               int64_t exp_stride, int* __restrict__ info) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ uint32_t tslot;
@@ -243,6 +425,23 @@ __global__ void __launch_bounds__(kLcUpdThreads, 1) k_lc_update(const double* __
       tc::bulk_g2s(smraw + kSlices * kATileBytes + s * kBTileBytes,
                    sl + lc_slice_index(s, RP, (int64_t)kLcTileN * ct, 0), kBTileBytes, &bar[0]);
     }
+  }
+  const int q = w & 3, h = w >> 2;
+  const int64_t rho = (int64_t)kLcTileM * rt + 32 * q + lane;
+  const bool rvalid = rho < R;
+  const int erow = rvalid ? ex[rho] : 0;
+  auto c_index = [&](int j) -> int64_t {  // -1: not updated by this thread
+    if (!rvalid || j >= T || (rho < T && rho < j)) return -1;
+    return rho < T ? koff + (int64_t)(c0 + nb + j) * m + c0 + nb + rho : qoff + (rho - T) * m + c0 + nb + j;
+  };
+  auto c_load = [&](int64_t o) -> ff {
+    if (o < 0) return ff(0.0);
+    return rho < T ? Lf[o] : G[o];
+  };
+  ff cbuf[8];
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) cbuf[jj] = c_load(c_index(kLcTileN * ct + 16 * h + jj));
+  if (tid == 0) {
     if (tc::mbar_wait(&bar[0], 0, kTcWaitLimit)) {
       tc::tc_fence_after();
       lc_issue_products(tmem, smA, smB);
@@ -252,46 +451,36 @@ __global__ void __launch_bounds__(kLcUpdThreads, 1) k_lc_update(const double* __
     tc::mma_commit(&bar[1]);
   }
   __syncwarp();
-  const bool done = tc::mbar_wait(&bar[1], 0, kTcWaitLimit);
+  if (!tc::mbar_wait(&bar[1], 0, kTcWaitLimit)) atomicExch(&serr, 1);
   tc::tc_fence_after();
-  __syncthreads();
-  if (!done || serr) {
+  __syncthreads();  // serr is the same in every thread from here on
+  if (serr) {
     if (tid == 0) {
       tc::mbar_wait(&bar[0], 0, kTcWaitLimit);  // copies still in flight land before the exit
       info[leaf] = -1;
     }
   } else {
-    // epilogue: warp w reads lanes 32 (w % 4) + lane = tile row, columns 32 (w / 4) .. + 31
-    const int q = w & 3, h = w >> 2;
-    const int64_t rho = (int64_t)kLcTileM * rt + 32 * q + lane;
-    const bool rvalid = rho < R;
-    const int erow = rvalid ? ex[rho] : 0;
     const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16);
 #pragma unroll 1
-    for (int cc = 0; cc < 4; ++cc) {
-      const int j0 = 32 * h + 8 * cc;
-      float s[kSlices][8];
+    for (int cc = 0; cc < 2; ++cc) {
+      const int j0 = 16 * h + 8 * cc;
+      ff nbuf[8];
 #pragma unroll
-      for (int d = 0; d < kSlices; ++d) tc::tmem_ld8(tl + d * kLcTileN + j0, s[d]);
-      tc::tmem_wait_ld();
-      if (!rvalid) continue;
+      for (int jj = 0; jj < 8; ++jj) nbuf[jj] = cc == 0 ? c_load(c_index(kLcTileN * ct + j0 + 8 + jj)) : ff(0.0);
+      ff v[8];
+      lc_tile_values(tl, j0, erow, cexp + j0, v);
 #pragma unroll
       for (int jj = 0; jj < 8; ++jj) {
-        const int j = kLcTileN * ct + j0 + jj;  // trailing column
-        if (j >= T || (rho < T && rho < j)) continue;
-        float sd[kSlices];
-#pragma unroll
-        for (int d = 0; d < kSlices; ++d) sd[d] = s[d][jj];
-        const ff v = tc::ff_ldexp(tc::combine_diagonals(sd), erow + cexp[j0 + jj]);
-        if (rho < T) {
-          const int64_t o = koff + (int64_t)(c0 + nb + j) * m + c0 + nb + rho;
-          const ff cv = FROM_K ? ff(K[o]) : Lf[o];
-          Lf[o] = cv - v;
-        } else {
-          const int64_t o = qoff + (rho - T) * m + c0 + nb + j;
-          G[o] = G[o] - v;
-        }
+        const int64_t o = c_index(kLcTileN * ct + j0 + jj);
+        if (o < 0) continue;
+        const ff out = cbuf[jj] - v[jj];
+        if (rho < T)
+          Lf[o] = out;
+        else
+          G[o] = out;
       }
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) cbuf[jj] = nbuf[jj];
     }
   }
   tc::tc_fence_before();
@@ -304,19 +493,21 @@ __global__ void __launch_bounds__(kLcUpdThreads, 1) k_lc_update(const double* __
 // (row-major doubles).  mode 0: A and B hold integers |v| <= 128, used as the single slice;
 // C is the tensor cores' fp32 sum.  mode 1: the float-pair split product of arbitrary values.
 // ---------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kLcUpdThreads, 1) k_tc_probe(const double* __restrict__ A,
-                                                               const double* __restrict__ B, int mode,
-                                                               double* __restrict__ C, int* __restrict__ status) {
+__global__ void __launch_bounds__(kLcProbeThreads, 1) k_tc_probe(const double* __restrict__ A,
+                                                                 const double* __restrict__ B, int mode,
+                                                                 double* __restrict__ C, int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tslot;
   __shared__ int rexp[kLcTileM + kLcTileN];
+  __shared__ int serr;
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
   uint16_t* sA = reinterpret_cast<uint16_t*>(smraw);
   uint16_t* sB = sA + kSlices * kATileBytes / 2;
   if (tid == 0) {
     tc::mbar_init(&bar, 1);
     tc::mbar_fence_init();
+    serr = 0;
   }
   if (w == 0) {
     tc::tmem_alloc(&tslot, kLcTmemCols);
@@ -356,10 +547,10 @@ __global__ void __launch_bounds__(kLcUpdThreads, 1) k_tc_probe(const double* __r
     tc::mma_commit(&bar);
   }
   __syncwarp();
-  const bool done = tc::mbar_wait(&bar, 0, kTcWaitLimit);
+  if (!tc::mbar_wait(&bar, 0, kTcWaitLimit)) atomicExch(&serr, 1);
   tc::tc_fence_after();
-  __syncthreads();
-  if (!done) {
+  __syncthreads();  // serr is the same in every thread from here on
+  if (serr) {
     if (tid == 0) status[0] = 1;
   } else {
     const int q = w & 3, h = w >> 2;
@@ -401,9 +592,12 @@ bool leaf_chol_tc_supported(const Tree& t, int r) {
   return t.max_leaf >= 1 && t.max_leaf <= kLcMaxLeaf && r >= 1 && r <= kLcMaxRank;
 }
 
+// Scratch per leaf: the slices of the rows below the block (kSlices x RP x 64 bf16) and of X
+// (kSlices x 64 x 64 bf16), then the row exponents of both.
 int64_t leaf_chol_tc_scratch_bytes(const Tree& t, int r) {
   const int64_t rp = lc_rp_max(t, r);
-  return t.nleaf * (rp * kLcNB * kSlices * (int64_t)sizeof(uint16_t) + rp * (int64_t)sizeof(int));
+  return t.nleaf * ((rp * kLcNB + (int64_t)kLcNB * kLcNB) * kSlices * (int64_t)sizeof(uint16_t) +
+                    (rp + kLcNB) * (int64_t)sizeof(int));
 }
 
 int leaf_chol_tc_steps(const Tree& t) { return (int)((t.max_leaf + kLcNB - 1) / kLcNB); }
@@ -412,7 +606,9 @@ bool leaf_chol_tc_has_update(const Tree& t, int p) { return t.max_leaf - (int64_
 
 struct LcArgs {
   uint16_t* slices;
+  uint16_t* xsl;
   int* rexp;
+  int* xexp;
   int64_t slice_stride, exp_stride;
 };
 
@@ -422,44 +618,43 @@ static LcArgs lc_args(const Tree& t, int r, void* scratch) {
   a.slice_stride = rp * kLcNB * kSlices;
   a.exp_stride = rp;
   a.slices = reinterpret_cast<uint16_t*>(scratch);
-  a.rexp = reinterpret_cast<int*>(a.slices + t.nleaf * a.slice_stride);
+  a.xsl = a.slices + t.nleaf * a.slice_stride;
+  a.rexp = reinterpret_cast<int*>(a.xsl + t.nleaf * (int64_t)kSlices * kLcNB * kLcNB);
+  a.xexp = a.rexp + t.nleaf * rp;
   return a;
 }
 
-void launch_leaf_chol_tc_panel(const double* K, ff* Lf, ff* G, int r, const Tree& t, int p, void* scratch,
-                               int* info, cudaStream_t st) {
+void launch_leaf_chol_tc_diag(ff* Lf, int r, const Tree& t, int p, void* scratch, int* info, cudaStream_t st) {
   const LcArgs a = lc_args(t, r, scratch);
-  const size_t smp = (size_t)kLcNB * (kLcNB + 1) * sizeof(ff) + (size_t)kLcNB * kLcPanelThreads * sizeof(ff);
-  const int c0 = kLcNB * p;
-  if (p == 0) {
-    smem_limit((const void*)k_lc_panel<true>, smp);
-    k_lc_panel<true><<<(unsigned)t.nleaf, kLcPanelThreads, smp, st>>>(K, Lf, G, r, dtree(t), c0, a.slices, a.rexp,
-                                                                      a.slice_stride, a.exp_stride, info);
-  } else {
-    smem_limit((const void*)k_lc_panel<false>, smp);
-    k_lc_panel<false><<<(unsigned)t.nleaf, kLcPanelThreads, smp, st>>>(K, Lf, G, r, dtree(t), c0, a.slices, a.rexp,
-                                                                       a.slice_stride, a.exp_stride, info);
-  }
+  const size_t smd = (size_t)2 * kLcNB * (kLcNB + 1) * sizeof(ff);
+  smem_limit((const void*)k_lc_diag, smd);
+  k_lc_diag<<<(unsigned)t.nleaf, kLcDiagThreads, smd, st>>>(Lf, dtree(t), kLcNB * p, a.xsl, a.xexp, info);
 }
 
-void launch_leaf_chol_tc_update(const double* K, ff* Lf, ff* G, int r, const Tree& t, int p, void* scratch,
-                                int* info, cudaStream_t st) {
+void launch_leaf_chol_tc_trsm(ff* Lf, ff* G, int r, const Tree& t, int p, void* scratch, int* info,
+                              cudaStream_t st) {
   const LcArgs a = lc_args(t, r, scratch);
-  const size_t smu = (size_t)kSlices * (kATileBytes + kBTileBytes);
+  const int c0 = kLcNB * p;
+  const size_t sm = (size_t)kSlices * (kATileBytes + kBTileBytes);
+  smem_limit((const void*)k_lc_trsm, sm);
+  const int64_t rmax = t.max_leaf - c0 - 1 + r;  // rows below the block of the largest leaf, nb >= 1
+  dim3 grid((unsigned)t.nleaf, (unsigned)((rmax + kLcTileM - 1) / kLcTileM));
+  k_lc_trsm<<<grid, kLcTcThreads, sm, st>>>(Lf, G, r, dtree(t), c0, a.xsl, a.xexp, a.slices, a.rexp, a.slice_stride,
+                                            a.exp_stride, info);
+}
+
+void launch_leaf_chol_tc_update(ff* Lf, ff* G, int r, const Tree& t, int p, void* scratch, int* info,
+                                cudaStream_t st) {
+  const LcArgs a = lc_args(t, r, scratch);
+  const size_t sm = (size_t)kSlices * (kATileBytes + kBTileBytes);
   const int c0 = kLcNB * p;
   const int64_t tmax = t.max_leaf - c0 - kLcNB;
   if (tmax <= 0) return;
   dim3 grid((unsigned)t.nleaf, (unsigned)((tmax + r + kLcTileM - 1) / kLcTileM),
             (unsigned)((tmax + kLcTileN - 1) / kLcTileN));
-  if (p == 0) {
-    smem_limit((const void*)k_lc_update<true>, smu);
-    k_lc_update<true><<<grid, kLcUpdThreads, smu, st>>>(K, Lf, G, r, dtree(t), c0, a.slices, a.rexp, a.slice_stride,
-                                                        a.exp_stride, info);
-  } else {
-    smem_limit((const void*)k_lc_update<false>, smu);
-    k_lc_update<false><<<grid, kLcUpdThreads, smu, st>>>(K, Lf, G, r, dtree(t), c0, a.slices, a.rexp,
-                                                         a.slice_stride, a.exp_stride, info);
-  }
+  smem_limit((const void*)k_lc_update, sm);
+  k_lc_update<<<grid, kLcTcThreads, sm, st>>>(Lf, G, r, dtree(t), c0, a.slices, a.rexp, a.slice_stride,
+                                              a.exp_stride, info);
 }
 
 }  // namespace km
@@ -481,7 +676,7 @@ extern "C" int km_probe_tc_gemm(int device, const double* A, const double* B, in
     cudaMemset(dst, 0, sizeof(int));
     const size_t smu = (size_t)kSlices * (kATileBytes + kBTileBytes);
     smem_limit((const void*)k_tc_probe, smu);
-    k_tc_probe<<<1, kLcUpdThreads, smu>>>(dA, dB, mode, dC, dst);
+    k_tc_probe<<<1, kLcProbeThreads, smu>>>(dA, dB, mode, dC, dst);
     int stv = 0;
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
       rc = KM_ERR_CUDA;

@@ -136,3 +136,19 @@ def test_leaf_tc_matches_cuda_core_leaf_kernels(lib):
         x0 = np.array(x0)
         assert abs(ld - ld0) < 1e-6
         assert np.linalg.norm(x - x0) / np.linalg.norm(x0) < 1e-9
+
+
+def test_second_factorisation_of_one_assembly(lib):
+    """A second symmetricfactorize! of the same assembly starts again from the leaf matrices."""
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    n = 8192
+    pts = uniform_points(n, 44)
+    rhs = np.random.default_rng(45).standard_normal((n, 2))
+    hk = K.KernelHODLR(K.KernelMatrix(pts, pts, [1.0, 0.1, 1e-3], K.Matern32()), 0.0, 72, K.FixedLevel(5),
+                       nystrom=True, precision=K.KM_PREC_MIXED)
+    K.symmetricfactorize(hk)
+    ld1, x1 = hk.logdet(), hk.ldiv(rhs)
+    K.symmetricfactorize(hk)
+    assert hk.logdet() == ld1
+    assert np.array_equal(hk.ldiv(rhs), x1)
