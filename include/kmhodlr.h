@@ -450,6 +450,14 @@ int km_profile_get(km_handle* h, int cls, double* total_ms, int64_t* launches);
 
 /* ---- diagnostics ------------------------------------------------------------------------- */
 
+/* Number of polls after which a bounded device-side wait of this handle's kernels gives up: the
+ * dataflow flags of the mixed-form node factorisation and the grid barriers of the ACA and tall
+ * panel-QR kernels.  polls < 0 restores the defaults (well above any legitimate wait); 0 makes
+ * every such wait give up at its first poll, as if the flag it waits for were never set.  A wait
+ * that gives up ends its kernel early and the call returns KM_ERR_TIMEOUT; the handle stays
+ * usable (assemble again).  For tests of that path.  No reference counterpart. */
+int km_set_wait_limit(km_handle* h, int64_t polls);
+
 /* Device FP64 FMA throughput in TFLOP/s measured by a short timed loop (roofline denominator
  * for FP64-ALU-bound kernels). */
 int km_probe_fp64_tflops(int device, double* out);

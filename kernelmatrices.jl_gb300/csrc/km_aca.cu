@@ -825,11 +825,18 @@ struct GridBar {
   unsigned* count;
   volatile unsigned* gen;
   volatile int* err;
+  long long limit;  // polls before a wait gives up (< 0: kGridSpinLimit; 0: at the first poll, as
+                    // if the other CTAs never arrived: the test of the timeout path)
 };
 
+// Returns true when every CTA has arrived and no barrier of this launch has run out; the answer
+// is the same for all threads of the CTA (thread 0's view, passed through shared memory), so the
+// CTA leaves its loop as a whole.
 __device__ bool grid_barrier(GridBar gb) {
+  __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
+    const long long lim = gb.limit < 0 ? kGridSpinLimit : gb.limit;
     const unsigned g = *gb.gen;
     __threadfence();
     if (atomicAdd(gb.count, 1u) == gridDim.x - 1) {
@@ -838,17 +845,18 @@ __device__ bool grid_barrier(GridBar gb) {
       atomicExch((unsigned*)gb.gen, g + 1);
     } else {
       long long spins = 0;
-      while (*gb.gen == g && *gb.err == 0) {
-        if (++spins > kGridSpinLimit) {
+      while ((gb.limit == 0 || *gb.gen == g) && *gb.err == 0) {
+        if (++spins > lim) {
           atomicExch((int*)gb.err, 1);
           break;
         }
       }
     }
     __threadfence();
+    s_ok = *gb.err == 0;
   }
   __syncthreads();
-  return *gb.err == 0;
+  return s_ok != 0;
 }
 
 // partial argmax record of one CTA: (|x| best, its index, first unflagged index)
@@ -1167,7 +1175,8 @@ int64_t aca_grid_scratch(int cap) {
 }
 
 bool launch_aca_grid(const double* pts, KParams kp, const AcaBlock* blocks, int b, int cap, double* P, uint8_t* F,
-                     int* piv, double rtol, int* rank, int* status, double* scratch, cudaStream_t st) {
+                     int* piv, double rtol, int* rank, int* status, double* scratch, cudaStream_t st,
+                     long long wait_limit) {
   int dev = 0, coop = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
@@ -1183,7 +1192,7 @@ bool launch_aca_grid(const double* pts, KParams kp, const AcaBlock* blocks, int 
   // barrier words live after the records in the scratch
   unsigned* words = reinterpret_cast<unsigned*>(scratch + (int64_t)G * (3 + 2 * cap) + 2 * G + 8);
   if (cudaMemsetAsync(words, 0, 4 * sizeof(unsigned), st) != cudaSuccess) return false;
-  GridBar gb{words, words + 1, reinterpret_cast<volatile int*>(words + 2)};
+  GridBar gb{words, words + 1, reinterpret_cast<volatile int*>(words + 2), wait_limit};
   void* args[] = {(void*)&pts, (void*)&kp, (void*)&blocks, (void*)&b, (void*)&P, (void*)&F, (void*)&piv,
                   (void*)&rtol, (void*)&rank, (void*)&status, (void*)&scratch, (void*)&gb};
   if (cudaLaunchCooperativeKernel((const void*)k_aca_grid, dim3(G), dim3(512), args, sm, st) != cudaSuccess) {
@@ -1480,7 +1489,8 @@ static int pq_grid_size(int64_t m) {
 }
 
 void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n, int kmax, double* taus,
-                          double* Ts, double* gemm_scratch, void* cublas_handle, int* grid_err, cudaStream_t st) {
+                          double* Ts, double* gemm_scratch, void* cublas_handle, int* grid_err, cudaStream_t st,
+                          long long wait_limit) {
   if (n <= 0 || kmax <= 0) return;
   cublasHandle_t cub = static_cast<cublasHandle_t>(cublas_handle);
   cublasSetStream(cub, st);
@@ -1495,7 +1505,7 @@ void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n
   double* part = gemm_scratch + mbig * kQB + 2 * (int64_t)kQB * std::max(kmax, 1);
   unsigned* words = reinterpret_cast<unsigned*>(part + 2 * 152 * kPqParts);
   cudaMemsetAsync(words, 0, 4 * sizeof(unsigned), st);
-  GridBar gb{words, words + 1, grid_err};
+  GridBar gb{words, words + 1, grid_err, wait_limit};
   auto factor_big = [&](int p, int b) {
     const int G = pq_grid_size(hdescs[p].m);
     const PanelDesc* dp = descs + p;

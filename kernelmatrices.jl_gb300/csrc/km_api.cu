@@ -82,6 +82,7 @@ struct km_handle {
   // CTAs per node of the float-pair node kernel at most (thread-block clusters on levels with
   // few nodes); 1 for handles of the batch and serving pools, whose streams fill the SMs already
   int node_cluster_max = 8;
+  int64_t wait_limit = -1;  // polls before a bounded device wait gives up (km_set_wait_limit)
   double tol = 0.0;
   int64_t maxrank = 0;
   int r = 0;
@@ -1139,6 +1140,13 @@ int km_set_stream(km_handle* h, void* stream) {
   return KM_OK;
 }
 
+int km_set_wait_limit(km_handle* h, int64_t polls) {
+  if (!h) return KM_ERR_BAD_ARG;
+  h->wait_limit = polls < 0 ? -1 : polls;
+  h->alloc_epoch += 1;  // launch graphs captured with the previous limit are not replayed
+  return KM_OK;
+}
+
 int km_profile_enable(km_handle* h, int on) {
   if (!h) return KM_ERR_BAD_ARG;
   cudaStreamSynchronize(h->stream);
@@ -1282,7 +1290,8 @@ static int aca_assemble(km_handle* h, const double* pts, bool dev, const Tree& t
         if (!h->blk[q].grid) continue;
         bool ok = false;
         KLV(h, KM_PROF_ACA, ok = launch_aca_grid(h->d_pts, h->kp, h->d_blk, q, h->blk[q].cap, h->d_panels, h->d_flags,
-                                                 h->d_piv, tol, h->d_brank, h->d_bstatus, h->d_acascr, st));
+                                                 h->d_piv, tol, h->d_brank, h->d_bstatus, h->d_acascr, st,
+                                                 h->wait_limit));
         if (!ok)
           KLV(h, KM_PROF_ACA, launch_aca_one(h->d_pts, h->kp, h->d_blk, q, maxcap, h->d_panels, h->d_flags, h->d_piv,
                                              tol, h->d_brank, h->d_bstatus, st));
@@ -1435,7 +1444,7 @@ static int general_factorize(km_handle* h) {
         if ((rc = grow(h, &h->d_pqg, panel_qr_gemm_scratch(pd.data() + pdoff[l], np, kmax_l[l])))) return rc;
         KLV(h, KM_PROF_LEAF_QR, launch_panel_qr_gemm(h->d_pdesc + pdoff[l], pd.data() + pdoff[l], np, kmax_l[l],
                                                      h->d_pqs, h->d_pqs + (int64_t)np * kmax_l[l], h->d_pqg,
-                                                     h->cublas, h->d_info + t.nleaf + nb, st));
+                                                     h->cublas, h->d_info + t.nleaf + nb, st, h->wait_limit));
       } else {
         KLV(h, KM_PROF_LEAF_QR, launch_panel_qr(h->d_pdesc + pdoff[l], np, kmax_l[l], h->d_pqs,
                                                 h->d_pqs + (int64_t)np * kmax_l[l], st));
@@ -1626,7 +1635,8 @@ static int factorize_launches(km_handle* h) {
       for (int l = 1; l <= t.L; ++l) {
         KLV(h, KM_PROF_NODE, launch_node_factor<ff>(P<ff>(h->d_R), P<ff>(h->d_SinvTf), r, l, t, P<ff>(h->d_Ct),
                                                     P<ff>(h->d_L22), P<ff>(h->d_Eref), P<ff>(h->d_Etau),
-                                                    h->d_info + t.nleaf, st, h->node_cluster_max));
+                                                    h->d_info + t.nleaf, st, h->node_cluster_max,
+                                                    (int)std::min<int64_t>(h->wait_limit, INT32_MAX)));
         side_level(h, l);
         {
           const NodeMatsH nm = node_mats(h);

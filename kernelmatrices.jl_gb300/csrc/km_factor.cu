@@ -351,10 +351,13 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
                                                      int64_t cbase, int64_t nbase, T* __restrict__ Ct_out,
                                                      T* __restrict__ L22_out, T* __restrict__ Eref,
                                                      T* __restrict__ Etau, int* __restrict__ info,
-                                                     int csize) {
+                                                     int csize, int wait_limit) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
   const int ld = r + 1;
+  // polls of a flag before a wait gives up; wait_limit 0: every wait gives up at its first poll,
+  // as if its flag were never set (the test of the timeout path)
+  const int lim = wait_limit < 0 ? kWaitLimit : wait_limit;
   T* X0 = sm;
   T* X1 = X0 + r * ld;
   T* X2 = X1 + r * ld;
@@ -474,8 +477,8 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       for (int k = 0; k < c; ++k) {
         if (k >= known && !timed_out) {
           int spins = 0;
-          while (vflag[k] == 0) {
-            if (++spins > kWaitLimit) {
+          while (wait_limit == 0 || vflag[k] == 0) {
+            if (++spins > lim) {
               if (lane == 0) info[node] = -1;
               timed_out = true;
               break;
@@ -617,8 +620,8 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
         if (lane == 0) vflag[j] = 1;
       } else if (!timed_out) {
         int spins = 0;
-        while (vflag[j] == 0) {
-          if (++spins > kWaitLimit) {
+        while (wait_limit == 0 || vflag[j] == 0) {
+          if (++spins > lim) {
             if (lane == 0) info[node] = -1;
             timed_out = true;
             break;
@@ -1015,7 +1018,7 @@ static int node_cluster_size(const void* fn, int64_t nodes, int threads, size_t 
 
 template <typename T>
 void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T* Ct, T* L22, T* Eref,
-                        T* Etau, int* info, cudaStream_t st, int max_cluster) {
+                        T* Etau, int* info, cudaStream_t st, int max_cluster, int wait_limit) {
   const int64_t cbase = (level == 1) ? 0 : t.nleaf + t.node_off[level - 1];
   const int64_t nbase = t.node_off[level];
   if constexpr (std::is_same<T, double>::value) {
@@ -1045,7 +1048,7 @@ void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T
       cfg.numAttrs = 1;
       const cudaError_t prior = cudaPeekAtLastError();
       if (cudaLaunchKernelEx(&cfg, k_node_factor<T>, R, SinvT, r, level, t.L, t.nleaf, cbase, nbase, Ct, L22, Eref,
-                             Etau, info, cs) == cudaSuccess)
+                             Etau, info, cs, wait_limit) == cudaSuccess)
         return;
       // the cluster launch was refused (nothing ran): one CTA per node instead; an error from
       // before this launch stays for the caller
@@ -1053,7 +1056,7 @@ void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T
     }
     {
       k_node_factor<T><<<(unsigned)nodes, 1024, sm, st>>>(R, SinvT, r, level, t.L, t.nleaf, cbase, nbase, Ct, L22,
-                                                          Eref, Etau, info, 1);
+                                                          Eref, Etau, info, 1, wait_limit);
     }
   }
 }
@@ -1244,9 +1247,9 @@ template bool launch_leaf_chol<ff>(const double*, ff*, const Tree&, int*, cudaSt
 template void launch_leaf_qr<double>(double*, int, const Tree&, double*, double*, cudaStream_t);
 template void launch_leaf_qr<ff>(ff*, int, const Tree&, ff*, ff*, cudaStream_t);
 template void launch_node_factor<double>(double*, const double*, int, int, const Tree&, double*, double*, double*,
-                                         double*, int*, cudaStream_t, int);
+                                         double*, int*, cudaStream_t, int, int);
 template void launch_node_factor<ff>(ff*, const ff*, int, int, const Tree&, ff*, ff*, ff*, ff*, int*, cudaStream_t,
-                                     int);
+                                     int, int);
 template void launch_logdet<double>(const double*, const Tree&, const double*, int, double*, int, double*, cudaStream_t);
 template void launch_logdet<ff>(const ff*, const Tree&, const ff*, int, double*, int, double*, cudaStream_t);
 

@@ -112,8 +112,10 @@ void launch_leaf_chol_tc_update(ff* Lf, ff* G, int r, const Tree& t, int p, void
                                 cudaStream_t st);
 void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st);
 template <typename T>
+// wait_limit: polls of a dataflow flag before a wait gives up (< 0: the kernel's default, 0: at
+// the first poll, the test of the timeout path); a wait that gives up sets info = -1
 void launch_node_factor(T* R, const T* SinvT, int r, int level, const Tree& t, T* Ct, T* L22, T* Eref, T* Etau,
-                        int* info, cudaStream_t st, int max_cluster = 8);
+                        int* info, cudaStream_t st, int max_cluster = 8, int wait_limit = -1);
 template <typename T>
 void launch_leaf_formq(T* Pan, const T* tau, int r, const Tree& t, cudaStream_t st);
 template <typename T>
@@ -181,8 +183,10 @@ void launch_aca(const double* pts, KParams kp, const AcaBlock* blocks, int nbloc
 // ACA of one large block (blocks[b].grid == 1) by all SMs in one cooperative launch, with
 // bounded grid barriers; scratch of aca_grid_scratch(cap) doubles.  Returns false when the
 // cooperative launch is unavailable (the caller then runs the block in the one-CTA kernel).
+// wait_limit: polls before a grid barrier gives up (< 0: default; 0: at the first poll)
 bool launch_aca_grid(const double* pts, KParams kp, const AcaBlock* blocks, int b, int cap, double* P, uint8_t* F,
-                     int* piv, double rtol, int* rank, int* status, double* scratch, cudaStream_t st);
+                     int* piv, double rtol, int* rank, int* status, double* scratch, cudaStream_t st,
+                     long long wait_limit = -1);
 int64_t aca_grid_scratch(int cap);
 // one-CTA ACA of a single block regardless of its grid flag (fallback)
 void launch_aca_one(const double* pts, KParams kp, const AcaBlock* blocks, int b, int maxcap, double* P,
@@ -195,7 +199,8 @@ void launch_panel_qr(const PanelDesc* descs, int n, int kmax, double* taus, doub
 // their block-reflector applications as cuBLAS DGEMMs (hdescs: host copies of descs;
 // gemm_scratch: panel_qr_gemm_scratch(hdescs, n, kmax) doubles)
 void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n, int kmax, double* taus,
-                          double* Ts, double* gemm_scratch, void* cublas_handle, int* grid_err, cudaStream_t st);
+                          double* Ts, double* gemm_scratch, void* cublas_handle, int* grid_err, cudaStream_t st,
+                          long long wait_limit = -1);
 int64_t panel_qr_gemm_scratch(const PanelDesc* hdescs, int n, int kmax);
 int64_t panel_qr_scratch(int n, int kmax);
 void launch_gnode(const GNodeDesc* nodes, int n, int* info, cudaStream_t st);

@@ -307,8 +307,9 @@ __global__ void __launch_bounds__(kLcTcThreads, 1) k_lc_trsm(ff* __restrict__ Lf
   tc::tc_fence_after();
   __syncthreads();  // serr is the same in every thread from here on
   if (serr) {
-    if (tid == 0) {
-      tc::mbar_wait(&bar[0], 0, kTcWaitLimit);  // copies still in flight land before the exit
+    if (tid == 0) {  // copies and products still in flight finish before the exit
+      tc::mbar_wait(&bar[0], 0, kTcWaitLimit);
+      tc::mbar_wait(&bar[1], 0, kTcWaitLimit);
       info[leaf] = -1;
     }
   } else {
@@ -455,8 +456,9 @@ __global__ void __launch_bounds__(kLcTcThreads, 1) k_lc_update(ff* __restrict__ 
   tc::tc_fence_after();
   __syncthreads();  // serr is the same in every thread from here on
   if (serr) {
-    if (tid == 0) {
-      tc::mbar_wait(&bar[0], 0, kTcWaitLimit);  // copies still in flight land before the exit
+    if (tid == 0) {  // copies and products still in flight finish before the exit
+      tc::mbar_wait(&bar[0], 0, kTcWaitLimit);
+      tc::mbar_wait(&bar[1], 0, kTcWaitLimit);
       info[leaf] = -1;
     }
   } else {

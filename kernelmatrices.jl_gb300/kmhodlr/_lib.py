@@ -119,6 +119,7 @@ SIGNATURES = {
     "km_probe_fp64_tflops": (C.c_int, [C.c_int, _DP]),
     "km_probe_fp32_tflops": (C.c_int, [C.c_int, _DP]),
     "km_probe_tc_gemm": (C.c_int, [C.c_int, _DP, _DP, C.c_int, _DP]),
+    "km_set_wait_limit": (C.c_int, [_H, C.c_int64]),
     "km_assemble_dev": (C.c_int, [_H, _P, C.c_int64, C.c_int, _DP, C.c_int, C.c_int, C.c_double, C.c_int64,
                                   C.c_int, C.c_int64]),
     "km_set_stream": (C.c_int, [_H, _P]),
