@@ -67,6 +67,36 @@ def engine_flops(n: int, L: int, m0: int = 256, r: int = RANK) -> dict:
     }
 
 
+def leaf_tc_mma_flops(m: int, nleaf: int, r: int = RANK) -> dict:
+    """bf16 tensor-core flops issued per step by the mixed form's tensor-core leaf stage (the
+    launch grids of km_leaf_tc.cu for leaves of m points): every 128 x 64 tile of the block-column
+    and update launches takes 28 slice products of K = 64, i.e. 28 x 2 x 128 x 64 x 64 flops; and
+    the algorithmic float-pair flops those tiles stand for (2 flops per multiply-add of the
+    block columns P = A X' and of the trailing updates C -= P P', lower triangles only)."""
+    per_tile = 28 * 2 * 128 * 64 * 64
+    tiles = 0
+    alg = 0.0
+    for c0 in range(0, m, 64):
+        nb = min(64, m - c0)
+        T = m - c0 - nb
+        R = T + r
+        RP = -(-R // 128) * 128
+        tiles += RP // 128                       # block column
+        alg += 2.0 * R * nb * nb
+        for rt in range(-(-R // 128)):           # trailing update
+            for ct in range(-(-T // 64)):
+                rlast = min(128 * rt + 127, R - 1)
+                if not (rlast < T and rlast < 64 * ct):
+                    tiles += 1
+        alg += 2.0 * nb * (T * (T + 1) / 2 + r * T)
+    return {"mma_flops": nleaf * tiles * float(per_tile), "alg_flops": nleaf * alg}
+
+
+def measured_peaks() -> dict:
+    f = ROOT / "MEASURED_PEAKS.json"
+    return json.loads(f.read_text()) if f.exists() else {}
+
+
 # ----------------------------------------------------------------------------------------------
 # clocks
 # ----------------------------------------------------------------------------------------------
@@ -400,6 +430,20 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                 "frac": achieved / peak, "traffic": traffic,
                 "per_launch_ms": prof[dom]["ms"] / max(prof[dom]["launches"], 1), "peak_source": src,
                 "fp64_peak_tflops": fp64_peak, "fp32_peak_tflops": fp32_peak}
+    # the tensor-core leaf kernels (mixed form): issued bf16 work against the measured bf16 peak
+    roof_tc = None
+    if head_prec == L.KM_PREC_MIXED and "leaf_tc" in prof:
+        tcw = leaf_tc_mma_flops(n // 2 ** LEVEL, 2 ** LEVEL)
+        sec = prof["leaf_tc"]["ms"] * 1e-3
+        pk = measured_peaks()
+        peak_tc = pk.get("bf16_tflops")
+        ach = tcw["mma_flops"] / sec / 1e12
+        roof_tc = {"kernel": "leaf_tc (k_lc_trsm, k_lc_update)", "bound": "tensor", "achieved": ach,
+                   "peak": peak_tc, "unit": "TFLOP/s", "frac": (ach / peak_tc) if peak_tc else None,
+                   "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peak_tc else "absent",
+                   "issued_bf16_tflop_per_step": tcw["mma_flops"] / 1e12,
+                   "algorithmic_float_pair_tflops": tcw["alg_flops"] / sec / 1e12,
+                   "ms_per_step": prof["leaf_tc"]["ms"], "launches": prof["leaf_tc"]["launches"]}
     accuracy = {"logdet_abs_err_mixed_vs_fp64": abs(mix["logdet"] - f64["logdet"]),
                 "solve_rel_err_mixed_vs_fp64": float(np.linalg.norm(mix["sol"] - f64["sol"]) /
                                                      np.linalg.norm(f64["sol"])),
@@ -415,6 +459,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
            "gpu_launches": int(head["launches"]),
            "clocks": head["clk"],
            "roofline": roof,
+           "roofline_tensor": roof_tc,
            "fp64_form": form_summary(f64),
            "mixed_form": form_summary(mix),
            "mixed_speedup_vs_fp64": f64["ms"] / mix["ms"],

@@ -29,10 +29,10 @@ def problems(sizes, seed=0):
     return out
 
 
-def single(prob, nprobe, seed, lvl):
+def single(prob, nprobe, seed, lvl, precision=0):
     import kmhodlr as K
     hk = K.KernelHODLR(K.KernelMatrix(prob.pts, prob.pts, prob.params, K.Matern32()), 0.0, RANK, lvl,
-                       nystrom=True)
+                       nystrom=True, precision=precision)
     K.symmetricfactorize(hk)
     return hk, hk.nll_grad_seeded(prob.y, nprobe, seed)
 
@@ -48,15 +48,19 @@ def test_seeded_probes_equal_host_probes(lib):
     assert hk.stats().device_bytes <= K.estimate_bytes(2048, RANK, K.LogLevel(8), 17, True)
 
 
-def test_batch_equals_single_and_oracle(lib):
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_batch_equals_single_and_oracle(lib, precision):
+    """Both forms: the batch equals single handles of the same form bit for bit; the oracle
+    tolerances are those of the FP64 form (NLL rel 1e-12, gradient 1e-6) and, for the mixed form,
+    its stated targets carried to the NLL (rel 1e-9) and gradient (rel 1e-5)."""
     import kmhodlr as K
     lvl = K.LogLevel(8)
     probs = problems([1024, 3000, 1500, 4096, 2048, 1200], seed=5)
-    eng = K.BatchEngine(nworkers=3)
+    eng = K.BatchEngine(nworkers=3, precision=precision)
     nll, grad, status = eng.nll_grad(probs, K.Matern32(), RANK, lvl, nprobe=72, seed=1000)
     assert np.all(status == 0)
     for b, p in enumerate(probs):
-        _, (nll1, g1) = single(p, 72, 1000 + b, lvl)
+        _, (nll1, g1) = single(p, 72, 1000 + b, lvl, precision)
         assert nll[b] == nll1, b
         assert np.array_equal(grad[b], g1), b
     # oracle parity on two of them with 8 probes
@@ -67,10 +71,11 @@ def test_batch_equals_single_and_oracle(lib):
         ok = O.KernelMatrix(p.pts, p.pts, np.array(p.params), O.KERNEL_MATERN32)
         ohk = O.build_hodlr(ok, 0.0, RANK, O.LogLevel(8), nystrom=True)
         O.symmetricfactorize(ohk)
-        assert abs(nll8[b] - O.negloglik(ohk, p.y)) < 1e-12 * abs(nll8[b]) + 1e-9
+        nll_tol, g_tol = (1e-12, 1e-6) if precision == 0 else (1e-9, 1e-5)
+        assert abs(nll8[b] - O.negloglik(ohk, p.y)) < nll_tol * abs(nll8[b]) + 1e-9
         V = O.rademacher_probes(n, 8, 50 + b)
         g0 = O.stoch_gradient(ok, ohk, p.y, 3, [V[:, c] for c in range(8)])
-        assert np.all(np.abs(grad8[b] - g0) <= 1e-6 * np.abs(g0) + 1e-8)
+        assert np.all(np.abs(grad8[b] - g0) <= g_tol * np.abs(g0) + 1e-8)
     eng.close()
 
 
@@ -115,11 +120,12 @@ def test_batch_reports_failing_problem_and_continues(lib):
     eng.close()
 
 
-def test_serve_same_alone_and_in_mix(lib):
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_serve_same_alone_and_in_mix(lib, precision):
     import kmhodlr as K
     lvl = K.LogLevel(8)
     probs = problems([2048, 1024, 4096, 1500, 3000, 1024, 2048, 8192], seed=21)
-    srv = K.Server(K.Matern32(), RANK, lvl, nworkers=4)
+    srv = K.Server(K.Matern32(), RANK, lvl, nworkers=4, precision=precision)
     alone = srv.wait(srv.submit_nll_grad(probs[0], nprobe=72, seed=9))
     assert alone.status == 0
     fa = srv.wait(srv.submit_factor(probs[2]))
@@ -142,7 +148,7 @@ def test_serve_same_alone_and_in_mix(lib):
     fb = srv.wait(t_fac)
     assert fb.status == 0
     # the factor's logdet and solve equal a single handle's
-    hk, _ = single(probs[2], 0, 0, lvl)
+    hk, _ = single(probs[2], 0, 0, lvl, precision)
     assert fa.logdet == hk.logdet()
     assert np.array_equal(x_alone, hk.ldiv(rhs))
     assert srv.wait(srv.submit_release(fa.factor_id)).status == 0
