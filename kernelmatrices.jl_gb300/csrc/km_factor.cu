@@ -905,6 +905,10 @@ __global__ void k_sum_partials(const double* __restrict__ partial, int np, doubl
   }
 }
 
+void launch_sum_partials(const double* partial, int np, double* out, cudaStream_t st) {
+  k_sum_partials<<<1, 32, 0, st>>>(partial, np, out);
+}
+
 // ---------------------------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------------------------

@@ -513,6 +513,125 @@ void launch_d2_assemble(const double* M, int r, double* Tmul, double* Tmult, cud
   k_d2_assemble<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(M, r, Tmul, Tmult);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Trace form of the stochastic gradient.  The gradient needs only the weighted sum over the
+// columns x_c of [T alpha] of x_c' dK_j x_c (weights w_c = 1/p for the probes, w = -1, or
+// -n / y'alpha for the profile likelihood, for alpha), never dK_j x_c itself.  Leaf by leaf,
+//   sum_c w_c x_c' dK_j x_c = <dK_j,leaf, G_leaf> + sum_c w_c (dphi_c' beta1_c + phi_c' beta2_c)
+// with the leaf Gram matrix G_leaf = sum_c w_c x_leaf,c x_leaf,c' (shared by the three
+// parameters), the leaf's own projections [phi ; dphi] and the landmark coefficients
+// [beta1 ; beta2] of the derivative product (k_dbeta).  This replaces three leaf products
+// dK_leaf X (m^2 k multiply-adds each) by one Gram matrix (m^2 k / 2) and three inner products.
+// ---------------------------------------------------------------------------------------------
+
+// G_leaf (lower triangle, column-major at d_leaf_koff) = sum_{c < p} x_c x_c' / p + wa x_p x_p'
+// for the columns of X (n x (p + 1), leading dimension n; T = double, or float pairs for the
+// mixed form).  grid = (ntile, ntile, nleaf) over 32 x 32 tiles, tiles above the diagonal exit;
+// block (32, 8), thread (tx, ty) takes rows ti*32 + tx, columns tj*32 + ty + 8 q.
+template <typename T>
+__global__ void k_leaf_gram(const T* __restrict__ X, int64_t n, int p, double wa, DTree t, T* __restrict__ G) {
+  const int ti = blockIdx.x, tj = blockIdx.y;
+  if (ti < tj) return;
+  const int64_t leaf = blockIdx.z;
+  const int m = d_leaf_size(t, leaf);
+  if (ti * 32 >= m) return;
+  const int64_t s = d_leaf_start(t, leaf);
+  __shared__ T xr[32][33];
+  __shared__ T xc[32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i = ti * 32 + tx;
+  acc_t<T> sp[4] = {}, sa[4] = {};
+  for (int c0 = 0; c0 <= p; c0 += 32) {
+    __syncthreads();
+    for (int e = ty * 32 + tx; e < 32 * 32; e += 256) {
+      const int cc = e >> 5, rr = e & 31;  // column cc of the chunk, row rr of the tile
+      const int c = c0 + cc;
+      const int ri = ti * 32 + rr, rj = tj * 32 + rr;
+      xr[rr][cc] = (c <= p && ri < m) ? X[(int64_t)c * n + s + ri] : T(0.0);
+      xc[rr][cc] = (c <= p && rj < m) ? X[(int64_t)c * n + s + rj] : T(0.0);
+    }
+    __syncthreads();
+    const int cend = min(32, p - c0);  // probe columns of this chunk; column p (alpha) apart
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int jl = ty + 8 * q;
+      for (int cc = 0; cc < cend; ++cc) sp[q] += xr[tx][cc] * xc[jl][cc];
+      if (p - c0 >= 0 && p - c0 < 32) sa[q] += xr[tx][p - c0] * xc[jl][p - c0];
+    }
+  }
+  const T wp = T(1.0) / T((double)p), w_a = T(wa);
+  T* Gl = G + d_leaf_koff(t, leaf);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int a = tj * 32 + ty + 8 * q;
+    if (i < m && a < m && i >= a) {
+      const T v = (p > 0 ? T(accv(sp[q]) * wp) : T(0.0)) + T(accv(sa[q]) * w_a);
+      Gl[i + (int64_t)a * m] = v;
+    }
+  }
+}
+
+// partial[leaf] = <dK_leaf, G_leaf> (both symmetric: the lower triangle, off-diagonal entries
+// twice) + sum_c w_c (dphi_c' beta1_c + phi_c' beta2_c), in FP64 and a fixed order.
+// VP: the leaf slots of the projection sweep ([phi ; dphi], 2r per column), beta: [beta1 ;
+// beta2] per (leaf, column), k = p + 1 columns.  grid = nleaf, block 256.
+template <typename T>
+__global__ void __launch_bounds__(256) k_leaf_grad_partial(const double* __restrict__ dK, const T* __restrict__ G,
+                                                           const double* __restrict__ VP, const T* __restrict__ beta,
+                                                           int r, int p, double wa, DTree t,
+                                                           double* __restrict__ partial) {
+  __shared__ double red[8];
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t ko = d_leaf_koff(t, leaf);
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  double acc = 0.0;
+  for (int a = w; a < m; a += 8) {  // warp per column, lanes over the rows i >= a
+    const double* dc = dK + ko + (int64_t)a * m;
+    const T* gc = G + ko + (int64_t)a * m;
+    for (int i = a + lane; i < m; i += 32) {
+      const double v = dc[i] * to_double(gc[i]);
+      acc += i > a ? 2.0 * v : v;
+    }
+  }
+  const int k = p + 1, r2 = 2 * r;
+  for (int c = w; c < k; c += 8) {  // warp per column, lanes over the r landmarks
+    const double* pv = VP + (leaf * k + c) * r2;
+    const T* bv = beta + (leaf * k + c) * r2;
+    double d = 0.0;
+    for (int q = lane; q < r; q += 32) d += pv[r + q] * to_double(bv[q]) + pv[q] * to_double(bv[r + q]);
+    d = warp_sum(d);
+    if (lane == 0) acc += (c < p ? 1.0 / (double)p : wa) * d;
+  }
+  acc = warp_sum(acc);
+  if (lane == 0) red[w] = acc;
+  __syncthreads();
+  if (tid == 0) {
+    double sum = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += red[q];
+    partial[leaf] = sum;
+  }
+}
+
+template <typename T>
+void launch_leaf_gram(const T* X, int64_t n, int p, double wa, const Tree& t, T* G, cudaStream_t st) {
+  const int nt = (int)((t.max_leaf + 31) / 32);
+  k_leaf_gram<T><<<dim3(nt, nt, (unsigned)t.nleaf), dim3(32, 8), 0, st>>>(X, n, p, wa, dtree(t), G);
+}
+
+template <typename T>
+void launch_leaf_grad_partial(const double* dK, const T* G, const double* VP, const T* beta, int r, int p, double wa,
+                              const Tree& t, double* partial, cudaStream_t st) {
+  k_leaf_grad_partial<T><<<(unsigned)t.nleaf, 256, 0, st>>>(dK, G, VP, beta, r, p, wa, dtree(t), partial);
+}
+
+template void launch_leaf_gram<double>(const double*, int64_t, int, double, const Tree&, double*, cudaStream_t);
+template void launch_leaf_gram<ff>(const ff*, int64_t, int, double, const Tree&, ff*, cudaStream_t);
+template void launch_leaf_grad_partial<double>(const double*, const double*, const double*, const double*, int, int,
+                                               double, const Tree&, double*, cudaStream_t);
+template void launch_leaf_grad_partial<ff>(const double*, const ff*, const double*, const ff*, int, int, double,
+                                           const Tree&, double*, cudaStream_t);
+
 void launch_small_gemm(const double* A, const double* B, int r, int transB, double* C, cudaStream_t st) {
   k_small_gemm<<<r, 128, 0, st>>>(A, B, r, transB, C);
 }
@@ -524,6 +643,7 @@ void launch_dbeta(const T* Sinv, const T* M2, int r, const double* VG, int64_t n
   k_dbeta<T><<<(unsigned)((npairs + 7) / 8), 256, sm, st>>>(Sinv, M2, r, VG, npairs, beta);
 }
 template void launch_dbeta<ff>(const ff*, const ff*, int, const double*, int64_t, ff*, cudaStream_t);
+template void launch_dbeta<double>(const double*, const double*, int, const double*, int64_t, double*, cudaStream_t);
 
 void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n, int k,
                      double* out, cudaStream_t st) {

@@ -125,6 +125,8 @@ template <typename T>
 void launch_logdet(const T* Lf, const Tree& t, const T* L22, int r, double* partial, int np, double* out,
                    cudaStream_t st);
 void launch_to_ff(const double* in, ff* out, int64_t n, cudaStream_t st);
+// out[0] = sum of partial[0 .. np) in index order (one thread)
+void launch_sum_partials(const double* partial, int np, double* out, cudaStream_t st);
 void launch_from_ff(const ff* in, double* out, int64_t n, cudaStream_t st);
 
 // products and solves
@@ -170,6 +172,14 @@ void launch_small_gemm(const double* A, const double* B, int r, int transB, doub
 template <typename T>
 void launch_dbeta(const T* Sinv, const T* M2, int r, const double* VG, int64_t npairs, T* beta, cudaStream_t st);
 void launch_axpby(double* y, const double* x, double a, double b, int64_t n, cudaStream_t st);
+// trace form of the stochastic gradient (km_grad.cu): the leaf Gram matrices of the columns of X
+// (n x (p + 1): p probes with weight 1/p, then alpha with weight wa), and per leaf
+// <dK_leaf, G_leaf> + sum_c w_c (dphi_c' beta1_c + phi_c' beta2_c)
+template <typename T>
+void launch_leaf_gram(const T* X, int64_t n, int p, double wa, const Tree& t, T* G, cudaStream_t st);
+template <typename T>
+void launch_leaf_grad_partial(const double* dK, const T* G, const double* VP, const T* beta, int r, int p, double wa,
+                              const Tree& t, double* partial, cudaStream_t st);
 // n x p Rademacher probes (+-1), entry (i, j) from a SplitMix64 hash of (seed, j*n + i)
 void launch_rademacher(double* out, int64_t n, int64_t p, uint64_t seed, cudaStream_t st);
 void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n, int k,
