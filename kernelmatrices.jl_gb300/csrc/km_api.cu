@@ -180,7 +180,10 @@ struct km_handle {
   double* d_hA = nullptr;     // a_j = dK_j u and b_j = K^{-1} a_j (6 n)
   double* d_hY = nullptr;     // second-derivative products of [W'^{-1} V | u]
   double* d_hdots = nullptr;
-  double* d_Gram = nullptr;  // leaf Gram matrices of the trace-form gradient (packed like d_K)
+  double* d_dPhi3 = nullptr;  // trace-form gradient: dK_j(X, P) for j = 0, 1, 2 (float pairs when mixed)
+  double* d_Sj3 = nullptr;    // dK_j(P, P), j = 0, 1, 2
+  double* d_Sj3F = nullptr;   // float-pair copy (mixed form)
+  double* d_VP4 = nullptr;    // projections [phi ; dphi_0 ; dphi_1 ; dphi_2] per (leaf, column), then the sums
   double* d_gpart = nullptr;  // per-leaf partial sums of the trace-form gradient, then 3 sums
   double* d_res = nullptr;   // refinement residual (n x rcap)
   double* d_rdots = nullptr;
@@ -345,7 +348,7 @@ void free_problem(km_handle* h) {
   h->d_Sinv = h->d_SinvF = h->d_M2 = h->d_M2F = h->d_Mtmp = h->d_GB = nullptr;
   h->gcap = h->tcap = 0;
   h->d_res = h->d_rdots = nullptr;
-  h->d_Gram = h->d_gpart = nullptr;
+  h->d_dPhi3 = h->d_Sj3 = h->d_Sj3F = h->d_VP4 = h->d_gpart = nullptr;
   h->rcap = 0;
   h->d2_pair = -1;
   h->d_hPhi3 = h->d_hD2 = h->d_hS = h->d_hT = h->d_hP = h->d_hG = h->d_hA = h->d_hY = h->d_hdots = nullptr;
@@ -1941,85 +1944,64 @@ int km_derivative_matvec(km_handle* h, int param, const double* x, double* y, in
 //   grad_j = 0.5 sum_c w_c x_c' dK_j x_c,   w_c = 1/p (probes), wa (alpha: -1, or -n / y'alpha
 // for the profile likelihood),
 // the same quantity as the reference's per-probe dots (stochasticgradient.jl:14-26) summed over
-// the probes: per leaf <dK_j, G> with the leaf Gram matrix G of X (formed once for the three
-// parameters), plus the landmark terms from the projection sweeps of derivative_apply.
+// the probes, split into the leaf terms <dK_j,l, G_l> (the leaf Gram matrices of X against the
+// derivative entries, both formed in registers) and the landmark quadratic forms of the
+// projections of X on [Phi dPhi_0 dPhi_1 dPhi_2] (one pass for the three parameters).
 static int gradient_trace(km_handle* h, int64_t p, double wa, double* grad) {
   const Tree& t = h->tree;
   const int r = h->r;
-  const int64_t n = t.n, kk = p + 1;
+  const int64_t n = t.n, kk = p + 1, W = 4 * r;
   cudaStream_t st = h->stream;
   int rc;
-  int64_t kbytes = 0;
-  for (int64_t q = 0; q < t.nleaf; ++q) kbytes += t.leaf_size(q) * t.leaf_size(q);
-  if ((rc = grow(h, &h->d_dK, kbytes)) || (rc = grow(h, &h->d_dPhi, t.n * r)) || (rc = grow(h, &h->d_Sj, r * r)) ||
-      (rc = grow(h, &h->d_Gram, kbytes)) || (rc = grow(h, &h->d_gpart, t.nleaf + 3)) ||
-      (rc = grow(h, &h->d_Sinv, r * r)) || (rc = grow(h, &h->d_M2, r * r)) || (rc = grow(h, &h->d_Mtmp, r * r)) ||
-      (rc = grow(h, &h->d_GB, t.nleaf * 2 * r * kk)))
+  if ((rc = grow(h, &h->d_dPhi3, 3 * t.n * r)) || (rc = grow(h, &h->d_Sj3, 3 * r * r)) ||
+      (rc = grow(h, &h->d_Sinv, r * r)) || (rc = grow(h, &h->d_VP4, (t.nleaf + 1) * kk * W)) ||
+      (rc = grow(h, &h->d_gpart, 3 * t.nleaf + 3 * (t.nleaf + 1) + 3)))
     return rc;
-  if (h->mixed && ((rc = grow(h, &h->d_dPhif, t.n * r)) || (rc = grow(h, &h->d_Phif, t.n * r)) ||
-                   (rc = grow(h, &h->d_SinvF, r * r)) || (rc = grow(h, &h->d_M2F, r * r))))
+  if (h->mixed && ((rc = grow(h, &h->d_Phif, t.n * r)) || (rc = grow(h, &h->d_SinvF, r * r)) ||
+                   (rc = grow(h, &h->d_Sj3F, 3 * r * r))))
     return rc;
-  if (kk > h->gcap) {
-    h->gcap = 0;
-    const int64_t slots = t.nleaf + t.nnode;
-    if ((rc = grow(h, &h->d_GP, slots * 2 * r * kk)) || (rc = grow(h, &h->d_GG, slots * 2 * r * kk))) return rc;
-    h->gcap = kk;
-  }
+  double* leafpart = h->d_gpart;
+  double* lmpart = h->d_gpart + 3 * t.nleaf;
+  double* sums = lmpart + 3 * (t.nleaf + 1);
+  // DerivativeHODLR (constructor.jl:66-95) for the three parameters: dK(X, P) and Sj = dK(P, P);
+  // the dK leaves are evaluated inside the leaf kernel
   KLV(h, KM_PROF_OTHER, launch_small_gemm(h->d_SinvT, h->d_SinvT, r, 1, h->d_Sinv, st));  // S^{-1}
+  for (int j = 0; j < 3; ++j)
+    KLV(h, KM_PROF_EVAL, launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, j, h->d_Sj3 + (int64_t)j * r * r, r, st));
   if (h->mixed) {
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Phif), t.n * r, st));
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Sinv, P<ff>(h->d_SinvF), (int64_t)r * r, st));
+    KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Sj3, P<ff>(h->d_Sj3F), (int64_t)3 * r * r, st));
+    KLV(h, KM_PROF_EVAL, launch_eval_dphi3<ff>(h->d_pts, h->d_lnd, r, t, h->kp, P<ff>(h->d_dPhi3), st));
     // X in float pairs (d_U is free here: no product dK X is formed)
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_T, P<ff>(h->d_U), n * kk, st));
-    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_gram<ff>(P<ff>(h->d_U), n, (int)p, wa, t, P<ff>(h->d_Gram), st));
+    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dk_gram<ff>(h->d_pts, h->kp, P<ff>(h->d_U), n, (int)p, wa, t, leafpart, st));
   } else {
-    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_gram<double>(h->d_T, n, (int)p, wa, t, h->d_Gram, st));
+    KLV(h, KM_PROF_EVAL, launch_eval_dphi3<double>(h->d_pts, h->d_lnd, r, t, h->kp, h->d_dPhi3, st));
+    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dk_gram<double>(h->d_pts, h->kp, h->d_T, n, (int)p, wa, t, leafpart, st));
   }
-  NodeMatsH nm2{nullptr, nullptr, nullptr, nullptr, 2 * r};
-  for (int j = 0; j < 3; ++j) {
-    // DerivativeHODLR (constructor.jl:66-95): dK leaves, dK(X, P), Sj = dK(P, P), M2 = S^{-1} Sj S^{-1}
-    KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, j, h->d_dK, st, h->mixed));
-    KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, j, h->d_dPhi, st, h->mixed));
-    KLV(h, KM_PROF_EVAL, launch_eval_dense(h->d_lnd, r, h->d_lnd, r, h->kp, j, h->d_Sj, r, st));
-    KLV(h, KM_PROF_OTHER, launch_small_gemm(h->d_Sj, h->d_Sinv, r, 0, h->d_Mtmp, st));
-    KLV(h, KM_PROF_OTHER, launch_small_gemm(h->d_Sinv, h->d_Mtmp, r, 0, h->d_M2, st));
-    if (t.L > 0) {
-      if (h->mixed) {
-        KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_dPhi, P<ff>(h->d_dPhif), t.n * r, st));
-        KLV(h, KM_PROF_LEAF_APPLY,
-            launch_leaf_dphiT<ff>(P<ff>(h->d_Phif), P<ff>(h->d_dPhif), r, t, h->d_T, n, h->d_GP, (int)kk, st));
-      } else {
-        KLV(h, KM_PROF_LEAF_APPLY,
-            launch_leaf_dphiT<double>(h->d_Phi, h->d_dPhi, r, t, h->d_T, n, h->d_GP, (int)kk, st));
-      }
-      for (int l = 1; l < t.L; ++l)
-        KLV(h, KM_PROF_SWEEP, launch_up<double>(t, nm2, l, h->d_GP, nullptr, (int)kk, UP_SUM_, st));
-      for (int l = t.L; l >= 1; --l)
-        KLV(h, KM_PROF_SWEEP, launch_down<double>(t, nm2, l, h->d_GP, h->d_GG, nullptr, (int)kk, DN_NYS_, st));
-    } else {
-      KM_CUDA(h, cudaMemsetAsync(h->d_GP, 0, sizeof(double) * 2 * r * kk, st));
-      KM_CUDA(h, cudaMemsetAsync(h->d_GG, 0, sizeof(double) * 2 * r * kk, st));
-    }
+  if (t.L > 0) {
     if (h->mixed) {
-      KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_M2, P<ff>(h->d_M2F), (int64_t)r * r, st));
-      KLV(h, KM_PROF_LEAF_APPLY, launch_dbeta<ff>(P<ff>(h->d_SinvF), P<ff>(h->d_M2F), r, h->d_GG, t.nleaf * kk,
-                                                  P<ff>(h->d_GB), st));
-      KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_grad_partial<ff>(h->d_dK, P<ff>(h->d_Gram), h->d_GP, P<ff>(h->d_GB), r,
-                                                              (int)p, wa, t, h->d_gpart, st));
+      KLV(h, KM_PROF_LEAF_APPLY,
+          launch_leaf_proj4<ff>(P<ff>(h->d_Phif), P<ff>(h->d_dPhi3), r, t, h->d_T, n, h->d_VP4, (int)kk, st));
     } else {
       KLV(h, KM_PROF_LEAF_APPLY,
-          launch_dbeta<double>(h->d_Sinv, h->d_M2, r, h->d_GG, t.nleaf * kk, h->d_GB, st));
-      KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_grad_partial<double>(h->d_dK, h->d_Gram, h->d_GP, h->d_GB, r, (int)p, wa,
-                                                                  t, h->d_gpart, st));
+          launch_leaf_proj4<double>(h->d_Phi, h->d_dPhi3, r, t, h->d_T, n, h->d_VP4, (int)kk, st));
     }
-    KLV(h, KM_PROF_OTHER, launch_sum_partials(h->d_gpart, (int)t.nleaf, h->d_gpart + t.nleaf + j, st));
+    KLV(h, KM_PROF_OTHER, launch_proj_total(h->d_VP4, (int)W, t.nleaf, (int)kk, st));
+    if (h->mixed)
+      KLV(h, KM_PROF_LEAF_APPLY, launch_landmark<ff>(h->d_VP4, r, (int)kk, (int)p, wa, P<ff>(h->d_SinvF),
+                                                     P<ff>(h->d_Sj3F), t.nleaf, lmpart, st));
+    else
+      KLV(h, KM_PROF_LEAF_APPLY, launch_landmark<double>(h->d_VP4, r, (int)kk, (int)p, wa, h->d_Sinv, h->d_Sj3,
+                                                         t.nleaf, lmpart, st));
+  } else {
+    // a single leaf: no off-diagonal block, no landmark term
+    KM_CUDA(h, cudaMemsetAsync(lmpart, 0, sizeof(double) * 3 * (t.nleaf + 1), st));
   }
-  h->dk_param = -1;  // d_dK holds the last parameter's leaves, but no float-pair copy of them
-  double sums[3];
-  KM_CUDA(h, cudaMemcpyAsync(sums, h->d_gpart + t.nleaf, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
-  if ((rc = sync(h, "gradient")) != KM_OK) return rc;
-  for (int j = 0; j < 3; ++j) grad[j] = 0.5 * sums[j];
-  return KM_OK;
+  KLV(h, KM_PROF_OTHER, launch_grad_final(leafpart, t.nleaf, lmpart, t.nleaf + 1, 0.5, sums, st));
+  KM_CUDA(h, cudaMemcpyAsync(grad, sums, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
+  return sync(h, "gradient");
 }
 
 static int nll_grad_impl(km_handle* h, const double* y, const double* probes, bool seeded, uint64_t seed,
@@ -2378,8 +2360,8 @@ extern "C" int km_maxlikdata(km_handle* h, const double* pts, const double* data
   return kd_impl(h, pts, data, n, leaf, perm, pts_sorted, data_sorted);
 }
 
-// Mirrors the allocations of assemble_impl (Nystrom), ensure_vec, ensure_xy, derivative_apply
-// and nll_grad_impl for one problem shape.
+// Mirrors the allocations of assemble_impl (Nystrom), ensure_vec, ensure_xy and nll_grad_impl
+// with the trace-form gradient for one problem shape.
 extern "C" int64_t km_estimate_bytes(int64_t n, int64_t rank, int level_kind, int64_t level, int64_t ncols,
                           int with_grad) {
   Tree t;
@@ -2397,9 +2379,9 @@ extern "C" int64_t km_estimate_bytes(int64_t n, int64_t rank, int level_kind, in
   b += 2 * d(n * k);                              // ensure_xy
   if (leaf_tc_enabled() && leaf_chol_tc_supported(t, (int)r))  // slices of the tensor-core leaf stage
     b += leaf_chol_tc_scratch_bytes(t, (int)r);
-  if (with_grad)  // derivative workspaces, plus the float-pair copies the mixed form keeps, and the
-                  // leaf Gram matrices and partial sums of the trace-form gradient
-    b += d(kb) + d(n * r) + d(r * r) + 2 * d(slots * 2 * r * k) + 2 * d(n * k) + d(k) + d(kb) + 2 * d(n * r) +
-         5 * d(r * r) + d(t.nleaf * 2 * r * k) + d(kb) + d(t.nleaf + 3);
+  if (with_grad)  // trace-form gradient: [T alpha] and its float-pair copy, dK_j(X, P) for the three
+                  // parameters, the float-pair Phi, S^{-1} and Sj, the projections, the partial sums
+    b += 2 * d(n * k) + d(k) + d(3 * n * r) + d(n * r) + 2 * d(3 * r * r) + 2 * d(r * r) +
+         d((t.nleaf + 1) * k * 4 * r) + d(6 * t.nleaf + 6);
   return b;
 }

@@ -10,8 +10,10 @@
 // where a and b are the sums of phi and dphi of the siblings along the leaf's path to the root.
 // The sums travel through the tree sweeps with 2r-long vectors [phi ; dphi].
 #include <algorithm>
+#include <type_traits>
 
 #include "km_kernels.h"
+#include "km_kfun.cuh"
 
 namespace km {
 
@@ -515,122 +517,398 @@ void launch_d2_assemble(const double* M, int r, double* Tmul, double* Tmult, cud
 
 // ---------------------------------------------------------------------------------------------
 // Trace form of the stochastic gradient.  The gradient needs only the weighted sum over the
-// columns x_c of [T alpha] of x_c' dK_j x_c (weights w_c = 1/p for the probes, w = -1, or
-// -n / y'alpha for the profile likelihood, for alpha), never dK_j x_c itself.  Leaf by leaf,
-//   sum_c w_c x_c' dK_j x_c = <dK_j,leaf, G_leaf> + sum_c w_c (dphi_c' beta1_c + phi_c' beta2_c)
-// with the leaf Gram matrix G_leaf = sum_c w_c x_leaf,c x_leaf,c' (shared by the three
-// parameters), the leaf's own projections [phi ; dphi] and the landmark coefficients
-// [beta1 ; beta2] of the derivative product (k_dbeta).  This replaces three leaf products
-// dK_leaf X (m^2 k multiply-adds each) by one Gram matrix (m^2 k / 2) and three inner products.
+// columns x_c of X = [T alpha] of x_c' dK_j x_c (w_c = 1/p for the probes; wa = -1, or
+// -n / y'alpha for the profile likelihood, for alpha), never dK_j x_c itself.  Every
+// off-diagonal block of the Nystrom HODLR is Phi_c2 S^{-1} Phi_c1' with the one landmark set
+// (nystrom_uvt, src/factorizations.jl:86-94), so the matrix is
+//   K_H = Phi S^{-1} Phi' + sum_leaves (K_l - Phi_l S^{-1} Phi_l'),
+// and with A = Phi' x and B_j = dPhi_j' x for the whole vector, phi_l and dphi_l for leaf l,
+//   x' dK_j x = q_j(A, B_j) + sum_l [ x_l' dK_j,l x_l - q_j(phi_l, dphi_l) ],
+//   q_j(u, v) = 2 u~' v - u~' Sj u~,   u~ = S^{-1} u,   Sj = dK_j(P, P),
+// the same quantity as the reference's per-probe products summed over the probes
+// (stochasticgradient.jl:14-26).  Leaf terms: sum_c w_c x_l,c' dK_j,l x_l,c = <dK_j,l, G_l>,
+// with the leaf Gram matrix G_l formed tile by tile in registers and the three derivatives
+// evaluated on the fly (k_leaf_dk_gram); landmark terms: the projections [phi ; dphi_0 ;
+// dphi_1 ; dphi_2] of every (leaf, column) pair (k_leaf_proj4), their sums over the leaves
+// (k_proj_total) and the weighted quadratic forms (k_landmark).  No dK leaf, Gram matrix or
+// tree sweep is stored.
 // ---------------------------------------------------------------------------------------------
 
-// G_leaf (lower triangle, column-major at d_leaf_koff) = sum_{c < p} x_c x_c' / p + wa x_p x_p'
-// for the columns of X (n x (p + 1), leading dimension n; T = double, or float pairs for the
-// mixed form).  grid = (ntile, ntile, nleaf) over 32 x 32 tiles, tiles above the diagonal exit;
-// block (32, 8), thread (tx, ty) takes rows ti*32 + tx, columns tj*32 + ty + 8 q.
+// dPhi3[j n r + s r + c m + i] = dK_j(x_{s+i}, p_c) for the three parameters j (the panel layout
+// of Phi, three panels), float pairs in the mixed form.  grid (ceil(m r / 256), nleaf), block 256.
 template <typename T>
-__global__ void k_leaf_gram(const T* __restrict__ X, int64_t n, int p, double wa, DTree t, T* __restrict__ G) {
-  const int ti = blockIdx.x, tj = blockIdx.y;
-  if (ti < tj) return;
-  const int64_t leaf = blockIdx.z;
+__global__ void k_eval_dphi3(const double* __restrict__ pts, const double* __restrict__ lnd, int r, DTree t,
+                             KParams kp, T* __restrict__ dPhi3) {
+  extern __shared__ double sl[];  // 2r
+  for (int q = threadIdx.x; q < 2 * r; q += blockDim.x) sl[q] = lnd[q];
+  __syncthreads();
+  const int64_t leaf = blockIdx.y;
   const int m = d_leaf_size(t, leaf);
-  if (ti * 32 >= m) return;
   const int64_t s = d_leaf_start(t, leaf);
-  __shared__ T xr[32][33];
-  __shared__ T xc[32][33];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i = ti * 32 + tx;
-  acc_t<T> sp[4] = {}, sa[4] = {};
-  for (int c0 = 0; c0 <= p; c0 += 32) {
-    __syncthreads();
-    for (int e = ty * 32 + tx; e < 32 * 32; e += 256) {
-      const int cc = e >> 5, rr = e & 31;  // column cc of the chunk, row rr of the tile
-      const int c = c0 + cc;
-      const int ri = ti * 32 + rr, rj = tj * 32 + rr;
-      xr[rr][cc] = (c <= p && ri < m) ? X[(int64_t)c * n + s + ri] : T(0.0);
-      xc[rr][cc] = (c <= p && rj < m) ? X[(int64_t)c * n + s + rj] : T(0.0);
-    }
-    __syncthreads();
-    const int cend = min(32, p - c0);  // probe columns of this chunk; column p (alpha) apart
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int jl = ty + 8 * q;
-      for (int cc = 0; cc < cend; ++cc) sp[q] += xr[tx][cc] * xc[jl][cc];
-      if (p - c0 >= 0 && p - c0 < 32) sa[q] += xr[tx][p - c0] * xc[jl][p - c0];
-    }
-  }
-  const T wp = T(1.0) / T((double)p), w_a = T(wa);
-  T* Gl = G + d_leaf_koff(t, leaf);
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int a = tj * 32 + ty + 8 * q;
-    if (i < m && a < m && i >= a) {
-      const T v = (p > 0 ? T(accv(sp[q]) * wp) : T(0.0)) + T(accv(sa[q]) * w_a);
-      Gl[i + (int64_t)a * m] = v;
-    }
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)m * r) return;
+  const int c = (int)(e / m), i = (int)(e % m);
+  const double x = pts[2 * (s + i)], y = pts[2 * (s + i) + 1];
+  const int64_t o = s * r + (int64_t)c * m + i, nr = t.n * (int64_t)r;
+  if constexpr (std::is_same<T, ff>::value) {
+    ff v[3];
+    dkernel3_ff(kp, x, y, sl[2 * c], sl[2 * c + 1], v);
+    dPhi3[o] = v[0];
+    dPhi3[o + nr] = v[1];
+    dPhi3[o + 2 * nr] = v[2];
+  } else {
+    double v[3];
+    dkernel3(kp, x, y, sl[2 * c], sl[2 * c + 1], v);
+    dPhi3[o] = v[0];
+    dPhi3[o + nr] = v[1];
+    dPhi3[o + 2 * nr] = v[2];
   }
 }
 
-// partial[leaf] = <dK_leaf, G_leaf> (both symmetric: the lower triangle, off-diagonal entries
-// twice) + sum_c w_c (dphi_c' beta1_c + phi_c' beta2_c), in FP64 and a fixed order.
-// VP: the leaf slots of the projection sweep ([phi ; dphi], 2r per column), beta: [beta1 ;
-// beta2] per (leaf, column), k = p + 1 columns.  grid = nleaf, block 256.
+// VP[(leaf k + c) W + q], W = 4r: [Phi_l' x_c ; dPhi_0,l' x_c ; dPhi_1,l' x_c ; dPhi_2,l' x_c]
+// for a chunk of 8 columns.  The leaf rows go in chunks of 16: the rows of the four m x r panels
+// and of x are staged in shared memory as T, and thread q < W owns output row q with 8
+// accumulators (every staged panel entry feeds 8 multiply-adds).
+// grid (nleaf, ceil(k / 8)), block 32 ceil(W / 32) <= 320.
+constexpr int kPRows = 16;
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_leaf_grad_partial(const double* __restrict__ dK, const T* __restrict__ G,
-                                                           const double* __restrict__ VP, const T* __restrict__ beta,
-                                                           int r, int p, double wa, DTree t,
-                                                           double* __restrict__ partial) {
-  __shared__ double red[8];
+__global__ void __launch_bounds__(320) k_leaf_proj4(const T* __restrict__ Phi, const T* __restrict__ dPhi3, int r,
+                                                   DTree t, const double* __restrict__ X, int64_t ldx,
+                                                   double* __restrict__ VP, int k) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int W = 4 * r, ldp = W + 1;
+  T* xs = reinterpret_cast<T*>(smraw);  // kPRows x 8, [i][c]: 8 columns of a row in 16-byte pieces
+  T* ps = xs + kPRows * 8;              // kPRows x (W + 1)
   const int64_t leaf = blockIdx.x;
   const int m = d_leaf_size(t, leaf);
-  const int64_t ko = d_leaf_koff(t, leaf);
-  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  double acc = 0.0;
-  for (int a = w; a < m; a += 8) {  // warp per column, lanes over the rows i >= a
-    const double* dc = dK + ko + (int64_t)a * m;
-    const T* gc = G + ko + (int64_t)a * m;
-    for (int i = a + lane; i < m; i += 32) {
-      const double v = dc[i] * to_double(gc[i]);
-      acc += i > a ? 2.0 * v : v;
+  const int64_t s = d_leaf_start(t, leaf);
+  const int64_t nr = t.n * (int64_t)r;
+  const int c0 = blockIdx.y * 8;
+  const int nc = min(8, k - c0);
+  const int tid = threadIdx.x;
+  acc_t<T> acc[8] = {};
+  for (int i0 = 0; i0 < m; i0 += kPRows) {
+    const int rows = min(kPRows, m - i0);
+    __syncthreads();
+    for (int e = tid; e < rows * W; e += blockDim.x) {
+      const int q = e / rows, i = e - q * rows;
+      const int mat = q / r, col = q - mat * r;
+      const T* src = mat == 0 ? Phi : dPhi3 + (int64_t)(mat - 1) * nr;
+      ps[i * ldp + q] = src[s * r + (int64_t)col * m + i0 + i];
+    }
+    for (int e = tid; e < 8 * kPRows; e += blockDim.x) {
+      const int c = e / kPRows, i = e - c * kPRows;
+      xs[i * 8 + c] = (c < nc && i < rows) ? from_double<T>(X[(int64_t)(c0 + c) * ldx + s + i0 + i]) : T(0.0);
+    }
+    __syncthreads();
+    if (tid < W)
+      for (int i = 0; i < rows; ++i) {
+        const T a = ps[i * ldp + tid];
+        T xv[8];
+        load8(xs + i * 8, xv);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[c] += a * xv[c];
+      }
+  }
+  if (tid < W)
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (c < nc) VP[(leaf * k + c0 + c) * W + tid] = to_double(accv(acc[c]));
+}
+
+// VP[(nleaf k + c) W + q] = sum over the leaves of VP[(leaf k + c) W + q]: A and B_j of the
+// whole vector, in a fixed order (warp w sums the leaves w, w + 8, ..., then the eight warp sums
+// are added in order).  grid (k, ceil(W / 32)), block 256.
+__global__ void k_proj_total(double* __restrict__ VP, int W, int64_t nleaf, int k) {
+  __shared__ double red[8][32];
+  const int c = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int q = blockIdx.y * 32 + lane;
+  double s = 0.0;
+  if (q < W) {
+#pragma unroll 4
+    for (int64_t l = w; l < nleaf; l += 8) s += VP[(l * k + c) * W + q];
+  }
+  red[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && q < W) {
+    double tot = 0.0;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) tot += red[u][lane];
+    VP[(nleaf * k + c) * W + q] = tot;
+  }
+}
+
+// Weighted quadratic forms of one leaf (blockIdx.x < nleaf, sign -1) or of the whole vector
+// (blockIdx.x = nleaf: the sums of k_proj_total, sign +1):
+//   part[j (nleaf + 1) + l] = sign * sum_c w_c q_j(u_c, v_j,c) = sign * (2 D_j - <Sj, H>),
+//   D_j = sum_c w_c u~_c' v_j,c,  H = sum_c w_c u~_c u~_c',  u~ = S^{-1} u,
+// with u = VP[.. + 0 : r] and v_j = VP[.. + (j + 1) r : (j + 2) r].  Columns go in chunks of 16:
+// the chunk's projections (W x 16) and S^{-1} are staged in shared memory as T; thread
+// (cc = tid % 16, g = tid / 16) forms u~ for the rows g, g + 16, ... of column cc, and each thread
+// keeps up to 13 entries of the packed lower triangle of H (r <= 80) in registers.
+// grid nleaf + 1, block 256.
+constexpr int kLmCols = 16;
+constexpr int kLmH = (kMaxNysRank * (kMaxNysRank + 1) / 2 + 255) / 256;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_landmark(const double* __restrict__ VP, int r, int k, int p, double wa,
+                                                  const T* __restrict__ Sinv, const T* __restrict__ Sj3,
+                                                  int64_t nleaf, double* __restrict__ part) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int W = 4 * r, rr = r * r;
+  T* si = reinterpret_cast<T*>(smraw);  // r x r, S^{-1} (column-major), padded to an even count
+  T* vs = si + ((rr + 1) & ~1);         // W x 16, [q][cc] (16-byte aligned for load8)
+  T* ut = vs + W * kLmCols;             // r x 16, u~
+  T* uw = ut + r * kLmCols;             // r x 16, w_c u~
+  __shared__ double red[8][6];
+  const int64_t l = blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
+  const int cc = tid & (kLmCols - 1), g = tid / kLmCols;
+  const int nh = r * (r + 1) / 2;
+  for (int e = tid; e < rr; e += blockDim.x) si[e] = Sinv[e];
+  // the entries of H this thread owns: e = tid + 256 u, (i, a) with i >= a, packed by columns
+  int hi[kLmH], ha[kLmH];
+#pragma unroll
+  for (int u = 0; u < kLmH; ++u) {
+    int e = tid + 256 * u, a = 0;
+    if (e < nh) {
+      while (e >= r - a) {
+        e -= r - a;
+        ++a;
+      }
+      hi[u] = a + e;
+      ha[u] = a;
+    } else {
+      hi[u] = ha[u] = 0;
     }
   }
-  const int k = p + 1, r2 = 2 * r;
-  for (int c = w; c < k; c += 8) {  // warp per column, lanes over the r landmarks
-    const double* pv = VP + (leaf * k + c) * r2;
-    const T* bv = beta + (leaf * k + c) * r2;
-    double d = 0.0;
-    for (int q = lane; q < r; q += 32) d += pv[r + q] * to_double(bv[q]) + pv[q] * to_double(bv[r + q]);
-    d = warp_sum(d);
-    if (lane == 0) acc += (c < p ? 1.0 / (double)p : wa) * d;
+  acc_t<T> h[kLmH] = {};
+  acc_t<T> d[3] = {};
+  for (int c0 = 0; c0 < k; c0 += kLmCols) {
+    const int nc = min(kLmCols, k - c0);
+    __syncthreads();
+    for (int e = tid; e < W * kLmCols; e += blockDim.x) {
+      const int c = e / W, q = e - c * W;
+      vs[q * kLmCols + c] = c < nc ? from_double<T>(VP[(l * k + c0 + c) * W + q]) : T(0.0);
+    }
+    __syncthreads();
+    const int col = c0 + cc;
+    const T w = cc < nc ? from_double<T>(col < p ? 1.0 / (double)p : wa) : T(0.0);
+    for (int i = g; i < r; i += 256 / kLmCols) {
+      acc_t<T> a{};
+      for (int q = 0; q < r; ++q) a += si[i + q * r] * vs[q * kLmCols + cc];
+      const T v = accv(a);
+      const T vw = T(v * w);
+      ut[i * kLmCols + cc] = v;
+      uw[i * kLmCols + cc] = vw;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) d[j] += vw * vs[((j + 1) * r + i) * kLmCols + cc];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < kLmH; ++u)
+      if (tid + 256 * u < nh) {
+#pragma unroll
+        for (int q0 = 0; q0 < kLmCols; q0 += 8) {
+          T x[8], y[8];
+          load8(uw + hi[u] * kLmCols + q0, x);
+          load8(ut + ha[u] * kLmCols + q0, y);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) h[u] += x[q] * y[q];
+        }
+      }
   }
-  acc = warp_sum(acc);
-  if (lane == 0) red[w] = acc;
+  // <Sj, H>: off-diagonal entries twice (Sj and H symmetric)
+  double v[6];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    v[j] = to_double(accv(d[j]));
+    double qj = 0.0;
+#pragma unroll
+    for (int u = 0; u < kLmH; ++u)
+      if (tid + 256 * u < nh) {
+        const double hv = to_double(accv(h[u])) * (hi[u] == ha[u] ? 1.0 : 2.0);
+        qj += to_double(Sj3[(int64_t)j * rr + hi[u] + (int64_t)ha[u] * r]) * hv;
+      }
+    v[3 + j] = qj;
+  }
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const double sv = warp_sum(v[j]);
+    if (lane == 0) red[wp][j] = sv;
+  }
   __syncthreads();
-  if (tid == 0) {
-    double sum = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sum += red[q];
-    partial[leaf] = sum;
+  if (tid < 3) {
+    double dj = 0.0, qj = 0.0;
+    for (int u = 0; u < 8; ++u) {
+      dj += red[u][tid];
+      qj += red[u][3 + tid];
+    }
+    const double sign = l == nleaf ? 1.0 : -1.0;
+    part[tid * (nleaf + 1) + l] = sign * (2.0 * dj - qj);
   }
 }
 
+__device__ __forceinline__ double twice(double x) { return x + x; }
+__device__ __forceinline__ ff twice(ff x) { return ff(x.hi + x.hi, x.lo + x.lo); }
+
+// part[j nleaf + leaf] = <dK_j,leaf, G_leaf> for the three parameters, G_leaf = sum_{c < p} x_c x_c'
+// / p + wa x_p x_p' over the columns of X (n x (p + 1), leading dimension n; double, or float
+// pairs for the mixed form).  The CTA walks the lower-triangle 32 x 32 tiles of its leaf: the tile
+// of G from 32-column chunks of X staged in shared memory (thread (tx, ty) takes rows tx and
+// columns ty + 8 q), the derivative entries evaluated in registers (dkernel3 / dkernel3_ff, one
+// distance and one exponential for the three), off-diagonal entries counted twice.
+// grid nleaf, block (32, 8).
 template <typename T>
-void launch_leaf_gram(const T* X, int64_t n, int p, double wa, const Tree& t, T* G, cudaStream_t st) {
-  const int nt = (int)((t.max_leaf + 31) / 32);
-  k_leaf_gram<T><<<dim3(nt, nt, (unsigned)t.nleaf), dim3(32, 8), 0, st>>>(X, n, p, wa, dtree(t), G);
+__global__ void __launch_bounds__(256) k_leaf_dk_gram(const double* __restrict__ pts, KParams kp,
+                                                      const T* __restrict__ X, int64_t n, int p, double wa,
+                                                      DTree t, double* __restrict__ part) {
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf);
+  const int nt = (m + 31) / 32;
+  __shared__ T xr[32][33];
+  __shared__ T xc[32][33];
+  __shared__ double red[8][3];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
+  const T wp = from_double<T>(p > 0 ? 1.0 / (double)p : 0.0), w_a = from_double<T>(wa);
+  acc_t<T> tot[3] = {};
+  for (int ti = 0; ti < nt; ++ti)
+    for (int tj = 0; tj <= ti; ++tj) {
+      const int i = ti * 32 + tx;
+      acc_t<T> sp[4] = {}, sa[4] = {};
+      for (int c0 = 0; c0 <= p; c0 += 32) {
+        __syncthreads();
+        for (int e = tid; e < 32 * 32; e += 256) {
+          const int cq = e >> 5, rq = e & 31;  // column cq of the chunk, row rq of the tile
+          const int c = c0 + cq;
+          const int ri = ti * 32 + rq, rj = tj * 32 + rq;
+          xr[rq][cq] = (c <= p && ri < m) ? X[(int64_t)c * n + s + ri] : T(0.0);
+          xc[rq][cq] = (c <= p && rj < m) ? X[(int64_t)c * n + s + rj] : T(0.0);
+        }
+        __syncthreads();
+        const int cend = min(32, p - c0);  // probe columns of this chunk; column p (alpha) apart
+        for (int cq = 0; cq < cend; ++cq) {
+          const T a = xr[tx][cq];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) sp[q] += a * xc[ty + 8 * q][cq];
+        }
+        if (p - c0 < 32) {
+          const T a = xr[tx][p - c0];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) sa[q] += a * xc[ty + 8 * q][p - c0];
+        }
+      }
+      const double xi = i < m ? pts[2 * (s + i)] : 0.0, yi = i < m ? pts[2 * (s + i) + 1] : 0.0;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int a = tj * 32 + ty + 8 * q;
+        if (i < m && a < m && i >= a) {
+          T gv = T(accv(sp[q]) * wp) + T(accv(sa[q]) * w_a);
+          if (i > a) gv = twice(gv);
+          const double xa = pts[2 * (s + a)], ya = pts[2 * (s + a) + 1];
+          if constexpr (std::is_same<T, ff>::value) {
+            ff dk[3];
+            dkernel3_ff(kp, xi, yi, xa, ya, dk);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) tot[j] += gv * dk[j];
+          } else {
+            double dk[3];
+            dkernel3(kp, xi, yi, xa, ya, dk);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) tot[j] += gv * dk[j];
+          }
+        }
+      }
+    }
+  double v[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    v[j] = warp_sum(to_double(accv(tot[j])));
+    if (tx == 0) red[ty][j] = v[j];
+  }
+  __syncthreads();
+  if (tid < 3) {
+    double sum = 0.0;
+    for (int u = 0; u < 8; ++u) sum += red[u][tid];
+    part[tid * t.nleaf + leaf] = sum;
+  }
+}
+
+// out[j] = scale (sum_q a[j na + q] + sum_q b[j nb + q]), j < 3: thread tid adds the entries tid,
+// tid + 256, ... in order, then the 256 sums are added by a fixed tree.  grid 3, block 256.
+__global__ void k_grad_final(const double* __restrict__ a, int64_t na, const double* __restrict__ b, int64_t nb,
+                             double scale, double* __restrict__ out) {
+  __shared__ double red[256];
+  const int j = blockIdx.x, tid = threadIdx.x;
+  double s = 0.0;
+  for (int64_t q = tid; q < na; q += 256) s += a[j * na + q];
+  for (int64_t q = tid; q < nb; q += 256) s += b[j * nb + q];
+  red[tid] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (tid < o) red[tid] += red[tid + o];
+    __syncthreads();
+  }
+  if (tid == 0) out[j] = scale * red[0];
 }
 
 template <typename T>
-void launch_leaf_grad_partial(const double* dK, const T* G, const double* VP, const T* beta, int r, int p, double wa,
-                              const Tree& t, double* partial, cudaStream_t st) {
-  k_leaf_grad_partial<T><<<(unsigned)t.nleaf, 256, 0, st>>>(dK, G, VP, beta, r, p, wa, dtree(t), partial);
+void launch_eval_dphi3(const double* pts, const double* lnd, int r, const Tree& t, KParams kp, T* dPhi3,
+                       cudaStream_t st) {
+  dim3 grid((unsigned)((t.max_leaf * r + 255) / 256), (unsigned)t.nleaf);
+  k_eval_dphi3<T><<<grid, 256, 2 * r * sizeof(double), st>>>(pts, lnd, r, dtree(t), kp, dPhi3);
 }
 
-template void launch_leaf_gram<double>(const double*, int64_t, int, double, const Tree&, double*, cudaStream_t);
-template void launch_leaf_gram<ff>(const ff*, int64_t, int, double, const Tree&, ff*, cudaStream_t);
-template void launch_leaf_grad_partial<double>(const double*, const double*, const double*, const double*, int, int,
-                                               double, const Tree&, double*, cudaStream_t);
-template void launch_leaf_grad_partial<ff>(const double*, const ff*, const double*, const ff*, int, int, double,
-                                           const Tree&, double*, cudaStream_t);
+template <typename T>
+void launch_leaf_proj4(const T* Phi, const T* dPhi3, int r, const Tree& t, const double* X, int64_t ldx, double* VP,
+                      int k, cudaStream_t st) {
+  const int W = 4 * r;
+  dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
+  const size_t sm = (size_t)(kPRows * 8 + kPRows * (W + 1)) * sizeof(T);
+  smem_limit((const void*)k_leaf_proj4<T>, sm);
+  k_leaf_proj4<T><<<grid, 32 * ((W + 31) / 32), sm, st>>>(Phi, dPhi3, r, dtree(t), X, ldx, VP, k);
+}
+
+void launch_proj_total(double* VP, int W, int64_t nleaf, int k, cudaStream_t st) {
+  k_proj_total<<<dim3((unsigned)k, (unsigned)((W + 31) / 32)), 256, 0, st>>>(VP, W, nleaf, k);
+}
+
+template <typename T>
+void launch_landmark(const double* VP, int r, int k, int p, double wa, const T* Sinv, const T* Sj3, int64_t nleaf,
+                     double* part, cudaStream_t st) {
+  const size_t sm = (size_t)(((r * r + 1) & ~1) + 4 * r * kLmCols + 2 * r * kLmCols) * sizeof(T);
+  smem_limit((const void*)k_landmark<T>, sm);
+  k_landmark<T><<<(unsigned)(nleaf + 1), 256, sm, st>>>(VP, r, k, p, wa, Sinv, Sj3, nleaf, part);
+}
+
+template <typename T>
+void launch_leaf_dk_gram(const double* pts, KParams kp, const T* X, int64_t n, int p, double wa, const Tree& t,
+                         double* part, cudaStream_t st) {
+  k_leaf_dk_gram<T><<<(unsigned)t.nleaf, dim3(32, 8), 0, st>>>(pts, kp, X, n, p, wa, dtree(t), part);
+}
+
+void launch_grad_final(const double* a, int64_t na, const double* b, int64_t nb, double scale, double* out,
+                       cudaStream_t st) {
+  k_grad_final<<<3, 256, 0, st>>>(a, na, b, nb, scale, out);
+}
+
+template void launch_eval_dphi3<double>(const double*, const double*, int, const Tree&, KParams, double*,
+                                        cudaStream_t);
+template void launch_eval_dphi3<ff>(const double*, const double*, int, const Tree&, KParams, ff*, cudaStream_t);
+template void launch_leaf_proj4<double>(const double*, const double*, int, const Tree&, const double*, int64_t,
+                                        double*, int, cudaStream_t);
+template void launch_leaf_proj4<ff>(const ff*, const ff*, int, const Tree&, const double*, int64_t, double*, int,
+                                    cudaStream_t);
+template void launch_landmark<double>(const double*, int, int, int, double, const double*, const double*, int64_t,
+                                      double*, cudaStream_t);
+template void launch_landmark<ff>(const double*, int, int, int, double, const ff*, const ff*, int64_t, double*,
+                                  cudaStream_t);
+template void launch_leaf_dk_gram<double>(const double*, KParams, const double*, int64_t, int, double, const Tree&,
+                                          double*, cudaStream_t);
+template void launch_leaf_dk_gram<ff>(const double*, KParams, const ff*, int64_t, int, double, const Tree&, double*,
+                                      cudaStream_t);
 
 void launch_small_gemm(const double* A, const double* B, int r, int transB, double* C, cudaStream_t st) {
   k_small_gemm<<<r, 128, 0, st>>>(A, B, r, transB, C);

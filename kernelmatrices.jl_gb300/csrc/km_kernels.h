@@ -172,14 +172,24 @@ void launch_small_gemm(const double* A, const double* B, int r, int transB, doub
 template <typename T>
 void launch_dbeta(const T* Sinv, const T* M2, int r, const double* VG, int64_t npairs, T* beta, cudaStream_t st);
 void launch_axpby(double* y, const double* x, double a, double b, int64_t n, cudaStream_t st);
-// trace form of the stochastic gradient (km_grad.cu): the leaf Gram matrices of the columns of X
-// (n x (p + 1): p probes with weight 1/p, then alpha with weight wa), and per leaf
-// <dK_leaf, G_leaf> + sum_c w_c (dphi_c' beta1_c + phi_c' beta2_c)
+// trace form of the stochastic gradient (km_grad.cu).  X: n x k (k = p + 1: p probes with weight
+// 1/p, then alpha with weight wa); W = 4r projection rows per (leaf, column) pair.
 template <typename T>
-void launch_leaf_gram(const T* X, int64_t n, int p, double wa, const Tree& t, T* G, cudaStream_t st);
+void launch_eval_dphi3(const double* pts, const double* lnd, int r, const Tree& t, KParams kp, T* dPhi3,
+                       cudaStream_t st);
 template <typename T>
-void launch_leaf_grad_partial(const double* dK, const T* G, const double* VP, const T* beta, int r, int p, double wa,
-                              const Tree& t, double* partial, cudaStream_t st);
+void launch_leaf_proj4(const T* Phi, const T* dPhi3, int r, const Tree& t, const double* X, int64_t ldx, double* VP,
+                      int k, cudaStream_t st);
+void launch_proj_total(double* VP, int W, int64_t nleaf, int k, cudaStream_t st);
+template <typename T>
+void launch_landmark(const double* VP, int r, int k, int p, double wa, const T* Sinv, const T* Sj3, int64_t nleaf,
+                     double* part, cudaStream_t st);
+template <typename T>
+void launch_leaf_dk_gram(const double* pts, KParams kp, const T* X, int64_t n, int p, double wa, const Tree& t,
+                         double* part, cudaStream_t st);
+// out[j] = scale * (sum_q a[j * na + q] + sum_q b[j * nb + q]) for j < 3, fixed order
+void launch_grad_final(const double* a, int64_t na, const double* b, int64_t nb, double scale, double* out,
+                       cudaStream_t st);
 // n x p Rademacher probes (+-1), entry (i, j) from a SplitMix64 hash of (seed, j*n + i)
 void launch_rademacher(double* out, int64_t n, int64_t p, uint64_t seed, cudaStream_t st);
 void launch_col_dots(const double* A, int64_t lda, const double* B, int64_t ldb, int64_t n, int k,
