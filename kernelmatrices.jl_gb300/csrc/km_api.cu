@@ -180,7 +180,7 @@ struct km_handle {
   double* d_hA = nullptr;     // a_j = dK_j u and b_j = K^{-1} a_j (6 n)
   double* d_hY = nullptr;     // second-derivative products of [W'^{-1} V | u]
   double* d_hdots = nullptr;
-  double* d_dPhi3 = nullptr;  // trace-form gradient: dK_j(X, P) for j = 0, 1, 2 (float pairs when mixed)
+  double* d_dPhi2 = nullptr;  // trace-form gradient: dK_j(X, P) for j = 0, 1 (float pairs when mixed)
   double* d_Sj3 = nullptr;    // dK_j(P, P), j = 0, 1, 2
   double* d_Sj3F = nullptr;   // float-pair copy (mixed form)
   double* d_VP4 = nullptr;    // projections [phi ; dphi_0 ; dphi_1 ; dphi_2] per (leaf, column), then the sums
@@ -348,7 +348,7 @@ void free_problem(km_handle* h) {
   h->d_Sinv = h->d_SinvF = h->d_M2 = h->d_M2F = h->d_Mtmp = h->d_GB = nullptr;
   h->gcap = h->tcap = 0;
   h->d_res = h->d_rdots = nullptr;
-  h->d_dPhi3 = h->d_Sj3 = h->d_Sj3F = h->d_VP4 = h->d_gpart = nullptr;
+  h->d_dPhi2 = h->d_Sj3 = h->d_Sj3F = h->d_VP4 = h->d_gpart = nullptr;
   h->rcap = 0;
   h->d2_pair = -1;
   h->d_hPhi3 = h->d_hD2 = h->d_hS = h->d_hT = h->d_hP = h->d_hG = h->d_hA = h->d_hY = h->d_hdots = nullptr;
@@ -1953,15 +1953,16 @@ static int gradient_trace(km_handle* h, int64_t p, double wa, double* grad) {
   const int64_t n = t.n, kk = p + 1, W = 4 * r;
   cudaStream_t st = h->stream;
   int rc;
-  if ((rc = grow(h, &h->d_dPhi3, 3 * t.n * r)) || (rc = grow(h, &h->d_Sj3, 3 * r * r)) ||
+  const int64_t nlp = t.nleaf * leaf_dk_gram_parts(t);  // partial sums of the leaf term
+  if ((rc = grow(h, &h->d_dPhi2, 2 * t.n * r)) || (rc = grow(h, &h->d_Sj3, 3 * r * r)) ||
       (rc = grow(h, &h->d_Sinv, r * r)) || (rc = grow(h, &h->d_VP4, (t.nleaf + 1) * kk * W)) ||
-      (rc = grow(h, &h->d_gpart, 3 * t.nleaf + 3 * (t.nleaf + 1) + 3)))
+      (rc = grow(h, &h->d_gpart, 3 * nlp + 3 * (t.nleaf + 1) + 3)))
     return rc;
   if (h->mixed && ((rc = grow(h, &h->d_Phif, t.n * r)) || (rc = grow(h, &h->d_SinvF, r * r)) ||
                    (rc = grow(h, &h->d_Sj3F, 3 * r * r))))
     return rc;
   double* leafpart = h->d_gpart;
-  double* lmpart = h->d_gpart + 3 * t.nleaf;
+  double* lmpart = h->d_gpart + 3 * nlp;
   double* sums = lmpart + 3 * (t.nleaf + 1);
   // DerivativeHODLR (constructor.jl:66-95) for the three parameters: dK(X, P) and Sj = dK(P, P);
   // the dK leaves are evaluated inside the leaf kernel
@@ -1972,22 +1973,23 @@ static int gradient_trace(km_handle* h, int64_t p, double wa, double* grad) {
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Phif), t.n * r, st));
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Sinv, P<ff>(h->d_SinvF), (int64_t)r * r, st));
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Sj3, P<ff>(h->d_Sj3F), (int64_t)3 * r * r, st));
-    KLV(h, KM_PROF_EVAL, launch_eval_dphi3<ff>(h->d_pts, h->d_lnd, r, t, h->kp, P<ff>(h->d_dPhi3), st));
+    KLV(h, KM_PROF_EVAL, launch_eval_dphi2<ff>(h->d_pts, h->d_lnd, r, t, h->kp, P<ff>(h->d_dPhi2), st));
     // X in float pairs (d_U is free here: no product dK X is formed)
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_T, P<ff>(h->d_U), n * kk, st));
     KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dk_gram<ff>(h->d_pts, h->kp, P<ff>(h->d_U), n, (int)p, wa, t, leafpart, st));
   } else {
-    KLV(h, KM_PROF_EVAL, launch_eval_dphi3<double>(h->d_pts, h->d_lnd, r, t, h->kp, h->d_dPhi3, st));
+    KLV(h, KM_PROF_EVAL, launch_eval_dphi2<double>(h->d_pts, h->d_lnd, r, t, h->kp, h->d_dPhi2, st));
     KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dk_gram<double>(h->d_pts, h->kp, h->d_T, n, (int)p, wa, t, leafpart, st));
   }
   if (t.L > 0) {
     if (h->mixed) {
       KLV(h, KM_PROF_LEAF_APPLY,
-          launch_leaf_proj4<ff>(P<ff>(h->d_Phif), P<ff>(h->d_dPhi3), r, t, h->d_T, n, h->d_VP4, (int)kk, st));
+          launch_leaf_proj3<ff>(P<ff>(h->d_Phif), P<ff>(h->d_dPhi2), r, t, P<ff>(h->d_U), n, h->d_VP4, (int)kk, st));
     } else {
       KLV(h, KM_PROF_LEAF_APPLY,
-          launch_leaf_proj4<double>(h->d_Phi, h->d_dPhi3, r, t, h->d_T, n, h->d_VP4, (int)kk, st));
+          launch_leaf_proj3<double>(h->d_Phi, h->d_dPhi2, r, t, h->d_T, n, h->d_VP4, (int)kk, st));
     }
+    KLV(h, KM_PROF_LEAF_APPLY, launch_nugget_proj(h->d_pts, h->d_lnd, r, t, h->d_T, n, h->d_VP4, (int)kk, st));
     KLV(h, KM_PROF_OTHER, launch_proj_total(h->d_VP4, (int)W, t.nleaf, (int)kk, st));
     if (h->mixed)
       KLV(h, KM_PROF_LEAF_APPLY, launch_landmark<ff>(h->d_VP4, r, (int)kk, (int)p, wa, P<ff>(h->d_SinvF),
@@ -1999,7 +2001,7 @@ static int gradient_trace(km_handle* h, int64_t p, double wa, double* grad) {
     // a single leaf: no off-diagonal block, no landmark term
     KM_CUDA(h, cudaMemsetAsync(lmpart, 0, sizeof(double) * 3 * (t.nleaf + 1), st));
   }
-  KLV(h, KM_PROF_OTHER, launch_grad_final(leafpart, t.nleaf, lmpart, t.nleaf + 1, 0.5, sums, st));
+  KLV(h, KM_PROF_OTHER, launch_grad_final(leafpart, nlp, lmpart, t.nleaf + 1, 0.5, sums, st));
   KM_CUDA(h, cudaMemcpyAsync(grad, sums, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
   return sync(h, "gradient");
 }
@@ -2379,9 +2381,9 @@ extern "C" int64_t km_estimate_bytes(int64_t n, int64_t rank, int level_kind, in
   b += 2 * d(n * k);                              // ensure_xy
   if (leaf_tc_enabled() && leaf_chol_tc_supported(t, (int)r))  // slices of the tensor-core leaf stage
     b += leaf_chol_tc_scratch_bytes(t, (int)r);
-  if (with_grad)  // trace-form gradient: [T alpha] and its float-pair copy, dK_j(X, P) for the three
-                  // parameters, the float-pair Phi, S^{-1} and Sj, the projections, the partial sums
-    b += 2 * d(n * k) + d(k) + d(3 * n * r) + d(n * r) + 2 * d(3 * r * r) + 2 * d(r * r) +
-         d((t.nleaf + 1) * k * 4 * r) + d(6 * t.nleaf + 6);
+  if (with_grad)  // trace-form gradient: [T alpha] and its float-pair copy, dK_j(X, P) for the scale
+                  // and range, the float-pair Phi, S^{-1} and Sj, the projections, the partial sums
+    b += 2 * d(n * k) + d(k) + d(2 * n * r) + d(n * r) + 2 * d(3 * r * r) + 2 * d(r * r) +
+         d((t.nleaf + 1) * k * 4 * r) + d(3 * t.nleaf * leaf_dk_gram_parts(t) + 3 * t.nleaf + 6);
   return b;
 }

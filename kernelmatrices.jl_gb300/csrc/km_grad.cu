@@ -529,16 +529,17 @@ void launch_d2_assemble(const double* M, int r, double* Tmul, double* Tmult, cud
 // (stochasticgradient.jl:14-26).  Leaf terms: sum_c w_c x_l,c' dK_j,l x_l,c = <dK_j,l, G_l>,
 // with the leaf Gram matrix G_l formed tile by tile in registers and the three derivatives
 // evaluated on the fly (k_leaf_dk_gram); landmark terms: the projections [phi ; dphi_0 ;
-// dphi_1 ; dphi_2] of every (leaf, column) pair (k_leaf_proj4), their sums over the leaves
+// dphi_1 ; dphi_2] of every (leaf, column) pair (k_leaf_proj3, k_nugget_proj), their sums over the leaves
 // (k_proj_total) and the weighted quadratic forms (k_landmark).  No dK leaf, Gram matrix or
 // tree sweep is stored.
 // ---------------------------------------------------------------------------------------------
 
-// dPhi3[j n r + s r + c m + i] = dK_j(x_{s+i}, p_c) for the three parameters j (the panel layout
-// of Phi, three panels), float pairs in the mixed form.  grid (ceil(m r / 256), nleaf), block 256.
+// dPhi2[j n r + s r + c m + i] = dK_j(x_{s+i}, p_c) for the scale and range parameters j = 0, 1
+// (the panel layout of Phi, two panels), float pairs in the mixed form.  The nugget derivative
+// [x == p] is handled by k_nugget_proj.  grid (ceil(m r / 256), nleaf), block 256.
 template <typename T>
-__global__ void k_eval_dphi3(const double* __restrict__ pts, const double* __restrict__ lnd, int r, DTree t,
-                             KParams kp, T* __restrict__ dPhi3) {
+__global__ void k_eval_dphi2(const double* __restrict__ pts, const double* __restrict__ lnd, int r, DTree t,
+                             KParams kp, T* __restrict__ dPhi2) {
   extern __shared__ double sl[];  // 2r
   for (int q = threadIdx.x; q < 2 * r; q += blockDim.x) sl[q] = lnd[q];
   __syncthreads();
@@ -553,68 +554,109 @@ __global__ void k_eval_dphi3(const double* __restrict__ pts, const double* __res
   if constexpr (std::is_same<T, ff>::value) {
     ff v[3];
     dkernel3_ff(kp, x, y, sl[2 * c], sl[2 * c + 1], v);
-    dPhi3[o] = v[0];
-    dPhi3[o + nr] = v[1];
-    dPhi3[o + 2 * nr] = v[2];
+    dPhi2[o] = v[0];
+    dPhi2[o + nr] = v[1];
   } else {
     double v[3];
     dkernel3(kp, x, y, sl[2 * c], sl[2 * c + 1], v);
-    dPhi3[o] = v[0];
-    dPhi3[o + nr] = v[1];
-    dPhi3[o + 2 * nr] = v[2];
+    dPhi2[o] = v[0];
+    dPhi2[o + nr] = v[1];
   }
 }
 
-// VP[(leaf k + c) W + q], W = 4r: [Phi_l' x_c ; dPhi_0,l' x_c ; dPhi_1,l' x_c ; dPhi_2,l' x_c]
-// for a chunk of 8 columns.  The leaf rows go in chunks of 16: the rows of the four m x r panels
-// and of x are staged in shared memory as T, and thread q < W owns output row q with 8
-// accumulators (every staged panel entry feeds 8 multiply-adds).
-// grid (nleaf, ceil(k / 8)), block 32 ceil(W / 32) <= 320.
-constexpr int kPRows = 16;
+// VP[(leaf k + c) W + mat r + q] = sum_i A_mat[i][q] X[i][c]: the projections phi = Phi_l' x_c,
+// dphi_0 = dPhi_0,l' x_c and dphi_1 = dPhi_1,l' x_c (W = 4r; the nugget block mat = 3 comes from
+// k_nugget_proj), one small GEMM per (leaf, matrix), register-tiled.  A CTA takes the r rows of
+// matrix mat = blockIdx.y and 8g columns (g <= 10); thread (u, v) = (tid % uq, tid / uq),
+// uq = ceil(r / 4), accumulates the 4 x 8 block q = u + uq a, c = c0 + v + g b (strided, so that
+// the shared-memory reads of a warp fall in distinct banks).  The leaf rows go in chunks of 32:
+// A_mat (r x 32) and X (8g x 32) are staged in shared memory as T along i with a padded stride;
+// rows past the leaf are zeros.  grid (nleaf, 3, ceil(k / 8g)), block uq g.
+constexpr int kPjK = 32, kPjS = kPjK + 1, kPjMaxG = 10, kPjMaxU = (kMaxNysRank + 3) / 4;
 
 template <typename T>
-__global__ void __launch_bounds__(320) k_leaf_proj4(const T* __restrict__ Phi, const T* __restrict__ dPhi3, int r,
-                                                   DTree t, const double* __restrict__ X, int64_t ldx,
-                                                   double* __restrict__ VP, int k) {
+__global__ void __launch_bounds__(kPjMaxU * kPjMaxG, 2)
+    k_leaf_proj3(const T* __restrict__ Phi, const T* __restrict__ dPhi2, int r, DTree t, const T* __restrict__ X,
+                 int64_t ldx, double* __restrict__ VP, int k, int g) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int W = 4 * r, ldp = W + 1;
-  T* xs = reinterpret_cast<T*>(smraw);  // kPRows x 8, [i][c]: 8 columns of a row in 16-byte pieces
-  T* ps = xs + kPRows * 8;              // kPRows x (W + 1)
+  const int uq = (r + 3) / 4;
+  T* As = reinterpret_cast<T*>(smraw);  // 4 uq x kPjS, [q][i]
+  T* Xs = As + 4 * uq * kPjS;           // 8g x kPjS, [c][i]
   const int64_t leaf = blockIdx.x;
   const int m = d_leaf_size(t, leaf);
   const int64_t s = d_leaf_start(t, leaf);
-  const int64_t nr = t.n * (int64_t)r;
-  const int c0 = blockIdx.y * 8;
-  const int nc = min(8, k - c0);
-  const int tid = threadIdx.x;
-  acc_t<T> acc[8] = {};
-  for (int i0 = 0; i0 < m; i0 += kPRows) {
-    const int rows = min(kPRows, m - i0);
+  const int mat = blockIdx.y;
+  const T* A = (mat == 0 ? Phi : dPhi2 + (int64_t)(mat - 1) * t.n * r) + s * r;
+  const int W = 4 * r;
+  const int c0 = blockIdx.z * 8 * g;
+  const int ncol = min(8 * g, k - c0);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int u = tid % uq, v = tid / uq;
+  acc_t<T> acc[4][8] = {};
+  for (int i0 = 0; i0 < m; i0 += kPjK) {
+    const int rows = min(kPjK, m - i0);
     __syncthreads();
-    for (int e = tid; e < rows * W; e += blockDim.x) {
-      const int q = e / rows, i = e - q * rows;
-      const int mat = q / r, col = q - mat * r;
-      const T* src = mat == 0 ? Phi : dPhi3 + (int64_t)(mat - 1) * nr;
-      ps[i * ldp + q] = src[s * r + (int64_t)col * m + i0 + i];
+    for (int e = tid; e < 4 * uq * kPjK; e += nth) {
+      const int q = e / kPjK, i = e - q * kPjK;
+      As[q * kPjS + i] = (q < r && i < rows) ? A[(int64_t)q * m + i0 + i] : T(0.0);
     }
-    for (int e = tid; e < 8 * kPRows; e += blockDim.x) {
-      const int c = e / kPRows, i = e - c * kPRows;
-      xs[i * 8 + c] = (c < nc && i < rows) ? from_double<T>(X[(int64_t)(c0 + c) * ldx + s + i0 + i]) : T(0.0);
+    for (int e = tid; e < 8 * g * kPjK; e += nth) {
+      const int cl = e / kPjK, i = e - cl * kPjK;
+      Xs[cl * kPjS + i] = (cl < ncol && i < rows) ? X[(int64_t)(c0 + cl) * ldx + s + i0 + i] : T(0.0);
     }
     __syncthreads();
-    if (tid < W)
-      for (int i = 0; i < rows; ++i) {
-        const T a = ps[i * ldp + tid];
-        T xv[8];
-        load8(xs + i * 8, xv);
+#pragma unroll 2
+    for (int i = 0; i < kPjK; ++i) {
+      T av[4], xv[8];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) acc[c] += a * xv[c];
-      }
+      for (int a = 0; a < 4; ++a) av[a] = As[(u + uq * a) * kPjS + i];
+#pragma unroll
+      for (int b = 0; b < 8; ++b) xv[b] = Xs[(v + g * b) * kPjS + i];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] += av[a] * xv[b];
+    }
   }
-  if (tid < W)
 #pragma unroll
-    for (int c = 0; c < 8; ++c)
-      if (c < nc) VP[(leaf * k + c0 + c) * W + tid] = to_double(accv(acc[c]));
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int q = u + uq * a, cl = v + g * b;
+      if (q < r && cl < ncol) VP[(leaf * k + c0 + cl) * W + mat * r + q] = to_double(accv(acc[a][b]));
+    }
+}
+
+// VP[(leaf k + c) W + 3r + q] = sum over the leaf's points x_i equal to landmark p_q (coordinate by
+// coordinate) of X[i][c]: the projection on the nugget derivative dK_2(X, P) = [x == p], a
+// 0/1 matrix with at most one entry per row for distinct points.  Thread q scans the leaf once;
+// a landmark with several equal points (repeated points) rescans it per column, in order.
+// grid nleaf, block 32 ceil(r / 32).
+__global__ void k_nugget_proj(const double* __restrict__ pts, const double* __restrict__ lnd, int r, DTree t,
+                              const double* __restrict__ X, int64_t ldx, double* __restrict__ VP, int k) {
+  const int q = threadIdx.x;
+  if (q >= r) return;
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf);
+  const int W = 4 * r;
+  const double px = lnd[2 * q], py = lnd[2 * q + 1];
+  int first = -1, cnt = 0;
+  for (int i = 0; i < m; ++i)
+    if (pts[2 * (s + i)] == px && pts[2 * (s + i) + 1] == py) {
+      if (first < 0) first = i;
+      ++cnt;
+    }
+  for (int c = 0; c < k; ++c) {
+    double v = 0.0;
+    if (cnt == 1) {
+      v = X[(int64_t)c * ldx + s + first];
+    } else if (cnt > 1) {
+      for (int i = first; i < m; ++i)
+        if (pts[2 * (s + i)] == px && pts[2 * (s + i) + 1] == py) v += X[(int64_t)c * ldx + s + i];
+    }
+    VP[(leaf * k + c) * W + 3 * r + q] = v;
+  }
 }
 
 // VP[(nleaf k + c) W + q] = sum over the leaves of VP[(leaf k + c) W + q]: A and B_j of the
@@ -649,6 +691,7 @@ __global__ void k_proj_total(double* __restrict__ VP, int W, int64_t nleaf, int 
 // keeps up to 13 entries of the packed lower triangle of H (r <= 80) in registers.
 // grid nleaf + 1, block 256.
 constexpr int kLmCols = 16;
+constexpr int kLmS = kLmCols + 2;  // padded row stride of u~: the rows of a quarter warp start in distinct banks
 constexpr int kLmH = (kMaxNysRank * (kMaxNysRank + 1) / 2 + 255) / 256;
 
 template <typename T>
@@ -659,8 +702,8 @@ __global__ void __launch_bounds__(256) k_landmark(const double* __restrict__ VP,
   const int W = 4 * r, rr = r * r;
   T* si = reinterpret_cast<T*>(smraw);  // r x r, S^{-1} (column-major), padded to an even count
   T* vs = si + ((rr + 1) & ~1);         // W x 16, [q][cc] (16-byte aligned for load8)
-  T* ut = vs + W * kLmCols;             // r x 16, u~
-  T* uw = ut + r * kLmCols;             // r x 16, w_c u~
+  T* ut = vs + W * kLmCols;             // r x 16 (row stride kLmS), u~
+  T* uw = ut + r * kLmS;                // r x 16 (row stride kLmS), w_c u~
   __shared__ double red[8][6];
   const int64_t l = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, wp = tid >> 5;
@@ -700,8 +743,8 @@ __global__ void __launch_bounds__(256) k_landmark(const double* __restrict__ VP,
       for (int q = 0; q < r; ++q) a += si[i + q * r] * vs[q * kLmCols + cc];
       const T v = accv(a);
       const T vw = T(v * w);
-      ut[i * kLmCols + cc] = v;
-      uw[i * kLmCols + cc] = vw;
+      ut[i * kLmS + cc] = v;
+      uw[i * kLmS + cc] = vw;
 #pragma unroll
       for (int j = 0; j < 3; ++j) d[j] += vw * vs[((j + 1) * r + i) * kLmCols + cc];
     }
@@ -712,8 +755,8 @@ __global__ void __launch_bounds__(256) k_landmark(const double* __restrict__ VP,
 #pragma unroll
         for (int q0 = 0; q0 < kLmCols; q0 += 8) {
           T x[8], y[8];
-          load8(uw + hi[u] * kLmCols + q0, x);
-          load8(ut + ha[u] * kLmCols + q0, y);
+          load8(uw + hi[u] * kLmS + q0, x);
+          load8(ut + ha[u] * kLmS + q0, y);
 #pragma unroll
           for (int q = 0; q < 8; ++q) h[u] += x[q] * y[q];
         }
@@ -753,13 +796,14 @@ __global__ void __launch_bounds__(256) k_landmark(const double* __restrict__ VP,
 __device__ __forceinline__ double twice(double x) { return x + x; }
 __device__ __forceinline__ ff twice(ff x) { return ff(x.hi + x.hi, x.lo + x.lo); }
 
-// part[j nleaf + leaf] = <dK_j,leaf, G_leaf> for the three parameters, G_leaf = sum_{c < p} x_c x_c'
+// part[j nleaf S + leaf S + z] = part z < S of <dK_j,leaf, G_leaf> for the three parameters, G_leaf = sum_{c < p} x_c x_c'
 // / p + wa x_p x_p' over the columns of X (n x (p + 1), leading dimension n; double, or float
-// pairs for the mixed form).  The CTA walks the lower-triangle 32 x 32 tiles of its leaf: the tile
+// pairs for the mixed form).  CTA (leaf, z) walks the lower-triangle 32 x 32 tiles z, z + S, ... of
+// its leaf (numbered row by row): the tile
 // of G from 32-column chunks of X staged in shared memory (thread (tx, ty) takes rows tx and
 // columns ty + 8 q), the derivative entries evaluated in registers (dkernel3 / dkernel3_ff, one
 // distance and one exponential for the three), off-diagonal entries counted twice.
-// grid nleaf, block (32, 8).
+// grid (nleaf, S), block (32, 8).
 template <typename T>
 __global__ void __launch_bounds__(256) k_leaf_dk_gram(const double* __restrict__ pts, KParams kp,
                                                       const T* __restrict__ X, int64_t n, int p, double wa,
@@ -774,8 +818,14 @@ __global__ void __launch_bounds__(256) k_leaf_dk_gram(const double* __restrict__
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * 32 + tx;
   const T wp = from_double<T>(p > 0 ? 1.0 / (double)p : 0.0), w_a = from_double<T>(wa);
   acc_t<T> tot[3] = {};
-  for (int ti = 0; ti < nt; ++ti)
-    for (int tj = 0; tj <= ti; ++tj) {
+  const int z = blockIdx.y, S = gridDim.y;
+  int ti = 0, tj = z;  // tile number z: row ti, column tj <= ti
+  while (tj > ti) {
+    tj -= ti + 1;
+    ++ti;
+  }
+  for (; ti < nt;) {
+    {
       const int i = ti * 32 + tx;
       acc_t<T> sp[4] = {}, sa[4] = {};
       for (int c0 = 0; c0 <= p; c0 += 32) {
@@ -822,6 +872,12 @@ __global__ void __launch_bounds__(256) k_leaf_dk_gram(const double* __restrict__
         }
       }
     }
+    tj += S;  // the next tile of this part
+    while (tj > ti) {
+      tj -= ti + 1;
+      ++ti;
+    }
+  }
   double v[3];
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
@@ -832,7 +888,7 @@ __global__ void __launch_bounds__(256) k_leaf_dk_gram(const double* __restrict__
   if (tid < 3) {
     double sum = 0.0;
     for (int u = 0; u < 8; ++u) sum += red[u][tid];
-    part[tid * t.nleaf + leaf] = sum;
+    part[(int64_t)tid * t.nleaf * S + leaf * S + z] = sum;
   }
 }
 
@@ -855,20 +911,25 @@ __global__ void k_grad_final(const double* __restrict__ a, int64_t na, const dou
 }
 
 template <typename T>
-void launch_eval_dphi3(const double* pts, const double* lnd, int r, const Tree& t, KParams kp, T* dPhi3,
+void launch_eval_dphi2(const double* pts, const double* lnd, int r, const Tree& t, KParams kp, T* dPhi2,
                        cudaStream_t st) {
   dim3 grid((unsigned)((t.max_leaf * r + 255) / 256), (unsigned)t.nleaf);
-  k_eval_dphi3<T><<<grid, 256, 2 * r * sizeof(double), st>>>(pts, lnd, r, dtree(t), kp, dPhi3);
+  k_eval_dphi2<T><<<grid, 256, 2 * r * sizeof(double), st>>>(pts, lnd, r, dtree(t), kp, dPhi2);
 }
 
 template <typename T>
-void launch_leaf_proj4(const T* Phi, const T* dPhi3, int r, const Tree& t, const double* X, int64_t ldx, double* VP,
-                      int k, cudaStream_t st) {
-  const int W = 4 * r;
-  dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
-  const size_t sm = (size_t)(kPRows * 8 + kPRows * (W + 1)) * sizeof(T);
-  smem_limit((const void*)k_leaf_proj4<T>, sm);
-  k_leaf_proj4<T><<<grid, 32 * ((W + 31) / 32), sm, st>>>(Phi, dPhi3, r, dtree(t), X, ldx, VP, k);
+void launch_leaf_proj3(const T* Phi, const T* dPhi2, int r, const Tree& t, const T* X, int64_t ldx, double* VP, int k,
+                       cudaStream_t st) {
+  const int g = std::min(kPjMaxG, (k + 7) / 8), uq = (r + 3) / 4;
+  dim3 grid((unsigned)t.nleaf, 3u, (unsigned)((k + 8 * g - 1) / (8 * g)));
+  const size_t sm = (size_t)(4 * uq + 8 * g) * kPjS * sizeof(T);
+  smem_limit((const void*)k_leaf_proj3<T>, sm);
+  k_leaf_proj3<T><<<grid, uq * g, sm, st>>>(Phi, dPhi2, r, dtree(t), X, ldx, VP, k, g);
+}
+
+void launch_nugget_proj(const double* pts, const double* lnd, int r, const Tree& t, const double* X, int64_t ldx,
+                        double* VP, int k, cudaStream_t st) {
+  k_nugget_proj<<<(unsigned)t.nleaf, 32 * ((r + 31) / 32), 0, st>>>(pts, lnd, r, dtree(t), X, ldx, VP, k);
 }
 
 void launch_proj_total(double* VP, int W, int64_t nleaf, int k, cudaStream_t st) {
@@ -878,15 +939,22 @@ void launch_proj_total(double* VP, int W, int64_t nleaf, int k, cudaStream_t st)
 template <typename T>
 void launch_landmark(const double* VP, int r, int k, int p, double wa, const T* Sinv, const T* Sj3, int64_t nleaf,
                      double* part, cudaStream_t st) {
-  const size_t sm = (size_t)(((r * r + 1) & ~1) + 4 * r * kLmCols + 2 * r * kLmCols) * sizeof(T);
+  const size_t sm = (size_t)(((r * r + 1) & ~1) + 4 * r * kLmCols + 2 * r * kLmS) * sizeof(T);
   smem_limit((const void*)k_landmark<T>, sm);
   k_landmark<T><<<(unsigned)(nleaf + 1), 256, sm, st>>>(VP, r, k, p, wa, Sinv, Sj3, nleaf, part);
+}
+
+int leaf_dk_gram_parts(const Tree& t) {
+  const int nt = (int)((t.max_leaf + 31) / 32);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(nt * (nt + 1) / 2, 4096 / std::max<int64_t>(t.nleaf, 1)));
 }
 
 template <typename T>
 void launch_leaf_dk_gram(const double* pts, KParams kp, const T* X, int64_t n, int p, double wa, const Tree& t,
                          double* part, cudaStream_t st) {
-  k_leaf_dk_gram<T><<<(unsigned)t.nleaf, dim3(32, 8), 0, st>>>(pts, kp, X, n, p, wa, dtree(t), part);
+  const int S = leaf_dk_gram_parts(t);
+  k_leaf_dk_gram<T><<<dim3((unsigned)t.nleaf, (unsigned)S), dim3(32, 8), 0, st>>>(pts, kp, X, n, p, wa, dtree(t),
+                                                                                  part);
 }
 
 void launch_grad_final(const double* a, int64_t na, const double* b, int64_t nb, double scale, double* out,
@@ -894,12 +962,12 @@ void launch_grad_final(const double* a, int64_t na, const double* b, int64_t nb,
   k_grad_final<<<3, 256, 0, st>>>(a, na, b, nb, scale, out);
 }
 
-template void launch_eval_dphi3<double>(const double*, const double*, int, const Tree&, KParams, double*,
+template void launch_eval_dphi2<double>(const double*, const double*, int, const Tree&, KParams, double*,
                                         cudaStream_t);
-template void launch_eval_dphi3<ff>(const double*, const double*, int, const Tree&, KParams, ff*, cudaStream_t);
-template void launch_leaf_proj4<double>(const double*, const double*, int, const Tree&, const double*, int64_t,
+template void launch_eval_dphi2<ff>(const double*, const double*, int, const Tree&, KParams, ff*, cudaStream_t);
+template void launch_leaf_proj3<double>(const double*, const double*, int, const Tree&, const double*, int64_t,
                                         double*, int, cudaStream_t);
-template void launch_leaf_proj4<ff>(const ff*, const ff*, int, const Tree&, const double*, int64_t, double*, int,
+template void launch_leaf_proj3<ff>(const ff*, const ff*, int, const Tree&, const ff*, int64_t, double*, int,
                                     cudaStream_t);
 template void launch_landmark<double>(const double*, int, int, int, double, const double*, const double*, int64_t,
                                       double*, cudaStream_t);

@@ -175,15 +175,18 @@ void launch_axpby(double* y, const double* x, double a, double b, int64_t n, cud
 // trace form of the stochastic gradient (km_grad.cu).  X: n x k (k = p + 1: p probes with weight
 // 1/p, then alpha with weight wa); W = 4r projection rows per (leaf, column) pair.
 template <typename T>
-void launch_eval_dphi3(const double* pts, const double* lnd, int r, const Tree& t, KParams kp, T* dPhi3,
+void launch_eval_dphi2(const double* pts, const double* lnd, int r, const Tree& t, KParams kp, T* dPhi2,
                        cudaStream_t st);
 template <typename T>
-void launch_leaf_proj4(const T* Phi, const T* dPhi3, int r, const Tree& t, const double* X, int64_t ldx, double* VP,
-                      int k, cudaStream_t st);
+void launch_leaf_proj3(const T* Phi, const T* dPhi2, int r, const Tree& t, const T* X, int64_t ldx, double* VP, int k,
+                       cudaStream_t st);
+void launch_nugget_proj(const double* pts, const double* lnd, int r, const Tree& t, const double* X, int64_t ldx,
+                        double* VP, int k, cudaStream_t st);
 void launch_proj_total(double* VP, int W, int64_t nleaf, int k, cudaStream_t st);
 template <typename T>
 void launch_landmark(const double* VP, int r, int k, int p, double wa, const T* Sinv, const T* Sj3, int64_t nleaf,
                      double* part, cudaStream_t st);
+int leaf_dk_gram_parts(const Tree& t);  // CTAs per leaf of the leaf term (partial sums per leaf)
 template <typename T>
 void launch_leaf_dk_gram(const double* pts, KParams kp, const T* X, int64_t n, int p, double wa, const Tree& t,
                          double* part, cudaStream_t st);
