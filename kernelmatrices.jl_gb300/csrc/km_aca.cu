@@ -15,7 +15,6 @@
 // the c2 rows:  y_c2 -= Q2 (z2 - L22^{-1}(z2 - C' z1)),  z1 = Q1' y_c1, z2 = Q2' y_c2.
 #include <climits>
 
-#include <cublas_v2.h>
 
 #include "km_kernels.h"
 
@@ -1435,14 +1434,15 @@ int64_t panel_qr_gemm_scratch(const PanelDesc* hdescs, int n, int kmax) {
   int64_t mbig = 0;
   for (int p = 0; p < n; ++p)
     if (hdescs[p].big) mbig = std::max<int64_t>(mbig, hdescs[p].m);
-  return mbig * kQB + 2 * (int64_t)kQB * std::max(kmax, 1) + 2 * 152 * kPqParts + 8;
+  return mbig * kQB + 2 * (int64_t)kQB * std::max(kmax, 1) + 2 * 152 * kPqParts + 8 +
+         dgemm_scratch(1, kQB, std::max(kmax, 1), mbig);
 }
 
 // C[:, j1:k] <- (I - V op(T) V') C[:, j1:k] for big panel p, block j0: W = V' C, W2 = op(T) W,
 // C -= V W2 (op(T) = T' while factoring, T while forming Q), then the small panels' blocks by
 // k_pq_update
 static void panel_block_gemm(const PanelDesc* descs, const PanelDesc& D, int p, int j0, int nblk, const double* Ts,
-                             double* scr, int kmax, cublasHandle_t cub, int transT, cudaStream_t st) {
+                             double* scr, int kmax, double* split, int64_t split_len, int transT, cudaStream_t st) {
   const int k = D.k;
   if (j0 >= k) return;
   const int jb = std::min(kQB, k - j0), j1 = j0 + jb;
@@ -1456,10 +1456,9 @@ static void panel_block_gemm(const PanelDesc* descs, const PanelDesc& D, int p, 
   k_pq_vcopy<<<g, 256, 0, st>>>(descs + p, j0, V);
   const double* Tm = Ts + ((int64_t)p * nblk + j0 / kQB) * kQB * kQB;
   double* C = D.A + (int64_t)j1 * D.lda + j0;
-  const double one = 1.0, zero = 0.0, mone = -1.0;
-  cublasDgemm(cub, CUBLAS_OP_T, CUBLAS_OP_N, jb, nt, (int)mr, &one, V, (int)mr, C, (int)D.lda, &zero, W, jb);
-  cublasDgemm(cub, transT ? CUBLAS_OP_T : CUBLAS_OP_N, CUBLAS_OP_N, jb, nt, jb, &one, Tm, kQB, W, jb, &zero, W2, jb);
-  cublasDgemm(cub, CUBLAS_OP_N, CUBLAS_OP_N, (int)mr, nt, jb, &mone, V, (int)mr, W2, jb, &one, C, (int)D.lda);
+  launch_dgemm(1, jb, nt, mr, 1.0, V, mr, C, D.lda, 0.0, W, jb, split, split_len, st);
+  launch_dgemm(transT, jb, nt, jb, 1.0, Tm, kQB, W, jb, 0.0, W2, jb, nullptr, 0, st);
+  launch_dgemm(0, mr, nt, jb, -1.0, V, mr, W2, jb, 1.0, C, D.lda, nullptr, 0, st);
 }
 
 // grid size of the cooperative factor / form steps of a tall panel (0: cooperative launch
@@ -1489,11 +1488,9 @@ static int pq_grid_size(int64_t m) {
 }
 
 void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n, int kmax, double* taus,
-                          double* Ts, double* gemm_scratch, void* cublas_handle, int* grid_err, cudaStream_t st,
+                          double* Ts, double* gemm_scratch, int* grid_err, cudaStream_t st,
                           long long wait_limit) {
   if (n <= 0 || kmax <= 0) return;
-  cublasHandle_t cub = static_cast<cublasHandle_t>(cublas_handle);
-  cublasSetStream(cub, st);
   const int nblk = (kmax + kQB - 1) / kQB;
   const int ntiles = (kmax + kQU - 1) / kQU;
   const size_t smu = ((size_t)2 * kQB * kQU + kQC * kQV) * sizeof(double);
@@ -1504,6 +1501,8 @@ void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n
     if (hdescs[p].big) mbig = std::max<int64_t>(mbig, hdescs[p].m);
   double* part = gemm_scratch + mbig * kQB + 2 * (int64_t)kQB * std::max(kmax, 1);
   unsigned* words = reinterpret_cast<unsigned*>(part + 2 * 152 * kPqParts);
+  double* split = part + 2 * 152 * kPqParts + 8;  // partial products of the split V'C reductions
+  const int64_t split_len = dgemm_scratch(1, kQB, std::max(kmax, 1), mbig);
   cudaMemsetAsync(words, 0, 4 * sizeof(unsigned), st);
   GridBar gb{words, words + 1, grid_err, wait_limit};
   auto factor_big = [&](int p, int b) {
@@ -1539,13 +1538,15 @@ void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n
       if (hdescs[p].big && b * kQB < hdescs[p].k) factor_big(p, b);
     k_pq_update<<<dim3((unsigned)n, (unsigned)ntiles), 256, smu, st>>>(descs, b * kQB, Ts, nblk, 1);
     for (int p = 0; p < n; ++p)
-      if (hdescs[p].big) panel_block_gemm(descs, hdescs[p], p, b * kQB, nblk, Ts, gemm_scratch, kmax, cub, 1, st);
+      if (hdescs[p].big)
+        panel_block_gemm(descs, hdescs[p], p, b * kQB, nblk, Ts, gemm_scratch, kmax, split, split_len, 1, st);
   }
   k_pq_rout<<<n, 256, 0, st>>>(descs);
   for (int b = nblk - 1; b >= 0; --b) {
     k_pq_update<<<dim3((unsigned)n, (unsigned)ntiles), 256, smu, st>>>(descs, b * kQB, Ts, nblk, 0);
     for (int p = 0; p < n; ++p)
-      if (hdescs[p].big) panel_block_gemm(descs, hdescs[p], p, b * kQB, nblk, Ts, gemm_scratch, kmax, cub, 0, st);
+      if (hdescs[p].big)
+        panel_block_gemm(descs, hdescs[p], p, b * kQB, nblk, Ts, gemm_scratch, kmax, split, split_len, 0, st);
     k_pq_form<<<n, 512, 0, st>>>(descs, b * kQB, taus, kmax, 1);
     for (int p = 0; p < n; ++p)
       if (hdescs[p].big && b * kQB < hdescs[p].k) form_big(p, b);

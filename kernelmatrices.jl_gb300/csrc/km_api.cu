@@ -5,7 +5,6 @@
 #include <cmath>
 #include <cstdlib>
 
-#include <cublas_v2.h>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -135,9 +134,9 @@ struct km_handle {
   GApplyItem* d_gfact = nullptr;      // factorisation updates, grouped by level
   std::vector<GNodeDesc> gnodes_h;    // host copies: the library-GEMM path of large nodes reads them
   std::vector<GApplyItem> gsolve_h, gfact_h;
-  double* d_gz = nullptr;             // projections and coefficients of one large node (4 x r x ncols)
+  double* d_gz = nullptr;             // projections and coefficients of one large node (4 x r x ncols),
+                                      // then the partial products of its split projections
   double* d_pqg = nullptr;            // explicit reflector block and products of the tall-panel QR
-  cublasHandle_t cublas = nullptr;
   std::vector<int64_t> gfoff;
   PanelDesc* d_pdesc = nullptr;
   LeafDesc* d_ldesc = nullptr;
@@ -472,21 +471,18 @@ static int run_gapply(km_handle* h, const std::vector<GApplyItem>& hl, GApplyIte
   cudaStream_t st = h->stream;
   if (b <= a) return KM_OK;
   KLV(h, KM_PROF_SWEEP, launch_gapply(dl + a, (int)(b - a), h->d_gnodes, h->gmaxr, maxcols, mode, X, Xin, ldX, kX, st));
-  int64_t need = 0;
+  int64_t need = 0, split = 0;
   for (int64_t q = a; q < b; ++q)
     if (hl[q].big) {
       const GNodeDesc& N = h->gnodes_h[hl[q].node];
       const int nc = hl[q].base ? hl[q].ncols : kX;
       need = std::max<int64_t>(need, 4 * (int64_t)N.r * nc);
+      split = std::max(split, std::max(dgemm_scratch(1, N.r, nc, N.s1), dgemm_scratch(1, N.r, nc, N.s2)));
     }
   if (need == 0) return KM_OK;
   int rc;
-  if ((rc = grow(h, &h->d_gz, need)) != KM_OK) return rc;
-  if (!h->cublas) {
-    if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS) return fail(h, KM_ERR_CUDA, "cublasCreate failed");
-  }
-  cublasSetStream(h->cublas, st);
-  const double one = 1.0, zero = 0.0, mone = -1.0;
+  if ((rc = grow(h, &h->d_gz, need + split)) != KM_OK) return rc;
+  const double one = 1.0, mone = -1.0;
   for (int64_t q = a; q < b; ++q) {
     const GApplyItem& I = hl[q];
     if (!I.big) continue;
@@ -504,16 +500,13 @@ static int run_gapply(km_handle* h, const std::vector<GApplyItem>& hl, GApplyIte
     double* Z2 = Z1 + (int64_t)r * nc;
     double* G1 = Z2 + (int64_t)r * nc;
     double* G2 = G1 + (int64_t)r * nc;
-    const int s1 = (int)N.s1, s2 = (int)N.s2;
-    const int ldi = (int)ld;
-    cublasStatus_t cs = CUBLAS_STATUS_SUCCESS;
-    auto gemm_t = [&](const double* Q, int s, const double* x, double* Z) {  // Z = Q' x
-      if (cs == CUBLAS_STATUS_SUCCESS)
-        cs = cublasDgemm(h->cublas, CUBLAS_OP_T, CUBLAS_OP_N, r, nc, s, &one, Q, s, x, ldi, &zero, Z, r);
+    const int64_t s1 = N.s1, s2 = N.s2;
+    double* spl = G2 + (int64_t)r * nc;  // partial products of the split Q' x reductions
+    auto gemm_t = [&](const double* Q, int64_t s, const double* x, double* Z) {  // Z = Q' x
+      launch_dgemm(1, r, nc, s, 1.0, Q, s, x, ld, 0.0, Z, r, spl, split, st);
     };
-    auto gemm_n = [&](const double* Q, int s, const double* G, double* y, const double* alpha) {  // y += a Q G
-      if (cs == CUBLAS_STATUS_SUCCESS)
-        cs = cublasDgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, s, nc, r, alpha, Q, s, G, r, &one, y, ldi);
+    auto gemm_n = [&](const double* Q, int64_t s, const double* G, double* y, const double* alpha) {  // y += a Q G
+      launch_dgemm(0, s, nc, r, *alpha, Q, s, G, r, 1.0, y, ld, nullptr, 0, st);
     };
     const GNodeDesc* dN = h->d_gnodes + I.node;
     KLV(h, KM_PROF_SWEEP, {
@@ -530,9 +523,8 @@ static int run_gapply(km_handle* h, const std::vector<GApplyItem>& hl, GApplyIte
         gemm_n(N.Q2, s2, G2, y2, (mode == 0 || mode == 1) ? &mone : &one);
       }
     });
-    if (cs != CUBLAS_STATUS_SUCCESS) return fail(h, KM_ERR_CUDA, "cublasDgemm failed");
   }
-  return KM_OK;
+  return check_launch(h, "factor application");
 }
 
 int general_fwd(km_handle* h, double* X, int k) {  // X <- W^{-1} X
@@ -1178,7 +1170,6 @@ int km_destroy(km_handle* h) {
   if (!h) return KM_OK;
   cudaSetDevice(h->cfg.device);
   free_problem(h);
-  if (h->cublas) cublasDestroy(h->cublas);
   if (h->fgraph) cudaGraphExecDestroy(h->fgraph);
   if (h->sgraph) cudaGraphExecDestroy(h->sgraph);
   prof_resolve(h);
@@ -1445,12 +1436,10 @@ static int general_factorize(km_handle* h) {
       bool anybig = false;
       for (int64_t p = pdoff[l]; p < pdoff[l + 1]; ++p) anybig |= pd[p].big != 0;
       if (anybig) {
-        if (!h->cublas && cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS)
-          return fail(h, KM_ERR_CUDA, "cublasCreate failed");
         if ((rc = grow(h, &h->d_pqg, panel_qr_gemm_scratch(pd.data() + pdoff[l], np, kmax_l[l])))) return rc;
         KLV(h, KM_PROF_LEAF_QR, launch_panel_qr_gemm(h->d_pdesc + pdoff[l], pd.data() + pdoff[l], np, kmax_l[l],
                                                      h->d_pqs, h->d_pqs + (int64_t)np * kmax_l[l], h->d_pqg,
-                                                     h->cublas, h->d_info + t.nleaf + nb, st, h->wait_limit));
+                                                     h->d_info + t.nleaf + nb, st, h->wait_limit));
       } else {
         KLV(h, KM_PROF_LEAF_QR, launch_panel_qr(h->d_pdesc + pdoff[l], np, kmax_l[l], h->d_pqs,
                                                 h->d_pqs + (int64_t)np * kmax_l[l], st));

@@ -219,12 +219,20 @@ void launch_aca_one(const double* pts, KParams kp, const AcaBlock* blocks, int b
 void launch_panel_qr(const PanelDesc* descs, int n, int kmax, double* taus, double* Ts, cudaStream_t st);
 // the same with the panels marked big handled by all SMs: their 8-column factor and form steps
 // as cooperative launches (bounded grid barriers; a barrier that runs out sets *grid_err) and
-// their block-reflector applications as cuBLAS DGEMMs (hdescs: host copies of descs;
+// their block-reflector applications as FP64 products over all SMs (launch_dgemm; hdescs: host
+// copies of descs;
 // gemm_scratch: panel_qr_gemm_scratch(hdescs, n, kmax) doubles)
 void launch_panel_qr_gemm(const PanelDesc* descs, const PanelDesc* hdescs, int n, int kmax, double* taus,
-                          double* Ts, double* gemm_scratch, void* cublas_handle, int* grid_err, cudaStream_t st,
+                          double* Ts, double* gemm_scratch, int* grid_err, cudaStream_t st,
                           long long wait_limit = -1);
 int64_t panel_qr_gemm_scratch(const PanelDesc* hdescs, int n, int kmax);
+// C = alpha op(A) B + beta C (FP64, column-major; op(A) = A' when transA), km_gemm.cu.  A long
+// reduction with op = T is split over CTAs when `scratch` holds dgemm_scratch(...) doubles
+// (scratch_len of them; fewer splits if it holds less, none if null).
+void launch_dgemm(int transA, int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+                  const double* B, int64_t ldb, double beta, double* C, int64_t ldc, double* scratch,
+                  int64_t scratch_len, cudaStream_t st);
+int64_t dgemm_scratch(int transA, int64_t M, int64_t N, int64_t K);
 int64_t panel_qr_scratch(int n, int kmax);
 void launch_gnode(const GNodeDesc* nodes, int n, int* info, cudaStream_t st);
 void launch_gapply(const GApplyItem* items, int n, const GNodeDesc* nodes, int maxr, int maxcols, int mode,

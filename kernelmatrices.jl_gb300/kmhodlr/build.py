@@ -67,7 +67,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> Path:
     with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcublas"]
+    cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -143,10 +143,11 @@ def test_grid_aca_large_block(lib):
     assert rel(hk.ldiv(rhs), O.hodlr_ldiv(ohk, rhs)) < 1e-9
 
 
-def test_tall_panels_library_gemm_path(lib):
+def test_tall_panels_split_gemm_path(lib):
     """n = 32768: the top blocks have 16384 rows, so their panel QR block reflectors and the
-    application of their node factors run as library GEMMs; ranks and pivots (RQ) equal the
-    oracle's, and logdet and solves agree as on the kernel path."""
+    application of their node factors run as the FP64 products of km_gemm.cu (split reductions
+    over all SMs); ranks and pivots (RQ) equal the oracle's, and logdet and solves agree as on the
+    per-node kernel path."""
     import kmhodlr as K
     from kmhodlr.data import uniform_points
     n = 32768
