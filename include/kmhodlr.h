@@ -253,6 +253,19 @@ int km_stoch_hessian(km_handle* h, const double* y, const double* probes, int64_
 int km_stoch_hessian_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed, double* nll,
                             double* grad, double* hess);
 
+/* Stochastic Hessian of the negative log PROFILE likelihood (the scale profiled out): nll and
+ * grad are km_profile_nll_grad's, hess = -F + 0.5 mean_v t'D2_jk t - 0.5 n (s_jk / y'u
+ * + (u'dK_j u)(u'dK_k u) / (y'u)^2) with s_jk the solve term of km_stoch_hessian and F its Fisher
+ * matrix.  Replaces stoch_hessian(..., profile = true) with HODLR_p_hess_slv
+ * (src/HODLR/src/stochastichessian.jl:15-31, 117-147) as called by nlpl_hessian
+ * (src/HODLR/src/maxlikfunctions.jl:120-136).  A pair whose second derivative is identically
+ * zero (where the reference raises "I didn't implement this speed-up for the profile likelihood")
+ * takes the reference's general path with a zero second-derivative function.  nprobe >= 1. */
+int km_stoch_profile_hessian(km_handle* h, const double* y, const double* probes, int64_t nprobe,
+                             double* nll, double* grad, double* hess);
+int km_stoch_profile_hessian_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed,
+                                    double* nll, double* grad, double* hess);
+
 /* k-d ordering of n 2-D points (AoS x, y) on the device, the input step of maxlikdata
  * (src/HODLR/src/constructor.jl:171-181), which sorts with NearestNeighbors.KDTree(pts).data.
  * That package's permutation is not reproduced; this library's ordering is: a range of more than

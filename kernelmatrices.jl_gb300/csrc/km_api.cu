@@ -1997,7 +1997,7 @@ static int gradient_trace(km_handle* h, int64_t p, double wa, double* grad) {
 
 static int nll_grad_impl(km_handle* h, const double* y, const double* probes, bool seeded, uint64_t seed,
                          int64_t nprobe, double* nll, double* grad, bool profile = false,
-                         double* fisher = nullptr) {
+                         double* fisher = nullptr, double* ya_out = nullptr) {
   if (!h || !y || !nll || nprobe < 0 || (grad && (nprobe < 1 || (!probes && !seeded))) || (fisher && !grad))
     return fail(h, KM_ERR_BAD_ARG, "bad likelihood arguments");
   cudaSetDevice(h->cfg.device);
@@ -2034,6 +2034,7 @@ static int nll_grad_impl(km_handle* h, const double* y, const double* probes, bo
   double ya = 0.0;
   for (int64_t i = 0; i < n; ++i) ya += y[i] * a[i];
   if (profile && !(ya > 0.0)) return fail(h, KM_ERR_BAD_ARG, "y' K^-1 y is not positive (zero data?)");
+  if (ya_out) *ya_out = ya;
   *nll = profile ? 0.5 * (ld + (double)n * std::log(ya)) : 0.5 * ld + 0.5 * ya;
   if (grad) {
     if (seeded)
@@ -2112,19 +2113,23 @@ int km_grad_fisher_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_
 // second derivative is not identically zero, and minus half the solve term
 // -u'dK_k K^{-1} dK_j u - u'dK_j K^{-1} dK_k u (+ u'D2_jk u), u = K^{-1} y (HODLR_hess_slv(_no2d)
 // :3-13, :50-56), written with the symmetry of K^{-1} and dK_j.  The probes, W'^{-1} V and u come
-// from the gradient and Fisher call.
+// from the gradient and Fisher call.  With `profile` (stoch_hessian(..., profile = true), the
+// Hessian of nlpl_hessian, maxlikfunctions.jl:120-136) NLL and gradient are the profile
+// likelihood's and the solve term is HODLR_p_hess_slv's (stochastichessian.jl:15-31); a pair whose
+// second derivative is identically zero, where the reference raises, takes its general path with
+// a zero second derivative (no D2 term, no trace term).
 static int hessian_impl(km_handle* h, const double* y, const double* probes, bool seeded, uint64_t seed,
-                        int64_t nprobe, double* nll, double* grad, double* hess) {
+                        int64_t nprobe, double* nll, double* grad, double* hess, bool profile = false) {
   if (!h || !hess || !grad || nprobe < 1) return fail(h, KM_ERR_BAD_ARG, "bad Hessian arguments");
-  double F[9];
-  int rc = nll_grad_impl(h, y, probes, seeded, seed, nprobe, nll, grad, false, F);
+  double F[9], ya = 0.0;
+  int rc = nll_grad_impl(h, y, probes, seeded, seed, nprobe, nll, grad, profile, F, &ya);
   if (rc != KM_OK) return rc;
   const Tree& t = h->tree;
   const int64_t n = t.n, p = nprobe;
   cudaStream_t st = h->stream;
   const double* u = h->d_T + n * p;  // d_T = [W'^{-1} V | K^{-1} y]
   if ((rc = grow(h, &h->d_hA, 6 * n)) || (rc = grow(h, &h->d_hY, n * (p + 1))) ||
-      (rc = grow(h, &h->d_hdots, p + 1 + 9)))
+      (rc = grow(h, &h->d_hdots, p + 1 + 12)))
     return rc;
   double* a = h->d_hA;      // a_j = dK_j u
   double* b = a + 3 * n;    // b_j = K^{-1} a_j
@@ -2133,11 +2138,12 @@ static int hessian_impl(km_handle* h, const double* y, const double* probes, boo
     KM_CUDA(h, cudaMemcpyAsync(b + j * n, a + j * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
     if ((rc = nested_solve(h, b + j * n, 1)) != KM_OK) return rc;
   }
-  double* d_ab = h->d_hdots + p + 1;  // d_ab[3 j + k] = a_k . b_j
+  double* d_ab = h->d_hdots + p + 1;  // d_ab[3 j + k] = a_k . b_j, then d_ab[9 + j] = u . a_j
   for (int j = 0; j < 3; ++j)
     for (int k = 0; k < 3; ++k)
       KLV(h, KM_PROF_OTHER, launch_col_dots(a + k * n, n, b + j * n, n, n, 1, d_ab + 3 * j + k, st));
-  double ab[9];
+  for (int j = 0; j < 3; ++j) KLV(h, KM_PROF_OTHER, launch_col_dots(a + j * n, n, u, n, n, 1, d_ab + 9 + j, st));
+  double ab[12];
   KM_CUDA(h, cudaMemcpyAsync(ab, d_ab, sizeof ab, cudaMemcpyDeviceToHost, st));
   if ((rc = sync(h, "hessian")) != KM_OK) return rc;
   std::vector<double> dd(p + 1);
@@ -2154,6 +2160,9 @@ static int hessian_impl(km_handle* h, const double* y, const double* probes, boo
         tr /= (double)p;
         sterm += dd[p];  // u' D2_jk u
       }
+      // profile likelihood (HODLR_p_hess_slv, stochastichessian.jl:15-31): with dotm = y'u,
+      // n (sterm / dotm + (u'dK_j u)(u'dK_k u) / dotm^2), since y'K^{-1} = u'
+      if (profile) sterm = (double)n * (sterm / ya + ab[9 + j] * ab[9 + k] / (ya * ya));
       hess[3 * j + k] = hess[3 * k + j] = -F[3 * j + k] + 0.5 * tr - 0.5 * sterm;
     }
   return KM_OK;
@@ -2168,6 +2177,17 @@ int km_stoch_hessian(km_handle* h, const double* y, const double* probes, int64_
 int km_stoch_hessian_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed, double* nll,
                             double* grad, double* hess) {
   return hessian_impl(h, y, nullptr, true, seed, nprobe, nll, grad, hess);
+}
+
+int km_stoch_profile_hessian(km_handle* h, const double* y, const double* probes, int64_t nprobe, double* nll,
+                             double* grad, double* hess) {
+  if (!probes) return fail(h, KM_ERR_BAD_ARG, "bad Hessian arguments");
+  return hessian_impl(h, y, probes, false, 0, nprobe, nll, grad, hess, true);
+}
+
+int km_stoch_profile_hessian_seeded(km_handle* h, const double* y, int64_t nprobe, uint64_t seed, double* nll,
+                                    double* grad, double* hess) {
+  return hessian_impl(h, y, nullptr, true, seed, nprobe, nll, grad, hess, true);
 }
 
 int km_profile_nll_grad(km_handle* h, const double* y, const double* probes, int64_t nprobe, double* nll,

@@ -9,7 +9,7 @@
 #   HODLR.stoch_gradient, HODLR.negloglik             stochasticgradient.jl:30-44, maxlikfunctions.jl:2-9
 #   HODLR.stoch_profile_gradient, profile_negloglik   stochasticgradient.jl:68-86, maxlikfunctions.jl:11-19
 #   grad_and_fisher_matrix, stoch_fisher              stochastichessian.jl:91-115,152-181
-#   stoch_hessian                                     stochastichessian.jl:117-147
+#   stoch_hessian (profile = false / true)            stochastichessian.jl:15-31, 117-147
 #   maxlikdata(...; sortmethod=:KDTree)               constructor.jl:171-181 (own k-d ordering)
 #   RKernelHODLR(K, tol, maxrank, lvl), R * v         constructor.jl:130-161, baseoverloads.jl:301-305
 #
@@ -195,16 +195,24 @@ function grad_and_fisher(K::GPUKernelHODLR, dat::Vector{Float64}, vecs::Vector{V
   return nll[], grad, Symmetric(fisher)
 end
 
-# stoch_hessian(K, HK, dat, d1funs, d2funs, vecs) (stochastichessian.jl:117-147, shuffle = false,
-# profile = false) with the built-in kernels' second derivatives: (nll, gradient, 3 x 3 Hessian).
-function stoch_hessian(K::GPUKernelHODLR, dat::Vector{Float64}, vecs::Vector{Vector{Float64}})
+# stoch_hessian(K, HK, dat, d1funs, d2funs, vecs; profile) (stochastichessian.jl:117-147,
+# shuffle = false) with the built-in kernels' second derivatives: (nll, gradient, 3 x 3 Hessian);
+# profile = true takes HODLR_p_hess_slv (:15-31), the Hessian of nlpl_hessian.
+function stoch_hessian(K::GPUKernelHODLR, dat::Vector{Float64}, vecs::Vector{Vector{Float64}};
+                       profile::Bool=false)
   probes = reduce(hcat, vecs)
   nll = Ref{Cdouble}(0.0)
   grad = zeros(3)
   hess = zeros(3, 3)
-  check(K.h, ccall((:km_stoch_hessian, libkm), Cint,
-                   (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
-                   K.h, dat, probes, size(probes, 2), nll, grad, hess))
+  if profile
+    check(K.h, ccall((:km_stoch_profile_hessian, libkm), Cint,
+                     (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                     K.h, dat, probes, size(probes, 2), nll, grad, hess))
+  else
+    check(K.h, ccall((:km_stoch_hessian, libkm), Cint,
+                     (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                     K.h, dat, probes, size(probes, 2), nll, grad, hess))
+  end
   return nll[], grad, Symmetric(hess)
 end
 

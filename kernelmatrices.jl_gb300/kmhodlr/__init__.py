@@ -10,7 +10,7 @@ from .hodlr import (  # noqa: F401
     probe_fp32_tflops,
     negloglik, stoch_gradient, nll_objective, profile_negloglik, stoch_profile_gradient, nlpl_objective,
     scaleparm_mle, gpsimulate, stoch_fisher, grad_and_fisher, grad_and_fisher_matrix, stoch_hessian,
-    grad_fisher_hessian, nll_hessian, kd_order, maxlikdata,
+    grad_fisher_hessian, nll_hessian, nlpl_hessian, kd_order, maxlikdata,
     RKernelHODLR,
 )
 from .serving import BatchEngine, Server, Problem, Result, estimate_bytes  # noqa: F401

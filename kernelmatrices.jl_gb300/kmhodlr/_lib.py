@@ -144,6 +144,8 @@ SIGNATURES = {
     "km_grad_fisher_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP, _DP]),
     "km_stoch_hessian": (C.c_int, [_H, _DP, _DP, C.c_int64, _DP, _DP, _DP]),
     "km_stoch_hessian_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP, _DP]),
+    "km_stoch_profile_hessian": (C.c_int, [_H, _DP, _DP, C.c_int64, _DP, _DP, _DP]),
+    "km_stoch_profile_hessian_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP, _DP]),
     "km_profile_nll_grad_seeded": (C.c_int, [_H, _DP, C.c_int64, C.c_uint64, _DP, _DP]),
     "km_trim": (C.c_int, [_H]),
     "km_estimate_bytes": (C.c_int64, [C.c_int64, C.c_int64, C.c_int, C.c_int64, C.c_int64, C.c_int]),

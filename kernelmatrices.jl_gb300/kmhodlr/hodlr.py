@@ -374,36 +374,41 @@ def grad_and_fisher(HK: KernelHODLR, dat: np.ndarray, vecs=None, nprobe: int = 0
     return _grad_fisher(HK, dat, vecs, nprobe, seed)
 
 
-def _hessian(HK: "KernelHODLR", dat: np.ndarray, vecs=None, nprobe: int = 0, seed: int = 0):
+def _hessian(HK: "KernelHODLR", dat: np.ndarray, vecs=None, nprobe: int = 0, seed: int = 0, profile: bool = False):
     lib = L.load()
+    fs = lib.km_stoch_profile_hessian_seeded if profile else lib.km_stoch_hessian_seeded
+    fv = lib.km_stoch_profile_hessian if profile else lib.km_stoch_hessian
     y = np.ascontiguousarray(dat, dtype=np.float64).reshape(-1)
     nll = C.c_double()
     g = np.zeros(3)
     H = np.zeros((3, 3), order="F")
     if vecs is None:
-        _check(HK._h, lib.km_stoch_hessian_seeded(HK._h, _dp(y), int(nprobe), int(seed), C.byref(nll), _dp(g),
-                                                  _dp(H)))
+        _check(HK._h, fs(HK._h, _dp(y), int(nprobe), int(seed), C.byref(nll), _dp(g), _dp(H)))
     else:
         V = np.asfortranarray(np.column_stack(vecs) if isinstance(vecs, (list, tuple)) else vecs, dtype=np.float64)
-        _check(HK._h, lib.km_stoch_hessian(HK._h, _dp(y), _dp(V), V.shape[1], C.byref(nll), _dp(g), _dp(H)))
+        _check(HK._h, fv(HK._h, _dp(y), _dp(V), V.shape[1], C.byref(nll), _dp(g), _dp(H)))
     return nll.value, g, H
 
 
-def stoch_hessian(HK: KernelHODLR, dat: np.ndarray, vecs=None, nprobe: int = 0, seed: int = 0) -> np.ndarray:
-    """``stoch_hessian(K, HK, dat, d1funs, d2funs, vecs)`` (src/HODLR/src/stochastichessian.jl:117-147,
-    shuffle = false, profile = false) for the three kernel parameters, with the closed-form second
-    derivatives of the built-in kernels as d2funs.  Probes are ``vecs`` (host) or ``nprobe``
-    seeded Rademacher probes drawn on the device."""
+def stoch_hessian(HK: KernelHODLR, dat: np.ndarray, vecs=None, nprobe: int = 0, seed: int = 0,
+                  profile: bool = False) -> np.ndarray:
+    """``stoch_hessian(K, HK, dat, d1funs, d2funs, vecs; profile)`` (src/HODLR/src/
+    stochastichessian.jl:117-147, shuffle = false) for the three kernel parameters, with the
+    closed-form second derivatives of the built-in kernels as d2funs; ``profile`` takes the
+    profile likelihood's solve term (HODLR_p_hess_slv, :15-31).  Probes are ``vecs`` (host) or
+    ``nprobe`` seeded Rademacher probes drawn on the device."""
     if not HK.factorized:
         raise KMError(L.KM_ERR_STATE, "The matrix needs to be factorized.")
-    return _hessian(HK, dat, vecs, nprobe, seed)[2]
+    return _hessian(HK, dat, vecs, nprobe, seed, profile)[2]
 
 
-def grad_fisher_hessian(HK: KernelHODLR, dat: np.ndarray, vecs=None, nprobe: int = 0, seed: int = 0):
-    """(NLL, gradient, stochastic Hessian) from one set of probes (see ``stoch_hessian``)."""
+def grad_fisher_hessian(HK: KernelHODLR, dat: np.ndarray, vecs=None, nprobe: int = 0, seed: int = 0,
+                        profile: bool = False):
+    """(NLL, gradient, stochastic Hessian) from one set of probes (see ``stoch_hessian``; with
+    ``profile`` the profile likelihood's NLL and gradient)."""
     if not HK.factorized:
         raise KMError(L.KM_ERR_STATE, "The matrix needs to be factorized.")
-    return _hessian(HK, dat, vecs, nprobe, seed)
+    return _hessian(HK, dat, vecs, nprobe, seed, profile)
 
 
 def nll_hessian(prms, pts: np.ndarray, dat: np.ndarray, kernel, rank: int, lvl, saav, device: int = 0) -> np.ndarray:
@@ -414,6 +419,16 @@ def nll_hessian(prms, pts: np.ndarray, dat: np.ndarray, kernel, rank: int, lvl, 
     HK = KernelHODLR(K, 0.0, rank, lvl, nystrom=True, sorted=True, device=device)
     symmetricfactorize(HK)
     return _hessian(HK, dat, saav)[2]
+
+
+def nlpl_hessian(prms, pts: np.ndarray, dat: np.ndarray, kernel, rank: int, lvl, saav, device: int = 0) -> np.ndarray:
+    """``nlpl_hessian(prms, data, opts)`` (src/HODLR/src/maxlikfunctions.jl:119-136): assemble
+    (Nystrom, ep = 0), factorise and return the stochastic Hessian of the negative log profile
+    likelihood over the probes ``saav`` (``stoch_hessian`` with ``profile = true``)."""
+    K = KernelMatrix(pts, pts, prms, kernel)
+    HK = KernelHODLR(K, 0.0, rank, lvl, nystrom=True, sorted=True, device=device)
+    symmetricfactorize(HK)
+    return _hessian(HK, dat, saav, profile=True)[2]
 
 
 def grad_and_fisher_matrix(prms, pts: np.ndarray, dat: np.ndarray, kernel, rank: int, lvl, saav,

@@ -1017,27 +1017,54 @@ def hess_slv_no2d(HK: KernelHODLR, DKj, DKk, data, HKsd) -> float:
     return float(np.dot(data, out))
 
 
+def p_hess_slv(HK: KernelHODLR, DKj, DKk, parts, data, HKsd, dotm) -> float:
+    """``HODLR_p_hess_slv`` (stochastichessian.jl:15-31): the solve term of the profile likelihood,
+    n * (data'out / dotm + (data' K^-1 dK_j u)(data' K^-1 dK_k u) / dotm^2) with
+    out = -K^-1 dK_k K^-1 dK_j u - K^-1 dK_j K^-1 dK_k u + K^-1 D2_jk u, u = K^-1 data and
+    dotm = data'u.  ``parts`` = (D2B2, D2BL, Sjk), or None for a second derivative that is zero
+    (the reference's general path with a zero function: the D2 term vanishes)."""
+    tmp1 = derivative_mul(DKj, HKsd)
+    tmp2 = derivative_mul(DKk, HKsd)
+    out = -hodlr_ldiv(HK, derivative_mul(DKk, hodlr_ldiv(HK, tmp1)))
+    out = out - hodlr_ldiv(HK, derivative_mul(DKj, hodlr_ldiv(HK, tmp2)))
+    if parts is not None:
+        out = out + hodlr_ldiv(HK, deriv2mul(DKj, DKk, parts[0], parts[1], parts[2], HKsd))
+    ret = float(np.dot(data, out)) / dotm
+    t2 = float(np.dot(data, hodlr_ldiv(HK, tmp1))) / (dotm * dotm)
+    t2 *= float(np.dot(data, hodlr_ldiv(HK, tmp2)))
+    return len(data) * (ret + t2)
+
+
 def hess_tr2(HK: KernelHODLR, DKj, DKk, D2B2, D2BL, Sjk, v) -> float:
     """``HODLR_hess_tr2`` (stochastichessian.jl:79-89): tp1 = W'^-1 v, tp1 . Deriv2mul(tp1)."""
     tp1 = factor_ldiv_t(HK.W, v)
     return float(np.dot(tp1, deriv2mul(DKj, DKk, D2B2, D2BL, Sjk, tp1)))
 
 
-def stoch_hessian(K: KernelMatrix, HK: KernelHODLR, dat: np.ndarray, vecs) -> np.ndarray:
-    """``stoch_hessian`` (stochastichessian.jl:117-147) with shuffle = false and profile = false:
-    minus the stochastic Fisher matrix, plus for every pair j <= k the solve term (with the
+def stoch_hessian(K: KernelMatrix, HK: KernelHODLR, dat: np.ndarray, vecs, profile: bool = False) -> np.ndarray:
+    """``stoch_hessian`` (stochastichessian.jl:117-147) with shuffle = false: minus the
+    stochastic Fisher matrix, plus for every pair j <= k the solve term (with the
     second-derivative product where the second derivative is not identically zero, otherwise
-    ``HODLR_hess_slv_no2d``) and the trace term (``HODLR_hess_extra``, :33-47).  Returns the
-    symmetric matrix of the upper triangle."""
+    ``HODLR_hess_slv_no2d``) and the trace term (``HODLR_hess_extra``, :33-47).  With
+    ``profile`` (nlpl_hessian, maxlikfunctions.jl:120-136) the solve term is
+    ``HODLR_p_hess_slv``; the reference raises for a ``ZeroFunction`` pair there, and such pairs
+    take its general path with a zero second derivative instead (no D2 term, zero trace term).
+    Returns the symmetric matrix of the upper triangle."""
     if HK.U is not None:
         raise RuntimeError("The matrix needs to be factorized.")
     m = len(K.parms)
     DKs = [derivative_hodlr(K, j, HK) for j in range(m)]
     out = -stoch_fisher(K, HK, DKs, vecs)
     HKsd = hodlr_ldiv(HK, dat)
+    dotm = float(np.dot(dat, HKsd))
     for j in range(m):
         for k in range(j, m):
-            if not d2_is_zero(K.kid, j, k):
+            if profile:
+                parts = None if d2_is_zero(K.kid, j, k) else second_derivative_parts(K, HK, j, k)
+                sterm = p_hess_slv(HK, DKs[j], DKs[k], parts, dat, HKsd, dotm)
+                t2 = 0.0 if parts is None else sum(hess_tr2(HK, DKs[j], DKs[k], *parts, v) for v in vecs) / len(vecs)
+                out[j, k] += 0.5 * t2 - 0.5 * sterm
+            elif not d2_is_zero(K.kid, j, k):
                 D2B2, D2BL, Sjk = second_derivative_parts(K, HK, j, k)
                 sterm = hess_slv(HK, DKs[j], DKs[k], D2B2, D2BL, Sjk, dat, HKsd)
                 t2 = sum(hess_tr2(HK, DKs[j], DKs[k], D2B2, D2BL, Sjk, v) for v in vecs) / len(vecs)

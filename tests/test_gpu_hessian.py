@@ -83,3 +83,41 @@ def test_hessian_after_reassembly_at_a_larger_shape(lib):
                           nystrom=True)
     K.symmetricfactorize(fresh)
     assert np.array_equal(H, K.stoch_hessian(fresh, y_b, V_b))
+
+
+@pytest.mark.parametrize("kid,params", [(O.KERNEL_MATERN32, (1.0, 0.1, 1e-2)), (O.KERNEL_RQ, (1.2, 0.15, 1e-2))])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_profile_hessian_matches_oracle(lib, kid, params, mixed):
+    """km_stoch_profile_hessian against the oracle's stoch_hessian(..., profile = true)
+    (HODLR_p_hess_slv, stochastichessian.jl:15-31) on the same points, data and probes, to the
+    tolerances of the plain Hessian; its NLL and gradient are the profile likelihood's."""
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    n, rank, level = 2048, 32, 3
+    pts = uniform_points(n, 47)
+    y = np.random.default_rng(29).standard_normal(n)
+    V = O.rademacher_probes(n, 8, 31)
+    vecs = [V[:, c] for c in range(V.shape[1])]
+    ok = O.KernelMatrix(pts, pts, np.array(params), kid)
+    ohk = O.build_hodlr(ok, 0.0, rank, O.FixedLevel(level), nystrom=True)
+    O.symmetricfactorize(ohk)
+    H0 = O.stoch_hessian(ok, ohk, y, vecs, profile=True)
+    nll0 = O.profile_negloglik(ohk, y)
+    g0 = O.stoch_profile_gradient(ok, ohk, y, 3, vecs)
+    prec = K.KM_PREC_MIXED if mixed else K.KM_PREC_FP64
+    kern = K.Matern32() if kid == O.KERNEL_MATERN32 else K.RatQuad()
+    hk = K.KernelHODLR(K.KernelMatrix(pts, pts, params, kern), 0.0, rank, K.FixedLevel(level), nystrom=True,
+                       precision=prec)
+    K.symmetricfactorize(hk)
+    nll, g, H = K.grad_fisher_hessian(hk, y, V, profile=True)
+    tol = (1e-5 if mixed else 1e-6) * np.max(np.abs(H0))
+    scale = np.sqrt(np.outer(np.abs(np.diag(H0)), np.abs(np.diag(H0))))
+    etol = (1e-4 if mixed else 1e-5) * scale
+    assert np.array_equal(H, H.T) and np.all(np.isfinite(H))
+    assert np.max(np.abs(H - H0)) <= tol, (H, H0)
+    assert np.all(np.abs(H - H0) <= etol), (H, H0)
+    assert abs(nll - nll0) <= (1e-9 if mixed else 1e-12) * abs(nll0)
+    assert np.all(np.abs(g - g0) <= (1e-5 if mixed else 1e-6) * np.abs(g0) + 1e-8)
+    # the profile form differs from the plain Hessian in its solve terms only
+    assert not np.allclose(H, K.stoch_hessian(hk, y, V))
+    assert np.array_equal(H, K.stoch_hessian(hk, y, V, profile=True))
