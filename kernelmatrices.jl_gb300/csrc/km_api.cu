@@ -88,6 +88,8 @@ struct km_handle {
 
   double* d_pts = nullptr;
   double* d_lnd = nullptr;
+  float* d_pts3 = nullptr;  // mixed form: points and landmarks as exact float triples (km_kfun.cuh)
+  float* d_lnd3 = nullptr;
   int64_t* d_lndidx = nullptr;
   double* d_K = nullptr;
   double* d_Lf = nullptr;
@@ -308,6 +310,7 @@ void free_problem(km_handle* h) {
   h->allocs.clear();
   h->bytes = 0;
   h->d_pts = h->d_lnd = h->d_K = h->d_Lf = h->d_Phi = h->d_Q = h->d_tauleaf = h->d_R = nullptr;
+  h->d_pts3 = h->d_lnd3 = nullptr;
   h->d_S = h->d_Sc = h->d_SinvT = h->d_SinvTf = h->d_Ct = h->d_L22 = h->d_Eref = h->d_Etau = nullptr;
   h->d_L22i = h->d_E = h->d_NT = nullptr;
   h->d_lcscr = nullptr;
@@ -1549,6 +1552,11 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   KM_CUDA(h, cudaMemcpyAsync(h->d_lndidx, idx.data(), sizeof(int64_t) * r, cudaMemcpyHostToDevice, st));
   KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + t.nnode + 1), st));
   KLV(h, KM_PROF_EVAL, launch_gather_points(h->d_pts, h->d_lndidx, r, h->d_lnd, st));
+  if (h->mixed) {
+    if ((rc = grow(h, &h->d_pts3, 8 * n)) || (rc = grow(h, &h->d_lnd3, 8 * r))) return rc;
+    KLV(h, KM_PROF_EVAL, launch_split_points(h->d_pts, n, h->d_pts3, st));
+    KLV(h, KM_PROF_EVAL, launch_split_points(h->d_lnd, r, h->d_lnd3, st));
+  }
   // S = K(P, P), its Cholesky factor and Sc^{-T} are single-CTA chains: they run on the side
   // stream while the leaves and the landmark columns are evaluated on the main stream
   side_begin(h);
@@ -1562,9 +1570,10 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   launch_to_ff(h->d_SinvT, P<ff>(h->d_SinvTf), (int64_t)r * r, h->side);
   h->stats.kernel_launches += 4;
   KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st, h->mixed,
-                                          h->leaf_tc ? P<ff>(h->d_Lf) : nullptr));
+                                          h->leaf_tc ? P<ff>(h->d_Lf) : nullptr, h->mixed ? h->d_pts3 : nullptr));
   h->lf_holds_k = h->leaf_tc;
-  KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, -1, h->d_Phi, st, h->mixed));
+  KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, -1, h->d_Phi, st, h->mixed,
+                                       h->mixed ? h->d_pts3 : nullptr, h->mixed ? h->d_lnd3 : nullptr));
   side_end(h);
   if ((rc = check_launch(h, "assemble")) != KM_OK) return rc;
   h->stats.assemble_ms = timer_stop(h);
@@ -1684,7 +1693,7 @@ int km_factorize(km_handle* h) {
   if (h->mixed && h->leaf_tc && !h->lf_holds_k) {
     // a second factorisation of the same assembly: the leaf matrices evaluated again (the same
     // kernel on the same points, so the same float pairs and FP64 values as the assembly's)
-    KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st, true, P<ff>(h->d_Lf)));
+    KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st, true, P<ff>(h->d_Lf), h->d_pts3));
   }
   h->lf_holds_k = false;
   const int64_t fk[5] = {(int64_t)h->alloc_epoch, t.n, t.L, r, h->mixed ? 1 : 0};
@@ -1962,13 +1971,16 @@ static int gradient_trace(km_handle* h, int64_t p, double wa, double* grad) {
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Phif), t.n * r, st));
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Sinv, P<ff>(h->d_SinvF), (int64_t)r * r, st));
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Sj3, P<ff>(h->d_Sj3F), (int64_t)3 * r * r, st));
-    KLV(h, KM_PROF_EVAL, launch_eval_dphi2<ff>(h->d_pts, h->d_lnd, r, t, h->kp, P<ff>(h->d_dPhi2), st));
+    KLV(h, KM_PROF_EVAL, launch_eval_dphi2<ff>(h->d_pts, h->d_lnd, h->d_pts3, h->d_lnd3, r, t, h->kp,
+                                                P<ff>(h->d_dPhi2), st));
     // X in float pairs (d_U is free here: no product dK X is formed)
     KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_T, P<ff>(h->d_U), n * kk, st));
-    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dk_gram<ff>(h->d_pts, h->kp, P<ff>(h->d_U), n, (int)p, wa, t, leafpart, st));
+    KLV(h, KM_PROF_LEAF_APPLY,
+        launch_leaf_dk_gram<ff>(h->d_pts, h->d_pts3, h->kp, P<ff>(h->d_U), n, (int)p, wa, t, leafpart, st));
   } else {
-    KLV(h, KM_PROF_EVAL, launch_eval_dphi2<double>(h->d_pts, h->d_lnd, r, t, h->kp, h->d_dPhi2, st));
-    KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dk_gram<double>(h->d_pts, h->kp, h->d_T, n, (int)p, wa, t, leafpart, st));
+    KLV(h, KM_PROF_EVAL, launch_eval_dphi2<double>(h->d_pts, h->d_lnd, nullptr, nullptr, r, t, h->kp, h->d_dPhi2, st));
+    KLV(h, KM_PROF_LEAF_APPLY,
+        launch_leaf_dk_gram<double>(h->d_pts, nullptr, h->kp, h->d_T, n, (int)p, wa, t, leafpart, st));
   }
   if (t.L > 0) {
     if (h->mixed) {
@@ -2383,7 +2395,7 @@ extern "C" int64_t km_estimate_bytes(int64_t n, int64_t rank, int level_kind, in
   int64_t kb = 0;
   for (int64_t j = 0; j < t.nleaf; ++j) kb += t.leaf_size(j) * t.leaf_size(j);
   auto d = [](int64_t c) { return 8 * std::max<int64_t>(c, 1); };
-  int64_t b = d(2 * n) + d(2 * r) + d(r) + 2 * d(kb) + 2 * d(n * r) + d(t.nleaf * r) + d(slots * r * r) +
+  int64_t b = d(2 * n) + d(2 * r) + d(4 * n) + d(4 * r) + d(r) + 2 * d(kb) + 2 * d(n * r) + d(t.nleaf * r) + d(slots * r * r) +
               4 * d(r * r) + 3 * d(nn * r * r) + d(nn * r) + d(nn * r * r) + d(nn * 2 * r * r) + d(nn * 5 * r * r) +
               4 * std::max<int64_t>(t.nleaf + t.nnode + 1, 1) + d(kLogdetBlocks) + d(4);
   b += 2 * d(slots * r * k) + d(nn * 2 * r * k);  // ensure_vec

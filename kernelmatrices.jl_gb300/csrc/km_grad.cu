@@ -538,7 +538,8 @@ void launch_d2_assemble(const double* M, int r, double* Tmul, double* Tmult, cud
 // (the panel layout of Phi, two panels), float pairs in the mixed form.  The nugget derivative
 // [x == p] is handled by k_nugget_proj.  grid (ceil(m r / 256), nleaf), block 256.
 template <typename T>
-__global__ void k_eval_dphi2(const double* __restrict__ pts, const double* __restrict__ lnd, int r, DTree t,
+__global__ void k_eval_dphi2(const double* __restrict__ pts, const double* __restrict__ lnd,
+                             const float* __restrict__ P3, const float* __restrict__ L3, int r, DTree t,
                              KParams kp, T* __restrict__ dPhi2) {
   extern __shared__ double sl[];  // 2r
   for (int q = threadIdx.x; q < 2 * r; q += blockDim.x) sl[q] = lnd[q];
@@ -552,8 +553,11 @@ __global__ void k_eval_dphi2(const double* __restrict__ pts, const double* __res
   const double x = pts[2 * (s + i)], y = pts[2 * (s + i) + 1];
   const int64_t o = s * r + (int64_t)c * m + i, nr = t.n * (int64_t)r;
   if constexpr (std::is_same<T, ff>::value) {
+    f3 x1, y1, x2, y2;
+    load_p3(P3, s + i, x1, y1);
+    load_p3(L3, c, x2, y2);
     ff v[3];
-    dkernel3_ff(kp, x, y, sl[2 * c], sl[2 * c + 1], v);
+    dkernel3_ffp(kp, x1, y1, x2, y2, v);
     dPhi2[o] = v[0];
     dPhi2[o + nr] = v[1];
   } else {
@@ -805,7 +809,8 @@ __device__ __forceinline__ ff twice(ff x) { return ff(x.hi + x.hi, x.lo + x.lo);
 // distance and one exponential for the three), off-diagonal entries counted twice.
 // grid (nleaf, S), block (32, 8).
 template <typename T>
-__global__ void __launch_bounds__(256) k_leaf_dk_gram(const double* __restrict__ pts, KParams kp,
+__global__ void __launch_bounds__(256) k_leaf_dk_gram(const double* __restrict__ pts, const float* __restrict__ P3,
+                                                      KParams kp,
                                                       const T* __restrict__ X, int64_t n, int p, double wa,
                                                       DTree t, double* __restrict__ part) {
   const int64_t leaf = blockIdx.x;
@@ -850,20 +855,31 @@ __global__ void __launch_bounds__(256) k_leaf_dk_gram(const double* __restrict__
           for (int q = 0; q < 4; ++q) sa[q] += a * xc[ty + 8 * q][p - c0];
         }
       }
-      const double xi = i < m ? pts[2 * (s + i)] : 0.0, yi = i < m ? pts[2 * (s + i) + 1] : 0.0;
+      double xi = 0.0, yi = 0.0;
+      f3 x3i{}, y3i{};
+      if (i < m) {
+        if constexpr (std::is_same<T, ff>::value) {
+          load_p3(P3, s + i, x3i, y3i);
+        } else {
+          xi = pts[2 * (s + i)];
+          yi = pts[2 * (s + i) + 1];
+        }
+      }
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int a = tj * 32 + ty + 8 * q;
         if (i < m && a < m && i >= a) {
           T gv = T(accv(sp[q]) * wp) + T(accv(sa[q]) * w_a);
           if (i > a) gv = twice(gv);
-          const double xa = pts[2 * (s + a)], ya = pts[2 * (s + a) + 1];
           if constexpr (std::is_same<T, ff>::value) {
+            f3 x3a, y3a;
+            load_p3(P3, s + a, x3a, y3a);
             ff dk[3];
-            dkernel3_ff(kp, xi, yi, xa, ya, dk);
+            dkernel3_ffp(kp, x3i, y3i, x3a, y3a, dk);
 #pragma unroll
             for (int j = 0; j < 3; ++j) tot[j] += gv * dk[j];
           } else {
+            const double xa = pts[2 * (s + a)], ya = pts[2 * (s + a) + 1];
             double dk[3];
             dkernel3(kp, xi, yi, xa, ya, dk);
 #pragma unroll
@@ -911,10 +927,10 @@ __global__ void k_grad_final(const double* __restrict__ a, int64_t na, const dou
 }
 
 template <typename T>
-void launch_eval_dphi2(const double* pts, const double* lnd, int r, const Tree& t, KParams kp, T* dPhi2,
-                       cudaStream_t st) {
+void launch_eval_dphi2(const double* pts, const double* lnd, const float* P3, const float* L3, int r, const Tree& t,
+                       KParams kp, T* dPhi2, cudaStream_t st) {
   dim3 grid((unsigned)((t.max_leaf * r + 255) / 256), (unsigned)t.nleaf);
-  k_eval_dphi2<T><<<grid, 256, 2 * r * sizeof(double), st>>>(pts, lnd, r, dtree(t), kp, dPhi2);
+  k_eval_dphi2<T><<<grid, 256, 2 * r * sizeof(double), st>>>(pts, lnd, P3, L3, r, dtree(t), kp, dPhi2);
 }
 
 template <typename T>
@@ -950,11 +966,11 @@ int leaf_dk_gram_parts(const Tree& t) {
 }
 
 template <typename T>
-void launch_leaf_dk_gram(const double* pts, KParams kp, const T* X, int64_t n, int p, double wa, const Tree& t,
-                         double* part, cudaStream_t st) {
+void launch_leaf_dk_gram(const double* pts, const float* P3, KParams kp, const T* X, int64_t n, int p, double wa,
+                         const Tree& t, double* part, cudaStream_t st) {
   const int S = leaf_dk_gram_parts(t);
-  k_leaf_dk_gram<T><<<dim3((unsigned)t.nleaf, (unsigned)S), dim3(32, 8), 0, st>>>(pts, kp, X, n, p, wa, dtree(t),
-                                                                                  part);
+  k_leaf_dk_gram<T><<<dim3((unsigned)t.nleaf, (unsigned)S), dim3(32, 8), 0, st>>>(pts, P3, kp, X, n, p, wa,
+                                                                                  dtree(t), part);
 }
 
 void launch_grad_final(const double* a, int64_t na, const double* b, int64_t nb, double scale, double* out,
@@ -962,9 +978,10 @@ void launch_grad_final(const double* a, int64_t na, const double* b, int64_t nb,
   k_grad_final<<<3, 256, 0, st>>>(a, na, b, nb, scale, out);
 }
 
-template void launch_eval_dphi2<double>(const double*, const double*, int, const Tree&, KParams, double*,
-                                        cudaStream_t);
-template void launch_eval_dphi2<ff>(const double*, const double*, int, const Tree&, KParams, ff*, cudaStream_t);
+template void launch_eval_dphi2<double>(const double*, const double*, const float*, const float*, int, const Tree&,
+                                        KParams, double*, cudaStream_t);
+template void launch_eval_dphi2<ff>(const double*, const double*, const float*, const float*, int, const Tree&,
+                                    KParams, ff*, cudaStream_t);
 template void launch_leaf_proj3<double>(const double*, const double*, int, const Tree&, const double*, int64_t,
                                         double*, int, cudaStream_t);
 template void launch_leaf_proj3<ff>(const ff*, const ff*, int, const Tree&, const ff*, int64_t, double*, int,
@@ -973,10 +990,10 @@ template void launch_landmark<double>(const double*, int, int, int, double, cons
                                       double*, cudaStream_t);
 template void launch_landmark<ff>(const double*, int, int, int, double, const ff*, const ff*, int64_t, double*,
                                   cudaStream_t);
-template void launch_leaf_dk_gram<double>(const double*, KParams, const double*, int64_t, int, double, const Tree&,
-                                          double*, cudaStream_t);
-template void launch_leaf_dk_gram<ff>(const double*, KParams, const ff*, int64_t, int, double, const Tree&, double*,
-                                      cudaStream_t);
+template void launch_leaf_dk_gram<double>(const double*, const float*, KParams, const double*, int64_t, int, double,
+                                          const Tree&, double*, cudaStream_t);
+template void launch_leaf_dk_gram<ff>(const double*, const float*, KParams, const ff*, int64_t, int, double,
+                                      const Tree&, double*, cudaStream_t);
 
 void launch_small_gemm(const double* A, const double* B, int r, int transB, double* C, cudaStream_t st) {
   k_small_gemm<<<r, 128, 0, st>>>(A, B, r, transB, C);

@@ -78,9 +78,13 @@ struct NodeMatsH {          // node factors (double or float pairs, by the calle
 // use_ff: float-pair evaluation on the FP32 pipe (mixed form, ~1e-14 relative), else FP64
 // Kff: also the float-pair entries of the kernel itself (mixed form, deriv < 0), lower triangle
 void launch_eval_leaves(const double* pts, const Tree& t, KParams kp, int deriv, double* K,
-                        cudaStream_t st, bool use_ff = false, ff* Kff = nullptr);
+                        cudaStream_t st, bool use_ff = false, ff* Kff = nullptr, const float* P3 = nullptr);
 void launch_eval_phi(const double* pts, const double* lnd, int r, const Tree& t, KParams kp,
-                     int deriv, double* Phi, cudaStream_t st, bool use_ff = false);
+                     int deriv, double* Phi, cudaStream_t st, bool use_ff = false, const float* P3 = nullptr,
+                     const float* L3 = nullptr);
+// P3: 8 floats a point, the exact float triples of x and y (km_kfun.cuh), for the float-pair
+// evaluations
+void launch_split_points(const double* pts, int64_t n, float* P3, cudaStream_t st);
 void launch_eval_dense(const double* a, int na, const double* b, int nb, KParams kp, int deriv,
                        double* out, int ld, cudaStream_t st);
 void launch_gather_points(const double* pts, const int64_t* idx, int r, double* lnd,
@@ -175,8 +179,8 @@ void launch_axpby(double* y, const double* x, double a, double b, int64_t n, cud
 // trace form of the stochastic gradient (km_grad.cu).  X: n x k (k = p + 1: p probes with weight
 // 1/p, then alpha with weight wa); W = 4r projection rows per (leaf, column) pair.
 template <typename T>
-void launch_eval_dphi2(const double* pts, const double* lnd, int r, const Tree& t, KParams kp, T* dPhi2,
-                       cudaStream_t st);
+void launch_eval_dphi2(const double* pts, const double* lnd, const float* P3, const float* L3, int r, const Tree& t,
+                       KParams kp, T* dPhi2, cudaStream_t st);
 template <typename T>
 void launch_leaf_proj3(const T* Phi, const T* dPhi2, int r, const Tree& t, const T* X, int64_t ldx, double* VP, int k,
                        cudaStream_t st);
@@ -188,8 +192,8 @@ void launch_landmark(const double* VP, int r, int k, int p, double wa, const T* 
                      double* part, cudaStream_t st);
 int leaf_dk_gram_parts(const Tree& t);  // CTAs per leaf of the leaf term (partial sums per leaf)
 template <typename T>
-void launch_leaf_dk_gram(const double* pts, KParams kp, const T* X, int64_t n, int p, double wa, const Tree& t,
-                         double* part, cudaStream_t st);
+void launch_leaf_dk_gram(const double* pts, const float* P3, KParams kp, const T* X, int64_t n, int p, double wa,
+                         const Tree& t, double* part, cudaStream_t st);
 // out[j] = scale * (sum_q a[j * na + q] + sum_q b[j * nb + q]) for j < 3, fixed order
 void launch_grad_final(const double* a, int64_t na, const double* b, int64_t nb, double scale, double* out,
                        cudaStream_t st);

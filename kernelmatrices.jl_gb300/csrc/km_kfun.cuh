@@ -7,9 +7,8 @@ namespace km {
 
 // ---------------------------------------------------------------------------------------------
 // Float-pair evaluation for the mixed form.  The FP64 evaluation is bound by the FP64 pipe
-// (sqrt, two divisions and exp per entry); here only the coordinate differences are formed in
-// FP64 and everything else runs on the FP32 pipe in float pairs, to about 1e-14 relative
-// (entries below 1e-37 round to 0).
+// (sqrt, two divisions and exp per entry); here everything runs on the FP32 pipe in float pairs,
+// to about 1e-14 relative (entries below 1e-37 round to 0).
 //
 // exp(-z), z >= 0: Cody-Waite reduction z = k ln2 + f with k = rint(z / ln2), |f| <= ln2/2, and
 // the Taylor series of exp(-f) to degree 13 (remainder < 2e-16 for |f| <= 0.347), scaled by
@@ -37,10 +36,43 @@ __device__ __forceinline__ ff ff_exp_neg(ff z) {
   return ff(p.hi * sc, p.lo * sc);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Coordinates as exact float triples.  A double x is split into h = fl32(x), m = fl32(x - h),
+// l = x - h - m (at most 7 significant bits, exact in a float), so x = h + m + l exactly; the
+// points are split once per assembly (k_split_points) and the float-pair evaluations form the
+// coordinate differences from the triples on the FP32 pipe, with no FP64 instruction: the FP64
+// pipe (2 operations per clock per SM) had bounded the float-pair evaluation kernels on the
+// conversions of the FP64 differences.  Two triples are equal component by component exactly
+// when the doubles are equal (x == y, the nugget's test).
+// ---------------------------------------------------------------------------------------------
+struct f3 {
+  float h, m, l;
+};
+
+__device__ __forceinline__ f3 split3(double x) {
+  const float h = __double2float_rn(x);
+  const double r1 = x - (double)h;  // exact
+  const float m = __double2float_rn(r1);
+  return f3{h, m, __double2float_rn(r1 - (double)m)};  // exact
+}
+
+__device__ __forceinline__ bool eq3(const f3& a, const f3& b) { return a.h == b.h && a.m == b.m && a.l == b.l; }
+
+// the float pair nearest (to about 2^-48 relative, or far below the pair's precision in absolute
+// terms) to a - b: the high and middle differences exactly by TwoSum, the low ones rounded
+__device__ __forceinline__ ff ff_sub3(const f3& a, const f3& b) {
+  float s, e, t, f;
+  ff_two_sum(a.h, -b.h, s, e);
+  ff_two_sum(a.m, -b.m, t, f);
+  ff r = ff(s, e) + ff(t, f);
+  return r + ff(__fsub_rn(a.l, b.l), 0.f);
+}
+
 // kernel_value (km_internal.h) in float pairs, without the nugget; the same formulas and
-// special cases.
-__device__ __forceinline__ ff kernel_value_ffv(const KParams& kp, double x1, double y1, double x2, double y2) {
-  const ff dx(__dsub_rn(x1, x2)), dy(__dsub_rn(y1, y2));
+// special cases, on split coordinates.
+__device__ __forceinline__ ff kernel_value_ffp(const KParams& kp, const f3& x1, const f3& y1, const f3& x2,
+                                               const f3& y2) {
+  const ff dx = ff_sub3(x1, x2), dy = ff_sub3(y1, y2);
   const ff r = sqrt(ff(dx * dx) + dy * dy);
   ff out;
   if (kp.kid == KM_KERNEL_RATQUAD) {
@@ -60,42 +92,66 @@ __device__ __forceinline__ ff kernel_value_ffv(const KParams& kp, double x1, dou
   return out;
 }
 
+__device__ __forceinline__ ff kernel_value_ffv(const KParams& kp, double x1, double y1, double x2, double y2) {
+  return kernel_value_ffp(kp, split3(x1), split3(y1), split3(x2), split3(y2));
+}
+
 __device__ __forceinline__ double kernel_value_ff(const KParams& kp, double x1, double y1, double x2, double y2) {
   double v = to_double(kernel_value_ffv(kp, x1, y1, x2, y2));
   if (x1 == x2 && y1 == y2) v = __dadd_rn(v, kp.p2);
   return v;
 }
 
-// dkernel_value (km_internal.h) in float pairs.
-__device__ __forceinline__ double dkernel_value_ff(const KParams& kp, int j, double x1, double y1, double x2,
-                                                   double y2) {
-  const bool same = (x1 == x2 && y1 == y2);
-  if (j == 2) return same ? 1.0 : 0.0;
-  const ff dx(__dsub_rn(x1, x2)), dy(__dsub_rn(y1, y2));
+// dkernel_value (km_internal.h) for the three parameters at once in float pairs, on split
+// coordinates: one distance and, for the Matern kernel, one exponential shared by the scale and
+// range derivatives.
+__device__ __forceinline__ void dkernel3_ffp(const KParams& kp, const f3& x1, const f3& y1, const f3& x2,
+                                             const f3& y2, ff (&out)[3]) {
+  out[2] = (eq3(x1, x2) && eq3(y1, y2)) ? ff(1.0) : ff(0.0);
+  const ff dx = ff_sub3(x1, x2), dy = ff_sub3(y1, y2);
   const ff r2 = ff(dx * dx) + dy * dy;
   const ff r = sqrt(r2);
   if (kp.kid == KM_KERNEL_RATQUAD) {
     const ff t = r / ff(kp.p1);
     const ff u = ff(1.0) + t * t;
-    if (j == 0) return to_double(ff(ff(2.0) * ff(kp.p0)) / ff(u * u));
+    out[0] = ff(ff(2.0) * ff(kp.p0)) / ff(u * u);
     const ff num = ff(ff(4.0) * ff(ff(kp.p0) * ff(kp.p0))) * r2;
     const ff p13 = ff(ff(kp.p1) * ff(kp.p1)) * ff(kp.p1);
-    return to_double((num / p13) / ff(ff(u * u) * u));
+    out[1] = (num / p13) / ff(ff(u * u) * u);
+    return;
   }
-  if (j == 0) {
-    if (!(r.hi > 0.f)) return 1.0;
-    const ff x = r / ff(kp.p1);
-    if (!(x.hi > 1.0e-8f)) return 1.0;
-    const ff z = ff(kSqrt3) * x;
-    return to_double(ff((ff(1.0) + z)) * ff_exp_neg(z));
-  }
-  if (!(r.hi > 0.f)) return 0.0;
+  out[0] = ff(1.0);
+  out[1] = ff(0.0);
+  if (!(r.hi > 0.f)) return;
   const ff x = r / ff(kp.p1);
-  if (!(x.hi > 1.0e-8f)) return 0.0;
+  if (!(x.hi > 1.0e-8f)) return;
   // -p0 * cor'(x) * r / p1^2 with cor'(x) = -3 x exp(-sqrt3 x)
-  const ff e = ff_exp_neg(ff(kSqrt3) * x);
+  const ff z = ff(kSqrt3) * x;
+  const ff e = ff_exp_neg(z);
+  out[0] = ff((ff(1.0) + z) * e);
   const ff num = ff(ff(3.0) * ff(kp.p0)) * ff(x * e);
-  return to_double(ff(num * r) / ff(ff(kp.p1) * ff(kp.p1)));
+  out[1] = ff(num * r) / ff(ff(kp.p1) * ff(kp.p1));
+}
+
+__device__ __forceinline__ void dkernel3_ff(const KParams& kp, double x1, double y1, double x2, double y2,
+                                            ff (&out)[3]) {
+  dkernel3_ffp(kp, split3(x1), split3(y1), split3(x2), split3(y2), out);
+}
+
+// dkernel_value (km_internal.h) in float pairs.
+__device__ __forceinline__ double dkernel_value_ff(const KParams& kp, int j, double x1, double y1, double x2,
+                                                   double y2) {
+  ff v[3];
+  dkernel3_ff(kp, x1, y1, x2, y2, v);
+  return to_double(v[j]);
+}
+
+// split coordinates of point i from the array of 8 floats a point (xh, xm, xl, yh, ym, yl, 0, 0)
+__device__ __forceinline__ void load_p3(const float* __restrict__ P3, int64_t i, f3& x, f3& y) {
+  const float4 a = *reinterpret_cast<const float4*>(P3 + 8 * i);
+  const float4 b = *reinterpret_cast<const float4*>(P3 + 8 * i + 4);
+  x = f3{a.x, a.y, a.z};
+  y = f3{a.w, b.x, b.y};
 }
 
 __device__ __forceinline__ double eval_entry(bool use_ff, const KParams& kp, int deriv, double x1, double y1,
@@ -135,35 +191,6 @@ __device__ __forceinline__ void dkernel3(const KParams& kp, double x1, double y1
   out[0] = __dmul_rn(__dadd_rn(1.0, z), e);
   const double dc = __dmul_rn(__dmul_rn(-3.0, x), e);
   out[1] = __ddiv_rn(__dmul_rn(__dmul_rn(-kp.p0, dc), r), __dmul_rn(kp.p1, kp.p1));
-}
-
-// dkernel_value_ff for the three parameters at once, as float pairs (the same formulas; one
-// float-pair exponential for the scale and range derivatives of the Matern kernel).
-__device__ __forceinline__ void dkernel3_ff(const KParams& kp, double x1, double y1, double x2, double y2,
-                                            ff (&out)[3]) {
-  out[2] = (x1 == x2 && y1 == y2) ? ff(1.0) : ff(0.0);
-  const ff dx(__dsub_rn(x1, x2)), dy(__dsub_rn(y1, y2));
-  const ff r2 = ff(dx * dx) + dy * dy;
-  const ff r = sqrt(r2);
-  if (kp.kid == KM_KERNEL_RATQUAD) {
-    const ff t = r / ff(kp.p1);
-    const ff u = ff(1.0) + t * t;
-    out[0] = ff(ff(2.0) * ff(kp.p0)) / ff(u * u);
-    const ff num = ff(ff(4.0) * ff(ff(kp.p0) * ff(kp.p0))) * r2;
-    const ff p13 = ff(ff(kp.p1) * ff(kp.p1)) * ff(kp.p1);
-    out[1] = (num / p13) / ff(ff(u * u) * u);
-    return;
-  }
-  out[0] = ff(1.0);
-  out[1] = ff(0.0);
-  if (!(r.hi > 0.f)) return;
-  const ff x = r / ff(kp.p1);
-  if (!(x.hi > 1.0e-8f)) return;
-  const ff z = ff(kSqrt3) * x;
-  const ff e = ff_exp_neg(z);
-  out[0] = ff((ff(1.0) + z) * e);
-  const ff num = ff(ff(3.0) * ff(kp.p0)) * ff(x * e);
-  out[1] = ff(num * r) / ff(ff(kp.p1) * ff(kp.p1));
 }
 
 }  // namespace km
