@@ -728,11 +728,9 @@ int nystrom_matvec(km_handle* h, const double* X, double* Y, int k) {
   if (h->method == KM_METHOD_ACA) return general_matvec(h, X, Y, k);
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
-  NodeMatsH nm = node_mats(h);
   if (t.L > 0) {
     KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_phiT(h->d_Phi, h->r, t, X, t.n, h->d_VP, k, st));
-    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up<double>(t, nm, l, h->d_VP, h->d_VD, k, UP_SUM_, st));
-    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down<double>(t, nm, l, h->d_VP, h->d_VG, h->d_VD, k, DN_NYS_, st));
+    KLV(h, KM_PROF_SWEEP, launch_nys_sums(h->d_VP, h->d_VG, t.nleaf, h->r, k, st));
   } else {
     cudaMemsetAsync(h->d_VG, 0, sizeof(double) * h->r * k, st);
   }
@@ -865,14 +863,12 @@ int derivative_apply(km_handle* h, int j, const double* X, double* Y, int k) {
     }
     h->dk_param = j;
   }
-  NodeMatsH nm2{nullptr, nullptr, nullptr, nullptr, 2 * r};
   if (t.L > 0) {
     if (h->mixed)
       KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dphiT<ff>(P<ff>(h->d_Phif), P<ff>(h->d_dPhif), r, t, X, t.n, h->d_GP, k, st));
     else
       KLV(h, KM_PROF_LEAF_APPLY, launch_leaf_dphiT<double>(h->d_Phi, h->d_dPhi, r, t, X, t.n, h->d_GP, k, st));
-    for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up<double>(t, nm2, l, h->d_GP, nullptr, k, UP_SUM_, st));
-    for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down<double>(t, nm2, l, h->d_GP, h->d_GG, nullptr, k, DN_NYS_, st));
+    KLV(h, KM_PROF_SWEEP, launch_nys_sums(h->d_GP, h->d_GG, t.nleaf, 2 * r, k, st));
   } else {
     KM_CUDA(h, cudaMemsetAsync(h->d_GG, 0, sizeof(double) * 2 * r * k, st));
   }

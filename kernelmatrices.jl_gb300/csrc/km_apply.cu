@@ -319,39 +319,15 @@ __global__ void __launch_bounds__(512) k_down(NodeMats<T> nm, int level, int L, 
   }
 }
 
-// VP[leaf][col] = Phi_leaf' x_leaf  (r values), Phi per leaf column-major m x r.
-// grid = (nleaf, ceil(k/8)), block 256, warp per column.
-__global__ void __launch_bounds__(256) k_leaf_phiT(const double* __restrict__ Phi, int r, DTree t,
-                                                   const double* __restrict__ X, int64_t ldx,
-                                                   double* __restrict__ VP, int k) {
-  extern __shared__ double sm[];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int col = blockIdx.y * 8 + w;
-  if (col >= k) return;
-  const int64_t leaf = blockIdx.x;
-  const int m = d_leaf_size(t, leaf);
-  const int64_t s = d_leaf_start(t, leaf);
-  double* x = sm + (size_t)w * m;
-  const double* src = X + (int64_t)col * ldx + s;
-  for (int i = lane; i < m; i += 32) x[i] = src[i];
-  __syncwarp();
-  const double* P = Phi + s * r;
-  double* out = VP + (leaf * k + col) * r;
-  for (int c = 0; c < r; ++c) {
-    const double* pc = P + (int64_t)c * m;
-    double acc = 0.0;
-    for (int i = lane; i < m; i += 32) acc += pc[i] * x[i];
-    acc = warp_sum(acc);
-    if (lane == 0) out[c] = acc;
-  }
-}
 
 // y_leaf = K_leaf x_leaf + Phi_leaf S^{-1} a_leaf, a_leaf = VG[leaf] (sum of the siblings'
 // projections along the path to the root).  This is the leaf product plus the sum over levels
 // of U (V' x) and V (U' x) with U = K(rows, P), V = K(cols, P) S^{-1}
 // (src/HODLR/src/baseoverloads.jl:158-169, src/factorizations.jl:86-94).
 // grid = (nleaf, ceil(k/8)), block 256: x chunk (m x 8) and beta (r x 8) staged in shared.
-__global__ void __launch_bounds__(256) k_leaf_nys_apply(const double* __restrict__ Kl, const double* __restrict__ Phi,
+constexpr int kNaRows = 128, kNaParts = 4;  // k_leaf_nys_apply: rows a pass x parts of each row's sum
+
+__global__ void __launch_bounds__(512) k_leaf_nys_apply(const double* __restrict__ Kl, const double* __restrict__ Phi,
                                                         const double* __restrict__ Sc, int r, DTree t,
                                                         const double* __restrict__ X, int64_t ldx,
                                                         const double* __restrict__ VG, double* __restrict__ Y,
@@ -391,16 +367,52 @@ __global__ void __launch_bounds__(256) k_leaf_nys_apply(const double* __restrict
     }
   }
   __syncthreads();
+  // y_i = sum_l K[i][l] x_l + sum_q Phi[i][q] beta_q for the nc columns: thread (row i of a block
+  // of kNaRows, part p of kNaParts) takes the columns l and landmarks q of its part, each loaded
+  // entry feeding the nc columns; the parts are added in order through shared memory.
   const double* K = Kl + d_leaf_koff(t, leaf);
   const double* P = Phi + s * r;
-  for (int e = threadIdx.x; e < nc * m; e += blockDim.x) {
-    const int c = e / m, i = e % m;
-    const double* xc = xs + c * m;
-    double acc = 0.0;
-    for (int l = 0; l < m; ++l) acc += K[i + (int64_t)l * m] * xc[l];
-    const double* bc = bs + c * r;
-    for (int q = 0; q < r; ++q) acc += P[i + (int64_t)q * m] * bc[q];
-    Y[(int64_t)(c0 + c) * ldy + s + i] = acc;
+  double* red = bs + 8 * r;  // kNaParts x kNaRows x 8
+  const int il = threadIdx.x % kNaRows, part = threadIdx.x / kNaRows;
+  const int l0 = (int)((int64_t)m * part / kNaParts), l1 = (int)((int64_t)m * (part + 1) / kNaParts);
+  const int q0 = r * part / kNaParts, q1 = r * (part + 1) / kNaParts;
+  for (int i0 = 0; i0 < m; i0 += kNaRows) {
+    const int i = i0 + il;
+    double acc[8] = {};
+    if (i < m && nc == 1) {  // one column: two independent chains, no idle column slots
+      double a1 = 0.0;
+      int l = l0;
+      for (; l + 1 < l1; l += 2) {
+        acc[0] += K[i + (int64_t)l * m] * xs[l];
+        a1 += K[i + (int64_t)(l + 1) * m] * xs[l + 1];
+      }
+      if (l < l1) acc[0] += K[i + (int64_t)l * m] * xs[l];
+      for (int q = q0; q < q1; ++q) a1 += P[i + (int64_t)q * m] * bs[q];
+      acc[0] += a1;
+    } else if (i < m) {
+      for (int l = l0; l < l1; ++l) {
+        const double kv = K[i + (int64_t)l * m];
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          if (c < nc) acc[c] += kv * xs[c * m + l];
+      }
+      for (int q = q0; q < q1; ++q) {
+        const double pv = P[i + (int64_t)q * m];
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          if (c < nc) acc[c] += pv * bs[c * r + q];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) red[(part * kNaRows + il) * 8 + c] = acc[c];
+    __syncthreads();
+    if (part == 0 && i < m)
+      for (int c = 0; c < nc; ++c) {
+        double v = red[il * 8 + c];
+        for (int u = 1; u < kNaParts; ++u) v += red[(u * kNaRows + il) * 8 + c];
+        Y[(int64_t)(c0 + c) * ldy + s + i] = v;
+      }
+    __syncthreads();
   }
 }
 
@@ -477,20 +489,46 @@ void launch_down(const Tree& t, const NodeMatsH& h, int level, const T* VP, T* V
                                           t.node_off[level], VP, VG, VD, k, mode, kcb);
 }
 
-void launch_leaf_phiT(const double* Phi, int r, const Tree& t, const double* X, int64_t ldx, double* VP,
-                      int k, cudaStream_t st) {
-  dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
-  const size_t sm = (size_t)8 * t.max_leaf * sizeof(double);
-  smem_limit((const void*)k_leaf_phiT, sm);
-  k_leaf_phiT<<<grid, 256, sm, st>>>(Phi, r, dtree(t), X, ldx, VP, k);
+// VG[(leaf k + c) W + q] = A[c][q] - VP[(leaf k + c) W + q], A = sum over the leaves of VP: the
+// landmark coefficients every leaf receives from the off-diagonal blocks of a Nystrom HODLR.
+// All its off-diagonal blocks are Phi_rows S^{-1} Phi_cols' with the one landmark set
+// (nystrom_uvt, src/factorizations.jl:86-94), so the blocks along a leaf's path to the root
+// together hold every other leaf once and the sum of the siblings' projections is the total
+// minus the leaf's own: one pass over the leaf slots in place of the up- and down-sweeps of
+// the tree.  A is summed in a fixed order (warp w takes the leaves w, w + 8, ..., then the warp
+// sums in order).  grid (k, ceil(W / 32)), block 256.
+__global__ void k_nys_sums(const double* __restrict__ VP, double* __restrict__ VG, int64_t nleaf, int W, int k) {
+  __shared__ double red[8][32];
+  const int c = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int q = blockIdx.y * 32 + lane;
+  double s = 0.0;
+  if (q < W) {
+#pragma unroll 4
+    for (int64_t l = w; l < nleaf; l += 8) s += VP[(l * k + c) * W + q];
+  }
+  red[w][lane] = s;
+  __syncthreads();
+  double tot = 0.0;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) tot += red[u][lane];
+  if (q < W)
+    for (int64_t l = w; l < nleaf; l += 8) {
+      const int64_t e = (l * k + c) * W + q;
+      VG[e] = tot - VP[e];
+    }
 }
+
+void launch_nys_sums(const double* VP, double* VG, int64_t nleaf, int W, int k, cudaStream_t st) {
+  k_nys_sums<<<dim3((unsigned)k, (unsigned)((W + 31) / 32)), 256, 0, st>>>(VP, VG, nleaf, W, k);
+}
+
 void launch_leaf_nys_apply(const double* Kl, const double* Phi, const double* Sc, int r, const Tree& t,
                            const double* X, int64_t ldx, const double* VG, double* Y, int64_t ldy, int k,
                            cudaStream_t st) {
   dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
-  const size_t sm = (size_t)8 * (t.max_leaf + r) * sizeof(double);
+  const size_t sm = ((size_t)8 * (t.max_leaf + r) + (size_t)kNaParts * kNaRows * 8) * sizeof(double);
   smem_limit((const void*)k_leaf_nys_apply, sm);
-  k_leaf_nys_apply<<<grid, 256, sm, st>>>(Kl, Phi, Sc, r, dtree(t), X, ldx, VG, Y, ldy, k);
+  k_leaf_nys_apply<<<grid, kNaParts * kNaRows, sm, st>>>(Kl, Phi, Sc, r, dtree(t), X, ldx, VG, Y, ldy, k);
 }
 
 template void launch_up<double>(const Tree&, const NodeMatsH&, int, double*, double*, int, int, cudaStream_t);

@@ -17,19 +17,20 @@
 
 namespace km {
 
-// VP[leaf][col] = [Phi_leaf' x ; dPhi_leaf' x]  (2r values) for a chunk of 8 columns.  The leaf is
-// processed in chunks of 32 rows: [Phi dPhi] (32 x 2r) and x (8 x 32) are staged in shared
-// memory as T, and thread q < 2r owns output row q with 8 accumulators.  T = double (FP64 form)
-// or ff (mixed form: float-pair copies of Phi and dPhi, x converted on load).
-// grid (nleaf, ceil(k/8)), block 256.
+// VP[leaf][col] = [Phi_leaf' x ; dPhi_leaf' x]  (nmat r values: nmat = 2, or nmat = 1 for
+// Phi_leaf' x alone) for a chunk of 8 columns.  The leaf is processed in chunks of 32 rows:
+// [Phi dPhi] (32 x nmat r) and x (8 x 32) are staged in shared memory as T, and thread
+// q < nmat r owns output row q with 8 accumulators.  T = double (FP64 form) or ff (mixed form:
+// float-pair copies of Phi and dPhi, x converted on load).
+// grid (nleaf, ceil(k/8)), block 32 ceil(nmat r / 32) or 256.
 constexpr int kDRows = 32;
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_leaf_dphiT(const T* __restrict__ Phi, const T* __restrict__ dPhi, int r,
                                                     DTree t, const double* __restrict__ X, int64_t ldx,
-                                                    double* __restrict__ VP, int k) {
+                                                    double* __restrict__ VP, int k, int nmat) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int r2 = 2 * r, ldp = r2 + 1;
+  const int r2 = nmat * r, ldp = r2 + 1;
   T* ps = reinterpret_cast<T*>(smraw);   // kDRows x (2r + 1)
   T* xs = ps + kDRows * ldp;              // 8 x kDRows
   const int64_t leaf = blockIdx.x;
@@ -308,7 +309,38 @@ void launch_leaf_dphiT(const T* Phi, const T* dPhi, int r, const Tree& t, const 
   dim3 grid((unsigned)t.nleaf, (unsigned)((k + 7) / 8));
   const size_t sm = ((size_t)kDRows * (2 * r + 1) + 8 * kDRows) * sizeof(T);
   smem_limit((const void*)k_leaf_dphiT<T>, sm);
-  k_leaf_dphiT<T><<<grid, 256, sm, st>>>(Phi, dPhi, r, dtree(t), X, ldx, VP, k);
+  k_leaf_dphiT<T><<<grid, 256, sm, st>>>(Phi, dPhi, r, dtree(t), X, ldx, VP, k, 2);
+}
+
+// VP[(leaf k + c) r + q] = Phi_leaf[:, q]' x_leaf,c: one warp per (leaf, landmark q), lanes over
+// the leaf's rows (coalesced reads of Phi's column and of x), a fixed-order warp sum per
+// column.  grid (nleaf, ceil(r / 8)), block 256.
+__global__ void __launch_bounds__(256) k_leaf_phiT(const double* __restrict__ Phi, int r, DTree t,
+                                                   const double* __restrict__ X, int64_t ldx,
+                                                   double* __restrict__ VP, int k) {
+  const int lane = threadIdx.x & 31, q = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (q >= r) return;
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf);
+  const double* pc = Phi + s * r + (int64_t)q * m;
+  for (int c = 0; c < k; ++c) {
+    const double* xc = X + (int64_t)c * ldx + s;
+    double a0 = 0.0, a1 = 0.0;
+    int i = lane;
+    for (; i + 32 < m; i += 64) {
+      a0 += pc[i] * xc[i];
+      a1 += pc[i + 32] * xc[i + 32];
+    }
+    if (i < m) a0 += pc[i] * xc[i];
+    const double v = warp_sum(a0 + a1);
+    if (lane == 0) VP[(leaf * k + c) * r + q] = v;
+  }
+}
+
+void launch_leaf_phiT(const double* Phi, int r, const Tree& t, const double* X, int64_t ldx, double* VP, int k,
+                      cudaStream_t st) {
+  k_leaf_phiT<<<dim3((unsigned)t.nleaf, (unsigned)((r + 7) / 8)), 256, 0, st>>>(Phi, r, dtree(t), X, ldx, VP, k);
 }
 
 template <typename T>
