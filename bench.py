@@ -157,9 +157,10 @@ class ClockSampler:
 
 def line_config(world: int) -> dict:
     """The workload keys shared by the GPU line and the reference line."""
-    return {"workload": WORKLOAD, "n": N_POINTS, "rank": RANK, "level": "FixedLevel(8)", "nrhs": NRHS,
+    return {"workload": WORKLOAD, "n": N_POINTS, "rank": RANK, "level": f"FixedLevel({LEVEL})", "nrhs": NRHS,
             "kernel": "matern32", "params": list(PARAMS),
-            "l2": "inputs larger than L2 (leaf factors alone 268 MB)", "parallelism": f"replicas{world}"}
+            "l2": "inputs larger than L2 (leaf factors alone 268 MB)", "parallelism": f"replicas{world}",
+            "calls": "km_assemble, km_matvec, km_factorize_solve (symmetricfactorize! + solve), km_logdet"}
 
 
 def host_threads() -> int:
@@ -332,16 +333,17 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             check(h, lib.km_assemble_dev(h, C.c_void_p(d_pts.data_ptr()), n, L.KM_KERNEL_MATERN32, pp, 3,
                                          L.KM_METHOD_NYSTROM, 0.0, RANK, L.KM_LEVEL_FIXED, LEVEL))
             check(h, lib.km_matvec_dev(h, C.c_void_p(d_x.data_ptr()), C.c_void_p(d_y.data_ptr()), 1))
-            check(h, lib.km_factorize(h))
-            check(h, lib.km_solve_dev(h, C.c_void_p(d_rhs.data_ptr()), C.c_void_p(d_sol.data_ptr()), NRHS))
+            # symmetricfactorize! then K \ b as one call (the forward half of the solve overlaps the
+            # factorisation; the same bits as km_factorize + km_solve_dev)
+            check(h, lib.km_factorize_solve_dev(h, C.c_void_p(d_rhs.data_ptr()), C.c_void_p(d_sol.data_ptr()),
+                                                NRHS))
             check(h, lib.km_logdet(h, C.byref(logdet)))
 
         def step_e2e():
             check(h, lib.km_assemble(h, dp(h_pts), n, L.KM_KERNEL_MATERN32, pp, 3, L.KM_METHOD_NYSTROM, 0.0, RANK,
                                      L.KM_LEVEL_FIXED, LEVEL))
             check(h, lib.km_matvec(h, dp(h_x), dp(h_y), 1))
-            check(h, lib.km_factorize(h))
-            check(h, lib.km_solve(h, dp(h_rhs), dp(h_sol), NRHS))
+            check(h, lib.km_factorize_solve(h, dp(h_rhs), dp(h_sol), NRHS))
             check(h, lib.km_logdet(h, C.byref(logdet)))
 
         def timed(fn, steps):
@@ -531,6 +533,50 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def run_grad(args):
+    """One likelihood request of the serving mix at its largest size: assemble (Nystrom rank 72,
+    LogLevel(8)), factorise and evaluate NLL + stochastic gradient with 72 seeded probes for one
+    dataset of n points (Matern nu = 3/2, range 0.1, nugget 1e-3); both precision forms, phase
+    times from host timers around the calls (each call ends with a device synchronisation)."""
+    import torch
+    import kmhodlr as K
+    from kmhodlr.data import uniform_points
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU (no CPU fallback)")
+    n = args.grad_n
+    pts = uniform_points(n, SEED + 21)
+    y = np.random.default_rng(SEED + 22).standard_normal(n)
+    km = K.KernelMatrix(pts, pts, PARAMS, K.Matern32())
+    forms = {}
+    head = L_prec(args.precision)
+    for prec in (head, 1 - head):
+        times = []
+        for it in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            hk = K.KernelHODLR(km, 0.0, RANK, K.LogLevel(8), nystrom=True, precision=prec)
+            K.symmetricfactorize(hk)
+            t1 = time.perf_counter()
+            nll, g = hk.nll_grad_seeded(y, 72, SEED + it)
+            t2 = time.perf_counter()
+            if it >= args.warmup:
+                times.append((t1 - t0, t2 - t1))
+            del hk
+        a = float(np.mean([t[0] for t in times]))
+        b = float(np.mean([t[1] for t in times]))
+        forms["mixed" if prec == 1 else "fp64"] = {"requests_per_s": 1.0 / (a + b), "ms_per_request": 1e3 * (a + b),
+                                                  "assemble_factor_ms": 1e3 * a, "nll_grad_ms": 1e3 * b,
+                                                  "nll": nll, "grad": [float(v) for v in g]}
+    h = forms[args.precision]
+    out = {"metric": "NLL+gradient requests/s", "value": h["requests_per_s"], "unit": "requests/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": h["ms_per_request"], "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head == 0 else "f32x2+f64", "data": "synthetic",
+           "config": {"workload": f"nllgrad_matern32_nystrom_n{n}_r72_loglevel8_72probes", "n": n,
+                      "params": list(PARAMS)},
+           "precision": args.precision, "forms": forms}
+    print(json.dumps(out), flush=True)
+
+
 def L_prec(name: str) -> int:
     return 1 if name == "mixed" else 0
 
@@ -689,6 +735,7 @@ def run_aca(args):
 
 
 def main():
+    global N_POINTS, LEVEL, WORKLOAD
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -699,14 +746,21 @@ def main():
                     help="reference arm: seconds of timed CPU work after which no further step starts")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed",
                     help="form reported as `value` (the other form is reported beside it)")
-    ap.add_argument("--workload", choices=["c2", "batch", "serve", "aca"], default="c2",
-                    help="c2: the headline factor+solve+logdet step; batch / serve / aca: the other forms")
+    ap.add_argument("--workload", choices=["c2", "batch", "serve", "aca", "grad"], default="c2",
+                    help="c2: the headline factor+solve+logdet step; batch / serve / aca / grad: the other forms")
     ap.add_argument("--workers", type=int, default=8, help="batch / serve: concurrent handles")
     ap.add_argument("--requests", type=int, default=10000, help="serve: number of requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: Poisson arrival rate (1/s)")
     ap.add_argument("--aca-n", type=int, default=2 ** 18, help="aca: number of points")
     ap.add_argument("--aca-nugget", type=float, default=1e-4, help="aca: nugget of the Matern kernel")
+    ap.add_argument("--grad-n", type=int, default=2 ** 18, help="grad: number of points")
+    ap.add_argument("--n", type=int, default=N_POINTS,
+                    help="c2: number of points (a smaller case of the same leaf size for profiling)")
+    ap.add_argument("--level", type=int, default=LEVEL, help="c2: FixedLevel of the smaller case")
     args = ap.parse_args()
+    if (args.n, args.level) != (N_POINTS, LEVEL):
+        N_POINTS, LEVEL = args.n, args.level
+        WORKLOAD = f"matern32_nystrom_n{N_POINTS}_r{RANK}_fixedlevel{LEVEL}_{NRHS}rhs"
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
@@ -720,6 +774,8 @@ def main():
         run_serve(args)
     elif args.workload == "aca":
         run_aca(args)
+    elif args.workload == "grad":
+        run_grad(args)
     else:
         run_ours(args, rank, world, local_rank)
 

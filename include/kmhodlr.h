@@ -166,6 +166,14 @@ int km_logdet(km_handle* h, double* out);
  * the handle's stream and the call returns once it is complete. */
 int km_matvec_dev(km_handle* h, const double* d_x, double* d_y, int64_t k);
 int km_solve_dev(km_handle* h, const double* d_b, double* d_x, int64_t k);
+
+/* symmetricfactorize!(HK) then HK \ b in one call (src/HODLR/src/symfact.jl:6-49,
+ * src/HODLR/src/baseoverloads.jl:181-192), as LAPACK's posv combines potrf and potrs: the forward
+ * half of the solve runs behind the factorisation's dependency points on a second stream.
+ * Status, factor and x are those of km_factorize followed by km_solve (_dev: device pointers,
+ * in place allowed). */
+int km_factorize_solve(km_handle* h, const double* b, double* x, int64_t k);
+int km_factorize_solve_dev(km_handle* h, const double* d_b, double* d_x, int64_t k);
 int km_factor_solve_dev(km_handle* h, int transpose, const double* d_b, double* d_x, int64_t k);
 int km_factor_mul_dev(km_handle* h, int transpose, const double* d_b, double* d_x, int64_t k);
 

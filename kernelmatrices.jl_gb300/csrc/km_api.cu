@@ -1,6 +1,7 @@
 // C ABI of libkmhodlr: handle lifecycle, partition, and the orchestration of the device kernels.
 // Each entry point mirrors one reference call (cited in include/kmhodlr.h).
 #include <algorithm>
+#include <type_traits>
 #include <mutex>
 #include <cmath>
 #include <cstdlib>
@@ -193,6 +194,18 @@ struct km_handle {
   cudaStream_t own_stream = nullptr;  // the handle's own stream (h->stream may be external)
   cudaStream_t side = nullptr;        // forms the solve operators while the node levels run
   cudaEvent_t sev[kMaxLevels + 3] = {};
+  // fused factorisation and solve (km_factorize_solve_dev): the forward half of the solve runs on
+  // `aux` behind the factorisation's dependency points (leaf factor ready: xev[0]; explicit leaf
+  // bases: xev[1]; node level l finalised: fev[l]; forward half done: xev[2])
+  cudaStream_t aux = nullptr;
+  cudaEvent_t xev[3] = {};
+  double* d_bkeep = nullptr;  // right-hand sides kept by an in-place fused call
+  cudaEvent_t fev[kMaxLevels + 2] = {};
+  struct FwdJob {
+    double* X;
+    int k;
+    bool ok;
+  }* fwd_job = nullptr;
   // profiler
   bool prof = false;
   // CUDA graphs of the launch sequences of a Nystrom factorisation and of a nested solve,
@@ -350,6 +363,7 @@ void free_problem(km_handle* h) {
   h->d_Sinv = h->d_SinvF = h->d_M2 = h->d_M2F = h->d_Mtmp = h->d_GB = nullptr;
   h->gcap = h->tcap = 0;
   h->d_res = h->d_rdots = nullptr;
+  h->d_bkeep = nullptr;
   h->d_dPhi2 = h->d_Sj3 = h->d_Sj3F = h->d_VP4 = h->d_gpart = nullptr;
   h->rcap = 0;
   h->d2_pair = -1;
@@ -601,11 +615,23 @@ T* P(double* p) {
   return reinterpret_cast<T*>(p);
 }
 
+// Leaf solve L x = b (op 0) or L' x = b (op 1) on k columns in place: by 64-row blocks with the
+// diagonal-block inverses the tensor-core leaf stage keeps, else by substitution.
+template <typename T>
+static bool leaf_solve(km_handle* h, int op, T* X, int k) {
+  const Tree& t = h->tree;
+  cudaStream_t st = h->stream;
+  if constexpr (std::is_same<T, ff>::value) {
+    if (h->leaf_tc) return KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri_blk(P<ff>(h->d_Lf), t, op, X, t.n, k, st));
+  }
+  return KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<T>(P<T>(h->d_Lf), t, op, X, 1, t.n, 0, X, 1, t.n, 0, k, st));
+}
+
 template <typename T>
 int nested_fwd_t(km_handle* h, T* X, int k) {  // X <- W^{-1} X
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
-  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<T>(P<T>(h->d_Lf), t, 0, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
+  if (!leaf_solve<T>(h, 0, X, k))
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
   if (t.L == 0) return check_launch(h, "fwd");
   NodeMatsH nm = node_mats(h);
@@ -627,8 +653,7 @@ int nested_bwd_t(km_handle* h, T* X, int k) {  // X <- W'^{-1} X
     for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VG), P<T>(h->d_VD), k, DN_BWD_, st));
     KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, P<T>(h->d_VG), X, t.n, k, -1.0, st));
   }
-  if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<T>(P<T>(h->d_Lf), t, 1, X, 1, t.n, 0, X, 1, t.n, 0, k, st)))
-    return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
+  if (!leaf_solve<T>(h, 1, X, k)) return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
   return check_launch(h, "bwd");
 }
 
@@ -1125,6 +1150,13 @@ int km_create(const km_config* cfg, km_handle** out) {
     return KM_ERR_CUDA;
   }
   for (auto& e : h->sev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  if (cudaStreamCreateWithPriority(&h->aux, cudaStreamNonBlocking, prio_low) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    return KM_ERR_CUDA;
+  }
+  for (auto& e : h->xev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  for (auto& e : h->fev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   *out = h;
   return KM_OK;
 }
@@ -1179,6 +1211,12 @@ int km_destroy(km_handle* h) {
   for (auto e : h->sev)
     if (e) cudaEventDestroy(e);
   if (h->side) cudaStreamDestroy(h->side);
+  if (h->aux) cudaStreamSynchronize(h->aux);
+  for (auto e : h->xev)
+    if (e) cudaEventDestroy(e);
+  for (auto e : h->fev)
+    if (e) cudaEventDestroy(e);
+  if (h->aux) cudaStreamDestroy(h->aux);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return KM_OK;
@@ -1598,10 +1636,61 @@ int km_assemble_dev(km_handle* h, const double* d_pts, int64_t n, int kernel_id,
 
 // The launch sequence of the nested Nystrom factorisation (main stream, side stream forked for
 // the solve operators), without host synchronisation, so that it can be captured in a graph.
+// Forward half of the solve, X <- W^{-1} X (nested_fwd_t), enqueued on the aux stream at the
+// factorisation's dependency points: the leaf solve as soon as the leaf factor is final, the leaf
+// projections once the explicit leaf bases exist, the up-sweep of level l once level l is
+// finalised, the down-sweep and the expansion after the last level.  Same kernels and order as
+// nested_fwd_t, so the same bits.
+extern "C++" {
+template <typename T>
+static void aux_fwd_leaf(km_handle* h) {
+  auto* job = h->fwd_job;
+  const Tree& t = h->tree;
+  cudaStream_t ax = h->aux;
+  cudaEventRecord(h->xev[0], h->stream);
+  cudaStreamWaitEvent(ax, h->xev[0], 0);
+  T* X = reinterpret_cast<T*>(job->X);
+  if constexpr (std::is_same<T, ff>::value) {
+    launch_to_ff(job->X, X, t.n * job->k, ax);
+    job->ok = h->leaf_tc ? launch_leaf_tri_blk(P<ff>(h->d_Lf), t, 0, X, t.n, job->k, ax)
+                         : launch_leaf_tri<ff>(P<ff>(h->d_Lf), t, 0, X, 1, t.n, 0, X, 1, t.n, 0, job->k, ax);
+  } else {
+    job->ok = launch_leaf_tri<double>(h->d_Lf, t, 0, X, 1, t.n, 0, X, 1, t.n, 0, job->k, ax);
+  }
+  h->stats.kernel_launches += 2;
+}
+
+template <typename T>
+static void aux_fwd_nodes(km_handle* h) {
+  auto* job = h->fwd_job;
+  const Tree& t = h->tree;
+  cudaStream_t ax = h->aux;
+  T* X = reinterpret_cast<T*>(job->X);
+  const int k = job->k;
+  if (t.L > 0) {
+    NodeMatsH nm = node_mats(h);
+    cudaStreamWaitEvent(ax, h->xev[1], 0);
+    launch_leaf_proj<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, X, t.n, P<T>(h->d_VP), k, ax);
+    for (int l = 1; l <= t.L; ++l) {
+      cudaStreamWaitEvent(ax, h->fev[l], 0);
+      launch_up<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VD), k, UP_FWD_, ax);
+    }
+    for (int l = t.L; l >= 1; --l)
+      launch_down<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VG), P<T>(h->d_VD), k, DN_FWD_, ax);
+    launch_leaf_expand<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, P<T>(h->d_VG), X, t.n, k, -1.0, ax);
+    h->stats.kernel_launches += 2 + 2 * t.L;
+  }
+  cudaEventRecord(h->xev[2], ax);
+  cudaStreamWaitEvent(h->stream, h->xev[2], 0);
+}
+
+}  // extern "C++"
+
 static int factorize_launches(km_handle* h) {
   const Tree& t = h->tree;
   const int r = h->r;
   cudaStream_t st = h->stream;
+  const bool fwd = h->fwd_job != nullptr;
   KM_CUDA(h, cudaMemsetAsync(h->d_info, 0, sizeof(int) * (t.nleaf + t.nnode), st));
   if (h->mixed && h->leaf_tc) {
     // L_j and A_j = L_j^{-1} Phi_j from one blocked Cholesky of [K_j; Phi_j'] whose trailing
@@ -1615,6 +1704,7 @@ static int factorize_launches(km_handle* h) {
         KLV(h, KM_PROF_LEAF_TC, launch_leaf_chol_tc_update(P<ff>(h->d_Lf), P<ff>(h->d_Q), r, t, p, h->d_lcscr,
                                                            h->d_info, st));
     }
+    if (fwd) aux_fwd_leaf<ff>(h);
   } else if (!(h->mixed ? KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<ff>(h->d_K, P<ff>(h->d_Lf), t, h->d_info, st))
                         : KL(h, KM_PROF_LEAF_CHOL, launch_leaf_chol<double>(h->d_K, h->d_Lf, t, h->d_info, st)))) {
     return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the leaf Cholesky kernel");
@@ -1627,11 +1717,13 @@ static int factorize_launches(km_handle* h) {
       if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<ff>(P<ff>(h->d_Lf), t, 0, P<ff>(h->d_Q), r, 0, 1, P<ff>(h->d_Q),
                                                        r, 0, 1, r, st)))
         return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
+      if (fwd) aux_fwd_leaf<ff>(h);
     }
     if (t.L > 0) {
       KLV(h, KM_PROF_LEAF_QR, launch_leaf_qr<ff>(P<ff>(h->d_Q), r, t, P<ff>(h->d_tauleaf), P<ff>(h->d_R), st));
       side_begin(h);
       launch_leaf_formq<ff>(P<ff>(h->d_Q), P<ff>(h->d_tauleaf), r, t, h->side);
+      if (fwd) cudaEventRecord(h->xev[1], h->side);
       for (int l = 1; l <= t.L; ++l) {
         KLV(h, KM_PROF_NODE, launch_node_factor<ff>(P<ff>(h->d_R), P<ff>(h->d_SinvTf), r, l, t, P<ff>(h->d_Ct),
                                                     P<ff>(h->d_L22), P<ff>(h->d_Eref), P<ff>(h->d_Etau),
@@ -1644,17 +1736,21 @@ static int factorize_launches(km_handle* h) {
                                    P<ff>(h->d_L22i), P<ff>(h->d_E), P<ff>((double*)nm.CtT), P<ff>((double*)nm.L22T),
                                    P<ff>((double*)nm.L22iT), P<ff>((double*)nm.ET), h->side);
         }
+        if (fwd) cudaEventRecord(h->fev[l], h->side);
       }
       side_end(h);
     }
+    if (fwd) aux_fwd_nodes<ff>(h);
   } else {
     KM_CUDA(h, cudaMemcpyAsync(h->d_Q, h->d_Phi, sizeof(double) * t.n * r, cudaMemcpyDeviceToDevice, st));
     if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<double>(h->d_Lf, t, 0, h->d_Q, r, 0, 1, h->d_Q, r, 0, 1, r, st)))
       return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
+    if (fwd) aux_fwd_leaf<double>(h);
     if (t.L > 0) {
       KLV(h, KM_PROF_LEAF_QR, launch_leaf_qr<double>(h->d_Q, r, t, h->d_tauleaf, h->d_R, st));
       side_begin(h);
       launch_leaf_formq<double>(h->d_Q, h->d_tauleaf, r, t, h->side);
+      if (fwd) cudaEventRecord(h->xev[1], h->side);
       for (int l = 1; l <= t.L; ++l) {
         KLV(h, KM_PROF_NODE, launch_node_factor<double>(h->d_R, h->d_SinvT, r, l, t, h->d_Ct, h->d_L22, h->d_Eref,
                                                         h->d_Etau, h->d_info + t.nleaf, st));
@@ -1665,9 +1761,11 @@ static int factorize_launches(km_handle* h) {
                                        (double*)nm.CtT, (double*)nm.L22T, (double*)nm.L22iT, (double*)nm.ET,
                                        h->side);
         }
+        if (fwd) cudaEventRecord(h->fev[l], h->side);
       }
       side_end(h);
     }
+    if (fwd) aux_fwd_nodes<double>(h);
   }
   return KM_OK;
 }
@@ -1693,7 +1791,11 @@ int km_factorize(km_handle* h) {
   }
   h->lf_holds_k = false;
   const int64_t fk[5] = {(int64_t)h->alloc_epoch, t.n, t.L, r, h->mixed ? 1 : 0};
-  rc = run_graphed(h, &h->fgraph, h->fkey, fk, [&]() -> int { return factorize_launches(h); });
+  auto* job = h->fwd_job;  // km_factorize_solve_dev: the forward half of a solve rides along
+  if (job)
+    rc = factorize_launches(h);
+  else
+    rc = run_graphed(h, &h->fgraph, h->fkey, fk, [&]() -> int { return factorize_launches(h); });
   if (rc != KM_OK) return rc;
   if ((rc = check_launch(h, "factorize")) != KM_OK) return rc;
   h->stats.factorize_ms = timer_stop(h);
@@ -1714,6 +1816,10 @@ int km_factorize(km_handle* h) {
     // the next assembly returns to the configured precision.
     h->mixed = false;
     h->stats.precision_fallbacks += 1;
+    if (job) {  // the forward half ran on the float-pair factor: the caller solves again
+      job->ok = false;
+      h->fwd_job = nullptr;
+    }
     return km_factorize(h);
   }
   if (rc != KM_OK) return rc;
@@ -1738,6 +1844,52 @@ int km_matvec_dev(km_handle* h, const double* d_x, double* d_y, int64_t k) {
   }
   h->stats.matvec_ms = timer_stop(h);
   return sync(h, "matvec");
+}
+
+// symmetricfactorize!(HK) followed by HK \ b (symfact.jl:6-49, baseoverloads.jl:181-192) in one
+// call, as LAPACK's posv combines potrf and potrs: the forward half of the solve runs on the aux
+// stream behind the factorisation's dependency points (aux_fwd_leaf, aux_fwd_nodes), using the
+// SMs that the upper node levels leave idle; the backward half and the refinement follow as in
+// km_solve_dev.  Same kernels in the same order as km_factorize + km_solve_dev, so the same
+// results; ACA handles take those two calls.
+int km_factorize_solve_dev(km_handle* h, const double* d_b, double* d_x, int64_t k) {
+  if (!h || !d_b || !d_x || k < 1) return fail(h, KM_ERR_BAD_ARG, "bad solve arguments");
+  cudaSetDevice(h->cfg.device);
+  if (!h->assembled) return fail(h, KM_ERR_STATE, "assemble first");
+  int rc;
+  if (h->method != KM_METHOD_NYSTROM) {
+    if ((rc = km_factorize(h)) != KM_OK) return rc;
+    return km_solve_dev(h, d_b, d_x, k);
+  }
+  if ((rc = ensure_vec(h, k)) != KM_OK) return rc;
+  const int64_t n = h->tree.n;
+  const double* b_keep = d_b;
+  if (d_x != d_b) {
+    KM_CUDA(h, cudaMemcpyAsync(d_x, d_b, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, h->stream));
+  } else {
+    // in place: the right-hand sides are kept for the refinement, or for a second solve after a
+    // precision fallback
+    if ((rc = grow(h, &h->d_bkeep, n * k)) != KM_OK) return rc;
+    KM_CUDA(h, cudaMemcpyAsync(h->d_bkeep, d_b, sizeof(double) * n * k, cudaMemcpyDeviceToDevice, h->stream));
+    b_keep = h->d_bkeep;
+  }
+  km_handle::FwdJob job{d_x, (int)k, true};
+  h->fwd_job = &job;
+  rc = km_factorize(h);
+  h->fwd_job = nullptr;
+  if (rc != KM_OK) return rc;
+  if (!job.ok) return km_solve_dev(h, b_keep, d_x, k);
+  timer_start(h);
+  if (h->mixed) {
+    ff* Xf = reinterpret_cast<ff*>(d_x);
+    if ((rc = nested_bwd_t<ff>(h, Xf, (int)k)) != KM_OK) return rc;
+    KLV(h, KM_PROF_OTHER, launch_from_ff(Xf, d_x, n * k, h->stream));
+  } else if ((rc = nested_bwd_t<double>(h, d_x, (int)k)) != KM_OK) {
+    return rc;
+  }
+  if (h->mixed && h->cfg.refine_max_iter > 0 && (rc = refine(h, b_keep, d_x, (int)k)) != KM_OK) return rc;
+  h->stats.solve_ms = timer_stop(h);
+  return sync(h, "solve");
 }
 
 int km_solve_dev(km_handle* h, const double* d_b, double* d_x, int64_t k) {
@@ -1817,6 +1969,9 @@ static int host_call(km_handle* h, const double* b, double* x, int64_t k,
 }
 
 int km_matvec(km_handle* h, const double* x, double* y, int64_t k) { return host_call(h, x, y, k, km_matvec_dev); }
+int km_factorize_solve(km_handle* h, const double* b, double* x, int64_t k) {
+  return host_call(h, b, x, k, km_factorize_solve_dev);
+}
 int km_solve(km_handle* h, const double* b, double* x, int64_t k) { return host_call(h, b, x, k, km_solve_dev); }
 
 static int fs0(km_handle* h, const double* b, double* x, int64_t k) { return km_factor_solve_dev(h, 0, b, x, k); }

@@ -477,12 +477,17 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
       for (int k = 0; k < c; ++k) {
         if (k >= known && !timed_out) {
           int spins = 0;
+          // a warp more than two columns behind the pivot it waits for is off the critical
+          // chain: it naps between polls, so that its polls do not take issue slots from the
+          // warp that forms the next column
+          const bool nap = c - k > 2;
           while (wait_limit == 0 || vflag[k] == 0) {
             if (++spins > lim) {
               if (lane == 0) info[node] = -1;
               timed_out = true;
               break;
             }
+            if (nap) __nanosleep(32);
           }
           __threadfence_block();
           known = k + 1;
@@ -620,12 +625,16 @@ __global__ void __launch_bounds__(1024) k_node_factor(T* __restrict__ R, const T
         if (lane == 0) vflag[j] = 1;
       } else if (!timed_out) {
         int spins = 0;
+        // only the warp that owns column j + 1 forms the next reflector; the others nap between
+        // polls so that their polls do not take issue slots from it
+        const bool nap = j + 1 < c0;
         while (wait_limit == 0 || vflag[j] == 0) {
           if (++spins > lim) {
             if (lane == 0) info[node] = -1;
             timed_out = true;
             break;
           }
+          if (nap) __nanosleep(32);
         }
         __threadfence_block();
       }

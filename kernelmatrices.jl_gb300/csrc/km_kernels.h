@@ -106,6 +106,10 @@ void launch_leaf_qr(T* Pan, int r, const Tree& t, T* tau, T* Rout, cudaStream_t 
 // update.  scratch: leaf_chol_tc_scratch_bytes(t, r) bytes; info as launch_leaf_chol (-1: a
 // bounded wait of a tensor-core launch ran out).
 bool leaf_chol_tc_supported(const Tree& t, int r);
+// L x = b (op 0) or L' x = b (op 1) on every leaf with a factor of the tensor-core stage (it
+// keeps the inverses of its 64 x 64 diagonal blocks), k columns of X in place (ld ldx); false if
+// the shape is not supported
+bool launch_leaf_tri_blk(const ff* Lf, const Tree& t, int op, ff* X, int64_t ldx, int k, cudaStream_t st);
 int64_t leaf_chol_tc_scratch_bytes(const Tree& t, int r);
 int leaf_chol_tc_steps(const Tree& t);
 bool leaf_chol_tc_has_update(const Tree& t, int p);

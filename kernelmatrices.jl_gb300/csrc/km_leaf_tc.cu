@@ -172,9 +172,13 @@ __global__ void __launch_bounds__(kLcDiagThreads) k_lc_diag(ff* __restrict__ Lf,
     }
     __syncthreads();
   }
+  // L in the lower triangle of the diagonal block; the strictly lower part of X = D^{-1} in its
+  // (otherwise unused) strictly upper triangle, X[i][c] at row c0 + c, column c0 + i, for the
+  // block solves of k_leaf_tri_blk (X's diagonal is 1 / D_ii, recomputed there the same way)
   for (int e = tid; e < nb * nb; e += NT) {
     const int i = e % nb, c = e / nb;
     if (i >= c) Lf[koff + (int64_t)(c0 + c) * m + c0 + i] = D[i * LD + c];
+    else Lf[koff + (int64_t)(c0 + c) * m + c0 + i] = X[c * LD + i];
   }
   if (tid == 0 && sbad != 0 && info[leaf] == 0) info[leaf] = sbad;
   // rows of X: four threads per row, 16 columns each
@@ -589,6 +593,121 @@ __global__ void __launch_bounds__(kLcProbeThreads, 1) k_tc_probe(const double* _
 // when some leaf has rows left after the block
 // ---------------------------------------------------------------------------------------------
 static int64_t lc_rp_max(const Tree& t, int r) { return lc_rows_padded(t.max_leaf + r); }
+
+// ---------------------------------------------------------------------------------------------
+// Leaf triangular solves with the factor of the tensor-core stage: L x = b (op 0) or L' x = b
+// (op 1) by 64-row blocks, x_q = X_q (b_q - L_q,<q x_<q) with X_q the inverse of diagonal block q
+// kept by k_lc_diag (strictly lower part in the block's upper triangle, diagonal 1 / D_ii), so
+// that both steps are block products spread over all threads: no sequential chain over rows
+// (the substitution of k_leaf_tri runs one warp per column through each block).  After x_q the
+// remaining rows are updated at once (right-looking).  Same arithmetic as the TC stage's own
+// block column products, which use the same inverses.  The block of NC = 4 right-hand sides
+// lives in shared memory (narrow chunks keep several CTAs per leaf and SM in flight); grid
+// (nleaf, ceil(k / NC)), block 256.
+// ---------------------------------------------------------------------------------------------
+template <int NC>
+__global__ void __launch_bounds__(256) k_leaf_tri_blk(const ff* __restrict__ Lf, DTree t, int op,
+                                                      ff* __restrict__ X, int64_t ldx, int k) {
+  extern __shared__ __align__(16) unsigned char lc_smem_s[];
+  constexpr int LD = kLcNB + 1;
+  const int64_t leaf = blockIdx.x;
+  const int m = d_leaf_size(t, leaf);
+  const int64_t s = d_leaf_start(t, leaf), koff = d_leaf_koff(t, leaf);
+  const int c0 = blockIdx.y * NC, nc = min(NC, k - c0);
+  const int tid = threadIdx.x;
+  ff* xs = reinterpret_cast<ff*>(lc_smem_s);  // NC x m, column c at xs[c * m]
+  ff* Xq = xs + NC * m;                       // 64 x 65, X_q[i][c] at Xq[i * LD + c]
+  for (int e = tid; e < NC * m; e += blockDim.x) {
+    const int c = e / m, i = e - c * m;
+    xs[e] = c < nc ? X[(int64_t)(c0 + c) * ldx + s + i] : ff(0.0);
+  }
+  const int nbk = (m + kLcNB - 1) / kLcNB;
+  for (int step = 0; step < nbk; ++step) {
+    const int q = op == 0 ? step : nbk - 1 - step;
+    const int b0 = kLcNB * q, nb = min(kLcNB, m - b0);
+    __syncthreads();
+    for (int e = tid; e < kLcNB * kLcNB; e += blockDim.x) {
+      const int i = e / kLcNB, c = e - i * kLcNB;
+      ff v(0.0);
+      if (i < nb && c < nb) {
+        if (c < i) v = Lf[koff + (int64_t)(b0 + i) * m + b0 + c];
+        else if (c == i) v = ff(1.0) / Lf[koff + (int64_t)(b0 + i) * m + b0 + i];
+      }
+      Xq[i * LD + c] = v;
+    }
+    __syncthreads();
+    // x_q = X_q y_q (op 0) or X_q' y_q (op 1): thread (row i, columns g, g + 4, ...)
+    const int i = tid & (kLcNB - 1), g = tid >> 6;
+    ff res[NC / 4];
+#pragma unroll
+    for (int u = 0; u < NC / 4; ++u) {
+      const int col = g + 4 * u;
+      acc_t<ff> a{};
+      if (col < nc && i < nb) {
+        const ff* y = xs + col * m + b0;
+        if (op == 0)
+          for (int c = 0; c < nb; ++c) a += Xq[i * LD + c] * y[c];
+        else
+          for (int c = 0; c < nb; ++c) a += Xq[c * LD + i] * y[c];
+      }
+      res[u] = accv(a);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < NC / 4; ++u) {
+      const int col = g + 4 * u;
+      if (col < nc && i < nb) xs[col * m + b0 + i] = res[u];
+    }
+    __syncthreads();
+    // remaining rows: op 0 rows below the block, op 1 rows above it
+    const int r0 = op == 0 ? b0 + nb : 0, r1 = op == 0 ? m : b0;
+    for (int row = r0 + tid; row < r1; row += blockDim.x) {
+      acc_t<ff> a[NC] = {};
+      int l = 0;
+      for (; l + 3 < nb; l += 4) {  // four entries of L loaded ahead of their multiply-adds
+        ff lv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          lv[u] = op == 0 ? Lf[koff + (int64_t)(b0 + l + u) * m + row] : Lf[koff + (int64_t)row * m + b0 + l + u];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int c = 0; c < NC; ++c)
+            if (c < nc) a[c] += lv[u] * xs[c * m + b0 + l + u];
+      }
+      for (; l < nb; ++l) {
+        const ff lv = op == 0 ? Lf[koff + (int64_t)(b0 + l) * m + row] : Lf[koff + (int64_t)row * m + b0 + l];
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+          if (c < nc) a[c] += lv * xs[c * m + b0 + l];
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (c < nc) xs[c * m + row] -= accv(a[c]);
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < nc * m; e += blockDim.x) {
+    const int c = e / m, i = e - c * m;
+    X[(int64_t)(c0 + c) * ldx + s + i] = xs[e];
+  }
+}
+
+template <int NC>
+static bool tri_blk_launch(const ff* Lf, const Tree& t, int op, ff* X, int64_t ldx, int k, cudaStream_t st) {
+  const size_t sm = ((size_t)NC * t.max_leaf + (size_t)kLcNB * (kLcNB + 1)) * sizeof(ff);
+  if (sm > 200 * 1024) return false;
+  smem_limit((const void*)k_leaf_tri_blk<NC>, sm);
+  k_leaf_tri_blk<NC><<<dim3((unsigned)t.nleaf, (unsigned)((k + NC - 1) / NC)), 256, sm, st>>>(Lf, dtree(t), op, X,
+                                                                                              ldx, k);
+  return true;
+}
+
+bool launch_leaf_tri_blk(const ff* Lf, const Tree& t, int op, ff* X, int64_t ldx, int k, cudaStream_t st) {
+  if (k <= 0) return true;
+  if (t.max_leaf > kLcMaxLeaf || (op != 0 && op != 1)) return false;
+  return tri_blk_launch<4>(Lf, t, op, X, ldx, k, st);
+}
 
 bool leaf_chol_tc_supported(const Tree& t, int r) {
   return t.max_leaf >= 1 && t.max_leaf <= kLcMaxLeaf && r >= 1 && r <= kLcMaxRank;

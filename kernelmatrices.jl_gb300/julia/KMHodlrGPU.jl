@@ -101,6 +101,15 @@ function symmetricfactorize!(K::GPUKernelHODLR; plel::Bool=false, verbose::Bool=
   return nothing
 end
 
+# symmetricfactorize!(K) then K \ src in one call (the forward half of the solve overlaps the
+# factorisation); the same factor and result as the two calls.
+function factorize_solve!(target::StridedVecOrMat{Float64}, K::GPUKernelHODLR, src::StridedVecOrMat{Float64})
+  check(K.h, ccall((:km_factorize_solve, libkm), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64),
+                   K.h, src, target, size(src, 2)))
+  K.factorized = true
+  return target
+end
+
 function mul!(target::StridedVecOrMat{Float64}, K::GPUKernelHODLR, src::StridedVecOrMat{Float64})
   check(K.h, ccall((:km_matvec, libkm), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64),
                    K.h, src, target, size(src, 2)))

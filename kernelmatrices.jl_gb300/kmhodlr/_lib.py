@@ -112,6 +112,8 @@ SIGNATURES = {
     "km_logdet": (C.c_int, [_H, _DP]),
     "km_matvec_dev": (C.c_int, [_H, _P, _P, C.c_int64]),
     "km_solve_dev": (C.c_int, [_H, _P, _P, C.c_int64]),
+    "km_factorize_solve": (C.c_int, [_H, _DP, _DP, C.c_int64]),
+    "km_factorize_solve_dev": (C.c_int, [_H, _P, _P, C.c_int64]),
     "km_factor_solve_dev": (C.c_int, [_H, C.c_int, _P, _P, C.c_int64]),
     "km_factor_mul_dev": (C.c_int, [_H, C.c_int, _P, _P, C.c_int64]),
     "km_derivative_matvec": (C.c_int, [_H, C.c_int, _DP, _DP, C.c_int64]),

@@ -323,6 +323,15 @@ def symmetricfactorize(K: KernelHODLR) -> None:
     K.factorized = True
 
 
+def factorize_solve(K: KernelHODLR, b: np.ndarray) -> np.ndarray:
+    """``symmetricfactorize!(K)`` followed by ``K \\ b`` (symfact.jl:6-49, baseoverloads.jl:181-192)
+    in one call (``km_factorize_solve``: the forward half of the solve overlaps the factorisation);
+    the same factor and solution as the two calls."""
+    x = K._apply("km_factorize_solve", b)
+    K.factorized = True
+    return x
+
+
 def logdet(K: KernelHODLR) -> float:
     return K.logdet()
 
