@@ -642,13 +642,20 @@ int nested_fwd_t(km_handle* h, T* X, int k) {  // X <- W^{-1} X
   return check_launch(h, "fwd");
 }
 
+// after_fwd: X comes straight from nested_fwd_t, whose leaf slots still hold z = Q'x (VP) and
+// the coefficients g it expanded (VG, x <- x - Q g); with Q'Q = I the new projections are
+// z - g, so the projection pass over the leaves is skipped (leaves of at least r rows, where
+// the leaf bases have r orthonormal columns).
 template <typename T>
-int nested_bwd_t(km_handle* h, T* X, int k) {  // X <- W'^{-1} X
+int nested_bwd_t(km_handle* h, T* X, int k, bool after_fwd = false) {  // X <- W'^{-1} X
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
   if (t.L > 0) {
     NodeMatsH nm = node_mats(h);
-    KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, X, t.n, P<T>(h->d_VP), k, st));
+    if (after_fwd && t.m0 >= h->r)
+      KLV(h, KM_PROF_LEAF_REFL, launch_slot_sub<T>(P<T>(h->d_VP), P<T>(h->d_VG), t.nleaf * (int64_t)k * h->r, st));
+    else
+      KLV(h, KM_PROF_LEAF_REFL, launch_leaf_proj<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, X, t.n, P<T>(h->d_VP), k, st));
     for (int l = 1; l < t.L; ++l) KLV(h, KM_PROF_SWEEP, launch_up<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VD), k, UP_PROJ_, st));
     for (int l = t.L; l >= 1; --l) KLV(h, KM_PROF_SWEEP, launch_down<T>(t, nm, l, P<T>(h->d_VP), P<T>(h->d_VG), P<T>(h->d_VD), k, DN_BWD_, st));
     KLV(h, KM_PROF_LEAF_REFL, launch_leaf_expand<T>(P<T>(h->d_Q), P<T>(h->d_tauleaf), h->r, t, P<T>(h->d_VG), X, t.n, k, -1.0, st));
@@ -718,12 +725,12 @@ int nested_solve(km_handle* h, double* X, int k) {
   }
   if (!h->mixed) {
     const int rc = nested_fwd_t<double>(h, X, k);
-    return rc != KM_OK ? rc : nested_bwd_t<double>(h, X, k);
+    return rc != KM_OK ? rc : nested_bwd_t<double>(h, X, k, true);
   }
   ff* Xf = reinterpret_cast<ff*>(X);
   KLV(h, KM_PROF_OTHER, launch_to_ff(X, Xf, h->tree.n * k, h->stream));
   int rc = nested_fwd_t<ff>(h, Xf, k);
-  if (rc == KM_OK) rc = nested_bwd_t<ff>(h, Xf, k);
+  if (rc == KM_OK) rc = nested_bwd_t<ff>(h, Xf, k, true);
   KLV(h, KM_PROF_OTHER, launch_from_ff(Xf, X, h->tree.n * k, h->stream));
   return rc;
 }
@@ -1882,9 +1889,9 @@ int km_factorize_solve_dev(km_handle* h, const double* d_b, double* d_x, int64_t
   timer_start(h);
   if (h->mixed) {
     ff* Xf = reinterpret_cast<ff*>(d_x);
-    if ((rc = nested_bwd_t<ff>(h, Xf, (int)k)) != KM_OK) return rc;
+    if ((rc = nested_bwd_t<ff>(h, Xf, (int)k, true)) != KM_OK) return rc;
     KLV(h, KM_PROF_OTHER, launch_from_ff(Xf, d_x, n * k, h->stream));
-  } else if ((rc = nested_bwd_t<double>(h, d_x, (int)k)) != KM_OK) {
+  } else if ((rc = nested_bwd_t<double>(h, d_x, (int)k, true)) != KM_OK) {
     return rc;
   }
   if (h->mixed && h->cfg.refine_max_iter > 0 && (rc = refine(h, b_keep, d_x, (int)k)) != KM_OK) return rc;

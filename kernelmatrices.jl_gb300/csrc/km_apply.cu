@@ -518,6 +518,22 @@ __global__ void k_nys_sums(const double* __restrict__ VP, double* __restrict__ V
     }
 }
 
+// VP[e] -= VG[e] for e < count: the leaf projections of the backward solve from those of the
+// forward solve (see nested_bwd_t).
+template <typename T>
+__global__ void k_slot_sub(T* __restrict__ VP, const T* __restrict__ VG, int64_t count) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
+    VP[e] = VP[e] - VG[e];
+}
+
+template <typename T>
+void launch_slot_sub(T* VP, const T* VG, int64_t count, cudaStream_t st) {
+  if (count <= 0) return;
+  k_slot_sub<T><<<(unsigned)std::min<int64_t>((count + 255) / 256, 4096), 256, 0, st>>>(VP, VG, count);
+}
+template void launch_slot_sub<double>(double*, const double*, int64_t, cudaStream_t);
+template void launch_slot_sub<ff>(ff*, const ff*, int64_t, cudaStream_t);
+
 void launch_nys_sums(const double* VP, double* VG, int64_t nleaf, int W, int k, cudaStream_t st) {
   k_nys_sums<<<dim3((unsigned)k, (unsigned)((W + 31) / 32)), 256, 0, st>>>(VP, VG, nleaf, W, k);
 }
