@@ -615,6 +615,10 @@ T* P(double* p) {
   return reinterpret_cast<T*>(p);
 }
 
+// The block solve re-reads a leaf's factor for every chunk of 4 right-hand sides; from 32
+// columns on (the probe blocks of the gradient) the substitution kernel's wider chunks win.
+static bool use_tri_blk(const km_handle* h, int64_t k) { return h->leaf_tc && k < 32; }
+
 // Leaf solve L x = b (op 0) or L' x = b (op 1) on k columns in place: by 64-row blocks with the
 // diagonal-block inverses the tensor-core leaf stage keeps, else by substitution.
 template <typename T>
@@ -622,7 +626,7 @@ static bool leaf_solve(km_handle* h, int op, T* X, int k) {
   const Tree& t = h->tree;
   cudaStream_t st = h->stream;
   if constexpr (std::is_same<T, ff>::value) {
-    if (h->leaf_tc) return KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri_blk(P<ff>(h->d_Lf), t, op, X, t.n, k, st));
+    if (use_tri_blk(h, k)) return KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri_blk(P<ff>(h->d_Lf), t, op, X, t.n, k, st));
   }
   return KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<T>(P<T>(h->d_Lf), t, op, X, 1, t.n, 0, X, 1, t.n, 0, k, st));
 }
@@ -1244,7 +1248,7 @@ static int aca_assemble(km_handle* h, const double* pts, bool dev, const Tree& t
                         int kernel_id, double tol, int64_t maxrank) {
   free_problem(h);
   h->tree = t;
-  h->kp = KParams{kernel_id, params[0], params[1], params[2]};
+  h->kp = make_kparams(kernel_id, params[0], params[1], params[2]);
   h->method = KM_METHOD_ACA;
   h->tol = tol;
   h->maxrank = maxrank;
@@ -1546,7 +1550,7 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
     h->vcap = h->xcap = h->gcap = h->tcap = h->rcap = h->hcap = 0;
   }
   h->tree = t;
-  h->kp = KParams{kernel_id, params[0], params[1], params[2]};
+  h->kp = make_kparams(kernel_id, params[0], params[1], params[2]);
   h->method = method;
   h->tol = tol;
   h->maxrank = maxrank;
@@ -1659,7 +1663,7 @@ static void aux_fwd_leaf(km_handle* h) {
   T* X = reinterpret_cast<T*>(job->X);
   if constexpr (std::is_same<T, ff>::value) {
     launch_to_ff(job->X, X, t.n * job->k, ax);
-    job->ok = h->leaf_tc ? launch_leaf_tri_blk(P<ff>(h->d_Lf), t, 0, X, t.n, job->k, ax)
+    job->ok = use_tri_blk(h, job->k) ? launch_leaf_tri_blk(P<ff>(h->d_Lf), t, 0, X, t.n, job->k, ax)
                          : launch_leaf_tri<ff>(P<ff>(h->d_Lf), t, 0, X, 1, t.n, 0, X, 1, t.n, 0, job->k, ax);
   } else {
     job->ok = launch_leaf_tri<double>(h->d_Lf, t, 0, X, 1, t.n, 0, X, 1, t.n, 0, job->k, ax);

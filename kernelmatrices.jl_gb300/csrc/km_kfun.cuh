@@ -45,6 +45,10 @@ __device__ __forceinline__ ff ff_exp_neg(ff z) {
 // conversions of the FP64 differences.  Two triples are equal component by component exactly
 // when the doubles are equal (x == y, the nugget's test).
 // ---------------------------------------------------------------------------------------------
+// p0 and p1 as float pairs (rounded on the host once, KParams)
+__device__ __forceinline__ ff kp_p0(const KParams& kp) { return ff(kp.p0h, kp.p0l); }
+__device__ __forceinline__ ff kp_p1(const KParams& kp) { return ff(kp.p1h, kp.p1l); }
+
 struct f3 {
   float h, m, l;
 };
@@ -76,16 +80,16 @@ __device__ __forceinline__ ff kernel_value_ffp(const KParams& kp, const f3& x1, 
   const ff r = sqrt(ff(dx * dx) + dy * dy);
   ff out;
   if (kp.kid == KM_KERNEL_RATQUAD) {
-    const ff t = r / ff(kp.p1);
+    const ff t = r / kp_p1(kp);
     const ff u = ff(1.0) + t * t;
-    out = ff(ff(kp.p0) * ff(kp.p0)) / ff(u * u);
+    out = ff(kp_p0(kp) * kp_p0(kp)) / ff(u * u);
   } else {
-    out = ff(kp.p0);
+    out = kp_p0(kp);
     if (r.hi > 0.f) {
-      const ff x = r / ff(kp.p1);
+      const ff x = r / kp_p1(kp);
       if (x.hi > 1.0e-8f) {
         const ff z = ff(kSqrt3) * x;
-        out = ff(ff(kp.p0) * (ff(1.0) + z)) * ff_exp_neg(z);
+        out = ff(kp_p0(kp) * (ff(1.0) + z)) * ff_exp_neg(z);
       }
     }
   }
@@ -112,25 +116,25 @@ __device__ __forceinline__ void dkernel3_ffp(const KParams& kp, const f3& x1, co
   const ff r2 = ff(dx * dx) + dy * dy;
   const ff r = sqrt(r2);
   if (kp.kid == KM_KERNEL_RATQUAD) {
-    const ff t = r / ff(kp.p1);
+    const ff t = r / kp_p1(kp);
     const ff u = ff(1.0) + t * t;
-    out[0] = ff(ff(2.0) * ff(kp.p0)) / ff(u * u);
-    const ff num = ff(ff(4.0) * ff(ff(kp.p0) * ff(kp.p0))) * r2;
-    const ff p13 = ff(ff(kp.p1) * ff(kp.p1)) * ff(kp.p1);
+    out[0] = ff(ff(2.0) * kp_p0(kp)) / ff(u * u);
+    const ff num = ff(ff(4.0) * ff(kp_p0(kp) * kp_p0(kp))) * r2;
+    const ff p13 = ff(kp_p1(kp) * kp_p1(kp)) * kp_p1(kp);
     out[1] = (num / p13) / ff(ff(u * u) * u);
     return;
   }
   out[0] = ff(1.0);
   out[1] = ff(0.0);
   if (!(r.hi > 0.f)) return;
-  const ff x = r / ff(kp.p1);
+  const ff x = r / kp_p1(kp);
   if (!(x.hi > 1.0e-8f)) return;
   // -p0 * cor'(x) * r / p1^2 with cor'(x) = -3 x exp(-sqrt3 x)
   const ff z = ff(kSqrt3) * x;
   const ff e = ff_exp_neg(z);
   out[0] = ff((ff(1.0) + z) * e);
-  const ff num = ff(ff(3.0) * ff(kp.p0)) * ff(x * e);
-  out[1] = ff(num * r) / ff(ff(kp.p1) * ff(kp.p1));
+  const ff num = ff(ff(3.0) * kp_p0(kp)) * ff(x * e);
+  out[1] = ff(num * r) / ff(kp_p1(kp) * kp_p1(kp));
 }
 
 __device__ __forceinline__ void dkernel3_ff(const KParams& kp, double x1, double y1, double x2, double y2,

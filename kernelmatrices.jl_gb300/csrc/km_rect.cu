@@ -277,7 +277,7 @@ extern "C" int km_rhodlr_create(const km_config* cfg, const double* x1, int64_t 
   R->n1 = n1;
   R->n2 = n2;
   R->levels = (int)lv;
-  R->kp = KParams{kernel_id, params[0], params[1], params[2]};
+  R->kp = make_kparams(kernel_id, params[0], params[1], params[2]);
   if (cudaStreamCreateWithFlags(&R->st, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     destroy(R);
