@@ -183,16 +183,34 @@ __global__ void __launch_bounds__(leaf_qr_threads<T>()) k_leaf_qr(T* __restrict_
     __syncthreads();
   }
   const int kmax = min(m, r);
-  for (int j = 0; j < kmax; ++j) {
-    T* aj = A + (int64_t)j * m;
+  // Two barriers a column: (1) thread 0 forms reflector j from alpha = a[j][j] and the norm of
+  // the rest of column j, which the warp that last updated that column left in sh_sig, while the
+  // other threads scale the previous reflector; (2) one warp per column c > j applies H_j with
+  // the unscaled vector x = a[j+1:, j] (v = scal x), and the warp of column j + 1 then leaves the
+  // norm of its rows below j + 1 for the next step.
+  __shared__ T sh_sig, sh_scal;
+  if (kmax > 0) {  // norm of column 0 below its first row
     T part = T(0.0);
-    for (int i = j + 1 + tid; i < m; i += blockDim.x) part += aj[i] * aj[i];
+    for (int i = 1 + tid; i < m; i += blockDim.x) part += A[i] * A[i];
     part = warp_sum_t(part);
     if (lane == 0) red[w] = part;
     __syncthreads();
+    if (w == 0) {
+      T v = lane < (int)(blockDim.x >> 5) ? red[lane] : T(0.0);
+      v = warp_sum_t(v);
+      if (lane == 0) sh_sig = v;
+    }
+  }
+  T prev_scal = T(0.0);
+  for (int j = 0; j < kmax; ++j) {
+    T* aj = A + (int64_t)j * m;
+    __syncthreads();
+    if (j > 0) {  // the previous reflector's vector, scaled in place (nobody reads it this phase)
+      T* ap = A + (int64_t)(j - 1) * m;
+      for (int i = j + tid; i < m; i += blockDim.x) ap[i] *= prev_scal;
+    }
     if (tid == 0) {
-      T sig = T(0.0);
-      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) sig += red[q];
+      const T sig = sh_sig;
       const T alpha = aj[j];
       T tj = T(0.0), beta = alpha, scal = T(0.0);
       if (sig != 0.0) {
@@ -202,27 +220,49 @@ __global__ void __launch_bounds__(leaf_qr_threads<T>()) k_leaf_qr(T* __restrict_
         scal = T(1.0) / (alpha - beta);
       }
       aj[j] = beta;
-      red[0] = scal;
+      sh_scal = scal;
       sh_tau = tj;
+      tau[leaf * r + j] = tj;
     }
     __syncthreads();
-    const T scal = red[0], tj = sh_tau;
-    for (int i = j + 1 + tid; i < m; i += blockDim.x) aj[i] *= scal;
-    if (tid == 0) tau[leaf * r + j] = tj;
-    __syncthreads();
+    const T scal = sh_scal, tj = sh_tau;
+    prev_scal = scal;
     if (tj != 0.0) {
-      // apply H_j = I - tau v v' to columns c > j (one warp per column)
+      // apply H_j = I - tau v v' to columns c > j (one warp per column), v = scal x
       for (int c = j + 1 + w; c < r; c += (int)(blockDim.x >> 5)) {
         T* ac = A + (int64_t)c * m;
-        T acc = (lane == 0) ? ac[j] : T(0.0);
+        T acc = T(0.0);
         for (int i = j + 1 + lane; i < m; i += 32) acc += aj[i] * ac[i];
-        acc = warp_sum_t(acc) * tj;
+        acc = (warp_sum_t(acc) * scal + ac[j]) * tj;
         if (lane == 0) ac[j] -= acc;
-        for (int i = j + 1 + lane; i < m; i += 32) ac[i] -= acc * aj[i];
+        const T f = acc * scal;
+        if (c == j + 1) {  // the next column: its norm below row j + 1 on the way
+          T nrm = T(0.0);
+          for (int i = j + 1 + lane; i < m; i += 32) {
+            const T v = ac[i] - f * aj[i];
+            ac[i] = v;
+            if (i > j + 1) nrm += v * v;
+          }
+          nrm = warp_sum_t(nrm);
+          if (lane == 0) sh_sig = nrm;
+        } else {
+          for (int i = j + 1 + lane; i < m; i += 32) ac[i] -= f * aj[i];
+        }
       }
+    } else if (j + 1 < kmax && w == 0) {  // H_j = I: the next column's norm as it stands
+      T* an = A + (int64_t)(j + 1) * m;
+      T nrm = T(0.0);
+      for (int i = j + 2 + lane; i < m; i += 32) nrm += an[i] * an[i];
+      nrm = warp_sum_t(nrm);
+      if (lane == 0) sh_sig = nrm;
     }
-    __syncthreads();
   }
+  __syncthreads();
+  if (kmax > 0) {  // the last reflector's vector
+    T* ap = A + (int64_t)(kmax - 1) * m;
+    for (int i = kmax + tid; i < m; i += blockDim.x) ap[i] *= prev_scal;
+  }
+  __syncthreads();
   for (int j = kmax + tid; j < r; j += blockDim.x) tau[leaf * r + j] = T(0.0);
   for (int e = tid; e < r * r; e += blockDim.x) {
     const int i = e % r, c = e / r;
