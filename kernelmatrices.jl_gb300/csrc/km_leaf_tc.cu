@@ -36,7 +36,8 @@ constexpr int kLcTileM = 128;          // rows of a tile (MMA M)
 constexpr int kLcTileN = 64;           // columns of a tile (MMA N)
 constexpr int kLcTcThreads = 512;      // 16 warps: warp w reads tensor-memory lanes 32 (w % 4) .. + 31,
                                        // columns 16 (w / 4) .. + 15 of a tile
-constexpr int kLcDiagThreads = 256;
+constexpr int kLcDiagThreads = 512;
+constexpr int kLcDiagCols = kLcNB * kLcNB / kLcDiagThreads;  // trailing-update columns a thread
 constexpr int kLcProbeThreads = 256;
 constexpr uint32_t kLcTmemCols = 512;  // kSlices x kLcTileN = 448 accumulator columns
 constexpr uint32_t kATileBytes = kLcTileM * kLcNB * 2;  // one slice of a 128-row tile
@@ -143,35 +144,38 @@ __global__ void __launch_bounds__(kLcDiagThreads) k_lc_diag(ff* __restrict__ Lf,
   }
   if (tid == 0) sbad = 0;
   __syncthreads();
+  // two barriers a column: every thread forms the pivot from D[j][j] (left in place until the
+  // end, the factor's diagonal goes to sdiag) and scales its share of column j and of row j of X;
+  // then the trailing update
+  __shared__ ff sdiag[kLcNB];
   for (int j = 0; j < nb; ++j) {
     const ff d = D[j * LD + j];
     const bool ok = d > 0.0;
     const ff sd = ok ? sqrt(d) : ff(1.0);
     const ff rinv = ff(1.0) / sd;
     if (!ok && tid == 0 && sbad == 0) sbad = c0 + j + 1;
-    __syncthreads();
     for (int i = j + 1 + tid; i < nb; i += NT) D[i * LD + j] = ff(D[i * LD + j] * rinv);
     for (int c = tid; c <= j; c += NT) X[j * LD + c] = ff(X[j * LD + c] * rinv);
-    if (tid == 0) D[j * LD + j] = sd;
+    if (tid == 0) sdiag[j] = sd;
     __syncthreads();
-    // trailing lower triangle of D (i >= c > j) and rows i > j of X (columns c <= j)
-    const int wr = nb - j - 1;
-    const int nd = wr * (wr + 1) / 2, nx = wr * (j + 1);
-    for (int e = tid; e < nd + nx; e += NT) {
-      if (e < nd) {
-        int a = (int)((sqrtf(8.f * (float)e + 1.f) - 1.f) * 0.5f);  // e = a (a + 1) / 2 + b, b <= a
-        if ((a + 1) * (a + 2) / 2 <= e) ++a;
-        if (a * (a + 1) / 2 > e) --a;
-        const int i = j + 1 + a, c = j + 1 + (e - a * (a + 1) / 2);
-        D[i * LD + c] -= D[i * LD + j] * D[c * LD + j];
-      } else {
-        const int q = e - nd;
-        const int i = j + 1 + q % wr, c = q / wr;
-        X[i * LD + c] -= D[i * LD + j] * X[j * LD + c];
+    // trailing lower triangle of D (i >= c > j) and rows i > j of X (columns c <= j): thread
+    // (row i = tid % 64, columns kLcDiagCols g .. + kLcDiagCols - 1 with g = tid / 64), the row's
+    // pivot-column entry loaded once
+    for (int e = tid; e < kLcNB * (kLcNB / kLcDiagCols); e += NT) {
+      const int i = e & (kLcNB - 1), g = e / kLcNB;
+      if (i > j && i < nb) {
+        const ff lij = D[i * LD + j];
+#pragma unroll
+        for (int c = kLcDiagCols * g; c < kLcDiagCols * g + kLcDiagCols; ++c) {
+          if (c <= j) X[i * LD + c] -= lij * X[j * LD + c];
+          else if (c <= i) D[i * LD + c] -= lij * D[c * LD + j];
+        }
       }
     }
     __syncthreads();
   }
+  for (int j = tid; j < nb; j += NT) D[j * LD + j] = sdiag[j];
+  __syncthreads();
   // L in the lower triangle of the diagonal block; the strictly lower part of X = D^{-1} in its
   // (otherwise unused) strictly upper triangle, X[i][c] at row c0 + c, column c0 + i, for the
   // block solves of k_leaf_tri_blk (X's diagonal is 1 / D_ii, recomputed there the same way)
