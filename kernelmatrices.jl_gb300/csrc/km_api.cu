@@ -78,6 +78,7 @@ struct km_handle {
   bool mixed = false;  // float-pair factor (KM_PREC_MIXED)
   bool leaf_tc = false;  // mixed form: leaf Cholesky and L^{-1} Phi on the tensor cores
   bool lf_holds_k = false;  // d_Lf holds the float-pair leaf matrices (written by the assembly)
+  bool q_holds_phi = false;  // d_Q holds Phi as float pairs (written by the mixed assembly)
   double* d_lcscr = nullptr;  // slices and row exponents of the tensor-core leaf stage
   // CTAs per node of the float-pair node kernel at most (thread-block clusters on levels with
   // few nodes); 1 for handles of the batch and serving pools, whose streams fill the SMs already
@@ -212,7 +213,7 @@ struct km_handle {
   // replayed while the handle's buffers (alloc_epoch) and the shapes in the key are unchanged
   uint64_t alloc_epoch = 0;
   cudaGraphExec_t fgraph = nullptr;
-  int64_t fkey[6] = {-1, -1, -1, -1, -1, 0};  // last entry: kernels in the graph
+  int64_t fkey[7] = {-1, -1, -1, -1, -1, -1, 0};  // last entry: kernels in the graph
   cudaGraphExec_t sgraph = nullptr;
   int64_t skey[8] = {-1, -1, -1, -1, -1, -1, -1, 0};
   bool graphs = true;
@@ -1530,7 +1531,7 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   if (t.nleaf > 65535) return fail(h, KM_ERR_UNSUPPORTED, "more than 65535 leaves");
   if (method == KM_METHOD_ACA) {
     if (!(tol >= 0.0) || maxrank < 0) return fail(h, KM_ERR_BAD_ARG, "ACA needs tol >= 0 and maxrank >= 0");
-    h->leaf_tc = h->lf_holds_k = false;
+    h->leaf_tc = h->lf_holds_k = h->q_holds_phi = false;
     return aca_assemble(h, pts, dev, t, params, kernel_id, tol, maxrank);
   }
   // Nystrom checks (src/HODLR/src/constructor.jl:26-28)
@@ -1618,7 +1619,9 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
                                           h->leaf_tc ? P<ff>(h->d_Lf) : nullptr, h->mixed ? h->d_pts3 : nullptr));
   h->lf_holds_k = h->leaf_tc;
   KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, -1, h->d_Phi, st, h->mixed,
-                                       h->mixed ? h->d_pts3 : nullptr, h->mixed ? h->d_lnd3 : nullptr));
+                                       h->mixed ? h->d_pts3 : nullptr, h->mixed ? h->d_lnd3 : nullptr,
+                                       h->mixed ? P<ff>(h->d_Q) : nullptr));
+  h->q_holds_phi = h->mixed;
   side_end(h);
   if ((rc = check_launch(h, "assemble")) != KM_OK) return rc;
   h->stats.assemble_ms = timer_stop(h);
@@ -1706,7 +1709,7 @@ static int factorize_launches(km_handle* h) {
   if (h->mixed && h->leaf_tc) {
     // L_j and A_j = L_j^{-1} Phi_j from one blocked Cholesky of [K_j; Phi_j'] whose trailing
     // updates run on the tensor cores (km_leaf_tc.cu)
-    KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Q), t.n * r, st));
+    if (!h->q_holds_phi) KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Q), t.n * r, st));
     for (int p = 0; p < leaf_chol_tc_steps(t); ++p) {
       KLV(h, KM_PROF_LEAF_CHOL, launch_leaf_chol_tc_diag(P<ff>(h->d_Lf), r, t, p, h->d_lcscr, h->d_info, st));
       KLV(h, KM_PROF_LEAF_TC, launch_leaf_chol_tc_trsm(P<ff>(h->d_Lf), P<ff>(h->d_Q), r, t, p, h->d_lcscr,
@@ -1724,7 +1727,7 @@ static int factorize_launches(km_handle* h) {
   if (h->mixed) {
     // float-pair factor: every FP64-pipe-bound step runs on the FP32 pipe in float-float
     if (!h->leaf_tc) {
-      KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Q), t.n * r, st));
+      if (!h->q_holds_phi) KLV(h, KM_PROF_OTHER, launch_to_ff(h->d_Phi, P<ff>(h->d_Q), t.n * r, st));
       if (!KL(h, KM_PROF_LEAF_TRI, launch_leaf_tri<ff>(P<ff>(h->d_Lf), t, 0, P<ff>(h->d_Q), r, 0, 1, P<ff>(h->d_Q),
                                                        r, 0, 1, r, st)))
         return fail(h, KM_ERR_UNSUPPORTED, "leaf too large for the triangular solve kernel");
@@ -1800,13 +1803,21 @@ int km_factorize(km_handle* h) {
     // kernel on the same points, so the same float pairs and FP64 values as the assembly's)
     KLV(h, KM_PROF_EVAL, launch_eval_leaves(h->d_pts, t, h->kp, -1, h->d_K, st, true, P<ff>(h->d_Lf), h->d_pts3));
   }
+  if (h->mixed && !h->q_holds_phi) {
+    // likewise the float pairs of Phi (a conversion of the FP64 copy could pick the other of two
+    // pairs with the same value, and the factor would differ in its last bits)
+    KLV(h, KM_PROF_EVAL, launch_eval_phi(h->d_pts, h->d_lnd, r, t, h->kp, -1, h->d_Phi, st, true, h->d_pts3,
+                                         h->d_lnd3, P<ff>(h->d_Q)));
+    h->q_holds_phi = true;
+  }
   h->lf_holds_k = false;
-  const int64_t fk[5] = {(int64_t)h->alloc_epoch, t.n, t.L, r, h->mixed ? 1 : 0};
+  const int64_t fk[6] = {(int64_t)h->alloc_epoch, t.n, t.L, r, h->mixed ? 1 : 0, h->q_holds_phi ? 1 : 0};
   auto* job = h->fwd_job;  // km_factorize_solve_dev: the forward half of a solve rides along
   if (job)
     rc = factorize_launches(h);
   else
     rc = run_graphed(h, &h->fgraph, h->fkey, fk, [&]() -> int { return factorize_launches(h); });
+  h->q_holds_phi = false;  // the factorisation works on d_Q in place
   if (rc != KM_OK) return rc;
   if ((rc = check_launch(h, "factorize")) != KM_OK) return rc;
   h->stats.factorize_ms = timer_stop(h);

@@ -86,11 +86,13 @@ __global__ void k_eval_leaves(const double* __restrict__ pts, const float* __res
 }
 
 // Phi[i, c] = k(x_i, p_c) for every point i and landmark c, stored per leaf column-major; the
-// float-pair kernel (use_ff, deriv < 0) on the split coordinates P3 and L3.
+// float-pair kernel (use_ff, deriv < 0) on the split coordinates P3 and L3, whose pairs also go
+// to Phif when given (the same values as the FP64 copy rounded back to pairs).
 // grid = (ceil(maxleaf*r / 256), nleaf), block = 256.
 __global__ void k_eval_phi(const double* __restrict__ pts, const double* __restrict__ lnd,
                            const float* __restrict__ P3, const float* __restrict__ L3, int r,
-                           DTree t, KParams kp, int deriv, bool use_ff, double* __restrict__ Phi) {
+                           DTree t, KParams kp, int deriv, bool use_ff, double* __restrict__ Phi,
+                           ff* __restrict__ Phif) {
   extern __shared__ double sl[];  // 2r
   for (int q = threadIdx.x; q < 2 * r; q += blockDim.x) sl[q] = lnd[q];
   __syncthreads();
@@ -104,9 +106,14 @@ __global__ void k_eval_phi(const double* __restrict__ pts, const double* __restr
     f3 x1, y1, x2, y2;
     load_p3(P3, s + i, x1, y1);
     load_p3(L3, c, x2, y2);
-    double v = to_double(kernel_value_ffp(kp, x1, y1, x2, y2));
-    if (eq3(x1, x2) && eq3(y1, y2)) v = __dadd_rn(v, kp.p2);
+    ff f = kernel_value_ffp(kp, x1, y1, x2, y2);
+    double v = to_double(f);
+    if (eq3(x1, x2) && eq3(y1, y2)) {
+      v = __dadd_rn(v, kp.p2);
+      f = ff(v);
+    }
     Phi[s * r + (int64_t)c * m + i] = v;
+    if (Phif) Phif[s * r + (int64_t)c * m + i] = f;
     return;
   }
   const double x = pts[2 * (s + i)], y = pts[2 * (s + i) + 1];
@@ -152,10 +159,12 @@ void launch_eval_leaves(const double* pts, const Tree& t, KParams kp, int deriv,
 }
 
 void launch_eval_phi(const double* pts, const double* lnd, int r, const Tree& t, KParams kp,
-                     int deriv, double* Phi, cudaStream_t st, bool use_ff, const float* P3, const float* L3) {
+                     int deriv, double* Phi, cudaStream_t st, bool use_ff, const float* P3, const float* L3,
+                     ff* Phif) {
   const int64_t per = t.max_leaf * r;
   dim3 grid((unsigned)((per + 255) / 256), (unsigned)t.nleaf);
-  k_eval_phi<<<grid, 256, 2 * r * sizeof(double), st>>>(pts, lnd, P3, L3, r, dtree(t), kp, deriv, use_ff, Phi);
+  k_eval_phi<<<grid, 256, 2 * r * sizeof(double), st>>>(pts, lnd, P3, L3, r, dtree(t), kp, deriv, use_ff, Phi,
+                                                         (use_ff && deriv < 0 && P3) ? Phif : nullptr);
 }
 
 void launch_split_points(const double* pts, int64_t n, float* P3, cudaStream_t st) {

@@ -315,7 +315,8 @@ void launch_leaf_dphiT(const T* Phi, const T* dPhi, int r, const Tree& t, const 
 // VP[(leaf k + c) r + q] = Phi_leaf[:, q]' x_leaf,c: one warp per (leaf, landmark q), lanes over
 // the leaf's rows (coalesced reads of Phi's column and of x), a fixed-order warp sum per
 // column.  grid (nleaf, ceil(r / 8)), block 256.
-__global__ void __launch_bounds__(256) k_leaf_phiT(const double* __restrict__ Phi, int r, DTree t,
+template <typename T>
+__global__ void __launch_bounds__(256) k_leaf_phiT(const T* __restrict__ Phi, int r, DTree t,
                                                    const double* __restrict__ X, int64_t ldx,
                                                    double* __restrict__ VP, int k) {
   const int lane = threadIdx.x & 31, q = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -323,24 +324,25 @@ __global__ void __launch_bounds__(256) k_leaf_phiT(const double* __restrict__ Ph
   const int64_t leaf = blockIdx.x;
   const int m = d_leaf_size(t, leaf);
   const int64_t s = d_leaf_start(t, leaf);
-  const double* pc = Phi + s * r + (int64_t)q * m;
+  const T* pc = Phi + s * r + (int64_t)q * m;
   for (int c = 0; c < k; ++c) {
     const double* xc = X + (int64_t)c * ldx + s;
-    double a0 = 0.0, a1 = 0.0;
+    acc_t<T> a0{}, a1{};
     int i = lane;
     for (; i + 32 < m; i += 64) {
-      a0 += pc[i] * xc[i];
-      a1 += pc[i + 32] * xc[i + 32];
+      a0 += pc[i] * from_double<T>(xc[i]);
+      a1 += pc[i + 32] * from_double<T>(xc[i + 32]);
     }
-    if (i < m) a0 += pc[i] * xc[i];
-    const double v = warp_sum(a0 + a1);
+    if (i < m) a0 += pc[i] * from_double<T>(xc[i]);
+    const double v = warp_sum(to_double(accv(a0) + accv(a1)));
     if (lane == 0) VP[(leaf * k + c) * r + q] = v;
   }
 }
 
 void launch_leaf_phiT(const double* Phi, int r, const Tree& t, const double* X, int64_t ldx, double* VP, int k,
                       cudaStream_t st) {
-  k_leaf_phiT<<<dim3((unsigned)t.nleaf, (unsigned)((r + 7) / 8)), 256, 0, st>>>(Phi, r, dtree(t), X, ldx, VP, k);
+  k_leaf_phiT<double><<<dim3((unsigned)t.nleaf, (unsigned)((r + 7) / 8)), 256, 0, st>>>(Phi, r, dtree(t), X, ldx, VP,
+                                                                                       k);
 }
 
 template <typename T>

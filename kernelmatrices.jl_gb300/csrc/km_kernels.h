@@ -81,7 +81,7 @@ void launch_eval_leaves(const double* pts, const Tree& t, KParams kp, int deriv,
                         cudaStream_t st, bool use_ff = false, ff* Kff = nullptr, const float* P3 = nullptr);
 void launch_eval_phi(const double* pts, const double* lnd, int r, const Tree& t, KParams kp,
                      int deriv, double* Phi, cudaStream_t st, bool use_ff = false, const float* P3 = nullptr,
-                     const float* L3 = nullptr);
+                     const float* L3 = nullptr, ff* Phif = nullptr);
 // P3: 8 floats a point, the exact float triples of x and y (km_kfun.cuh), for the float-pair
 // evaluations
 void launch_split_points(const double* pts, int64_t n, float* P3, cudaStream_t st);
