@@ -228,25 +228,46 @@ __global__ void __launch_bounds__(leaf_qr_threads<T>()) k_leaf_qr(T* __restrict_
     const T scal = sh_scal, tj = sh_tau;
     prev_scal = scal;
     if (tj != 0.0) {
-      // apply H_j = I - tau v v' to columns c > j (one warp per column), v = scal x
-      for (int c = j + 1 + w; c < r; c += (int)(blockDim.x >> 5)) {
+      // apply H_j = I - tau v v' to columns c > j, v = scal x.  Float pairs (32 warps): a warp
+      // takes the columns c and c + nwarps together, two independent dot products and updates in
+      // flight; FP64 (8 warps, bound by the FP64 pipe): one column a warp
+      constexpr bool kPair = std::is_same<T, ff>::value;
+      const int nwarps = (int)(blockDim.x >> 5);
+      for (int c = j + 1 + w; c < r; c += (kPair ? 2 : 1) * nwarps) {
+        const int c2 = c + nwarps;
+        const bool two = kPair && c2 < r;
         T* ac = A + (int64_t)c * m;
-        T acc = T(0.0);
-        for (int i = j + 1 + lane; i < m; i += 32) acc += aj[i] * ac[i];
+        T* ac2 = A + (int64_t)(two ? c2 : c) * m;
+        T acc = T(0.0), acc2 = T(0.0);
+        for (int i = j + 1 + lane; i < m; i += 32) {
+          const T x = aj[i];
+          acc += x * ac[i];
+          if (two) acc2 += x * ac2[i];
+        }
         acc = (warp_sum_t(acc) * scal + ac[j]) * tj;
-        if (lane == 0) ac[j] -= acc;
-        const T f = acc * scal;
+        if (two) acc2 = (warp_sum_t(acc2) * scal + ac2[j]) * tj;
+        if (lane == 0) {
+          ac[j] -= acc;
+          if (two) ac2[j] -= acc2;
+        }
+        const T f = acc * scal, f2 = acc2 * scal;
         if (c == j + 1) {  // the next column: its norm below row j + 1 on the way
           T nrm = T(0.0);
           for (int i = j + 1 + lane; i < m; i += 32) {
-            const T v = ac[i] - f * aj[i];
+            const T x = aj[i];
+            const T v = ac[i] - f * x;
             ac[i] = v;
             if (i > j + 1) nrm += v * v;
+            if (two) ac2[i] -= f2 * x;
           }
           nrm = warp_sum_t(nrm);
           if (lane == 0) sh_sig = nrm;
         } else {
-          for (int i = j + 1 + lane; i < m; i += 32) ac[i] -= f * aj[i];
+          for (int i = j + 1 + lane; i < m; i += 32) {
+            const T x = aj[i];
+            ac[i] -= f * x;
+            if (two) ac2[i] -= f2 * x;
+          }
         }
       }
     } else if (j + 1 < kmax && w == 0) {  // H_j = I: the next column's norm as it stands
