@@ -38,7 +38,7 @@ struct NodeMats {
 // up-sweep modes
 enum { UP_PROJ = 0, UP_FWD = 1, UP_MULT = 2, UP_SUM = 3 };
 // down-sweep modes
-enum { DN_FWD = 0, DN_BWD = 1, DN_MUL = 2, DN_MULT = 3, DN_NYS = 4 };
+enum { DN_FWD = 0, DN_BWD = 1, DN_MUL = 2, DN_MULT = 3 };
 
 // sum_l a[l*sa] b[l], l < n, with four independent partial sums (term l into sum l % 4, the
 // tail after the last full group of four into the first).  The node matrices come from L2.  In
@@ -232,25 +232,23 @@ __global__ void __launch_bounds__(512) k_down(NodeMats<T> nm, int level, int L, 
   const T* CtT = nm.CtT + node * rr;
   const T* L22iT = nm.L22iT + node * rr;
   if constexpr (STAGE) {
-    if (mode != DN_NYS) {
-      T* sE = tb + kcb * r2;  // 2 r^2: E
-      T* sA = sE + 2 * rr;    // r^2: Ct or CtT
-      T* sB = sA + rr;        // r^2: L22iT or L22
-      if (!top) {
-        stage_async(sE, E, 2 * r * r, tid, nth);
-        E = sE;
-      }
-      if (mode == DN_BWD) {
-        stage_async(sA, Ct, r * r, tid, nth);
-        stage_async(sB, L22iT, r * r, tid, nth);
-        Ct = sA;
-        L22iT = sB;
-      } else if (mode == DN_MUL) {
-        stage_async(sA, CtT, r * r, tid, nth);
-        stage_async(sB, L22, r * r, tid, nth);
-        CtT = sA;
-        L22 = sB;
-      }
+    T* sE = tb + kcb * r2;  // 2 r^2: E
+    T* sA = sE + 2 * rr;    // r^2: Ct or CtT
+    T* sB = sA + rr;        // r^2: L22iT or L22
+    if (!top) {
+      stage_async(sE, E, 2 * r * r, tid, nth);
+      E = sE;
+    }
+    if (mode == DN_BWD) {
+      stage_async(sA, Ct, r * r, tid, nth);
+      stage_async(sB, L22iT, r * r, tid, nth);
+      Ct = sA;
+      L22iT = sB;
+    } else if (mode == DN_MUL) {
+      stage_async(sA, CtT, r * r, tid, nth);
+      stage_async(sB, L22, r * r, tid, nth);
+      CtT = sA;
+      L22 = sB;
     }
   }
   for (int e = tid; e < kc * r; e += nth) {
@@ -260,17 +258,6 @@ __global__ void __launch_bounds__(512) k_down(NodeMats<T> nm, int level, int L, 
   if constexpr (STAGE) stage_wait();
   __syncthreads();
   auto child = [&](int side, int c, int i) -> int64_t { return ((cslot0 + 2 * kk + side) * k + c0 + c) * r + i; };
-  if (mode == DN_NYS) {
-    // coefficient sums: child c1 gets parent + phi(c2), child c2 gets parent + phi(c1)
-    for (int e = tid; e < kc * r; e += nth) {
-      const int c = e / r, i = e % r;
-      const T b = g[c * r + i];
-      const T p1 = VP[child(0, c, i)], p2 = VP[child(1, c, i)];
-      VG[child(0, c, i)] = b + p2;
-      VG[child(1, c, i)] = b + p1;
-    }
-    return;
-  }
   for (int e = tid; e < kc * r2; e += nth) {
     const int c = e / r2, i = e % r2;
     base[c * r2 + i] = top ? T(0.0) : dot4(E + i, r2, g + c * r, r);
@@ -478,7 +465,7 @@ void launch_down(const Tree& t, const NodeMatsH& h, int level, const T* VP, T* V
   dim3 grid((unsigned)t.nodes_at(level), (unsigned)((k + kcb - 1) / kcb));
   const size_t sm = (size_t)kcb * 5 * h.r * sizeof(T);
   const size_t sms = sm + (size_t)4 * h.r * h.r * sizeof(T);
-  if (mode != DN_NYS && (int64_t)grid.x * grid.y <= sweep_sm_count() && sms <= kStageSmemMax) {
+  if ((int64_t)grid.x * grid.y <= sweep_sm_count() && sms <= kStageSmemMax) {
     smem_limit((const void*)k_down<T, true>, sms);
     k_down<T, true><<<grid, nth, sms, st>>>(nm, level, t.L, child_slot0(t, level), t.nleaf + t.node_off[level],
                                             t.node_off[level], VP, VG, VD, k, mode, kcb);

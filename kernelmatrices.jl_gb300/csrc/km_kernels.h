@@ -144,7 +144,7 @@ enum { UP_PROJ_ = 0, UP_FWD_ = 1, UP_MULT_ = 2, UP_SUM_ = 3 };
 void launch_nys_sums(const double* VP, double* VG, int64_t nleaf, int W, int k, cudaStream_t st);
 template <typename T>
 void launch_slot_sub(T* VP, const T* VG, int64_t count, cudaStream_t st);
-enum { DN_FWD_ = 0, DN_BWD_ = 1, DN_MUL_ = 2, DN_MULT_ = 3, DN_NYS_ = 4 };
+enum { DN_FWD_ = 0, DN_BWD_ = 1, DN_MUL_ = 2, DN_MULT_ = 3 };
 template <typename T>
 void launch_up(const Tree& t, const NodeMatsH& h, int level, T* VP, T* VD, int k, int mode, cudaStream_t st);
 template <typename T>

@@ -304,3 +304,59 @@ def test_stoch_hessian_oracle():
         lhs = O.deriv2mul(DKs[0], DKs[1], D2B2, D2BL, Sjk, 2.0 * a - b)
         rhs = 2.0 * O.deriv2mul(DKs[0], DKs[1], D2B2, D2BL, Sjk, a) - O.deriv2mul(DKs[0], DKs[1], D2B2, D2BL, Sjk, b)
         assert np.allclose(lhs, rhs, rtol=1e-10, atol=1e-10 * np.abs(rhs).max())
+
+
+def test_nystrom_landmark_identity():
+    """Every off-diagonal block of a Nystrom HODLR is Phi_I S^-1 Phi_J' with the one landmark set
+    (nystrom_uvt, src/factorizations.jl:86-94), and every derivative block is
+    Phi_j,I S^-1 Phi_J' - Phi_I S^-1 S_j S^-1 Phi_J' + Phi_I S^-1 Phi_j,J' (DBlock_mul,
+    src/HODLR/src/utils.jl:76-82).  The blocks on a leaf's path to the root hold every other leaf
+    once, so with the leaf projections p_l = Phi_l' x_l, q_l = Phi_j,l' x_l and their sums P, Q:
+
+    * K x on leaf i = L_i x_i + Phi_i S^-1 (P - p_i), the sibling sums as total minus own leaf;
+    * dK x on leaf i = dL_i x_i + Phi_j,i S^-1 (P - p_i) - Phi_i S^-1 S_j S^-1 (P - p_i)
+      + Phi_i S^-1 (Q - q_i);
+    * x' dK x = sum_i x_i' dL_i x_i + f(P, Q) - sum_i f(p_i, q_i), f(p, q) = 2 u'q - u' S_j u with
+      u = S^-1 p (the quadratic form of the trace-form gradient).
+
+    Checked against the restated block-by-block products (baseoverloads.jl:152-179, 216-234)."""
+    n, rank = 768, 20
+    rng = np.random.default_rng(14)
+    pts = rng.uniform(size=(n, 2))
+    pts = pts[O.kd_order(pts, 16)]
+    for kid, p in ((O.KERNEL_MATERN32, [1.2, 0.1, 1e-2]), (O.KERNEL_RQ, [0.9, 0.15, 1e-2])):
+        K = O.KernelMatrix(pts, pts, np.asarray(p), kid)
+        HK = O.build_hodlr(K, 0.0, rank, O.FixedLevel(4), nystrom=True)
+        lnd = pts[O.nystrom_landmarks(n, rank)]
+        Sc = sla.cho_factor(O.kernel_block(kid, lnd, lnd, p), lower=False)
+        x = rng.standard_normal((n, 3))
+        leaves = [(a - 1, b) for a, b, _, _ in HK.leafindices]
+        phi = [O.kernel_block(kid, pts[a:b], lnd, p) for a, b in leaves]
+        P_l = [f.T @ x[a:b] for f, (a, b) in zip(phi, leaves)]
+        P = sum(P_l)
+        got = np.concatenate([HK.L[i] @ x[a:b] + phi[i] @ sla.cho_solve(Sc, P - P_l[i])
+                              for i, (a, b) in enumerate(leaves)])
+        ref = O.hodlr_mul(HK, x)
+        assert rel(got, ref) < 1e-12
+        for j in range(3):
+            DK = O.derivative_hodlr(K, j, HK)
+            Sj = O.dkernel_block(kid, j, lnd, lnd, p)
+            phj = [O.dkernel_block(kid, j, pts[a:b], lnd, p) for a, b in leaves]
+            Q_l = [f.T @ x[a:b] for f, (a, b) in zip(phj, leaves)]
+            Q = sum(Q_l)
+            got = []
+            for i, (a, b) in enumerate(leaves):
+                u = sla.cho_solve(Sc, P - P_l[i])
+                got.append(DK.L[i] @ x[a:b] + phj[i] @ u - phi[i] @ sla.cho_solve(Sc, Sj @ u)
+                           + phi[i] @ sla.cho_solve(Sc, Q - Q_l[i]))
+            ref = O.derivative_mul(DK, x)
+            assert rel(np.concatenate(got), ref) < 1e-11
+
+            def f(pp, qq):
+                u = sla.cho_solve(Sc, pp)
+                return np.einsum("rc,rc->c", u, 2.0 * qq - Sj @ u)
+
+            quad = sum(np.einsum("rc,rc->c", x[a:b], DK.L[i] @ x[a:b]) for i, (a, b) in enumerate(leaves))
+            quad = quad + f(P, Q) - sum(f(P_l[i], Q_l[i]) for i in range(len(leaves)))
+            qref = np.einsum("rc,rc->c", x, ref)
+            assert np.allclose(quad, qref, rtol=1e-10, atol=1e-10 * np.abs(qref).max())
