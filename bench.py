@@ -152,6 +152,29 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------------------------
+# replicas (N > 1): the path does not shard, so every rank runs the whole workload on its own
+# inputs; the timed region ends when the slowest rank ends
+# ----------------------------------------------------------------------------------------------
+
+def max_over_ranks(t_ms: float, dist=None, device: str = "cuda") -> float:
+    """Duration of a timed region as the slowest rank saw it: an all-reduce MAX over the ranks
+    of the process group (``dist`` = torch.distributed after init, None for one process).  The
+    caller brackets the region with barriers on every rank."""
+    if dist is None:
+        return float(t_ms)
+    import torch
+    tt = torch.tensor([float(t_ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_value(world: int, steps: int, ms: float) -> float:
+    """Whole-job steps per second: every one of ``world`` replicas ran ``steps`` steps within the
+    slowest rank's ``ms`` milliseconds."""
+    return world * steps / (ms / 1e3)
+
+
+# ----------------------------------------------------------------------------------------------
 # CPU legs (the oracle restatement of the reference)
 # ----------------------------------------------------------------------------------------------
 
@@ -360,11 +383,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             barrier()
             st1 = L.KmStats()
             lib.km_get_stats(h, C.byref(st1))
-            t = e0.elapsed_time(e1)
-            if dist is not None:
-                tt = torch.tensor([t], device="cuda")
-                dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-                t = float(tt.item())
+            t = max_over_ranks(e0.elapsed_time(e1), dist)
             return t, st1.kernel_launches - st0.kernel_launches
 
         # clocks are sampled from the start of the warm-up through the end of the timed region
@@ -401,12 +420,12 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     fp32_peak = kmhodlr.probe_fp32_tflops(dev)
 
     def form_summary(fm):
-        return {"value": world * args.steps / (fm["ms"] / 1e3), "ms_per_step": fm["ms"] / args.steps,
-                "e2e_value": world * args.steps / (fm["ms_e2e"] / 1e3), "kernel_ms_per_step": fm["prof"]}
+        return {"value": replica_value(world, args.steps, fm["ms"]), "ms_per_step": fm["ms"] / args.steps,
+                "e2e_value": replica_value(world, args.steps, fm["ms_e2e"]), "kernel_ms_per_step": fm["prof"]}
 
     step_ms = head["ms"] / args.steps
-    value = world * args.steps / (head["ms"] / 1e3)
-    e2e_value = world * args.steps / (head["ms_e2e"] / 1e3)
+    value = replica_value(world, args.steps, head["ms"])
+    e2e_value = replica_value(world, args.steps, head["ms_e2e"])
     flops = engine_flops(n, LEVEL)
     prof = head["prof"]
     dom = max((k for k in prof if k in flops), key=lambda k: prof[k]["ms"], default=None)
