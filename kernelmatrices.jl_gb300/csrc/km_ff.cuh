@@ -9,6 +9,9 @@
 // (nvcc does not reassociate float arithmetic).
 #pragma once
 #include <cuda_runtime.h>
+#ifndef __CUDA_ARCH__
+#include <cstring>
+#endif
 
 namespace km {
 
@@ -20,6 +23,40 @@ using ::fmin;
 using ::log;
 using ::sqrt;
 
+// Exact float -> double conversion on the integer pipes, from the IEEE-754 binary32 and binary64
+// layouts: the sign stays, a normal float's biased exponent E becomes E - 127 + 1023 and its 23
+// significand bits move up by 29; a subnormal float M 2^-149 is normalised at its leading bit p
+// (exponent p - 149, significand M shifted up by 52 - p without that bit); zeros keep their sign,
+// infinities and NaNs keep the all-ones exponent and the payload.  Every float is a double, so
+// the result equals the hardware conversion, which on GB300 runs on the FP64 pipe (2 lanes per
+// clock per SM) and had bounded the kernels that write FP64 copies of float-pair values.
+__host__ __device__ __forceinline__ unsigned long long f2d_bits(unsigned u) {
+  const unsigned long long s = (unsigned long long)(u >> 31) << 63;
+  const unsigned E = (u >> 23) & 0xffu, M = u & 0x7fffffu;
+  if (E == 0xffu) return s | (0x7ffull << 52) | ((unsigned long long)M << 29);
+  if (E != 0u) return s | ((unsigned long long)(E + 896u) << 52) | ((unsigned long long)M << 29);
+  if (M == 0u) return s;
+#ifdef __CUDA_ARCH__
+  const int p = 31 - __clz((int)M);
+#else
+  const int p = 31 - __builtin_clz(M);
+#endif
+  return s | ((unsigned long long)(p + 874) << 52) | (((unsigned long long)M << (52 - p)) & 0xfffffffffffffull);
+}
+
+__host__ __device__ __forceinline__ double f2d_exact(float f) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)f2d_bits(__float_as_uint(f)));
+#else
+  unsigned u;
+  std::memcpy(&u, &f, sizeof u);
+  const unsigned long long b = f2d_bits(u);
+  double d;
+  std::memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+
 struct __align__(8) ff {  // 8-byte aligned: one 64-bit load or store per value
   float hi, lo;
   __host__ __device__ constexpr ff() : hi(0.f), lo(0.f) {}
@@ -27,7 +64,9 @@ struct __align__(8) ff {  // 8-byte aligned: one 64-bit load or store per value
   // rounding a double to the nearest float pair (plain round-to-nearest casts, so that
   // constants such as ff(0.0) or ff(1.0) fold at compile time and cost no FP64 instruction)
   __host__ __device__ constexpr ff(double x) : hi(static_cast<float>(x)), lo(static_cast<float>(x - static_cast<double>(static_cast<float>(x)))) {}
-  __device__ explicit operator double() const { return (double)hi + (double)lo; }
+  // hi + lo rounded to a double: the exact conversions of both parts and one FP64 add, the same
+  // value as (double)hi + (double)lo
+  __device__ explicit operator double() const { return __dadd_rn(f2d_exact(hi), f2d_exact(lo)); }
 };
 
 __device__ __forceinline__ void ff_two_sum(float a, float b, float& s, float& e) {
