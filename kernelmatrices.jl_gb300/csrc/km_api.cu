@@ -201,6 +201,10 @@ struct km_handle {
   cudaStream_t aux = nullptr;
   cudaEvent_t xev[3] = {};
   double* d_bkeep = nullptr;  // right-hand sides kept by an in-place fused call
+  // pinned host copy of the pivot status words (d_info), filled by an asynchronous copy that the
+  // call's closing synchronisation covers: no separate round trip to read them
+  int* h_info = nullptr;
+  int64_t h_info_cap = 0;
   cudaEvent_t fev[kMaxLevels + 2] = {};
   struct FwdJob {
     double* X;
@@ -840,9 +844,26 @@ void side_end(km_handle* h) {
   cudaStreamWaitEvent(h->stream, h->sev[kMaxLevels + 2], 0);
 }
 
-int check_info(km_handle* h, int64_t count, const char* what) {
-  std::vector<int> info(count);
-  KM_CUDA(h, cudaMemcpy(info.data(), h->d_info, sizeof(int) * count, cudaMemcpyDeviceToHost));
+// Enqueues the copy of d_info[0 .. count) into the pinned h_info on the handle's stream; the
+// words are valid after the next synchronisation of that stream.
+int fetch_info_async(km_handle* h, int64_t count) {
+  if (count > h->h_info_cap) {
+    if (h->h_info) cudaFreeHost(h->h_info);
+    h->h_info = nullptr;
+    h->h_info_cap = 0;
+    if (cudaMallocHost(&h->h_info, sizeof(int) * (size_t)count) != cudaSuccess) {
+      cudaGetLastError();
+      h->h_info = nullptr;
+      return fail(h, KM_ERR_OOM, "pinned host buffer for the pivot status");
+    }
+    h->h_info_cap = count;
+  }
+  KM_CUDA(h, cudaMemcpyAsync(h->h_info, h->d_info, sizeof(int) * count, cudaMemcpyDeviceToHost, h->stream));
+  return KM_OK;
+}
+
+// The leaf pivot status in info[0 .. count): PosDefException for the first failing leaf.
+int check_info_words(km_handle* h, const int* info, int64_t count, const char* what) {
   for (int64_t i = 0; i < count; ++i) {
     if (info[i] < 0) return fail(h, KM_ERR_TIMEOUT, "a bounded wait of the tensor-core leaf update ran out");
     if (info[i] != 0) {
@@ -853,6 +874,12 @@ int check_info(km_handle* h, int64_t count, const char* what) {
     }
   }
   return KM_OK;
+}
+
+int check_info(km_handle* h, int64_t count, const char* what) {
+  std::vector<int> info(count);
+  KM_CUDA(h, cudaMemcpy(info.data(), h->d_info, sizeof(int) * count, cudaMemcpyDeviceToHost));
+  return check_info_words(h, info.data(), count, what);
 }
 
 // Y = dK_j X for the exact derivative of the Nystrom HODLR in parameter j (device pointers).
@@ -1230,6 +1257,7 @@ int km_destroy(km_handle* h) {
     if (e) cudaEventDestroy(e);
   if (h->aux) cudaStreamDestroy(h->aux);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  if (h->h_info) cudaFreeHost(h->h_info);
   delete h;
   return KM_OK;
 }
@@ -1624,11 +1652,11 @@ static int assemble_impl(km_handle* h, const double* pts, bool dev, int64_t n, i
   h->q_holds_phi = h->mixed;
   side_end(h);
   if ((rc = check_launch(h, "assemble")) != KM_OK) return rc;
+  if ((rc = fetch_info_async(h, t.nleaf + t.nnode + 1)) != KM_OK) return rc;  // last word: chol(S) status
   h->stats.assemble_ms = timer_stop(h);
   if ((rc = sync(h, "assemble")) != KM_OK) return rc;
-  int sinfo = 0;
-  KM_CUDA(h, cudaMemcpy(&sinfo, h->d_info + t.nleaf + t.nnode, sizeof(int), cudaMemcpyDeviceToHost));
-  if (sinfo != 0) return fail(h, KM_ERR_NOT_SPD, "PosDefException: landmark matrix K(P, P) is not positive definite");
+  if (h->h_info[t.nleaf + t.nnode] != 0)
+    return fail(h, KM_ERR_NOT_SPD, "PosDefException: landmark matrix K(P, P) is not positive definite");
   h->assembled = true;
   h->factorized = false;
   return KM_OK;
@@ -1820,13 +1848,12 @@ int km_factorize(km_handle* h) {
   h->q_holds_phi = false;  // the factorisation works on d_Q in place
   if (rc != KM_OK) return rc;
   if ((rc = check_launch(h, "factorize")) != KM_OK) return rc;
+  if ((rc = fetch_info_async(h, t.nleaf + t.nnode)) != KM_OK) return rc;  // leaf and node pivot status
   h->stats.factorize_ms = timer_stop(h);
   if ((rc = sync(h, "factorize")) != KM_OK) return rc;
-  rc = check_info(h, t.nleaf, "leaf");
+  rc = check_info_words(h, h->h_info, t.nleaf, "leaf");
   if (rc == KM_OK) {
-    std::vector<int> info(t.nnode);
-    if (t.nnode > 0)
-      KM_CUDA(h, cudaMemcpy(info.data(), h->d_info + t.nleaf, sizeof(int) * t.nnode, cudaMemcpyDeviceToHost));
+    const int* info = h->h_info + t.nleaf;
     for (int64_t i = 0; i < t.nnode && rc == KM_OK; ++i) {
       if (info[i] < 0) return fail(h, KM_ERR_TIMEOUT, "a bounded wait inside the node factorisation ran out");
       if (info[i]) rc = fail(h, KM_ERR_NOT_SPD, "PosDefException: a low-rank capacitance block is not positive definite");
@@ -2043,9 +2070,14 @@ int km_logdet(km_handle* h, double* out) {
                                                 h->d_scalar, h->stream));
   h->stats.kernel_launches += 1;  // the logdet runs a partial and a final reduction kernel
   if ((rc = check_launch(h, "logdet")) != KM_OK) return rc;
+  // the end mark goes before the read-back, so the one synchronisation below covers both
+  cudaEventRecord(h->ev1, h->stream);
   KM_CUDA(h, cudaMemcpyAsync(out, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  h->stats.logdet_ms = timer_stop(h);
-  return sync(h, "logdet");
+  if ((rc = sync(h, "logdet")) != KM_OK) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->stats.logdet_ms = ms;
+  return KM_OK;
 }
 
 int km_block_ranks(km_handle* h, int64_t* out) {
