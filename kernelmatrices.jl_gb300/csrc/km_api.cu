@@ -846,17 +846,20 @@ void side_end(km_handle* h) {
 
 // Enqueues the copy of d_info[0 .. count) into the pinned h_info on the handle's stream; the
 // words are valid after the next synchronisation of that stream.
+// The buffer starts at 8192 words (trees of up to 4096 leaves) and doubles: freeing pinned memory
+// synchronises the device, which would stall the other handles of a pool, so it regrows rarely.
 int fetch_info_async(km_handle* h, int64_t count) {
   if (count > h->h_info_cap) {
+    const int64_t cap = std::max<int64_t>(count, std::max<int64_t>(8192, 2 * h->h_info_cap));
     if (h->h_info) cudaFreeHost(h->h_info);
     h->h_info = nullptr;
     h->h_info_cap = 0;
-    if (cudaMallocHost(&h->h_info, sizeof(int) * (size_t)count) != cudaSuccess) {
+    if (cudaMallocHost(&h->h_info, sizeof(int) * (size_t)cap) != cudaSuccess) {
       cudaGetLastError();
       h->h_info = nullptr;
       return fail(h, KM_ERR_OOM, "pinned host buffer for the pivot status");
     }
-    h->h_info_cap = count;
+    h->h_info_cap = cap;
   }
   KM_CUDA(h, cudaMemcpyAsync(h->h_info, h->d_info, sizeof(int) * count, cudaMemcpyDeviceToHost, h->stream));
   return KM_OK;
