@@ -912,21 +912,37 @@ __global__ void __launch_bounds__(256) k_node_factor_f64(double* __restrict__ R,
   }
 }
 
-// Sc^{-T} (upper triangular) from the landmark Cholesky factor Sc (lower): one thread per
-// column of Sc^{-1} (forward substitution), one CTA.
+// Sc^{-T} (upper triangular) from the landmark Cholesky factor Sc (lower): X = Sc^{-1} by forward
+// substitution on all r columns at once, one CTA with Sc and the right-hand sides in shared
+// memory.  At step l the columns j <= l take x[l][j] = b[l][j] / Sc[l][l], then the rows i > l of
+// those columns take b[i][j] -= Sc[i][l] x[l][j].  Every x[i][j] sees the operations of the
+// row-by-row substitution of its column in the same order (b = e_j; l = j, ..., i - 1; one
+// division), two barriers a row instead of a serial chain of r^2 / 2 steps per thread.
 __global__ void k_tri_inv_t(const double* __restrict__ Sc, int r, double* __restrict__ SinvT) {
   extern __shared__ double s[];
   const int ld = r + 1;
-  for (int e = threadIdx.x; e < r * r; e += blockDim.x) s[(e % r) + (e / r) * ld] = Sc[e];
+  double* L = s;           // Sc, element (i, c) at i + c * ld
+  double* B = s + r * ld;  // right-hand sides, then X
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int e = tid; e < r * r; e += nth) {
+    const int i = e % r, c = e / r;
+    L[i + c * ld] = Sc[e];
+    B[i + c * ld] = (i == c) ? 1.0 : 0.0;
+  }
   __syncthreads();
-  for (int j = threadIdx.x; j < r; j += blockDim.x) {
-    // x = Sc^{-1} e_j, rows i >= j
-    for (int i = 0; i < r; ++i) SinvT[j + i * r] = 0.0;
-    for (int i = j; i < r; ++i) {
-      double v = (i == j) ? 1.0 : 0.0;
-      for (int l = j; l < i; ++l) v -= s[i + l * ld] * SinvT[j + l * r];
-      SinvT[j + i * r] = v / s[i + i * ld];
+  for (int l = 0; l < r; ++l) {
+    for (int j = tid; j <= l; j += nth) B[l + j * ld] = B[l + j * ld] / L[l + l * ld];
+    __syncthreads();
+    const int w = r - 1 - l;
+    for (int e = tid; e < w * (l + 1); e += nth) {
+      const int i = l + 1 + e % w, j = e / w;
+      B[i + j * ld] -= L[i + l * ld] * B[l + j * ld];
     }
+    __syncthreads();
+  }
+  for (int e = tid; e < r * r; e += nth) {
+    const int j = e % r, i = e / r;  // SinvT[j + i r] = X[i][j] for i >= j
+    SinvT[e] = (i >= j) ? B[i + j * ld] : 0.0;
   }
 }
 
@@ -1027,9 +1043,9 @@ void launch_leaf_qr(T* Pan, int r, const Tree& t, T* tau, T* Rout, cudaStream_t 
 }
 
 void launch_tri_inv_t(const double* Sc, int r, double* SinvT, cudaStream_t st) {
-  const size_t sm = (size_t)r * (r + 1) * sizeof(double);
+  const size_t sm = (size_t)2 * r * (r + 1) * sizeof(double);
   smem_limit((const void*)k_tri_inv_t, sm);
-  k_tri_inv_t<<<1, 128, sm, st>>>(Sc, r, SinvT);
+  k_tri_inv_t<<<1, 512, sm, st>>>(Sc, r, SinvT);
 }
 
 // SM count of the current device (cached per device)

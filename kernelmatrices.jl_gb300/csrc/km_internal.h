@@ -54,16 +54,20 @@ struct KParams {
   int kid;          // km_kernel_id
   double p0, p1, p2;
   float p0h, p0l, p1h, p1l;  // p0 and p1 rounded to float pairs once (the float-pair evaluations)
+  float ip1h, ip1l;          // 1 / p1 (FP64 division) rounded to a float pair
 };
 
-// KParams with the float-pair copies of p0 and p1: hi = fl32(p), lo = fl32(p - hi), the rounding
-// of the float-pair type's constructor
+// KParams with the float-pair copies of p0, p1 and 1 / p1: hi = fl32(p), lo = fl32(p - hi), the
+// rounding of the float-pair type's constructor
 inline KParams make_kparams(int kid, double p0, double p1, double p2) {
-  KParams k{kid, p0, p1, p2, 0.f, 0.f, 0.f, 0.f};
+  KParams k{kid, p0, p1, p2, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   k.p0h = static_cast<float>(p0);
   k.p0l = static_cast<float>(p0 - static_cast<double>(k.p0h));
   k.p1h = static_cast<float>(p1);
   k.p1l = static_cast<float>(p1 - static_cast<double>(k.p1h));
+  const double ip1 = 1.0 / p1;
+  k.ip1h = static_cast<float>(ip1);
+  k.ip1l = static_cast<float>(ip1 - static_cast<double>(k.ip1h));
   return k;
 }
 

@@ -12,7 +12,10 @@ namespace km {
 //
 // exp(-z), z >= 0: Cody-Waite reduction z = k ln2 + f with k = rint(z / ln2), |f| <= ln2/2, and
 // the Taylor series of exp(-f) to degree 13 (remainder < 2e-16 for |f| <= 0.347), scaled by
-// 2^-k.  The constants are the mathematical values ln 2 and 1/i!, rounded to float pairs.
+// 2^-k.  The constants are the mathematical values ln 2 and 1/i!, rounded to float pairs.  The
+// terms of degree 9 to 13 are below 2^-32 of the sum (0.347^9 / 9! = 2e-10), so their Horner
+// steps run in plain floats on the high part of -f (errors below 2^-55 of the sum); the terms of
+// degree 0 to 8 in float pairs.
 // ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ ff ff_exp_neg(ff z) {
   if (!(z.hi < 87.0f)) return ff(0.f, 0.f);
@@ -29,9 +32,12 @@ __device__ __forceinline__ ff ff_exp_neg(ff z) {
   constexpr double c[14] = {1.0, 1.0, 1.0 / 2, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720, 1.0 / 5040,
                             1.0 / 40320, 1.0 / 362880, 1.0 / 3628800, 1.0 / 39916800, 1.0 / 479001600,
                             1.0 / 6227020800.0};
-  ff p(c[13]);
+  float q = static_cast<float>(c[13]);
 #pragma unroll
-  for (int i = 12; i >= 0; --i) p = ff(c[i]) + p * u;
+  for (int i = 12; i >= 9; --i) q = __fmaf_rn(q, u.hi, static_cast<float>(c[i]));
+  ff p = ff(c[8]) + ff(q, 0.f) * u;
+#pragma unroll
+  for (int i = 7; i >= 0; --i) p = ff(c[i]) + p * u;
   const float sc = __int_as_float((127 - (int)k) << 23);  // 2^-k, k in [0, 126)
   return ff(p.hi * sc, p.lo * sc);
 }
@@ -48,6 +54,9 @@ __device__ __forceinline__ ff ff_exp_neg(ff z) {
 // p0 and p1 as float pairs (rounded on the host once, KParams)
 __device__ __forceinline__ ff kp_p0(const KParams& kp) { return ff(kp.p0h, kp.p0l); }
 __device__ __forceinline__ ff kp_p1(const KParams& kp) { return ff(kp.p1h, kp.p1l); }
+// 1 / p1 as a float pair: r / p1 is formed as r * (1 / p1), one float-pair product in place of a
+// float-pair division (the same accuracy, about 2^-47 relative)
+__device__ __forceinline__ ff kp_ip1(const KParams& kp) { return ff(kp.ip1h, kp.ip1l); }
 
 struct f3 {
   float h, m, l;
@@ -73,20 +82,20 @@ __device__ __forceinline__ ff ff_sub3(const f3& a, const f3& b) {
 }
 
 // kernel_value (km_internal.h) in float pairs, without the nugget; the same formulas and
-// special cases, on split coordinates.
+// special cases, on split coordinates, with r / p1 formed as r * (1 / p1).
 __device__ __forceinline__ ff kernel_value_ffp(const KParams& kp, const f3& x1, const f3& y1, const f3& x2,
                                                const f3& y2) {
   const ff dx = ff_sub3(x1, x2), dy = ff_sub3(y1, y2);
   const ff r = sqrt(ff(dx * dx) + dy * dy);
   ff out;
   if (kp.kid == KM_KERNEL_RATQUAD) {
-    const ff t = r / kp_p1(kp);
+    const ff t = r * kp_ip1(kp);
     const ff u = ff(1.0) + t * t;
     out = ff(kp_p0(kp) * kp_p0(kp)) / ff(u * u);
   } else {
     out = kp_p0(kp);
     if (r.hi > 0.f) {
-      const ff x = r / kp_p1(kp);
+      const ff x = r * kp_ip1(kp);
       if (x.hi > 1.0e-8f) {
         const ff z = ff(kSqrt3) * x;
         out = ff(kp_p0(kp) * (ff(1.0) + z)) * ff_exp_neg(z);
@@ -108,7 +117,7 @@ __device__ __forceinline__ double kernel_value_ff(const KParams& kp, double x1, 
 
 // dkernel_value (km_internal.h) for the three parameters at once in float pairs, on split
 // coordinates: one distance and, for the Matern kernel, one exponential shared by the scale and
-// range derivatives.
+// range derivatives; r / p1 formed as r * (1 / p1).
 __device__ __forceinline__ void dkernel3_ffp(const KParams& kp, const f3& x1, const f3& y1, const f3& x2,
                                              const f3& y2, ff (&out)[3]) {
   out[2] = (eq3(x1, x2) && eq3(y1, y2)) ? ff(1.0) : ff(0.0);
@@ -116,7 +125,7 @@ __device__ __forceinline__ void dkernel3_ffp(const KParams& kp, const f3& x1, co
   const ff r2 = ff(dx * dx) + dy * dy;
   const ff r = sqrt(r2);
   if (kp.kid == KM_KERNEL_RATQUAD) {
-    const ff t = r / kp_p1(kp);
+    const ff t = r * kp_ip1(kp);
     const ff u = ff(1.0) + t * t;
     out[0] = ff(ff(2.0) * kp_p0(kp)) / ff(u * u);
     const ff num = ff(ff(4.0) * ff(kp_p0(kp) * kp_p0(kp))) * r2;
@@ -127,7 +136,7 @@ __device__ __forceinline__ void dkernel3_ffp(const KParams& kp, const f3& x1, co
   out[0] = ff(1.0);
   out[1] = ff(0.0);
   if (!(r.hi > 0.f)) return;
-  const ff x = r / kp_p1(kp);
+  const ff x = r * kp_ip1(kp);
   if (!(x.hi > 1.0e-8f)) return;
   // -p0 * cor'(x) * r / p1^2 with cor'(x) = -3 x exp(-sqrt3 x)
   const ff z = ff(kSqrt3) * x;
